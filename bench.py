@@ -1,0 +1,336 @@
+"""Benchmark: DOF·stage updates/s of the GB300 DGSEM path (FP64).
+
+Default workload: the batched ensemble of 256 dry warm-bubble members, each a
+64x32-element StructuredMesh of 20 km x 10 km at polydeg 3 (32,768 DOF per
+member, 8,388,608 DOF in total), seeded bubble amplitude U[1, 3] K and centre
+jitter +-1 km, energy + gravity equations with (flux_ranocha,
+flux_nonconservative_waruszewski_etal) / (FluxLMARS(340), flux_zero), slip
+walls in z, CarpenterKennedy2N54 at CFL 1 with per-member dt.  One bench
+"step" is one RK step (5 stages) of every member; DOF·stage/s = DOF x 5 x
+steps / time.  Inputs are larger than L2 (u alone is 336 MB), so no flush is
+needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Multi-GPU: replicas only (every rank runs its own ensemble; no collective on
+the data path); value = all ranks' DOF·stages / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import __graft_entry__ as entry  # noqa: E402
+
+METRIC = "DOF·stage/s on 1 GB300 (FP64) vs CPU; rainy Newton iters/node learned vs plain"
+UNIT = "DOF·stage/s"
+LX, LZ = 20000.0, 10000.0
+NX, NZ, POLYDEG = 64, 32, 3
+C_LMARS = 340.0
+
+
+def member_bubbles(nmembers, seed0=0):
+    """Seeded per-member bubble parameters (Philox, one stream per member)."""
+    out = []
+    for m in range(nmembers):
+        rng = np.random.Generator(np.random.Philox(seed0 + m))
+        amp = rng.uniform(1.0, 3.0)
+        dx, dz = rng.uniform(-1000.0, 1000.0, size=2)
+        out.append((10000.0 + dx, 2000.0 + dz, amp))
+    return out
+
+
+def make_ensemble(tg, nmembers):
+    eq = tg.CompressibleEulerEnergyEquationsWithGravity2D(c_p=1004, c_v=717, gravity=9.81)
+    solver = tg.DGSEM(POLYDEG, (tg.FluxLMARS(C_LMARS), tg.flux_zero),
+                      tg.VolumeIntegralFluxDifferencing(
+                          (tg.flux_ranocha, tg.flux_nonconservative_waruszewski_etal)))
+    mesh = tg.StructuredMesh((NX, NZ), (0.0, 0.0), (LX, LZ), periodicity=(True, False))
+    ics = [tg.WarmBubble(xc=xc, zc=zc, dtheta=a) for xc, zc, a in member_bubbles(nmembers)]
+    bcs = {"y_neg": tg.boundary_condition_slip_wall, "y_pos": tg.boundary_condition_slip_wall}
+    if nmembers == 1:
+        semi = tg.SemidiscretizationHyperbolic(mesh, eq, ics[0], solver, boundary_conditions=bcs)
+    else:
+        semi = tg.SemidiscretizationEnsemble([mesh] * nmembers, eq, ics, solver,
+                                             boundary_conditions=bcs)
+    return eq, semi
+
+
+# ---- algorithmic work per DOF·stage (counted from the formulas; see DESIGN) --
+def flops_per_element_launch(n, nelem):
+    """FP64 flops of one element-kernel launch: per symmetric pair 101 (flux_ranocha
+    with shared means, half the Waruszewski term, both D_split products), per
+    node 8 (cons2prim), per (node, active variable) 2(n-1)+1 slot sums, Jacobian
+    1 and stage update 5, plus 2 per face-node surface term."""
+    P = n * n * (n - 1)
+    per_elem = P * 101 + n * n * 8 + n * n * 4 * (2 * (n - 1) + 1 + 1 + 5) + 4 * n * 4 * 2
+    return per_elem * nelem
+
+
+def bytes_per_element_launch(n, nelem):
+    """Compulsory DRAM bytes of one element-kernel (stage mode) launch: read u
+    (5 vars), Ja (4), invJ (1), sfv (4 faces x n x 4 vars per element), k (4);
+    write u (4 active vars) and k (4)."""
+    nodes = n * n * nelem
+    return 8 * (nodes * (5 + 4 + 1 + 4 + 4 + 4) + nelem * 4 * n * 4)
+
+
+# ---- clocks during the timed region ----------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.lines = []
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---- CPU legs (the oracle, test infrastructure) -----------------------------
+def cpu_oracle_rate(nmembers_sample, steps, warmup=0):
+    """Times the C++ OpenMP oracle (restatement of the reference's rhs! + CK2N54
+    stage) on `nmembers_sample` members for `steps` RK steps each; returns
+    DOF·stage/s and the thread count."""
+    orc = entry.load_oracle()
+    orc.build()
+    cases = []
+    for xc, zc, amp in member_bubbles(nmembers_sample):
+        c = orc.Euler2D(POLYDEG, NX, NZ, 0.0, LX, 0.0, LZ, True, False, 1004.0, 717.0, 9.81,
+                        C_LMARS)
+        u = c.initial_condition(1, (xc, zc, 2000.0, amp, 0.0))
+        cases.append((c, u, np.zeros_like(u)))
+    for c, u, k in cases[:1]:
+        for _ in range(warmup):
+            c.ck_steps(u, k, 0.0, 1.0, 1)
+    t0 = time.perf_counter()
+    for c, u, k in cases:
+        c.ck_steps(u, k, 0.0, 1.0, steps)
+    el = time.perf_counter() - t0
+    dofs = nmembers_sample * NX * NZ * (POLYDEG + 1) ** 2
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return dofs * 5 * steps / el, threads, el
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, _ = dist_init()
+    if rank != 0:
+        return
+    sample = args.ref_members
+    rate, threads, el = cpu_oracle_rate(sample, max(args.steps, 1), warmup=args.warmup > 0)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el / max(args.steps, 1) * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"ensemble of {args.members} dry warm-bubble members "
+                               f"(64x32, polydeg 3); sample of {sample} members per step",
+                   "members": args.members, "dofs": args.members * NX * NZ * 16},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{sample} members x {args.steps} CK2N54 steps"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "Julia/Trixi are not installed on this box; the reference CPU rhs! is the "
+                "C++ OpenMP restatement in oracle/ (pinned to the reference's golden l2/linf)",
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_init()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    tg = entry.load_package()
+    eq, semi = make_ensemble(tg, args.members)
+    u0 = semi.compute_coefficients()
+    semi.set_state(u0)
+    nmem = semi.nmembers
+    stream = torch.cuda.ExternalStream(semi.stream())
+    dofs = semi.ndofs
+    # warm-up (also triggers the elements-per-CTA autotuner and graph capture)
+    t_m = np.zeros(nmem)
+    t_m = semi.rk_steps(max(args.warmup, 1), cfl=1.0, t=t_m)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    t_m = semi.rk_steps(args.steps, cfl=1.0, t=t_m)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    clock_info = clocks.stop()
+    if world > 1:
+        tt = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+        ms = float(tt.item())
+    value = world * dofs * 5 * args.steps / (ms * 1e-3)
+    status = semi.status()
+
+    # kernel timing for the roofline (same stream, CUDA events, stage mode)
+    ms_if, ms_el = semi.time_kernels(reps=10)
+    n = semi.n
+    fl = flops_per_element_launch(n, semi.nelements)
+    by = bytes_per_element_launch(n, semi.nelements)
+    peak_fp64 = tg.fp64_peak()
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        hbm_peak, hbm_src = float(peaks["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        hbm_peak, hbm_src = 6800.0, "fallback"
+    achieved_tf = fl / (ms_el * 1e-3) / 1e12
+    achieved_gbs = by / (ms_el * 1e-3) / 1e9
+
+    # end to end through the C ABI with pinned host buffers: per step, H2D of
+    # the state, one RK step (5 stages), D2H of the state
+    u_pin = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True).numpy()
+    u_pin[...] = u0
+    semi.set_state(u_pin)
+    t_e = np.zeros(nmem)
+    for _ in range(2):
+        semi.set_state(u_pin)
+        t_e = semi.rk_steps(1, cfl=1.0, t=t_e)
+        semi.get_state(u_pin)
+    e2e_steps = max(3, args.steps // 2)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        semi.set_state(u_pin)
+        t_e = semi.rk_steps(1, cfl=1.0, t=t_e)
+        semi.get_state(u_pin)
+    el = time.perf_counter() - t0
+    if world > 1:
+        tt = torch.tensor([el], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        el = float(tt.item())
+    e2e = world * dofs * 5 * e2e_steps / el
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rate, threads, cel = cpu_oracle_rate(args.cpu_members, 1)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_members} members x 1 CK2N54 step (5 stages) of the same "
+                         f"ensemble, oracle/ C++ OpenMP ({cel:.1f} s)"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded warm-bubble ensemble)",
+            "config": {"workload": f"ensemble of {args.members} dry warm-bubble members, "
+                                   "64x32 StructuredMesh, polydeg 3, CK2N54 CFL 1",
+                       "members": args.members, "dofs": dofs, "elements": semi.nelements,
+                       "elements_per_cta": semi.elements_per_block(),
+                       "l2": "inputs larger than L2 (u 336 MB + k 268 MB per step)",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "fp64", "achieved": achieved_tf, "peak": peak_fp64 / 1e12,
+                         "unit": "TFLOP/s", "frac": achieved_tf / (peak_fp64 / 1e12),
+                         "traffic": None,
+                         "kernel": "k_element (volume + surface + Jacobian + RK stage)",
+                         "peak_source": "FP64 FMA probe in this run (tag_fp64_peak)",
+                         "hbm_achieved_gbs": achieved_gbs, "hbm_peak_gbs": hbm_peak,
+                         "hbm_frac": achieved_gbs / hbm_peak, "hbm_peak_source": hbm_src,
+                         "ms_element": ms_el, "ms_interface": ms_if,
+                         "flops_per_launch": fl, "bytes_per_launch": by},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(u0.nbytes),
+                    "d2h_bytes_per_step": int(u0.nbytes)},
+            "gpu_launches": args.steps * 11,
+            "clocks": clock_info,
+            "status": status,
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line))
+    semi.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--members", type=int, default=256)
+    ap.add_argument("--cpu-members", type=int, default=8)
+    ap.add_argument("--ref-members", type=int, default=16)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,152 @@
+/*
+ * trixiatmo_gpu.h — C ABI of libtrixiatmo_gpu.so, the GB300 (sm_103a) DGSEM
+ * right-hand side and Runge-Kutta stage engine that stands in for Trixi.jl's
+ * `rhs!` as TrixiAtmo.jl drives it.
+ *
+ * All entry points are `extern "C"`, take plain pointers and sizes and return
+ * an int status (TAG_OK = 0).  Arrays cross the boundary in Julia's
+ * column-major layout (first index fastest), exactly as Trixi stores them:
+ *   u, du                  u[v, i, j, element]            (Trixi `wrap_array(u_ode, semi)`)
+ *   contravariant_vectors  [component, direction, i, j, element]
+ *   inverse_jacobian       [i, j, element]
+ *   node_coordinates       [component, i, j, element]
+ *   derivative_split       [i, ii]  (dg.basis.derivative_split)
+ *   weights                [i]      (dg.basis.weights)
+ * Element, face and interface indices are 0-based.  Faces: 0 = xi-, 1 = xi+,
+ * 2 = eta-, 3 = eta+ (Trixi directions 1..4).
+ *
+ * Ownership: the caller owns every host array and keeps it alive for the
+ * duration of the call (Julia: GC.@preserve).  The library copies what it
+ * needs to device memory in tag_create and owns all device buffers.
+ * Threading: one host thread per handle; work is ordered on the handle's own
+ * CUDA stream; calls on one handle are not re-entrant.
+ */
+#ifndef TRIXIATMO_GPU_H
+#define TRIXIATMO_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define TAG_OK 0
+#define TAG_E_INVALID 1        /* bad argument / unsupported configuration     */
+#define TAG_E_CUDA 2           /* a CUDA runtime call failed                   */
+#define TAG_E_NO_DEVICE 3      /* no CUDA device visible                       */
+#define TAG_E_STATE 4          /* device status word has an error bit set      */
+
+/* ---- device status word bits (tag_status) ------------------------------ */
+#define TAG_S_NAN 0x1u         /* non-finite value met in a kernel             */
+#define TAG_S_NEG_DENSITY 0x2u /* rho <= 0 met                                 */
+#define TAG_S_NEG_PRESSURE 0x4u/* p <= 0 met                                   */
+#define TAG_S_NEWTON_MAXIT 0x8u/* Newton limiter hit max_iterations (warning)  */
+
+/* ---- equation systems, fluxes, boundary kinds --------------------------- */
+#define TAG_EQ_EULER_ENERGY_2D 1 /* CompressibleEulerEnergyEquationsWithGravity2D */
+
+#define TAG_VF_RANOCHA_WARUSZEWSKI 1 /* (flux_ranocha, flux_nonconservative_waruszewski_etal) */
+#define TAG_SF_LMARS 1               /* (FluxLMARS(c), flux_zero)                       */
+
+#define TAG_BC_SLIP_WALL_STRUCTURED 1 /* boundary_condition_slip_wall reached from a StructuredMesh */
+#define TAG_BC_SLIP_WALL_NORMAL 2     /* boundary_condition_slip_wall reached from a P4estMesh      */
+
+typedef struct tag_handle_s* tag_handle;
+
+/* Semidiscretization description: what Trixi's `SemidiscretizationHyperbolic`
+ * holds in (equations, solver, cache) for this path. */
+typedef struct {
+  int32_t equations;      /* TAG_EQ_*                                         */
+  int32_t volume_flux;    /* TAG_VF_*                                         */
+  int32_t surface_flux;   /* TAG_SF_*                                         */
+  int32_t polydeg;        /* N; nodes per direction n = N + 1                 */
+  int32_t nelements;
+  int32_t ninterfaces;
+  int32_t nboundaries;    /* boundary faces                                   */
+  int32_t nmembers;       /* ensemble members (0 or 1: a single mesh)         */
+  const double* derivative_split;      /* [n, n]                               */
+  const double* weights;               /* [n]                                  */
+  const double* contravariant_vectors; /* [2, 2, n, n, E]                      */
+  const double* inverse_jacobian;      /* [n, n, E]                            */
+  const double* node_coordinates;      /* [2, n, n, E]                         */
+  const int32_t* interface_elements;   /* [2, I]: primary, secondary element   */
+  const int32_t* interface_faces;      /* [2, I]: primary, secondary face      */
+  const int32_t* interface_flip;       /* [I]: 1 if the secondary face runs backward */
+  const int32_t* boundary_elements;    /* [B]                                  */
+  const int32_t* boundary_faces;       /* [B]                                  */
+  const int32_t* boundary_kinds;       /* [B]: TAG_BC_*                        */
+  const int32_t* element_member;       /* [E]: ensemble member of each element
+                                          (null when nmembers <= 1).  Members are
+                                          independent meshes (no interface joins
+                                          two members); each has its own t, dt and
+                                          CFL reduction.                         */
+  double params[8];  /* EULER_ENERGY_2D: c_p, c_v, gravity, LMARS speed of sound */
+} tag_config;
+
+/* Creates a handle on the current CUDA device.  Replaces the cache build of
+ * Trixi.SemidiscretizationHyperbolic (reference: src/semidiscretization/
+ * semidiscretization_hyperbolic_2d_manifold_in_3d.jl:78-111, create_cache in
+ * src/solvers/solvers.jl:7-33): geometry and connectivity are uploaded once. */
+int tag_create(const tag_config* cfg, tag_handle* out);
+int tag_destroy(tag_handle h);
+
+/* Number of solution entries nv * n^2 * E (length of Trixi's u_ode). */
+int64_t tag_ndofs_total(tag_handle h);
+
+/* du = rhs(u, t): Trixi.rhs_hyperbolic!(du_ode, u_ode, semi, t) as called by
+ * test/test_2d_rainy_euler.jl:38 and overridden in
+ * src/solvers/dgsem_p4est/dg_2d_manifold_in_3d_covariant.jl:8-71.
+ * u and du are host pointers when on_device == 0, device pointers otherwise. */
+int tag_rhs(tag_handle h, const double* u, double* du, double t, int32_t on_device);
+
+/* Load / read back the handle's resident solution (the ODE state u_ode). */
+int tag_set_state(tag_handle h, const double* u_host);
+int tag_get_state(tag_handle h, double* u_host);
+/* Device pointer of the resident state (for callers that keep data on the GPU). */
+int tag_state_device_ptr(tag_handle h, double** u_dev);
+
+/* Trixi.max_dt(u, t, mesh, constant_speed = False(), equations, dg, cache) on
+ * the resident state (the minimum over members for an ensemble); reference
+ * pattern src/callbacks_step/stepsize_dg2d.jl:5-44. */
+int tag_max_dt(tag_handle h, double* out);
+
+/* Advances the resident state by `nsteps` CarpenterKennedy2N54 steps.  With
+ * fixed_dt > 0 every step uses it, otherwise dt = cfl * max_dt(u) before each
+ * step (StepsizeCallback), per ensemble member.  t points to nmembers doubles
+ * (one when there is a single mesh): the members' times, read and updated.
+ * Each step is one CUDA-graph replay of a dt kernel and
+ * 5 x (interface kernel + element kernel). */
+int tag_rk_steps(tag_handle h, int32_t nsteps, double cfl, double fixed_dt, double* t);
+
+/* Per-member max_dt of the resident state (out: nmembers doubles). */
+int tag_max_dt_members(tag_handle h, double* out);
+
+/* Times `reps` launches of each stage kernel on the handle's stream with CUDA
+ * events (after a warm-up) and returns the mean milliseconds per launch of the
+ * interface kernel and of the element kernel (stage mode). The resident state
+ * is advanced by the timed stages. */
+int tag_time_kernels(tag_handle h, int32_t reps, double* ms_interface, double* ms_element);
+
+/* Reads (and clears when clear != 0) the device status word (TAG_S_* bits). */
+int tag_status(tag_handle h, uint32_t* flags, int32_t clear);
+
+/* The handle's CUDA stream (cudaStream_t as void*), for callers that order
+ * their own work against the library's. */
+void* tag_stream(tag_handle h);
+
+/* Tuning knob: elements per CTA of the element kernel (0 = autotune). */
+int tag_set_elements_per_block(tag_handle h, int32_t epb);
+int tag_get_elements_per_block(tag_handle h, int32_t* epb);
+
+/* FP64 FMA throughput probe (FLOP/s, FMA = 2) on the current device; the
+ * denominator of the FP64 roofline. */
+int tag_fp64_peak(double* flops_per_s);
+
+/* Last error message of this thread (static storage). */
+const char* tag_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TRIXIATMO_GPU_H */

@@ -1,0 +1,130 @@
+"""ORACLE — test infrastructure only.
+
+ctypes wrapper around ``oracle/_build/liboracle.so``, the C++ CPU restatement
+of the reference's `rhs!` used as the checker for the CUDA path (and as the
+timed CPU baseline).  Only ``tests/``, ``__graft_entry__.smoke()`` and
+``bench.py``'s CPU legs may import this module; the product library never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (g++ + OpenMP)."""
+    cmd = ["make", "-C", _HERE]
+    if force:
+        cmd.insert(1, "-B")
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        L.orc_euler2d_create.restype = ctypes.c_void_p
+        L.orc_euler2d_create.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] * 4 + [
+            ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 4
+        L.orc_euler2d_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_euler2d_ndofs.restype = ctypes.c_int64
+        L.orc_euler2d_ndofs.argtypes = [ctypes.c_void_p]
+        L.orc_euler2d_basis.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp]
+        L.orc_euler2d_geometry.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+        L.orc_euler2d_initial_condition.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
+        L.orc_euler2d_rhs.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double]
+        L.orc_euler2d_max_dt.restype = ctypes.c_double
+        L.orc_euler2d_max_dt.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_euler2d_ck_steps.restype = ctypes.c_double
+        L.orc_euler2d_ck_steps.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_int, ctypes.c_double]
+        L.orc_euler2d_ssprk43_run.restype = ctypes.c_int
+        L.orc_euler2d_ssprk43_run.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double,
+                                              ctypes.c_double, ctypes.c_double]
+        L.orc_euler2d_errors_gravity_waves.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+class Euler2D:
+    """Dry Euler (energy + gravity) on a StructuredMesh rectangle, CPU oracle."""
+
+    nv = 5
+
+    def __init__(self, polydeg, nx, ny, x0, x1, y0, y1, periodic_x=True, periodic_y=False,
+                 c_p=1004.0, c_v=717.0, g=9.81, c_lmars=340.0):
+        self.n = polydeg + 1
+        self.nelem = nx * ny
+        self.h = lib().orc_euler2d_create(polydeg, nx, ny, x0, x1, y0, y1, int(periodic_x),
+                                          int(periodic_y), c_p, c_v, g, c_lmars)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_euler2d_destroy(self.h)
+            self.h = None
+
+    @property
+    def ndofs(self):
+        return self.nelem * self.n * self.n
+
+    def shape(self):
+        return (self.nelem, self.n, self.n, self.nv)
+
+    def basis(self):
+        n = self.n
+        x, w = np.zeros(n), np.zeros(n)
+        D, Ds = np.zeros((n, n)), np.zeros((n, n))
+        lib().orc_euler2d_basis(self.h, _p(x), _p(w), _p(D), _p(Ds))
+        return x, w, D, Ds
+
+    def geometry(self):
+        n, E = self.n, self.nelem
+        Ja = np.zeros((E, n, n, 2, 2))
+        invJ = np.zeros((E, n, n))
+        xy = np.zeros((E, n, n, 2))
+        lib().orc_euler2d_geometry(self.h, _p(Ja), _p(invJ), _p(xy))
+        return Ja, invJ, xy
+
+    def initial_condition(self, which=0, params=(10000.0, 2000.0, 2000.0, 2.0, 0.0)):
+        u = np.zeros(self.shape())
+        prm = np.asarray(params, dtype=np.float64)
+        lib().orc_euler2d_initial_condition(self.h, which, _p(prm), _p(u))
+        return u
+
+    def rhs(self, u, t=0.0):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        du = np.zeros_like(u)
+        lib().orc_euler2d_rhs(self.h, _p(u), _p(du), t)
+        return du
+
+    def max_dt(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        return lib().orc_euler2d_max_dt(self.h, _p(u))
+
+    def ck_steps(self, u, k, t, cfl, nsteps, fixed_dt=0.0):
+        return lib().orc_euler2d_ck_steps(self.h, _p(u), _p(k), t, cfl, nsteps, fixed_dt)
+
+    def ssprk43_run(self, u, t0, t_end, cfl):
+        return lib().orc_euler2d_ssprk43_run(self.h, _p(u), t0, t_end, cfl)
+
+    def errors_gravity_waves(self, u):
+        l2, linf = np.zeros(5), np.zeros(5)
+        lib().orc_euler2d_errors_gravity_waves(self.h, _p(u), _p(l2), _p(linf))
+        return l2, linf

@@ -1,0 +1,29 @@
+"""trixiatmo_gb300 — GB300-native (sm_103a, FP64) DGSEM `rhs!` for TrixiAtmo.jl.
+
+The hot path is libtrixiatmo_gpu.so (CUDA kernels behind the C ABI in
+include/trixiatmo_gpu.h).  This package is the host-side mirror of the
+reference's Julia API for that path, used by the tests and the benchmark.
+The directory name is not a Python identifier; load it with
+``load_package()`` from ``__graft_entry__`` (or importlib) under the name
+``trixiatmo_gb300``.
+"""
+from . import _lib
+from .basis import LobattoLegendreBasis
+from .equations import (CompressibleEulerEnergyEquationsWithGravity2D, FluxLMARS,
+                        VolumeIntegralFluxDifferencing, boundary_condition_periodic,
+                        boundary_condition_slip_wall, flux_nonconservative_waruszewski_etal,
+                        flux_ranocha, flux_zero, speed_of_sound_isothermal)
+from .initial_conditions import WarmBubble, initial_condition_gravity_waves, seeded_perturbation
+from .meshes import StructuredMesh
+from .semidiscretization import (DGSEM, SemidiscretizationEnsemble, SemidiscretizationHyperbolic,
+                                 fp64_peak)
+
+__all__ = [
+    "LobattoLegendreBasis", "CompressibleEulerEnergyEquationsWithGravity2D", "FluxLMARS",
+    "VolumeIntegralFluxDifferencing", "boundary_condition_periodic",
+    "boundary_condition_slip_wall", "flux_nonconservative_waruszewski_etal", "flux_ranocha",
+    "flux_zero", "speed_of_sound_isothermal", "WarmBubble", "initial_condition_gravity_waves",
+    "seeded_perturbation", "StructuredMesh", "DGSEM", "SemidiscretizationHyperbolic",
+    "SemidiscretizationEnsemble",
+    "fp64_peak",
+]

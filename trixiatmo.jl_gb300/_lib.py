@@ -1,0 +1,119 @@
+"""ctypes binding of the C ABI in include/trixiatmo_gpu.h.
+
+This is the same binding a Julia `ccall` shim makes; it loads the in-tree
+``_build/libtrixiatmo_gpu.so`` and raises if the library is missing — there is
+no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+TAG_OK = 0
+TAG_E_INVALID = 1
+TAG_E_CUDA = 2
+TAG_E_NO_DEVICE = 3
+TAG_E_STATE = 4
+
+TAG_S_NAN = 0x1
+TAG_S_NEG_DENSITY = 0x2
+TAG_S_NEG_PRESSURE = 0x4
+TAG_S_NEWTON_MAXIT = 0x8
+
+TAG_EQ_EULER_ENERGY_2D = 1
+TAG_VF_RANOCHA_WARUSZEWSKI = 1
+TAG_SF_LMARS = 1
+TAG_BC_SLIP_WALL_STRUCTURED = 1
+TAG_BC_SLIP_WALL_NORMAL = 2
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int32)
+
+
+class TagConfig(ctypes.Structure):
+    _fields_ = [
+        ("equations", ctypes.c_int32),
+        ("volume_flux", ctypes.c_int32),
+        ("surface_flux", ctypes.c_int32),
+        ("polydeg", ctypes.c_int32),
+        ("nelements", ctypes.c_int32),
+        ("ninterfaces", ctypes.c_int32),
+        ("nboundaries", ctypes.c_int32),
+        ("nmembers", ctypes.c_int32),
+        ("derivative_split", _dp),
+        ("weights", _dp),
+        ("contravariant_vectors", _dp),
+        ("inverse_jacobian", _dp),
+        ("node_coordinates", _dp),
+        ("interface_elements", _ip),
+        ("interface_faces", _ip),
+        ("interface_flip", _ip),
+        ("boundary_elements", _ip),
+        ("boundary_faces", _ip),
+        ("boundary_kinds", _ip),
+        ("element_member", _ip),
+        ("params", ctypes.c_double * 8),
+    ]
+
+
+# exported symbol -> (restype, argtypes)
+SIGNATURES = {
+    "tag_create": (ctypes.c_int, [ctypes.POINTER(TagConfig), ctypes.POINTER(ctypes.c_void_p)]),
+    "tag_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "tag_ndofs_total": (ctypes.c_int64, [ctypes.c_void_p]),
+    "tag_rhs": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, ctypes.c_double, ctypes.c_int32]),
+    "tag_set_state": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "tag_get_state": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "tag_state_device_ptr": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(_dp)]),
+    "tag_max_dt": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "tag_max_dt_members": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "tag_time_kernels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp, _dp]),
+    "tag_rk_steps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double,
+                                    ctypes.c_double, _dp]),
+    "tag_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32),
+                                  ctypes.c_int32]),
+    "tag_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "tag_set_elements_per_block": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "tag_get_elements_per_block": (ctypes.c_int, [ctypes.c_void_p, _ip]),
+    "tag_fp64_peak": (ctypes.c_int, [_dp]),
+    "tag_last_error": (ctypes.c_char_p, []),
+}
+
+_lib = None
+
+
+class TagError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"trixiatmo_gpu error {code}: {msg}")
+        self.code = code
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load the CUDA library; raises if it cannot be found or built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_build.LIB):
+        if not build_if_missing:
+            raise OSError(f"libtrixiatmo_gpu.so not built: {_build.LIB}")
+        _build.build()
+    L = ctypes.CDLL(_build.LIB)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(rc: int):
+    if rc != TAG_OK:
+        msg = load().tag_last_error()
+        raise TagError(rc, msg.decode() if msg else "")
+    return rc

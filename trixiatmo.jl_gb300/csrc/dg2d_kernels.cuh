@@ -1,0 +1,320 @@
+// DGSEM kernels for 2D curvilinear quadrilateral meshes (StructuredMesh /
+// P4estMesh{2} in Cartesian form), templated on the device physics policy and
+// on the number of nodes per direction n.
+//
+// One stage of the semidiscretization is two launches:
+//   k_interface  — prolong2interfaces + calc_interface_flux + calc_boundary_flux:
+//                  one thread per (interface or boundary face, face node); writes
+//                  the outward numerical flux of both sides into sfv.
+//   k_element    — volume integral (flux differencing), surface integral,
+//                  apply_jacobian, sources and (optionally) the 2N Runge-Kutta
+//                  stage update and the CFL speed reduction, EPB elements per CTA.
+// Layouts: u[e][j][i][v] (Trixi's u[v, i, j, e]); Ja[e][j][i][d][c]
+// (contravariant_vectors[c, d, i, j, e]); invJ[e][j][i]; sfv[e][face][l][NA].
+#pragma once
+#include "tag_common.cuh"
+
+namespace tag {
+
+struct BasisDev {
+  double Ds[kMaxNodes * kMaxNodes];  // Dsplit[a * n + b] (row a, column b)
+  double winv0, winvN;               // 1 / w_0, 1 / w_N
+};
+
+enum ElementMode : int { kModeRhs = 0, kModeStage = 1 };
+
+struct StageArgs {
+  double A, B;                    // 2N coefficients of this stage
+  const double* dt;               // per-member dt (device)
+  double* max_speed;              // per-member CFL speed accumulator, or null
+  const int* member;              // member of each element, or null (one member)
+};
+
+// ---------------------------------------------------------------------------
+// Interface + boundary fluxes
+// ---------------------------------------------------------------------------
+template <class Phys, int n>
+__global__ void __launch_bounds__(256) k_interface(
+    typename Phys::Params P, const double* __restrict__ u, const double* __restrict__ Ja,
+    const double* __restrict__ invJ, const int* __restrict__ if_e, const int* __restrict__ if_f,
+    const int* __restrict__ if_flip, int nif, const int* __restrict__ bd_e,
+    const int* __restrict__ bd_f, const int* __restrict__ bd_kind, int nbd,
+    double* __restrict__ sfv) {
+  constexpr int NV = Phys::NV, NA = Phys::NA;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = tid / n, l = tid % n;
+  if (k < nif) {
+    const int e0 = if_e[2 * k], e1 = if_e[2 * k + 1];
+    const int f0 = if_f[2 * k], f1 = if_f[2 * k + 1];
+    const int l1 = if_flip[k] ? n - 1 - l : l;
+    int i0, j0, i1, j1;
+    face_node(f0, l, n, i0, j0);
+    face_node(f1, l1, n, i1, j1);
+    const size_t q0 = ((size_t)e0 * n + j0) * n + i0;
+    const size_t q1 = ((size_t)e1 * n + j1) * n + i1;
+    double ul[NV], ur[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      ul[v] = u[q0 * NV + v];
+      ur[v] = u[q1 * NV + v];
+    }
+    const double s = ((invJ[q0] < 0.0) ? -1.0 : 1.0) * ((f0 & 1) ? 1.0 : -1.0);
+    const double n1 = s * Ja[q0 * 4 + 2 * (f0 >> 1)];
+    const double n2 = s * Ja[q0 * 4 + 2 * (f0 >> 1) + 1];
+    double F[NA];
+    Phys::surface_flux(P, ul, ur, n1, n2, F);
+    double* s0 = sfv + (((size_t)e0 * 4 + f0) * n + l) * NA;
+    double* s1 = sfv + (((size_t)e1 * 4 + f1) * n + l1) * NA;
+#pragma unroll
+    for (int v = 0; v < NA; ++v) {
+      s0[v] = F[v];
+      s1[v] = -F[v];
+    }
+    return;
+  }
+  const int kb = k - nif;
+  if (kb < nbd) {
+    const int e = bd_e[kb], f = bd_f[kb], kind = bd_kind[kb];
+    int i, j;
+    face_node(f, l, n, i, j);
+    const size_t q = ((size_t)e * n + j) * n + i;
+    double ui[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) ui[v] = u[q * NV + v];
+    const double sj = (invJ[q] < 0.0) ? -1.0 : 1.0;
+    double n1 = sj * Ja[q * 4 + 2 * (f >> 1)];
+    double n2 = sj * Ja[q * 4 + 2 * (f >> 1) + 1];
+    double F[NA];
+    if (kind == TAG_BC_SLIP_WALL_STRUCTURED) {
+      Phys::boundary_flux(P, ui, n1, n2, f, kind, F);
+#pragma unroll
+      for (int v = 0; v < NA; ++v) F[v] *= sj;
+    } else {
+      const double so = (f & 1) ? 1.0 : -1.0;
+      Phys::boundary_flux(P, ui, so * n1, so * n2, f, kind, F);
+    }
+    double* s0 = sfv + (((size_t)e * 4 + f) * n + l) * NA;
+#pragma unroll
+    for (int v = 0; v < NA; ++v) s0[v] = F[v];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Element kernel
+// ---------------------------------------------------------------------------
+template <class Phys, int n>
+struct ElemSmem {
+  static constexpr int NV = Phys::NV, NA = Phys::NA, NQ = Phys::NQ;
+  static constexpr int nn = n * n;
+  static constexpr int npl = n * (n - 1) / 2;   // pairs per line
+  static constexpr int P = 2 * n * npl;         // pairs per element
+  static constexpr int TPE = (P > nn) ? P : nn; // threads per element
+  // doubles per element
+  static constexpr int oU = 0;
+  static constexpr int oQ = oU + nn * NV;
+  static constexpr int oJa = oQ + nn * NQ;
+  static constexpr int oC = oJa + nn * 4;        // slots [2][nn][n][NA]
+  static constexpr int oL = oC + 2 * nn * n * NA; // CFL speeds [2][nn]
+  static constexpr int per_elem = oL + 2 * nn;
+  static size_t bytes(int epb) { return sizeof(double) * (size_t)per_elem * epb + sizeof(BasisDev); }
+};
+
+template <class Phys, int n, int MODE>
+__global__ void k_element(typename Phys::Params Pp, const BasisDev basis, double* __restrict__ u,
+                          double* __restrict__ du, double* __restrict__ kreg,
+                          const double* __restrict__ Ja, const double* __restrict__ invJ,
+                          const double* __restrict__ sfv, int nelem, int epb, StageArgs st,
+                          unsigned* __restrict__ status) {
+  using S = ElemSmem<Phys, n>;
+  constexpr int NV = Phys::NV, NA = Phys::NA, NQ = Phys::NQ;
+  constexpr int nn = S::nn, npl = S::npl;
+  extern __shared__ double smem[];
+  BasisDev* sb = reinterpret_cast<BasisDev*>(smem);
+  double* base = smem + sizeof(BasisDev) / sizeof(double);
+
+  const int e_first = blockIdx.x * epb;
+  const int ne = min(epb, nelem - e_first);
+  const int nthr = blockDim.x;
+  unsigned bad = 0;
+
+  // --- phase 0: basis + element data to shared memory
+  for (int t = threadIdx.x; t < (int)(sizeof(BasisDev) / sizeof(double)); t += nthr)
+    smem[t] = reinterpret_cast<const double*>(&basis)[t];
+  {
+    const double* ug = u + (size_t)e_first * nn * NV;
+    for (int t = threadIdx.x; t < ne * nn * NV; t += nthr) {
+      const int el = t / (nn * NV), r = t % (nn * NV);
+      base[el * S::per_elem + S::oU + r] = ug[t];
+    }
+    const double* jg = Ja + (size_t)e_first * nn * 4;
+    for (int t = threadIdx.x; t < ne * nn * 4; t += nthr) {
+      const int el = t / (nn * 4), r = t % (nn * 4);
+      base[el * S::per_elem + S::oJa + r] = jg[t];
+    }
+  }
+  __syncthreads();
+
+  // --- phase 1: per-node primitives; zero the self slots
+  for (int t = threadIdx.x; t < ne * nn; t += nthr) {
+    const int el = t / nn, node = t % nn;
+    double* eb = base + el * S::per_elem;
+    Phys::node_prims(Pp, eb + S::oU + node * NV, eb + S::oQ + node * NQ, bad);
+    const int i = node % n, j = node / n;
+#pragma unroll
+    for (int v = 0; v < NA; ++v) {
+      eb[S::oC + ((0 * nn + node) * n + i) * NA + v] = 0.0;
+      eb[S::oC + ((1 * nn + node) * n + j) * NA + v] = 0.0;
+    }
+  }
+  __syncthreads();
+
+  // --- phase 2: one thread per symmetric pair (a < b) on a line
+  for (int t = threadIdx.x; t < ne * S::P; t += nthr) {
+    const int el = t / S::P, p = t % S::P;
+    const int d = p / (n * npl), r = p % (n * npl);
+    const int line = r / npl;
+    int q = r % npl, a = 0;
+    while (q >= n - 1 - a) { q -= n - 1 - a; ++a; }
+    const int b = a + 1 + q;
+    const int na_ = d == 0 ? line * n + a : a * n + line;
+    const int nb_ = d == 0 ? line * n + b : b * n + line;
+    double* eb = base + el * S::per_elem;
+    const double* ja_a = eb + S::oJa + na_ * 4 + 2 * d;
+    const double* ja_b = eb + S::oJa + nb_ * 4 + 2 * d;
+    const double n1 = 0.5 * (ja_a[0] + ja_b[0]);
+    const double n2 = 0.5 * (ja_a[1] + ja_b[1]);
+    double Fa[NA], Fb[NA];
+    Phys::volume_pair(Pp, eb + S::oQ + na_ * NQ, eb + S::oQ + nb_ * NQ, n1, n2, Fa, Fb);
+    const double dab = sb->Ds[a * n + b], dba = sb->Ds[b * n + a];
+    double* ca = eb + S::oC + ((d * nn + na_) * n + b) * NA;
+    double* cb = eb + S::oC + ((d * nn + nb_) * n + a) * NA;
+#pragma unroll
+    for (int v = 0; v < NA; ++v) {
+      ca[v] = dab * Fa[v];
+      cb[v] = dba * Fb[v];
+    }
+  }
+  __syncthreads();
+
+  // --- phase 3: per (node, variable): slot sums, surface integral, Jacobian,
+  //     stage update
+  for (int t = threadIdx.x; t < ne * nn * NA; t += nthr) {
+    const int el = t / (nn * NA), r = t % (nn * NA);
+    const int node = r / NA, v = r % NA;
+    const int i = node % n, j = node / n;
+    const int e = e_first + el;
+    double* eb = base + el * S::per_elem;
+    double acc = 0.0;
+#pragma unroll
+    for (int b = 0; b < n; ++b) acc += eb[S::oC + ((0 * nn + node) * n + b) * NA + v];
+#pragma unroll
+    for (int b = 0; b < n; ++b) acc += eb[S::oC + ((1 * nn + node) * n + b) * NA + v];
+    const double* se = sfv + (size_t)e * 4 * n * NA;
+    if (i == 0) acc += se[(0 * n + j) * NA + v] * sb->winv0;
+    if (i == n - 1) acc += se[(1 * n + j) * NA + v] * sb->winvN;
+    if (j == 0) acc += se[(2 * n + i) * NA + v] * sb->winv0;
+    if (j == n - 1) acc += se[(3 * n + i) * NA + v] * sb->winvN;
+    const size_t gq = (size_t)e * nn + node;
+    const double dv = acc * (-invJ[gq]);
+    if (!isfinite(dv)) bad |= TAG_S_NAN;
+    if (MODE == kModeRhs) {
+      du[gq * NV + v] = dv;
+    } else {
+      const size_t kq = gq * NA + v;
+      const double dt = st.dt[st.member ? st.member[e] : 0];
+      const double kn = st.A * kreg[kq] + dt * dv;
+      kreg[kq] = kn;
+      const double un = eb[S::oU + node * NV + v] + st.B * kn;
+      eb[S::oU + node * NV + v] = un;
+      u[gq * NV + v] = un;
+    }
+  }
+  if (MODE == kModeRhs) {
+    // passive variables have zero time derivative
+    for (int t = threadIdx.x; t < ne * nn * (NV - NA); t += nthr) {
+      const int el = t / (nn * (NV - NA)), r = t % (nn * (NV - NA));
+      const int node = r / (NV - NA), v = NA + r % (NV - NA);
+      du[((size_t)(e_first + el) * nn + node) * NV + v] = 0.0;
+    }
+  }
+
+  // --- phase 4 (last stage of a step): CFL speeds of the updated state
+  if (MODE == kModeStage && st.max_speed != nullptr) {
+    __syncthreads();
+    for (int t = threadIdx.x; t < ne * nn; t += nthr) {
+      const int el = t / nn, node = t % nn;
+      double* eb = base + el * S::per_elem;
+      double l1, l2;
+      Phys::max_speeds(Pp, eb + S::oU + node * NV, l1, l2);
+      const double* ja = eb + S::oJa + node * 4;
+      const double ij = fabs(invJ[(size_t)(e_first + el) * nn + node]);
+      eb[S::oL + node] = fabs(ja[0] * l1 + ja[1] * l2) * ij;
+      eb[S::oL + nn + node] = fabs(ja[2] * l1 + ja[3] * l2) * ij;
+    }
+    __syncthreads();
+    for (int el = threadIdx.x; el < ne; el += nthr) {
+      double* eb = base + el * S::per_elem;
+      double m1 = 0.0, m2 = 0.0;
+      for (int node = 0; node < nn; ++node) {
+        m1 = fmax(m1, eb[S::oL + node]);
+        m2 = fmax(m2, eb[S::oL + nn + node]);
+      }
+      eb[S::oL] = m1 + m2;  // element's scaled speed (slot 0 reused)
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      // one atomic per run of consecutive elements of the same member
+      int cur = st.member ? st.member[e_first] : 0;
+      double run = 0.0;
+      for (int el = 0; el < ne; ++el) {
+        const int m = st.member ? st.member[e_first + el] : 0;
+        if (m != cur) {
+          atomic_max_nonneg(st.max_speed + cur, run);
+          cur = m;
+          run = 0.0;
+        }
+        run = fmax(run, base[el * S::per_elem + S::oL]);
+      }
+      atomic_max_nonneg(st.max_speed + cur, run);
+    }
+  }
+  if (bad) atomicOr(status, bad);
+}
+
+// ---------------------------------------------------------------------------
+// CFL speed reduction of a state (Trixi.max_dt) and per-step scalars
+// ---------------------------------------------------------------------------
+template <class Phys, int n>
+__global__ void k_max_speed(typename Phys::Params Pp, const double* __restrict__ u,
+                            const double* __restrict__ Ja, const double* __restrict__ invJ,
+                            int nelem, const int* __restrict__ member,
+                            double* __restrict__ max_speed) {
+  constexpr int NV = Phys::NV, nn = n * n;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nelem) return;
+  double m1 = 0.0, m2 = 0.0;
+  for (int node = 0; node < nn; ++node) {
+    const size_t q = (size_t)e * nn + node;
+    double l1, l2;
+    Phys::max_speeds(Pp, u + q * NV, l1, l2);
+    const double* ja = Ja + q * 4;
+    const double ij = fabs(invJ[q]);
+    m1 = fmax(m1, fabs(ja[0] * l1 + ja[1] * l2) * ij);
+    m2 = fmax(m2, fabs(ja[2] * l1 + ja[3] * l2) * ij);
+  }
+  atomic_max_nonneg(max_speed + (member ? member[e] : 0), m1 + m2);
+}
+
+// Start of an RK step, per member: t += previous dt; dt = cfl * 2 / (n *
+// max_speed) (or the fixed dt); reset the speed accumulator for the step's
+// last stage.  max_speed starts at nextfloat(0) like the reference.
+__global__ void k_begin_step(MemberScalars s, const StepCtl* ctl, int nmembers, int n) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nmembers) return;
+  s.t[m] += s.dt[m];
+  const double ms = s.max_speed[m] > 0.0 ? s.max_speed[m] : 4.9406564584124654e-324;
+  s.dt[m] = ctl->fixed_dt > 0.0 ? ctl->fixed_dt : ctl->cfl * (2.0 / (n * ms));
+  s.max_speed[m] = 0.0;
+}
+
+}  // namespace tag

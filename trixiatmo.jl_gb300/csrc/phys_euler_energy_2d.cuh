@@ -1,0 +1,135 @@
+// Device physics of CompressibleEulerEnergyEquationsWithGravity2D
+// (reference: src/equations/compressible_euler_energy_with_gravity_2d.jl).
+// State u = (rho, rho_v1, rho_v2, rho_e, phi); phi = g z is passive (zero flux,
+// zero time derivative), so kernels evolve NA = 4 active variables.
+#pragma once
+#include "tag_common.cuh"
+
+namespace tag {
+
+struct PhysEnergy2D {
+  static constexpr int NV = 5;  // stored variables per node
+  static constexpr int NA = 4;  // variables with nonzero du
+  static constexpr int NQ = 5;  // per-node primitives kept in shared memory
+
+  struct Params {
+    double gamma, gm1, inv_gm1, c_lmars, inv_2c;
+  };
+
+  static Params make_params(const double* p) {
+    Params q;
+    const double c_p = p[0], c_v = p[1];
+    q.gamma = c_p / c_v;
+    q.gm1 = q.gamma - 1.0;
+    q.inv_gm1 = 1.0 / (q.gamma - 1.0);
+    q.c_lmars = p[3];
+    q.inv_2c = 0.5 / p[3];
+    return q;
+  }
+
+  // cons2prim (:527-536) -> q = (rho, v1, v2, p, phi); flags bad states.
+  TAG_DEV static void node_prims(const Params& P, const double* u, double* q, unsigned& bad) {
+    const double rho = u[0];
+    const double v1 = u[1] / rho, v2 = u[2] / rho;
+    const double p = P.gm1 * (u[3] - 0.5 * (u[1] * v1 + u[2] * v2));
+    q[0] = rho; q[1] = v1; q[2] = v2; q[3] = p; q[4] = u[4];
+    if (!(rho > 0.0)) bad |= TAG_S_NEG_DENSITY;
+    if (!(p > 0.0)) bad |= TAG_S_NEG_PRESSURE;
+  }
+
+  // One symmetric pair of the volume integral: flux_ranocha (:366-395) plus the
+  // nonconservative flux_nonconservative_waruszewski_etal (:186-205), both with
+  // the averaged contravariant vector (n1, n2).  Returns Fa = F + G/2 (added to
+  // node a with Dsplit[a,b]) and Fb = F - G/2 (node b, Dsplit[b,a]); G(b,a) = -G(a,b).
+  TAG_DEV static void volume_pair(const Params& P, const double* qa, const double* qb,
+                                  double n1, double n2, double* Fa, double* Fb) {
+    const double rho_a = qa[0], v1_a = qa[1], v2_a = qa[2], p_a = qa[3];
+    const double rho_b = qb[0], v1_b = qb[1], v2_b = qb[2], p_b = qb[3];
+    const double vn_a = v1_a * n1 + v2_a * n2;
+    const double vn_b = v1_b * n1 + v2_b * n2;
+    const double rho_mean = ln_mean(rho_a, rho_b);
+    const double inv_rho_p_mean = p_a * p_b * inv_ln_mean(rho_a * p_b, rho_b * p_a);
+    const double v1_avg = 0.5 * (v1_a + v1_b);
+    const double v2_avg = 0.5 * (v2_a + v2_b);
+    const double p_avg = 0.5 * (p_a + p_b);
+    const double vsq_avg = 0.5 * (v1_a * v1_b + v2_a * v2_b);
+    const double f1 = rho_mean * 0.5 * (vn_a + vn_b);
+    const double f2 = f1 * v1_avg + p_avg * n1;
+    const double f3 = f1 * v2_avg + p_avg * n2;
+    const double f4 = f1 * (vsq_avg + inv_rho_p_mean * P.inv_gm1) + 0.5 * (p_a * vn_b + p_b * vn_a);
+    // 0.5 * waruszewski: rho_avg = ln_mean(rho_a, rho_b) (same mean as above)
+    const double h = 0.5 * rho_mean * (qb[4] - qa[4]);
+    const double g2 = n1 * h, g3 = n2 * h, g4 = n1 * h * v1_avg + n2 * h * v2_avg;
+    Fa[0] = f1;      Fb[0] = f1;
+    Fa[1] = f2 + g2; Fb[1] = f2 - g2;
+    Fa[2] = f3 + g3; Fb[2] = f3 - g3;
+    Fa[3] = f4 + g4; Fb[3] = f4 - g4;
+  }
+
+  // FluxLMARS (:397-430) between states ul, ur for the (unnormalised) normal n.
+  TAG_DEV static void lmars(const Params& P, const double* ul, const double* ur, double n1,
+                            double n2, double* F) {
+    const double rho_ll = ul[0], rho_rr = ur[0];
+    const double v1_ll = ul[1] / rho_ll, v2_ll = ul[2] / rho_ll;
+    const double v1_rr = ur[1] / rho_rr, v2_rr = ur[2] / rho_rr;
+    const double p_ll = P.gm1 * (ul[3] - 0.5 * (ul[1] * v1_ll + ul[2] * v2_ll));
+    const double p_rr = P.gm1 * (ur[3] - 0.5 * (ur[1] * v1_rr + ur[2] * v2_rr));
+    const double v_ll = v1_ll * n1 + v2_ll * n2;
+    const double v_rr = v1_rr * n1 + v2_rr * n2;
+    const double norm_ = sqrt(n1 * n1 + n2 * n2);
+    const double c = P.c_lmars;
+    const double rho = 0.5 * (rho_ll + rho_rr);
+    const double p = 0.5 * (p_ll + p_rr) - 0.5 * c * rho * (v_rr - v_ll) / norm_;
+    const double v = 0.5 * (v_ll + v_rr) - 1.0 / (2.0 * c * rho) * (p_rr - p_ll) * norm_;
+    if (v >= 0.0) {
+      F[0] = ul[0] * v; F[1] = ul[1] * v; F[2] = ul[2] * v; F[3] = ul[3] * v + p_ll * v;
+    } else {
+      F[0] = ur[0] * v; F[1] = ur[1] * v; F[2] = ur[2] * v; F[3] = ur[3] * v + p_rr * v;
+    }
+    F[1] += p * n1;
+    F[2] += p * n2;
+  }
+
+  // Interface: surface flux (FluxLMARS, flux_zero) with the primary's outward
+  // normal; F is stored for the primary and -F for the secondary.
+  TAG_DEV static void surface_flux(const Params& P, const double* ul, const double* ur, double n1,
+                                   double n2, double* F) {
+    lmars(P, ul, ur, n1, n2, F);
+  }
+
+  // Slip wall.  kind TAG_BC_SLIP_WALL_STRUCTURED: normal (n1, n2) is the
+  // sign-corrected contravariant vector in the +xi/+eta sense; the reference
+  // method :102-129 mirrors v2 and orders the states by the parity of the face;
+  // the returned flux is OUTWARD (negated on xi-/eta- faces).
+  // kind TAG_BC_SLIP_WALL_NORMAL: (n1, n2) is the outward normal; :77-100.
+  TAG_DEV static void boundary_flux(const Params& P, const double* ui, double n1, double n2,
+                                    int face, int kind, double* F) {
+    if (kind == TAG_BC_SLIP_WALL_STRUCTURED) {
+      const double ub[5] = {ui[0], ui[1], -ui[2], ui[3], ui[4]};
+      if (face & 1) {
+        lmars(P, ui, ub, n1, n2, F);
+      } else {
+        lmars(P, ub, ui, n1, n2, F);
+        F[0] = -F[0]; F[1] = -F[1]; F[2] = -F[2]; F[3] = -F[3];
+      }
+    } else {
+      const double nn = sqrt(n1 * n1 + n2 * n2);
+      const double nx = n1 / nn, ny = n2 / nn;
+      const double un = nx * ui[1] + ny * ui[2];
+      const double ub[5] = {ui[0], ui[1] - 2.0 * un * nx, ui[2] - 2.0 * un * ny, ui[3], ui[4]};
+      lmars(P, ui, ub, n1, n2, F);
+    }
+  }
+
+  // max_abs_speeds (:518-524)
+  TAG_DEV static void max_speeds(const Params& P, const double* u, double& l1, double& l2) {
+    const double rho = u[0];
+    const double v1 = u[1] / rho, v2 = u[2] / rho;
+    const double p = P.gm1 * (u[3] - 0.5 * (u[1] * v1 + u[2] * v2));
+    const double c = sqrt(P.gamma * p / rho);
+    l1 = fabs(v1) + c;
+    l2 = fabs(v2) + c;
+  }
+};
+
+}  // namespace tag

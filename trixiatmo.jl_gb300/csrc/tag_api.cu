@@ -1,0 +1,606 @@
+// C ABI of libtrixiatmo_gpu.so (declared in include/trixiatmo_gpu.h): handle
+// management, device memory, stage sequencing, CUDA-graph capture of the RK
+// step and the elements-per-CTA autotuner.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dg2d_kernels.cuh"
+#include "phys_euler_energy_2d.cuh"
+
+using namespace tag;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define TAG_CUDA(call)                                                                    \
+  do {                                                                                    \
+    cudaError_t err_ = (call);                                                            \
+    if (err_ != cudaSuccess)                                                              \
+      return fail(TAG_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(err_));      \
+  } while (0)
+
+struct Ops;
+
+}  // namespace
+
+struct tag_handle_s {
+  int eq = 0, n = 0, nelem = 0, nif = 0, nbd = 0, nv = 0, na = 0;
+  PhysEnergy2D::Params p_energy{};
+  BasisDev basis{};
+  cudaStream_t stream = nullptr;
+  double *d_u = nullptr, *d_k = nullptr, *d_Ja = nullptr, *d_invJ = nullptr, *d_xy = nullptr,
+         *d_sfv = nullptr, *d_tmp_u = nullptr, *d_tmp_du = nullptr;
+  int *d_if_e = nullptr, *d_if_f = nullptr, *d_if_flip = nullptr, *d_bd_e = nullptr,
+      *d_bd_f = nullptr, *d_bd_kind = nullptr;
+  int nmembers = 1;
+  int* d_member = nullptr;        // [E] or null
+  double* d_mscal = nullptr;      // [3 * nmembers]: t, dt, max_speed
+  StepCtl* d_ctl = nullptr;
+  double* h_pin = nullptr;        // pinned staging, 3 * nmembers + 2 doubles
+  unsigned* d_status = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int graph_epb = -1;
+  bool speed_valid = false;
+  int epb = 0;
+  const Ops* ops = nullptr;
+};
+
+namespace {
+
+// Launchers for one (physics, n) instantiation.
+struct Ops {
+  int (*interface)(tag_handle h, const double* u);
+  int (*element)(tag_handle h, int mode, double* u, double* du, int stage, bool last);
+  int (*max_speed)(tag_handle h, const double* u);
+  int (*init)(int max_smem);
+  size_t (*smem_bytes)(int epb);
+  int threads_per_element;
+};
+
+template <class Phys>
+const typename Phys::Params& params_of(tag_handle h);
+template <>
+const PhysEnergy2D::Params& params_of<PhysEnergy2D>(tag_handle h) {
+  return h->p_energy;
+}
+
+template <class Phys, int n>
+struct OpsImpl {
+  using S = ElemSmem<Phys, n>;
+  static int interface(tag_handle h, const double* u) {
+    const int total = (h->nif + h->nbd) * n;
+    if (total == 0) return TAG_OK;
+    const int threads = 256;
+    k_interface<Phys, n><<<(total + threads - 1) / threads, threads, 0, h->stream>>>(
+        params_of<Phys>(h), u, h->d_Ja, h->d_invJ, h->d_if_e, h->d_if_f, h->d_if_flip, h->nif,
+        h->d_bd_e, h->d_bd_f, h->d_bd_kind, h->nbd, h->d_sfv);
+    TAG_CUDA(cudaGetLastError());
+    return TAG_OK;
+  }
+  static int element(tag_handle h, int mode, double* u, double* du, int stage, bool last) {
+    const int epb = h->epb > 0 ? h->epb : 4;
+    const int blocks = (h->nelem + epb - 1) / epb;
+    const int threads = std::min(1024, epb * S::TPE);
+    const size_t smem = S::bytes(epb);
+    const CK2N54 ck = ck2n54();
+    StageArgs st{};
+    st.member = h->d_member;
+    if (mode == kModeStage) {
+      st.A = ck.A[stage];
+      st.B = ck.B[stage];
+      st.dt = h->d_mscal + h->nmembers;
+      st.max_speed = last ? h->d_mscal + 2 * h->nmembers : nullptr;
+      k_element<Phys, n, kModeStage><<<blocks, threads, smem, h->stream>>>(
+          params_of<Phys>(h), h->basis, u, du, h->d_k, h->d_Ja, h->d_invJ, h->d_sfv, h->nelem,
+          epb, st, h->d_status);
+    } else {
+      k_element<Phys, n, kModeRhs><<<blocks, threads, smem, h->stream>>>(
+          params_of<Phys>(h), h->basis, u, du, h->d_k, h->d_Ja, h->d_invJ, h->d_sfv, h->nelem,
+          epb, st, h->d_status);
+    }
+    TAG_CUDA(cudaGetLastError());
+    return TAG_OK;
+  }
+  static int max_speed(tag_handle h, const double* u) {
+    const int threads = 128;
+    k_max_speed<Phys, n><<<(h->nelem + threads - 1) / threads, threads, 0, h->stream>>>(
+        params_of<Phys>(h), u, h->d_Ja, h->d_invJ, h->nelem, h->d_member,
+        h->d_mscal + 2 * h->nmembers);
+    TAG_CUDA(cudaGetLastError());
+    return TAG_OK;
+  }
+  // opt the element kernels into the device's full dynamic shared memory once,
+  // outside any stream capture
+  static int init(int max_smem) {
+    TAG_CUDA(cudaFuncSetAttribute(k_element<Phys, n, kModeStage>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    TAG_CUDA(cudaFuncSetAttribute(k_element<Phys, n, kModeRhs>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    return TAG_OK;
+  }
+  static size_t smem_bytes(int epb) { return S::bytes(epb); }
+  static const Ops* get() {
+    static const Ops ops{&interface, &element, &max_speed, &init, &smem_bytes, S::TPE};
+    return &ops;
+  }
+};
+
+template <class Phys>
+const Ops* ops_for_n(int n) {
+  switch (n) {
+    case 2: return OpsImpl<Phys, 2>::get();
+    case 3: return OpsImpl<Phys, 3>::get();
+    case 4: return OpsImpl<Phys, 4>::get();
+    case 5: return OpsImpl<Phys, 5>::get();
+    case 6: return OpsImpl<Phys, 6>::get();
+    case 7: return OpsImpl<Phys, 7>::get();
+    case 8: return OpsImpl<Phys, 8>::get();
+    default: return nullptr;
+  }
+}
+
+template <class T>
+int upload(T** dst, const T* src, size_t count, cudaStream_t s) {
+  if (count == 0) return TAG_OK;
+  TAG_CUDA(cudaMalloc(dst, count * sizeof(T)));
+  if (src) {
+    TAG_CUDA(cudaMemcpyAsync(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  } else {
+    TAG_CUDA(cudaMemsetAsync(*dst, 0, count * sizeof(T), s));
+  }
+  return TAG_OK;
+}
+
+// Julia column-major [n, n] -> row-major Dsplit[a * n + b] = derivative_split[a, b]
+void load_basis(BasisDev& b, const double* dsplit_colmajor, const double* w, int n) {
+  std::memset(&b, 0, sizeof(b));
+  for (int a = 0; a < n; ++a)
+    for (int c = 0; c < n; ++c) b.Ds[a * n + c] = dsplit_colmajor[a + n * c];
+  b.winv0 = 1.0 / w[0];
+  b.winvN = 1.0 / w[n - 1];
+}
+
+MemberScalars member_scalars(tag_handle h) {
+  return MemberScalars{h->d_mscal, h->d_mscal + h->nmembers, h->d_mscal + 2 * h->nmembers};
+}
+
+int begin_step(tag_handle h) {
+  k_begin_step<<<(h->nmembers + 127) / 128, 128, 0, h->stream>>>(member_scalars(h), h->d_ctl,
+                                                                  h->nmembers, h->n);
+  TAG_CUDA(cudaGetLastError());
+  return TAG_OK;
+}
+
+int reset_and_reduce_speeds(tag_handle h) {
+  TAG_CUDA(cudaMemsetAsync(h->d_mscal + 2 * h->nmembers, 0, sizeof(double) * h->nmembers,
+                           h->stream));
+  return h->ops->max_speed(h, h->d_u);
+}
+
+int stage_sequence(tag_handle h) {
+  // one RK step: begin-step scalars, then 5 x (interface, element)
+  int rc0 = begin_step(h);
+  if (rc0) return rc0;
+  for (int s = 0; s < 5; ++s) {
+    int rc = h->ops->interface(h, h->d_u);
+    if (rc) return rc;
+    rc = h->ops->element(h, kModeStage, h->d_u, nullptr, s, s == 4);
+    if (rc) return rc;
+  }
+  return TAG_OK;
+}
+
+int build_graph(tag_handle h) {
+  if (h->graph && h->graph_epb == h->epb) return TAG_OK;
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  cudaGraph_t g;
+  TAG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = stage_sequence(h);
+  cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
+  if (rc) return rc;
+  if (e2 != cudaSuccess) return fail(TAG_E_CUDA, cudaGetErrorString(e2));
+  TAG_CUDA(cudaGraphInstantiate(&h->graph, g, 0));
+  cudaGraphDestroy(g);
+  h->graph_epb = h->epb;
+  return TAG_OK;
+}
+
+// Times the element kernel (rhs mode, on the state `u`) for candidate
+// elements-per-CTA values and keeps the fastest.  The trial launches' status
+// bits are discarded.
+int autotune(tag_handle h, const double* u) {
+  if (h->epb > 0) return TAG_OK;
+  int dev;
+  TAG_CUDA(cudaGetDevice(&dev));
+  int max_smem = 0;
+  TAG_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (!h->d_tmp_du) TAG_CUDA(cudaMalloc(&h->d_tmp_du, sizeof(double) * h->nelem * h->n * h->n * h->nv));
+  cudaEvent_t a, b;
+  TAG_CUDA(cudaEventCreate(&a));
+  TAG_CUDA(cudaEventCreate(&b));
+  int best = 1;
+  float best_ms = 1e30f;
+  const int cands[] = {1, 2, 3, 4, 6, 8, 12, 16};
+  for (int c : cands) {
+    if ((size_t)h->ops->smem_bytes(c) > (size_t)max_smem) continue;
+    if (c * h->ops->threads_per_element > 1024) continue;
+    h->epb = c;
+    double* uu = const_cast<double*>(u);
+    int rc = h->ops->interface(h, uu);
+    if (rc) return rc;
+    for (int w = 0; w < 2; ++w) {
+      rc = h->ops->element(h, kModeRhs, uu, h->d_tmp_du, 0, false);
+      if (rc) return rc;
+    }
+    TAG_CUDA(cudaEventRecord(a, h->stream));
+    for (int r = 0; r < 5; ++r) h->ops->element(h, kModeRhs, uu, h->d_tmp_du, 0, false);
+    TAG_CUDA(cudaEventRecord(b, h->stream));
+    TAG_CUDA(cudaEventSynchronize(b));
+    float ms = 0.f;
+    TAG_CUDA(cudaEventElapsedTime(&ms, a, b));
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = c;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  h->epb = best;
+  TAG_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned), h->stream));
+  return TAG_OK;
+}
+
+__global__ void k_fp64_probe(double* out, int iters, double seed) {
+  double a0 = seed + threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4,
+         a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+  const double b = 0.999999999, c = 1.0e-9;
+  for (int i = 0; i < iters; ++i) {
+    a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+    a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* tag_last_error(void) { return g_last_error.c_str(); }
+
+int tag_create(const tag_config* cfg, tag_handle* out) {
+  if (!cfg || !out) return fail(TAG_E_INVALID, "null argument");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(TAG_E_NO_DEVICE, "no CUDA device visible");
+  if (cfg->equations != TAG_EQ_EULER_ENERGY_2D)
+    return fail(TAG_E_INVALID, "unsupported equations id");
+  if (cfg->volume_flux != TAG_VF_RANOCHA_WARUSZEWSKI || cfg->surface_flux != TAG_SF_LMARS)
+    return fail(TAG_E_INVALID, "unsupported flux combination");
+  const int n = cfg->polydeg + 1;
+  if (n < 2 || n > kMaxNodes) return fail(TAG_E_INVALID, "polydeg out of range 1..7");
+  if (cfg->nelements <= 0 || cfg->ninterfaces < 0 || cfg->nboundaries < 0)
+    return fail(TAG_E_INVALID, "bad mesh sizes");
+  if (!cfg->derivative_split || !cfg->weights || !cfg->contravariant_vectors ||
+      !cfg->inverse_jacobian)
+    return fail(TAG_E_INVALID, "missing basis or geometry arrays");
+  for (int k = 0; k < cfg->ninterfaces; ++k) {
+    for (int s = 0; s < 2; ++s) {
+      const int e = cfg->interface_elements[2 * k + s], f = cfg->interface_faces[2 * k + s];
+      if (e < 0 || e >= cfg->nelements || f < 0 || f > 3)
+        return fail(TAG_E_INVALID, "interface index out of range");
+    }
+  }
+  if (cfg->nmembers > 1) {
+    if (!cfg->element_member) return fail(TAG_E_INVALID, "element_member missing");
+    for (int e = 0; e < cfg->nelements; ++e)
+      if (cfg->element_member[e] < 0 || cfg->element_member[e] >= cfg->nmembers)
+        return fail(TAG_E_INVALID, "element_member out of range");
+    for (int k = 0; k < cfg->ninterfaces; ++k)
+      if (cfg->element_member[cfg->interface_elements[2 * k]] !=
+          cfg->element_member[cfg->interface_elements[2 * k + 1]])
+        return fail(TAG_E_INVALID, "an interface joins two ensemble members");
+  }
+  for (int k = 0; k < cfg->nboundaries; ++k) {
+    const int e = cfg->boundary_elements[k], f = cfg->boundary_faces[k],
+              kind = cfg->boundary_kinds[k];
+    if (e < 0 || e >= cfg->nelements || f < 0 || f > 3 ||
+        (kind != TAG_BC_SLIP_WALL_STRUCTURED && kind != TAG_BC_SLIP_WALL_NORMAL))
+      return fail(TAG_E_INVALID, "boundary index or kind out of range");
+  }
+
+  tag_handle h = new tag_handle_s();
+  h->eq = cfg->equations;
+  h->n = n;
+  h->nelem = cfg->nelements;
+  h->nif = cfg->ninterfaces;
+  h->nbd = cfg->nboundaries;
+  h->nmembers = cfg->nmembers > 1 ? cfg->nmembers : 1;
+  h->nv = PhysEnergy2D::NV;
+  h->na = PhysEnergy2D::NA;
+  h->p_energy = PhysEnergy2D::make_params(cfg->params);
+  h->ops = ops_for_n<PhysEnergy2D>(n);
+  load_basis(h->basis, cfg->derivative_split, cfg->weights, n);
+  auto cleanup = [&](int rc) {
+    tag_destroy(h);
+    return rc;
+  };
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return cleanup(fail(TAG_E_CUDA, "stream create failed"));
+  const size_t nodes = (size_t)h->nelem * n * n;
+  int rc = TAG_OK;
+  if ((rc = upload(&h->d_u, (const double*)nullptr, nodes * h->nv, h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_k, (const double*)nullptr, nodes * h->na, h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_Ja, cfg->contravariant_vectors, nodes * 4, h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_invJ, cfg->inverse_jacobian, nodes, h->stream))) return cleanup(rc);
+  if (cfg->node_coordinates)
+    if ((rc = upload(&h->d_xy, cfg->node_coordinates, nodes * 2, h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_sfv, (const double*)nullptr, (size_t)h->nelem * 4 * n * h->na, h->stream)))
+    return cleanup(rc);
+  if ((rc = upload(&h->d_if_e, cfg->interface_elements, (size_t)2 * h->nif, h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_if_f, cfg->interface_faces, (size_t)2 * h->nif, h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_if_flip, cfg->interface_flip, (size_t)h->nif, h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_bd_e, cfg->boundary_elements, (size_t)h->nbd, h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_bd_f, cfg->boundary_faces, (size_t)h->nbd, h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_bd_kind, cfg->boundary_kinds, (size_t)h->nbd, h->stream))) return cleanup(rc);
+  if (cfg->nmembers > 1)
+    if ((rc = upload(&h->d_member, cfg->element_member, (size_t)h->nelem, h->stream)))
+      return cleanup(rc);
+  if ((rc = upload(&h->d_mscal, (const double*)nullptr, (size_t)3 * h->nmembers, h->stream)))
+    return cleanup(rc);
+  if ((rc = upload(&h->d_ctl, (const StepCtl*)nullptr, 1, h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_status, (const unsigned*)nullptr, 1, h->stream))) return cleanup(rc);
+  if (cudaMallocHost(&h->h_pin, sizeof(double) * (3 * h->nmembers + 2)) != cudaSuccess)
+    return cleanup(fail(TAG_E_CUDA, "pinned alloc failed"));
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess)
+    return cleanup(fail(TAG_E_CUDA, "upload failed"));
+  {
+    int dev = 0, max_smem = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if ((rc = h->ops->init(max_smem))) return cleanup(rc);
+  }
+  *out = h;
+  return TAG_OK;
+}
+
+int tag_destroy(tag_handle h) {
+  if (!h) return TAG_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  double* dp[] = {h->d_u, h->d_k, h->d_Ja, h->d_invJ, h->d_xy, h->d_sfv, h->d_tmp_u, h->d_tmp_du};
+  for (double* p : dp)
+    if (p) cudaFree(p);
+  int* ip[] = {h->d_if_e, h->d_if_f, h->d_if_flip, h->d_bd_e, h->d_bd_f, h->d_bd_kind};
+  for (int* p : ip)
+    if (p) cudaFree(p);
+  if (h->d_member) cudaFree(h->d_member);
+  if (h->d_mscal) cudaFree(h->d_mscal);
+  if (h->d_ctl) cudaFree(h->d_ctl);
+  if (h->d_status) cudaFree(h->d_status);
+  if (h->h_pin) cudaFreeHost(h->h_pin);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return TAG_OK;
+}
+
+int64_t tag_ndofs_total(tag_handle h) {
+  return h ? (int64_t)h->nelem * h->n * h->n * h->nv : -1;
+}
+
+int tag_rhs(tag_handle h, const double* u, double* du, double t, int32_t on_device) {
+  if (!h || !u || !du) return fail(TAG_E_INVALID, "null argument");
+  (void)t;
+  const size_t bytes = sizeof(double) * (size_t)tag_ndofs_total(h);
+  const double* ud = u;
+  double* dud = du;
+  if (!on_device) {
+    if (!h->d_tmp_u) TAG_CUDA(cudaMalloc(&h->d_tmp_u, bytes));
+    if (!h->d_tmp_du) TAG_CUDA(cudaMalloc(&h->d_tmp_du, bytes));
+    TAG_CUDA(cudaMemcpyAsync(h->d_tmp_u, u, bytes, cudaMemcpyHostToDevice, h->stream));
+    ud = h->d_tmp_u;
+    dud = h->d_tmp_du;
+  }
+  int rc = autotune(h, ud);
+  if (rc) return rc;
+  rc = h->ops->interface(h, ud);
+  if (rc) return rc;
+  rc = h->ops->element(h, kModeRhs, const_cast<double*>(ud), dud, 0, false);
+  if (rc) return rc;
+  if (!on_device) TAG_CUDA(cudaMemcpyAsync(du, dud, bytes, cudaMemcpyDeviceToHost, h->stream));
+  TAG_CUDA(cudaStreamSynchronize(h->stream));
+  return TAG_OK;
+}
+
+int tag_set_state(tag_handle h, const double* u_host) {
+  if (!h || !u_host) return fail(TAG_E_INVALID, "null argument");
+  TAG_CUDA(cudaMemcpyAsync(h->d_u, u_host, sizeof(double) * (size_t)tag_ndofs_total(h),
+                           cudaMemcpyHostToDevice, h->stream));
+  TAG_CUDA(cudaMemsetAsync(h->d_k, 0, sizeof(double) * (size_t)h->nelem * h->n * h->n * h->na,
+                           h->stream));
+  TAG_CUDA(cudaStreamSynchronize(h->stream));
+  h->speed_valid = false;
+  return TAG_OK;
+}
+
+int tag_get_state(tag_handle h, double* u_host) {
+  if (!h || !u_host) return fail(TAG_E_INVALID, "null argument");
+  TAG_CUDA(cudaMemcpyAsync(u_host, h->d_u, sizeof(double) * (size_t)tag_ndofs_total(h),
+                           cudaMemcpyDeviceToHost, h->stream));
+  TAG_CUDA(cudaStreamSynchronize(h->stream));
+  return TAG_OK;
+}
+
+int tag_state_device_ptr(tag_handle h, double** u_dev) {
+  if (!h || !u_dev) return fail(TAG_E_INVALID, "null argument");
+  *u_dev = h->d_u;
+  h->speed_valid = false;  // the caller may write through the pointer
+  return TAG_OK;
+}
+
+int tag_max_dt_members(tag_handle h, double* out) {
+  if (!h || !out) return fail(TAG_E_INVALID, "null argument");
+  int rc = reset_and_reduce_speeds(h);
+  if (rc) return rc;
+  TAG_CUDA(cudaMemcpyAsync(h->h_pin, h->d_mscal + 2 * h->nmembers, sizeof(double) * h->nmembers,
+                           cudaMemcpyDeviceToHost, h->stream));
+  TAG_CUDA(cudaStreamSynchronize(h->stream));
+  for (int m = 0; m < h->nmembers; ++m) {
+    double ms = h->h_pin[m];
+    if (!(ms > 0.0)) ms = 4.9406564584124654e-324;
+    out[m] = 2.0 / (h->n * ms);
+  }
+  h->speed_valid = true;
+  return TAG_OK;
+}
+
+int tag_max_dt(tag_handle h, double* out) {
+  if (!h || !out) return fail(TAG_E_INVALID, "null argument");
+  std::vector<double> v(h->nmembers);
+  int rc = tag_max_dt_members(h, v.data());
+  if (rc) return rc;
+  *out = *std::min_element(v.begin(), v.end());
+  return TAG_OK;
+}
+
+int tag_rk_steps(tag_handle h, int32_t nsteps, double cfl, double fixed_dt, double* t) {
+  if (!h || !t || nsteps < 0) return fail(TAG_E_INVALID, "bad argument");
+  if (nsteps == 0) return TAG_OK;
+  int rc = autotune(h, h->d_u);
+  if (rc) return rc;
+  if (!h->speed_valid)
+    if ((rc = reset_and_reduce_speeds(h))) return rc;
+  TAG_CUDA(cudaStreamSynchronize(h->stream));
+  const int M = h->nmembers;
+  for (int m = 0; m < M; ++m) {
+    h->h_pin[m] = t[m];
+    h->h_pin[M + m] = 0.0;
+  }
+  h->h_pin[3 * M] = cfl;
+  h->h_pin[3 * M + 1] = fixed_dt;
+  // t and dt (max_speed, the third array, is kept); then the control block
+  TAG_CUDA(cudaMemcpyAsync(h->d_mscal, h->h_pin, sizeof(double) * 2 * M, cudaMemcpyHostToDevice,
+                           h->stream));
+  TAG_CUDA(cudaMemcpyAsync(h->d_ctl, h->h_pin + 3 * M, sizeof(StepCtl), cudaMemcpyHostToDevice,
+                           h->stream));
+  if ((rc = build_graph(h))) return rc;
+  for (int s = 0; s < nsteps; ++s) TAG_CUDA(cudaGraphLaunch(h->graph, h->stream));
+  TAG_CUDA(cudaMemcpyAsync(h->h_pin, h->d_mscal, sizeof(double) * 2 * M, cudaMemcpyDeviceToHost,
+                           h->stream));
+  TAG_CUDA(cudaStreamSynchronize(h->stream));
+  for (int m = 0; m < M; ++m) t[m] = h->h_pin[m] + h->h_pin[M + m];
+  h->speed_valid = true;
+  return TAG_OK;
+}
+
+int tag_time_kernels(tag_handle h, int32_t reps, double* ms_interface, double* ms_element) {
+  if (!h || !ms_interface || !ms_element || reps <= 0) return fail(TAG_E_INVALID, "bad argument");
+  int rc = autotune(h, h->d_u);
+  if (rc) return rc;
+  if ((rc = reset_and_reduce_speeds(h))) return rc;
+  h->h_pin[0] = 1.0;  // cfl
+  h->h_pin[1] = 0.0;
+  TAG_CUDA(cudaMemcpyAsync(h->d_ctl, h->h_pin, sizeof(StepCtl), cudaMemcpyHostToDevice, h->stream));
+  if ((rc = begin_step(h))) return rc;
+  std::vector<cudaEvent_t> ev(3 * reps);
+  for (auto& e : ev) TAG_CUDA(cudaEventCreate(&e));
+  // warm-up stage
+  if ((rc = h->ops->interface(h, h->d_u))) return rc;
+  if ((rc = h->ops->element(h, kModeStage, h->d_u, nullptr, 0, false))) return rc;
+  for (int r = 0; r < reps; ++r) {
+    TAG_CUDA(cudaEventRecord(ev[3 * r], h->stream));
+    if ((rc = h->ops->interface(h, h->d_u))) return rc;
+    TAG_CUDA(cudaEventRecord(ev[3 * r + 1], h->stream));
+    if ((rc = h->ops->element(h, kModeStage, h->d_u, nullptr, (r + 1) % 5, false))) return rc;
+    TAG_CUDA(cudaEventRecord(ev[3 * r + 2], h->stream));
+  }
+  TAG_CUDA(cudaStreamSynchronize(h->stream));
+  double si = 0.0, se = 0.0;
+  for (int r = 0; r < reps; ++r) {
+    float a = 0.f, b = 0.f;
+    TAG_CUDA(cudaEventElapsedTime(&a, ev[3 * r], ev[3 * r + 1]));
+    TAG_CUDA(cudaEventElapsedTime(&b, ev[3 * r + 1], ev[3 * r + 2]));
+    si += a;
+    se += b;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  *ms_interface = si / reps;
+  *ms_element = se / reps;
+  h->speed_valid = false;
+  return TAG_OK;
+}
+
+int tag_status(tag_handle h, uint32_t* flags, int32_t clear) {
+  if (!h || !flags) return fail(TAG_E_INVALID, "null argument");
+  unsigned v = 0;
+  TAG_CUDA(cudaMemcpyAsync(&v, h->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
+  if (clear) TAG_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned), h->stream));
+  TAG_CUDA(cudaStreamSynchronize(h->stream));
+  *flags = v;
+  return TAG_OK;
+}
+
+void* tag_stream(tag_handle h) { return h ? (void*)h->stream : nullptr; }
+
+int tag_set_elements_per_block(tag_handle h, int32_t epb) {
+  if (!h || epb < 0) return fail(TAG_E_INVALID, "bad argument");
+  if (epb > 0) {
+    int dev, max_smem = 0;
+    TAG_CUDA(cudaGetDevice(&dev));
+    TAG_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    if (h->ops->smem_bytes(epb) > (size_t)max_smem || epb * h->ops->threads_per_element > 1024)
+      return fail(TAG_E_INVALID, "elements per block too large for one CTA");
+  }
+  h->epb = epb;
+  return TAG_OK;
+}
+
+int tag_get_elements_per_block(tag_handle h, int32_t* epb) {
+  if (!h || !epb) return fail(TAG_E_INVALID, "null argument");
+  *epb = h->epb;
+  return TAG_OK;
+}
+
+int tag_fp64_peak(double* flops_per_s) {
+  if (!flops_per_s) return fail(TAG_E_INVALID, "null argument");
+  int dev, sms = 0;
+  TAG_CUDA(cudaGetDevice(&dev));
+  TAG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int threads = 256, blocks = sms * 8, iters = 1 << 14;
+  double* out = nullptr;
+  TAG_CUDA(cudaMalloc(&out, sizeof(double) * threads * blocks));
+  cudaEvent_t a, b;
+  TAG_CUDA(cudaEventCreate(&a));
+  TAG_CUDA(cudaEventCreate(&b));
+  k_fp64_probe<<<blocks, threads>>>(out, iters, 1.0);
+  float best = 1e30f;
+  for (int r = 0; r < 3; ++r) {
+    TAG_CUDA(cudaEventRecord(a));
+    k_fp64_probe<<<blocks, threads>>>(out, iters, 1.0 + r);
+    TAG_CUDA(cudaEventRecord(b));
+    TAG_CUDA(cudaEventSynchronize(b));
+    float ms;
+    TAG_CUDA(cudaEventElapsedTime(&ms, a, b));
+    best = std::min(best, ms);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  *flops_per_s = 2.0 * 8.0 * iters * (double)threads * blocks / (best * 1e-3);
+  return TAG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,80 @@
+// Shared device helpers for the DGSEM kernels (FP64 on CUDA cores).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/trixiatmo_gpu.h"
+
+#define TAG_DEV __device__ __forceinline__
+
+namespace tag {
+
+constexpr int kMaxNodes = 8;  // n = polydeg + 1 supported up to polydeg 7
+
+// Logarithmic mean and its inverse in the form of Ranocha et al., ACM TOMS 49
+// (2023), arXiv:2112.10517: a 4-term series in f2 = ((x-y)/(x+y))^2 when
+// f2 < 1e-4, else (y-x)/log(y/x).  Trixi.ln_mean / Trixi.inv_ln_mean are the
+// reference's definitions (imported at src/TrixiAtmo.jl:37).
+TAG_DEV double ln_mean(double x, double y) {
+  const double f2 = (x * (x - 2.0 * y) + y * y) / (x * (x + 2.0 * y) + y * y);
+  if (f2 < 1.0e-4) {
+    return (x + y) * 52.5 / (105.0 + f2 * (35.0 + f2 * (21.0 + f2 * 15.0)));
+  }
+  return (y - x) / log(y / x);
+}
+
+TAG_DEV double inv_ln_mean(double x, double y) {
+  const double f2 = (x * (x - 2.0 * y) + y * y) / (x * (x + 2.0 * y) + y * y);
+  if (f2 < 1.0e-4) {
+    return (105.0 + f2 * (35.0 + f2 * (21.0 + f2 * 15.0))) / (52.5 * (x + y));
+  }
+  return log(y / x) / (y - x);
+}
+
+// Face node (i, j) of face f (0 = xi-, 1 = xi+, 2 = eta-, 3 = eta+) at index l.
+TAG_DEV void face_node(int f, int l, int n, int& i, int& j) {
+  if (f < 2) {
+    i = (f == 0) ? 0 : n - 1;
+    j = l;
+  } else {
+    i = l;
+    j = (f == 2) ? 0 : n - 1;
+  }
+}
+
+// Atomic max of a non-negative double stored as its IEEE bit pattern.
+TAG_DEV void atomic_max_nonneg(double* addr, double v) {
+  atomicMax(reinterpret_cast<unsigned long long*>(addr),
+            static_cast<unsigned long long>(__double_as_longlong(v)));
+}
+
+// Carpenter-Kennedy RK4(3)5[2N] coefficients (NASA TM-109112, 1994).
+struct CK2N54 {
+  double A[5], B[5], c[5];
+};
+
+__host__ __device__ inline CK2N54 ck2n54() {
+  return CK2N54{{0.0, -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
+                 -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0},
+                {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13612068292357.0,
+                 1720146321549.0 / 2090206949498.0, 3134564353537.0 / 4481467310338.0,
+                 2277821191437.0 / 14882151754819.0},
+                {0.0, 1432997174477.0 / 9575080441755.0, 2526269341429.0 / 6820363962896.0,
+                 2006345519317.0 / 3224310063776.0, 2802321613138.0 / 2924317926251.0}};
+}
+
+// Step control shared by all ensemble members (device memory, so a captured
+// graph picks up new values without re-instantiation).
+struct StepCtl {
+  double cfl;
+  double fixed_dt;
+};
+
+// Per-member step scalars, each an array of nmembers doubles in device memory.
+struct MemberScalars {
+  double* t;          // start time of the current step
+  double* dt;         // current step size
+  double* max_speed;  // running max over elements of (max lambda1 + max lambda2)
+};
+
+}  // namespace tag

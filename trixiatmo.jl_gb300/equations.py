@@ -1,0 +1,91 @@
+"""Equation, flux and boundary-condition descriptors of the host mirror.
+
+They carry the parameters and identifiers the C ABI needs; all arithmetic on
+the solution happens in the CUDA kernels.  Names follow TrixiAtmo/Trixi:
+`CompressibleEulerEnergyEquationsWithGravity2D`
+(src/equations/compressible_euler_energy_with_gravity_2d.jl:40-60),
+`flux_ranocha` (:366), `flux_nonconservative_waruszewski_etal` (:186),
+`FluxLMARS` (:397), `flux_zero`, `boundary_condition_slip_wall` (:77, :102).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import _lib
+
+
+class CompressibleEulerEnergyEquationsWithGravity2D:
+    """State (rho, rho_v1, rho_v2, rho_e, phi); rho_e total energy w/o potential."""
+
+    nvariables = 5
+    ndims = 2
+    eq_id = _lib.TAG_EQ_EULER_ENERGY_2D
+
+    def __init__(self, *, c_p, c_v, gravity):
+        self.c_p = float(c_p)
+        self.c_v = float(c_v)
+        self.g = float(gravity)
+        self.R = self.c_p - self.c_v
+        self.gamma = self.c_p / self.c_v
+        self.inv_gamma_minus_one = 1.0 / (self.gamma - 1.0)
+        self.p_0 = 100000.0
+
+    # host-side conversions used to build initial states (compute_coefficients!)
+    def prim2cons(self, rho, v1, v2, p, phi):
+        rv1, rv2 = rho * v1, rho * v2
+        return np.stack([rho * np.ones_like(p), rv1 * np.ones_like(p), rv2 * np.ones_like(p),
+                         p * self.inv_gamma_minus_one + 0.5 * (rv1 * v1 + rv2 * v2),
+                         phi * np.ones_like(p)], axis=-1)
+
+    def cons2prim(self, u):
+        rho = u[..., 0]
+        v1 = u[..., 1] / rho
+        v2 = u[..., 2] / rho
+        p = (self.gamma - 1.0) * (u[..., 3] - 0.5 * (u[..., 1] * v1 + u[..., 2] * v2))
+        return rho, v1, v2, p, u[..., 4]
+
+
+class _NamedFlux:
+    def __init__(self, name):
+        self.name = name
+
+    def __repr__(self):
+        return self.name
+
+
+flux_ranocha = _NamedFlux("flux_ranocha")
+flux_nonconservative_waruszewski_etal = _NamedFlux("flux_nonconservative_waruszewski_etal")
+flux_zero = _NamedFlux("flux_zero")
+
+
+class FluxLMARS:
+    """Low Mach number approximate Riemann solver with a fixed speed of sound."""
+
+    def __init__(self, speed_of_sound):
+        self.speed_of_sound = float(speed_of_sound)
+
+    def __repr__(self):
+        return f"FluxLMARS({self.speed_of_sound})"
+
+
+class VolumeIntegralFluxDifferencing:
+    def __init__(self, volume_flux):
+        self.volume_flux = volume_flux
+
+
+class _BC:
+    def __init__(self, name):
+        self.name = name
+
+    def __repr__(self):
+        return self.name
+
+
+boundary_condition_slip_wall = _BC("boundary_condition_slip_wall")
+boundary_condition_periodic = _BC("boundary_condition_periodic")
+
+
+def speed_of_sound_isothermal(equations, T0):
+    return math.sqrt(equations.gamma * equations.R * T0)

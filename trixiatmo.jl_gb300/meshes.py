@@ -1,0 +1,119 @@
+"""Host-side mesh geometry and connectivity (the arrays Trixi's cache holds).
+
+`StructuredMesh` mirrors `Trixi.StructuredMesh(cells_per_dimension,
+coordinates_min, coordinates_max; periodicity)` as used by the reference's
+elixirs (e.g. examples/euler/dry_air/buoyancy/elixir_energy_inertia_gravity_waves.jl:46-50).
+Geometry is built once on the host, like Trixi's `create_cache`, and uploaded
+by `tag_create`.  Arrays are stored so that their C-order memory equals
+Trixi's column-major layout:
+  node_coordinates[e, j, i, c]          == node_coordinates[c, i, j, e]
+  contravariant_vectors[e, j, i, d, c]  == contravariant_vectors[c, d, i, j, e]
+  inverse_jacobian[e, j, i]             == inverse_jacobian[i, j, e]
+Element e of an nx x ny mesh is cell (cx, cy) with e = cx + nx * cy.
+Faces: 0 = xi-, 1 = xi+, 2 = eta-, 3 = eta+.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .basis import LobattoLegendreBasis
+
+
+class Connectivity:
+    """Interface and boundary-face lists in the C ABI's form."""
+
+    def __init__(self):
+        self.if_elements = []  # (primary, secondary)
+        self.if_faces = []
+        self.if_flip = []
+        self.bd_elements = []
+        self.bd_faces = []
+        self.bd_names = []  # boundary name per face ("x_neg", ...)
+
+    def arrays(self):
+        ie = np.asarray(self.if_elements, dtype=np.int32).reshape(-1, 2)
+        ifc = np.asarray(self.if_faces, dtype=np.int32).reshape(-1, 2)
+        fl = np.asarray(self.if_flip, dtype=np.int32)
+        be = np.asarray(self.bd_elements, dtype=np.int32)
+        bf = np.asarray(self.bd_faces, dtype=np.int32)
+        return ie, ifc, fl, be, bf
+
+
+class StructuredMesh:
+    """2D StructuredMesh on [xmin, xmax] x [ymin, ymax] (or a mapping)."""
+
+    ndims = 2
+
+    def __init__(self, cells_per_dimension, coordinates_min=None, coordinates_max=None,
+                 periodicity=(True, True), mapping=None):
+        self.nx, self.ny = map(int, cells_per_dimension)
+        self.periodicity = tuple(bool(p) for p in periodicity)
+        if mapping is None:
+            x0, y0 = map(float, coordinates_min)
+            x1, y1 = map(float, coordinates_max)
+
+            def mapping(xi, eta):
+                return (x0 + 0.5 * (xi + 1.0) * (x1 - x0), y0 + 0.5 * (eta + 1.0) * (y1 - y0))
+        self.mapping = mapping
+
+    @property
+    def nelements(self):
+        return self.nx * self.ny
+
+    def geometry(self, basis: LobattoLegendreBasis):
+        """node_coordinates, contravariant_vectors, inverse_jacobian."""
+        nx, ny, n = self.nx, self.ny, basis.n
+        E = nx * ny
+        xr = basis.nodes
+        dxr, dyr = 2.0 / nx, 2.0 / ny
+        cx = np.arange(nx)
+        cy = np.arange(ny)
+        ox = -1.0 + cx * dxr + 0.5 * dxr
+        oy = -1.0 + cy * dyr + 0.5 * dyr
+        # xi[cy, cx, j, i], eta[...]
+        XI = ox[None, :, None, None] + 0.5 * dxr * xr[None, None, None, :]
+        ETA = oy[:, None, None, None] + 0.5 * dyr * xr[None, None, :, None]
+        XI, ETA = np.broadcast_arrays(XI, ETA)
+        X, Y = self.mapping(XI, ETA)
+        X = np.broadcast_to(X, XI.shape).reshape(E, n, n)
+        Y = np.broadcast_to(Y, XI.shape).reshape(E, n, n)
+        D = basis.derivative_matrix
+        # derivatives: xi along i (last axis), eta along j
+        x_xi = np.einsum("ik,ejk->eji", D, X)
+        y_xi = np.einsum("ik,ejk->eji", D, Y)
+        x_eta = np.einsum("jk,eki->eji", D, X)
+        y_eta = np.einsum("jk,eki->eji", D, Y)
+        coords = np.stack([X, Y], axis=-1)
+        Ja = np.zeros((E, n, n, 2, 2))
+        Ja[..., 0, 0] = y_eta
+        Ja[..., 0, 1] = -x_eta
+        Ja[..., 1, 0] = -y_xi
+        Ja[..., 1, 1] = x_xi
+        invJ = 1.0 / (x_xi * y_eta - x_eta * y_xi)
+        return (np.ascontiguousarray(coords), np.ascontiguousarray(Ja),
+                np.ascontiguousarray(invJ))
+
+    def connectivity(self):
+        c = Connectivity()
+        nx, ny = self.nx, self.ny
+        px, py = self.periodicity
+        for cyi in range(ny):
+            for cxi in range(nx):
+                e = cxi + nx * cyi
+                if cxi < nx - 1 or px:
+                    c.if_elements.append((e, (cxi + 1) % nx + nx * cyi))
+                    c.if_faces.append((1, 0))
+                    c.if_flip.append(0)
+                if cyi < ny - 1 or py:
+                    c.if_elements.append((e, cxi + nx * ((cyi + 1) % ny)))
+                    c.if_faces.append((3, 2))
+                    c.if_flip.append(0)
+                if not px and cxi == 0:
+                    c.bd_elements.append(e); c.bd_faces.append(0); c.bd_names.append("x_neg")
+                if not px and cxi == nx - 1:
+                    c.bd_elements.append(e); c.bd_faces.append(1); c.bd_names.append("x_pos")
+                if not py and cyi == 0:
+                    c.bd_elements.append(e); c.bd_faces.append(2); c.bd_names.append("y_neg")
+                if not py and cyi == ny - 1:
+                    c.bd_elements.append(e); c.bd_faces.append(3); c.bd_names.append("y_pos")
+        return c

@@ -1,0 +1,301 @@
+"""`DGSEM`, `SemidiscretizationHyperbolic` and `SemidiscretizationEnsemble`:
+the host mirror of the reference's API for the `rhs!` path, backed by
+libtrixiatmo_gpu.so.
+
+    semi = SemidiscretizationHyperbolic(mesh, equations, initial_condition, solver,
+                                        boundary_conditions=...)
+    du = semi.rhs(u, t)               # Trixi.rhs_hyperbolic!(du, u, semi, t)
+    dt = semi.max_dt()                # Trixi.max_dt on the resident state
+    t  = semi.rk_steps(nsteps, cfl)   # CarpenterKennedy2N54 + StepsizeCallback
+
+Reference anchors: semidiscretization constructor
+src/semidiscretization/semidiscretization_hyperbolic_2d_manifold_in_3d.jl:78-111,
+the `rhs_hyperbolic!` override src/solvers/dgsem_p4est/dg_2d_manifold_in_3d_covariant.jl:8-71,
+`max_dt` src/callbacks_step/stepsize_dg2d.jl:5-44.
+`SemidiscretizationEnsemble` (no counterpart in the reference) runs many
+independent members — each its own mesh, initial state, time and dt — in the
+same launches.  Errors are raised as `TagError` (the reference raises Julia
+`error`s).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .basis import LobattoLegendreBasis
+from .equations import (CompressibleEulerEnergyEquationsWithGravity2D, FluxLMARS,
+                        boundary_condition_slip_wall, flux_nonconservative_waruszewski_etal,
+                        flux_ranocha, flux_zero)
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int32)
+
+
+def _ptr(a, t=_dp):
+    return a.ctypes.data_as(t) if a is not None and a.size else None
+
+
+class DGSEM:
+    def __init__(self, polydeg, surface_flux, volume_integral):
+        self.polydeg = int(polydeg)
+        self.basis = LobattoLegendreBasis(self.polydeg)
+        self.surface_flux = surface_flux
+        self.volume_integral = volume_integral
+
+
+def _flux_ids(equations, solver):
+    vf = solver.volume_integral.volume_flux
+    sf = solver.surface_flux
+    if isinstance(equations, CompressibleEulerEnergyEquationsWithGravity2D):
+        if not (isinstance(vf, tuple) and vf[0] is flux_ranocha
+                and vf[1] is flux_nonconservative_waruszewski_etal):
+            raise ValueError("volume flux must be (flux_ranocha, flux_nonconservative_waruszewski_etal)")
+        if not (isinstance(sf, tuple) and isinstance(sf[0], FluxLMARS) and sf[1] is flux_zero):
+            raise ValueError("surface flux must be (FluxLMARS(c), flux_zero)")
+        return _lib.TAG_VF_RANOCHA_WARUSZEWSKI, _lib.TAG_SF_LMARS, [
+            equations.c_p, equations.c_v, equations.g, sf[0].speed_of_sound]
+    raise ValueError(f"unsupported equations {type(equations).__name__}")
+
+
+def _bc_kinds(names, boundary_conditions):
+    kinds = []
+    bcs = boundary_conditions or {}
+    for name in names:
+        bc = bcs.get(name)
+        if bc is boundary_condition_slip_wall:
+            kinds.append(_lib.TAG_BC_SLIP_WALL_STRUCTURED)
+        else:
+            raise ValueError(f"no supported boundary condition for {name}: {bc}")
+    return kinds
+
+
+class _Handle:
+    """Owns one tag_handle built from one or more member meshes."""
+
+    def __init__(self, meshes, equations, solver, boundary_conditions):
+        basis = solver.basis
+        self.n = basis.n
+        self.equations = equations
+        coords, Ja, invJ = [], [], []
+        ie, ifc, fl, be, bf, bk, member = [], [], [], [], [], [], []
+        cache = {}
+        offset = 0
+        for m, mesh in enumerate(meshes):
+            key = id(mesh)
+            if key not in cache:
+                cache[key] = (mesh.geometry(basis), mesh.connectivity())
+            (xy, ja, ij), conn = cache[key]
+            a_ie, a_ifc, a_fl, a_be, a_bf = conn.arrays()
+            coords.append(xy); Ja.append(ja); invJ.append(ij)
+            ie.append(a_ie + offset); ifc.append(a_ifc); fl.append(a_fl)
+            be.append(a_be + offset); bf.append(a_bf)
+            bk.append(np.asarray(_bc_kinds(conn.bd_names, boundary_conditions), dtype=np.int32))
+            member.append(np.full(mesh.nelements, m, dtype=np.int32))
+            offset += mesh.nelements
+        self.nelements = offset
+        self.nmembers = len(meshes)
+        self.member_nelements = [mesh.nelements for mesh in meshes]
+        self.node_coordinates = np.ascontiguousarray(np.concatenate(coords))
+        self.contravariant_vectors = np.ascontiguousarray(np.concatenate(Ja))
+        self.inverse_jacobian = np.ascontiguousarray(np.concatenate(invJ))
+        ie = np.ascontiguousarray(np.concatenate(ie), dtype=np.int32).reshape(-1, 2)
+        ifc = np.ascontiguousarray(np.concatenate(ifc), dtype=np.int32).reshape(-1, 2)
+        fl = np.ascontiguousarray(np.concatenate(fl), dtype=np.int32)
+        be = np.ascontiguousarray(np.concatenate(be), dtype=np.int32)
+        bf = np.ascontiguousarray(np.concatenate(bf), dtype=np.int32)
+        bk = np.ascontiguousarray(np.concatenate(bk), dtype=np.int32)
+        member = np.ascontiguousarray(np.concatenate(member), dtype=np.int32)
+        vf_id, sf_id, params = _flux_ids(equations, solver)
+        L = _lib.load()
+        cfg = _lib.TagConfig()
+        cfg.equations = equations.eq_id
+        cfg.volume_flux = vf_id
+        cfg.surface_flux = sf_id
+        cfg.polydeg = solver.polydeg
+        cfg.nelements = self.nelements
+        cfg.ninterfaces = ie.shape[0]
+        cfg.nboundaries = be.shape[0]
+        cfg.nmembers = self.nmembers
+        keep = [np.asfortranarray(basis.derivative_split), np.ascontiguousarray(basis.weights)]
+        cfg.derivative_split = keep[0].ctypes.data_as(_dp)
+        cfg.weights = _ptr(keep[1])
+        cfg.contravariant_vectors = _ptr(self.contravariant_vectors)
+        cfg.inverse_jacobian = _ptr(self.inverse_jacobian)
+        cfg.node_coordinates = _ptr(self.node_coordinates)
+        cfg.interface_elements = _ptr(ie, _ip)
+        cfg.interface_faces = _ptr(ifc, _ip)
+        cfg.interface_flip = _ptr(fl, _ip)
+        cfg.boundary_elements = _ptr(be, _ip)
+        cfg.boundary_faces = _ptr(bf, _ip)
+        cfg.boundary_kinds = _ptr(bk, _ip)
+        cfg.element_member = _ptr(member, _ip) if self.nmembers > 1 else None
+        for k, p in enumerate(params):
+            cfg.params[k] = p
+        h = ctypes.c_void_p()
+        _lib.check(L.tag_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self.h = h
+        self.L = L
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.tag_destroy(self.h)
+            self.h = None
+
+
+class SemidiscretizationHyperbolic:
+    def __init__(self, mesh, equations, initial_condition, solver, *, boundary_conditions=None,
+                 source_terms=None):
+        if source_terms is not None:
+            raise ValueError("source terms are not supported for this equation set")
+        self.mesh = mesh
+        self.equations = equations
+        self.solver = solver
+        self.initial_condition = initial_condition
+        self._H = _Handle([mesh], equations, solver, boundary_conditions)
+        self.n = self._H.n
+        self.nelements = self._H.nelements
+        self.nmembers = 1
+        self.node_coordinates = self._H.node_coordinates
+        self.contravariant_vectors = self._H.contravariant_vectors
+        self.inverse_jacobian = self._H.inverse_jacobian
+        self._h = self._H.h
+        self._L = self._H.L
+
+    # ---- lifecycle -------------------------------------------------------
+    def close(self):
+        if getattr(self, "_H", None):
+            self._H.close()
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def shape(self):
+        return (self.nelements, self.n, self.n, self.equations.nvariables)
+
+    @property
+    def ndofs(self):
+        """Trixi's DOF count: nodes = nelements * n^2."""
+        return self.nelements * self.n * self.n
+
+    # ---- initial data ------------------------------------------------------
+    def compute_coefficients(self, t=0.0, initial_condition=None):
+        ic = initial_condition or self.initial_condition
+        x = self.node_coordinates
+        return np.ascontiguousarray(ic(x, t, self.equations), dtype=np.float64)
+
+    # ---- hot path ------------------------------------------------------------
+    def rhs(self, u, t=0.0, du=None):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        if u.size != self.ndofs * self.equations.nvariables:
+            raise ValueError("u has the wrong size")
+        if du is None:
+            du = np.empty_like(u)
+        _lib.check(self._L.tag_rhs(self._h, _ptr(u), _ptr(du), float(t), 0))
+        return du
+
+    def rhs_device(self, u_ptr: int, du_ptr: int, t=0.0):
+        _lib.check(self._L.tag_rhs(self._h, ctypes.cast(u_ptr, _dp), ctypes.cast(du_ptr, _dp),
+                                   float(t), 1))
+
+    def set_state(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        if u.size != self.ndofs * self.equations.nvariables:
+            raise ValueError("u has the wrong size")
+        _lib.check(self._L.tag_set_state(self._h, _ptr(u)))
+
+    def get_state(self, out=None):
+        if out is None:
+            out = np.empty(self.shape)
+        _lib.check(self._L.tag_get_state(self._h, _ptr(out)))
+        return out
+
+    def max_dt(self):
+        v = ctypes.c_double()
+        _lib.check(self._L.tag_max_dt(self._h, ctypes.byref(v)))
+        return v.value
+
+    def max_dt_members(self):
+        out = np.zeros(self.nmembers)
+        _lib.check(self._L.tag_max_dt_members(self._h, _ptr(out)))
+        return out
+
+    def rk_steps(self, nsteps, cfl=1.0, t=0.0, fixed_dt=0.0):
+        """CarpenterKennedy2N54 steps; t is a scalar (single mesh) or one time
+        per ensemble member.  Returns the new time(s)."""
+        tt = np.ascontiguousarray(np.broadcast_to(np.asarray(t, dtype=np.float64),
+                                                  (self.nmembers,)).copy())
+        _lib.check(self._L.tag_rk_steps(self._h, int(nsteps), float(cfl), float(fixed_dt),
+                                        _ptr(tt)))
+        return float(tt[0]) if self.nmembers == 1 and np.ndim(t) == 0 else tt
+
+    def time_kernels(self, reps=10):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        _lib.check(self._L.tag_time_kernels(self._h, int(reps), ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def status(self, clear=True):
+        v = ctypes.c_uint32()
+        _lib.check(self._L.tag_status(self._h, ctypes.byref(v), int(clear)))
+        return v.value
+
+    def stream(self):
+        return self._L.tag_stream(self._h)
+
+    def set_elements_per_block(self, epb):
+        _lib.check(self._L.tag_set_elements_per_block(self._h, int(epb)))
+
+    def elements_per_block(self):
+        v = ctypes.c_int32()
+        _lib.check(self._L.tag_get_elements_per_block(self._h, ctypes.byref(v)))
+        return v.value
+
+
+class SemidiscretizationEnsemble(SemidiscretizationHyperbolic):
+    """Independent ensemble members (same equations and solver; each member its
+    own mesh and initial condition) resident in one handle: every stage is one
+    interface launch and one element launch over all members, each member with
+    its own time, dt and CFL reduction."""
+
+    def __init__(self, meshes, equations, initial_conditions, solver, *,
+                 boundary_conditions=None):
+        if len(meshes) != len(initial_conditions):
+            raise ValueError("one initial condition per member")
+        self.meshes = list(meshes)
+        self.equations = equations
+        self.solver = solver
+        self.initial_conditions = list(initial_conditions)
+        self._H = _Handle(self.meshes, equations, solver, boundary_conditions)
+        self.n = self._H.n
+        self.nelements = self._H.nelements
+        self.nmembers = self._H.nmembers
+        self.member_nelements = self._H.member_nelements
+        self.member_offsets = np.concatenate([[0], np.cumsum(self.member_nelements)])
+        self.node_coordinates = self._H.node_coordinates
+        self.contravariant_vectors = self._H.contravariant_vectors
+        self.inverse_jacobian = self._H.inverse_jacobian
+        self._h = self._H.h
+        self._L = self._H.L
+
+    def compute_coefficients(self, t=0.0, initial_condition=None):
+        parts = []
+        for m, ic in enumerate(self.initial_conditions):
+            a, b = self.member_offsets[m], self.member_offsets[m + 1]
+            parts.append(ic(self.node_coordinates[a:b], t, self.equations))
+        return np.ascontiguousarray(np.concatenate(parts), dtype=np.float64)
+
+    def member_slice(self, m):
+        return slice(int(self.member_offsets[m]), int(self.member_offsets[m + 1]))
+
+
+def fp64_peak():
+    v = ctypes.c_double()
+    _lib.check(_lib.load().tag_fp64_peak(ctypes.byref(v)))
+    return v.value
