@@ -276,9 +276,9 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        rate, threads, cel = cpu_oracle_rate(args.cpu_members, 1)
+        rate, threads, cel = cpu_oracle_rate(args.cpu_members, args.cpu_steps)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{args.cpu_members} members x 1 CK2N54 step (5 stages) of the same "
+               "sample": f"{args.cpu_members} members x {args.cpu_steps} CK2N54 steps (5 stages each) of the same "
                          f"ensemble, oracle/ C++ OpenMP ({cel:.1f} s)"}
     if rank == 0:
         line = {
@@ -322,7 +322,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--members", type=int, default=256)
-    ap.add_argument("--cpu-members", type=int, default=8)
+    ap.add_argument("--cpu-members", type=int, default=64)
+    ap.add_argument("--cpu-steps", type=int, default=8)
     ap.add_argument("--ref-members", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
