@@ -72,14 +72,24 @@ def test_rhs_matches_oracle_seeded(tg, orc, gpu_lib, polydeg):
 
 
 def test_rhs_matches_oracle_bubble(tg, orc, gpu_lib):
-    """Unperturbed warm bubble at cfg0 resolution (64x32, N = 3)."""
+    """Unperturbed warm bubble at cfg0 resolution (64x32, N = 3), at rest.
+
+    Away from the bubble du is the residual of a near-hydrostatic balance:
+    O(1e-7) left over from flux terms of size |p| |Ja| |Dsplit| |invJ| ~ 5e3, so
+    any two FP64 evaluation orders differ there by ~1e-10 absolute.  The
+    tolerance is therefore taken relative to that term magnitude."""
     eq, semi = make_semi(tg, 64, 32, 3)
     u = semi.compute_coefficients()
     du = semi.rhs(u)
     du_ref = oracle_case(orc, 64, 32, 3).rhs(u)
-    # at rest only rho_v2 carries a signal (buoyancy); the rest is rounding noise
-    assert close(du, du_ref), max_norm_rel(du, du_ref)
-    assert np.abs(du[..., 2] - du_ref[..., 2]).max() <= RTOL * np.abs(du_ref[..., 2]).max()
+    _, _, _, p, _ = eq.cons2prim(u)
+    term = (np.abs(p).max() * np.abs(semi.contravariant_vectors).max() *
+            np.abs(semi.solver.basis.derivative_split).max() *
+            np.abs(semi.inverse_jacobian).max())
+    assert np.abs(du - du_ref).max() <= RTOL * term, (np.abs(du - du_ref).max(), term)
+    # the buoyancy signal itself (rho_v2 inside the bubble) agrees far better
+    big = np.abs(du_ref[..., 2]) > 1e-3 * np.abs(du_ref[..., 2]).max()
+    assert np.abs(du[..., 2] - du_ref[..., 2])[big].max() <= 1e-8 * np.abs(du_ref[..., 2]).max()
     semi.close()
 
 
