@@ -79,6 +79,8 @@ SIGNATURES = {
     "tag_get_elements_per_block": (ctypes.c_int, [ctypes.c_void_p, _ip]),
     "tag_fp64_peak": (ctypes.c_int, [_dp]),
     "tag_last_error": (ctypes.c_char_p, []),
+    "tag_rhs_noalloc": (ctypes.c_int, [ctypes.POINTER(TagConfig), _dp, _dp, ctypes.c_void_p,
+                                       ctypes.POINTER(ctypes.c_uint32)]),
 }
 
 _lib = None

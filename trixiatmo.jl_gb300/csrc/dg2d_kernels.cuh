@@ -308,7 +308,7 @@ __global__ void k_max_speed(typename Phys::Params Pp, const double* __restrict__
 // Start of an RK step, per member: t += previous dt; dt = cfl * 2 / (n *
 // max_speed) (or the fixed dt); reset the speed accumulator for the step's
 // last stage.  max_speed starts at nextfloat(0) like the reference.
-__global__ void k_begin_step(MemberScalars s, const StepCtl* ctl, int nmembers, int n) {
+static __global__ void k_begin_step(MemberScalars s, const StepCtl* ctl, int nmembers, int n) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= nmembers) return;
   s.t[m] += s.dt[m];

@@ -34,6 +34,8 @@ struct Ops;
 
 }  // namespace
 
+void tag::set_last_error(const std::string& msg) { g_last_error = msg; }
+
 struct tag_handle_s {
   int eq = 0, n = 0, nelem = 0, nif = 0, nbd = 0, nv = 0, na = 0;
   PhysEnergy2D::Params p_energy{};

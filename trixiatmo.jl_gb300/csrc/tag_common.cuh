@@ -1,6 +1,7 @@
 // Shared device helpers for the DGSEM kernels (FP64 on CUDA cores).
 #pragma once
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 #include "../../include/trixiatmo_gpu.h"
@@ -8,6 +9,9 @@
 #define TAG_DEV __device__ __forceinline__
 
 namespace tag {
+
+// Sets the message tag_last_error() returns on this thread (defined in tag_api.cu).
+void set_last_error(const std::string& msg);
 
 constexpr int kMaxNodes = 8;  // n = polydeg + 1 supported up to polydeg 7
 
