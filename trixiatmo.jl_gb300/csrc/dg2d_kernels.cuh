@@ -146,10 +146,11 @@ __global__ void k_element(typename Phys::Params Pp, const BasisDev basis, double
       const int el = t / (nn * NV), r = t % (nn * NV);
       base[el * S::per_elem + S::oU + r] = ug[t];
     }
+    // contravariant vectors are kept halved: the pair normal is the sum
     const double* jg = Ja + (size_t)e_first * nn * 4;
     for (int t = threadIdx.x; t < ne * nn * 4; t += nthr) {
       const int el = t / (nn * 4), r = t % (nn * 4);
-      base[el * S::per_elem + S::oJa + r] = jg[t];
+      base[el * S::per_elem + S::oJa + r] = 0.5 * jg[t];
     }
   }
   __syncthreads();
@@ -181,17 +182,17 @@ __global__ void k_element(typename Phys::Params Pp, const BasisDev basis, double
     double* eb = base + el * S::per_elem;
     const double* ja_a = eb + S::oJa + na_ * 4 + 2 * d;
     const double* ja_b = eb + S::oJa + nb_ * 4 + 2 * d;
-    const double n1 = 0.5 * (ja_a[0] + ja_b[0]);
-    const double n2 = 0.5 * (ja_a[1] + ja_b[1]);
+    const double n1 = ja_a[0] + ja_b[0];
+    const double n2 = ja_a[1] + ja_b[1];
     double Fa[NA], Fb[NA];
     Phys::volume_pair(Pp, eb + S::oQ + na_ * NQ, eb + S::oQ + nb_ * NQ, n1, n2, Fa, Fb);
-    const double dab = sb->Ds[a * n + b], dba = sb->Ds[b * n + a];
+    // raw pair fluxes; the D_split weights are applied in the slot reduction
     double* ca = eb + S::oC + ((d * nn + na_) * n + b) * NA;
     double* cb = eb + S::oC + ((d * nn + nb_) * n + a) * NA;
 #pragma unroll
     for (int v = 0; v < NA; ++v) {
-      ca[v] = dab * Fa[v];
-      cb[v] = dba * Fb[v];
+      ca[v] = Fa[v];
+      cb[v] = Fb[v];
     }
   }
   __syncthreads();
@@ -206,9 +207,11 @@ __global__ void k_element(typename Phys::Params Pp, const BasisDev basis, double
     double* eb = base + el * S::per_elem;
     double acc = 0.0;
 #pragma unroll
-    for (int b = 0; b < n; ++b) acc += eb[S::oC + ((0 * nn + node) * n + b) * NA + v];
+    for (int b = 0; b < n; ++b)
+      acc = fma(sb->Ds[i * n + b], eb[S::oC + ((0 * nn + node) * n + b) * NA + v], acc);
 #pragma unroll
-    for (int b = 0; b < n; ++b) acc += eb[S::oC + ((1 * nn + node) * n + b) * NA + v];
+    for (int b = 0; b < n; ++b)
+      acc = fma(sb->Ds[j * n + b], eb[S::oC + ((1 * nn + node) * n + b) * NA + v], acc);
     const double* se = sfv + (size_t)e * 4 * n * NA;
     if (i == 0) acc += se[(0 * n + j) * NA + v] * sb->winv0;
     if (i == n - 1) acc += se[(1 * n + j) * NA + v] * sb->winvN;
@@ -246,8 +249,8 @@ __global__ void k_element(typename Phys::Params Pp, const BasisDev basis, double
       double* eb = base + el * S::per_elem;
       double l1, l2;
       Phys::max_speeds(Pp, eb + S::oU + node * NV, l1, l2);
-      const double* ja = eb + S::oJa + node * 4;
-      const double ij = fabs(invJ[(size_t)(e_first + el) * nn + node]);
+      const double* ja = eb + S::oJa + node * 4;  // halved
+      const double ij = 2.0 * fabs(invJ[(size_t)(e_first + el) * nn + node]);
       eb[S::oL + node] = fabs(ja[0] * l1 + ja[1] * l2) * ij;
       eb[S::oL + nn + node] = fabs(ja[2] * l1 + ja[3] * l2) * ij;
     }

@@ -10,7 +10,7 @@ namespace tag {
 struct PhysEnergy2D {
   static constexpr int NV = 5;  // stored variables per node
   static constexpr int NA = 4;  // variables with nonzero du
-  static constexpr int NQ = 5;  // per-node primitives kept in shared memory
+  static constexpr int NQ = 6;  // per-node quantities kept in shared memory
 
   struct Params {
     double gamma, gm1, inv_gm1, c_lmars, inv_2c;
@@ -27,39 +27,49 @@ struct PhysEnergy2D {
     return q;
   }
 
-  // cons2prim (:527-536) -> q = (rho, v1, v2, p, phi); flags bad states.
+  // cons2prim (:527-536), once per node:
+  //   q = (rho, v1/2, v2/2, p/2, phi/2, beta = rho/p); flags bad states.
   TAG_DEV static void node_prims(const Params& P, const double* u, double* q, unsigned& bad) {
     const double rho = u[0];
-    const double v1 = u[1] / rho, v2 = u[2] / rho;
+    const double irho = 1.0 / rho;
+    const double v1 = u[1] * irho, v2 = u[2] * irho;
     const double p = P.gm1 * (u[3] - 0.5 * (u[1] * v1 + u[2] * v2));
-    q[0] = rho; q[1] = v1; q[2] = v2; q[3] = p; q[4] = u[4];
+    q[0] = rho;
+    q[1] = 0.5 * v1;
+    q[2] = 0.5 * v2;
+    q[3] = 0.5 * p;
+    q[4] = 0.5 * u[4];
+    q[5] = rho / p;
     if (!(rho > 0.0)) bad |= TAG_S_NEG_DENSITY;
     if (!(p > 0.0)) bad |= TAG_S_NEG_PRESSURE;
   }
 
-  // One symmetric pair of the volume integral: flux_ranocha (:366-395) plus the
-  // nonconservative flux_nonconservative_waruszewski_etal (:186-205), both with
-  // the averaged contravariant vector (n1, n2).  Returns Fa = F + G/2 (added to
-  // node a with Dsplit[a,b]) and Fb = F - G/2 (node b, Dsplit[b,a]); G(b,a) = -G(a,b).
+  // One symmetric pair of the volume integral: flux_ranocha (:366-395) plus half
+  // the nonconservative flux_nonconservative_waruszewski_etal (:186-205), both
+  // with the averaged contravariant vector (n1, n2).  Returns Fa = F + G/2 (to
+  // node a, weighted by Dsplit[a,b]) and Fb = F - G/2 (to node b, Dsplit[b,a]);
+  // G(b,a) = -G(a,b).  Written on the half-valued node quantities of
+  // node_prims; p_ll p_rr inv_ln_mean(rho_ll p_rr, rho_rr p_ll) is evaluated as
+  // the equal inv_ln_mean(rho_ll/p_ll, rho_rr/p_rr).
   TAG_DEV static void volume_pair(const Params& P, const double* qa, const double* qb,
                                   double n1, double n2, double* Fa, double* Fb) {
-    const double rho_a = qa[0], v1_a = qa[1], v2_a = qa[2], p_a = qa[3];
-    const double rho_b = qb[0], v1_b = qb[1], v2_b = qb[2], p_b = qb[3];
-    const double vn_a = v1_a * n1 + v2_a * n2;
-    const double vn_b = v1_b * n1 + v2_b * n2;
-    const double rho_mean = ln_mean(rho_a, rho_b);
-    const double inv_rho_p_mean = p_a * p_b * inv_ln_mean(rho_a * p_b, rho_b * p_a);
-    const double v1_avg = 0.5 * (v1_a + v1_b);
-    const double v2_avg = 0.5 * (v2_a + v2_b);
-    const double p_avg = 0.5 * (p_a + p_b);
-    const double vsq_avg = 0.5 * (v1_a * v1_b + v2_a * v2_b);
-    const double f1 = rho_mean * 0.5 * (vn_a + vn_b);
+    double rho_mean, inv_rho_p_mean;
+    ln_mean_pair(qa[0], qb[0], qa[5], qb[5], rho_mean, inv_rho_p_mean);
+    const double v1_avg = qa[1] + qb[1];
+    const double v2_avg = qa[2] + qb[2];
+    const double p_avg = qa[3] + qb[3];
+    const double vsq_avg = 2.0 * (qa[1] * qb[1] + qa[2] * qb[2]);
+    const double vn = v1_avg * n1 + v2_avg * n2;  // 0.5 (vn_a + vn_b)
+    const double f1 = rho_mean * vn;
     const double f2 = f1 * v1_avg + p_avg * n1;
     const double f3 = f1 * v2_avg + p_avg * n2;
-    const double f4 = f1 * (vsq_avg + inv_rho_p_mean * P.inv_gm1) + 0.5 * (p_a * vn_b + p_b * vn_a);
-    // 0.5 * waruszewski: rho_avg = ln_mean(rho_a, rho_b) (same mean as above)
-    const double h = 0.5 * rho_mean * (qb[4] - qa[4]);
-    const double g2 = n1 * h, g3 = n2 * h, g4 = n1 * h * v1_avg + n2 * h * v2_avg;
+    // 0.5 (p_a vn_b + p_b vn_a)
+    const double c1 = qa[3] * qb[1] + qb[3] * qa[1];
+    const double c2 = qa[3] * qb[2] + qb[3] * qa[2];
+    const double f4 = f1 * (vsq_avg + inv_rho_p_mean * P.inv_gm1) + 2.0 * (n1 * c1 + n2 * c2);
+    // half of waruszewski: 0.5 ln_mean(rho) (phi_b - phi_a) * (0, n1, n2, n . v_avg)
+    const double h = rho_mean * (qb[4] - qa[4]);
+    const double g2 = n1 * h, g3 = n2 * h, g4 = h * vn;
     Fa[0] = f1;      Fb[0] = f1;
     Fa[1] = f2 + g2; Fb[1] = f2 - g2;
     Fa[2] = f3 + g3; Fb[2] = f3 - g3;
