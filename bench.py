@@ -1,16 +1,23 @@
 """Benchmark: DOF·stage updates/s of the GB300 DGSEM path (FP64).
 
-Default workload: the batched ensemble of 256 dry warm-bubble members, each a
-64x32-element StructuredMesh of 20 km x 10 km at polydeg 3 (32,768 DOF per
-member, 8,388,608 DOF in total), seeded bubble amplitude U[1, 3] K and centre
-jitter +-1 km, energy + gravity equations with (flux_ranocha,
-flux_nonconservative_waruszewski_etal) / (FluxLMARS(340), flux_zero), slip
-walls in z, CarpenterKennedy2N54 at CFL 1 with per-member dt.  One bench
-"step" is one RK step (5 stages) of every member; DOF·stage/s = DOF x 5 x
-steps / time.  Inputs are larger than L2 (u alone is 336 MB), so no flush is
-needed between steps.
+Workloads (--workload):
+  shell (default) — 3D dry Euler on a cubed-sphere shell: radius 6.371e6 m,
+      top at 30 km, 6 panels x 16x16 elements x 8 radial layers (12,288
+      elements), polydeg 5 (2,654,208 DOF); isothermal 250 K hydrostatic
+      atmosphere at rest with 16 seeded Gaussian density bumps (relative
+      amplitude 1e-3, width 500 km); gravity (well-balanced nonconservative
+      term) and Coriolis (Omega = 7.292e-5); (flux_ranocha,
+      flux_nonconservative_waruszewski_etal) / (FluxLMARS(340), flux_zero);
+      slip walls inside/outside; CarpenterKennedy2N54 at CFL 1.  The default
+      20 steps are the 100 RK stages of the benchmark configuration.
+  ensemble — 256 dry warm-bubble members, each a 64x32-element StructuredMesh
+      of 20 km x 10 km at polydeg 3 (8,388,608 DOF), seeded bubble amplitude
+      U[1, 3] K and centre jitter +-1 km, per-member dt.
+One bench "step" is one RK step (5 stages) of the whole workload;
+DOF·stage/s = DOF x 5 x steps / time.  Inputs are larger than L2 (shell: u
+127 MB + Ja 191 MB + k 106 MB; ensemble: u 336 MB), so no flush is needed.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload W]
 
 Multi-GPU: replicas only (every rank runs its own ensemble; no collective on
 the data path); value = all ranks' DOF·stages / max-over-ranks time.
@@ -67,7 +74,44 @@ def make_ensemble(tg, nmembers):
     return eq, semi
 
 
-# ---- algorithmic work per DOF·stage (counted from the formulas; see DESIGN) --
+def make_shell(tg, trees=16, layers=8, polydeg=5):
+    eq = tg.CompressibleEulerEnergyEquationsWithGravity3D(
+        c_p=1004, c_v=717, gravity=tg.EARTH_GRAVITATIONAL_ACCELERATION)
+    mesh = tg.P4estMeshCubedSphereTopography(trees, layers, 6.371e6, 30000.0, polydeg=polydeg)
+    solver = tg.DGSEM(polydeg, (tg.FluxLMARS(340.0), tg.flux_zero),
+                      tg.VolumeIntegralFluxDifferencing(
+                          (tg.flux_ranocha, tg.flux_nonconservative_waruszewski_etal)))
+    ic = tg.IsothermalShell(T=250.0, amplitude=1e-3, width=500e3, ncenters=16, seed=1,
+                            radius=6.371e6)
+    semi = tg.SemidiscretizationHyperbolic(
+        mesh, eq, ic, solver, source_terms=tg.source_terms_coriolis,
+        boundary_conditions={"inside": tg.boundary_condition_slip_wall,
+                             "outside": tg.boundary_condition_slip_wall})
+    return eq, semi
+
+
+def flops_per_element_launch_3d(n, nelem):
+    """FP64 flops of one 3D element-kernel launch, counted from the reference
+    formulas: per symmetric pair 120 (flux_ranocha 3D with its two logarithmic
+    means in the 4-term form, half the Waruszewski term, both D_split
+    products), per node 11 (cons2prim), per (node, active variable)
+    3(n-1) direction sums + Jacobian + Coriolis + 5 for the stage update, plus
+    2 per face-node surface term."""
+    pairs = 3 * n * n * n * (n - 1) // 2
+    nodes = n ** 3
+    per_elem = pairs * 120 + nodes * 11 + nodes * 5 * (3 * (n - 1) + 1 + 1 + 5) + 6 * n * n * 5 * 2
+    return per_elem * nelem
+
+
+def bytes_per_element_launch_3d(n, nelem):
+    """Compulsory DRAM bytes of one 3D element-kernel (stage mode) launch: read
+    u (6), Ja (9), invJ (1), k (5), sfv (6 faces x n^2 x 5 per element); write u
+    (5 active) and k (5)."""
+    nodes = n ** 3 * nelem
+    return 8 * (nodes * (6 + 9 + 1 + 5 + 5 + 5) + nelem * 6 * n * n * 5)
+
+
+# ---- algorithmic work per DOF·stage (counted from the formulas) ---------------
 def flops_per_element_launch(n, nelem):
     """FP64 flops of one element-kernel launch: per symmetric pair 101 (flux_ranocha
     with shared means, half the Waruszewski term, both D_split products), per
@@ -163,6 +207,33 @@ def cpu_oracle_rate(nmembers_sample, steps, warmup=0):
     return dofs * 5 * steps / el, threads, el
 
 
+def cpu_oracle_rate_shell(steps):
+    """Times the oracle on the full shell workload for `steps` RK steps (the
+    host mirror builds the same geometry arrays the GPU path receives; no GPU
+    code runs)."""
+    orc = entry.load_oracle()
+    orc.build()
+    tg = entry.load_package()
+    eq = tg.CompressibleEulerEnergyEquationsWithGravity3D(
+        c_p=1004, c_v=717, gravity=tg.EARTH_GRAVITATIONAL_ACCELERATION)
+    mesh = tg.P4estMeshCubedSphereTopography(16, 8, 6.371e6, 30000.0, polydeg=5)
+    basis = tg.LobattoLegendreBasis(5)
+    xyz, Ja, invJ = mesh.geometry(basis)
+    conn = mesh.connectivity(basis)
+    o = orc.Euler3D(5, Ja, invJ, xyz, *conn.arrays(), c_p=1004.0, c_v=717.0,
+                    g=tg.EARTH_GRAVITATIONAL_ACCELERATION, c_lmars=340.0,
+                    omega=tg.EARTH_ROTATION_RATE)
+    ic = tg.IsothermalShell(T=250.0, amplitude=1e-3, width=500e3, ncenters=16, seed=1,
+                            radius=6.371e6)
+    u = np.ascontiguousarray(ic(xyz, 0.0, eq))
+    k = np.zeros_like(u)
+    t0 = time.perf_counter()
+    o.ck_steps(u, k, 0.0, 1.0, steps)
+    el = time.perf_counter() - t0
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return invJ.size * 5 * steps / el, threads, el
+
+
 def dist_init():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -170,25 +241,38 @@ def dist_init():
     return world, rank, local
 
 
+def _note():
+    return ("Julia/Trixi are not installed on this box; the reference CPU rhs! is the C++ OpenMP "
+            "restatement in oracle/ (pinned to the reference's golden l2/linf)")
+
+
 def run_reference(args):
     world, rank, _ = dist_init()
     if rank != 0:
         return
-    sample = args.ref_members
-    rate, threads, el = cpu_oracle_rate(sample, max(args.steps, 1), warmup=args.warmup > 0)
+    steps = max(args.steps, 1)
+    if args.workload == "shell":
+        rate, threads, el = cpu_oracle_rate_shell(steps)
+        config = {"workload": "3D cubed-sphere shell 6x16x16x8, polydeg 5, isothermal + Coriolis, "
+                              "CK2N54 CFL 1", "dofs": 2654208}
+        sample = f"the full shell workload, {steps} CK2N54 steps"
+    else:
+        sample_m = args.ref_members
+        rate, threads, el = cpu_oracle_rate(sample_m, steps, warmup=args.warmup > 0)
+        config = {"workload": f"ensemble of {args.members} dry warm-bubble members (64x32, "
+                              f"polydeg 3)", "members": args.members,
+                  "dofs": args.members * NX * NZ * 16}
+        sample = f"{sample_m} members x {steps} CK2N54 steps"
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": el / max(args.steps, 1) * 1e3, "higher_is_better": True,
+        "ms_per_step": el / steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"ensemble of {args.members} dry warm-bubble members "
-                               f"(64x32, polydeg 3); sample of {sample} members per step",
-                   "members": args.members, "dofs": args.members * NX * NZ * 16},
+        "config": config,
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{sample} members x {args.steps} CK2N54 steps"},
+                         "sample": sample},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "Julia/Trixi are not installed on this box; the reference CPU rhs! is the "
-                "C++ OpenMP restatement in oracle/ (pinned to the reference's golden l2/linf)",
+        "note": _note(),
     }
     print(json.dumps(line))
 
@@ -203,14 +287,30 @@ def run_ours(args):
     else:
         torch.cuda.set_device(0)
     tg = entry.load_package()
-    eq, semi = make_ensemble(tg, args.members)
+    if args.workload == "shell":
+        eq, semi = make_shell(tg)
+        n = semi.n
+        fl = flops_per_element_launch_3d(n, semi.nelements)
+        by = bytes_per_element_launch_3d(n, semi.nelements)
+        workload = ("3D dry Euler on a cubed-sphere shell, 6 panels x 16x16 elements x 8 layers, "
+                    "polydeg 5, isothermal 250 K + seeded density bumps, gravity + Coriolis, "
+                    "CK2N54 CFL 1")
+        l2_note = "inputs larger than L2 (u 127 MB, Ja 191 MB, k 106 MB)"
+    else:
+        eq, semi = make_ensemble(tg, args.members)
+        n = semi.n
+        fl = flops_per_element_launch(n, semi.nelements)
+        by = bytes_per_element_launch(n, semi.nelements)
+        workload = (f"ensemble of {args.members} dry warm-bubble members, 64x32 StructuredMesh, "
+                    "polydeg 3, CK2N54 CFL 1, per-member dt")
+        l2_note = "inputs larger than L2 (u 336 MB + k 268 MB)"
     u0 = semi.compute_coefficients()
     semi.set_state(u0)
     nmem = semi.nmembers
     stream = torch.cuda.ExternalStream(semi.stream())
     dofs = semi.ndofs
-    # warm-up (also triggers the elements-per-CTA autotuner and graph capture)
     t_m = np.zeros(nmem)
+    # warm-up (also runs the elements-per-CTA autotuner and the graph capture)
     t_m = semi.rk_steps(max(args.warmup, 1), cfl=1.0, t=t_m)
     torch.cuda.synchronize()
     if world > 1:
@@ -236,9 +336,6 @@ def run_ours(args):
 
     # kernel timing for the roofline (same stream, CUDA events, stage mode)
     ms_if, ms_el = semi.time_kernels(reps=10)
-    n = semi.n
-    fl = flops_per_element_launch(n, semi.nelements)
-    by = bytes_per_element_launch(n, semi.nelements)
     peak_fp64 = tg.fp64_peak()
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -247,12 +344,12 @@ def run_ours(args):
         hbm_peak, hbm_src = 6800.0, "fallback"
     achieved_tf = fl / (ms_el * 1e-3) / 1e12
     achieved_gbs = by / (ms_el * 1e-3) / 1e9
+    traffic = TRAFFIC_PER_DOF.get(args.workload)
 
     # end to end through the C ABI with pinned host buffers: per step, H2D of
     # the state, one RK step (5 stages), D2H of the state
     u_pin = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True).numpy()
     u_pin[...] = u0
-    semi.set_state(u_pin)
     t_e = np.zeros(nmem)
     for _ in range(2):
         semi.set_state(u_pin)
@@ -276,27 +373,33 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        rate, threads, cel = cpu_oracle_rate(args.cpu_members, args.cpu_steps)
-        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{args.cpu_members} members x {args.cpu_steps} CK2N54 steps (5 stages each) of the same "
-                         f"ensemble, oracle/ C++ OpenMP ({cel:.1f} s)"}
+        if args.workload == "shell":
+            rate, threads, cel = cpu_oracle_rate_shell(args.cpu_steps_shell)
+            smp = (f"the full shell, {args.cpu_steps_shell} CK2N54 steps (5 stages each), "
+                   f"oracle/ C++ OpenMP ({cel:.1f} s)")
+        else:
+            rate, threads, cel = cpu_oracle_rate(args.cpu_members, args.cpu_steps)
+            smp = (f"{args.cpu_members} members x {args.cpu_steps} CK2N54 steps (5 stages each) "
+                   f"of the same ensemble, oracle/ C++ OpenMP ({cel:.1f} s)")
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": smp}
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded warm-bubble ensemble)",
-            "config": {"workload": f"ensemble of {args.members} dry warm-bubble members, "
-                                   "64x32 StructuredMesh, polydeg 3, CK2N54 CFL 1",
-                       "members": args.members, "dofs": dofs, "elements": semi.nelements,
-                       "elements_per_cta": semi.elements_per_block(),
-                       "l2": "inputs larger than L2 (u 336 MB + k 268 MB per step)",
+            "data": "synthetic (seeded)",
+            "config": {"workload": workload, "dofs": dofs, "elements": semi.nelements,
+                       "polydeg": n - 1, "members": nmem,
+                       "elements_per_cta": semi.elements_per_block(), "l2": l2_note,
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "fp64", "achieved": achieved_tf, "peak": peak_fp64 / 1e12,
                          "unit": "TFLOP/s", "frac": achieved_tf / (peak_fp64 / 1e12),
-                         "traffic": None,
-                         "kernel": "k_element (volume + surface + Jacobian + RK stage)",
-                         "peak_source": "FP64 FMA probe in this run (tag_fp64_peak)",
+                         "traffic": (traffic * dofs) if traffic else None,
+                         "traffic_source": "ncu dram__bytes_read+write per DOF of a capture, "
+                                           "scaled by DOF" if traffic else None,
+                         "kernel": "element kernel (volume + surface + Jacobian + sources + "
+                                   "RK stage)",
+                         "peak_source": "FP64 FMA probe in this run (tag_fp64_peak), of measured",
                          "hbm_achieved_gbs": achieved_gbs, "hbm_peak_gbs": hbm_peak,
                          "hbm_frac": achieved_gbs / hbm_peak, "hbm_peak_source": hbm_src,
                          "ms_element": ms_el, "ms_interface": ms_if,
@@ -315,12 +418,19 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+# DRAM bytes per DOF of the element kernel from ncu captures (read + write),
+# used to report `traffic` for the full-size launch.
+TRAFFIC_PER_DOF = {}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="shell", choices=["shell", "ensemble"])
+    ap.add_argument("--cpu-steps-shell", type=int, default=2)
     ap.add_argument("--members", type=int, default=256)
     ap.add_argument("--cpu-members", type=int, default=64)
     ap.add_argument("--cpu-steps", type=int, default=8)

@@ -13,7 +13,16 @@
  *   derivative_split       [i, ii]  (dg.basis.derivative_split)
  *   weights                [i]      (dg.basis.weights)
  * Element, face and interface indices are 0-based.  Faces: 0 = xi-, 1 = xi+,
- * 2 = eta-, 3 = eta+ (Trixi directions 1..4).
+ * 2 = eta-, 3 = eta+ (Trixi directions 1..4) and, in 3D, 4 = zeta-, 5 = zeta+.
+ * 3D arrays: u[v, i, j, k, element], contravariant_vectors[c, d, i, j, k, element],
+ * inverse_jacobian[i, j, k, element]; face-local node indices (l1, l2) are
+ * (j, k), (i, k), (i, j) on xi, eta, zeta faces.
+ *
+ * Interface orientation (interface_flip): 2D — 1 if the secondary face's node
+ * order runs backward.  3D — a code o in 0..7 mapping the primary's (l1, l2)
+ * to the secondary's (s1, s2): swap the two when o & 1, then s1 = n-1-s1 when
+ * o & 2 and s2 = n-1-s2 when o & 4 (covers every face-to-face orientation of a
+ * conforming hexahedral mesh such as the cubed-sphere shell).
  *
  * Ownership: the caller owns every host array and keeps it alive for the
  * duration of the call (Julia: GC.@preserve).  The library copies what it
@@ -45,6 +54,7 @@ extern "C" {
 
 /* ---- equation systems, fluxes, boundary kinds --------------------------- */
 #define TAG_EQ_EULER_ENERGY_2D 1 /* CompressibleEulerEnergyEquationsWithGravity2D */
+#define TAG_EQ_EULER_ENERGY_3D 2 /* CompressibleEulerEnergyEquationsWithGravity3D + source_terms_coriolis */
 
 #define TAG_VF_RANOCHA_WARUSZEWSKI 1 /* (flux_ranocha, flux_nonconservative_waruszewski_etal) */
 #define TAG_SF_LMARS 1               /* (FluxLMARS(c), flux_zero)                       */
@@ -81,7 +91,9 @@ typedef struct {
                                           independent meshes (no interface joins
                                           two members); each has its own t, dt and
                                           CFL reduction.                         */
-  double params[8];  /* EULER_ENERGY_2D: c_p, c_v, gravity, LMARS speed of sound */
+  double params[8];  /* EULER_ENERGY_2D: c_p, c_v, gravity, LMARS speed of sound;
+                        EULER_ENERGY_3D: the same, then the Coriolis angular
+                        velocity (0 disables the source) */
 } tag_config;
 
 /* Creates a handle on the current CUDA device.  Replaces the cache build of

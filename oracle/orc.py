@@ -54,6 +54,18 @@ def lib():
         L.orc_euler2d_ssprk43_run.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double,
                                               ctypes.c_double, ctypes.c_double]
         L.orc_euler2d_errors_gravity_waves.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+        _ip = ctypes.POINTER(ctypes.c_int32)
+        L.orc_euler3d_create.restype = ctypes.c_void_p
+        L.orc_euler3d_create.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int,
+                                         _ip, _ip, _ip, ctypes.c_int, _ip, _ip] + \
+            [ctypes.c_double] * 5
+        L.orc_euler3d_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_euler3d_rhs.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double]
+        L.orc_euler3d_max_dt.restype = ctypes.c_double
+        L.orc_euler3d_max_dt.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_euler3d_ck_steps.restype = ctypes.c_double
+        L.orc_euler3d_ck_steps.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_int, ctypes.c_double]
         _lib = L
     return _lib
 
@@ -128,3 +140,45 @@ class Euler2D:
         l2, linf = np.zeros(5), np.zeros(5)
         lib().orc_euler2d_errors_gravity_waves(self.h, _p(u), _p(l2), _p(linf))
         return l2, linf
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+class Euler3D:
+    """Dry Euler (energy + gravity) 3D on a hexahedral mesh; geometry and
+    connectivity are the host mirror's arrays (the same ones the C ABI takes)."""
+
+    nv = 6
+
+    def __init__(self, polydeg, Ja, invJ, xyz, if_elements, if_faces, if_orient, bd_elements,
+                 bd_faces, c_p=1004.0, c_v=717.0, g=9.81, c_lmars=340.0, omega=0.0):
+        self.n = polydeg + 1
+        self.nelem = invJ.shape[0]
+        self._keep = [np.ascontiguousarray(a) for a in (Ja, invJ, xyz)]
+        ints = [np.ascontiguousarray(a, dtype=np.int32) for a in
+                (if_elements, if_faces, if_orient, bd_elements, bd_faces)]
+        self._keep += ints
+        self.h = lib().orc_euler3d_create(polydeg, self.nelem, _p(self._keep[0]),
+                                          _p(self._keep[1]), _p(self._keep[2]),
+                                          len(ints[2]), _ip(ints[0]), _ip(ints[1]),
+                                          _ip(ints[2]), len(ints[3]), _ip(ints[3]),
+                                          _ip(ints[4]), c_p, c_v, g, c_lmars, omega)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_euler3d_destroy(self.h)
+            self.h = None
+
+    def rhs(self, u, t=0.0):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        du = np.zeros_like(u)
+        lib().orc_euler3d_rhs(self.h, _p(u), _p(du), t)
+        return du
+
+    def max_dt(self, u):
+        return lib().orc_euler3d_max_dt(self.h, _p(np.ascontiguousarray(u)))
+
+    def ck_steps(self, u, k, t, cfl, nsteps, fixed_dt=0.0):
+        return lib().orc_euler3d_ck_steps(self.h, _p(u), _p(k), t, cfl, nsteps, fixed_dt)

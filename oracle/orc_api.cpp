@@ -15,7 +15,9 @@
 
 #include "orc_basis.hpp"
 #include "orc_dg2d.hpp"
+#include "orc_dg3d.hpp"
 #include "orc_euler_energy_2d.hpp"
+#include "orc_euler_energy_3d.hpp"
 #include "orc_time.hpp"
 
 namespace orc {
@@ -92,6 +94,39 @@ inline EulerEnergy2D::State ic_warm_bubble(const EulerEnergy2D& eq, const double
   const double rho_e = rho * eq.c_v * T + 0.5 * rho * v1 * v1;
   return {rho, rho * v1, 0.0, rho_e, eq.g * x[1]};
 }
+
+struct EnergyPhys3D {
+  using State = EulerEnergy3D::State;
+  static constexpr int nv = 6;
+  static constexpr bool has_noncons = true;
+  static constexpr bool has_sources = true;
+  EulerEnergy3D eq;
+  double c_lmars = 340.0, omega = 0.0;
+  State volume_flux(const State& a, const State& b, const double* n) const {
+    return eq.flux_ranocha(a, b, n);
+  }
+  State volume_noncons(const State& a, const State& b, const double* n) const {
+    return eq.noncons_waruszewski(a, b, n);
+  }
+  State surface_flux(const State& a, const State& b, const double* n) const {
+    return eq.flux_lmars(a, b, n, c_lmars);
+  }
+  State surface_noncons(const State&, const State&, const double*) const { return State{}; }
+  State bc_normal(const State& ui, const double* n) const { return eq.slip_wall_normal(ui, n, c_lmars); }
+  State source(const State& u, const double*, double) const { return eq.coriolis(u, omega); }
+  void max_abs_speeds(const State& u, double* l) const { eq.max_abs_speeds(u, l); }
+};
+
+// 3D case: geometry and connectivity are copied from the caller's arrays
+// (built by the host mirror exactly as passed to the C ABI).
+struct Euler3DCase {
+  EnergyPhys3D phys;
+  Basis basis;
+  std::vector<double> Ja, invJ, xyz;
+  Mesh3D mesh;
+  std::unique_ptr<DG3D<EnergyPhys3D>> dg;
+  size_t ndofs() const { return (size_t)mesh.nelem * basis.n * basis.n * basis.n; }
+};
 
 }  // namespace orc
 
@@ -261,6 +296,66 @@ void orc_euler2d_errors_gravity_waves(void* h, const double* u, double* l2, doub
       }
   }
   for (int v = 0; v < 5; ++v) l2[v] = std::sqrt(l2[v] / vol);
+}
+
+
+// ---- 3D: CompressibleEulerEnergyEquationsWithGravity3D on a hexahedral mesh
+void* orc_euler3d_create(int polydeg, int nelem, const double* Ja, const double* invJ,
+                         const double* xyz, int nif, const int* if_e, const int* if_f,
+                         const int* if_orient, int nbd, const int* bd_e, const int* bd_f,
+                         double c_p, double c_v, double g, double c_lmars, double omega) {
+  auto* c = new Euler3DCase();
+  c->phys.eq = EulerEnergy3D(c_p, c_v, g);
+  c->phys.c_lmars = c_lmars;
+  c->phys.omega = omega;
+  c->basis = make_lgl_basis(polydeg);
+  const int n = c->basis.n;
+  const size_t nodes = (size_t)nelem * n * n * n;
+  c->Ja.assign(Ja, Ja + nodes * 9);
+  c->invJ.assign(invJ, invJ + nodes);
+  if (xyz) c->xyz.assign(xyz, xyz + nodes * 3);
+  c->mesh.n = n;
+  c->mesh.nelem = nelem;
+  c->mesh.Ja = c->Ja.data();
+  c->mesh.invJ = c->invJ.data();
+  c->mesh.xyz = xyz ? c->xyz.data() : nullptr;
+  for (int k = 0; k < nif; ++k) {
+    c->mesh.if_e0.push_back(if_e[2 * k]);
+    c->mesh.if_e1.push_back(if_e[2 * k + 1]);
+    c->mesh.if_f0.push_back(if_f[2 * k]);
+    c->mesh.if_f1.push_back(if_f[2 * k + 1]);
+    c->mesh.if_orient.push_back(if_orient[k]);
+  }
+  for (int k = 0; k < nbd; ++k) {
+    c->mesh.bd_e.push_back(bd_e[k]);
+    c->mesh.bd_f.push_back(bd_f[k]);
+  }
+  c->dg.reset(new DG3D<EnergyPhys3D>(c->phys, c->basis, c->mesh));
+  return c;
+}
+
+void orc_euler3d_destroy(void* h) { delete static_cast<Euler3DCase*>(h); }
+
+void orc_euler3d_rhs(void* h, const double* u, double* du, double t) {
+  static_cast<Euler3DCase*>(h)->dg->rhs(u, du, t);
+}
+
+double orc_euler3d_max_dt(void* h, const double* u) {
+  return static_cast<Euler3DCase*>(h)->dg->max_dt(u);
+}
+
+double orc_euler3d_ck_steps(void* h, double* u, double* k, double t, double cfl, int nsteps,
+                            double fixed_dt) {
+  auto* c = static_cast<Euler3DCase*>(h);
+  const size_t N = c->ndofs() * 6;
+  std::vector<double> du(N);
+  for (int s = 0; s < nsteps; ++s) {
+    const double dt = fixed_dt > 0 ? fixed_dt : cfl * c->dg->max_dt(u);
+    ck2n54_step([&](const double* uu, double* dd, double tt) { c->dg->rhs(uu, dd, tt); }, u, k,
+                du.data(), N, t, dt);
+    t += dt;
+  }
+  return t;
 }
 
 }  // extern "C"

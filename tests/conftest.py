@@ -24,6 +24,9 @@ def tg():
 def orc():
     """The CPU oracle (checker)."""
     mod = _entry.load_oracle()
+    odir = os.path.join(ROOT, "oracle")
+    if odir not in sys.path:
+        sys.path.insert(0, odir)
     mod.build()
     return mod
 

@@ -1,0 +1,113 @@
+"""GPU parity of the 3D dry-Euler path (energy + gravity + Coriolis on the
+cubed-sphere shell) against the CPU oracle, through the C ABI.
+
+Tolerance as for 2D: ||a - a_oracle||_max <= 1e-12 ||a_oracle||_max over the
+whole vector; on seeded far-from-balance states every variable also within
+1e-11 of its own max norm.
+"""
+import numpy as np
+import pytest
+
+from test_oracle_golden_3d import check_golden, oracle_3d, perturb3d, shell_case
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12
+RTOL_VAR = 1e-11
+
+
+def max_norm_rel(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+def per_var(a, b):
+    out = 0.0
+    for v in range(b.shape[-1]):
+        s = np.abs(b[..., v]).max()
+        d = np.abs(a[..., v] - b[..., v]).max()
+        out = max(out, d / s if s > 0 else (0.0 if d == 0 else np.inf))
+    return out
+
+
+def make_semi(tg, trees, layers, polydeg, coriolis=True):
+    eq = tg.CompressibleEulerEnergyEquationsWithGravity3D(
+        c_p=1004, c_v=717, gravity=tg.EARTH_GRAVITATIONAL_ACCELERATION)
+    mesh = tg.P4estMeshCubedSphereTopography(trees, layers, tg.EARTH_RADIUS, 30000.0,
+                                             polydeg=polydeg)
+    solver = tg.DGSEM(polydeg, (tg.FluxLMARS(340.0), tg.flux_zero),
+                      tg.VolumeIntegralFluxDifferencing(
+                          (tg.flux_ranocha, tg.flux_nonconservative_waruszewski_etal)))
+    semi = tg.SemidiscretizationHyperbolic(
+        mesh, eq, tg.initial_condition_baroclinic_instability, solver,
+        source_terms=tg.source_terms_coriolis if coriolis else None,
+        boundary_conditions={"inside": tg.boundary_condition_slip_wall,
+                             "outside": tg.boundary_condition_slip_wall})
+    return eq, mesh, semi
+
+
+@pytest.mark.parametrize("polydeg", [2, 3, 4, 5, 7])
+def test_rhs3d_matches_oracle_seeded(tg, orc, gpu_lib, polydeg):
+    eq, mesh, semi = make_semi(tg, 2, 2, polydeg)
+    u = perturb3d(semi.compute_coefficients(), eq, seed=300 + polydeg)
+    du = semi.rhs(u)
+    o = oracle_3d(orc, tg, polydeg, semi.contravariant_vectors, semi.inverse_jacobian,
+                  semi.node_coordinates, mesh.connectivity(solver_basis(semi)))
+    du_ref = o.rhs(u)
+    assert max_norm_rel(du, du_ref) <= RTOL, max_norm_rel(du, du_ref)
+    assert per_var(du, du_ref) <= RTOL_VAR, per_var(du, du_ref)
+    assert semi.status() == 0
+    semi.close()
+
+
+def solver_basis(semi):
+    return semi.solver.basis
+
+
+def test_rhs3d_independent_of_elements_per_block(tg, gpu_lib):
+    eq, mesh, semi = make_semi(tg, 2, 2, 4)
+    u = perturb3d(semi.compute_coefficients(), eq, seed=9)
+    outs = []
+    for epb in (1, 2, 3):
+        semi.set_elements_per_block(epb)
+        outs.append(semi.rhs(u))
+        outs.append(semi.rhs(u))
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+    semi.close()
+
+
+def test_rk3d_steps_match_oracle(tg, orc, gpu_lib):
+    eq, mesh, semi = make_semi(tg, 3, 2, 4)
+    u0 = semi.compute_coefficients()
+    semi.set_state(u0)
+    dt = semi.max_dt()
+    o = oracle_3d(orc, tg, 4, semi.contravariant_vectors, semi.inverse_jacobian,
+                  semi.node_coordinates, mesh.connectivity(solver_basis(semi)))
+    assert abs(dt - o.max_dt(u0)) <= 1e-13 * dt
+    t = semi.rk_steps(3, cfl=1.0, t=0.0)
+    uo = u0.copy()
+    t_ref = o.ck_steps(uo, np.zeros_like(uo), 0.0, 1.0, 3)
+    assert abs(t - t_ref) <= 1e-12 * t_ref
+    ug = semi.get_state()
+    assert max_norm_rel(ug, uo) <= RTOL
+    assert max_norm_rel(ug - u0, uo - u0) <= 1e-9
+    assert semi.status() == 0
+    semi.close()
+
+
+def test_gpu_reproduces_reference_golden_3d(tg, orc, gpu_lib):
+    """The reference's elixir_energy_baroclinic_instability golden
+    (test/test_3d_euler_energy.jl:7-29), time-stepped entirely on the GPU
+    (ten CK2N54 steps of 1 ms, one CUDA-graph replay each)."""
+    import analysis
+    eq, mesh, semi = make_semi(tg, 8, 4, 5)
+    u = semi.compute_coefficients()
+    semi.set_state(u)
+    t = semi.rk_steps(10, fixed_dt=0.001, t=0.0)
+    assert abs(t - 0.01) < 1e-15
+    ug = semi.get_state()
+    l2, linf = analysis.error_norms(
+        ug, semi.node_coordinates, semi.inverse_jacobian, solver_basis(semi).nodes,
+        lambda x: tg.initial_condition_baroclinic_instability(x, 0.0, eq), 3)
+    check_golden(l2, linf)
+    semi.close()

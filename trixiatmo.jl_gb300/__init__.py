@@ -9,14 +9,19 @@ The directory name is not a Python identifier; load it with
 """
 from . import _lib
 from .basis import LobattoLegendreBasis
-from .equations import (CompressibleEulerEnergyEquationsWithGravity2D, FluxLMARS,
+from .equations import (CompressibleEulerEnergyEquationsWithGravity2D,
+                        CompressibleEulerEnergyEquationsWithGravity3D, FluxLMARS,
                         VolumeIntegralFluxDifferencing, boundary_condition_periodic,
                         boundary_condition_slip_wall, flux_nonconservative_waruszewski_etal,
                         flux_ranocha, flux_zero, speed_of_sound_isothermal)
-from .initial_conditions import WarmBubble, initial_condition_gravity_waves, seeded_perturbation
+from .initial_conditions import (EARTH_GRAVITATIONAL_ACCELERATION, EARTH_RADIUS,
+                                 EARTH_ROTATION_RATE, IsothermalShell, WarmBubble,
+                                 initial_condition_baroclinic_instability,
+                                 initial_condition_gravity_waves, seeded_perturbation)
 from .meshes import StructuredMesh
+from .meshes3d import P4estMeshCubedSphereTopography
 from .semidiscretization import (DGSEM, SemidiscretizationEnsemble, SemidiscretizationHyperbolic,
-                                 fp64_peak)
+                                 fp64_peak, source_terms_coriolis)
 
 __all__ = [
     "LobattoLegendreBasis", "CompressibleEulerEnergyEquationsWithGravity2D", "FluxLMARS",
@@ -24,6 +29,8 @@ __all__ = [
     "boundary_condition_slip_wall", "flux_nonconservative_waruszewski_etal", "flux_ranocha",
     "flux_zero", "speed_of_sound_isothermal", "WarmBubble", "initial_condition_gravity_waves",
     "seeded_perturbation", "StructuredMesh", "DGSEM", "SemidiscretizationHyperbolic",
-    "SemidiscretizationEnsemble",
-    "fp64_peak",
+    "SemidiscretizationEnsemble", "CompressibleEulerEnergyEquationsWithGravity3D",
+    "EARTH_GRAVITATIONAL_ACCELERATION", "EARTH_RADIUS", "EARTH_ROTATION_RATE", "IsothermalShell",
+    "initial_condition_baroclinic_instability", "P4estMeshCubedSphereTopography",
+    "source_terms_coriolis", "fp64_peak",
 ]

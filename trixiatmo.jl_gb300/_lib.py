@@ -23,6 +23,7 @@ TAG_S_NEG_PRESSURE = 0x4
 TAG_S_NEWTON_MAXIT = 0x8
 
 TAG_EQ_EULER_ENERGY_2D = 1
+TAG_EQ_EULER_ENERGY_3D = 2
 TAG_VF_RANOCHA_WARUSZEWSKI = 1
 TAG_SF_LMARS = 1
 TAG_BC_SLIP_WALL_STRUCTURED = 1

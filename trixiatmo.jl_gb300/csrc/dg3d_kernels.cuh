@@ -1,0 +1,323 @@
+// DGSEM kernels for 3D curvilinear hexahedral meshes (P4estMesh{3} in
+// Cartesian form), templated on the device physics policy and on the number of
+// nodes per direction n.  One stage = k_interface3d + k_element3d.
+//
+// Volume integral schedule: every line of n nodes has n(n-1)/2 symmetric
+// pairs; they are evaluated in round-robin order (the circle method of
+// tournament scheduling) so that within a round the pairs of a line touch
+// disjoint nodes.  Each round therefore adds D_split-weighted pair fluxes
+// straight into per-direction node accumulators without atomics, and the
+// summation order is fixed (bitwise reproducible).
+// Layouts: u[e][k][j][i][v]; Ja[e][k][j][i][d][c]; invJ[e][k][j][i];
+// sfv[e][face][l2][l1][NA].
+#pragma once
+#include "dg2d_kernels.cuh"
+
+namespace tag {
+
+TAG_DEV void face_node3d(int f, int l1, int l2, int n, int& i, int& j, int& k) {
+  const int end = (f & 1) ? n - 1 : 0;
+  const int d = f >> 1;
+  i = d == 0 ? end : l1;
+  j = d == 0 ? l1 : (d == 1 ? end : l2);
+  k = d == 2 ? end : l2;
+}
+
+TAG_DEV void orient_map(int o, int l1, int l2, int n, int& s1, int& s2) {
+  int a = (o & 1) ? l2 : l1, b = (o & 1) ? l1 : l2;
+  if (o & 2) a = n - 1 - a;
+  if (o & 4) b = n - 1 - b;
+  s1 = a;
+  s2 = b;
+}
+
+// Pair (a, b) of line-slot s in round r of the circle method on m = n rounded
+// up to even positions; returns false for the bye of odd n.
+TAG_DEV bool round_robin_pair(int n, int r, int s, int& a, int& b) {
+  const int m = (n + 1) & ~1;
+  const int mm = m - 1;
+  int x, y;
+  if (s == 0) {
+    x = mm;
+    y = r;
+  } else {
+    x = (r + s) % mm;
+    y = (r - s + mm) % mm;
+  }
+  if (x >= n || y >= n) return false;
+  a = min(x, y);
+  b = max(x, y);
+  return true;
+}
+
+template <class Phys, int n>
+__global__ void __launch_bounds__(256) k_interface3d(
+    typename Phys::Params P, const double* __restrict__ u, const double* __restrict__ Ja,
+    const double* __restrict__ invJ, const int* __restrict__ if_e, const int* __restrict__ if_f,
+    const int* __restrict__ if_o, int nif, const int* __restrict__ bd_e,
+    const int* __restrict__ bd_f, int nbd, double* __restrict__ sfv) {
+  constexpr int NV = Phys::NV, NA = Phys::NA, nn = n * n;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int kf = tid / nn, r = tid % nn;
+  const int l1 = r % n, l2 = r / n;
+  if (kf < nif) {
+    const int e0 = if_e[2 * kf], e1 = if_e[2 * kf + 1];
+    const int f0 = if_f[2 * kf], f1 = if_f[2 * kf + 1];
+    int s1, s2, i0, j0, k0, i1, j1, k1;
+    orient_map(if_o[kf], l1, l2, n, s1, s2);
+    face_node3d(f0, l1, l2, n, i0, j0, k0);
+    face_node3d(f1, s1, s2, n, i1, j1, k1);
+    const size_t q0 = (((size_t)e0 * n + k0) * n + j0) * n + i0;
+    const size_t q1 = (((size_t)e1 * n + k1) * n + j1) * n + i1;
+    double ul[NV], ur[NV], nrm[3];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      ul[v] = u[q0 * NV + v];
+      ur[v] = u[q1 * NV + v];
+    }
+    const double s = ((invJ[q0] < 0.0) ? -1.0 : 1.0) * ((f0 & 1) ? 1.0 : -1.0);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) nrm[c] = s * Ja[(q0 * 3 + (f0 >> 1)) * 3 + c];
+    double F[NA];
+    Phys::surface_flux(P, ul, ur, nrm, F);
+    double* a0 = sfv + ((((size_t)e0 * 6 + f0) * n + l2) * n + l1) * NA;
+    double* a1 = sfv + ((((size_t)e1 * 6 + f1) * n + s2) * n + s1) * NA;
+#pragma unroll
+    for (int v = 0; v < NA; ++v) {
+      a0[v] = F[v];
+      a1[v] = -F[v];
+    }
+    return;
+  }
+  const int kb = kf - nif;
+  if (kb < nbd) {
+    const int e = bd_e[kb], f = bd_f[kb];
+    int i, j, k;
+    face_node3d(f, l1, l2, n, i, j, k);
+    const size_t q = (((size_t)e * n + k) * n + j) * n + i;
+    double ui[NV], nrm[3];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) ui[v] = u[q * NV + v];
+    const double s = ((invJ[q] < 0.0) ? -1.0 : 1.0) * ((f & 1) ? 1.0 : -1.0);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) nrm[c] = s * Ja[(q * 3 + (f >> 1)) * 3 + c];
+    double F[NA];
+    Phys::boundary_flux(P, ui, nrm, F);
+    double* a0 = sfv + ((((size_t)e * 6 + f) * n + l2) * n + l1) * NA;
+#pragma unroll
+    for (int v = 0; v < NA; ++v) a0[v] = F[v];
+  }
+}
+
+template <class Phys, int n>
+struct ElemSmem3D {
+  static constexpr int NV = Phys::NV, NA = Phys::NA, NQ = Phys::NQ;
+  static constexpr int nn = n * n, nnn = n * n * n;
+  static constexpr int S = ((n + 1) & ~1) / 2;     // pair slots per line and round (incl. a bye)
+  static constexpr int R = ((n + 1) & ~1) - 1;     // rounds
+  static constexpr int P = 3 * nn * S;             // pair threads per element
+  static constexpr int TPE = (P > nnn) ? P : nnn;  // threads per element
+  static constexpr int oU = 0;
+  static constexpr int oQ = oU + nnn * NV;
+  static constexpr int oJa = oQ + nnn * NQ;       // halved
+  static constexpr int oA = oJa + nnn * 9;        // accumulators [3][nnn][NA]
+  static constexpr int oL = oA + 3 * nnn * NA;    // CFL speeds [3][nnn]
+  static constexpr int per_elem = oL + 3 * nnn;
+  static size_t bytes(int epb) { return sizeof(double) * (size_t)per_elem * epb + sizeof(BasisDev); }
+};
+
+template <class Phys, int n, int MODE>
+__global__ void k_element3d(typename Phys::Params Pp, const BasisDev basis, double* __restrict__ u,
+                            double* __restrict__ du, double* __restrict__ kreg,
+                            const double* __restrict__ Ja, const double* __restrict__ invJ,
+                            const double* __restrict__ sfv, int nelem, int epb, StageArgs st,
+                            unsigned* __restrict__ status) {
+  using S = ElemSmem3D<Phys, n>;
+  constexpr int NV = Phys::NV, NA = Phys::NA, NQ = Phys::NQ;
+  constexpr int nn = S::nn, nnn = S::nnn;
+  extern __shared__ double smem[];
+  BasisDev* sb = reinterpret_cast<BasisDev*>(smem);
+  double* base = smem + sizeof(BasisDev) / sizeof(double);
+  const int e_first = blockIdx.x * epb;
+  const int ne = min(epb, nelem - e_first);
+  const int nthr = blockDim.x;
+  unsigned bad = 0;
+
+  for (int t = threadIdx.x; t < (int)(sizeof(BasisDev) / sizeof(double)); t += nthr)
+    smem[t] = reinterpret_cast<const double*>(&basis)[t];
+  {
+    const double* ug = u + (size_t)e_first * nnn * NV;
+    for (int t = threadIdx.x; t < ne * nnn * NV; t += nthr) {
+      const int el = t / (nnn * NV), r = t % (nnn * NV);
+      base[el * S::per_elem + S::oU + r] = ug[t];
+    }
+    const double* jg = Ja + (size_t)e_first * nnn * 9;
+    for (int t = threadIdx.x; t < ne * nnn * 9; t += nthr) {
+      const int el = t / (nnn * 9), r = t % (nnn * 9);
+      base[el * S::per_elem + S::oJa + r] = 0.5 * jg[t];
+    }
+  }
+  __syncthreads();
+
+  // per-node quantities; zero the accumulators
+  for (int t = threadIdx.x; t < ne * nnn; t += nthr) {
+    const int el = t / nnn, node = t % nnn;
+    double* eb = base + el * S::per_elem;
+    Phys::node_prims(Pp, eb + S::oU + node * NV, eb + S::oQ + node * NQ, bad);
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int v = 0; v < NA; ++v) eb[S::oA + (d * nnn + node) * NA + v] = 0.0;
+  }
+  __syncthreads();
+
+  // volume integral: R rounds, one symmetric pair per thread and round
+  for (int r = 0; r < S::R; ++r) {
+    for (int t = threadIdx.x; t < ne * S::P; t += nthr) {
+      const int el = t / S::P, p = t % S::P;
+      const int slot = p % S::S, line = (p / S::S) % nn, d = p / (S::S * nn);
+      int a, b;
+      if (!round_robin_pair(n, r, slot, a, b)) continue;
+      // line = p1 + n * p2 over the two other directions (ascending)
+      const int p1 = line % n, p2 = line / n;
+      int na_, nb_;
+      if (d == 0) {
+        na_ = (p2 * n + p1) * n + a;
+        nb_ = (p2 * n + p1) * n + b;
+      } else if (d == 1) {
+        na_ = (p2 * n + a) * n + p1;
+        nb_ = (p2 * n + b) * n + p1;
+      } else {
+        na_ = (a * n + p2) * n + p1;
+        nb_ = (b * n + p2) * n + p1;
+      }
+      double* eb = base + el * S::per_elem;
+      const double* ja_a = eb + S::oJa + na_ * 9 + 3 * d;
+      const double* ja_b = eb + S::oJa + nb_ * 9 + 3 * d;
+      const double nrm[3] = {ja_a[0] + ja_b[0], ja_a[1] + ja_b[1], ja_a[2] + ja_b[2]};
+      double Fa[NA], Fb[NA];
+      Phys::volume_pair(Pp, eb + S::oQ + na_ * NQ, eb + S::oQ + nb_ * NQ, nrm, Fa, Fb);
+      const double dab = sb->Ds[a * n + b], dba = sb->Ds[b * n + a];
+      double* ca = eb + S::oA + (d * nnn + na_) * NA;
+      double* cb = eb + S::oA + (d * nnn + nb_) * NA;
+#pragma unroll
+      for (int v = 0; v < NA; ++v) {
+        ca[v] = fma(dab, Fa[v], ca[v]);
+        cb[v] = fma(dba, Fb[v], cb[v]);
+      }
+    }
+    __syncthreads();
+  }
+
+  // per (node, variable): direction sums, surface integral, Jacobian, sources,
+  // stage update
+  for (int t = threadIdx.x; t < ne * nnn * NA; t += nthr) {
+    const int el = t / (nnn * NA), r = t % (nnn * NA);
+    const int node = r / NA, v = r % NA;
+    const int i = node % n, j = (node / n) % n, k = node / nn;
+    const int e = e_first + el;
+    double* eb = base + el * S::per_elem;
+    double acc = eb[S::oA + (0 * nnn + node) * NA + v] + eb[S::oA + (1 * nnn + node) * NA + v] +
+                 eb[S::oA + (2 * nnn + node) * NA + v];
+    const double* se = sfv + (size_t)e * 6 * nn * NA;
+    if (i == 0) acc += se[((0 * n + k) * n + j) * NA + v] * sb->winv0;
+    if (i == n - 1) acc += se[((1 * n + k) * n + j) * NA + v] * sb->winvN;
+    if (j == 0) acc += se[((2 * n + k) * n + i) * NA + v] * sb->winv0;
+    if (j == n - 1) acc += se[((3 * n + k) * n + i) * NA + v] * sb->winvN;
+    if (k == 0) acc += se[((4 * n + j) * n + i) * NA + v] * sb->winv0;
+    if (k == n - 1) acc += se[((5 * n + j) * n + i) * NA + v] * sb->winvN;
+    const size_t gq = (size_t)e * nnn + node;
+    const double dv = acc * (-invJ[gq]) + Phys::source(Pp, eb + S::oU + node * NV, v);
+    if (!isfinite(dv)) bad |= TAG_S_NAN;
+    if (MODE == kModeRhs) {
+      du[gq * NV + v] = dv;
+    } else {
+      const size_t kq = gq * NA + v;
+      const double dt = st.dt[st.member ? st.member[e] : 0];
+      const double kn = st.A * kreg[kq] + dt * dv;
+      kreg[kq] = kn;
+      const double un = eb[S::oU + node * NV + v] + st.B * kn;
+      // all reads of this node's old state (the Coriolis source) precede the
+      // barrier below; write the new value to global memory now and to
+      // shared memory after it
+      u[gq * NV + v] = un;
+      eb[S::oA + node * NA + v] = un;  // stage the new value (direction-0 slot is free)
+    }
+  }
+  if (MODE == kModeRhs) {
+    for (int t = threadIdx.x; t < ne * nnn * (NV - NA); t += nthr) {
+      const int el = t / (nnn * (NV - NA)), r = t % (nnn * (NV - NA));
+      const int node = r / (NV - NA), v = NA + r % (NV - NA);
+      du[((size_t)(e_first + el) * nnn + node) * NV + v] = 0.0;
+    }
+  }
+  if (MODE == kModeStage && st.max_speed != nullptr) {
+    __syncthreads();
+    for (int t = threadIdx.x; t < ne * nnn; t += nthr) {
+      const int el = t / nnn, node = t % nnn;
+      double* eb = base + el * S::per_elem;
+      double un[NV];
+#pragma unroll
+      for (int v = 0; v < NA; ++v) un[v] = eb[S::oA + node * NA + v];
+#pragma unroll
+      for (int v = NA; v < NV; ++v) un[v] = eb[S::oU + node * NV + v];
+      double lam[3];
+      Phys::max_speeds(Pp, un, lam);
+      const double* ja = eb + S::oJa + node * 9;  // halved
+      const double ij = 2.0 * fabs(invJ[(size_t)(e_first + el) * nnn + node]);
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        eb[S::oL + d * nnn + node] =
+            fabs(ja[3 * d] * lam[0] + ja[3 * d + 1] * lam[1] + ja[3 * d + 2] * lam[2]) * ij;
+    }
+    __syncthreads();
+    for (int el = threadIdx.x; el < ne; el += nthr) {
+      double* eb = base + el * S::per_elem;
+      double m[3] = {0.0, 0.0, 0.0};
+      for (int node = 0; node < nnn; ++node)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) m[d] = fmax(m[d], eb[S::oL + d * nnn + node]);
+      eb[S::oL] = m[0] + m[1] + m[2];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int cur = st.member ? st.member[e_first] : 0;
+      double run = 0.0;
+      for (int el = 0; el < ne; ++el) {
+        const int mb = st.member ? st.member[e_first + el] : 0;
+        if (mb != cur) {
+          atomic_max_nonneg(st.max_speed + cur, run);
+          cur = mb;
+          run = 0.0;
+        }
+        run = fmax(run, base[el * S::per_elem + S::oL]);
+      }
+      atomic_max_nonneg(st.max_speed + cur, run);
+    }
+  }
+  if (bad) atomicOr(status, bad);
+}
+
+template <class Phys, int n>
+__global__ void k_max_speed3d(typename Phys::Params Pp, const double* __restrict__ u,
+                              const double* __restrict__ Ja, const double* __restrict__ invJ,
+                              int nelem, const int* __restrict__ member,
+                              double* __restrict__ max_speed) {
+  constexpr int NV = Phys::NV, nnn = n * n * n;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nelem) return;
+  double m[3] = {0.0, 0.0, 0.0};
+  for (int node = 0; node < nnn; ++node) {
+    const size_t q = (size_t)e * nnn + node;
+    double lam[3];
+    Phys::max_speeds(Pp, u + q * NV, lam);
+    const double* ja = Ja + q * 9;
+    const double ij = fabs(invJ[q]);
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      m[d] = fmax(m[d], fabs(ja[3 * d] * lam[0] + ja[3 * d + 1] * lam[1] + ja[3 * d + 2] * lam[2]) * ij);
+  }
+  atomic_max_nonneg(max_speed + (member ? member[e] : 0), m[0] + m[1] + m[2]);
+}
+
+}  // namespace tag

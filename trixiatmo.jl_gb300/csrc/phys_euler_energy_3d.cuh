@@ -1,0 +1,132 @@
+// Device physics of CompressibleEulerEnergyEquationsWithGravity3D
+// (reference: src/equations/compressible_euler_energy_with_gravity_3d.jl) and
+// the Coriolis source (src/equations/initial_condition_compressible_euler_3d.jl:245-269).
+// State u = (rho, rho_v1, rho_v2, rho_v3, rho_e, phi); phi is passive, so
+// kernels evolve NA = 5 active variables.
+#pragma once
+#include "tag_common.cuh"
+
+namespace tag {
+
+struct PhysEnergy3D {
+  static constexpr int NV = 6;
+  static constexpr int NA = 5;
+  static constexpr int NQ = 8;  // rho, v1/2, v2/2, v3/2, p/2, phi/2, rho/p, (pad)
+
+  struct Params {
+    double gamma, gm1, inv_gm1, c_lmars, omega;
+  };
+
+  static Params make_params(const double* p) {
+    Params q;
+    q.gamma = p[0] / p[1];
+    q.gm1 = q.gamma - 1.0;
+    q.inv_gm1 = 1.0 / (q.gamma - 1.0);
+    q.c_lmars = p[3];
+    q.omega = p[4];
+    return q;
+  }
+
+  TAG_DEV static void node_prims(const Params& P, const double* u, double* q, unsigned& bad) {
+    const double rho = u[0];
+    const double irho = 1.0 / rho;
+    const double v1 = u[1] * irho, v2 = u[2] * irho, v3 = u[3] * irho;
+    const double p = P.gm1 * (u[4] - 0.5 * (u[1] * v1 + u[2] * v2 + u[3] * v3));
+    q[0] = rho;
+    q[1] = 0.5 * v1;
+    q[2] = 0.5 * v2;
+    q[3] = 0.5 * v3;
+    q[4] = 0.5 * p;
+    q[5] = 0.5 * u[5];
+    q[6] = rho / p;
+    q[7] = 0.0;
+    if (!(rho > 0.0)) bad |= TAG_S_NEG_DENSITY;
+    if (!(p > 0.0)) bad |= TAG_S_NEG_PRESSURE;
+  }
+
+  // flux_ranocha (3D, :382-415) + half of flux_nonconservative_waruszewski_etal
+  // (3D, :135-159) for one symmetric pair; see PhysEnergy2D::volume_pair.
+  TAG_DEV static void volume_pair(const Params& P, const double* qa, const double* qb,
+                                  const double* nrm, double* Fa, double* Fb) {
+    double rho_mean, inv_rho_p_mean;
+    ln_mean_pair(qa[0], qb[0], qa[6], qb[6], rho_mean, inv_rho_p_mean);
+    const double n1 = nrm[0], n2 = nrm[1], n3 = nrm[2];
+    const double v1 = qa[1] + qb[1], v2 = qa[2] + qb[2], v3 = qa[3] + qb[3];
+    const double p_avg = qa[4] + qb[4];
+    const double vsq = 2.0 * (qa[1] * qb[1] + qa[2] * qb[2] + qa[3] * qb[3]);
+    const double vn = v1 * n1 + v2 * n2 + v3 * n3;
+    const double f1 = rho_mean * vn;
+    const double f2 = f1 * v1 + p_avg * n1;
+    const double f3 = f1 * v2 + p_avg * n2;
+    const double f4 = f1 * v3 + p_avg * n3;
+    const double c1 = qa[4] * qb[1] + qb[4] * qa[1];
+    const double c2 = qa[4] * qb[2] + qb[4] * qa[2];
+    const double c3 = qa[4] * qb[3] + qb[4] * qa[3];
+    const double f5 = f1 * (vsq + inv_rho_p_mean * P.inv_gm1) + 2.0 * (n1 * c1 + n2 * c2 + n3 * c3);
+    const double h = rho_mean * (qb[5] - qa[5]);
+    const double g2 = n1 * h, g3 = n2 * h, g4 = n3 * h, g5 = h * vn;
+    Fa[0] = f1;      Fb[0] = f1;
+    Fa[1] = f2 + g2; Fb[1] = f2 - g2;
+    Fa[2] = f3 + g3; Fb[2] = f3 - g3;
+    Fa[3] = f4 + g4; Fb[3] = f4 - g4;
+    Fa[4] = f5 + g5; Fb[4] = f5 - g5;
+  }
+
+  // FluxLMARS (3D, :430-466)
+  TAG_DEV static void lmars(const Params& P, const double* ul, const double* ur, const double* n,
+                            double* F) {
+    const double irl = 1.0 / ul[0], irr = 1.0 / ur[0];
+    const double v1l = ul[1] * irl, v2l = ul[2] * irl, v3l = ul[3] * irl;
+    const double v1r = ur[1] * irr, v2r = ur[2] * irr, v3r = ur[3] * irr;
+    const double pl = P.gm1 * (ul[4] - 0.5 * (ul[1] * v1l + ul[2] * v2l + ul[3] * v3l));
+    const double pr = P.gm1 * (ur[4] - 0.5 * (ur[1] * v1r + ur[2] * v2r + ur[3] * v3r));
+    const double vl = v1l * n[0] + v2l * n[1] + v3l * n[2];
+    const double vr = v1r * n[0] + v2r * n[1] + v3r * n[2];
+    const double norm_ = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    const double c = P.c_lmars;
+    const double rho = 0.5 * (ul[0] + ur[0]);
+    const double p = 0.5 * (pl + pr) - 0.5 * c * rho * (vr - vl) / norm_;
+    const double v = 0.5 * (vl + vr) - 1.0 / (2.0 * c * rho) * (pr - pl) * norm_;
+    const double* us = v >= 0.0 ? ul : ur;
+    const double ps = v >= 0.0 ? pl : pr;
+    F[0] = v * us[0];
+    F[1] = v * us[1] + p * n[0];
+    F[2] = v * us[2] + p * n[1];
+    F[3] = v * us[3] + p * n[2];
+    F[4] = v * us[4] + ps * v;
+  }
+
+  TAG_DEV static void surface_flux(const Params& P, const double* ul, const double* ur,
+                                   const double* n, double* F) {
+    lmars(P, ul, ur, n, F);
+  }
+
+  // boundary_condition_slip_wall (3D), :93-116, with the outward normal n.
+  TAG_DEV static void boundary_flux(const Params& P, const double* ui, const double* n, double* F) {
+    const double nn = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    const double e0 = n[0] / nn, e1 = n[1] / nn, e2 = n[2] / nn;
+    const double un = e0 * ui[1] + e1 * ui[2] + e2 * ui[3];
+    const double ub[6] = {ui[0], ui[1] - 2.0 * un * e0, ui[2] - 2.0 * un * e1,
+                          ui[3] - 2.0 * un * e2, ui[4], ui[5]};
+    lmars(P, ui, ub, n, F);
+  }
+
+  // coriolis_source: du2 += 2 Omega rho_v2, du3 -= 2 Omega rho_v1
+  TAG_DEV static double source(const Params& P, const double* u, int v) {
+    if (v == 1) return 2.0 * P.omega * u[2];
+    if (v == 2) return -2.0 * P.omega * u[1];
+    return 0.0;
+  }
+
+  TAG_DEV static void max_speeds(const Params& P, const double* u, double* l) {
+    const double irho = 1.0 / u[0];
+    const double v1 = u[1] * irho, v2 = u[2] * irho, v3 = u[3] * irho;
+    const double p = P.gm1 * (u[4] - 0.5 * (u[1] * v1 + u[2] * v2 + u[3] * v3));
+    const double c = sqrt(P.gamma * p / u[0]);
+    l[0] = fabs(v1) + c;
+    l[1] = fabs(v2) + c;
+    l[2] = fabs(v3) + c;
+  }
+};
+
+}  // namespace tag

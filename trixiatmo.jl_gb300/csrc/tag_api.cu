@@ -10,7 +10,9 @@
 #include <vector>
 
 #include "dg2d_kernels.cuh"
+#include "dg3d_kernels.cuh"
 #include "phys_euler_energy_2d.cuh"
+#include "phys_euler_energy_3d.cuh"
 
 using namespace tag;
 
@@ -38,7 +40,9 @@ void tag::set_last_error(const std::string& msg) { g_last_error = msg; }
 
 struct tag_handle_s {
   int eq = 0, n = 0, nelem = 0, nif = 0, nbd = 0, nv = 0, na = 0;
+  int dim = 2, npe = 0, nface = 4, jpn = 4;  // nodes per element, faces, Ja doubles per node
   PhysEnergy2D::Params p_energy{};
+  PhysEnergy3D::Params p_energy3d{};
   BasisDev basis{};
   cudaStream_t stream = nullptr;
   double *d_u = nullptr, *d_k = nullptr, *d_Ja = nullptr, *d_invJ = nullptr, *d_xy = nullptr,
@@ -75,6 +79,10 @@ const typename Phys::Params& params_of(tag_handle h);
 template <>
 const PhysEnergy2D::Params& params_of<PhysEnergy2D>(tag_handle h) {
   return h->p_energy;
+}
+template <>
+const PhysEnergy3D::Params& params_of<PhysEnergy3D>(tag_handle h) {
+  return h->p_energy3d;
 }
 
 template <class Phys, int n>
@@ -148,6 +156,77 @@ const Ops* ops_for_n(int n) {
     case 6: return OpsImpl<Phys, 6>::get();
     case 7: return OpsImpl<Phys, 7>::get();
     case 8: return OpsImpl<Phys, 8>::get();
+    default: return nullptr;
+  }
+}
+
+template <class Phys, int n>
+struct OpsImpl3D {
+  using S = ElemSmem3D<Phys, n>;
+  static int interface(tag_handle h, const double* u) {
+    const int total = (h->nif + h->nbd) * n * n;
+    if (total == 0) return TAG_OK;
+    k_interface3d<Phys, n><<<(total + 255) / 256, 256, 0, h->stream>>>(
+        params_of<Phys>(h), u, h->d_Ja, h->d_invJ, h->d_if_e, h->d_if_f, h->d_if_flip, h->nif,
+        h->d_bd_e, h->d_bd_f, h->nbd, h->d_sfv);
+    TAG_CUDA(cudaGetLastError());
+    return TAG_OK;
+  }
+  static int element(tag_handle h, int mode, double* u, double* du, int stage, bool last) {
+    const int epb = h->epb > 0 ? h->epb : 1;
+    const int blocks = (h->nelem + epb - 1) / epb;
+    const int threads = std::min(1024, ((epb * S::TPE + 31) / 32) * 32);
+    const size_t smem = S::bytes(epb);
+    const CK2N54 ck = ck2n54();
+    StageArgs st{};
+    st.member = h->d_member;
+    if (mode == kModeStage) {
+      st.A = ck.A[stage];
+      st.B = ck.B[stage];
+      st.dt = h->d_mscal + h->nmembers;
+      st.max_speed = last ? h->d_mscal + 2 * h->nmembers : nullptr;
+      k_element3d<Phys, n, kModeStage><<<blocks, threads, smem, h->stream>>>(
+          params_of<Phys>(h), h->basis, u, du, h->d_k, h->d_Ja, h->d_invJ, h->d_sfv, h->nelem,
+          epb, st, h->d_status);
+    } else {
+      k_element3d<Phys, n, kModeRhs><<<blocks, threads, smem, h->stream>>>(
+          params_of<Phys>(h), h->basis, u, du, h->d_k, h->d_Ja, h->d_invJ, h->d_sfv, h->nelem,
+          epb, st, h->d_status);
+    }
+    TAG_CUDA(cudaGetLastError());
+    return TAG_OK;
+  }
+  static int max_speed(tag_handle h, const double* u) {
+    const int threads = 128;
+    k_max_speed3d<Phys, n><<<(h->nelem + threads - 1) / threads, threads, 0, h->stream>>>(
+        params_of<Phys>(h), u, h->d_Ja, h->d_invJ, h->nelem, h->d_member,
+        h->d_mscal + 2 * h->nmembers);
+    TAG_CUDA(cudaGetLastError());
+    return TAG_OK;
+  }
+  static int init(int max_smem) {
+    TAG_CUDA(cudaFuncSetAttribute(k_element3d<Phys, n, kModeStage>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    TAG_CUDA(cudaFuncSetAttribute(k_element3d<Phys, n, kModeRhs>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    return TAG_OK;
+  }
+  static size_t smem_bytes(int epb) { return S::bytes(epb); }
+  static const Ops* get() {
+    static const Ops ops{&interface, &element, &max_speed, &init, &smem_bytes, S::TPE};
+    return &ops;
+  }
+};
+
+template <class Phys>
+const Ops* ops3d_for_n(int n) {
+  switch (n) {
+    case 3: return OpsImpl3D<Phys, 3>::get();
+    case 4: return OpsImpl3D<Phys, 4>::get();
+    case 5: return OpsImpl3D<Phys, 5>::get();
+    case 6: return OpsImpl3D<Phys, 6>::get();
+    case 7: return OpsImpl3D<Phys, 7>::get();
+    case 8: return OpsImpl3D<Phys, 8>::get();
     default: return nullptr;
   }
 }
@@ -230,7 +309,7 @@ int autotune(tag_handle h, const double* u) {
   TAG_CUDA(cudaGetDevice(&dev));
   int max_smem = 0;
   TAG_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  if (!h->d_tmp_du) TAG_CUDA(cudaMalloc(&h->d_tmp_du, sizeof(double) * h->nelem * h->n * h->n * h->nv));
+  if (!h->d_tmp_du) TAG_CUDA(cudaMalloc(&h->d_tmp_du, sizeof(double) * h->nelem * h->npe * h->nv));
   cudaEvent_t a, b;
   TAG_CUDA(cudaEventCreate(&a));
   TAG_CUDA(cudaEventCreate(&b));
@@ -239,7 +318,7 @@ int autotune(tag_handle h, const double* u) {
   const int cands[] = {1, 2, 3, 4, 6, 8, 12, 16};
   for (int c : cands) {
     if ((size_t)h->ops->smem_bytes(c) > (size_t)max_smem) continue;
-    if (c * h->ops->threads_per_element > 1024) continue;
+    if (c * h->ops->threads_per_element > 1024 && c > 1) continue;
     h->epb = c;
     double* uu = const_cast<double*>(u);
     int rc = h->ops->interface(h, uu);
@@ -288,12 +367,15 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
     return fail(TAG_E_NO_DEVICE, "no CUDA device visible");
-  if (cfg->equations != TAG_EQ_EULER_ENERGY_2D)
+  if (cfg->equations != TAG_EQ_EULER_ENERGY_2D && cfg->equations != TAG_EQ_EULER_ENERGY_3D)
     return fail(TAG_E_INVALID, "unsupported equations id");
+  const int dim = cfg->equations == TAG_EQ_EULER_ENERGY_3D ? 3 : 2;
+  const int nface = 2 * dim;
   if (cfg->volume_flux != TAG_VF_RANOCHA_WARUSZEWSKI || cfg->surface_flux != TAG_SF_LMARS)
     return fail(TAG_E_INVALID, "unsupported flux combination");
   const int n = cfg->polydeg + 1;
   if (n < 2 || n > kMaxNodes) return fail(TAG_E_INVALID, "polydeg out of range 1..7");
+  if (dim == 3 && n < 3) return fail(TAG_E_INVALID, "3D meshes need polydeg >= 2");
   if (cfg->nelements <= 0 || cfg->ninterfaces < 0 || cfg->nboundaries < 0)
     return fail(TAG_E_INVALID, "bad mesh sizes");
   if (!cfg->derivative_split || !cfg->weights || !cfg->contravariant_vectors ||
@@ -302,9 +384,12 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
   for (int k = 0; k < cfg->ninterfaces; ++k) {
     for (int s = 0; s < 2; ++s) {
       const int e = cfg->interface_elements[2 * k + s], f = cfg->interface_faces[2 * k + s];
-      if (e < 0 || e >= cfg->nelements || f < 0 || f > 3)
+      if (e < 0 || e >= cfg->nelements || f < 0 || f >= nface)
         return fail(TAG_E_INVALID, "interface index out of range");
     }
+    const int o = cfg->interface_flip ? cfg->interface_flip[k] : 0;
+    if (o < 0 || o > (dim == 3 ? 7 : 1))
+      return fail(TAG_E_INVALID, "interface orientation out of range");
   }
   if (cfg->nmembers > 1) {
     if (!cfg->element_member) return fail(TAG_E_INVALID, "element_member missing");
@@ -317,10 +402,11 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
         return fail(TAG_E_INVALID, "an interface joins two ensemble members");
   }
   for (int k = 0; k < cfg->nboundaries; ++k) {
-    const int e = cfg->boundary_elements[k], f = cfg->boundary_faces[k],
-              kind = cfg->boundary_kinds[k];
-    if (e < 0 || e >= cfg->nelements || f < 0 || f > 3 ||
-        (kind != TAG_BC_SLIP_WALL_STRUCTURED && kind != TAG_BC_SLIP_WALL_NORMAL))
+    const int e = cfg->boundary_elements[k], f = cfg->boundary_faces[k];
+    const int kind = cfg->boundary_kinds ? cfg->boundary_kinds[k] : TAG_BC_SLIP_WALL_NORMAL;
+    if (e < 0 || e >= cfg->nelements || f < 0 || f >= nface ||
+        (kind != TAG_BC_SLIP_WALL_STRUCTURED && kind != TAG_BC_SLIP_WALL_NORMAL) ||
+        (dim == 3 && kind != TAG_BC_SLIP_WALL_NORMAL))
       return fail(TAG_E_INVALID, "boundary index or kind out of range");
   }
 
@@ -331,10 +417,21 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
   h->nif = cfg->ninterfaces;
   h->nbd = cfg->nboundaries;
   h->nmembers = cfg->nmembers > 1 ? cfg->nmembers : 1;
-  h->nv = PhysEnergy2D::NV;
-  h->na = PhysEnergy2D::NA;
-  h->p_energy = PhysEnergy2D::make_params(cfg->params);
-  h->ops = ops_for_n<PhysEnergy2D>(n);
+  h->dim = dim;
+  h->nface = nface;
+  h->npe = dim == 3 ? n * n * n : n * n;
+  h->jpn = dim * dim;
+  if (dim == 3) {
+    h->nv = PhysEnergy3D::NV;
+    h->na = PhysEnergy3D::NA;
+    h->p_energy3d = PhysEnergy3D::make_params(cfg->params);
+    h->ops = ops3d_for_n<PhysEnergy3D>(n);
+  } else {
+    h->nv = PhysEnergy2D::NV;
+    h->na = PhysEnergy2D::NA;
+    h->p_energy = PhysEnergy2D::make_params(cfg->params);
+    h->ops = ops_for_n<PhysEnergy2D>(n);
+  }
   load_basis(h->basis, cfg->derivative_split, cfg->weights, n);
   auto cleanup = [&](int rc) {
     tag_destroy(h);
@@ -342,22 +439,25 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
   };
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
     return cleanup(fail(TAG_E_CUDA, "stream create failed"));
-  const size_t nodes = (size_t)h->nelem * n * n;
+  const size_t nodes = (size_t)h->nelem * h->npe;
+  const size_t face_nodes = (size_t)h->nelem * nface * (dim == 3 ? n * n : n);
   int rc = TAG_OK;
   if ((rc = upload(&h->d_u, (const double*)nullptr, nodes * h->nv, h->stream))) return cleanup(rc);
   if ((rc = upload(&h->d_k, (const double*)nullptr, nodes * h->na, h->stream))) return cleanup(rc);
-  if ((rc = upload(&h->d_Ja, cfg->contravariant_vectors, nodes * 4, h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_Ja, cfg->contravariant_vectors, nodes * h->jpn, h->stream))) return cleanup(rc);
   if ((rc = upload(&h->d_invJ, cfg->inverse_jacobian, nodes, h->stream))) return cleanup(rc);
   if (cfg->node_coordinates)
-    if ((rc = upload(&h->d_xy, cfg->node_coordinates, nodes * 2, h->stream))) return cleanup(rc);
-  if ((rc = upload(&h->d_sfv, (const double*)nullptr, (size_t)h->nelem * 4 * n * h->na, h->stream)))
+    if ((rc = upload(&h->d_xy, cfg->node_coordinates, nodes * dim, h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_sfv, (const double*)nullptr, face_nodes * h->na, h->stream)))
     return cleanup(rc);
   if ((rc = upload(&h->d_if_e, cfg->interface_elements, (size_t)2 * h->nif, h->stream))) return cleanup(rc);
   if ((rc = upload(&h->d_if_f, cfg->interface_faces, (size_t)2 * h->nif, h->stream))) return cleanup(rc);
   if ((rc = upload(&h->d_if_flip, cfg->interface_flip, (size_t)h->nif, h->stream))) return cleanup(rc);
   if ((rc = upload(&h->d_bd_e, cfg->boundary_elements, (size_t)h->nbd, h->stream))) return cleanup(rc);
   if ((rc = upload(&h->d_bd_f, cfg->boundary_faces, (size_t)h->nbd, h->stream))) return cleanup(rc);
-  if ((rc = upload(&h->d_bd_kind, cfg->boundary_kinds, (size_t)h->nbd, h->stream))) return cleanup(rc);
+  if (cfg->boundary_kinds)
+    if ((rc = upload(&h->d_bd_kind, cfg->boundary_kinds, (size_t)h->nbd, h->stream)))
+      return cleanup(rc);
   if (cfg->nmembers > 1)
     if ((rc = upload(&h->d_member, cfg->element_member, (size_t)h->nelem, h->stream)))
       return cleanup(rc);
@@ -400,7 +500,7 @@ int tag_destroy(tag_handle h) {
 }
 
 int64_t tag_ndofs_total(tag_handle h) {
-  return h ? (int64_t)h->nelem * h->n * h->n * h->nv : -1;
+  return h ? (int64_t)h->nelem * h->npe * h->nv : -1;
 }
 
 int tag_rhs(tag_handle h, const double* u, double* du, double t, int32_t on_device) {
@@ -431,7 +531,7 @@ int tag_set_state(tag_handle h, const double* u_host) {
   if (!h || !u_host) return fail(TAG_E_INVALID, "null argument");
   TAG_CUDA(cudaMemcpyAsync(h->d_u, u_host, sizeof(double) * (size_t)tag_ndofs_total(h),
                            cudaMemcpyHostToDevice, h->stream));
-  TAG_CUDA(cudaMemsetAsync(h->d_k, 0, sizeof(double) * (size_t)h->nelem * h->n * h->n * h->na,
+  TAG_CUDA(cudaMemsetAsync(h->d_k, 0, sizeof(double) * (size_t)h->nelem * h->npe * h->na,
                            h->stream));
   TAG_CUDA(cudaStreamSynchronize(h->stream));
   h->speed_valid = false;
@@ -563,7 +663,8 @@ int tag_set_elements_per_block(tag_handle h, int32_t epb) {
     int dev, max_smem = 0;
     TAG_CUDA(cudaGetDevice(&dev));
     TAG_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    if (h->ops->smem_bytes(epb) > (size_t)max_smem || epb * h->ops->threads_per_element > 1024)
+    if (h->ops->smem_bytes(epb) > (size_t)max_smem ||
+        (epb > 1 && epb * h->ops->threads_per_element > 1024))
       return fail(TAG_E_INVALID, "elements per block too large for one CTA");
   }
   h->epb = epb;

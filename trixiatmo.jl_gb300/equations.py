@@ -47,6 +47,37 @@ class CompressibleEulerEnergyEquationsWithGravity2D:
         return rho, v1, v2, p, u[..., 4]
 
 
+class CompressibleEulerEnergyEquationsWithGravity3D:
+    """State (rho, rho_v1, rho_v2, rho_v3, rho_e, phi)
+    (src/equations/compressible_euler_energy_with_gravity_3d.jl:45-65)."""
+
+    nvariables = 6
+    ndims = 3
+    eq_id = _lib.TAG_EQ_EULER_ENERGY_3D
+
+    def __init__(self, *, c_p, c_v, gravity):
+        self.c_p = float(c_p)
+        self.c_v = float(c_v)
+        self.g = float(gravity)
+        self.R = self.c_p - self.c_v
+        self.gamma = self.c_p / self.c_v
+        self.inv_gamma_minus_one = 1.0 / (self.gamma - 1.0)
+        self.p_0 = 100000.0
+
+    def prim2cons(self, rho, v1, v2, v3, p, phi):
+        one = np.ones_like(p)
+        return np.stack([rho * one, rho * v1 * one, rho * v2 * one, rho * v3 * one,
+                         p * self.inv_gamma_minus_one + 0.5 * rho * (v1 * v1 + v2 * v2 + v3 * v3),
+                         phi * one], axis=-1)
+
+    def cons2prim(self, u):
+        rho = u[..., 0]
+        v1, v2, v3 = u[..., 1] / rho, u[..., 2] / rho, u[..., 3] / rho
+        p = (self.gamma - 1.0) * (u[..., 4] - 0.5 * (u[..., 1] * v1 + u[..., 2] * v2 +
+                                                     u[..., 3] * v3))
+        return rho, v1, v2, v3, p, u[..., 5]
+
+
 class _NamedFlux:
     def __init__(self, name):
         self.name = name

@@ -63,3 +63,124 @@ def seeded_perturbation(u, equations, seed, amplitude=1e-2, velocity=5.0):
     _, _, _, p, phi = equations.cons2prim(u)
     p = p * (1.0 + amplitude * rng.uniform(-1, 1, u.shape[:-1]))
     return equations.prim2cons(rho, v1, v2, p, phi)
+
+
+# ---- 3D spherical-shell states ------------------------------------------------
+EARTH_RADIUS = 6.37122e6                  # src/equations/reference_data.jl:11
+EARTH_GRAVITATIONAL_ACCELERATION = 9.80616  # :19
+EARTH_ROTATION_RATE = 7.292e-5            # :27
+SECONDS_PER_DAY = 8.64e4                  # :35
+
+
+def cartesian_to_sphere(x):
+    """(lon in [0, 2pi), lat, r) of Cartesian points (src/auxiliary/auxiliary.jl:25-34)."""
+    r = np.linalg.norm(x, axis=-1)
+    lam = np.arctan2(x[..., 1], x[..., 0])
+    lam = np.where(lam < 0, lam + 2 * np.pi, lam)
+    return lam, np.arcsin(x[..., 2] / r), r
+
+
+def _baroclinic_basic_state(lon, lat, z):
+    """Balanced zonal state (rho, u, p) of Ullrich et al. (2013), as in
+    src/equations/initial_condition_compressible_euler_3d.jl:4-66."""
+    a = EARTH_RADIUS
+    b = 2.0
+    g = EARTH_GRAVITATIONAL_ACCELERATION
+    k = 3.0
+    p0 = 1.0e5
+    Rg = 287.0
+    TE, TP = 310.0, 240.0
+    lapse = 0.005
+    omega = EARTH_ROTATION_RATE
+    r = z + a
+    T0 = 0.5 * (TE + TP)
+    A = 1.0 / lapse
+    B = (T0 - TP) / (T0 * TP)
+    C = 0.5 * (k + 2) * (TE - TP) / (TE * TP)
+    H = Rg * T0 / g
+    sz = z / (b * H)
+    t1 = np.exp(lapse / T0 * z)
+    t2 = np.exp(-sz ** 2)
+    tau1 = A * lapse / T0 * t1 + B * (1 - 2 * sz ** 2) * t2
+    tau2 = C * (1 - 2 * sz ** 2) * t2
+    inttau1 = A * (t1 - 1) + B * z * t2
+    inttau2 = C * z * t2
+    t3 = r / a * np.cos(lat)
+    t4 = t3 ** k - k / (k + 2) * t3 ** (k + 2)
+    T = 1.0 / ((r / a) ** 2 * (tau1 - tau2 * t4))
+    big_u = g / a * k * T * inttau2 * (t3 ** (k - 1) - t3 ** (k + 1))
+    t5 = a * np.cos(lat)
+    u = -omega * t5 + np.sqrt(omega ** 2 * t5 ** 2 + t5 * big_u)
+    p = p0 * np.exp(-g / Rg * (inttau1 - inttau2 * t4))
+    rho = p / (Rg * T)
+    return rho, u, p
+
+
+def _baroclinic_perturbation(lon, lat, z):
+    """Stream-function perturbation (u', v'), :68-108."""
+    d0 = 1.0 / 6.0
+    vp = 1.0
+    plon, plat = np.pi / 9, 2 * np.pi / 9
+    pertz = 15000.0
+    gc = np.arccos(np.clip(np.sin(plat) * np.sin(lat) +
+                           np.cos(plat) * np.cos(lat) * np.cos(lon - plon), -1, 1))
+    active = (z <= pertz) & (gc <= d0)
+    taper = 1 - 3 * z ** 2 / pertz ** 2 + 2 * z ** 3 / pertz ** 3
+    s = np.sin(0.5 * np.pi * gc / d0)
+    c = np.cos(0.5 * np.pi * gc / d0)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        factor = 16 / (3 * np.sqrt(3)) * vp * taper * c ** 3 * s
+        up = -factor * (-np.sin(plat) * np.cos(lat) +
+                        np.cos(plat) * np.sin(lat) * np.cos(lon - plon)) / np.sin(gc)
+        vpp = factor * np.cos(plat) * np.sin(lon - plon) / np.sin(gc)
+    return np.where(active, up, 0.0), np.where(active, vpp, 0.0)
+
+
+def initial_condition_baroclinic_instability(x, t, equations):
+    """:110-160 — balanced zonal flow plus a localized stream-function bump;
+    phi = -a^2 g / |x|."""
+    lon, lat, r = cartesian_to_sphere(x)
+    z = np.maximum(r - EARTH_RADIUS, 0.0)
+    rho, u, p = _baroclinic_basic_state(lon, lat, z)
+    up, vp = _baroclinic_perturbation(lon, lat, z)
+    u = u + up
+    v = vp
+    v1 = -np.sin(lon) * u - np.sin(lat) * np.cos(lon) * v
+    v2 = np.cos(lon) * u - np.sin(lat) * np.sin(lon) * v
+    v3 = np.cos(lat) * v
+    phi = -EARTH_RADIUS ** 2 * EARTH_GRAVITATIONAL_ACCELERATION / r
+    return equations.prim2cons(rho, v1, v2, v3, p, phi)
+
+
+class IsothermalShell:
+    """Isothermal atmosphere at rest in hydrostatic balance on the shell (the
+    pattern of initial_condition_isothermal, :171-196, with temperature T),
+    phi = g (a - a^2 / r), plus seeded Gaussian density perturbations of
+    relative amplitude `amplitude` and horizontal width `width` centred at
+    `ncenters` points drawn uniformly on the sphere (Philox stream `seed`)."""
+
+    def __init__(self, T=250.0, amplitude=1e-3, width=500e3, ncenters=16, seed=1,
+                 radius=EARTH_RADIUS, gravity=EARTH_GRAVITATIONAL_ACCELERATION):
+        self.T, self.amplitude, self.width = T, amplitude, width
+        self.radius, self.g = radius, gravity
+        rng = np.random.Generator(np.random.Philox(seed))
+        zc = rng.uniform(-1, 1, ncenters)
+        lc = rng.uniform(0, 2 * np.pi, ncenters)
+        s = np.sqrt(1 - zc ** 2)
+        self.centers = np.stack([s * np.cos(lc), s * np.sin(lc), zc], axis=-1)
+
+    def __call__(self, x, t, equations):
+        a, g = self.radius, self.g
+        r = np.linalg.norm(x, axis=-1)
+        rr = np.maximum(r - a, 0.0) + a
+        p = equations.p_0 * np.exp(g * (a * a / rr - a) / (equations.R * self.T))
+        rho = p / (equations.R * self.T)
+        unit = x / r[..., None]
+        bump = np.zeros_like(r)
+        for c in self.centers:
+            ang = np.arccos(np.clip(unit @ c, -1.0, 1.0))
+            bump += np.exp(-(a * ang / self.width) ** 2)
+        rho = rho * (1.0 + self.amplitude * bump)
+        phi = g * (a - a * a / rr)
+        z = np.zeros_like(r)
+        return equations.prim2cons(rho, z, z, z, p, phi)

@@ -25,9 +25,11 @@ import numpy as np
 
 from . import _lib
 from .basis import LobattoLegendreBasis
-from .equations import (CompressibleEulerEnergyEquationsWithGravity2D, FluxLMARS,
+from .equations import (CompressibleEulerEnergyEquationsWithGravity2D,
+                        CompressibleEulerEnergyEquationsWithGravity3D, FluxLMARS,
                         boundary_condition_slip_wall, flux_nonconservative_waruszewski_etal,
                         flux_ranocha, flux_zero)
+from .initial_conditions import EARTH_ROTATION_RATE
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)
@@ -45,9 +47,35 @@ class DGSEM:
         self.volume_integral = volume_integral
 
 
-def _flux_ids(equations, solver):
+class _SourceTerms:
+    def __init__(self, name):
+        self.name = name
+
+    def __repr__(self):
+        return self.name
+
+
+# `source_terms_coriolis` (src/equations/initial_condition_compressible_euler_3d.jl:257-269):
+# -2 Omega x rho v with Omega = EARTH_ROTATION_RATE about the z axis.
+source_terms_coriolis = _SourceTerms("source_terms_coriolis")
+
+
+def _flux_ids(equations, solver, source_terms=None):
     vf = solver.volume_integral.volume_flux
     sf = solver.surface_flux
+    if isinstance(equations, CompressibleEulerEnergyEquationsWithGravity3D):
+        if not (isinstance(vf, tuple) and vf[0] is flux_ranocha
+                and vf[1] is flux_nonconservative_waruszewski_etal):
+            raise ValueError("volume flux must be (flux_ranocha, flux_nonconservative_waruszewski_etal)")
+        if not (isinstance(sf, tuple) and isinstance(sf[0], FluxLMARS) and sf[1] is flux_zero):
+            raise ValueError("surface flux must be (FluxLMARS(c), flux_zero)")
+        if source_terms not in (None, source_terms_coriolis):
+            raise ValueError(f"unsupported source terms {source_terms}")
+        omega = EARTH_ROTATION_RATE if source_terms is source_terms_coriolis else 0.0
+        return _lib.TAG_VF_RANOCHA_WARUSZEWSKI, _lib.TAG_SF_LMARS, [
+            equations.c_p, equations.c_v, equations.g, sf[0].speed_of_sound, omega]
+    if source_terms is not None:
+        raise ValueError("source terms are not supported for this equation set")
     if isinstance(equations, CompressibleEulerEnergyEquationsWithGravity2D):
         if not (isinstance(vf, tuple) and vf[0] is flux_ranocha
                 and vf[1] is flux_nonconservative_waruszewski_etal):
@@ -59,13 +87,16 @@ def _flux_ids(equations, solver):
     raise ValueError(f"unsupported equations {type(equations).__name__}")
 
 
-def _bc_kinds(names, boundary_conditions):
+def _bc_kinds(names, boundary_conditions, ndims):
     kinds = []
     bcs = boundary_conditions or {}
     for name in names:
         bc = bcs.get(name)
         if bc is boundary_condition_slip_wall:
-            kinds.append(_lib.TAG_BC_SLIP_WALL_STRUCTURED)
+            # StructuredMesh (2D) reaches the reference's orientation-argument
+            # method; P4estMesh (the 3D shell) the normal-vector method
+            kinds.append(_lib.TAG_BC_SLIP_WALL_STRUCTURED if ndims == 2
+                         else _lib.TAG_BC_SLIP_WALL_NORMAL)
         else:
             raise ValueError(f"no supported boundary condition for {name}: {bc}")
     return kinds
@@ -74,10 +105,13 @@ def _bc_kinds(names, boundary_conditions):
 class _Handle:
     """Owns one tag_handle built from one or more member meshes."""
 
-    def __init__(self, meshes, equations, solver, boundary_conditions):
+    def __init__(self, meshes, equations, solver, boundary_conditions, source_terms=None):
         basis = solver.basis
         self.n = basis.n
         self.equations = equations
+        self.ndims = meshes[0].ndims
+        if any(m.ndims != self.ndims for m in meshes) or equations.ndims != self.ndims:
+            raise ValueError("mesh and equations dimensions differ")
         coords, Ja, invJ = [], [], []
         ie, ifc, fl, be, bf, bk, member = [], [], [], [], [], [], []
         cache = {}
@@ -85,13 +119,16 @@ class _Handle:
         for m, mesh in enumerate(meshes):
             key = id(mesh)
             if key not in cache:
-                cache[key] = (mesh.geometry(basis), mesh.connectivity())
+                geom = mesh.geometry(basis)
+                conn = mesh.connectivity(basis) if self.ndims == 3 else mesh.connectivity()
+                cache[key] = (geom, conn)
             (xy, ja, ij), conn = cache[key]
             a_ie, a_ifc, a_fl, a_be, a_bf = conn.arrays()
             coords.append(xy); Ja.append(ja); invJ.append(ij)
             ie.append(a_ie + offset); ifc.append(a_ifc); fl.append(a_fl)
             be.append(a_be + offset); bf.append(a_bf)
-            bk.append(np.asarray(_bc_kinds(conn.bd_names, boundary_conditions), dtype=np.int32))
+            bk.append(np.asarray(_bc_kinds(conn.bd_names, boundary_conditions, self.ndims),
+                                 dtype=np.int32))
             member.append(np.full(mesh.nelements, m, dtype=np.int32))
             offset += mesh.nelements
         self.nelements = offset
@@ -107,7 +144,8 @@ class _Handle:
         bf = np.ascontiguousarray(np.concatenate(bf), dtype=np.int32)
         bk = np.ascontiguousarray(np.concatenate(bk), dtype=np.int32)
         member = np.ascontiguousarray(np.concatenate(member), dtype=np.int32)
-        vf_id, sf_id, params = _flux_ids(equations, solver)
+        self.connectivity_arrays = (ie, ifc, fl, be, bf, bk)
+        vf_id, sf_id, params = _flux_ids(equations, solver, source_terms)
         L = _lib.load()
         cfg = _lib.TagConfig()
         cfg.equations = equations.eq_id
@@ -147,13 +185,12 @@ class _Handle:
 class SemidiscretizationHyperbolic:
     def __init__(self, mesh, equations, initial_condition, solver, *, boundary_conditions=None,
                  source_terms=None):
-        if source_terms is not None:
-            raise ValueError("source terms are not supported for this equation set")
         self.mesh = mesh
         self.equations = equations
         self.solver = solver
         self.initial_condition = initial_condition
-        self._H = _Handle([mesh], equations, solver, boundary_conditions)
+        self.source_terms = source_terms
+        self._H = _Handle([mesh], equations, solver, boundary_conditions, source_terms)
         self.n = self._H.n
         self.nelements = self._H.nelements
         self.nmembers = 1
@@ -177,13 +214,17 @@ class SemidiscretizationHyperbolic:
         return self._h
 
     @property
+    def ndims(self):
+        return self._H.ndims
+
+    @property
     def shape(self):
-        return (self.nelements, self.n, self.n, self.equations.nvariables)
+        return (self.nelements,) + (self.n,) * self.ndims + (self.equations.nvariables,)
 
     @property
     def ndofs(self):
-        """Trixi's DOF count: nodes = nelements * n^2."""
-        return self.nelements * self.n * self.n
+        """Trixi's DOF count: nodes = nelements * n^ndims."""
+        return self.nelements * self.n ** self.ndims
 
     # ---- initial data ------------------------------------------------------
     def compute_coefficients(self, t=0.0, initial_condition=None):
