@@ -171,6 +171,44 @@ __global__ void k_element3d(typename Phys::Params Pp, const BasisDev basis, doub
   }
   __syncthreads();
 
+  // per element: can a node pair leave the series range of the logarithmic
+  // means?  If so, the per-node logarithms are computed (once per node)
+  if (Phys::kNodeLogs) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = (nthr + 31) >> 5;
+    for (int el = warp; el < ne; el += nwarps) {
+      const double* eb = base + el * S::per_elem;
+      double r0 = 1e300, r1 = 0.0, b0 = 1e300, b1 = 0.0;
+      for (int node = lane; node < nnn; node += 32) {
+        const double* q = eb + S::oQ + node * NQ;
+        r0 = fmin(r0, q[Phys::kRho]); r1 = fmax(r1, q[Phys::kRho]);
+        b0 = fmin(b0, q[Phys::kBeta]); b1 = fmax(b1, q[Phys::kBeta]);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        r0 = fmin(r0, __shfl_xor_sync(0xffffffffu, r0, o));
+        r1 = fmax(r1, __shfl_xor_sync(0xffffffffu, r1, o));
+        b0 = fmin(b0, __shfl_xor_sync(0xffffffffu, b0, o));
+        b1 = fmax(b1, __shfl_xor_sync(0xffffffffu, b1, o));
+      }
+      if (lane == 0)
+        base[el * S::per_elem + S::oL] = (needs_logs(r0, r1) || needs_logs(b0, b1)) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+  }
+  if (Phys::kNodeLogs) for (int t = threadIdx.x; t < ne * nnn; t += nthr) {
+    const int el = t / nnn, node = t % nnn;
+    double* eb = base + el * S::per_elem;
+    double* q = eb + S::oQ + node * NQ;
+    if (eb[S::oL] != 0.0) {
+      q[Phys::kLogRho] = log(q[Phys::kRho]);
+      q[Phys::kLogBeta] = log(q[Phys::kBeta]);
+    } else {
+      q[Phys::kLogRho] = 0.0;
+      q[Phys::kLogBeta] = 0.0;
+    }
+  }
+  if (Phys::kNodeLogs) __syncthreads();
+
   // volume integral: R rounds, one symmetric pair per thread and round
   for (int r = 0; r < S::R; ++r) {
     for (int t = threadIdx.x; t < ne * S::P; t += nthr) {

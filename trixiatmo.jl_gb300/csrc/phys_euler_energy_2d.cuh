@@ -10,7 +10,11 @@ namespace tag {
 struct PhysEnergy2D {
   static constexpr int NV = 5;  // stored variables per node
   static constexpr int NA = 4;  // variables with nonzero du
-  static constexpr int NQ = 6;  // per-node quantities kept in shared memory
+  // per-node quantities kept in shared memory (odd stride: no bank conflicts):
+  // rho, v1/2, v2/2, p/2, phi/2, beta = rho/p, log rho, log beta, (pad)
+  static constexpr int NQ = 9;
+  static constexpr int kRho = 0, kBeta = 5, kLogRho = 6, kLogBeta = 7;
+  static constexpr bool kNodeLogs = false;  // 2D elements rarely leave the series range
 
   struct Params {
     double gamma, gm1, inv_gm1, c_lmars, inv_2c;
@@ -40,6 +44,7 @@ struct PhysEnergy2D {
     q[3] = 0.5 * p;
     q[4] = 0.5 * u[4];
     q[5] = rho / p;
+    q[8] = 0.0;
     if (!(rho > 0.0)) bad |= TAG_S_NEG_DENSITY;
     if (!(p > 0.0)) bad |= TAG_S_NEG_PRESSURE;
   }
@@ -54,7 +59,8 @@ struct PhysEnergy2D {
   TAG_DEV static void volume_pair(const Params& P, const double* qa, const double* qb,
                                   double n1, double n2, double* Fa, double* Fb) {
     double rho_mean, inv_rho_p_mean;
-    ln_mean_pair(qa[0], qb[0], qa[5], qb[5], rho_mean, inv_rho_p_mean);
+    ln_mean_pair<kNodeLogs>(qa[0], qb[0], qa[5], qb[5], qa[6], qb[6], qa[7], qb[7], rho_mean,
+                            inv_rho_p_mean);
     const double v1_avg = qa[1] + qb[1];
     const double v2_avg = qa[2] + qb[2];
     const double p_avg = qa[3] + qb[3];

@@ -11,7 +11,12 @@ namespace tag {
 struct PhysEnergy3D {
   static constexpr int NV = 6;
   static constexpr int NA = 5;
-  static constexpr int NQ = 8;  // rho, v1/2, v2/2, v3/2, p/2, phi/2, rho/p, (pad)
+  // rho, v1/2, v2/2, v3/2, p/2, phi/2, beta = rho/p, log rho, log beta (odd stride)
+  static constexpr int NQ = 9;
+  static constexpr int kRho = 0, kBeta = 6, kLogRho = 7, kLogBeta = 8;
+  // tall shell elements (km-sized vertical node spacing) put many vertical
+  // pairs out of the series range: logarithms once per node
+  static constexpr bool kNodeLogs = true;
 
   struct Params {
     double gamma, gm1, inv_gm1, c_lmars, omega;
@@ -39,7 +44,6 @@ struct PhysEnergy3D {
     q[4] = 0.5 * p;
     q[5] = 0.5 * u[5];
     q[6] = rho / p;
-    q[7] = 0.0;
     if (!(rho > 0.0)) bad |= TAG_S_NEG_DENSITY;
     if (!(p > 0.0)) bad |= TAG_S_NEG_PRESSURE;
   }
@@ -49,7 +53,8 @@ struct PhysEnergy3D {
   TAG_DEV static void volume_pair(const Params& P, const double* qa, const double* qb,
                                   const double* nrm, double* Fa, double* Fb) {
     double rho_mean, inv_rho_p_mean;
-    ln_mean_pair(qa[0], qb[0], qa[6], qb[6], rho_mean, inv_rho_p_mean);
+    ln_mean_pair<kNodeLogs>(qa[0], qb[0], qa[6], qb[6], qa[7], qb[7], qa[8], qb[8], rho_mean,
+                            inv_rho_p_mean);
     const double n1 = nrm[0], n2 = nrm[1], n3 = nrm[2];
     const double v1 = qa[1] + qb[1], v2 = qa[2] + qb[2], v3 = qa[3] + qb[3];
     const double p_avg = qa[4] + qb[4];

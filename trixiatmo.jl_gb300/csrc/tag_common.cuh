@@ -45,32 +45,85 @@ TAG_DEV double inv_ln_mean(double x, double y) {
 // f2 = 1e-4, (y-x)/log(y/x) above) to rounding.  For f2 >= 0.01 the exact
 // logarithmic form is used.
 //   rho_mean = ln_mean(xa, xb), inv_beta_mean = inv_ln_mean(ya, yb).
-TAG_DEV void ln_mean_pair(double xa, double xb, double ya, double yb, double& rho_mean,
-                          double& inv_beta_mean) {
+// For f2 >= 0.01 the logarithmic form (y - x)/log(y/x) is evaluated with the
+// per-node logarithms Lx = log x, Ly = log y (log(y/x) = Ly - Lx; with
+// |y/x - 1| > 0.2 there the difference is accurate to ~1e-14 relative).  The
+// caller guarantees the logarithms are valid whenever a pair can leave the
+// series range (see kLogMeanRange).
+constexpr double kSeriesF2 = 1.0e-2;
+// An element whose node values x satisfy ((max-min)/(max+min))^2 below this
+// bound never leaves the series range (margin for rounding of f2).
+constexpr double kLogMeanRange = 0.9e-2;
+
+// The rare branch, kept out of line so that the common path is not predicated
+// with its extra reciprocal.
+static __device__ __noinline__ void ln_mean_pair_log(double sx, double dx, double sy, double dy, double R,
+                                              double Q, bool lx, bool ly, double Lxa, double Lxb,
+                                              double Lya, double Lyb, double& rho_mean,
+                                              double& inv_beta_mean) {
+  const double nx = lx ? dx : 0.5 * sx * R;
+  const double ex = lx ? Lxb - Lxa : 1.0;
+  const double ny = ly ? Lyb - Lya : 2.0 * Q;
+  const double ey = ly ? dy : sy;
+  const double r2 = 1.0 / (ex * ey);
+  rho_mean = nx * ey * r2;
+  inv_beta_mean = ny * ex * r2;
+}
+
+// kNodeLogs: true when the caller supplies per-node logarithms (elements
+// whose pairs often leave the series range, e.g. tall 3D elements); false to
+// take the logarithms inside the rare branch (2D elements rarely need them).
+template <bool kNodeLogs>
+TAG_DEV void ln_mean_pair(double xa, double xb, double ya, double yb, double Lxa, double Lxb,
+                          double Lya, double Lyb, double& rho_mean, double& inv_beta_mean) {
   const double sx = xa + xb, dx = xb - xa;
   const double sy = ya + yb, dy = yb - ya;
   const double r = 1.0 / (sx * sy);
   const double isx = sy * r, isy = sx * r;
   const double tx = dx * isx, ty = dy * isy;
   const double f2x = tx * tx, f2y = ty * ty;
-  if (f2x < 1.0e-2 && f2y < 1.0e-2) {
+  if constexpr (kNodeLogs) {
+    // the series are needed by both branches: evaluate them once
     const double R = 1.0 + f2x * (-1.0 / 3.0 + f2x * (-4.0 / 45.0 + f2x * (-44.0 / 945.0 +
                      f2x * (-428.0 / 14175.0 + f2x * (-10196.0 / 467775.0 +
                      f2x * (-10719068.0 / 638512875.0 + f2x * (-25865068.0 / 1915538625.0)))))));
     const double Q = 1.0 + f2y * (1.0 / 3.0 + f2y * (1.0 / 5.0 + f2y * (1.0 / 7.0 +
                      f2y * (1.0 / 9.0 + f2y * (1.0 / 11.0 + f2y * (1.0 / 13.0 + f2y * (1.0 / 15.0)))))));
-    rho_mean = 0.5 * sx * R;
-    inv_beta_mean = 2.0 * isy * Q;
+    if (f2x < kSeriesF2 && f2y < kSeriesF2) {
+      rho_mean = 0.5 * sx * R;
+      inv_beta_mean = 2.0 * isy * Q;
+    } else {
+      // rho_mean = nx / ex, inv_beta_mean = ny / ey, one more reciprocal
+      ln_mean_pair_log(sx, dx, sy, dy, R, Q, f2x >= kSeriesF2, f2y >= kSeriesF2, Lxa, Lxb, Lya,
+                       Lyb, rho_mean, inv_beta_mean);
+    }
   } else {
-    rho_mean = f2x < 1.0e-2 ? 0.5 * sx * (1.0 / (1.0 + f2x * (1.0 / 3.0 + f2x * (1.0 / 5.0 +
-                              f2x * (1.0 / 7.0 + f2x * (1.0 / 9.0 + f2x * (1.0 / 11.0 +
-                              f2x * (1.0 / 13.0 + f2x * (1.0 / 15.0)))))))))
-                            : dx / log(xb / xa);
-    inv_beta_mean = f2y < 1.0e-2 ? 2.0 * isy * (1.0 + f2y * (1.0 / 3.0 + f2y * (1.0 / 5.0 +
-                                   f2y * (1.0 / 7.0 + f2y * (1.0 / 9.0 + f2y * (1.0 / 11.0 +
-                                   f2y * (1.0 / 13.0 + f2y * (1.0 / 15.0))))))))
-                                 : log(yb / ya) / dy;
+    if (f2x < kSeriesF2 && f2y < kSeriesF2) {
+      const double R = 1.0 + f2x * (-1.0 / 3.0 + f2x * (-4.0 / 45.0 + f2x * (-44.0 / 945.0 +
+                       f2x * (-428.0 / 14175.0 + f2x * (-10196.0 / 467775.0 +
+                       f2x * (-10719068.0 / 638512875.0 + f2x * (-25865068.0 / 1915538625.0)))))));
+      const double Q = 1.0 + f2y * (1.0 / 3.0 + f2y * (1.0 / 5.0 + f2y * (1.0 / 7.0 +
+                       f2y * (1.0 / 9.0 + f2y * (1.0 / 11.0 + f2y * (1.0 / 13.0 + f2y * (1.0 / 15.0)))))));
+      rho_mean = 0.5 * sx * R;
+      inv_beta_mean = 2.0 * isy * Q;
+    } else {
+      rho_mean = f2x < kSeriesF2 ? 0.5 * sx * (1.0 / (1.0 + f2x * (1.0 / 3.0 + f2x * (1.0 / 5.0 +
+                                   f2x * (1.0 / 7.0 + f2x * (1.0 / 9.0 + f2x * (1.0 / 11.0 +
+                                   f2x * (1.0 / 13.0 + f2x * (1.0 / 15.0)))))))))
+                                 : dx / log(xb / xa);
+      inv_beta_mean = f2y < kSeriesF2 ? 2.0 * isy * (1.0 + f2y * (1.0 / 3.0 + f2y * (1.0 / 5.0 +
+                                        f2y * (1.0 / 7.0 + f2y * (1.0 / 9.0 + f2y * (1.0 / 11.0 +
+                                        f2y * (1.0 / 13.0 + f2y * (1.0 / 15.0))))))))
+                                      : log(yb / ya) / dy;
+    }
   }
+}
+
+// Whether the values of one element can push a node pair out of the series
+// range of ln_mean_pair.
+TAG_DEV bool needs_logs(double vmin, double vmax) {
+  const double t = (vmax - vmin) / (vmax + vmin);
+  return t * t >= kLogMeanRange;
 }
 
 // Face node (i, j) of face f (0 = xi-, 1 = xi+, 2 = eta-, 3 = eta+) at index l.
