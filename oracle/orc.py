@@ -18,6 +18,11 @@ _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
 _lib = None
 
 _dp = ctypes.POINTER(ctypes.c_double)
+_ip_t = ctypes.POINTER(ctypes.c_int32)
+
+
+def _ip(a):
+    return a.ctypes.data_as(_ip_t)
 
 
 def build(force: bool = False) -> str:
@@ -54,7 +59,7 @@ def lib():
         L.orc_euler2d_ssprk43_run.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double,
                                               ctypes.c_double, ctypes.c_double]
         L.orc_euler2d_errors_gravity_waves.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
-        _ip = ctypes.POINTER(ctypes.c_int32)
+        _ip = _ip_t
         L.orc_euler3d_create.restype = ctypes.c_void_p
         L.orc_euler3d_create.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int,
                                          _ip, _ip, _ip, ctypes.c_int, _ip, _ip] + \
@@ -66,6 +71,28 @@ def lib():
         L.orc_euler3d_ck_steps.restype = ctypes.c_double
         L.orc_euler3d_ck_steps.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_int, ctypes.c_double]
+        L.orc_rainy_create.restype = ctypes.c_void_p
+        L.orc_rainy_create.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] * 4 + [ctypes.c_int] * 4
+        L.orc_rainy_geometry.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_rainy_initial_condition_convergence.argtypes = [ctypes.c_void_p, ctypes.c_double, _dp]
+        L.orc_rainy_errors_convergence.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, _dp, _dp]
+        L.orc_rainy_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_rainy_rhs.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double]
+        L.orc_rainy_max_dt.restype = ctypes.c_double
+        L.orc_rainy_max_dt.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_rainy_newton.restype = ctypes.c_long
+        L.orc_rainy_newton.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double,
+                                       ctypes.c_int, ctypes.c_int, _dp, _ip,
+                                       ctypes.POINTER(ctypes.c_long)]
+        L.orc_rainy_ck_steps.restype = ctypes.c_double
+        L.orc_rainy_ck_steps.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double,
+                                         ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                         ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                         ctypes.c_double]
+        L.orc_rainy_flux_ec.argtypes = [_dp, _dp, _dp, _dp]
+        L.orc_rainy_flux.argtypes = [_dp, _dp, _dp]
+        L.orc_rainy_saturation_vapour_pressure.restype = ctypes.c_double
+        L.orc_rainy_saturation_vapour_pressure.argtypes = [ctypes.c_double]
         _lib = L
     return _lib
 
@@ -142,10 +169,6 @@ class Euler2D:
         return l2, linf
 
 
-def _ip(a):
-    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
-
-
 class Euler3D:
     """Dry Euler (energy + gravity) 3D on a hexahedral mesh; geometry and
     connectivity are the host mirror's arrays (the same ones the C ABI takes)."""
@@ -182,3 +205,76 @@ class Euler3D:
 
     def ck_steps(self, u, k, t, cfl, nsteps, fixed_dt=0.0):
         return lib().orc_euler3d_ck_steps(self.h, _p(u), _p(k), t, cfl, nsteps, fixed_dt)
+
+
+class Rainy2D:
+    """Rainy Euler (flux_ec_rain / flux_lax_friedrichs, source_terms_rainy,
+    simple slip walls) on a StructuredMesh rectangle, with the Newton stage
+    limiter."""
+
+    nv = 9
+
+    def __init__(self, polydeg, nx, ny, x0, x1, y0, y1, periodic_x=True, periodic_y=False,
+                 weak_form=False, source_kind=0):
+        self.n = polydeg + 1
+        self.nelem = nx * ny
+        self.h = lib().orc_rainy_create(polydeg, nx, ny, x0, x1, y0, y1, int(periodic_x),
+                                        int(periodic_y), int(weak_form), int(source_kind))
+
+    def geometry(self):
+        xy = np.zeros((self.nelem, self.n, self.n, 2))
+        lib().orc_rainy_geometry(self.h, _p(xy))
+        return xy
+
+    def initial_condition_convergence(self, t=0.0):
+        u = np.zeros((self.nelem, self.n, self.n, 9))
+        lib().orc_rainy_initial_condition_convergence(self.h, t, _p(u))
+        return u
+
+    def errors_convergence(self, u, t):
+        l2, linf = np.zeros(9), np.zeros(9)
+        lib().orc_rainy_errors_convergence(self.h, _p(np.ascontiguousarray(u)), t, _p(l2), _p(linf))
+        return l2, linf
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_rainy_destroy(self.h)
+            self.h = None
+
+    def rhs(self, u, t=0.0):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        du = np.zeros_like(u)
+        lib().orc_rainy_rhs(self.h, _p(u), _p(du), t)
+        return du
+
+    def max_dt(self, u):
+        return lib().orc_rainy_max_dt(self.h, _p(np.ascontiguousarray(u)))
+
+    def newton(self, u, mode=1, tol=1e-12, maxit=20, polish=0, guesses=None):
+        """In-place Newton limiter; returns (total updates, per-node updates, nfail)."""
+        iters = np.zeros(u.size // 9, dtype=np.int32)
+        nf = ctypes.c_long()
+        g = None if guesses is None else _p(np.ascontiguousarray(guesses, dtype=np.float64))
+        tot = lib().orc_rainy_newton(self.h, _p(u), mode, tol, maxit, polish, g, _ip(iters),
+                                     ctypes.byref(nf))
+        return tot, iters, nf.value
+
+    def ck_steps(self, u, k, t, cfl, nsteps, fixed_dt=0.0, mode=0, tol=1e-9, maxit=20,
+                 t_end=0.0):
+        return lib().orc_rainy_ck_steps(self.h, _p(u), _p(k), t, cfl, nsteps, fixed_dt, mode, tol,
+                                        maxit, t_end)
+
+
+def rainy_flux_ec(ul, ur, n):
+    f = np.zeros(9)
+    lib().orc_rainy_flux_ec(_p(np.ascontiguousarray(ul, dtype=np.float64)),
+                            _p(np.ascontiguousarray(ur, dtype=np.float64)),
+                            _p(np.ascontiguousarray(n, dtype=np.float64)), _p(f))
+    return f
+
+
+def rainy_flux(u, n):
+    f = np.zeros(9)
+    lib().orc_rainy_flux(_p(np.ascontiguousarray(u, dtype=np.float64)),
+                         _p(np.ascontiguousarray(n, dtype=np.float64)), _p(f))
+    return f

@@ -18,6 +18,7 @@
 #include "orc_dg3d.hpp"
 #include "orc_euler_energy_2d.hpp"
 #include "orc_euler_energy_3d.hpp"
+#include "orc_rainy_2d.hpp"
 #include "orc_time.hpp"
 
 namespace orc {
@@ -47,6 +48,14 @@ struct EnergyPhys {
   }
   State source(const State&, const double*, double) const { return State{}; }
   void max_abs_speeds(const State& u, double& l1, double& l2) const { eq.max_abs_speeds(u, l1, l2); }
+  // flux(u, normal_direction), compressible_euler_energy_with_gravity_2d.jl:154-166
+  State flux(const State& u, const double* n) const {
+    double rho, v1, v2, p;
+    eq.cons2prim(u, rho, v1, v2, p);
+    const double vn = v1 * n[0] + v2 * n[1];
+    const double rvn = rho * vn;
+    return {rvn, rvn * v1 + p * n[0], rvn * v2 + p * n[1], (u[3] + p) * vn, 0.0};
+  }
 };
 
 struct Euler2DCase {
@@ -127,6 +136,164 @@ struct Euler3DCase {
   std::unique_ptr<DG3D<EnergyPhys3D>> dg;
   size_t ndofs() const { return (size_t)mesh.nelem * basis.n * basis.n * basis.n; }
 };
+
+struct RainyPhys {
+  using State = RainyEuler2D::State;
+  static constexpr int nv = 9;
+  static constexpr bool has_noncons = false;
+  static constexpr bool has_sources = true;
+  RainyEuler2D eq;
+  State volume_flux(const State& a, const State& b, const double* n) const {
+    return eq.flux_ec_rain(a, b, n);
+  }
+  State volume_noncons(const State&, const State&, const double*) const { return State{}; }
+  State surface_flux(const State& a, const State& b, const double* n) const {
+    return eq.flux_llf(a, b, n);
+  }
+  State surface_noncons(const State&, const State&, const double*) const { return State{}; }
+  State bc_structured(const State& ui, const double* n, int direction) const {
+    return eq.slip_wall_structured(ui, n, direction);
+  }
+  State bc_normal(const State& ui, const double* n) const {
+    return eq.slip_wall_structured(ui, n, 2);
+  }
+  int source_kind = 0;  // 0: source_terms_rainy; 1: convergence-test manufactured source
+  State flux(const State& u, const double* n) const { return eq.flux(u, n); }
+  State source(const State& u, const double* x, double t) const {
+    return source_kind == 0 ? eq.source_rainy(u) : source_convergence(x, t);
+  }
+  void max_abs_speeds(const State& u, double& l1, double& l2) const { eq.max_abs_speeds(u, l1, l2); }
+
+  // source_terms_convergence_test_rainy,
+  // examples/euler/precipitation/tests/convergence_test.jl:42-124
+  State source_convergence(const double* x, double t) const {
+    const RainyEuler2D& q = eq;
+    const double c_help = q.v_0 * 1.9386213994279082 * std::pow(3.14159265358979323846 * q.N_0, -0.125);
+    const double c = 2.0, A = 0.1, L = 2.0, f = 1.0 / L, om = 2.0 * 3.14159265358979323846 * f;
+    const double si = std::sin(om * (x[0] + x[1] - t)), co = std::cos(om * (x[0] + x[1] - t));
+    const double rho = c + A * si;
+    const double rho_x = om * A * co, rho_t = -rho_x;
+    const double T = rho + 250.0;
+    const double svp = q.e_s(T);
+    const double rv = svp / (q.R_v * T);
+    const double rc = rho / q.c_l * 3000.0;
+    const double rr = rho / q.c_l * 1000.0;
+    const double rm = rv + rc;
+    const double rd = rho - rm - rr;
+    const double vr = q.v_rain(rm, rr);
+    const double svp_t = rho_t * q.e_s_T(T);
+    const double svp_x = rho_x * q.e_s_T(T);
+    const double rv_t = (svp_t * T - rho_t * svp) / (q.R_v * T * T);
+    const double rv_x = (svp_x * T - rho_x * svp) / (q.R_v * T * T);
+    const double rc_t = rho_t / q.c_l * 3000.0, rc_x = rho_x / q.c_l * 3000.0;
+    const double rr_t = rho_t / q.c_l * 1000.0, rr_x = rho_x / q.c_l * 1000.0;
+    const double rm_t = rv_t + rc_t, rm_x = rv_x + rc_x;
+    const double rd_t = rho_t - rm_t - rr_t, rd_x = rho_x - rm_x - rr_x;
+    double e_t = (q.c_vd * rd_t + q.c_vv * rv_t + q.c_l * (rc_t + rr_t)) * T;
+    e_t += (q.c_vd * rd + q.c_vv * rv + q.c_l * (rc + rr)) * rho_t;
+    e_t += rv_t * q.ref_L + rho_t;
+    double e_x = (q.c_vd * rd_x + q.c_vv * rv_x + q.c_l * (rc_x + rr_x)) * T;
+    e_x += (q.c_vd * rd + q.c_vv * rv + q.c_l * (rc + rr)) * rho_x;
+    e_x += rv_x * q.ref_L + rho_x;
+    double p_x = (rd_x * q.R_d + rv_x * q.R_v) * T;
+    p_x += (rd * q.R_d + rv * q.R_v) * rho_x;
+    double vr_x = c_help * 0.125 * ((rr_x * rm - rr * rm_x) / ((rm + rr) * (rm + rr)));
+    vr_x *= std::pow(rr / (rm + rr), -0.875);
+    const double rrvr_x = rr_x * vr + rr * vr_x;
+    State s{};
+    s[0] = rd_t + 2.0 * rd_x;
+    s[1] = rm_t + 2.0 * rm_x;
+    s[2] = rr_t + 2.0 * rr_x - rrvr_x;
+    s[3] = rho_x + p_x - rrvr_x;
+    s[4] = rho_x + p_x - rrvr_x;
+    s[5] = e_t + 2.0 * (e_x + p_x) - (q.c_l * rho_x * rr * vr);
+    s[5] -= (q.c_l * T + 1.0) * rrvr_x;
+    return s;
+  }
+};
+
+// initial_condition_convergence_test_rainy, convergence_test.jl:8-40
+inline RainyEuler2D::State ic_rainy_convergence(const RainyEuler2D& q, const double* x, double t) {
+  const double c = 2.0, A = 0.1, L = 2.0, om = 2.0 * 3.14159265358979323846 / L;
+  const double rho = c + A * std::sin(om * (x[0] + x[1] - t));
+  const double T = rho + 250.0;
+  const double rv = q.e_s(T) / (q.R_v * T);
+  const double rc = rho / q.c_l * 3000.0;
+  const double rr = rho / q.c_l * 1000.0;
+  const double rm = rv + rc;
+  const double rd = rho - rm - rr;
+  double e = (q.c_vd * rd + q.c_vv * rv + q.c_l * (rc + rr)) * T;
+  e += rv * q.ref_L + rho;
+  return {rd, rm, rr, rho, rho, e, rv, rc, T};
+}
+
+struct RainyCase {
+  RainyPhys phys;
+  Basis basis;
+  Mesh2D mesh;
+  std::unique_ptr<DG2D<RainyPhys>> dg;
+  size_t ndofs() const { return (size_t)mesh.nelem * basis.n * basis.n; }
+};
+
+// Newton solve of the saturation system on every node, restating
+// src/callbacks_stage/nonlinear_solve_dg2d.jl:6-44 (warm start from slots 7-9,
+// negative rain clamped in the stored state after the node copy is taken,
+// guess -= J \ res).  mode 0: the reference's absolute criterion
+// max|res| < tol; mode 1: relative criterion |res_1| < tol |E_internal|,
+// |res_2|, |res_3| < tol 1e7 rho_moist.  guesses (nodes x 3, may be null)
+// replace the warm start.  After convergence up to `polish` further Newton
+// updates are applied while they change the iterate.  Returns the total
+// number of Newton updates until the criterion held; iters (may be null)
+// receives them per node.
+inline void solve3(const double* J, const double* r, double* dx) {
+  const double a = J[0], b = J[1], c = J[2], d = J[3], e = J[4], f = J[5], g = J[6], h = J[7],
+               i = J[8];
+  const double A = e * i - f * h, B = -(d * i - f * g), C = d * h - e * g;
+  const double det = a * A + b * B + c * C;
+  const double id = 1.0 / det;
+  dx[0] = (A * r[0] + (c * h - b * i) * r[1] + (b * f - c * e) * r[2]) * id;
+  dx[1] = (B * r[0] + (a * i - c * g) * r[1] + (c * d - a * f) * r[2]) * id;
+  dx[2] = (C * r[0] + (b * g - a * h) * r[1] + (a * e - b * d) * r[2]) * id;
+}
+
+inline bool newton_done(const RainyEuler2D& eq, const RainyEuler2D::State& u, const double* r,
+                        int mode, double tol) {
+  if (mode == 0) return std::max(std::fabs(r[0]), std::max(std::fabs(r[1]), std::fabs(r[2]))) < tol;
+  const double rho = u[0] + u[1] + u[2];
+  const double e_int = u[5] - 0.5 * (u[3] * u[3] + u[4] * u[4]) / rho;
+  const double s2 = tol * 1.0e7 * std::fabs(u[1]);
+  return std::fabs(r[0]) < tol * std::fabs(e_int) && std::fabs(r[1]) <= s2 && std::fabs(r[2]) <= s2;
+}
+
+inline int newton_node(const RainyEuler2D& eq, const RainyEuler2D::State& u, double* x, int mode,
+                       double tol, int maxit, int polish, bool* converged) {
+  double r[3], J[9], dx[3];
+  int it = 0;
+  *converged = false;
+  for (; it < maxit; ++it) {
+    eq.residual(u, x, r);
+    if (newton_done(eq, u, r, mode, tol)) {
+      *converged = true;
+      break;
+    }
+    eq.jacobian(u, x, J);
+    solve3(J, r, dx);
+    for (int k = 0; k < 3; ++k) x[k] -= dx[k];
+  }
+  if (!*converged) {
+    eq.residual(u, x, r);
+    *converged = newton_done(eq, u, r, mode, tol);
+  }
+  for (int p = 0; p < polish && *converged; ++p) {
+    eq.residual(u, x, r);
+    eq.jacobian(u, x, J);
+    solve3(J, r, dx);
+    const double y[3] = {x[0] - dx[0], x[1] - dx[1], x[2] - dx[2]};
+    if (y[0] == x[0] && y[1] == x[1] && y[2] == x[2]) break;
+    x[0] = y[0]; x[1] = y[1]; x[2] = y[2];
+  }
+  return it;
+}
 
 }  // namespace orc
 
@@ -357,5 +524,177 @@ double orc_euler3d_ck_steps(void* h, double* u, double* k, double t, double cfl,
   }
   return t;
 }
+
+
+// ---- 2D rainy Euler (flux_ec_rain / flux_lax_friedrichs, source_terms_rainy,
+//      simple slip walls) on a StructuredMesh rectangle
+// weak_form: VolumeIntegralWeakForm (else flux differencing with flux_ec_rain);
+// source_kind: 0 source_terms_rainy, 1 the convergence-test source.
+void* orc_rainy_create(int polydeg, int nx, int ny, double x0, double x1, double y0, double y1,
+                       int periodic_x, int periodic_y, int weak_form, int source_kind) {
+  auto* c = new RainyCase();
+  c->phys.source_kind = source_kind;
+  c->basis = make_lgl_basis(polydeg);
+  c->mesh = structured_rectangle(c->basis, nx, ny, x0, x1, y0, y1, periodic_x != 0,
+                                 periodic_y != 0, 1);
+  c->dg.reset(new DG2D<RainyPhys>(c->phys, c->basis, c->mesh));
+  c->dg->weak_form = weak_form != 0;
+  return c;
+}
+
+void orc_rainy_geometry(void* h, double* xy) {
+  auto* c = static_cast<RainyCase*>(h);
+  std::memcpy(xy, c->mesh.xy.data(), c->mesh.xy.size() * sizeof(double));
+}
+
+void orc_rainy_initial_condition_convergence(void* h, double t, double* u) {
+  auto* c = static_cast<RainyCase*>(h);
+  const size_t nd = c->ndofs();
+  for (size_t q = 0; q < nd; ++q) {
+    const auto s = ic_rainy_convergence(c->phys.eq, &c->mesh.xy[q * 2], t);
+    for (int v = 0; v < 9; ++v) u[q * 9 + v] = s[v];
+  }
+}
+
+// l2 / linf errors against the convergence-test solution at time t (analysis
+// nodes of degree 2N, as in orc_euler2d_errors_gravity_waves).
+void orc_rainy_errors_convergence(void* h, const double* u, double t, double* l2, double* linf) {
+  auto* c = static_cast<RainyCase*>(h);
+  const Basis& b = c->basis;
+  const int n = b.n;
+  const Basis a = make_lgl_basis(2 * (n - 1));
+  const int na = a.n;
+  const std::vector<double> V = interpolation_matrix(b.x, a.x);
+  for (int v = 0; v < 9; ++v) { l2[v] = 0.0; linf[v] = 0.0; }
+  double vol = 0.0;
+  constexpr int K = 12;  // 9 vars + x + y + J
+  std::vector<double> fu(n * n * K), tmp(na * n * K), fa(na * na * K);
+  for (int e = 0; e < c->mesh.nelem; ++e) {
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        const size_t q = (size_t)(e * n + j) * n + i;
+        for (int v = 0; v < 9; ++v) fu[(j * n + i) * K + v] = u[q * 9 + v];
+        fu[(j * n + i) * K + 9] = c->mesh.xy[q * 2];
+        fu[(j * n + i) * K + 10] = c->mesh.xy[q * 2 + 1];
+        fu[(j * n + i) * K + 11] = 1.0 / c->mesh.invJ[q];
+      }
+    for (int j = 0; j < n; ++j)
+      for (int ia = 0; ia < na; ++ia)
+        for (int v = 0; v < K; ++v) {
+          double s = 0;
+          for (int i = 0; i < n; ++i) s += V[ia * n + i] * fu[(j * n + i) * K + v];
+          tmp[(j * na + ia) * K + v] = s;
+        }
+    for (int ja = 0; ja < na; ++ja)
+      for (int ia = 0; ia < na; ++ia)
+        for (int v = 0; v < K; ++v) {
+          double s = 0;
+          for (int j = 0; j < n; ++j) s += V[ja * n + j] * tmp[(j * na + ia) * K + v];
+          fa[(ja * na + ia) * K + v] = s;
+        }
+    for (int ja = 0; ja < na; ++ja)
+      for (int ia = 0; ia < na; ++ia) {
+        const double* f = &fa[(ja * na + ia) * K];
+        const double x[2] = {f[9], f[10]};
+        const auto ex = ic_rainy_convergence(c->phys.eq, x, t);
+        const double wJ = a.w[ia] * a.w[ja] * f[11];
+        for (int v = 0; v < 9; ++v) {
+          const double d = ex[v] - f[v];
+          l2[v] += d * d * wJ;
+          linf[v] = std::max(linf[v], std::fabs(d));
+        }
+        vol += wJ;
+      }
+  }
+  for (int v = 0; v < 9; ++v) l2[v] = std::sqrt(l2[v] / vol);
+}
+
+void orc_rainy_destroy(void* h) { delete static_cast<RainyCase*>(h); }
+
+void orc_rainy_rhs(void* h, const double* u, double* du, double t) {
+  static_cast<RainyCase*>(h)->dg->rhs(u, du, t);
+}
+
+double orc_rainy_max_dt(void* h, const double* u) {
+  return static_cast<RainyCase*>(h)->dg->max_dt(u);
+}
+
+// Newton stage limiter over all nodes (see newton_node); returns the summed
+// Newton updates and the number of nodes that did not converge in *nfail.
+long orc_rainy_newton(void* h, double* u, int mode, double tol, int maxit, int polish,
+                      const double* guesses, int* iters, long* nfail) {
+  auto* c = static_cast<RainyCase*>(h);
+  const long nodes = (long)c->ndofs();
+  long total = 0, bad = 0;
+#pragma omp parallel for reduction(+ : total, bad) schedule(static)
+  for (long q = 0; q < nodes; ++q) {
+    double* un = u + q * 9;
+    RainyEuler2D::State s;
+    for (int v = 0; v < 9; ++v) s[v] = un[v];
+    double x[3] = {un[6], un[7], un[8]};
+    if (guesses) {
+      x[0] = guesses[q * 3];
+      x[1] = guesses[q * 3 + 1];
+      x[2] = guesses[q * 3 + 2];
+    }
+    if (un[2] < 0.0) un[2] = 0.0;
+    bool conv;
+    const int it = newton_node(c->phys.eq, s, x, mode, tol, maxit, polish, &conv);
+    if (iters) iters[q] = it;
+    total += it;
+    if (!conv) ++bad;
+    un[6] = x[0];
+    un[7] = x[1];
+    un[8] = x[2];
+  }
+  if (nfail) *nfail = bad;
+  return total;
+}
+
+// CK2N54 steps with the Newton stage limiter after every stage (the
+// reference's solve(ode, ...; stage_limiter! = NonlinearSolveDG(...))).
+double orc_rainy_ck_steps(void* h, double* u, double* k, double t, double cfl, int nsteps,
+                          double fixed_dt, int mode, double tol, int maxit, double t_end) {
+  auto* c = static_cast<RainyCase*>(h);
+  const size_t N = c->ndofs() * 9;
+  std::vector<double> du(N);
+  for (int s = 0; s < nsteps; ++s) {
+    if (t_end > 0 && t >= t_end) break;
+    double dt = fixed_dt > 0 ? fixed_dt : cfl * c->dg->max_dt(u);
+    if (t_end > 0 && t + dt > t_end) dt = t_end - t;
+    for (int st = 0; st < CK2N54::stages; ++st) {
+      c->dg->rhs(u, du.data(), t + CK2N54::c[st] * dt);
+      const double a = CK2N54::A[st], bb = CK2N54::B[st];
+#pragma omp parallel for schedule(static)
+      for (long q = 0; q < (long)N; ++q) {
+        k[q] = a * k[q] + dt * du[q];
+        u[q] = u[q] + bb * k[q];
+      }
+      long nf;
+      orc_rainy_newton(h, u, mode, tol, maxit, 0, nullptr, nullptr, &nf);
+    }
+    t += dt;
+  }
+  return t;
+}
+
+// Pointwise helpers for tests: flux_ec_rain, flux_llf, residual, Jacobian.
+void orc_rainy_flux_ec(const double* ul, const double* ur, const double* n, double* f) {
+  RainyEuler2D eq;
+  RainyEuler2D::State a, b;
+  for (int v = 0; v < 9; ++v) { a[v] = ul[v]; b[v] = ur[v]; }
+  const auto r = eq.flux_ec_rain(a, b, n);
+  for (int v = 0; v < 9; ++v) f[v] = r[v];
+}
+
+void orc_rainy_flux(const double* u, const double* n, double* f) {
+  RainyEuler2D eq;
+  RainyEuler2D::State a;
+  for (int v = 0; v < 9; ++v) a[v] = u[v];
+  const auto r = eq.flux(a, n);
+  for (int v = 0; v < 9; ++v) f[v] = r[v];
+}
+
+double orc_rainy_saturation_vapour_pressure(double T) { return RainyEuler2D().e_s(T); }
 
 }  // extern "C"

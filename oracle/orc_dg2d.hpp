@@ -141,7 +141,29 @@ struct DG2D {
   }
   double& sf(int e, int f, int l, int v) { return sfv[(((size_t)e * 4 + f) * n + l) * nv + v]; }
 
+  bool weak_form = false;  // VolumeIntegralWeakForm instead of flux differencing
+
+  // weak form (:100-130 pattern): du[ii] += D_hat[ii, i] * f~(u_i)
+  void volume_integral_weak(const double* u, double* du, int e) const {
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        const State ui = get(u, i, j, e);
+        double a1[2], a2[2];
+        ja(0, i, j, e, a1);
+        ja(1, i, j, e, a2);
+        const State f1 = phys.flux(ui, a1), f2 = phys.flux(ui, a2);
+        for (int ii = 0; ii < n; ++ii)
+          for (int v = 0; v < nv; ++v) du[node(ii, j, e) * nv + v] += b.dh(ii, i) * f1[v];
+        for (int jj = 0; jj < n; ++jj)
+          for (int v = 0; v < nv; ++v) du[node(i, jj, e) * nv + v] += b.dh(jj, j) * f2[v];
+      }
+  }
+
   void volume_integral(const double* u, double* du, int e) const {
+    if (weak_form) {
+      volume_integral_weak(u, du, e);
+      return;
+    }
     // symmetric two-point flux, each pair once (:148-181 pattern)
     for (int j = 0; j < n; ++j)
       for (int i = 0; i < n; ++i) {
