@@ -55,12 +55,20 @@ extern "C" {
 /* ---- equation systems, fluxes, boundary kinds --------------------------- */
 #define TAG_EQ_EULER_ENERGY_2D 1 /* CompressibleEulerEnergyEquationsWithGravity2D */
 #define TAG_EQ_EULER_ENERGY_3D 2 /* CompressibleEulerEnergyEquationsWithGravity3D + source_terms_coriolis */
+#define TAG_EQ_RAINY_2D 3        /* CompressibleRainyEulerEquations2D (+ Newton stage limiter) */
 
 #define TAG_VF_RANOCHA_WARUSZEWSKI 1 /* (flux_ranocha, flux_nonconservative_waruszewski_etal) */
+#define TAG_VF_EC_RAIN 2             /* VolumeIntegralFluxDifferencing(flux_ec_rain)    */
+#define TAG_VF_WEAK_FORM 3           /* VolumeIntegralWeakForm (physical flux)          */
 #define TAG_SF_LMARS 1               /* (FluxLMARS(c), flux_zero)                       */
+#define TAG_SF_LAX_FRIEDRICHS 2      /* flux_lax_friedrichs (max_abs_speed_naive)       */
+
+#define TAG_SRC_RAINY 1              /* source_terms_rainy (microphysics + gravity)     */
+#define TAG_SRC_RAINY_CONVERGENCE 2  /* manufactured source of the rainy convergence test */
 
 #define TAG_BC_SLIP_WALL_STRUCTURED 1 /* boundary_condition_slip_wall reached from a StructuredMesh */
 #define TAG_BC_SLIP_WALL_NORMAL 2     /* boundary_condition_slip_wall reached from a P4estMesh      */
+#define TAG_BC_SIMPLE_SLIP_WALL 3     /* boundary_condition_simple_slip_wall (rainy, StructuredMesh) */
 
 typedef struct tag_handle_s* tag_handle;
 
@@ -93,7 +101,8 @@ typedef struct {
                                           CFL reduction.                         */
   double params[8];  /* EULER_ENERGY_2D: c_p, c_v, gravity, LMARS speed of sound;
                         EULER_ENERGY_3D: the same, then the Coriolis angular
-                        velocity (0 disables the source) */
+                        velocity (0 disables the source);
+                        RAINY_2D: params[0] = TAG_SRC_* source kind */
 } tag_config;
 
 /* Creates a handle on the current CUDA device.  Replaces the cache build of
@@ -139,6 +148,50 @@ int tag_max_dt_members(tag_handle h, double* out);
  * interface kernel and of the element kernel (stage mode). The resident state
  * is advanced by the timed stages. */
 int tag_time_kernels(tag_handle h, int32_t reps, double* ms_interface, double* ms_element);
+
+/* ---- rainy Euler: saturation Newton solve (stage limiter) ---------------- */
+/* Settings of the Newton stage limiter that tag_rk_steps applies after every
+ * stage of a TAG_EQ_RAINY_2D handle (reference: NonlinearSolveDG,
+ * src/callbacks_stage/nonlinear_solve_dg.jl:18-44; defaults tolerance 1e-9,
+ * max_iterations 20).  mode 0: the reference's criterion max|residual| < tol;
+ * mode 1: relative, |res_1| < tol |E_internal| and |res_2|, |res_3| <=
+ * tol 1e7 rho_moist.  polish: up to this many extra Newton updates after
+ * convergence while they still change the iterate. */
+int tag_set_newton(tag_handle h, int32_t mode, double tol, int32_t max_iterations,
+                   int32_t polish);
+
+typedef struct {
+  int64_t nodes;            /* nodes solved                                    */
+  int64_t updates;          /* Newton updates until convergence, summed        */
+  int64_t fallbacks;        /* learned guesses that failed within 8 updates    */
+  int64_t not_converged;    /* nodes that never met the tolerance              */
+} tag_newton_stats;
+
+/* One Newton solve of the saturation system on every node of the resident
+ * state (the stage limiter's work once, nonlinear_solve_dg2d.jl:6-44).
+ * use_learned != 0 starts from the MLP guess set by tag_set_mlp and falls back
+ * to the warm start (slots 7-9) when it has not converged after 8 updates.
+ * iters (host, may be null): per-node update counts. */
+int tag_newton_solve(tag_handle h, int32_t use_learned, int32_t* iters, tag_newton_stats* stats);
+
+/* The same solve on n host states u[n][9] (slots 7-9 updated in place); mlp
+ * (host, 1293 floats, may be null) selects the learned initial guess. */
+int tag_newton_solve_states(double* u, int64_t n, int32_t mode, double tol, int32_t max_iterations,
+                            int32_t polish, const float* mlp, int32_t* iters,
+                            tag_newton_stats* stats);
+
+/* Uploads the FP32 MLP parameters (1293 floats: W1[32][5], b1[32], W2[32][32],
+ * b2[32], W3[32], b3, in_mean[5], in_scale[5], out_mean, out_scale). */
+int tag_set_mlp(tag_handle h, const float* params);
+
+/* MLP utilities on the current device (host arrays): forward pass; mean
+ * squared error of the normalised output and its gradient w.r.t. the 1281
+ * trainable parameters; Adam training over shuffled mini-batches. */
+int tag_mlp_forward(const float* params, const float* x, int64_t n, float* y);
+int tag_mlp_loss_grad(const float* params, const float* x, const float* t, int64_t n,
+                      float* grad, float* loss);
+int tag_mlp_train(float* params, const float* x, const float* t, int64_t n, int32_t epochs,
+                  int32_t batch, float lr, uint64_t seed, float* loss_per_epoch);
 
 /* Reads (and clears when clear != 0) the device status word (TAG_S_* bits). */
 int tag_status(tag_handle h, uint32_t* flags, int32_t clear);

@@ -1,0 +1,172 @@
+"""GPU parity of the rainy-Euler path (flux_ec_rain / weak form, flux_lax_friedrichs,
+rain microphysics, simple slip walls, Newton stage limiter) against the CPU
+oracle, the reference's rainy convergence golden reproduced on the GPU, the MLP
+training kernels against the NumPy restatement, and the learned Newton guess.
+All calls go through the C ABI.
+"""
+import numpy as np
+import pytest
+
+from test_oracle_rainy import GOLDEN_L2, GOLDEN_LINF, RTOL as GOLDEN_RTOL
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12
+
+
+def max_norm_rel(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+def make_rainy(tg, nx, ny, polydeg=3, weak=False, convergence=False, x1=20000.0, y1=10000.0,
+               periodic=(True, False)):
+    eq = tg.CompressibleRainyEulerEquations2D()
+    vi = tg.VolumeIntegralWeakForm() if weak else tg.VolumeIntegralFluxDifferencing(tg.flux_ec_rain)
+    solver = tg.DGSEM(polydeg, tg.flux_lax_friedrichs, vi)
+    mesh = tg.StructuredMesh((nx, ny), (0.0, 0.0), (x1, y1), periodicity=periodic)
+    src = tg.source_terms_convergence_test_rainy if convergence else tg.source_terms_rainy
+    ic = tg.initial_condition_convergence_test_rainy if convergence else tg.MoistBubbleRainy()
+    bcs = {"y_neg": tg.boundary_condition_simple_slip_wall,
+           "y_pos": tg.boundary_condition_simple_slip_wall}
+    semi = tg.SemidiscretizationHyperbolic(mesh, eq, ic, solver, source_terms=src,
+                                           boundary_conditions=bcs)
+    return eq, semi
+
+
+def moving(u, seed=1, vel=8.0):
+    rng = np.random.Generator(np.random.Philox(seed))
+    out = u.copy()
+    rho = u[..., 0] + u[..., 1] + u[..., 2]
+    v = vel * rng.uniform(-1, 1, u.shape[:-1] + (2,))
+    out[..., 3] = rho * v[..., 0]
+    out[..., 4] = rho * v[..., 1]
+    out[..., 5] = u[..., 5] + 0.5 * rho * (v ** 2).sum(-1)
+    return out
+
+
+def solved_state(orc, u):
+    """Saturation-consistent slots (the state the limiter leaves behind)."""
+    c = orc.Rainy2D(1, 1, 1, 0.0, 1.0, 0.0, 1.0, True, True)
+    v = np.ascontiguousarray(u.reshape(-1, 9)).copy()
+    c.newton(v, mode=1, tol=1e-13, maxit=50)
+    return v.reshape(u.shape)
+
+
+@pytest.mark.parametrize("polydeg", [2, 3, 4])
+def test_rainy_rhs_matches_oracle(tg, orc, gpu_lib, polydeg):
+    eq, semi = make_rainy(tg, 8, 4, polydeg)
+    u = solved_state(orc, moving(semi.compute_coefficients(), seed=polydeg))
+    du = semi.rhs(u)
+    du_ref = orc.Rainy2D(polydeg, 8, 4, 0.0, 20000.0, 0.0, 10000.0, True, False).rhs(u)
+    assert max_norm_rel(du, du_ref) <= RTOL, max_norm_rel(du, du_ref)
+    # the moisture and rain tendencies on their own scale
+    for v in (1, 2):
+        s = np.abs(du_ref[..., v]).max()
+        assert np.abs(du[..., v] - du_ref[..., v]).max() <= 1e-10 * s
+    semi.close()
+
+
+def test_rainy_weak_form_convergence_source_matches_oracle(tg, orc, gpu_lib):
+    eq, semi = make_rainy(tg, 6, 6, 3, weak=True, convergence=True, x1=2.0, y1=2.0,
+                          periodic=(True, True))
+    u = semi.compute_coefficients()
+    for t in (0.0, 0.37):
+        du = semi.rhs(u, t)
+        du_ref = orc.Rainy2D(3, 6, 6, 0.0, 2.0, 0.0, 2.0, True, True, weak_form=True,
+                             source_kind=1).rhs(u, t)
+        assert max_norm_rel(du, du_ref) <= RTOL, max_norm_rel(du, du_ref)
+    semi.close()
+
+
+def test_rainy_newton_matches_oracle(tg, orc, gpu_lib):
+    eq, semi = make_rainy(tg, 8, 4, 3)
+    u0 = semi.compute_coefficients()
+    semi.set_state(u0)
+    semi.set_newton(mode=1, tol=1e-12, max_iterations=30)
+    st, iters = semi.newton_solve(learned=False)
+    ug = semi.get_state()
+    uo = u0.copy()
+    c = orc.Rainy2D(3, 8, 4, 0.0, 20000.0, 0.0, 10000.0, True, False)
+    tot, it_o, nf = c.newton(uo, mode=1, tol=1e-12, maxit=30)
+    assert st["not_converged"] == 0 and nf == 0
+    for v in (6, 7, 8):
+        assert np.abs(ug[..., v] - uo[..., v]).max() <= 1e-11 * np.abs(uo[..., v]).max()
+    assert np.mean(iters == it_o) > 0.99
+    semi.close()
+
+
+def test_rainy_rk_steps_with_limiter_match_oracle(tg, orc, gpu_lib):
+    eq, semi = make_rainy(tg, 8, 4, 3)
+    u0 = solved_state(orc, moving(semi.compute_coefficients(), seed=7, vel=3.0))
+    semi.set_state(u0)
+    t = semi.rk_steps(3, cfl=0.5, t=0.0)
+    uo = u0.copy()
+    c = orc.Rainy2D(3, 8, 4, 0.0, 20000.0, 0.0, 10000.0, True, False)
+    t_ref = c.ck_steps(uo, np.zeros_like(uo), 0.0, 0.5, 3, 0.0, 0, 1e-9, 20)
+    assert abs(t - t_ref) <= 1e-12 * t_ref
+    assert max_norm_rel(semi.get_state(), uo) <= 1e-12
+    semi.close()
+
+
+def test_gpu_reproduces_rainy_convergence_golden(tg, orc, gpu_lib):
+    """test/test_2d_rainy_euler.jl:7-40 with every stage, limiter and CFL
+    reduction on the GPU (the last step shortened to land on t = 2)."""
+    eq, semi = make_rainy(tg, 6, 6, 3, weak=True, convergence=True, x1=2.0, y1=2.0,
+                          periodic=(True, True))
+    u0 = semi.compute_coefficients()
+    semi.set_state(u0)
+    semi.set_newton(mode=0, tol=1e-8, max_iterations=20)
+    t, t_end = 0.0, 2.0
+    while t < t_end - 1e-15:
+        dt = semi.max_dt()
+        if t + dt >= t_end:
+            t = semi.rk_steps(1, fixed_dt=t_end - t, t=t)
+        else:
+            t = semi.rk_steps(1, cfl=1.0, t=t)
+    assert abs(t - t_end) < 1e-13
+    c = orc.Rainy2D(3, 6, 6, 0.0, 2.0, 0.0, 2.0, True, True, weak_form=True, source_kind=1)
+    l2, linf = c.errors_convergence(semi.get_state(), t_end)
+    for v in range(9):
+        assert abs(l2[v] - GOLDEN_L2[v]) <= GOLDEN_RTOL * GOLDEN_L2[v], (v, l2[v], GOLDEN_L2[v])
+        assert abs(linf[v] - GOLDEN_LINF[v]) <= GOLDEN_RTOL * GOLDEN_LINF[v], (v, linf[v])
+    semi.close()
+
+
+def test_mlp_kernels_match_numpy_restatement(tg, orc, gpu_lib):
+    import mlp_ref
+    lg = tg.learned_guess
+    rng = np.random.default_rng(4)
+    X = rng.normal(size=(3000, 5)).astype(np.float32) * 3 + 1
+    T = (rng.normal(size=3000) * 10 + 280).astype(np.float32)
+    p = lg.set_normalization(lg.init_params(5), X, T)
+    y = lg.forward(p, X)
+    y_ref = mlp_ref.forward(p, X)
+    assert np.abs(y - y_ref).max() <= 1e-4 * np.abs(y_ref).max()
+    loss, g = lg.loss_grad(p, X, T)
+    loss_ref, g_ref = mlp_ref.loss_grad(p, X, T)
+    assert abs(loss - loss_ref) <= 1e-4 * loss_ref
+    assert np.abs(g - g_ref).max() <= 1e-3 * np.abs(g_ref).max()
+
+
+def test_learned_guess_trains_and_reduces_newton_iterations(tg, gpu_lib):
+    lg = tg.learned_guess
+    p, st, losses = lg.train_guess(n=200_000, epochs=8, seed=3)
+    assert st["not_converged"] == 0
+    assert losses[-1] < 0.1 * losses[0]
+    eq, semi = make_rainy(tg, 16, 8, 3)
+    u0 = semi.compute_coefficients()
+    semi.set_mlp(p)
+    semi.set_newton(mode=1, tol=1e-12, max_iterations=30, polish=2)
+    semi.set_state(u0)
+    st_plain, it_plain = semi.newton_solve(learned=False)
+    u_plain = semi.get_state()
+    semi.set_state(u0)
+    st_learn, it_learn = semi.newton_solve(learned=True)
+    u_learn = semi.get_state()
+    assert st_plain["not_converged"] == 0 and st_learn["not_converged"] == 0
+    # same solution (to the tolerance) from either start
+    for v in (6, 7, 8):
+        assert np.abs(u_learn[..., v] - u_plain[..., v]).max() <= 1e-10 * np.abs(u_plain[..., v]).max()
+    # the learned start needs fewer Newton updates than the plain warm start
+    assert it_learn.mean() < it_plain.mean()
+    semi.close()

@@ -7,15 +7,19 @@ The directory name is not a Python identifier; load it with
 ``load_package()`` from ``__graft_entry__`` (or importlib) under the name
 ``trixiatmo_gb300``.
 """
-from . import _lib
+from . import _lib, learned_guess
 from .basis import LobattoLegendreBasis
 from .equations import (CompressibleEulerEnergyEquationsWithGravity2D,
-                        CompressibleEulerEnergyEquationsWithGravity3D, FluxLMARS,
+                        CompressibleEulerEnergyEquationsWithGravity3D,
+                        CompressibleRainyEulerEquations2D, VolumeIntegralWeakForm,
+                        boundary_condition_simple_slip_wall, flux_ec_rain, flux_lax_friedrichs,
+                        source_terms_convergence_test_rainy, source_terms_rainy, FluxLMARS,
                         VolumeIntegralFluxDifferencing, boundary_condition_periodic,
                         boundary_condition_slip_wall, flux_nonconservative_waruszewski_etal,
                         flux_ranocha, flux_zero, speed_of_sound_isothermal)
 from .initial_conditions import (EARTH_GRAVITATIONAL_ACCELERATION, EARTH_RADIUS,
-                                 EARTH_ROTATION_RATE, IsothermalShell, WarmBubble,
+                                 EARTH_ROTATION_RATE, IsothermalShell, MoistBubbleRainy,
+                                 WarmBubble, initial_condition_convergence_test_rainy,
                                  initial_condition_baroclinic_instability,
                                  initial_condition_gravity_waves, seeded_perturbation)
 from .meshes import StructuredMesh
@@ -32,5 +36,8 @@ __all__ = [
     "SemidiscretizationEnsemble", "CompressibleEulerEnergyEquationsWithGravity3D",
     "EARTH_GRAVITATIONAL_ACCELERATION", "EARTH_RADIUS", "EARTH_ROTATION_RATE", "IsothermalShell",
     "initial_condition_baroclinic_instability", "P4estMeshCubedSphereTopography",
-    "source_terms_coriolis", "fp64_peak",
+    "source_terms_coriolis", "fp64_peak", "CompressibleRainyEulerEquations2D",
+    "VolumeIntegralWeakForm", "boundary_condition_simple_slip_wall", "flux_ec_rain",
+    "flux_lax_friedrichs", "source_terms_convergence_test_rainy", "source_terms_rainy",
+    "MoistBubbleRainy", "initial_condition_convergence_test_rainy", "learned_guess",
 ]

@@ -24,6 +24,15 @@ TAG_S_NEWTON_MAXIT = 0x8
 
 TAG_EQ_EULER_ENERGY_2D = 1
 TAG_EQ_EULER_ENERGY_3D = 2
+TAG_EQ_RAINY_2D = 3
+TAG_VF_EC_RAIN = 2
+TAG_VF_WEAK_FORM = 3
+TAG_SF_LAX_FRIEDRICHS = 2
+TAG_SRC_RAINY = 1
+TAG_SRC_RAINY_CONVERGENCE = 2
+TAG_BC_SIMPLE_SLIP_WALL = 3
+MLP_PARAMS = 1293
+MLP_TRAINABLE = 1281
 TAG_VF_RANOCHA_WARUSZEWSKI = 1
 TAG_SF_LMARS = 1
 TAG_BC_SLIP_WALL_STRUCTURED = 1
@@ -59,6 +68,13 @@ class TagConfig(ctypes.Structure):
     ]
 
 
+class NewtonStats(ctypes.Structure):
+    _fields_ = [("nodes", ctypes.c_int64), ("updates", ctypes.c_int64),
+                ("fallbacks", ctypes.c_int64), ("not_converged", ctypes.c_int64)]
+
+
+_fp = ctypes.POINTER(ctypes.c_float)
+
 # exported symbol -> (restype, argtypes)
 SIGNATURES = {
     "tag_create": (ctypes.c_int, [ctypes.POINTER(TagConfig), ctypes.POINTER(ctypes.c_void_p)]),
@@ -80,6 +96,18 @@ SIGNATURES = {
     "tag_get_elements_per_block": (ctypes.c_int, [ctypes.c_void_p, _ip]),
     "tag_fp64_peak": (ctypes.c_int, [_dp]),
     "tag_last_error": (ctypes.c_char_p, []),
+    "tag_set_newton": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double,
+                                      ctypes.c_int32, ctypes.c_int32]),
+    "tag_newton_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _ip,
+                                        ctypes.POINTER(NewtonStats)]),
+    "tag_newton_solve_states": (ctypes.c_int, [_dp, ctypes.c_int64, ctypes.c_int32,
+                                               ctypes.c_double, ctypes.c_int32, ctypes.c_int32,
+                                               _fp, _ip, ctypes.POINTER(NewtonStats)]),
+    "tag_set_mlp": (ctypes.c_int, [ctypes.c_void_p, _fp]),
+    "tag_mlp_forward": (ctypes.c_int, [_fp, _fp, ctypes.c_int64, _fp]),
+    "tag_mlp_loss_grad": (ctypes.c_int, [_fp, _fp, _fp, ctypes.c_int64, _fp, _fp]),
+    "tag_mlp_train": (ctypes.c_int, [_fp, _fp, _fp, ctypes.c_int64, ctypes.c_int32,
+                                     ctypes.c_int32, ctypes.c_float, ctypes.c_uint64, _fp]),
     "tag_rhs_noalloc": (ctypes.c_int, [ctypes.POINTER(TagConfig), _dp, _dp, ctypes.c_void_p,
                                        ctypes.POINTER(ctypes.c_uint32)]),
 }

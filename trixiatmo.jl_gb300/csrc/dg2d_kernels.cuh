@@ -19,7 +19,10 @@ namespace tag {
 struct BasisDev {
   double Ds[kMaxNodes * kMaxNodes];  // Dsplit[a * n + b] (row a, column b)
   double winv0, winvN;               // 1 / w_0, 1 / w_N
+  double Dh[kMaxNodes * kMaxNodes];  // D_hat[a * n + b] (weak form)
 };
+
+enum VolumeKind : int { kVolFluxDiff = 0, kVolWeak = 1 };
 
 enum ElementMode : int { kModeRhs = 0, kModeStage = 1 };
 
@@ -28,6 +31,10 @@ struct StageArgs {
   const double* dt;               // per-member dt (device)
   double* max_speed;              // per-member CFL speed accumulator, or null
   const int* member;              // member of each element, or null (one member)
+  double c_stage;                 // stage time fraction (stage mode)
+  const double* t_member;         // per-member step start time (stage mode)
+  double t_rhs;                   // time of an rhs evaluation (rhs mode)
+  const double* xy;               // node coordinates (sources), or null
 };
 
 // ---------------------------------------------------------------------------
@@ -115,11 +122,12 @@ struct ElemSmem {
   static constexpr int oJa = oQ + nn * NQ;
   static constexpr int oC = oJa + nn * 4;        // slots [2][nn][n][NA]
   static constexpr int oL = oC + 2 * nn * n * NA; // CFL speeds [2][nn]
-  static constexpr int per_elem = oL + 2 * nn;
+  static constexpr int oS = oL + 2 * nn;          // sources [nn][NA]
+  static constexpr int per_elem = oS + (Phys::kHasSources ? nn * NA : 0);
   static size_t bytes(int epb) { return sizeof(double) * (size_t)per_elem * epb + sizeof(BasisDev); }
 };
 
-template <class Phys, int n, int MODE>
+template <class Phys, int n, int MODE, int VOL = kVolFluxDiff>
 __global__ void k_element(typename Phys::Params Pp, const BasisDev basis, double* __restrict__ u,
                           double* __restrict__ du, double* __restrict__ kreg,
                           const double* __restrict__ Ja, const double* __restrict__ invJ,
@@ -161,10 +169,12 @@ __global__ void k_element(typename Phys::Params Pp, const BasisDev basis, double
     double* eb = base + el * S::per_elem;
     Phys::node_prims(Pp, eb + S::oU + node * NV, eb + S::oQ + node * NQ, bad);
     const int i = node % n, j = node / n;
+    if constexpr (VOL == kVolFluxDiff) {
 #pragma unroll
-    for (int v = 0; v < NA; ++v) {
-      eb[S::oC + ((0 * nn + node) * n + i) * NA + v] = 0.0;
-      eb[S::oC + ((1 * nn + node) * n + j) * NA + v] = 0.0;
+      for (int v = 0; v < NA; ++v) {
+        eb[S::oC + ((0 * nn + node) * n + i) * NA + v] = 0.0;
+        eb[S::oC + ((1 * nn + node) * n + j) * NA + v] = 0.0;
+      }
     }
   }
   __syncthreads();
@@ -207,8 +217,22 @@ __global__ void k_element(typename Phys::Params Pp, const BasisDev basis, double
   }
   if (Phys::kNodeLogs) __syncthreads();
 
+  // --- phase 2 (weak form): contravariant fluxes per node,
+  //     F~_d = f(u, Ja^d) into slot 0 of direction d
+  if constexpr (VOL == kVolWeak) {
+    for (int t = threadIdx.x; t < ne * nn * 2; t += nthr) {
+      const int el = t / (nn * 2), r = t % (nn * 2);
+      const int node = r >> 1, d = r & 1;
+      double* eb = base + el * S::per_elem;
+      const double* ja = eb + S::oJa + node * 4 + 2 * d;  // halved
+      double F[NA];
+      Phys::flux(Pp, eb + S::oU + node * NV, 2.0 * ja[0], 2.0 * ja[1], F);
+#pragma unroll
+      for (int v = 0; v < NA; ++v) eb[S::oC + ((d * nn + node) * n + 0) * NA + v] = F[v];
+    }
+  }
   // --- phase 2: one thread per symmetric pair (a < b) on a line
-  for (int t = threadIdx.x; t < ne * S::P; t += nthr) {
+  if constexpr (VOL == kVolFluxDiff) for (int t = threadIdx.x; t < ne * S::P; t += nthr) {
     const int el = t / S::P, p = t % S::P;
     const int d = p / (n * npl), r = p % (n * npl);
     const int line = r / npl;
@@ -233,10 +257,25 @@ __global__ void k_element(typename Phys::Params Pp, const BasisDev basis, double
       cb[v] = Fb[v];
     }
   }
+  // --- phase 2b: sources per node (from the state before the update)
+  if constexpr (Phys::kHasSources) {
+    for (int t = threadIdx.x; t < ne * nn; t += nthr) {
+      const int el = t / nn, node = t % nn;
+      const int e = e_first + el;
+      double* eb = base + el * S::per_elem;
+      double tt = st.t_rhs;
+      if (MODE == kModeStage) {
+        const int m = st.member ? st.member[e] : 0;
+        tt = st.t_member[m] + st.c_stage * st.dt[m];
+      }
+      const double* x = st.xy ? st.xy + ((size_t)e * nn + node) * 2 : nullptr;
+      Phys::source(Pp, eb + S::oU + node * NV, x, tt, eb + S::oS + node * NA);
+    }
+  }
   __syncthreads();
 
   // --- phase 3: per (node, variable): slot sums, surface integral, Jacobian,
-  //     stage update
+  //     sources, stage update
   for (int t = threadIdx.x; t < ne * nn * NA; t += nthr) {
     const int el = t / (nn * NA), r = t % (nn * NA);
     const int node = r / NA, v = r % NA;
@@ -244,19 +283,30 @@ __global__ void k_element(typename Phys::Params Pp, const BasisDev basis, double
     const int e = e_first + el;
     double* eb = base + el * S::per_elem;
     double acc = 0.0;
+    if constexpr (VOL == kVolFluxDiff) {
 #pragma unroll
-    for (int b = 0; b < n; ++b)
-      acc = fma(sb->Ds[i * n + b], eb[S::oC + ((0 * nn + node) * n + b) * NA + v], acc);
+      for (int b = 0; b < n; ++b)
+        acc = fma(sb->Ds[i * n + b], eb[S::oC + ((0 * nn + node) * n + b) * NA + v], acc);
 #pragma unroll
-    for (int b = 0; b < n; ++b)
-      acc = fma(sb->Ds[j * n + b], eb[S::oC + ((1 * nn + node) * n + b) * NA + v], acc);
+      for (int b = 0; b < n; ++b)
+        acc = fma(sb->Ds[j * n + b], eb[S::oC + ((1 * nn + node) * n + b) * NA + v], acc);
+    } else {
+      // weak form: du(i, j) = sum_b D_hat[i, b] F~_1(b, j) + D_hat[j, b] F~_2(i, b)
+#pragma unroll
+      for (int b = 0; b < n; ++b)
+        acc = fma(sb->Dh[i * n + b], eb[S::oC + ((0 * nn + j * n + b) * n + 0) * NA + v], acc);
+#pragma unroll
+      for (int b = 0; b < n; ++b)
+        acc = fma(sb->Dh[j * n + b], eb[S::oC + ((1 * nn + b * n + i) * n + 0) * NA + v], acc);
+    }
     const double* se = sfv + (size_t)e * 4 * n * NA;
     if (i == 0) acc += se[(0 * n + j) * NA + v] * sb->winv0;
     if (i == n - 1) acc += se[(1 * n + j) * NA + v] * sb->winvN;
     if (j == 0) acc += se[(2 * n + i) * NA + v] * sb->winv0;
     if (j == n - 1) acc += se[(3 * n + i) * NA + v] * sb->winvN;
     const size_t gq = (size_t)e * nn + node;
-    const double dv = acc * (-invJ[gq]);
+    double dv = acc * (-invJ[gq]);
+    if constexpr (Phys::kHasSources) dv += eb[S::oS + node * NA + v];
     if (!isfinite(dv)) bad |= TAG_S_NAN;
     if (MODE == kModeRhs) {
       du[gq * NV + v] = dv;

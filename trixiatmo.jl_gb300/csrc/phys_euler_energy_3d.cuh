@@ -17,6 +17,7 @@ struct PhysEnergy3D {
   // tall shell elements (km-sized vertical node spacing) put many vertical
   // pairs out of the series range: logarithms once per node
   static constexpr bool kNodeLogs = true;
+  static constexpr bool kHasSources = true;  // Coriolis, added per (node, variable)
 
   struct Params {
     double gamma, gm1, inv_gm1, c_lmars, omega;

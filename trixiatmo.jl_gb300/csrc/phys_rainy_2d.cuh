@@ -1,0 +1,306 @@
+// Device physics of CompressibleRainyEulerEquations2D
+// (reference: src/equations/compressible_rainy_euler_2d.jl).
+// State u = (rho_dry, rho_moist, rho_rain, rho_v1, rho_v2, energy, rho_vapour,
+// rho_cloud, temperature); slots 7-9 are the saturation-system unknowns (set by
+// the Newton stage limiter).  All 9 slots are evolved: the volume flux of
+// slots 7-9 is zero but the Lax-Friedrichs dissipation acts on them.
+#pragma once
+#include "tag_common.cuh"
+
+namespace tag {
+
+struct RainyConst {
+  // :72-109
+  static constexpr double c_l = 4186.0, c_pd = 1004.0, c_vd = 717.0, c_pv = 1885.0, c_vv = 1424.0;
+  static constexpr double R_d = 287.0, R_v = 461.0;
+  static constexpr double ref_s_p = 610.7, ref_temp = 273.15, ref_L = 2500000.0;
+  static constexpr double g = 9.80616, N_0 = 8000000.0, v_0 = 130.0;
+  static constexpr double pi = 3.14159265358979323846;
+};
+
+// saturation_vapour_pressure (:397-419) and its derivative (:421-446)
+TAG_DEV double rainy_e_s(double T) {
+  using C = RainyConst;
+  const double e = C::ref_s_p * pow(T / C::ref_temp, (C::c_pv - C::c_l) / C::R_v);
+  return e * exp(((C::ref_L - (C::c_pv - C::c_l) * C::ref_temp) / C::R_v) *
+                 (1.0 / C::ref_temp - 1.0 / T));
+}
+
+TAG_DEV double rainy_e_s_T(double T) {
+  using C = RainyConst;
+  const double c1 = (C::c_pv - C::c_l) / C::R_v;
+  const double c2 = (C::ref_L - (C::c_pv - C::c_l) * C::ref_temp) / C::R_v;
+  double d = C::ref_s_p / pow(C::ref_temp, c1);
+  d *= (c1 * pow(T, c1 - 1.0) + c2 * pow(T, c1 - 2.0));
+  d *= exp(c2 * (1.0 / C::ref_temp - 1.0 / T));
+  return d;
+}
+
+// terminal_velocity_rain, :380-395
+TAG_DEV double rainy_v_rain(double rho_moist, double rho_rain) {
+  using C = RainyConst;
+  if (rho_rain > 0.0)
+    return C::v_0 * 1.9386213994279082 * pow(rho_rain / (C::pi * (rho_moist + rho_rain) * C::N_0), 0.125);
+  return 0.0;
+}
+
+// One logarithmic mean (or its inverse) with its own reciprocal: the series of
+// ln_mean_pair in the common range, the reference's (y-x)/log(y/x) outside.
+TAG_DEV double ln_mean_single(double x, double y) {
+  const double s = x + y, d = y - x;
+  const double t = d / s, f2 = t * t;
+  if (f2 < kSeriesF2) {
+    const double R = 1.0 + f2 * (-1.0 / 3.0 + f2 * (-4.0 / 45.0 + f2 * (-44.0 / 945.0 +
+                     f2 * (-428.0 / 14175.0 + f2 * (-10196.0 / 467775.0 +
+                     f2 * (-10719068.0 / 638512875.0 + f2 * (-25865068.0 / 1915538625.0)))))));
+    return 0.5 * s * R;
+  }
+  return d / log(y / x);
+}
+
+TAG_DEV double inv_ln_mean_single(double x, double y) {
+  const double s = x + y, d = y - x;
+  const double t = d / s, f2 = t * t;
+  if (f2 < kSeriesF2) {
+    const double Q = 1.0 + f2 * (1.0 / 3.0 + f2 * (1.0 / 5.0 + f2 * (1.0 / 7.0 +
+                     f2 * (1.0 / 9.0 + f2 * (1.0 / 11.0 + f2 * (1.0 / 13.0 + f2 * (1.0 / 15.0)))))));
+    return 2.0 * Q / s;
+  }
+  return log(y / x) / d;
+}
+
+struct PhysRainy2D {
+  static constexpr int NV = 9;
+  static constexpr int NA = 9;
+  // rho_d, rho_m, rho_r, v1/2, v2/2, rho_vapour, rho_cloud, T, 1/T,
+  // v_rain(rho_vapour + rho_cloud, rho_r), (v1^2 + v2^2)/4
+  static constexpr int NQ = 11;
+  static constexpr int kRho = 0, kBeta = 0, kLogRho = 0, kLogBeta = 0;
+  static constexpr bool kNodeLogs = false;
+  static constexpr bool kHasSources = true;
+
+  struct Params {
+    int source_kind;  // TAG_SRC_RAINY or TAG_SRC_RAINY_CONVERGENCE
+    int pad;
+  };
+
+  static Params make_params(const double* p) {
+    Params q;
+    q.source_kind = (int)p[0];
+    q.pad = 0;
+    return q;
+  }
+
+  // cons2nonlinearsystemsol, :219-260
+  TAG_DEV static void nlsol(const double* u, double& rv, double& rc, double& T) {
+    using C = RainyConst;
+    const double rho = u[0] + u[1] + u[2];
+    if (u[1] == 0.0 && u[2] == 0.0) {
+      const double ri = 1.0 / rho;
+      const double v1 = u[3] * ri, v2 = u[4] * ri;
+      T = (u[5] - 0.5 * (v1 * v1 + v2 * v2) * rho) / (C::c_vd * rho);
+      rv = 0.0;
+      rc = 0.0;
+      return;
+    }
+    rv = u[6];
+    rc = u[7];
+    T = u[8];
+    if (rv < 0.0 && fabs(rv) <= 1e-15) rv = 0.0;
+    if (rc < 0.0 && fabs(rc) <= 1e-15) rc = 0.0;
+  }
+
+  TAG_DEV static void node_prims(const Params&, const double* u, double* q, unsigned& bad) {
+    double rv, rc, T;
+    nlsol(u, rv, rc, T);
+    const double ri = 1.0 / (u[0] + u[1] + u[2]);
+    const double v1 = u[3] * ri, v2 = u[4] * ri;
+    q[0] = u[0];
+    q[1] = u[1];
+    q[2] = u[2];
+    q[3] = 0.5 * v1;
+    q[4] = 0.5 * v2;
+    q[5] = rv;
+    q[6] = rc;
+    q[7] = T;
+    q[8] = 1.0 / T;
+    q[9] = rainy_v_rain(rv + rc, u[2]);
+    q[10] = 0.25 * (v1 * v1 + v2 * v2);
+    if (!(u[0] > 0.0)) bad |= TAG_S_NEG_DENSITY;
+    if (!(T > 0.0)) bad |= TAG_S_NEG_PRESSURE;
+  }
+
+  // flux_ec_rain, :872-961, for one symmetric pair (no nonconservative part)
+  TAG_DEV static void volume_pair(const Params&, const double* a, const double* b, double n1,
+                                  double n2, double* Fa, double* Fb) {
+    using C = RainyConst;
+    const double v1a = a[3] + b[3], v2a = a[4] + b[4];
+    const double K = a[10] + b[10];
+    const double vdn = n1 * v1a + n2 * v2a;
+    const double vrn = 0.5 * n2 * (a[9] + b[9]);
+    const double rd_avg = 0.5 * (a[0] + b[0]);
+    const double rv_avg = 0.5 * (a[5] + b[5]);
+    const double rc_avg = 0.5 * (a[6] + b[6]);
+    const double rr_avg = 0.5 * (a[2] + b[2]);
+    const double rd_log = (a[0] != 0.0 && b[0] != 0.0) ? ln_mean_single(a[0], b[0]) : 0.0;
+    const double rv_log = (a[5] != 0.0 && b[5] != 0.0) ? ln_mean_single(a[5], b[5]) : 0.0;
+    const double iT_avg = 0.5 * (a[8] + b[8]);
+    const double iT_log = inv_ln_mean_single(a[8], b[8]);
+    const double p_int = (C::R_d * rd_avg + C::R_v * rv_avg) / iT_avg;
+    const double f_v = rv_log * vdn;
+    const double f_c = rc_avg * vdn;
+    const double f_d = rd_log * vdn;
+    const double f_r = rr_avg * (vdn - vrn);
+    const double f_m = f_v + f_c;
+    const double f_rho = f_d + f_m + f_r;
+    const double f_m1 = f_rho * v1a + p_int * n1;
+    const double f_m2 = f_rho * v2a + p_int * n2;
+    const double f_e = (C::c_vd * iT_log - K) * f_d + (C::c_vv * iT_log - K + C::ref_L) * f_v +
+                       (C::c_l * iT_log - K) * (f_c + f_r) + (v1a * f_m1 + v2a * f_m2);
+    Fa[0] = Fb[0] = f_d;
+    Fa[1] = Fb[1] = f_m;
+    Fa[2] = Fb[2] = f_r;
+    Fa[3] = Fb[3] = f_m1;
+    Fa[4] = Fb[4] = f_m2;
+    Fa[5] = Fb[5] = f_e;
+    Fa[6] = Fb[6] = 0.0;
+    Fa[7] = Fb[7] = 0.0;
+    Fa[8] = Fb[8] = 0.0;
+  }
+
+  // flux(u, normal_direction), :504-545
+  TAG_DEV static void flux(const Params&, const double* u, double n1, double n2, double* f) {
+    using C = RainyConst;
+    double rv, rc, T;
+    nlsol(u, rv, rc, T);
+    const double rho = u[0] + u[1] + u[2];
+    const double ri = 1.0 / rho;
+    const double v1 = u[3] * ri, v2 = u[4] * ri;
+    const double vr = rainy_v_rain(u[1], u[2]);
+    const double vn = v1 * n1 + v2 * n2;
+    const double vrn = vr * n2;
+    const double p = (C::R_d * u[0] + C::R_v * rv) * T;
+    f[0] = u[0] * vn;
+    f[1] = u[1] * vn;
+    f[2] = u[2] * (vn - vrn);
+    f[3] = rho * vn * v1 + p * n1 - u[2] * vrn * v1;
+    f[4] = rho * vn * v2 + p * n2 - u[2] * vrn * v2;
+    f[5] = (u[5] + p) * vn - (C::c_l * T + 0.5 * (v1 * v1 + v2 * v2)) * u[2] * vrn;
+    f[6] = f[7] = f[8] = 0.0;
+  }
+
+  // speed_of_sound (:332-366) and the normal speeds of max_abs_speed_naive (:595-611)
+  TAG_DEV static double sound(const double* u) {
+    using C = RainyConst;
+    double rv, rc, T;
+    nlsol(u, rv, rc, T);
+    const double ri = 1.0 / (u[0] + u[1] + u[2]);
+    const double p = (C::R_d * u[0] + C::R_v * rv) * T;
+    const double q_v = rv / u[0];
+    const double q_l = (rc + u[2]) / u[0];
+    const double gm = 1.0 + (C::R_d + C::R_v * q_v) / (C::c_vd + C::c_vv * q_v + C::c_l * q_l);
+    return sqrt(gm * p * ri);
+  }
+
+  // flux_lax_friedrichs: central flux + 0.5 max_abs_speed_naive (u_rr - u_ll)
+  TAG_DEV static void surface_flux(const Params& P, const double* ul, const double* ur, double n1,
+                                   double n2, double* F) {
+    double fl[9], fr[9];
+    flux(P, ul, n1, n2, fl);
+    flux(P, ur, n1, n2, fr);
+    const double ril = 1.0 / (ul[0] + ul[1] + ul[2]), rir = 1.0 / (ur[0] + ur[1] + ur[2]);
+    const double vl = fabs(ul[3] * ril * n1 + ul[4] * ril * n2) + fabs(rainy_v_rain(ul[1], ul[2]) * n2);
+    const double vr = fabs(ur[3] * rir * n1 + ur[4] * rir * n2) + fabs(rainy_v_rain(ur[1], ur[2]) * n2);
+    const double lam = fmax(vl, vr) + fmax(sound(ul), sound(ur)) * sqrt(n1 * n1 + n2 * n2);
+#pragma unroll
+    for (int v = 0; v < 9; ++v) F[v] = 0.5 * (fl[v] + fr[v]) - 0.5 * lam * (ur[v] - ul[v]);
+  }
+
+  // boundary_condition_simple_slip_wall reached from a StructuredMesh
+  // (:973-994): rho_v2 mirrored, states ordered by the face parity; OUTWARD flux.
+  TAG_DEV static void boundary_flux(const Params& P, const double* ui, double n1, double n2,
+                                    int face, int kind, double* F) {
+    (void)kind;
+    double ub[9];
+#pragma unroll
+    for (int v = 0; v < 9; ++v) ub[v] = ui[v];
+    ub[4] = -ui[4];
+    if (face & 1) {
+      surface_flux(P, ui, ub, n1, n2, F);
+    } else {
+      surface_flux(P, ub, ui, n1, n2, F);
+#pragma unroll
+      for (int v = 0; v < 9; ++v) F[v] = -F[v];
+    }
+  }
+
+  // source_terms_rainy (:548-577) or the manufactured source of
+  // examples/euler/precipitation/tests/convergence_test.jl:42-124; s[9]
+  TAG_DEV static void source(const Params& P, const double* u, const double* x, double t,
+                             double* s) {
+    using C = RainyConst;
+    if (P.source_kind == TAG_SRC_RAINY) {
+      double rv, rc, T;
+      nlsol(u, rv, rc, T);
+      const double rho = u[0] + u[1] + u[2];
+      const double rho_vs = rainy_e_s(T) / (C::R_v * T);
+      double S_ev = (3.86e-3 - 9.41e-5 * (T - C::ref_temp)) * (1.0 + 9.1 * pow(u[2], 0.1875));
+      S_ev *= (rho_vs - rv) * pow(u[2], 0.5);
+      const double S_auto = 0.001 * rc;
+      const double S_acc = 1.72 * rc * pow(u[2], 0.875);
+      const double S_rain = S_auto + S_acc - S_ev;
+      s[0] = 0.0; s[1] = -S_rain; s[2] = S_rain; s[3] = 0.0;
+      s[4] = -rho * C::g; s[5] = -u[4] * C::g; s[6] = s[7] = s[8] = 0.0;
+      return;
+    }
+    // manufactured solution (source kind TAG_SRC_RAINY_CONVERGENCE)
+    const double c_help = C::v_0 * 1.9386213994279082 * pow(C::pi * C::N_0, -0.125);
+    const double A = 0.1, om = 2.0 * C::pi / 2.0;
+    double si, co;
+    sincos(om * (x[0] + x[1] - t), &si, &co);
+    const double rho = 2.0 + A * si;
+    const double rho_x = om * A * co, rho_t = -rho_x;
+    const double T = rho + 250.0;
+    const double svp = rainy_e_s(T), dsvp = rainy_e_s_T(T);
+    const double rv = svp / (C::R_v * T);
+    const double rc = rho / C::c_l * 3000.0, rr = rho / C::c_l * 1000.0;
+    const double rm = rv + rc, rd = rho - rm - rr;
+    const double vr = rainy_v_rain(rm, rr);
+    const double svp_t = rho_t * dsvp, svp_x = rho_x * dsvp;
+    const double rv_t = (svp_t * T - rho_t * svp) / (C::R_v * T * T);
+    const double rv_x = (svp_x * T - rho_x * svp) / (C::R_v * T * T);
+    const double rc_t = rho_t / C::c_l * 3000.0, rc_x = rho_x / C::c_l * 3000.0;
+    const double rr_t = rho_t / C::c_l * 1000.0, rr_x = rho_x / C::c_l * 1000.0;
+    const double rm_t = rv_t + rc_t, rm_x = rv_x + rc_x;
+    const double rd_t = rho_t - rm_t - rr_t, rd_x = rho_x - rm_x - rr_x;
+    double e_t = (C::c_vd * rd_t + C::c_vv * rv_t + C::c_l * (rc_t + rr_t)) * T;
+    e_t += (C::c_vd * rd + C::c_vv * rv + C::c_l * (rc + rr)) * rho_t;
+    e_t += rv_t * C::ref_L + rho_t;
+    double e_x = (C::c_vd * rd_x + C::c_vv * rv_x + C::c_l * (rc_x + rr_x)) * T;
+    e_x += (C::c_vd * rd + C::c_vv * rv + C::c_l * (rc + rr)) * rho_x;
+    e_x += rv_x * C::ref_L + rho_x;
+    double p_x = (rd_x * C::R_d + rv_x * C::R_v) * T;
+    p_x += (rd * C::R_d + rv * C::R_v) * rho_x;
+    double vr_x = c_help * 0.125 * ((rr_x * rm - rr * rm_x) / ((rm + rr) * (rm + rr)));
+    vr_x *= pow(rr / (rm + rr), -0.875);
+    const double rrvr_x = rr_x * vr + rr * vr_x;
+    s[0] = rd_t + 2.0 * rd_x;
+    s[1] = rm_t + 2.0 * rm_x;
+    s[2] = rr_t + 2.0 * rr_x - rrvr_x;
+    s[3] = rho_x + p_x - rrvr_x;
+    s[4] = rho_x + p_x - rrvr_x;
+    s[5] = e_t + 2.0 * (e_x + p_x) - (C::c_l * rho_x * rr * vr) - (C::c_l * T + 1.0) * rrvr_x;
+    s[6] = s[7] = s[8] = 0.0;
+    (void)u;
+  }
+
+  // max_abs_speeds, :588-593
+  TAG_DEV static void max_speeds(const Params&, const double* u, double& l1, double& l2) {
+    const double ri = 1.0 / (u[0] + u[1] + u[2]);
+    const double c = sound(u);
+    l1 = fabs(u[3] * ri) + c;
+    l2 = fabs(u[4] * ri) + c + fabs(rainy_v_rain(u[1], u[2]));
+  }
+};
+
+}  // namespace tag

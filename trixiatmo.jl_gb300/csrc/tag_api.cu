@@ -11,8 +11,10 @@
 
 #include "dg2d_kernels.cuh"
 #include "dg3d_kernels.cuh"
+#include "newton_rainy.cuh"
 #include "phys_euler_energy_2d.cuh"
 #include "phys_euler_energy_3d.cuh"
+#include "phys_rainy_2d.cuh"
 
 using namespace tag;
 
@@ -43,6 +45,13 @@ struct tag_handle_s {
   int dim = 2, npe = 0, nface = 4, jpn = 4;  // nodes per element, faces, Ja doubles per node
   PhysEnergy2D::Params p_energy{};
   PhysEnergy3D::Params p_energy3d{};
+  PhysRainy2D::Params p_rainy{};
+  // rainy: Newton stage limiter settings, MLP parameters, statistics counters
+  bool has_limiter = false;
+  NewtonArgs newton{0, 20, 0, 0, 8, 1e-9, nullptr, nullptr, nullptr};
+  float* d_mlp = nullptr;
+  unsigned long long* d_counters = nullptr;
+  int* d_iters = nullptr;
   BasisDev basis{};
   cudaStream_t stream = nullptr;
   double *d_u = nullptr, *d_k = nullptr, *d_Ja = nullptr, *d_invJ = nullptr, *d_xy = nullptr,
@@ -67,7 +76,7 @@ namespace {
 // Launchers for one (physics, n) instantiation.
 struct Ops {
   int (*interface)(tag_handle h, const double* u);
-  int (*element)(tag_handle h, int mode, double* u, double* du, int stage, bool last);
+  int (*element)(tag_handle h, int mode, double* u, double* du, int stage, bool last, double t);
   int (*max_speed)(tag_handle h, const double* u);
   int (*init)(int max_smem);
   size_t (*smem_bytes)(int epb);
@@ -84,8 +93,12 @@ template <>
 const PhysEnergy3D::Params& params_of<PhysEnergy3D>(tag_handle h) {
   return h->p_energy3d;
 }
+template <>
+const PhysRainy2D::Params& params_of<PhysRainy2D>(tag_handle h) {
+  return h->p_rainy;
+}
 
-template <class Phys, int n>
+template <class Phys, int n, int VOL = kVolFluxDiff>
 struct OpsImpl {
   using S = ElemSmem<Phys, n>;
   static int interface(tag_handle h, const double* u) {
@@ -98,7 +111,8 @@ struct OpsImpl {
     TAG_CUDA(cudaGetLastError());
     return TAG_OK;
   }
-  static int element(tag_handle h, int mode, double* u, double* du, int stage, bool last) {
+  static int element(tag_handle h, int mode, double* u, double* du, int stage, bool last,
+                     double t) {
     const int epb = h->epb > 0 ? h->epb : 4;
     const int blocks = (h->nelem + epb - 1) / epb;
     const int threads = std::min(1024, epb * S::TPE);
@@ -106,16 +120,20 @@ struct OpsImpl {
     const CK2N54 ck = ck2n54();
     StageArgs st{};
     st.member = h->d_member;
+    st.xy = h->d_xy;
+    st.t_rhs = t;
     if (mode == kModeStage) {
       st.A = ck.A[stage];
       st.B = ck.B[stage];
+      st.c_stage = ck.c[stage];
+      st.t_member = h->d_mscal;
       st.dt = h->d_mscal + h->nmembers;
       st.max_speed = last ? h->d_mscal + 2 * h->nmembers : nullptr;
-      k_element<Phys, n, kModeStage><<<blocks, threads, smem, h->stream>>>(
+      k_element<Phys, n, kModeStage, VOL><<<blocks, threads, smem, h->stream>>>(
           params_of<Phys>(h), h->basis, u, du, h->d_k, h->d_Ja, h->d_invJ, h->d_sfv, h->nelem,
           epb, st, h->d_status);
     } else {
-      k_element<Phys, n, kModeRhs><<<blocks, threads, smem, h->stream>>>(
+      k_element<Phys, n, kModeRhs, VOL><<<blocks, threads, smem, h->stream>>>(
           params_of<Phys>(h), h->basis, u, du, h->d_k, h->d_Ja, h->d_invJ, h->d_sfv, h->nelem,
           epb, st, h->d_status);
     }
@@ -133,9 +151,9 @@ struct OpsImpl {
   // opt the element kernels into the device's full dynamic shared memory once,
   // outside any stream capture
   static int init(int max_smem) {
-    TAG_CUDA(cudaFuncSetAttribute(k_element<Phys, n, kModeStage>,
+    TAG_CUDA(cudaFuncSetAttribute(k_element<Phys, n, kModeStage, VOL>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    TAG_CUDA(cudaFuncSetAttribute(k_element<Phys, n, kModeRhs>,
+    TAG_CUDA(cudaFuncSetAttribute(k_element<Phys, n, kModeRhs, VOL>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
     return TAG_OK;
   }
@@ -146,16 +164,16 @@ struct OpsImpl {
   }
 };
 
-template <class Phys>
+template <class Phys, int VOL = kVolFluxDiff>
 const Ops* ops_for_n(int n) {
   switch (n) {
-    case 2: return OpsImpl<Phys, 2>::get();
-    case 3: return OpsImpl<Phys, 3>::get();
-    case 4: return OpsImpl<Phys, 4>::get();
-    case 5: return OpsImpl<Phys, 5>::get();
-    case 6: return OpsImpl<Phys, 6>::get();
-    case 7: return OpsImpl<Phys, 7>::get();
-    case 8: return OpsImpl<Phys, 8>::get();
+    case 2: return OpsImpl<Phys, 2, VOL>::get();
+    case 3: return OpsImpl<Phys, 3, VOL>::get();
+    case 4: return OpsImpl<Phys, 4, VOL>::get();
+    case 5: return OpsImpl<Phys, 5, VOL>::get();
+    case 6: return OpsImpl<Phys, 6, VOL>::get();
+    case 7: return OpsImpl<Phys, 7, VOL>::get();
+    case 8: return OpsImpl<Phys, 8, VOL>::get();
     default: return nullptr;
   }
 }
@@ -172,7 +190,8 @@ struct OpsImpl3D {
     TAG_CUDA(cudaGetLastError());
     return TAG_OK;
   }
-  static int element(tag_handle h, int mode, double* u, double* du, int stage, bool last) {
+  static int element(tag_handle h, int mode, double* u, double* du, int stage, bool last,
+                     double) {
     const int epb = h->epb > 0 ? h->epb : 1;
     const int blocks = (h->nelem + epb - 1) / epb;
     const int threads = std::min(1024, ((epb * S::TPE + 31) / 32) * 32);
@@ -250,6 +269,15 @@ void load_basis(BasisDev& b, const double* dsplit_colmajor, const double* w, int
     for (int c = 0; c < n; ++c) b.Ds[a * n + c] = dsplit_colmajor[a + n * c];
   b.winv0 = 1.0 / w[0];
   b.winvN = 1.0 / w[n - 1];
+  // D_hat = -M^{-1} D^T M from D_split = 2 D - M^{-1} B:
+  //   D[a][c] = (Ds[a][c] + (M^{-1} B)[a][c]) / 2,  D_hat[a][c] = -D[c][a] w_c / w_a
+  for (int a = 0; a < n; ++a)
+    for (int c = 0; c < n; ++c) {
+      double dca = b.Ds[c * n + a];
+      if (c == a && c == 0) dca -= 1.0 / w[0];
+      if (c == a && c == n - 1) dca += 1.0 / w[n - 1];
+      b.Dh[a * n + c] = -0.5 * dca * w[c] / w[a];
+    }
 }
 
 MemberScalars member_scalars(tag_handle h) {
@@ -276,8 +304,19 @@ int stage_sequence(tag_handle h) {
   for (int s = 0; s < 5; ++s) {
     int rc = h->ops->interface(h, h->d_u);
     if (rc) return rc;
-    rc = h->ops->element(h, kModeStage, h->d_u, nullptr, s, s == 4);
+    rc = h->ops->element(h, kModeStage, h->d_u, nullptr, s, s == 4, 0.0);
     if (rc) return rc;
+    if (h->has_limiter) {
+      // stage limiter: saturation Newton solve on every node (warm start)
+      const long nodes = (long)h->nelem * h->npe;
+      NewtonArgs a = h->newton;
+      a.learned = 0;
+      a.iters = nullptr;
+      a.counters = nullptr;
+      k_newton_rainy<<<(unsigned)((nodes + 255) / 256), 256, 0, h->stream>>>(h->d_u, nodes, a,
+                                                                              h->d_status);
+      TAG_CUDA(cudaGetLastError());
+    }
   }
   return TAG_OK;
 }
@@ -324,11 +363,11 @@ int autotune(tag_handle h, const double* u) {
     int rc = h->ops->interface(h, uu);
     if (rc) return rc;
     for (int w = 0; w < 2; ++w) {
-      rc = h->ops->element(h, kModeRhs, uu, h->d_tmp_du, 0, false);
+      rc = h->ops->element(h, kModeRhs, uu, h->d_tmp_du, 0, false, 0.0);
       if (rc) return rc;
     }
     TAG_CUDA(cudaEventRecord(a, h->stream));
-    for (int r = 0; r < 5; ++r) h->ops->element(h, kModeRhs, uu, h->d_tmp_du, 0, false);
+    for (int r = 0; r < 5; ++r) h->ops->element(h, kModeRhs, uu, h->d_tmp_du, 0, false, 0.0);
     TAG_CUDA(cudaEventRecord(b, h->stream));
     TAG_CUDA(cudaEventSynchronize(b));
     float ms = 0.f;
@@ -367,12 +406,21 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
     return fail(TAG_E_NO_DEVICE, "no CUDA device visible");
-  if (cfg->equations != TAG_EQ_EULER_ENERGY_2D && cfg->equations != TAG_EQ_EULER_ENERGY_3D)
+  if (cfg->equations != TAG_EQ_EULER_ENERGY_2D && cfg->equations != TAG_EQ_EULER_ENERGY_3D &&
+      cfg->equations != TAG_EQ_RAINY_2D)
     return fail(TAG_E_INVALID, "unsupported equations id");
   const int dim = cfg->equations == TAG_EQ_EULER_ENERGY_3D ? 3 : 2;
   const int nface = 2 * dim;
-  if (cfg->volume_flux != TAG_VF_RANOCHA_WARUSZEWSKI || cfg->surface_flux != TAG_SF_LMARS)
+  const bool rainy = cfg->equations == TAG_EQ_RAINY_2D;
+  if (!rainy && (cfg->volume_flux != TAG_VF_RANOCHA_WARUSZEWSKI || cfg->surface_flux != TAG_SF_LMARS))
     return fail(TAG_E_INVALID, "unsupported flux combination");
+  if (rainy && ((cfg->volume_flux != TAG_VF_EC_RAIN && cfg->volume_flux != TAG_VF_WEAK_FORM) ||
+                cfg->surface_flux != TAG_SF_LAX_FRIEDRICHS))
+    return fail(TAG_E_INVALID, "unsupported flux combination for the rainy equations");
+  if (rainy && cfg->params[0] != TAG_SRC_RAINY && cfg->params[0] != TAG_SRC_RAINY_CONVERGENCE)
+    return fail(TAG_E_INVALID, "unsupported source kind for the rainy equations");
+  if (rainy && cfg->params[0] == TAG_SRC_RAINY_CONVERGENCE && !cfg->node_coordinates)
+    return fail(TAG_E_INVALID, "the convergence-test source needs node coordinates");
   const int n = cfg->polydeg + 1;
   if (n < 2 || n > kMaxNodes) return fail(TAG_E_INVALID, "polydeg out of range 1..7");
   if (dim == 3 && n < 3) return fail(TAG_E_INVALID, "3D meshes need polydeg >= 2");
@@ -405,8 +453,10 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
     const int e = cfg->boundary_elements[k], f = cfg->boundary_faces[k];
     const int kind = cfg->boundary_kinds ? cfg->boundary_kinds[k] : TAG_BC_SLIP_WALL_NORMAL;
     if (e < 0 || e >= cfg->nelements || f < 0 || f >= nface ||
-        (kind != TAG_BC_SLIP_WALL_STRUCTURED && kind != TAG_BC_SLIP_WALL_NORMAL) ||
-        (dim == 3 && kind != TAG_BC_SLIP_WALL_NORMAL))
+        (kind != TAG_BC_SLIP_WALL_STRUCTURED && kind != TAG_BC_SLIP_WALL_NORMAL &&
+         kind != TAG_BC_SIMPLE_SLIP_WALL) ||
+        (dim == 3 && kind != TAG_BC_SLIP_WALL_NORMAL) ||
+        (rainy != (kind == TAG_BC_SIMPLE_SLIP_WALL)))
       return fail(TAG_E_INVALID, "boundary index or kind out of range");
   }
 
@@ -421,7 +471,14 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
   h->nface = nface;
   h->npe = dim == 3 ? n * n * n : n * n;
   h->jpn = dim * dim;
-  if (dim == 3) {
+  if (rainy) {
+    h->nv = PhysRainy2D::NV;
+    h->na = PhysRainy2D::NA;
+    h->p_rainy = PhysRainy2D::make_params(cfg->params);
+    h->ops = cfg->volume_flux == TAG_VF_WEAK_FORM ? ops_for_n<PhysRainy2D, kVolWeak>(n)
+                                                  : ops_for_n<PhysRainy2D, kVolFluxDiff>(n);
+    h->has_limiter = true;
+  } else if (dim == 3) {
     h->nv = PhysEnergy3D::NV;
     h->na = PhysEnergy3D::NA;
     h->p_energy3d = PhysEnergy3D::make_params(cfg->params);
@@ -465,6 +522,11 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
     return cleanup(rc);
   if ((rc = upload(&h->d_ctl, (const StepCtl*)nullptr, 1, h->stream))) return cleanup(rc);
   if ((rc = upload(&h->d_status, (const unsigned*)nullptr, 1, h->stream))) return cleanup(rc);
+  if (rainy) {
+    if ((rc = upload(&h->d_counters, (const unsigned long long*)nullptr, 4, h->stream)))
+      return cleanup(rc);
+    if ((rc = upload(&h->d_iters, (const int*)nullptr, nodes, h->stream))) return cleanup(rc);
+  }
   if (cudaMallocHost(&h->h_pin, sizeof(double) * (3 * h->nmembers + 2)) != cudaSuccess)
     return cleanup(fail(TAG_E_CUDA, "pinned alloc failed"));
   if (cudaStreamSynchronize(h->stream) != cudaSuccess)
@@ -490,6 +552,9 @@ int tag_destroy(tag_handle h) {
   for (int* p : ip)
     if (p) cudaFree(p);
   if (h->d_member) cudaFree(h->d_member);
+  if (h->d_mlp) cudaFree(h->d_mlp);
+  if (h->d_counters) cudaFree(h->d_counters);
+  if (h->d_iters) cudaFree(h->d_iters);
   if (h->d_mscal) cudaFree(h->d_mscal);
   if (h->d_ctl) cudaFree(h->d_ctl);
   if (h->d_status) cudaFree(h->d_status);
@@ -505,7 +570,6 @@ int64_t tag_ndofs_total(tag_handle h) {
 
 int tag_rhs(tag_handle h, const double* u, double* du, double t, int32_t on_device) {
   if (!h || !u || !du) return fail(TAG_E_INVALID, "null argument");
-  (void)t;
   const size_t bytes = sizeof(double) * (size_t)tag_ndofs_total(h);
   const double* ud = u;
   double* dud = du;
@@ -520,7 +584,7 @@ int tag_rhs(tag_handle h, const double* u, double* du, double t, int32_t on_devi
   if (rc) return rc;
   rc = h->ops->interface(h, ud);
   if (rc) return rc;
-  rc = h->ops->element(h, kModeRhs, const_cast<double*>(ud), dud, 0, false);
+  rc = h->ops->element(h, kModeRhs, const_cast<double*>(ud), dud, 0, false, t);
   if (rc) return rc;
   if (!on_device) TAG_CUDA(cudaMemcpyAsync(du, dud, bytes, cudaMemcpyDeviceToHost, h->stream));
   TAG_CUDA(cudaStreamSynchronize(h->stream));
@@ -621,12 +685,12 @@ int tag_time_kernels(tag_handle h, int32_t reps, double* ms_interface, double* m
   for (auto& e : ev) TAG_CUDA(cudaEventCreate(&e));
   // warm-up stage
   if ((rc = h->ops->interface(h, h->d_u))) return rc;
-  if ((rc = h->ops->element(h, kModeStage, h->d_u, nullptr, 0, false))) return rc;
+  if ((rc = h->ops->element(h, kModeStage, h->d_u, nullptr, 0, false, 0.0))) return rc;
   for (int r = 0; r < reps; ++r) {
     TAG_CUDA(cudaEventRecord(ev[3 * r], h->stream));
     if ((rc = h->ops->interface(h, h->d_u))) return rc;
     TAG_CUDA(cudaEventRecord(ev[3 * r + 1], h->stream));
-    if ((rc = h->ops->element(h, kModeStage, h->d_u, nullptr, (r + 1) % 5, false))) return rc;
+    if ((rc = h->ops->element(h, kModeStage, h->d_u, nullptr, (r + 1) % 5, false, 0.0))) return rc;
     TAG_CUDA(cudaEventRecord(ev[3 * r + 2], h->stream));
   }
   TAG_CUDA(cudaStreamSynchronize(h->stream));
@@ -641,6 +705,57 @@ int tag_time_kernels(tag_handle h, int32_t reps, double* ms_interface, double* m
   for (auto& e : ev) cudaEventDestroy(e);
   *ms_interface = si / reps;
   *ms_element = se / reps;
+  h->speed_valid = false;
+  return TAG_OK;
+}
+
+int tag_set_newton(tag_handle h, int32_t mode, double tol, int32_t max_iterations,
+                   int32_t polish) {
+  if (!h || !h->has_limiter) return fail(TAG_E_INVALID, "not a rainy handle");
+  if ((mode != 0 && mode != 1) || !(tol > 0.0) || max_iterations < 1 || polish < 0)
+    return fail(TAG_E_INVALID, "bad Newton settings");
+  h->newton.mode = mode;
+  h->newton.tol = tol;
+  h->newton.maxit = max_iterations;
+  h->newton.polish = polish;
+  h->graph_epb = -2;  // limiter settings are baked into the captured graph
+  return TAG_OK;
+}
+
+int tag_set_mlp(tag_handle h, const float* params) {
+  if (!h || !h->has_limiter || !params) return fail(TAG_E_INVALID, "bad argument");
+  if (!h->d_mlp) TAG_CUDA(cudaMalloc(&h->d_mlp, sizeof(float) * kMlpParams));
+  TAG_CUDA(cudaMemcpyAsync(h->d_mlp, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice,
+                           h->stream));
+  TAG_CUDA(cudaStreamSynchronize(h->stream));
+  return TAG_OK;
+}
+
+int tag_newton_solve(tag_handle h, int32_t use_learned, int32_t* iters, tag_newton_stats* stats) {
+  if (!h || !h->has_limiter) return fail(TAG_E_INVALID, "not a rainy handle");
+  if (use_learned && !h->d_mlp) return fail(TAG_E_INVALID, "no MLP parameters set");
+  const long nodes = (long)h->nelem * h->npe;
+  NewtonArgs a = h->newton;
+  a.learned = use_learned ? 1 : 0;
+  a.mlp = h->d_mlp;
+  a.iters = h->d_iters;
+  a.counters = h->d_counters;
+  TAG_CUDA(cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * 4, h->stream));
+  k_newton_rainy<<<(unsigned)((nodes + 255) / 256), 256, 0, h->stream>>>(h->d_u, nodes, a,
+                                                                          h->d_status);
+  TAG_CUDA(cudaGetLastError());
+  unsigned long long c[4];
+  TAG_CUDA(cudaMemcpyAsync(c, h->d_counters, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+  if (iters)
+    TAG_CUDA(cudaMemcpyAsync(iters, h->d_iters, sizeof(int) * nodes, cudaMemcpyDeviceToHost,
+                             h->stream));
+  TAG_CUDA(cudaStreamSynchronize(h->stream));
+  if (stats) {
+    stats->nodes = nodes;
+    stats->updates = (int64_t)c[0];
+    stats->fallbacks = (int64_t)c[1];
+    stats->not_converged = (int64_t)c[2];
+  }
   h->speed_valid = false;
   return TAG_OK;
 }

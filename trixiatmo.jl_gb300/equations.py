@@ -78,6 +78,29 @@ class CompressibleEulerEnergyEquationsWithGravity3D:
         return rho, v1, v2, v3, p, u[..., 5]
 
 
+class CompressibleRainyEulerEquations2D:
+    """State (rho_dry, rho_moist, rho_rain, rho_v1, rho_v2, energy, rho_vapour,
+    rho_cloud, temperature) (src/equations/compressible_rainy_euler_2d.jl:49-110);
+    slots 7-9 solve the saturation system (Newton stage limiter)."""
+
+    nvariables = 9
+    ndims = 2
+    eq_id = _lib.TAG_EQ_RAINY_2D
+    c_l, c_pd, c_vd, c_pv, c_vv = 4186.0, 1004.0, 717.0, 1885.0, 1424.0
+    R_d, R_v = 287.0, 461.0
+    ref_saturation_pressure, ref_temperature = 610.7, 273.15
+    ref_latent_heat_vap_temp, ref_pressure = 2500000.0, 100000.0
+    gravity = 9.80616
+
+    def saturation_vapour_pressure(self, T):
+        """:397-419 (Clausius-Clapeyron)."""
+        e = self.ref_saturation_pressure * (T / self.ref_temperature) ** (
+            (self.c_pv - self.c_l) / self.R_v)
+        return e * np.exp(((self.ref_latent_heat_vap_temp - (self.c_pv - self.c_l) *
+                            self.ref_temperature) / self.R_v) *
+                          (1.0 / self.ref_temperature - 1.0 / T))
+
+
 class _NamedFlux:
     def __init__(self, name):
         self.name = name
@@ -89,6 +112,8 @@ class _NamedFlux:
 flux_ranocha = _NamedFlux("flux_ranocha")
 flux_nonconservative_waruszewski_etal = _NamedFlux("flux_nonconservative_waruszewski_etal")
 flux_zero = _NamedFlux("flux_zero")
+flux_ec_rain = _NamedFlux("flux_ec_rain")
+flux_lax_friedrichs = _NamedFlux("flux_lax_friedrichs")
 
 
 class FluxLMARS:
@@ -106,6 +131,10 @@ class VolumeIntegralFluxDifferencing:
         self.volume_flux = volume_flux
 
 
+class VolumeIntegralWeakForm:
+    pass
+
+
 class _BC:
     def __init__(self, name):
         self.name = name
@@ -116,6 +145,21 @@ class _BC:
 
 boundary_condition_slip_wall = _BC("boundary_condition_slip_wall")
 boundary_condition_periodic = _BC("boundary_condition_periodic")
+boundary_condition_simple_slip_wall = _BC("boundary_condition_simple_slip_wall")
+
+
+class _Source:
+    def __init__(self, name, kind):
+        self.name = name
+        self.kind = kind
+
+    def __repr__(self):
+        return self.name
+
+
+source_terms_rainy = _Source("source_terms_rainy", _lib.TAG_SRC_RAINY)
+source_terms_convergence_test_rainy = _Source("source_terms_convergence_test_rainy",
+                                              _lib.TAG_SRC_RAINY_CONVERGENCE)
 
 
 def speed_of_sound_isothermal(equations, T0):

@@ -184,3 +184,54 @@ class IsothermalShell:
         phi = g * (a - a * a / rr)
         z = np.zeros_like(r)
         return equations.prim2cons(rho, z, z, z, p, phi)
+
+
+# ---- 2D rainy states ---------------------------------------------------------
+def initial_condition_convergence_test_rainy(x, t, equations):
+    """examples/euler/precipitation/tests/convergence_test.jl:8-40 (manufactured
+    solution, travelling along x + y)."""
+    eq = equations
+    rho = 2.0 + 0.1 * np.sin(np.pi * (x[..., 0] + x[..., 1] - t))
+    T = rho + 250.0
+    rv = eq.saturation_vapour_pressure(T) / (eq.R_v * T)
+    rc = rho / eq.c_l * 3000.0
+    rr = rho / eq.c_l * 1000.0
+    rm = rv + rc
+    rd = rho - rm - rr
+    e = (eq.c_vd * rd + eq.c_vv * rv + eq.c_l * (rc + rr)) * T + rv * eq.ref_latent_heat_vap_temp + rho
+    return np.stack([rd, rm, rr, rho, rho, e, rv, rc, T], axis=-1)
+
+
+class MoistBubbleRainy:
+    """Seeded moist state for the learned-Newton-guess benchmark (20 km x 10 km):
+    a dry-adiabatic-ish background (surface 288 K, lapse 6.5 K/km, hydrostatic
+    pressure), per-node relative humidity U[rh_min, rh_max], a saturated bubble
+    (RH = 1) of radius `radius` at (xc, zc), cloud and rain mixing ratios
+    U[0, qmax] of the dry density, and zero velocity.  Slots 7-9 hold the
+    constructed (vapour, cloud, temperature) triple — not the saturation
+    equilibrium, which the Newton solve then finds (the 'plain' warm start)."""
+
+    def __init__(self, seed=2, rh_min=0.2, rh_max=1.0, qmax=1e-3, xc=10000.0, zc=2000.0,
+                 radius=2000.0, T0=288.0, lapse=0.0065):
+        self.seed, self.rh_min, self.rh_max, self.qmax = seed, rh_min, rh_max, qmax
+        self.xc, self.zc, self.radius = xc, zc, radius
+        self.T0, self.lapse = T0, lapse
+
+    def __call__(self, x, t, equations):
+        eq = equations
+        shape = x.shape[:-1]
+        rng = np.random.Generator(np.random.Philox(self.seed))
+        z = x[..., 1]
+        T = self.T0 - self.lapse * z
+        p = 1e5 * (T / self.T0) ** (eq.gravity / (eq.R_d * self.lapse))
+        rh = rng.uniform(self.rh_min, self.rh_max, shape)
+        r = np.sqrt((x[..., 0] - self.xc) ** 2 + (z - self.zc) ** 2)
+        rh = np.where(r <= self.radius, 1.0, rh)
+        rv = rh * eq.saturation_vapour_pressure(T) / (eq.R_v * T)
+        rd = (p - rv * eq.R_v * T) / (eq.R_d * T)
+        rc = rng.uniform(0.0, self.qmax, shape) * rd
+        rr = rng.uniform(0.0, self.qmax, shape) * rd
+        rm = rv + rc
+        e = (eq.c_vd * rd + eq.c_vv * rv + eq.c_l * (rc + rr)) * T + rv * eq.ref_latent_heat_vap_temp
+        z0 = np.zeros_like(T)
+        return np.stack([rd, rm, rr, z0, z0, e, rv, rc, T], axis=-1)

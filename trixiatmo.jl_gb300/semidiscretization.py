@@ -26,9 +26,11 @@ import numpy as np
 from . import _lib
 from .basis import LobattoLegendreBasis
 from .equations import (CompressibleEulerEnergyEquationsWithGravity2D,
-                        CompressibleEulerEnergyEquationsWithGravity3D, FluxLMARS,
-                        boundary_condition_slip_wall, flux_nonconservative_waruszewski_etal,
-                        flux_ranocha, flux_zero)
+                        CompressibleEulerEnergyEquationsWithGravity3D,
+                        CompressibleRainyEulerEquations2D, FluxLMARS, VolumeIntegralWeakForm,
+                        _Source, boundary_condition_simple_slip_wall,
+                        boundary_condition_slip_wall, flux_ec_rain, flux_lax_friedrichs,
+                        flux_nonconservative_waruszewski_etal, flux_ranocha, flux_zero)
 from .initial_conditions import EARTH_ROTATION_RATE
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -61,8 +63,22 @@ source_terms_coriolis = _SourceTerms("source_terms_coriolis")
 
 
 def _flux_ids(equations, solver, source_terms=None):
-    vf = solver.volume_integral.volume_flux
+    vi = solver.volume_integral
+    vf = getattr(vi, "volume_flux", None)
     sf = solver.surface_flux
+    if isinstance(equations, CompressibleRainyEulerEquations2D):
+        if isinstance(vi, VolumeIntegralWeakForm):
+            vid = _lib.TAG_VF_WEAK_FORM
+        elif vf is flux_ec_rain:
+            vid = _lib.TAG_VF_EC_RAIN
+        else:
+            raise ValueError("volume integral must be weak form or flux differencing with "
+                             "flux_ec_rain")
+        if sf is not flux_lax_friedrichs:
+            raise ValueError("surface flux must be flux_lax_friedrichs")
+        if not isinstance(source_terms, _Source):
+            raise ValueError("rainy equations need source_terms_rainy or the convergence-test source")
+        return vid, _lib.TAG_SF_LAX_FRIEDRICHS, [float(source_terms.kind)]
     if isinstance(equations, CompressibleEulerEnergyEquationsWithGravity3D):
         if not (isinstance(vf, tuple) and vf[0] is flux_ranocha
                 and vf[1] is flux_nonconservative_waruszewski_etal):
@@ -92,7 +108,9 @@ def _bc_kinds(names, boundary_conditions, ndims):
     bcs = boundary_conditions or {}
     for name in names:
         bc = bcs.get(name)
-        if bc is boundary_condition_slip_wall:
+        if bc is boundary_condition_simple_slip_wall:
+            kinds.append(_lib.TAG_BC_SIMPLE_SLIP_WALL)
+        elif bc is boundary_condition_slip_wall:
             # StructuredMesh (2D) reaches the reference's orientation-argument
             # method; P4estMesh (the 3D shell) the normal-vector method
             kinds.append(_lib.TAG_BC_SLIP_WALL_STRUCTURED if ndims == 2
@@ -281,6 +299,27 @@ class SemidiscretizationHyperbolic:
         a, b = ctypes.c_double(), ctypes.c_double()
         _lib.check(self._L.tag_time_kernels(self._h, int(reps), ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
+
+    # ---- rainy: saturation Newton solve ------------------------------------
+    def set_newton(self, mode=0, tol=1e-9, max_iterations=20, polish=0):
+        """Stage-limiter settings (NonlinearSolveDG defaults: tol 1e-9, 20 iterations)."""
+        _lib.check(self._L.tag_set_newton(self._h, int(mode), float(tol), int(max_iterations),
+                                          int(polish)))
+
+    def set_mlp(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        assert p.size == _lib.MLP_PARAMS
+        _lib.check(self._L.tag_set_mlp(self._h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+
+    def newton_solve(self, learned=False):
+        """One Newton solve on every node of the resident state; returns
+        (stats dict, per-node update counts)."""
+        iters = np.zeros(self.ndofs, dtype=np.int32)
+        st = _lib.NewtonStats()
+        _lib.check(self._L.tag_newton_solve(self._h, int(bool(learned)), _ptr(iters, _ip),
+                                            ctypes.byref(st)))
+        return ({"nodes": st.nodes, "updates": st.updates, "fallbacks": st.fallbacks,
+                 "not_converged": st.not_converged}, iters)
 
     def status(self, clear=True):
         v = ctypes.c_uint32()
