@@ -155,8 +155,11 @@ int tag_time_kernels(tag_handle h, int32_t reps, double* ms_interface, double* m
  * src/callbacks_stage/nonlinear_solve_dg.jl:18-44; defaults tolerance 1e-9,
  * max_iterations 20).  mode 0: the reference's criterion max|residual| < tol;
  * mode 1: relative, |res_1| < tol |E_internal| and |res_2|, |res_3| <=
- * tol 1e7 rho_moist.  polish: up to this many extra Newton updates after
- * convergence while they still change the iterate. */
+ * tol 1e7 rho_moist.  polish (canonical finish, not in the reference; 0 = off):
+ * a converged iterate is snapped to a grid fixed by the node's state (vapour
+ * and cloud to 2^-24 of the power of two above rho_moist, temperature to
+ * 2^-18 K) and this many Newton updates are taken from there, so that solves
+ * converged from different starts return the same bits. */
 int tag_set_newton(tag_handle h, int32_t mode, double tol, int32_t max_iterations,
                    int32_t polish);
 
@@ -169,8 +172,12 @@ typedef struct {
 
 /* One Newton solve of the saturation system on every node of the resident
  * state (the stage limiter's work once, nonlinear_solve_dg2d.jl:6-44).
- * use_learned != 0 starts from the MLP guess set by tag_set_mlp and falls back
- * to the warm start (slots 7-9) when it has not converged after 8 updates.
+ * use_learned != 0 starts from the learned guess and falls back to the warm
+ * start (slots 7-9) when it has not converged after 8 updates.  The learned
+ * guess is the closed-form unsaturated equilibrium T_unsat = (e_int - rho_m L)
+ * / (c_vd rho_d + c_vv rho_m + c_l rho_r) where e_s(T_unsat)/(R_v T_unsat) >=
+ * rho_m (exact there), else T_unsat plus the offset predicted by the MLP set
+ * with tag_set_mlp (inputs rho_d, rho_m, rho_r, e_int, T_unsat).
  * iters (host, may be null): per-node update counts. */
 int tag_newton_solve(tag_handle h, int32_t use_learned, int32_t* iters, tag_newton_stats* stats);
 

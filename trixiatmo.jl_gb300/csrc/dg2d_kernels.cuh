@@ -92,7 +92,9 @@ __global__ void __launch_bounds__(256) k_interface(
     double n1 = sj * Ja[q * 4 + 2 * (f >> 1)];
     double n2 = sj * Ja[q * 4 + 2 * (f >> 1) + 1];
     double F[NA];
-    if (kind == TAG_BC_SLIP_WALL_STRUCTURED) {
+    // StructuredMesh walls: normal in the +xi/+eta sense, states ordered by
+    // the face parity inside boundary_flux, result turned outward here
+    if (kind == TAG_BC_SLIP_WALL_STRUCTURED || kind == TAG_BC_SIMPLE_SLIP_WALL) {
       Phys::boundary_flux(P, ui, n1, n2, f, kind, F);
 #pragma unroll
       for (int v = 0; v < NA; ++v) F[v] *= sj;

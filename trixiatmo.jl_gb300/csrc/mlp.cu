@@ -4,9 +4,9 @@
 //
 // Training data are (state, converged temperature) pairs produced by the
 // reference's Newton algorithm (k_newton_rainy run to a tight tolerance from
-// the warm start, the same iteration as nonlinear_solve_dg2d.jl:6-44); the network
-// predicts the normalised temperature from the normalised inputs of
-// mlp_inputs().  Gradients of one batch are accumulated per CTA in a fixed
+// the warm start, the same iteration as nonlinear_solve_dg2d.jl:6-44); on the
+// nodes that are saturated at equilibrium the network predicts the normalised
+// offset T* - T_unsat from the normalised inputs of mlp_inputs().  Gradients of one batch are accumulated per CTA in a fixed
 // order and then summed over CTAs in a fixed order, so training is bitwise
 // reproducible for a given seed.
 #include <cuda_runtime.h>

@@ -18,20 +18,28 @@ constexpr int oW1 = 0, oB1 = oW1 + kMlpH * kMlpIn, oW2 = oB1 + kMlpH, oB2 = oW2 
               oInScale = oInMean + kMlpIn, oOutMean = oInScale + kMlpIn,
               oOutScale = oOutMean + 1;
 
-// Network inputs of a rainy state: (rho_dry, rho_moist, rho_rain, internal
-// energy E - |rho v|^2 / (2 rho), a dry-heat-capacity temperature estimate
-// e_int / (c_vd rho_d + c_vv rho_m + c_l rho_r)).  The benchmark description
-// names (rho, rho E, rho v, rho c, rho r); cloud water is an unknown of the
-// saturation system, not an input, so the conserved moist density stands in.
-TAG_DEV void mlp_inputs(const double* u, float* x) {
+// Temperature of the unsaturated equilibrium (all moisture as vapour):
+// e_int = (c_vd rho_d + c_vv rho_m + c_l rho_r) T + rho_m L, e_int the internal
+// energy E - |rho v|^2 / (2 rho).  It is the exact solution of the saturation
+// system when e_s(T) / (R_v T) >= rho_m there, and a lower bound otherwise.
+TAG_DEV double rainy_t_unsat(const double* u, double& e_int) {
   using C = RainyConst;
   const double rho = u[0] + u[1] + u[2];
-  const double e_int = u[5] - 0.5 * (u[3] * u[3] + u[4] * u[4]) / rho;
+  e_int = u[5] - 0.5 * (u[3] * u[3] + u[4] * u[4]) / rho;
+  return (e_int - u[1] * C::ref_L) / (C::c_vd * u[0] + C::c_vv * u[1] + C::c_l * u[2]);
+}
+
+// Network inputs of a rainy state: (rho_dry, rho_moist, rho_rain, internal
+// energy, unsaturated-equilibrium temperature).  The network predicts the
+// latent-heat offset T* - T_unsat of nodes that are saturated at equilibrium.
+// Cloud water is an unknown of the saturation system, not an input, so the
+// conserved moist density stands in for (rho_v, rho_c).
+TAG_DEV void mlp_inputs(const double* u, double e_int, double t_unsat, float* x) {
   x[0] = (float)u[0];
   x[1] = (float)u[1];
   x[2] = (float)u[2];
   x[3] = (float)e_int;
-  x[4] = (float)(e_int / (C::c_vd * u[0] + C::c_vv * u[1] + C::c_l * u[2]));
+  x[4] = (float)t_unsat;
 }
 
 TAG_DEV float mlp_forward(const float* __restrict__ P, const float* xin) {
@@ -59,7 +67,8 @@ TAG_DEV float mlp_forward(const float* __restrict__ P, const float* xin) {
 struct NewtonArgs {
   int mode;          // 0: max|res| < tol (reference); 1: relative to E_int and 1e7 rho_moist
   int maxit;         // Newton updates allowed
-  int polish;        // further updates after convergence while they change the iterate
+  int polish;        // canonical finish: Newton updates from the converged iterate snapped
+                     // to a fixed grid (0: stop at the criterion, as the reference does)
   int learned;       // start from the MLP guess (fallback to the warm start after maxit_learned)
   int maxit_learned; // 8
   double tol;
@@ -112,7 +121,24 @@ TAG_DEV bool rainy_newton_done(const double* u, const double* r, int mode, doubl
   return fabs(r[0]) < tol * fabs(e_int) && fabs(r[1]) <= s2 && fabs(r[2]) <= s2;
 }
 
+// Snaps a converged iterate to a grid fixed by the node's state: vapour and
+// cloud to 2^-24 of the power of two above rho_moist, temperature to 2^-18 K.
+// Two runs converged from different starts land on the same grid point unless
+// they straddle a cell edge (their distance is ~1e-12 of a cell at the
+// tolerance); Newton updates from that common point then agree bit for bit.
+TAG_DEV void rainy_snap(const double* u, double* x) {
+  int e;
+  frexp(fabs(u[1]), &e);
+  const double gm = ldexp(1.0, e - 24), gt = ldexp(1.0, -18);
+  x[0] = rint(x[0] / gm) * gm;
+  x[1] = rint(x[1] / gm) * gm;
+  x[2] = rint(x[2] / gt) * gt;
+}
+
 // Newton from x; returns updates until the criterion held (maxit if never).
+// With polish > 0 a converged iterate is snapped (rainy_snap) and `polish`
+// further updates are taken from there; if the criterion then fails, the
+// iterate before the snap is kept.
 TAG_DEV int rainy_newton_run(const double* u, double* x, int mode, double tol, int maxit,
                              int polish, bool& converged) {
   double r[3], dx[3];
@@ -133,16 +159,45 @@ TAG_DEV int rainy_newton_run(const double* u, double* x, int mode, double tol, i
     rainy_residual(u, x, r);
     converged = rainy_newton_done(u, r, mode, tol);
   }
-  for (int p = 0; p < polish && converged; ++p) {
-    rainy_residual(u, x, r);
-    rainy_newton_step(u, x, r, dx);
-    const double y0 = x[0] - dx[0], y1 = x[1] - dx[1], y2 = x[2] - dx[2];
-    if (y0 == x[0] && y1 == x[1] && y2 == x[2]) break;
-    x[0] = y0;
-    x[1] = y1;
-    x[2] = y2;
+  if (polish > 0 && converged) {
+    double y[3] = {x[0], x[1], x[2]};
+    rainy_snap(u, y);
+    for (int p = 0; p < polish; ++p) {
+      rainy_residual(u, y, r);
+      rainy_newton_step(u, y, r, dx);
+      y[0] -= dx[0];
+      y[1] -= dx[1];
+      y[2] -= dx[2];
+    }
+    rainy_residual(u, y, r);
+    if (rainy_newton_done(u, r, mode, tol)) {
+      x[0] = y[0];
+      x[1] = y[1];
+      x[2] = y[2];
+    }
   }
   return it;
+}
+
+// Learned start: the closed-form unsaturated equilibrium where it is valid,
+// else T_unsat plus the network's latent-heat offset, with vapour and cloud
+// from the saturation relation at that temperature.
+TAG_DEV void rainy_learned_guess(const float* __restrict__ P, const double* u, double* x) {
+  using C = RainyConst;
+  double e_int;
+  const double tu = rainy_t_unsat(u, e_int);
+  if (tu > 0.0 && rainy_e_s(tu) / (C::R_v * tu) >= u[1]) {
+    x[0] = u[1];
+    x[1] = 0.0;
+    x[2] = tu;
+    return;
+  }
+  float xin[kMlpIn];
+  mlp_inputs(u, e_int, tu, xin);
+  const double T = tu + fmax((double)mlp_forward(P, xin), 0.0);
+  x[2] = T;
+  x[0] = fmin(rainy_e_s(T) / (C::R_v * T), u[1]);
+  x[1] = u[1] - x[0];
 }
 
 static __global__ void __launch_bounds__(256) k_newton_rainy(double* __restrict__ u, long nodes,
@@ -163,14 +218,8 @@ static __global__ void __launch_bounds__(256) k_newton_rainy(double* __restrict_
   bool conv = false;
   int its = 0, fallback = 0;
   if (a.learned && a.mlp) {
-    using C = RainyConst;
-    float xin[kMlpIn];
-    mlp_inputs(s, xin);
-    const double T = (double)mlp_forward(sp, xin);
     double xg[3];
-    xg[2] = T;
-    xg[0] = fmin(rainy_e_s(T) / (C::R_v * T), s[1]);
-    xg[1] = s[1] - xg[0];
+    rainy_learned_guess(sp, s, xg);
     its = rainy_newton_run(s, xg, a.mode, a.tol, a.maxit_learned, a.polish, conv);
     if (conv && isfinite(xg[2])) {
       x[0] = xg[0];

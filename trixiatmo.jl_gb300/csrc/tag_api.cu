@@ -81,7 +81,19 @@ struct Ops {
   int (*init)(int max_smem);
   size_t (*smem_bytes)(int epb);
   int threads_per_element;
+  int (*max_threads)();  // per-CTA thread limit of the element kernels (registers)
 };
+
+// Largest multiple of 32 threads both element kernels (stage and rhs mode) of
+// one instantiation can be launched with.
+template <class K1, class K2>
+int launch_thread_cap(K1 k1, K2 k2, int& cap) {
+  cudaFuncAttributes a, b;
+  TAG_CUDA(cudaFuncGetAttributes(&a, k1));
+  TAG_CUDA(cudaFuncGetAttributes(&b, k2));
+  cap = (std::min(a.maxThreadsPerBlock, b.maxThreadsPerBlock) / 32) * 32;
+  return TAG_OK;
+}
 
 template <class Phys>
 const typename Phys::Params& params_of(tag_handle h);
@@ -115,7 +127,7 @@ struct OpsImpl {
                      double t) {
     const int epb = h->epb > 0 ? h->epb : 4;
     const int blocks = (h->nelem + epb - 1) / epb;
-    const int threads = std::min(1024, epb * S::TPE);
+    const int threads = std::min(cap(), epb * S::TPE);
     const size_t smem = S::bytes(epb);
     const CK2N54 ck = ck2n54();
     StageArgs st{};
@@ -155,11 +167,18 @@ struct OpsImpl {
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
     TAG_CUDA(cudaFuncSetAttribute(k_element<Phys, n, kModeRhs, VOL>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    return TAG_OK;
+    return launch_thread_cap(k_element<Phys, n, kModeStage, VOL>, k_element<Phys, n, kModeRhs, VOL>,
+                             cap());
   }
+  static int& cap() {
+    static int c = 1024;
+    return c;
+  }
+  static int max_threads() { return cap(); }
   static size_t smem_bytes(int epb) { return S::bytes(epb); }
   static const Ops* get() {
-    static const Ops ops{&interface, &element, &max_speed, &init, &smem_bytes, S::TPE};
+    static const Ops ops{&interface, &element, &max_speed, &init, &smem_bytes, S::TPE,
+                         &max_threads};
     return &ops;
   }
 };
@@ -194,7 +213,7 @@ struct OpsImpl3D {
                      double) {
     const int epb = h->epb > 0 ? h->epb : 1;
     const int blocks = (h->nelem + epb - 1) / epb;
-    const int threads = std::min(1024, ((epb * S::TPE + 31) / 32) * 32);
+    const int threads = std::min(cap(), ((epb * S::TPE + 31) / 32) * 32);
     const size_t smem = S::bytes(epb);
     const CK2N54 ck = ck2n54();
     StageArgs st{};
@@ -228,11 +247,18 @@ struct OpsImpl3D {
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
     TAG_CUDA(cudaFuncSetAttribute(k_element3d<Phys, n, kModeRhs>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    return TAG_OK;
+    return launch_thread_cap(k_element3d<Phys, n, kModeStage>, k_element3d<Phys, n, kModeRhs>,
+                             cap());
   }
+  static int& cap() {
+    static int c = 1024;
+    return c;
+  }
+  static int max_threads() { return cap(); }
   static size_t smem_bytes(int epb) { return S::bytes(epb); }
   static const Ops* get() {
-    static const Ops ops{&interface, &element, &max_speed, &init, &smem_bytes, S::TPE};
+    static const Ops ops{&interface, &element, &max_speed, &init, &smem_bytes, S::TPE,
+                         &max_threads};
     return &ops;
   }
 };
@@ -304,7 +330,9 @@ int stage_sequence(tag_handle h) {
   for (int s = 0; s < 5; ++s) {
     int rc = h->ops->interface(h, h->d_u);
     if (rc) return rc;
-    rc = h->ops->element(h, kModeStage, h->d_u, nullptr, s, s == 4, 0.0);
+    // with a stage limiter the next step's CFL speed is taken from the
+    // limited state, after the last Newton solve, not inside the element kernel
+    rc = h->ops->element(h, kModeStage, h->d_u, nullptr, s, s == 4 && !h->has_limiter, 0.0);
     if (rc) return rc;
     if (h->has_limiter) {
       // stage limiter: saturation Newton solve on every node (warm start)
@@ -316,6 +344,10 @@ int stage_sequence(tag_handle h) {
       k_newton_rainy<<<(unsigned)((nodes + 255) / 256), 256, 0, h->stream>>>(h->d_u, nodes, a,
                                                                               h->d_status);
       TAG_CUDA(cudaGetLastError());
+      if (s == 4) {
+        rc = h->ops->max_speed(h, h->d_u);
+        if (rc) return rc;
+      }
     }
   }
   return TAG_OK;
@@ -357,7 +389,7 @@ int autotune(tag_handle h, const double* u) {
   const int cands[] = {1, 2, 3, 4, 6, 8, 12, 16};
   for (int c : cands) {
     if ((size_t)h->ops->smem_bytes(c) > (size_t)max_smem) continue;
-    if (c * h->ops->threads_per_element > 1024 && c > 1) continue;
+    if (c * h->ops->threads_per_element > h->ops->max_threads() && c > 1) continue;
     h->epb = c;
     double* uu = const_cast<double*>(u);
     int rc = h->ops->interface(h, uu);
@@ -779,7 +811,7 @@ int tag_set_elements_per_block(tag_handle h, int32_t epb) {
     TAG_CUDA(cudaGetDevice(&dev));
     TAG_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     if (h->ops->smem_bytes(epb) > (size_t)max_smem ||
-        (epb > 1 && epb * h->ops->threads_per_element > 1024))
+        (epb > 1 && epb * h->ops->threads_per_element > h->ops->max_threads()))
       return fail(TAG_E_INVALID, "elements per block too large for one CTA");
   }
   h->epb = epb;

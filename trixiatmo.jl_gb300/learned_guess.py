@@ -1,16 +1,19 @@
 """Learned initial guess for the rainy saturation Newton solve.
 
-A small FP32 MLP (5 -> 32 -> 32 -> 1, tanh) maps the conserved moisture state
-of a node to the temperature that solves the saturation system; the Newton
+The guess has two branches.  Where the unsaturated equilibrium is valid
+(e_s(T_unsat) / (R_v T_unsat) >= rho_moist, with T_unsat = (e_int - rho_m L) /
+(c_vd rho_d + c_vv rho_m + c_l rho_r)) it is exact and closed-form.  Elsewhere
+a small FP32 MLP (5 -> 32 -> 32 -> 1, tanh) predicts the latent-heat offset
+T* - T_unsat from (rho_dry, rho_moist, rho_rain, e_int, T_unsat), and vapour
+and cloud follow from the saturation relation at that temperature.  The Newton
 iteration (the reference's stage limiter, src/callbacks_stage/nonlinear_solve_dg2d.jl)
-then starts from that temperature and the vapour/cloud split it implies.  It
-keeps the reference's tolerance, and falls back to the plain warm start when
-the learned start has not converged after 8 updates.
+then starts from that guess with the reference's tolerance, and falls back to
+the plain warm start when it has not converged after 8 updates.
 
 Training pairs (state, converged temperature) come from the reference's Newton
-algorithm run to a tight tolerance from the warm start (tag_newton_solve_states);
+algorithm run to the tolerance from the warm start (tag_newton_solve_states);
 training and inference run in the library's own CUDA kernels (tag_mlp_train,
-k_newton_rainy).  Parameter layout: see include/trixiatmo_gpu.h (tag_set_mlp).
+k_newton_rainy).  Parameter layout: include/trixiatmo_gpu.h (tag_set_mlp).
 """
 from __future__ import annotations
 
@@ -36,15 +39,28 @@ O_OUT_SCALE = O_OUT_MEAN + 1
 _fp = ctypes.POINTER(ctypes.c_float)
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)
-C_VD, C_VV, C_L = 717.0, 1424.0, 4186.0
+C_VD, C_VV, C_L, L_VAP = 717.0, 1424.0, 4186.0, 2500000.0
+
+
+def t_unsat(u):
+    """Unsaturated-equilibrium temperature and internal energy of states u[..., 9]."""
+    rho = u[..., 0] + u[..., 1] + u[..., 2]
+    e_int = u[..., 5] - 0.5 * (u[..., 3] ** 2 + u[..., 4] ** 2) / rho
+    return (e_int - u[..., 1] * L_VAP) / (C_VD * u[..., 0] + C_VV * u[..., 1] + C_L * u[..., 2]), e_int
+
+
+def saturated(u, equations=None):
+    """Nodes whose equilibrium is saturated (the network's branch)."""
+    from .equations import CompressibleRainyEulerEquations2D
+    eq = equations or CompressibleRainyEulerEquations2D()
+    tu, _ = t_unsat(u)
+    return ~((tu > 0) & (eq.saturation_vapour_pressure(tu) / (eq.R_v * tu) >= u[..., 1]))
 
 
 def features(u):
     """Network inputs of rainy states u[..., 9] (same as mlp_inputs on the device)."""
-    rho = u[..., 0] + u[..., 1] + u[..., 2]
-    e_int = u[..., 5] - 0.5 * (u[..., 3] ** 2 + u[..., 4] ** 2) / rho
-    t_est = e_int / (C_VD * u[..., 0] + C_VV * u[..., 1] + C_L * u[..., 2])
-    return np.stack([u[..., 0], u[..., 1], u[..., 2], e_int, t_est], axis=-1).astype(np.float32)
+    tu, e_int = t_unsat(u)
+    return np.stack([u[..., 0], u[..., 1], u[..., 2], e_int, tu], axis=-1).astype(np.float32)
 
 
 def init_params(seed=0):
@@ -133,14 +149,16 @@ def sample_states(n, seed=11, equations=None):
     return MoistBubbleRainy(seed=seed)(x, 0.0, eq)
 
 
-def train_guess(n=1_000_000, epochs=20, seed=11, mode=1, tol=1e-12):
-    """Generates (state, T*) pairs with the Newton solve and trains the MLP.
-    Returns (params, stats of the data generation, per-epoch losses)."""
+def train_guess(n=1_000_000, epochs=20, seed=11, mode=1, tol=1e-12, batch=4096, lr=3e-3):
+    """Generates n (state, T*) pairs with the Newton solve and trains the MLP on
+    the offset T* - T_unsat of the saturated ones.  Returns (params, stats of
+    the data generation, per-epoch losses)."""
     u = sample_states(n, seed)
-    solved, st, _ = newton_solve_states(u.copy(), mode=mode, tol=tol, max_iterations=50)
-    ok = np.isfinite(solved[:, 8])
+    solved, st, _ = newton_solve_states(u.copy(), mode=mode, tol=tol, max_iterations=50, polish=1)
+    tu, _ = t_unsat(u)
+    ok = np.isfinite(solved[:, 8]) & saturated(u)
     X = features(u[ok])
-    T = solved[ok, 8].astype(np.float32)
+    T = (solved[ok, 8] - tu[ok]).astype(np.float32)
     p = set_normalization(init_params(seed), X, T)
-    p, losses = train(p, X, T, epochs=epochs, seed=seed)
+    p, losses = train(p, X, T, epochs=epochs, batch=batch, lr=lr, seed=seed)
     return p, st, losses
