@@ -90,6 +90,88 @@ def make_shell(tg, trees=16, layers=8, polydeg=5):
     return eq, semi
 
 
+def make_rainy(tg, nx=128, ny=64, polydeg=3):
+    """Moist bubble of the learned-guess benchmark: 128x64 elements over
+    20 km x 10 km, polydeg 3 (131,072 nodes), flux_ec_rain / flux_lax_friedrichs,
+    rain microphysics, simple slip walls in z."""
+    eq = tg.CompressibleRainyEulerEquations2D()
+    solver = tg.DGSEM(polydeg, tg.flux_lax_friedrichs,
+                      tg.VolumeIntegralFluxDifferencing(tg.flux_ec_rain))
+    mesh = tg.StructuredMesh((nx, ny), (0.0, 0.0), (LX, LZ), periodicity=(True, False))
+    bcs = {"y_neg": tg.boundary_condition_simple_slip_wall,
+           "y_pos": tg.boundary_condition_simple_slip_wall}
+    semi = tg.SemidiscretizationHyperbolic(mesh, eq, tg.MoistBubbleRainy(), solver,
+                                           source_terms=tg.source_terms_rainy,
+                                           boundary_conditions=bcs)
+    return eq, semi
+
+
+def rainy_newton_section(tg, train_states=1_000_000, epochs=40):
+    """Saturation Newton solve of the moist-bubble state at tolerance 1e-12
+    (relative), once from the plain warm start and once from the learned
+    guess; the network is trained first on GPU-generated pairs from a
+    different seed (held-out states)."""
+    import torch
+    lg = tg.learned_guess
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    params, gen, losses = lg.train_guess(n=train_states, epochs=epochs, seed=11, batch=2048)
+    t_train = time.perf_counter() - t0
+    eq, semi = make_rainy(tg)
+    u0 = semi.compute_coefficients()
+    semi.set_mlp(params)
+    semi.set_newton(mode=1, tol=1e-12, max_iterations=30, polish=1)
+    res = {}
+    for name, learned in (("plain", False), ("learned", True)):
+        best = 1e30
+        for _ in range(3):
+            semi.set_state(u0)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            st, it = semi.newton_solve(learned=learned)
+            best = min(best, time.perf_counter() - t1)
+        res[name] = (st, it, semi.get_state(), best)
+    same = np.all(res["plain"][2].reshape(-1, 9) == res["learned"][2].reshape(-1, 9), axis=1)
+    ip, il = res["plain"][1].mean(), res["learned"][1].mean()
+    sat = lg.saturated(u0.reshape(-1, 9))
+    out = {
+        "workload": "rainy moist bubble 128x64 elements, polydeg 3, 131072 nodes; "
+                    "tolerance 1e-12 relative; canonical finish (snap + 1 update) on both",
+        "iters_per_node_plain": ip, "iters_per_node_learned": il, "reduction": ip / il,
+        "iters_saturated_nodes": {"plain": float(res["plain"][1][sat].mean()),
+                                  "learned": float(res["learned"][1][sat].mean()),
+                                  "fraction": float(sat.mean())},
+        "bitwise_equal_fraction": float(same.mean()),
+        "fallbacks": int(res["learned"][0]["fallbacks"]),
+        "not_converged": int(res["plain"][0]["not_converged"] + res["learned"][0]["not_converged"]),
+        "solve_ms_plain": res["plain"][3] * 1e3, "solve_ms_learned": res["learned"][3] * 1e3,
+        "training": {"states": train_states, "epochs": epochs,
+                     "seconds_incl_generation": t_train, "loss_first": float(losses[0]),
+                     "loss_last": float(losses[-1])},
+    }
+    semi.close()
+    return out
+
+
+def sequential_member_rate(tg, steps):
+    """DOF·stage/s of one ensemble member run alone (the rate of running the
+    members one by one on the same GPU)."""
+    import torch
+    eq, semi = make_ensemble(tg, 1)
+    semi.set_state(semi.compute_coefficients())
+    t = semi.rk_steps(3, cfl=1.0, t=0.0)
+    stream = torch.cuda.ExternalStream(semi.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    t = semi.rk_steps(steps, cfl=1.0, t=t)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    rate = semi.ndofs * 5 * steps / (e0.elapsed_time(e1) * 1e-3)
+    semi.close()
+    return rate
+
+
 def flops_per_element_launch_3d(n, nelem):
     """FP64 flops of one 3D element-kernel launch, counted from the reference
     formulas: per symmetric pair 120 (flux_ranocha 3D with its two logarithmic
@@ -412,6 +494,12 @@ def run_ours(args):
         }
         if cpu is not None:
             line["cpu_baseline"] = cpu
+        if args.workload == "ensemble":
+            seq = sequential_member_rate(tg, args.steps)
+            line["ensemble_vs_sequential"] = {"sequential_member_rate": seq,
+                                              "speedup": value / world / seq}
+        if world == 1 and not args.no_rainy:
+            line["rainy_newton"] = rainy_newton_section(tg)
         print(json.dumps(line))
     semi.close()
     if world > 1:
@@ -436,6 +524,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=8)
     ap.add_argument("--ref-members", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-rainy", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
