@@ -71,6 +71,21 @@ def lib():
         L.orc_euler3d_ck_steps.restype = ctypes.c_double
         L.orc_euler3d_ck_steps.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_int, ctypes.c_double]
+        L.orc_moist_create.restype = ctypes.c_void_p
+        L.orc_moist_create.argtypes = ([ctypes.c_int] * 3 + [ctypes.c_double] * 4 +
+                                       [ctypes.c_int] * 6 + [ctypes.c_double] * 2 + [ctypes.c_int])
+        L.orc_moist_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_moist_initial_condition.argtypes = [ctypes.c_void_p, ctypes.c_double, _dp]
+        L.orc_moist_errors.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, _dp, _dp]
+        L.orc_moist_rhs.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double]
+        L.orc_moist_max_dt.restype = ctypes.c_double
+        L.orc_moist_max_dt.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_moist_ck_steps.restype = ctypes.c_double
+        L.orc_moist_ck_steps.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double,
+                                         ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                         ctypes.c_double]
+        L.orc_moist_flux_chandrashekar.argtypes = [_dp, _dp, _dp, _dp]
+        L.orc_moist_flux.argtypes = [_dp, _dp, _dp]
         L.orc_rainy_create.restype = ctypes.c_void_p
         L.orc_rainy_create.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] * 4 + [ctypes.c_int] * 4
         L.orc_rainy_geometry.argtypes = [ctypes.c_void_p, _dp]
@@ -209,6 +224,69 @@ class Euler3D:
 
     def ck_steps(self, u, k, t, cfl, nsteps, fixed_dt=0.0):
         return lib().orc_euler3d_ck_steps(self.h, _p(u), _p(k), t, cfl, nsteps, fixed_dt)
+
+
+class Moist2D:
+    """Moist Euler on a StructuredMesh rectangle.  surface_kind 0: FluxLMARS(c),
+    1: flux_lax_friedrichs, 2: flux_chandrashekar; source_kind 0: none,
+    1: geopotential, 2: moist bubble (geopotential + phase change), 3 / 4: the
+    dry / moist convergence tests; wall_kind 1: StructuredMesh slip wall,
+    2: outward normal (P4estMesh); ic_kind 0: gemein bubble (dry, v1 = 20),
+    1 / 2: dry / moist convergence test."""
+
+    nv = 6
+
+    def __init__(self, polydeg, nx, ny, x0, x1, y0, y1, periodic_x=True, periodic_y=False,
+                 weak_form=False, surface_kind=0, source_kind=1, wall_kind=1, c_lmars=360.0,
+                 gravity=9.80616, ic_kind=0):
+        self.n = polydeg + 1
+        self.nelem = nx * ny
+        self.h = lib().orc_moist_create(polydeg, nx, ny, x0, x1, y0, y1, int(periodic_x),
+                                        int(periodic_y), int(weak_form), int(surface_kind),
+                                        int(source_kind), int(wall_kind), c_lmars, gravity,
+                                        int(ic_kind))
+
+    def initial_condition(self, t=0.0):
+        u = np.zeros((self.nelem, self.n, self.n, 6))
+        lib().orc_moist_initial_condition(self.h, t, _p(u))
+        return u
+
+    def errors(self, u, t):
+        l2, linf = np.zeros(6), np.zeros(6)
+        lib().orc_moist_errors(self.h, _p(np.ascontiguousarray(u)), t, _p(l2), _p(linf))
+        return l2, linf
+
+    def rhs(self, u, t=0.0):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        du = np.zeros_like(u)
+        lib().orc_moist_rhs(self.h, _p(u), _p(du), t)
+        return du
+
+    def max_dt(self, u):
+        return lib().orc_moist_max_dt(self.h, _p(np.ascontiguousarray(u)))
+
+    def ck_steps(self, u, k, t, cfl, nsteps, fixed_dt=0.0, t_end=0.0):
+        return lib().orc_moist_ck_steps(self.h, _p(u), _p(k), t, cfl, nsteps, fixed_dt, t_end)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_moist_destroy(self.h)
+            self.h = None
+
+
+def moist_flux_chandrashekar(ul, ur, n):
+    f = np.zeros(6)
+    lib().orc_moist_flux_chandrashekar(_p(np.ascontiguousarray(ul, dtype=np.float64)),
+                                       _p(np.ascontiguousarray(ur, dtype=np.float64)),
+                                       _p(np.ascontiguousarray(n, dtype=np.float64)), _p(f))
+    return f
+
+
+def moist_flux(u, n):
+    f = np.zeros(6)
+    lib().orc_moist_flux(_p(np.ascontiguousarray(u, dtype=np.float64)),
+                         _p(np.ascontiguousarray(n, dtype=np.float64)), _p(f))
+    return f
 
 
 class Rainy2D:

@@ -18,6 +18,7 @@
 #include "orc_dg3d.hpp"
 #include "orc_euler_energy_2d.hpp"
 #include "orc_euler_energy_3d.hpp"
+#include "orc_moist_2d.hpp"
 #include "orc_rainy_2d.hpp"
 #include "orc_time.hpp"
 
@@ -311,7 +312,133 @@ inline int newton_node(const RainyEuler2D& eq, const RainyEuler2D::State& u, dou
   return it;
 }
 
+// CompressibleMoistEulerEquations2D on a StructuredMesh.  Volume: flux
+// differencing with flux_chandrashekar or the weak form; surface flux 0:
+// FluxLMARS(c), 1: flux_lax_friedrichs, 2: flux_chandrashekar; sources 0: none,
+// 1: source_terms_geopotential, 2: source_terms_moist_bubble, 3/4: the dry /
+// moist convergence tests' sources.
+struct MoistPhys {
+  using State = MoistEuler2D::State;
+  static constexpr int nv = 6;
+  static constexpr bool has_noncons = false;
+  static constexpr bool has_sources = true;
+  MoistEuler2D eq;
+  int surface_kind = 0, source_kind = 1;
+  double c_lmars = 360.0;
+  State volume_flux(const State& a, const State& b, const double* n) const {
+    return eq.flux_chandrashekar(a, b, n);
+  }
+  State volume_noncons(const State&, const State&, const double*) const { return State{}; }
+  State surface_flux(const State& a, const State& b, const double* n) const {
+    if (surface_kind == 1) return eq.flux_llf(a, b, n);
+    if (surface_kind == 2) return eq.flux_chandrashekar(a, b, n);
+    return eq.flux_lmars(a, b, n, c_lmars);
+  }
+  State surface_noncons(const State&, const State&, const double*) const { return State{}; }
+  State bc_structured(const State& ui, const double* n, int direction) const {
+    return eq.slip_wall_structured(ui, n, direction);
+  }
+  State bc_normal(const State& ui, const double* n) const { return eq.slip_wall(ui, n); }
+  State flux(const State& u, const double* n) const { return eq.flux(u, n); }
+  State source(const State& u, const double* x, double t) const {
+    switch (source_kind) {
+      case 1: return eq.source_geopotential(u);
+      case 2: return eq.source_moist_bubble(u);
+      case 3: return eq.source_convergence_dry(u, x, t);
+      case 4: return eq.source_convergence_moist(u, x, t);
+      default: return State{};
+    }
+  }
+  void max_abs_speeds(const State& u, double& l1, double& l2) const { eq.max_abs_speeds(u, l1, l2); }
+};
+
+struct MoistCase {
+  MoistPhys phys;
+  Basis basis;
+  Mesh2D mesh;
+  std::unique_ptr<DG2D<MoistPhys>> dg;
+  int ic_kind = 0;
+  size_t ndofs() const { return (size_t)mesh.nelem * basis.n * basis.n; }
+};
+
+// Initial states of the moist tests.  kind 0: the warm bubble of
+// examples/euler/dry_air/buoyancy/elixir_gemein_bubble.jl:20-51 (v1 = 20,
+// no moisture); 1 / 2: the dry / moist convergence tests (:173-200, :244-272).
+inline MoistEuler2D::State ic_moist(const MoistEuler2D& eq, int kind, const double* x, double t) {
+  if (kind == 1) return eq.ic_convergence_dry(x, t);
+  if (kind == 2) return eq.ic_convergence_moist(x, t);
+  const double xc = 10000.0, zc = 2000.0, rc = 2000.0, theta_ref = 300.0;
+  const double r = std::sqrt((x[0] - xc) * (x[0] - xc) + (x[1] - zc) * (x[1] - zc));
+  double dth = 0.0;
+  if (r <= rc) {
+    const double c = std::cos(3.14159265358979323846 * (0.5 * r / rc));
+    dth = 2.0 * c * c;
+  }
+  const double theta = theta_ref + dth;
+  const double p = eq.p_0 * std::pow(1.0 - eq.kappa * eq.g * x[1] / (eq.R_d * theta_ref),
+                                     eq.c_pd / eq.R_d);
+  const double rho = p / (std::pow(p / eq.p_0, eq.kappa) * eq.R_d * theta);
+  const double T = p / (eq.R_d * rho);
+  const double v1 = 20.0;
+  return {rho, rho * v1, 0.0, rho * eq.c_vd * T + 0.5 * rho * v1 * v1, 0.0, 0.0};
+}
+
+// l2 / linf errors of a 2D StructuredMesh solution against exact(x) on the
+// analysis nodes of degree 2N (Trixi's AnalysisCallback, l2 normalised by the
+// domain volume).
+template <int NVAR, class Exact>
+void errors_2d(const Basis& b, const Mesh2D& mesh, const double* u, Exact&& exact, double* l2,
+               double* linf) {
+  const int n = b.n;
+  const Basis a = make_lgl_basis(2 * (n - 1));
+  const int na = a.n;
+  const std::vector<double> V = interpolation_matrix(b.x, a.x);
+  for (int v = 0; v < NVAR; ++v) { l2[v] = 0.0; linf[v] = 0.0; }
+  double vol = 0.0;
+  constexpr int K = NVAR + 3;
+  std::vector<double> fu(n * n * K), tmp(na * n * K), fa(na * na * K);
+  for (int e = 0; e < mesh.nelem; ++e) {
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        const size_t q = (size_t)(e * n + j) * n + i;
+        for (int v = 0; v < NVAR; ++v) fu[(j * n + i) * K + v] = u[q * NVAR + v];
+        fu[(j * n + i) * K + NVAR] = mesh.xy[q * 2];
+        fu[(j * n + i) * K + NVAR + 1] = mesh.xy[q * 2 + 1];
+        fu[(j * n + i) * K + NVAR + 2] = 1.0 / mesh.invJ[q];
+      }
+    for (int j = 0; j < n; ++j)
+      for (int ia = 0; ia < na; ++ia)
+        for (int v = 0; v < K; ++v) {
+          double s = 0;
+          for (int i = 0; i < n; ++i) s += V[ia * n + i] * fu[(j * n + i) * K + v];
+          tmp[(j * na + ia) * K + v] = s;
+        }
+    for (int ja = 0; ja < na; ++ja)
+      for (int ia = 0; ia < na; ++ia)
+        for (int v = 0; v < K; ++v) {
+          double s = 0;
+          for (int j = 0; j < n; ++j) s += V[ja * n + j] * tmp[(j * na + ia) * K + v];
+          fa[(ja * na + ia) * K + v] = s;
+        }
+    for (int ja = 0; ja < na; ++ja)
+      for (int ia = 0; ia < na; ++ia) {
+        const double* f = &fa[(ja * na + ia) * K];
+        const double x[2] = {f[NVAR], f[NVAR + 1]};
+        const auto ex = exact(x);
+        const double wJ = a.w[ia] * a.w[ja] * f[NVAR + 2];
+        for (int v = 0; v < NVAR; ++v) {
+          const double d = ex[v] - f[v];
+          l2[v] += d * d * wJ;
+          linf[v] = std::max(linf[v], std::fabs(d));
+        }
+        vol += wJ;
+      }
+  }
+  for (int v = 0; v < NVAR; ++v) l2[v] = std::sqrt(l2[v] / vol);
+}
+
 }  // namespace orc
+
 
 using namespace orc;
 
@@ -720,5 +847,84 @@ void orc_rainy_flux(const double* u, const double* n, double* f) {
 }
 
 double orc_rainy_saturation_vapour_pressure(double T) { return RainyEuler2D().e_s(T); }
+
+// ---- 2D moist Euler (CompressibleMoistEulerEquations2D) -------------------
+// wall_kind: 1 StructuredMesh slip wall semantics, 2 outward-normal (P4estMesh).
+void* orc_moist_create(int polydeg, int nx, int ny, double x0, double x1, double y0, double y1,
+                       int periodic_x, int periodic_y, int weak_form, int surface_kind,
+                       int source_kind, int wall_kind, double c_lmars, double gravity,
+                       int ic_kind) {
+  auto* c = new MoistCase();
+  c->phys.eq.init(1004.0, 717.0, 1885.0, 1424.0, gravity);
+  c->phys.surface_kind = surface_kind;
+  c->phys.source_kind = source_kind;
+  c->phys.c_lmars = c_lmars;
+  c->ic_kind = ic_kind;
+  c->basis = make_lgl_basis(polydeg);
+  c->mesh = structured_rectangle(c->basis, nx, ny, x0, x1, y0, y1, periodic_x != 0,
+                                 periodic_y != 0, wall_kind);
+  c->dg.reset(new DG2D<MoistPhys>(c->phys, c->basis, c->mesh));
+  c->dg->weak_form = weak_form != 0;
+  return c;
+}
+
+void orc_moist_destroy(void* h) { delete static_cast<MoistCase*>(h); }
+
+void orc_moist_initial_condition(void* h, double t, double* u) {
+  auto* c = static_cast<MoistCase*>(h);
+  const size_t nd = c->ndofs();
+  for (size_t q = 0; q < nd; ++q) {
+    const auto s = ic_moist(c->phys.eq, c->ic_kind, &c->mesh.xy[q * 2], t);
+    for (int v = 0; v < 6; ++v) u[q * 6 + v] = s[v];
+  }
+}
+
+void orc_moist_errors(void* h, const double* u, double t, double* l2, double* linf) {
+  auto* c = static_cast<MoistCase*>(h);
+  errors_2d<6>(c->basis, c->mesh, u,
+               [&](const double* x) { return ic_moist(c->phys.eq, c->ic_kind, x, t); }, l2, linf);
+}
+
+void orc_moist_rhs(void* h, const double* u, double* du, double t) {
+  static_cast<MoistCase*>(h)->dg->rhs(u, du, t);
+}
+
+double orc_moist_max_dt(void* h, const double* u) { return static_cast<MoistCase*>(h)->dg->max_dt(u); }
+
+// CK2N54 steps at cfl (or fixed_dt), the last one shortened to land on t_end
+// (> 0) as OrdinaryDiffEq does; returns the new time.
+double orc_moist_ck_steps(void* h, double* u, double* k, double t, double cfl, int nsteps,
+                          double fixed_dt, double t_end) {
+  auto* c = static_cast<MoistCase*>(h);
+  const size_t N = c->ndofs() * 6;
+  std::vector<double> du(N);
+  for (int s = 0; s < nsteps; ++s) {
+    if (t_end > 0 && t >= t_end) break;
+    double dt = fixed_dt > 0 ? fixed_dt : cfl * c->dg->max_dt(u);
+    if (t_end > 0 && t + dt > t_end) dt = t_end - t;
+    ck2n54_step([&](const double* uu, double* dd, double tt) { c->dg->rhs(uu, dd, tt); }, u, k,
+                du.data(), N, t, dt);
+    t += dt;
+  }
+  return t;
+}
+
+void orc_moist_flux_chandrashekar(const double* ul, const double* ur, const double* n, double* f) {
+  MoistEuler2D eq;
+  eq.init(1004.0, 717.0, 1885.0, 1424.0, 9.80616);
+  MoistEuler2D::State a, b;
+  for (int v = 0; v < 6; ++v) { a[v] = ul[v]; b[v] = ur[v]; }
+  const auto r = eq.flux_chandrashekar(a, b, n);
+  for (int v = 0; v < 6; ++v) f[v] = r[v];
+}
+
+void orc_moist_flux(const double* u, const double* n, double* f) {
+  MoistEuler2D eq;
+  eq.init(1004.0, 717.0, 1885.0, 1424.0, 9.80616);
+  MoistEuler2D::State a;
+  for (int v = 0; v < 6; ++v) a[v] = u[v];
+  const auto r = eq.flux(a, n);
+  for (int v = 0; v < 6; ++v) f[v] = r[v];
+}
 
 }  // extern "C"
