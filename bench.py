@@ -508,7 +508,8 @@ def run_ours(args):
 
 # DRAM bytes per DOF of the element kernel from ncu captures (read + write),
 # used to report `traffic` for the full-size launch.
-TRAFFIC_PER_DOF = {}
+TRAFFIC_PER_DOF = {"shell": 282.45,      # k_element3d, stage mode, full shell
+                   "ensemble": 205.27}    # k_element 2D, stage mode, 128-member ensemble
 
 
 def main():

@@ -56,15 +56,22 @@ extern "C" {
 #define TAG_EQ_EULER_ENERGY_2D 1 /* CompressibleEulerEnergyEquationsWithGravity2D */
 #define TAG_EQ_EULER_ENERGY_3D 2 /* CompressibleEulerEnergyEquationsWithGravity3D + source_terms_coriolis */
 #define TAG_EQ_RAINY_2D 3        /* CompressibleRainyEulerEquations2D (+ Newton stage limiter) */
+#define TAG_EQ_MOIST_EULER_2D 4  /* CompressibleMoistEulerEquations2D                             */
 
 #define TAG_VF_RANOCHA_WARUSZEWSKI 1 /* (flux_ranocha, flux_nonconservative_waruszewski_etal) */
 #define TAG_VF_EC_RAIN 2             /* VolumeIntegralFluxDifferencing(flux_ec_rain)    */
 #define TAG_VF_WEAK_FORM 3           /* VolumeIntegralWeakForm (physical flux)          */
+#define TAG_VF_CHANDRASHEKAR 4       /* VolumeIntegralFluxDifferencing(flux_chandrashekar), moist */
 #define TAG_SF_LMARS 1               /* (FluxLMARS(c), flux_zero)                       */
 #define TAG_SF_LAX_FRIEDRICHS 2      /* flux_lax_friedrichs (max_abs_speed_naive)       */
+#define TAG_SF_CHANDRASHEKAR 3       /* flux_chandrashekar as surface flux (moist)      */
 
 #define TAG_SRC_RAINY 1              /* source_terms_rainy (microphysics + gravity)     */
 #define TAG_SRC_RAINY_CONVERGENCE 2  /* manufactured source of the rainy convergence test */
+#define TAG_SRC_GEOPOTENTIAL 3       /* source_terms_geopotential (moist)               */
+#define TAG_SRC_MOIST_BUBBLE 4       /* source_terms_moist_bubble: geopotential + phase change */
+#define TAG_SRC_MOIST_CONVERGENCE_DRY 5 /* source_terms_convergence_test_dry (moist equations) */
+#define TAG_SRC_MOIST_CONVERGENCE 6  /* source_terms_convergence_test_moist            */
 
 #define TAG_BC_SLIP_WALL_STRUCTURED 1 /* boundary_condition_slip_wall reached from a StructuredMesh */
 #define TAG_BC_SLIP_WALL_NORMAL 2     /* boundary_condition_slip_wall reached from a P4estMesh      */
@@ -102,7 +109,9 @@ typedef struct {
   double params[8];  /* EULER_ENERGY_2D: c_p, c_v, gravity, LMARS speed of sound;
                         EULER_ENERGY_3D: the same, then the Coriolis angular
                         velocity (0 disables the source);
-                        RAINY_2D: params[0] = TAG_SRC_* source kind */
+                        RAINY_2D: params[0] = TAG_SRC_* source kind;
+                        MOIST_EULER_2D: c_pd, c_vd, c_pv, c_vv, gravity, LMARS
+                        speed of sound, TAG_SRC_* source kind (0: none) */
 } tag_config;
 
 /* Creates a handle on the current CUDA device.  Replaces the cache build of

@@ -1,0 +1,167 @@
+"""GPU parity of the moist-Euler path (flux_chandrashekar / weak form, FluxLMARS /
+flux_lax_friedrichs / flux_chandrashekar surface fluxes, pressure-Riemann slip
+walls, geopotential, phase-change and manufactured sources) against the CPU
+oracle, and the reference's three moist goldens reproduced with every stage on
+the GPU.  All calls go through the C ABI."""
+import numpy as np
+import pytest
+
+from test_oracle_moist import CASES, check_golden
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12
+CP = dict(c_pd=1004, c_vd=717, c_pv=1885, c_vv=1424)
+
+
+def max_norm_rel(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+def moist_state(eq, u, seed, vel=15.0):
+    """Seeded moisture and velocities on top of a dry state, keeping T."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    out = u.copy()
+    rho = u[..., 0]
+    _, T = eq.get_current_condition(u)
+    qv = rng.uniform(1e-3, 1.5e-2, rho.shape)
+    ql = rng.uniform(0.0, 2e-3, rho.shape)
+    v = vel * rng.uniform(-1, 1, rho.shape + (2,))
+    qd = 1.0 - qv - ql
+    out[..., 1] = rho * v[..., 0]
+    out[..., 2] = rho * v[..., 1]
+    out[..., 3] = (rho * (qd * eq.c_vd + qv * eq.c_vv + ql * eq.c_pl) * T + rho * qv * eq.L_00 +
+                   0.5 * rho * (v ** 2).sum(-1))
+    out[..., 4] = rho * qv
+    out[..., 5] = rho * ql
+    return out
+
+
+def bubble_semi(tg, polydeg, nx=8, ny=6, surface="lmars", p4est=False, source=None):
+    eq = tg.CompressibleMoistEulerEquations2D(**CP, gravity=9.80616)
+    sf = {"lmars": tg.FluxLMARS(360.0), "llf": tg.flux_lax_friedrichs,
+          "ec": tg.flux_chandrashekar}[surface]
+    solver = tg.DGSEM(polydeg, sf, tg.VolumeIntegralFluxDifferencing(tg.flux_chandrashekar))
+    if p4est:
+        mesh = tg.P4estMesh((2, 2), polydeg=1, coordinates_min=(0.0, -5000.0),
+                            coordinates_max=(20000.0, 15000.0), initial_refinement_level=2,
+                            periodicity=(True, False))
+    else:
+        mesh = tg.StructuredMesh((nx, ny), (0.0, -5000.0), (20000.0, 15000.0),
+                                 periodicity=(True, False))
+    bcs = {"y_neg": tg.boundary_condition_slip_wall, "y_pos": tg.boundary_condition_slip_wall}
+    semi = tg.SemidiscretizationHyperbolic(mesh, eq, tg.initial_condition_gemein_bubble, solver,
+                                           boundary_conditions=bcs,
+                                           source_terms=source or tg.source_terms_geopotential)
+    return eq, mesh, semi
+
+
+@pytest.mark.parametrize("polydeg", [2, 3, 4, 5])
+@pytest.mark.parametrize("surface,source", [("lmars", "geopotential"), ("llf", "moist_bubble"),
+                                            ("ec", "moist_bubble")])
+def test_moist_rhs_matches_oracle(tg, orc, gpu_lib, polydeg, surface, source):
+    src = {"geopotential": tg.source_terms_geopotential,
+           "moist_bubble": tg.source_terms_moist_bubble}[source]
+    eq, mesh, semi = bubble_semi(tg, polydeg, surface=surface, source=src)
+    u = moist_state(eq, semi.compute_coefficients(), seed=polydeg)
+    du = semi.rhs(u)
+    c = orc.Moist2D(polydeg, 8, 6, 0.0, 20000.0, -5000.0, 15000.0, True, False,
+                    surface_kind={"lmars": 0, "llf": 1, "ec": 2}[surface],
+                    source_kind={"geopotential": 1, "moist_bubble": 2}[source], wall_kind=1)
+    du_ref = c.rhs(u)
+    assert max_norm_rel(du, du_ref) <= RTOL, max_norm_rel(du, du_ref)
+    for v in range(6):
+        s = np.abs(du_ref[..., v]).max()
+        assert np.abs(du[..., v] - du_ref[..., v]).max() <= 1e-11 * s, v
+    semi.close()
+
+
+def test_moist_rhs_p4est_walls_and_order(tg, orc, gpu_lib):
+    """P4estMesh element order and outward-normal slip walls."""
+    eq, mesh, semi = bubble_semi(tg, 3, p4est=True)
+    u = moist_state(eq, semi.compute_coefficients(), seed=11)
+    du = semi.rhs(u)
+    c = orc.Moist2D(3, 8, 8, 0.0, 20000.0, -5000.0, 15000.0, True, False, surface_kind=0,
+                    source_kind=1, wall_kind=2)
+    du_ref = c.rhs(u[mesh.inv])
+    assert max_norm_rel(du[mesh.inv], du_ref) <= RTOL
+    semi.close()
+
+
+def test_moist_weak_form_and_manufactured_sources(tg, orc, gpu_lib):
+    for kind, src, ic, sf, weak in (
+            (3, tg.source_terms_convergence_test_dry, tg.initial_condition_convergence_test_dry,
+             tg.flux_lax_friedrichs, True),
+            (4, tg.source_terms_convergence_test_moist,
+             tg.initial_condition_convergence_test_moist, tg.flux_chandrashekar, False)):
+        g = 0.0 if kind == 3 else 9.80616
+        eq = tg.CompressibleMoistEulerEquations2D(**CP, gravity=g)
+        vi = (tg.VolumeIntegralWeakForm() if weak
+              else tg.VolumeIntegralFluxDifferencing(tg.flux_chandrashekar))
+        mesh = tg.StructuredMesh((6, 5), (0.0, 0.0), (2.0, 2.0), periodicity=(True, True))
+        semi = tg.SemidiscretizationHyperbolic(mesh, eq, ic, tg.DGSEM(3, sf, vi), source_terms=src)
+        u = semi.compute_coefficients()
+        rng = np.random.default_rng(kind)
+        u = u * (1.0 + 1e-3 * rng.standard_normal(u.shape))
+        c = orc.Moist2D(3, 6, 5, 0.0, 2.0, 0.0, 2.0, True, True, weak_form=weak,
+                        surface_kind=1 if kind == 3 else 2, source_kind=kind, gravity=g,
+                        ic_kind=kind - 2)
+        c0 = orc.Moist2D(3, 6, 5, 0.0, 2.0, 0.0, 2.0, True, True, weak_form=weak,
+                         surface_kind=1 if kind == 3 else 2, source_kind=0, gravity=g)
+        for t in (0.0, 0.3):
+            du = semi.rhs(u, t)
+            du_ref = c.rhs(u, t)
+            scale = np.abs(c0.rhs(u, t)).max()
+            assert np.abs(du - du_ref).max() <= RTOL * scale, (kind, t)
+        semi.close()
+
+
+def _gpu_golden_run(tg, semi, cfl, t_end):
+    semi.set_state(semi.compute_coefficients())
+    t = 0.0
+    while t < t_end - 1e-15:
+        dt = cfl * semi.max_dt()
+        if t + dt >= t_end:
+            t = semi.rk_steps(1, fixed_dt=t_end - t, t=t)
+        else:
+            t = semi.rk_steps(1, cfl=cfl, t=t)
+    assert abs(t - t_end) < 1e-13
+    return semi.get_state(), t
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_gpu_reproduces_moist_golden(tg, orc, gpu_lib, name):
+    kw, cfl, golden = CASES[name]
+    g = kw.get("gravity", 9.80616)
+    eq = tg.CompressibleMoistEulerEquations2D(**CP, gravity=g)
+    if name == "dry_bubble":
+        mesh = tg.P4estMesh((2, 2), polydeg=1, coordinates_min=(0.0, -5000.0),
+                            coordinates_max=(20000.0, 15000.0), initial_refinement_level=5,
+                            periodicity=(True, False))
+        solver = tg.DGSEM(4, tg.FluxLMARS(360.0),
+                          tg.VolumeIntegralFluxDifferencing(tg.flux_chandrashekar))
+        semi = tg.SemidiscretizationHyperbolic(
+            mesh, eq, tg.initial_condition_gemein_bubble, solver,
+            boundary_conditions={"y_neg": tg.boundary_condition_slip_wall,
+                                 "y_pos": tg.boundary_condition_slip_wall},
+            source_terms=tg.source_terms_geopotential)
+    elif name == "moist_source":
+        mesh = tg.StructuredMesh((10, 8), (0.0, 0.0), (2.0, 2.0), periodicity=(True, True))
+        solver = tg.DGSEM(3, tg.flux_chandrashekar,
+                          tg.VolumeIntegralFluxDifferencing(tg.flux_chandrashekar))
+        semi = tg.SemidiscretizationHyperbolic(
+            mesh, eq, tg.initial_condition_convergence_test_moist, solver,
+            source_terms=tg.source_terms_convergence_test_moist)
+    else:
+        mesh = tg.StructuredMesh((10, 8), (0.0, 0.0), (2.0, 2.0), periodicity=(True, True))
+        solver = tg.DGSEM(3, tg.flux_lax_friedrichs)
+        semi = tg.SemidiscretizationHyperbolic(
+            mesh, eq, tg.initial_condition_convergence_test_dry, solver,
+            source_terms=tg.source_terms_convergence_test_dry)
+    u, t = _gpu_golden_run(tg, semi, cfl, 0.1)
+    if name == "dry_bubble":
+        u = u[mesh.inv]
+    c = orc.Moist2D(**kw)
+    l2, linf = c.errors(u, t)
+    check_golden(l2, linf, golden, 5e-8 if name == "dry_bubble" else 1.4901161193847656e-8)
+    semi.close()

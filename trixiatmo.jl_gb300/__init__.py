@@ -16,13 +16,19 @@ from .equations import (CompressibleEulerEnergyEquationsWithGravity2D,
                         source_terms_convergence_test_rainy, source_terms_rainy, FluxLMARS,
                         VolumeIntegralFluxDifferencing, boundary_condition_periodic,
                         boundary_condition_slip_wall, flux_nonconservative_waruszewski_etal,
-                        flux_ranocha, flux_zero, speed_of_sound_isothermal)
+                        flux_ranocha, flux_zero, speed_of_sound_isothermal,
+                        CompressibleMoistEulerEquations2D, flux_chandrashekar,
+                        source_terms_geopotential, source_terms_moist_bubble,
+                        source_terms_convergence_test_dry, source_terms_convergence_test_moist)
 from .initial_conditions import (EARTH_GRAVITATIONAL_ACCELERATION, EARTH_RADIUS,
                                  EARTH_ROTATION_RATE, IsothermalShell, MoistBubbleRainy,
                                  WarmBubble, initial_condition_convergence_test_rainy,
                                  initial_condition_baroclinic_instability,
-                                 initial_condition_gravity_waves, seeded_perturbation)
-from .meshes import StructuredMesh
+                                 initial_condition_gravity_waves, seeded_perturbation,
+                                 initial_condition_gemein_bubble,
+                                 initial_condition_convergence_test_dry,
+                                 initial_condition_convergence_test_moist)
+from .meshes import P4estMesh, StructuredMesh
 from .meshes3d import P4estMeshCubedSphereTopography
 from .semidiscretization import (DGSEM, SemidiscretizationEnsemble, SemidiscretizationHyperbolic,
                                  fp64_peak, source_terms_coriolis)
@@ -40,4 +46,9 @@ __all__ = [
     "VolumeIntegralWeakForm", "boundary_condition_simple_slip_wall", "flux_ec_rain",
     "flux_lax_friedrichs", "source_terms_convergence_test_rainy", "source_terms_rainy",
     "MoistBubbleRainy", "initial_condition_convergence_test_rainy", "learned_guess",
+    "CompressibleMoistEulerEquations2D", "flux_chandrashekar", "source_terms_geopotential",
+    "source_terms_moist_bubble", "source_terms_convergence_test_dry",
+    "source_terms_convergence_test_moist", "initial_condition_gemein_bubble",
+    "initial_condition_convergence_test_dry", "initial_condition_convergence_test_moist",
+    "P4estMesh",
 ]

@@ -31,6 +31,13 @@ TAG_SF_LAX_FRIEDRICHS = 2
 TAG_SRC_RAINY = 1
 TAG_SRC_RAINY_CONVERGENCE = 2
 TAG_BC_SIMPLE_SLIP_WALL = 3
+TAG_EQ_MOIST_EULER_2D = 4
+TAG_VF_CHANDRASHEKAR = 4
+TAG_SF_CHANDRASHEKAR = 3
+TAG_SRC_GEOPOTENTIAL = 3
+TAG_SRC_MOIST_BUBBLE = 4
+TAG_SRC_MOIST_CONVERGENCE_DRY = 5
+TAG_SRC_MOIST_CONVERGENCE = 6
 MLP_PARAMS = 1293
 MLP_TRAINABLE = 1281
 TAG_VF_RANOCHA_WARUSZEWSKI = 1

@@ -14,6 +14,7 @@
 #include "newton_rainy.cuh"
 #include "phys_euler_energy_2d.cuh"
 #include "phys_euler_energy_3d.cuh"
+#include "phys_moist_2d.cuh"
 #include "phys_rainy_2d.cuh"
 
 using namespace tag;
@@ -46,6 +47,7 @@ struct tag_handle_s {
   PhysEnergy2D::Params p_energy{};
   PhysEnergy3D::Params p_energy3d{};
   PhysRainy2D::Params p_rainy{};
+  PhysMoist2D::Params p_moist{};
   // rainy: Newton stage limiter settings, MLP parameters, statistics counters
   bool has_limiter = false;
   NewtonArgs newton{0, 20, 0, 0, 8, 1e-9, nullptr, nullptr, nullptr};
@@ -108,6 +110,10 @@ const PhysEnergy3D::Params& params_of<PhysEnergy3D>(tag_handle h) {
 template <>
 const PhysRainy2D::Params& params_of<PhysRainy2D>(tag_handle h) {
   return h->p_rainy;
+}
+template <>
+const PhysMoist2D::Params& params_of<PhysMoist2D>(tag_handle h) {
+  return h->p_moist;
 }
 
 template <class Phys, int n, int VOL = kVolFluxDiff>
@@ -427,6 +433,57 @@ __global__ void k_fp64_probe(double* out, int iters, double seed) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
 }
 
+// Supported (equations, volume flux, surface flux, source) combinations;
+// returns the reason a configuration is rejected, or null.
+const char* check_equations(const tag_config* cfg) {
+  const int vf = cfg->volume_flux, sf = cfg->surface_flux;
+  switch (cfg->equations) {
+    case TAG_EQ_EULER_ENERGY_2D:
+    case TAG_EQ_EULER_ENERGY_3D:
+      if (vf != TAG_VF_RANOCHA_WARUSZEWSKI || sf != TAG_SF_LMARS)
+        return "unsupported flux combination";
+      return nullptr;
+    case TAG_EQ_RAINY_2D: {
+      if ((vf != TAG_VF_EC_RAIN && vf != TAG_VF_WEAK_FORM) || sf != TAG_SF_LAX_FRIEDRICHS)
+        return "unsupported flux combination for the rainy equations";
+      const double k = cfg->params[0];
+      if (k != TAG_SRC_RAINY && k != TAG_SRC_RAINY_CONVERGENCE)
+        return "unsupported source kind for the rainy equations";
+      if (k == TAG_SRC_RAINY_CONVERGENCE && !cfg->node_coordinates)
+        return "the convergence-test source needs node coordinates";
+      return nullptr;
+    }
+    case TAG_EQ_MOIST_EULER_2D: {
+      if ((vf != TAG_VF_CHANDRASHEKAR && vf != TAG_VF_WEAK_FORM) ||
+          (sf != TAG_SF_LMARS && sf != TAG_SF_LAX_FRIEDRICHS && sf != TAG_SF_CHANDRASHEKAR))
+        return "unsupported flux combination for the moist equations";
+      const double k = cfg->params[6];
+      if (k != 0 && k != TAG_SRC_GEOPOTENTIAL && k != TAG_SRC_MOIST_BUBBLE &&
+          k != TAG_SRC_MOIST_CONVERGENCE_DRY && k != TAG_SRC_MOIST_CONVERGENCE)
+        return "unsupported source kind for the moist equations";
+      if ((k == TAG_SRC_MOIST_CONVERGENCE_DRY || k == TAG_SRC_MOIST_CONVERGENCE) &&
+          !cfg->node_coordinates)
+        return "the convergence-test source needs node coordinates";
+      if (sf == TAG_SF_LMARS && !(cfg->params[5] > 0.0))
+        return "FluxLMARS needs a positive speed of sound";
+      return nullptr;
+    }
+    default:
+      return "unsupported equations id";
+  }
+}
+
+bool boundary_kind_ok(int eq, int kind) {
+  switch (eq) {
+    case TAG_EQ_EULER_ENERGY_2D:
+    case TAG_EQ_MOIST_EULER_2D:
+      return kind == TAG_BC_SLIP_WALL_STRUCTURED || kind == TAG_BC_SLIP_WALL_NORMAL;
+    case TAG_EQ_EULER_ENERGY_3D: return kind == TAG_BC_SLIP_WALL_NORMAL;
+    case TAG_EQ_RAINY_2D: return kind == TAG_BC_SIMPLE_SLIP_WALL;
+    default: return false;
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -438,21 +495,12 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
     return fail(TAG_E_NO_DEVICE, "no CUDA device visible");
-  if (cfg->equations != TAG_EQ_EULER_ENERGY_2D && cfg->equations != TAG_EQ_EULER_ENERGY_3D &&
-      cfg->equations != TAG_EQ_RAINY_2D)
-    return fail(TAG_E_INVALID, "unsupported equations id");
+  const char* why = check_equations(cfg);
+  if (why) return fail(TAG_E_INVALID, why);
   const int dim = cfg->equations == TAG_EQ_EULER_ENERGY_3D ? 3 : 2;
   const int nface = 2 * dim;
   const bool rainy = cfg->equations == TAG_EQ_RAINY_2D;
-  if (!rainy && (cfg->volume_flux != TAG_VF_RANOCHA_WARUSZEWSKI || cfg->surface_flux != TAG_SF_LMARS))
-    return fail(TAG_E_INVALID, "unsupported flux combination");
-  if (rainy && ((cfg->volume_flux != TAG_VF_EC_RAIN && cfg->volume_flux != TAG_VF_WEAK_FORM) ||
-                cfg->surface_flux != TAG_SF_LAX_FRIEDRICHS))
-    return fail(TAG_E_INVALID, "unsupported flux combination for the rainy equations");
-  if (rainy && cfg->params[0] != TAG_SRC_RAINY && cfg->params[0] != TAG_SRC_RAINY_CONVERGENCE)
-    return fail(TAG_E_INVALID, "unsupported source kind for the rainy equations");
-  if (rainy && cfg->params[0] == TAG_SRC_RAINY_CONVERGENCE && !cfg->node_coordinates)
-    return fail(TAG_E_INVALID, "the convergence-test source needs node coordinates");
+  const bool moist = cfg->equations == TAG_EQ_MOIST_EULER_2D;
   const int n = cfg->polydeg + 1;
   if (n < 2 || n > kMaxNodes) return fail(TAG_E_INVALID, "polydeg out of range 1..7");
   if (dim == 3 && n < 3) return fail(TAG_E_INVALID, "3D meshes need polydeg >= 2");
@@ -485,10 +533,7 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
     const int e = cfg->boundary_elements[k], f = cfg->boundary_faces[k];
     const int kind = cfg->boundary_kinds ? cfg->boundary_kinds[k] : TAG_BC_SLIP_WALL_NORMAL;
     if (e < 0 || e >= cfg->nelements || f < 0 || f >= nface ||
-        (kind != TAG_BC_SLIP_WALL_STRUCTURED && kind != TAG_BC_SLIP_WALL_NORMAL &&
-         kind != TAG_BC_SIMPLE_SLIP_WALL) ||
-        (dim == 3 && kind != TAG_BC_SLIP_WALL_NORMAL) ||
-        (rainy != (kind == TAG_BC_SIMPLE_SLIP_WALL)))
+        !boundary_kind_ok(cfg->equations, kind))
       return fail(TAG_E_INVALID, "boundary index or kind out of range");
   }
 
@@ -510,6 +555,13 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
     h->ops = cfg->volume_flux == TAG_VF_WEAK_FORM ? ops_for_n<PhysRainy2D, kVolWeak>(n)
                                                   : ops_for_n<PhysRainy2D, kVolFluxDiff>(n);
     h->has_limiter = true;
+  } else if (moist) {
+    h->nv = PhysMoist2D::NV;
+    h->na = PhysMoist2D::NA;
+    h->p_moist = PhysMoist2D::make_params(cfg->params);
+    h->p_moist.surface = cfg->surface_flux;
+    h->ops = cfg->volume_flux == TAG_VF_WEAK_FORM ? ops_for_n<PhysMoist2D, kVolWeak>(n)
+                                                  : ops_for_n<PhysMoist2D, kVolFluxDiff>(n);
   } else if (dim == 3) {
     h->nv = PhysEnergy3D::NV;
     h->na = PhysEnergy3D::NA;

@@ -119,6 +119,31 @@ TAG_DEV void ln_mean_pair(double xa, double xb, double ya, double yb, double Lxa
   }
 }
 
+// One logarithmic mean (or its inverse) with its own reciprocal: the series of
+// ln_mean_pair in the common range, the reference's (y-x)/log(y/x) outside.
+TAG_DEV double ln_mean_single(double x, double y) {
+  const double s = x + y, d = y - x;
+  const double t = d / s, f2 = t * t;
+  if (f2 < kSeriesF2) {
+    const double R = 1.0 + f2 * (-1.0 / 3.0 + f2 * (-4.0 / 45.0 + f2 * (-44.0 / 945.0 +
+                     f2 * (-428.0 / 14175.0 + f2 * (-10196.0 / 467775.0 +
+                     f2 * (-10719068.0 / 638512875.0 + f2 * (-25865068.0 / 1915538625.0)))))));
+    return 0.5 * s * R;
+  }
+  return d / log(y / x);
+}
+
+TAG_DEV double inv_ln_mean_single(double x, double y) {
+  const double s = x + y, d = y - x;
+  const double t = d / s, f2 = t * t;
+  if (f2 < kSeriesF2) {
+    const double Q = 1.0 + f2 * (1.0 / 3.0 + f2 * (1.0 / 5.0 + f2 * (1.0 / 7.0 +
+                     f2 * (1.0 / 9.0 + f2 * (1.0 / 11.0 + f2 * (1.0 / 13.0 + f2 * (1.0 / 15.0)))))));
+    return 2.0 * Q / s;
+  }
+  return log(y / x) / d;
+}
+
 // Whether the values of one element can push a node pair out of the series
 // range of ln_mean_pair.
 TAG_DEV bool needs_logs(double vmin, double vmax) {

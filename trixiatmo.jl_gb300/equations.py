@@ -101,6 +101,36 @@ class CompressibleRainyEulerEquations2D:
                           (1.0 / self.ref_temperature - 1.0 / T))
 
 
+class CompressibleMoistEulerEquations2D:
+    """State (rho, rho_v1, rho_v2, rho_E, rho_qv, rho_ql)
+    (src/equations/compressible_moist_euler_2d.jl:5-32); gravity enters
+    through source_terms_geopotential."""
+
+    nvariables = 6
+    ndims = 2
+    eq_id = _lib.TAG_EQ_MOIST_EULER_2D
+
+    def __init__(self, *, c_pd, c_vd, c_pv, c_vv, gravity):
+        self.c_pd, self.c_vd = float(c_pd), float(c_vd)
+        self.c_pv, self.c_vv = float(c_pv), float(c_vv)
+        self.g = float(gravity)
+        self.p_0 = 100000.0
+        self.R_d = self.c_pd - self.c_vd
+        self.R_v = self.c_pv - self.c_vv
+        self.c_pl = 4186.0
+        self.gamma = self.c_pd / self.c_vd
+        self.kappa = 1.0 - 1.0 / self.gamma
+        self.L_00 = 3147620.0
+
+    def get_current_condition(self, u):
+        """(p, T) of states u[..., 6] (:383-402)."""
+        rho_qd = u[..., 0] - u[..., 4] - u[..., 5]
+        rho_e = u[..., 3] - 0.5 * (u[..., 1] ** 2 + u[..., 2] ** 2) / u[..., 0]
+        T = (rho_e - self.L_00 * u[..., 4]) / (rho_qd * self.c_vd + u[..., 4] * self.c_vv +
+                                                u[..., 5] * self.c_pl)
+        return (rho_qd * self.R_d + u[..., 4] * self.R_v) * T, T
+
+
 class _NamedFlux:
     def __init__(self, name):
         self.name = name
@@ -114,6 +144,7 @@ flux_nonconservative_waruszewski_etal = _NamedFlux("flux_nonconservative_warusze
 flux_zero = _NamedFlux("flux_zero")
 flux_ec_rain = _NamedFlux("flux_ec_rain")
 flux_lax_friedrichs = _NamedFlux("flux_lax_friedrichs")
+flux_chandrashekar = _NamedFlux("flux_chandrashekar")
 
 
 class FluxLMARS:
@@ -132,7 +163,7 @@ class VolumeIntegralFluxDifferencing:
 
 
 class VolumeIntegralWeakForm:
-    pass
+    """The weak-form volume integral (Trixi's default of `DGSEM`)."""
 
 
 class _BC:
@@ -160,6 +191,14 @@ class _Source:
 source_terms_rainy = _Source("source_terms_rainy", _lib.TAG_SRC_RAINY)
 source_terms_convergence_test_rainy = _Source("source_terms_convergence_test_rainy",
                                               _lib.TAG_SRC_RAINY_CONVERGENCE)
+# moist equations, src/equations/compressible_moist_euler_2d.jl:320-340, :376-380,
+# :203-241, :275-317
+source_terms_geopotential = _Source("source_terms_geopotential", _lib.TAG_SRC_GEOPOTENTIAL)
+source_terms_moist_bubble = _Source("source_terms_moist_bubble", _lib.TAG_SRC_MOIST_BUBBLE)
+source_terms_convergence_test_dry = _Source("source_terms_convergence_test_dry",
+                                            _lib.TAG_SRC_MOIST_CONVERGENCE_DRY)
+source_terms_convergence_test_moist = _Source("source_terms_convergence_test_moist",
+                                              _lib.TAG_SRC_MOIST_CONVERGENCE)
 
 
 def speed_of_sound_isothermal(equations, T0):

@@ -235,3 +235,45 @@ class MoistBubbleRainy:
         e = (eq.c_vd * rd + eq.c_vv * rv + eq.c_l * (rc + rr)) * T + rv * eq.ref_latent_heat_vap_temp
         z0 = np.zeros_like(T)
         return np.stack([rd, rm, rr, z0, z0, e, rv, rc, T], axis=-1)
+
+
+# ---- CompressibleMoistEulerEquations2D ------------------------------------
+def initial_condition_gemein_bubble(x, t, equations):
+    """Warm bubble of examples/euler/dry_air/buoyancy/elixir_gemein_bubble.jl:20-51
+    (Wicker & Skamarock 1998) for the moist equations without moisture: neutral
+    theta_ref = 300 K background, cos^2 bubble of 2 K and radius 2 km at
+    (10 km, 2 km), uniform v1 = 20 m/s."""
+    eq = equations
+    xc, zc, rc, theta_ref = 10000.0, 2000.0, 2000.0, 300.0
+    r = np.sqrt((x[..., 0] - xc) ** 2 + (x[..., 1] - zc) ** 2)
+    dtheta = np.where(r <= rc, 2.0 * np.cos(np.pi * (0.5 * r / rc)) ** 2, 0.0)
+    theta = theta_ref + dtheta
+    p = eq.p_0 * (1.0 - eq.kappa * eq.g * x[..., 1] / (eq.R_d * theta_ref)) ** (eq.c_pd / eq.R_d)
+    rho = p / ((p / eq.p_0) ** eq.kappa * eq.R_d * theta)
+    T = p / (eq.R_d * rho)
+    v1 = 20.0
+    z0 = np.zeros_like(rho)
+    return np.stack([rho, rho * v1, z0, rho * eq.c_vd * T + 0.5 * rho * v1 * v1, z0, z0],
+                    axis=-1)
+
+
+def initial_condition_convergence_test_dry(x, t, equations):
+    """src/equations/compressible_moist_euler_2d.jl:173-200."""
+    eq = equations
+    ini = 2.0 + 0.1 * np.sin(np.pi * (x[..., 0] + x[..., 1] - t))
+    T = (ini - 1.0) / eq.c_vd
+    E = eq.c_vd * T + 1.0
+    z0 = np.zeros_like(ini)
+    return np.stack([ini, ini, ini, E * ini, z0, z0], axis=-1)
+
+
+def initial_condition_convergence_test_moist(x, t, equations):
+    """src/equations/compressible_moist_euler_2d.jl:244-272."""
+    eq = equations
+    ini = 2.0 + 0.1 * np.sin(np.pi * (x[..., 0] + x[..., 1] - t))
+    qv = 100.0 / eq.L_00
+    ql = qv / 10.0
+    mu = (1.0 - qv - ql) * eq.c_vd + qv * eq.c_vv + ql * eq.c_pl
+    T = (ini - 1.0) / mu + 10.0 / eq.c_vd + 40.0
+    E = mu * T + qv * eq.L_00 + 1.0
+    return np.stack([ini, ini, ini, E * ini, qv * ini, ql * ini], axis=-1)

@@ -117,3 +117,70 @@ class StructuredMesh:
                 if not py and cyi == ny - 1:
                     c.bd_elements.append(e); c.bd_faces.append(3); c.bd_names.append("y_pos")
         return c
+
+
+def _morton(qx, qy, level):
+    """p4est's Morton index of quadrant (qx, qy) at a uniform level (x is the
+    low bit of each pair)."""
+    m = 0
+    for b in range(level):
+        m |= ((qx >> b) & 1) << (2 * b)
+        m |= ((qy >> b) & 1) << (2 * b + 1)
+    return m
+
+
+class P4estMesh:
+    """2D `P4estMesh(trees_per_dimension; polydeg, coordinates_min,
+    coordinates_max, initial_refinement_level, periodicity)` of a rectangle
+    (the form the reference's elixirs use, e.g.
+    examples/euler/dry_air/buoyancy/elixir_gemein_bubble.jl:72-77): a brick of
+    trees, each refined uniformly, with an affine mapping.  Elements follow
+    p4est's order (trees with x fastest, the quadrants of a tree in Morton
+    order); slip walls take the outward-normal (P4estMesh) method."""
+
+    ndims = 2
+    normal_walls = True
+
+    def __init__(self, trees_per_dimension, *, polydeg=1, coordinates_min, coordinates_max,
+                 initial_refinement_level=0, periodicity=True):
+        tx, ty = map(int, trees_per_dimension)
+        if isinstance(periodicity, bool):
+            periodicity = (periodicity, periodicity)
+        L = int(initial_refinement_level)
+        k = 1 << L
+        self.trees_per_dimension = (tx, ty)
+        self.level = L
+        self.polydeg = int(polydeg)
+        self._grid = StructuredMesh((tx * k, ty * k), coordinates_min, coordinates_max,
+                                    periodicity)
+        nx = tx * k
+        perm = np.empty(tx * ty * k * k, dtype=np.int64)
+        for tyi in range(ty):
+            for txi in range(tx):
+                tree = txi + tx * tyi
+                for qy in range(k):
+                    for qx in range(k):
+                        e = tree * k * k + _morton(qx, qy, L)
+                        perm[e] = (txi * k + qx) + nx * (tyi * k + qy)
+        self.perm = perm                 # p4est element -> row-major cell
+        self.inv = np.argsort(perm)      # row-major cell -> p4est element
+
+    @property
+    def nelements(self):
+        return self._grid.nelements
+
+    def geometry(self, basis: LobattoLegendreBasis):
+        xy, ja, ij = self._grid.geometry(basis)
+        return (np.ascontiguousarray(xy[self.perm]), np.ascontiguousarray(ja[self.perm]),
+                np.ascontiguousarray(ij[self.perm]))
+
+    def connectivity(self):
+        g = self._grid.connectivity()
+        c = Connectivity()
+        c.if_elements = [(int(self.inv[a]), int(self.inv[b])) for a, b in g.if_elements]
+        c.if_faces = list(g.if_faces)
+        c.if_flip = list(g.if_flip)
+        c.bd_elements = [int(self.inv[e]) for e in g.bd_elements]
+        c.bd_faces = list(g.bd_faces)
+        c.bd_names = list(g.bd_names)
+        return c

@@ -27,9 +27,10 @@ from . import _lib
 from .basis import LobattoLegendreBasis
 from .equations import (CompressibleEulerEnergyEquationsWithGravity2D,
                         CompressibleEulerEnergyEquationsWithGravity3D,
-                        CompressibleRainyEulerEquations2D, FluxLMARS, VolumeIntegralWeakForm,
-                        _Source, boundary_condition_simple_slip_wall,
-                        boundary_condition_slip_wall, flux_ec_rain, flux_lax_friedrichs,
+                        CompressibleMoistEulerEquations2D, CompressibleRainyEulerEquations2D,
+                        FluxLMARS, VolumeIntegralWeakForm, _Source,
+                        boundary_condition_simple_slip_wall, boundary_condition_slip_wall,
+                        flux_chandrashekar, flux_ec_rain, flux_lax_friedrichs,
                         flux_nonconservative_waruszewski_etal, flux_ranocha, flux_zero)
 from .initial_conditions import EARTH_ROTATION_RATE
 
@@ -42,7 +43,9 @@ def _ptr(a, t=_dp):
 
 
 class DGSEM:
-    def __init__(self, polydeg, surface_flux, volume_integral):
+    def __init__(self, polydeg, surface_flux, volume_integral=None):
+        if volume_integral is None:
+            volume_integral = VolumeIntegralWeakForm()
         self.polydeg = int(polydeg)
         self.basis = LobattoLegendreBasis(self.polydeg)
         self.surface_flux = surface_flux
@@ -79,6 +82,32 @@ def _flux_ids(equations, solver, source_terms=None):
         if not isinstance(source_terms, _Source):
             raise ValueError("rainy equations need source_terms_rainy or the convergence-test source")
         return vid, _lib.TAG_SF_LAX_FRIEDRICHS, [float(source_terms.kind)]
+    if isinstance(equations, CompressibleMoistEulerEquations2D):
+        if isinstance(vi, VolumeIntegralWeakForm):
+            vid = _lib.TAG_VF_WEAK_FORM
+        elif vf is flux_chandrashekar:
+            vid = _lib.TAG_VF_CHANDRASHEKAR
+        else:
+            raise ValueError("volume integral must be weak form or flux differencing with "
+                             "flux_chandrashekar")
+        c_lmars = 0.0
+        if isinstance(sf, FluxLMARS):
+            sid, c_lmars = _lib.TAG_SF_LMARS, sf.speed_of_sound
+        elif sf is flux_lax_friedrichs:
+            sid = _lib.TAG_SF_LAX_FRIEDRICHS
+        elif sf is flux_chandrashekar:
+            sid = _lib.TAG_SF_CHANDRASHEKAR
+        else:
+            raise ValueError("surface flux must be FluxLMARS(c), flux_lax_friedrichs or "
+                             "flux_chandrashekar")
+        if source_terms is not None and not isinstance(source_terms, _Source):
+            raise ValueError(f"unsupported source terms {source_terms}")
+        src = 0 if source_terms is None else source_terms.kind
+        if src not in (0, _lib.TAG_SRC_GEOPOTENTIAL, _lib.TAG_SRC_MOIST_BUBBLE,
+                       _lib.TAG_SRC_MOIST_CONVERGENCE_DRY, _lib.TAG_SRC_MOIST_CONVERGENCE):
+            raise ValueError(f"{source_terms} is not a source of the moist equations")
+        eq = equations
+        return vid, sid, [eq.c_pd, eq.c_vd, eq.c_pv, eq.c_vv, eq.g, c_lmars, float(src)]
     if isinstance(equations, CompressibleEulerEnergyEquationsWithGravity3D):
         if not (isinstance(vf, tuple) and vf[0] is flux_ranocha
                 and vf[1] is flux_nonconservative_waruszewski_etal):
@@ -103,7 +132,7 @@ def _flux_ids(equations, solver, source_terms=None):
     raise ValueError(f"unsupported equations {type(equations).__name__}")
 
 
-def _bc_kinds(names, boundary_conditions, ndims):
+def _bc_kinds(names, boundary_conditions, ndims, normal_walls=False):
     kinds = []
     bcs = boundary_conditions or {}
     for name in names:
@@ -113,7 +142,7 @@ def _bc_kinds(names, boundary_conditions, ndims):
         elif bc is boundary_condition_slip_wall:
             # StructuredMesh (2D) reaches the reference's orientation-argument
             # method; P4estMesh (the 3D shell) the normal-vector method
-            kinds.append(_lib.TAG_BC_SLIP_WALL_STRUCTURED if ndims == 2
+            kinds.append(_lib.TAG_BC_SLIP_WALL_STRUCTURED if ndims == 2 and not normal_walls
                          else _lib.TAG_BC_SLIP_WALL_NORMAL)
         else:
             raise ValueError(f"no supported boundary condition for {name}: {bc}")
@@ -145,7 +174,8 @@ class _Handle:
             coords.append(xy); Ja.append(ja); invJ.append(ij)
             ie.append(a_ie + offset); ifc.append(a_ifc); fl.append(a_fl)
             be.append(a_be + offset); bf.append(a_bf)
-            bk.append(np.asarray(_bc_kinds(conn.bd_names, boundary_conditions, self.ndims),
+            bk.append(np.asarray(_bc_kinds(conn.bd_names, boundary_conditions, self.ndims,
+                                           getattr(mesh, "normal_walls", False)),
                                  dtype=np.int32))
             member.append(np.full(mesh.nelements, m, dtype=np.int32))
             offset += mesh.nelements
