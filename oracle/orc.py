@@ -71,6 +71,17 @@ def lib():
         L.orc_euler3d_ck_steps.restype = ctypes.c_double
         L.orc_euler3d_ck_steps.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_int, ctypes.c_double]
+        L.orc_cov_create.restype = ctypes.c_void_p
+        L.orc_cov_create.argtypes = ([ctypes.c_int] * 2 + [_dp, _dp, ctypes.c_int, _ip, _ip, _ip] +
+                                     [ctypes.c_double] * 2 + [ctypes.c_int] * 7)
+        L.orc_cov_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_cov_rhs.argtypes = [ctypes.c_void_p, _dp, _dp]
+        L.orc_cov_max_dt.restype = ctypes.c_double
+        L.orc_cov_max_dt.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_cov_ck_steps.restype = ctypes.c_double
+        L.orc_cov_ck_steps.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double,
+                                       ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                       ctypes.c_double]
         L.orc_moist_create.restype = ctypes.c_void_p
         L.orc_moist_create.argtypes = ([ctypes.c_int] * 3 + [ctypes.c_double] * 4 +
                                        [ctypes.c_int] * 6 + [ctypes.c_double] * 2 + [ctypes.c_int])
@@ -224,6 +235,46 @@ class Euler3D:
 
     def ck_steps(self, u, k, t, cfl, nsteps, fixed_dt=0.0):
         return lib().orc_euler3d_ck_steps(self.h, _p(u), _p(k), t, cfl, nsteps, fixed_dt)
+
+
+class CovSWE:
+    """Covariant shallow water on the cubed sphere; geometry (aux, xyz) and
+    connectivity are the arrays passed to the C ABI.  fluxes: dict with keys
+    volume (0 weak, 1 flux differencing), vol_sym (0 central, 1 ec), vol_nc
+    (0/1 noncons ec), surf_sym, surf_diss (LLF), surf_nc (0, 1 ec,
+    2 surface_simplified)."""
+
+    def __init__(self, polydeg, aux, xyz, if_e, if_f, if_flip, g, omega, split, fluxes):
+        self.n = polydeg + 1
+        self.aux = np.ascontiguousarray(aux, dtype=np.float64)
+        self.xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        self.nelem = self.aux.shape[0]
+        ie = np.ascontiguousarray(if_e, dtype=np.int32)
+        ifc = np.ascontiguousarray(if_f, dtype=np.int32)
+        fl = np.ascontiguousarray(if_flip, dtype=np.int32)
+        f = dict(volume=0, vol_sym=0, vol_nc=0, surf_sym=0, surf_diss=1, surf_nc=0)
+        f.update(fluxes)
+        self.h = lib().orc_cov_create(polydeg, self.nelem, _p(self.aux), _p(self.xyz),
+                                      len(fl), _ip(ie), _ip(ifc), _ip(fl), g, omega, int(split),
+                                      f["volume"], f["vol_sym"], f["vol_nc"], f["surf_sym"],
+                                      f["surf_diss"], f["surf_nc"])
+
+    def rhs(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        du = np.zeros_like(u)
+        lib().orc_cov_rhs(self.h, _p(u), _p(du))
+        return du
+
+    def max_dt(self, u):
+        return lib().orc_cov_max_dt(self.h, _p(np.ascontiguousarray(u)))
+
+    def ck_steps(self, u, k, t, cfl, nsteps, fixed_dt=0.0, t_end=0.0):
+        return lib().orc_cov_ck_steps(self.h, _p(u), _p(k), t, cfl, nsteps, fixed_dt, t_end)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_cov_destroy(self.h)
+            self.h = None
 
 
 class Moist2D:

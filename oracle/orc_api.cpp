@@ -19,6 +19,7 @@
 #include "orc_euler_energy_2d.hpp"
 #include "orc_euler_energy_3d.hpp"
 #include "orc_moist_2d.hpp"
+#include "orc_cov_swe.hpp"
 #include "orc_rainy_2d.hpp"
 #include "orc_time.hpp"
 
@@ -925,6 +926,57 @@ void orc_moist_flux(const double* u, const double* n, double* f) {
   for (int v = 0; v < 6; ++v) a[v] = u[v];
   const auto r = eq.flux(a, n);
   for (int v = 0; v < 6; ++v) f[v] = r[v];
+}
+
+// ---- covariant shallow water on the cubed sphere --------------------------
+// aux: [E][n][n][26] (the reference's aux_node_vars), xyz: [E][n][n][3];
+// interfaces as passed to the C ABI (orientation 1 = secondary runs backward).
+// flux ids: see orc::CovFluxes.
+void* orc_cov_create(int polydeg, int nelem, const double* aux, const double* xyz, int nif,
+                     const int* if_e, const int* if_f, const int* if_flip, double g, double omega,
+                     int split, int volume, int vol_sym, int vol_nc, int surf_sym, int surf_diss,
+                     int surf_nc) {
+  auto* c = new CovDG();
+  c->eq.g = g;
+  c->eq.omega = omega;
+  c->eq.split = split != 0;
+  c->fx = CovFluxes{volume, vol_sym, vol_nc, surf_sym, surf_diss, surf_nc};
+  c->b = make_lgl_basis(polydeg);
+  c->n = polydeg + 1;
+  c->nelem = nelem;
+  const size_t nodes = (size_t)nelem * c->n * c->n;
+  c->aux.assign(aux, aux + nodes * 26);
+  c->xyz.assign(xyz, xyz + nodes * 3);
+  for (int k = 0; k < nif; ++k) {
+    c->if_e0.push_back(if_e[2 * k]);
+    c->if_e1.push_back(if_e[2 * k + 1]);
+    c->if_f0.push_back(if_f[2 * k]);
+    c->if_f1.push_back(if_f[2 * k + 1]);
+    c->if_flip.push_back(if_flip[k]);
+  }
+  return c;
+}
+
+void orc_cov_destroy(void* h) { delete static_cast<CovDG*>(h); }
+
+void orc_cov_rhs(void* h, const double* u, double* du) { static_cast<CovDG*>(h)->rhs(u, du); }
+
+double orc_cov_max_dt(void* h, const double* u) { return static_cast<CovDG*>(h)->max_dt(u); }
+
+double orc_cov_ck_steps(void* h, double* u, double* k, double t, double cfl, int nsteps,
+                        double fixed_dt, double t_end) {
+  auto* c = static_cast<CovDG*>(h);
+  const size_t N = (size_t)c->nelem * c->n * c->n * 3;
+  std::vector<double> du(N);
+  for (int s = 0; s < nsteps; ++s) {
+    if (t_end > 0 && t >= t_end) break;
+    double dt = fixed_dt > 0 ? fixed_dt : cfl * c->max_dt(u);
+    if (t_end > 0 && t + dt > t_end) dt = t_end - t;
+    ck2n54_step([&](const double* uu, double* dd, double) { c->rhs(uu, dd); }, u, k, du.data(), N,
+                t, dt);
+    t += dt;
+  }
+  return t;
 }
 
 }  // extern "C"

@@ -7,7 +7,7 @@ The directory name is not a Python identifier; load it with
 ``load_package()`` from ``__graft_entry__`` (or importlib) under the name
 ``trixiatmo_gb300``.
 """
-from . import _lib, learned_guess
+from . import _lib, covariant, learned_guess
 from .basis import LobattoLegendreBasis
 from .equations import (CompressibleEulerEnergyEquationsWithGravity2D,
                         CompressibleEulerEnergyEquationsWithGravity3D,
@@ -50,5 +50,5 @@ __all__ = [
     "source_terms_moist_bubble", "source_terms_convergence_test_dry",
     "source_terms_convergence_test_moist", "initial_condition_gemein_bubble",
     "initial_condition_convergence_test_dry", "initial_condition_convergence_test_moist",
-    "P4estMesh",
+    "P4estMesh", "covariant",
 ]

@@ -38,6 +38,7 @@ TAG_SRC_GEOPOTENTIAL = 3
 TAG_SRC_MOIST_BUBBLE = 4
 TAG_SRC_MOIST_CONVERGENCE_DRY = 5
 TAG_SRC_MOIST_CONVERGENCE = 6
+TAG_EQ_COVARIANT_SWE = 5
 MLP_PARAMS = 1293
 MLP_TRAINABLE = 1281
 TAG_VF_RANOCHA_WARUSZEWSKI = 1
