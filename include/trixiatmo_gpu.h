@@ -57,14 +57,20 @@ extern "C" {
 #define TAG_EQ_EULER_ENERGY_3D 2 /* CompressibleEulerEnergyEquationsWithGravity3D + source_terms_coriolis */
 #define TAG_EQ_RAINY_2D 3        /* CompressibleRainyEulerEquations2D (+ Newton stage limiter) */
 #define TAG_EQ_MOIST_EULER_2D 4  /* CompressibleMoistEulerEquations2D                             */
+#define TAG_EQ_COVARIANT_SWE 5   /* (Split)CovariantShallowWaterEquations2D on a 2D manifold     */
 
 #define TAG_VF_RANOCHA_WARUSZEWSKI 1 /* (flux_ranocha, flux_nonconservative_waruszewski_etal) */
 #define TAG_VF_EC_RAIN 2             /* VolumeIntegralFluxDifferencing(flux_ec_rain)    */
 #define TAG_VF_WEAK_FORM 3           /* VolumeIntegralWeakForm (physical flux)          */
 #define TAG_VF_CHANDRASHEKAR 4       /* VolumeIntegralFluxDifferencing(flux_chandrashekar), moist */
+#define TAG_VF_COV_CENTRAL 5         /* covariant: flux differencing with flux_central  */
+#define TAG_VF_COV_EC 6              /* covariant: flux differencing with flux_ec (split form) */
 #define TAG_SF_LMARS 1               /* (FluxLMARS(c), flux_zero)                       */
 #define TAG_SF_LAX_FRIEDRICHS 2      /* flux_lax_friedrichs (max_abs_speed_naive)       */
 #define TAG_SF_CHANDRASHEKAR 3       /* flux_chandrashekar as surface flux (moist)      */
+#define TAG_SF_COV_EC 4              /* covariant: flux_ec                              */
+#define TAG_SF_COV_EC_LLF 5          /* covariant: FluxPlusDissipation(flux_ec, DissipationLocalLaxFriedrichs()) */
+#define TAG_SF_COV_CENTRAL 6         /* covariant: flux_central (no dissipation)        */
 
 #define TAG_SRC_RAINY 1              /* source_terms_rainy (microphysics + gravity)     */
 #define TAG_SRC_RAINY_CONVERGENCE 2  /* manufactured source of the rainy convergence test */
@@ -111,7 +117,21 @@ typedef struct {
                         velocity (0 disables the source);
                         RAINY_2D: params[0] = TAG_SRC_* source kind;
                         MOIST_EULER_2D: c_pd, c_vd, c_pv, c_vv, gravity, LMARS
-                        speed of sound, TAG_SRC_* source kind (0: none) */
+                        speed of sound, TAG_SRC_* source kind (0: none);
+                        COVARIANT_SWE: gravity, rotation rate, split form (0/1),
+                        volume nonconservative flux (0 none, 1
+                        flux_nonconservative_ec), surface nonconservative flux
+                        (0 none, 1 flux_nonconservative_ec, 2
+                        flux_nonconservative_surface_simplified); the surface
+                        flux TAG_SF_LAX_FRIEDRICHS is flux_central + local
+                        Lax-Friedrichs dissipation; source_terms_geometric_coriolis
+                        is always applied */
+  const double* aux_node_vars;  /* COVARIANT_SWE: [26, n, n, E], the reference's
+                                   cache.auxiliary_variables.aux_node_vars
+                                   (src/equations/equations.jl:139-215);
+                                   node_coordinates is then [3, n, n, E];
+                                   contravariant_vectors / inverse_jacobian are
+                                   not used */
 } tag_config;
 
 /* Creates a handle on the current CUDA device.  Replaces the cache build of
@@ -119,6 +139,14 @@ typedef struct {
  * semidiscretization_hyperbolic_2d_manifold_in_3d.jl:78-111, create_cache in
  * src/solvers/solvers.jl:7-33): geometry and connectivity are uploaded once. */
 int tag_create(const tag_config* cfg, tag_handle* out);
+
+/* One handle for many independent members (COVARIANT_SWE), each its own mesh,
+ * polynomial degree, geometry and initial state: an uneven ensemble.  The
+ * solution is the members' u concatenated in the given order; each member has
+ * its own t, dt and CFL reduction; every stage is one interface launch and one
+ * element launch over all members (elements grouped by degree).  No counterpart
+ * in the reference, which runs one semidiscretization per process. */
+int tag_create_ensemble(const tag_config* members, int32_t nmembers, tag_handle* out);
 int tag_destroy(tag_handle h);
 
 /* Number of solution entries nv * n^2 * E (length of Trixi's u_ode). */

@@ -1,0 +1,157 @@
+"""GPU parity of the covariant shallow-water path (weak form and split
+entropy-conservative flux differencing, transformed interface fluxes across
+cubed-sphere panel edges, geometric/Coriolis sources, per-member CFL) against
+the CPU oracle; reference goldens reproduced with every stage on the GPU; an
+uneven ensemble (polydeg 3, 5, 7 in one launch per stage) against its members
+run alone.  All calls go through the C ABI."""
+import numpy as np
+import pytest
+
+from test_oracle_cov_swe import GOLDEN, LOOSE_RTOL, RTOL, check_golden, setup
+
+pytestmark = pytest.mark.gpu
+
+G_, OM_ = 9.80616, 7.292e-5
+
+
+def solver_for(tg, fluxes):
+    cv = tg.covariant
+    vol = (tg.VolumeIntegralWeakForm() if fluxes["volume"] == 0 else
+           tg.VolumeIntegralFluxDifferencing(
+               ((cv.flux_central, cv.flux_ec)[fluxes["vol_sym"]], cv.flux_nonconservative_ec)
+               if fluxes.get("vol_nc") else (cv.flux_central, cv.flux_ec)[fluxes["vol_sym"]]))
+    if fluxes["surf_sym"] == 0:
+        sym = tg.flux_lax_friedrichs if fluxes["surf_diss"] else cv.flux_central
+    else:
+        sym = (cv.FluxPlusDissipation(cv.flux_ec, cv.DissipationLocalLaxFriedrichs())
+               if fluxes["surf_diss"] else cv.flux_ec)
+    nc = {0: None, 1: cv.flux_nonconservative_ec,
+          2: cv.flux_nonconservative_surface_simplified}[fluxes.get("surf_nc", 0)]
+    return sym if nc is None else (sym, nc)
+
+
+def make_semi(tg, name, k=5, polydeg=3):
+    from test_oracle_cov_swe import case
+    cv = tg.covariant
+    eq, ic, fluxes, cfl, metric, topo = case(tg, name)
+    from trixiatmo_gb300.initial_conditions import EARTH_RADIUS
+    mesh = cv.P4estMeshCubedSphere2D(k, EARTH_RADIUS, polydeg=polydeg)
+    sf = solver_for(tg, fluxes)
+    vol = (tg.VolumeIntegralWeakForm() if fluxes["volume"] == 0 else
+           tg.VolumeIntegralFluxDifferencing(
+               ((cv.flux_central, cv.flux_ec)[fluxes["vol_sym"]], cv.flux_nonconservative_ec)
+               if fluxes.get("vol_nc") else (cv.flux_central, cv.flux_ec)[fluxes["vol_sym"]]))
+    solver = tg.DGSEM(polydeg, sf, vol)
+    semi = tg.SemidiscretizationHyperbolic(mesh, eq, cv.transform_initial_condition(ic, eq), solver,
+                                           source_terms=cv.source_terms_geometric_coriolis,
+                                           auxiliary_field=topo, metric_terms=metric)
+    return eq, mesh, semi, fluxes, cfl
+
+
+def oracle_for(orc, semi, mesh, eq, fluxes):
+    conn = mesh.connectivity(semi.solver.basis)
+    ie, ifc, fl, _, _ = conn.arrays()
+    return orc.CovSWE(semi.solver.polydeg, semi.aux_node_vars, semi.node_coordinates, ie, ifc, fl,
+                      G_, OM_, eq.split, fluxes)
+
+
+def perturbed(u, seed, amp=1e-2):
+    rng = np.random.Generator(np.random.Philox(seed))
+    v = u.copy()
+    v[..., 0] *= 1 + amp * rng.uniform(-1, 1, v.shape[:-1])
+    scale = np.abs(v[..., 1:]).max()
+    v[..., 1:] += amp * scale * rng.uniform(-1, 1, v.shape[:-1] + (2,))
+    return v
+
+
+@pytest.mark.parametrize("polydeg", [3, 4, 5, 7])
+@pytest.mark.parametrize("name", ["geostrophic_balance", "unsteady_solid_body_rotation",
+                                  "isolated_mountain"])
+def test_cov_rhs_matches_oracle(tg, orc, gpu_lib, name, polydeg):
+    eq, mesh, semi, fluxes, _ = make_semi(tg, name, k=3, polydeg=polydeg)
+    u = perturbed(semi.compute_coefficients(), seed=polydeg)
+    du = semi.rhs(u)
+    du_ref = oracle_for(orc, semi, mesh, eq, fluxes).rhs(u)
+    for v in range(3):
+        s = np.abs(du_ref[..., v]).max()
+        err = np.abs(du[..., v] - du_ref[..., v]).max()
+        assert err <= 1e-11 * s, (v, err / s)
+    assert np.abs(du - du_ref).max() <= RTOL_RHS * np.abs(du_ref).max()
+    semi.close()
+
+
+RTOL_RHS = 1e-12
+
+
+def test_cov_rk_steps_match_oracle(tg, orc, gpu_lib):
+    eq, mesh, semi, fluxes, cfl = make_semi(tg, "isolated_mountain", k=4, polydeg=3)
+    u0 = semi.compute_coefficients()
+    semi.set_state(u0)
+    t = semi.rk_steps(4, cfl=cfl, t=0.0)
+    uo = np.ascontiguousarray(u0).copy()
+    t_ref = oracle_for(orc, semi, mesh, eq, fluxes).ck_steps(uo, np.zeros_like(uo), 0.0, cfl, 4)
+    assert abs(t - t_ref) <= 1e-12 * t_ref
+    ug = semi.get_state()
+    for v in range(3):
+        assert np.abs(ug[..., v] - uo[..., v]).max() <= 1e-11 * np.abs(uo[..., v]).max()
+    semi.close()
+
+
+@pytest.mark.parametrize("name", ["geostrophic_balance", "isolated_mountain", "well_balanced",
+                                  "unsteady_solid_body_rotation"])
+def test_gpu_reproduces_covariant_golden(tg, orc, gpu_lib, name):
+    cv = tg.covariant
+    eq, mesh, semi, fluxes, cfl = make_semi(tg, name)
+    semi.set_state(semi.compute_coefficients())
+    t, t_end = 0.0, cv.SECONDS_PER_DAY
+    while t < t_end:
+        dt = cfl * semi.max_dt()
+        if t + dt >= t_end:
+            t = semi.rk_steps(1, fixed_dt=t_end - t, t=t)
+            break
+        t = semi.rk_steps(1, cfl=cfl, t=t)
+    assert abs(t - t_end) <= 1e-9
+    u = semi.get_state()
+    ue = semi.compute_coefficients(t_end)
+    l2, linf = cv.error_norms(u, ue, semi.aux_node_vars, semi.solver.basis)
+    check_golden(name, l2, linf, LOOSE_RTOL.get(name, RTOL))
+    semi.close()
+
+
+def test_uneven_ensemble_matches_members_alone(tg, gpu_lib):
+    """Members of polydeg 3, 5, 7 and 3..5 trees per face edge in one handle:
+    rhs and RK steps (each member its own dt) are bitwise those of the members
+    run alone."""
+    cv = tg.covariant
+    from trixiatmo_gb300.initial_conditions import EARTH_RADIUS
+    eq = cv.SplitCovariantShallowWaterEquations2D(G_, OM_)
+    specs = [(3, 3), (4, 5), (3, 7), (5, 3), (4, 7), (3, 5)]
+    meshes, solvers, ics = [], [], []
+    for m, (k, N) in enumerate(specs):
+        meshes.append(cv.P4estMeshCubedSphere2D(k, EARTH_RADIUS, polydeg=N))
+        solvers.append(tg.DGSEM(N, (cv.FluxPlusDissipation(cv.flux_ec,
+                                                           cv.DissipationLocalLaxFriedrichs()),
+                                    cv.flux_nonconservative_surface_simplified),
+                                tg.VolumeIntegralFluxDifferencing(
+                                    (cv.flux_ec, cv.flux_nonconservative_ec))))
+        ics.append(cv.transform_initial_condition(cv.initial_condition_geostrophic_balance, eq))
+    ens = tg.SemidiscretizationCovariantEnsemble(
+        meshes, eq, ics, solvers, source_terms=cv.source_terms_geometric_coriolis)
+    u = ens.compute_coefficients()
+    rng = np.random.default_rng(0)
+    u = u * (1 + 1e-3 * rng.standard_normal(u.shape))
+    du = ens.rhs(u)
+    ens.set_state(u)
+    t = ens.rk_steps(3, cfl=0.4, t=np.zeros(len(specs)))
+    ue = ens.get_state()
+    for m, (k, N) in enumerate(specs):
+        alone = tg.SemidiscretizationHyperbolic(meshes[m], eq, ics[m], solvers[m],
+                                                source_terms=cv.source_terms_geometric_coriolis)
+        um = np.ascontiguousarray(ens.member_state(u, m))
+        assert np.array_equal(alone.rhs(um), ens.member_state(du, m)), m
+        alone.set_state(um)
+        tm = alone.rk_steps(3, cfl=0.4, t=0.0)
+        assert tm == t[m]
+        assert np.array_equal(alone.get_state(), ens.member_state(ue, m)), m
+        alone.close()
+    ens.close()

@@ -30,8 +30,9 @@ from .initial_conditions import (EARTH_GRAVITATIONAL_ACCELERATION, EARTH_RADIUS,
                                  initial_condition_convergence_test_moist)
 from .meshes import P4estMesh, StructuredMesh
 from .meshes3d import P4estMeshCubedSphereTopography
-from .semidiscretization import (DGSEM, SemidiscretizationEnsemble, SemidiscretizationHyperbolic,
-                                 fp64_peak, source_terms_coriolis)
+from .semidiscretization import (DGSEM, SemidiscretizationCovariant,
+                                 SemidiscretizationCovariantEnsemble, SemidiscretizationEnsemble,
+                                 SemidiscretizationHyperbolic, fp64_peak, source_terms_coriolis)
 
 __all__ = [
     "LobattoLegendreBasis", "CompressibleEulerEnergyEquationsWithGravity2D", "FluxLMARS",
@@ -50,5 +51,6 @@ __all__ = [
     "source_terms_moist_bubble", "source_terms_convergence_test_dry",
     "source_terms_convergence_test_moist", "initial_condition_gemein_bubble",
     "initial_condition_convergence_test_dry", "initial_condition_convergence_test_moist",
-    "P4estMesh", "covariant",
+    "P4estMesh", "covariant", "SemidiscretizationCovariant",
+    "SemidiscretizationCovariantEnsemble",
 ]

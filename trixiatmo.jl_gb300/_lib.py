@@ -39,6 +39,11 @@ TAG_SRC_MOIST_BUBBLE = 4
 TAG_SRC_MOIST_CONVERGENCE_DRY = 5
 TAG_SRC_MOIST_CONVERGENCE = 6
 TAG_EQ_COVARIANT_SWE = 5
+TAG_VF_COV_CENTRAL = 5
+TAG_VF_COV_EC = 6
+TAG_SF_COV_EC = 4
+TAG_SF_COV_EC_LLF = 5
+TAG_SF_COV_CENTRAL = 6
 MLP_PARAMS = 1293
 MLP_TRAINABLE = 1281
 TAG_VF_RANOCHA_WARUSZEWSKI = 1
@@ -73,6 +78,7 @@ class TagConfig(ctypes.Structure):
         ("boundary_kinds", _ip),
         ("element_member", _ip),
         ("params", ctypes.c_double * 8),
+        ("aux_node_vars", _dp),
     ]
 
 
@@ -86,6 +92,8 @@ _fp = ctypes.POINTER(ctypes.c_float)
 # exported symbol -> (restype, argtypes)
 SIGNATURES = {
     "tag_create": (ctypes.c_int, [ctypes.POINTER(TagConfig), ctypes.POINTER(ctypes.c_void_p)]),
+    "tag_create_ensemble": (ctypes.c_int, [ctypes.POINTER(TagConfig), ctypes.c_int32,
+                                           ctypes.POINTER(ctypes.c_void_p)]),
     "tag_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "tag_ndofs_total": (ctypes.c_int64, [ctypes.c_void_p]),
     "tag_rhs": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, ctypes.c_double, ctypes.c_int32]),

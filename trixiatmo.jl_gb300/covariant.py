@@ -392,13 +392,14 @@ def compute_aux_vars(mesh, basis, equations, metric_terms=None, bottom_topograph
         d2 = np.einsum("jk,ekic->ejic", D, Gc)
     else:
         d = []
-        for wrt in (0, 1):
-            a = _Dual(xi1, 1.0 if wrt == 0 else 0.0)
-            b = _Dual(xi2, 1.0 if wrt == 1 else 0.0)
-            Ad = _basis_covariant(v, a, b, mesh.radius, spherical)
-            Ad = [[_Dual.lift(Ad[r][c]) for c in range(2)] for r in range(3)]
-            g = _metric_covariant(Ad)
-            d.append(np.stack([np.broadcast_to(gg.d, (E, n, n)) for gg in g], -1))
+        with np.errstate(invalid="ignore", divide="ignore"):
+            for wrt in (0, 1):
+                a = _Dual(xi1, 1.0 if wrt == 0 else 0.0)
+                b = _Dual(xi2, 1.0 if wrt == 1 else 0.0)
+                Ad = _basis_covariant(v, a, b, mesh.radius, spherical)
+                Ad = [[_Dual.lift(Ad[r][c]) for c in range(2)] for r in range(3)]
+                g = _metric_covariant(Ad)
+                d.append(np.stack([np.broadcast_to(gg.d, (E, n, n)) for gg in g], -1))
         d1, d2 = d
     # Christoffel symbols of the first kind, then raised with G^-1
     # (containers_2d_manifold_in_3d_covariant.jl:417-441)
@@ -413,6 +414,9 @@ def compute_aux_vars(mesh, basis, equations, metric_terms=None, bottom_topograph
     aux[..., 23] = c12 * g1[0][0] + c22 * g2[0][0]
     aux[..., 24] = c12 * g1[0][1] + c22 * g2[0][1]
     aux[..., 25] = c12 * g1[1][1] + c22 * g2[1][1]
+    if not np.isfinite(aux).all():
+        raise ValueError("the metric terms are singular at a node (spherical global coordinates "
+                         "are singular at the poles; use GlobalCartesianCoordinates)")
     return np.ascontiguousarray(aux), np.ascontiguousarray(xyz)
 
 

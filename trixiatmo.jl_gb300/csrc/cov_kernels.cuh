@@ -1,0 +1,524 @@
+// Covariant shallow-water equations on a 2D manifold (the cubed sphere):
+// device physics and kernels.
+//
+// Reference: src/equations/covariant_shallow_water.jl (fluxes :155-176,
+// sources :216-243, speeds :246-305), covariant_shallow_water_split.jl
+// (flux_ec :101-116, nonconservative fluxes :142-220, sources :273-302), the
+// Lax-Friedrichs dissipation of src/equations/equations.jl:243-257, and the
+// covariant DGSEM of src/solvers/dgsem_p4est/dg_2d_manifold_in_3d_covariant.jl
+// (weak form :98-131, flux differencing :135-234, interfaces :239-432,
+// sources :435-452, apply_jacobian :461-478), max_dt of
+// src/callbacks_step/stepsize_dg2d.jl:47-71.
+//
+// A handle holds one or more element groups; a group is a run of elements of
+// one polynomial degree (an uneven ensemble has one group per run of members
+// with equal degree).  Every stage is one interface launch and one element
+// launch over all groups: each CTA finds its group and runs the body
+// instantiated for that group's n.  The solution is u[node][3] with the
+// nodes of each element contiguous; aux[node][26] is the reference's
+// aux_node_vars; pk[node][16] a packed copy of what the element kernel reads.
+#pragma once
+#include "dg2d_kernels.cuh"
+
+namespace tag {
+
+// packed per-node element data
+enum CovPack : int {
+  kPJ = 0, kPGc11, kPGc12, kPGc22, kPGv11, kPGv12, kPGv22, kPHs,
+  kPC111, kPC112, kPC122, kPC211, kPC212, kPC222, kPF, kPPad, kPack = 16
+};
+
+struct CovParams {
+  double g;
+  int split;     // SplitCovariantShallowWaterEquations2D
+  int volume;    // 0 weak form, 1 flux differencing
+  int vol_sym;   // 0 flux_central, 1 flux_ec
+  int vol_nc;    // 0 none, 1 flux_nonconservative_ec
+  int surf_sym;  // 0 flux_central, 1 flux_ec
+  int surf_diss; // 0 none, 1 local Lax-Friedrichs
+  int surf_nc;   // 0 none, 1 flux_nonconservative_ec, 2 flux_nonconservative_surface_simplified
+};
+
+struct CovGroup {
+  int n;         // nodes per direction
+  int e0, ne;    // elements [e0, e0 + ne)
+  long node0;    // first node of element e0
+  long sf0;      // first double of element e0 in the surface-flux array
+  int if0, nif;  // interfaces [if0, if0 + nif)
+  int epb;       // elements per CTA
+  int blk0;      // first CTA of the group in the element launch
+  int iblk0;     // first CTA of the group in the interface launch
+  int basis;     // offset of the group's BasisDev in the basis array
+};
+
+constexpr int kCovMaxGroups = 64;
+
+struct CovGroups {
+  int count;
+  CovGroup g[kCovMaxGroups];
+};
+
+TAG_DEV int cov_find_group(const CovGroups& G, int blk, bool iface) {
+  int lo = 0;
+  for (int k = 1; k < G.count; ++k)
+    if ((iface ? G.g[k].iblk0 : G.g[k].blk0) <= blk) lo = k;
+  return lo;
+}
+
+// packs aux (26) and the Coriolis parameter f = 2 Omega z / |x| per node
+__global__ void k_cov_pack(const double* __restrict__ aux, const double* __restrict__ xyz,
+                           long nodes, double omega, double* __restrict__ pk) {
+  const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nodes) return;
+  const double* a = aux + q * 26;
+  double* p = pk + q * kPack;
+  p[kPJ] = a[12];
+  p[kPGc11] = a[16]; p[kPGc12] = a[17]; p[kPGc22] = a[18];
+  p[kPGv11] = a[13]; p[kPGv12] = a[14]; p[kPGv22] = a[15];
+  p[kPHs] = a[19];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) p[kPC111 + k] = a[20 + k];
+  const double* x = xyz + q * 3;
+  p[kPF] = 2.0 * omega * x[2] / sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+  p[kPPad] = 0.0;
+}
+
+// ---- pointwise physics on packed data -----------------------------------------
+TAG_DEV double cov_gcon(const double* p, int i, int j) {
+  return (i == 0 && j == 0) ? p[kPGc11] : (i == 1 && j == 1) ? p[kPGc22] : p[kPGc12];
+}
+
+// contravariant flux component o of one node (standard or split form)
+TAG_DEV void cov_flux(const CovParams& P, const double* u, const double* p, int o, double* f) {
+  const double J = p[kPJ];
+  const double m = J * u[1 + o];
+  if (P.split) {
+    const double ih = 1.0 / u[0];
+    f[0] = m;
+    f[1] = m * (u[1] * ih);
+    f[2] = m * (u[2] * ih);
+    return;
+  }
+  const double vo = u[1 + o] / u[0];
+  const double gt = 0.5 * P.g * u[0] * u[0];
+  f[0] = m;
+  f[1] = J * (u[1] * vo + cov_gcon(p, 0, o) * gt);
+  f[2] = J * (u[2] * vo + cov_gcon(p, 1, o) * gt);
+}
+
+// symmetric two-point volume flux of nodes a and b along o
+TAG_DEV void cov_vol_sym(const CovParams& P, const double* ua, const double* pa, const double* ub,
+                         const double* pb, int o, double* f) {
+  if (P.vol_sym == 1) {
+    const double m = 0.5 * (pa[kPJ] * ua[1 + o] + pb[kPJ] * ub[1 + o]);
+    f[0] = m;
+    f[1] = 0.5 * (ua[1] / ua[0] + ub[1] / ub[0]) * m;
+    f[2] = 0.5 * (ua[2] / ua[0] + ub[2] / ub[0]) * m;
+    return;
+  }
+  double fa[3], fb[3];
+  cov_flux(P, ua, pa, o, fa);
+  cov_flux(P, ub, pb, o, fb);
+#pragma unroll
+  for (int v = 0; v < 3; ++v) f[v] = 0.5 * (fa[v] + fb[v]);
+}
+
+// flux_nonconservative_ec of (a, b) along o: momentum components only
+TAG_DEV void cov_noncons_ec(const CovParams& P, const double* ua, const double* pa, const double* ub,
+                            const double* pb, double hs_jump, int o, double* g2) {
+  const double vb0 = ub[1] / ub[0], vb1 = ub[2] / ub[0];
+  const double vc0 = pb[kPGv11] * vb0 + pb[kPGv12] * vb1;
+  const double vc1 = pb[kPGv12] * vb0 + pb[kPGv22] * vb1;
+  const double half_m = 0.5 * ua[1 + o];
+  const double ph = P.g * ua[0] * (ub[0] + hs_jump);
+  const double geo0 = half_m * (pa[kPGc11] * vc0 + pa[kPGc12] * vc1 - vb0);
+  const double geo1 = half_m * (pa[kPGc12] * vc0 + pa[kPGc22] * vc1 - vb1);
+  g2[0] = pa[kPJ] * (geo0 + cov_gcon(pa, 0, o) * ph);
+  g2[1] = pa[kPJ] * (geo1 + cov_gcon(pa, 1, o) * ph);
+}
+
+// source_terms_geometric_coriolis (standard or split), after apply_jacobian
+TAG_DEV void cov_source(const CovParams& P, const double* u, const double* p, double* s) {
+  const double hv0 = u[1], hv1 = u[2];
+  const double ih = 1.0 / u[0];
+  const double v0 = hv0 * ih, v1 = hv1 * ih;
+  const double T00 = hv0 * v0, T01 = hv0 * v1, T10 = hv1 * v0, T11 = hv1 * v1;
+  double sg0, sg1;
+  if (!P.split) {
+    const double gt = 0.5 * P.g * u[0] * u[0];
+    sg0 = p[kPC111] * (T00 + gt * p[kPGc11]) + p[kPC112] * (T01 + gt * p[kPGc12]) +
+          p[kPC112] * (T10 + gt * p[kPGc12]) + p[kPC122] * (T11 + gt * p[kPGc22]);
+    sg1 = p[kPC211] * (T00 + gt * p[kPGc11]) + p[kPC212] * (T01 + gt * p[kPGc12]) +
+          p[kPC212] * (T10 + gt * p[kPGc12]) + p[kPC222] * (T11 + gt * p[kPGc22]);
+  } else {
+    // C = G_cov T, w_i = (Gamma^1 C[0,:])_i + (Gamma^2 C[1,:])_i
+    const double C00 = p[kPGv11] * T00 + p[kPGv12] * T10, C01 = p[kPGv11] * T01 + p[kPGv12] * T11;
+    const double C10 = p[kPGv12] * T00 + p[kPGv22] * T10, C11 = p[kPGv12] * T01 + p[kPGv22] * T11;
+    const double w0 = (p[kPC111] * C00 + p[kPC112] * C01) + (p[kPC211] * C10 + p[kPC212] * C11);
+    const double w1 = (p[kPC112] * C00 + p[kPC122] * C01) + (p[kPC212] * C10 + p[kPC222] * C11);
+    const double s0 = p[kPC111] * T00 + p[kPC112] * T01 + p[kPC112] * T10 + p[kPC122] * T11;
+    const double s1 = p[kPC211] * T00 + p[kPC212] * T01 + p[kPC212] * T10 + p[kPC222] * T11;
+    sg0 = 0.5 * (s0 - (p[kPGc11] * w0 + p[kPGc12] * w1));
+    sg1 = 0.5 * (s1 - (p[kPGc12] * w0 + p[kPGc22] * w1));
+  }
+  const double fJ = p[kPF] * p[kPJ];
+  s[0] = 0.0;
+  s[1] = -(sg0 + fJ * (p[kPGc12] * hv0 - p[kPGc11] * hv1));
+  s[2] = -(sg1 + fJ * (p[kPGc22] * hv0 - p[kPGc12] * hv1));
+}
+
+// ---- interface fluxes ------------------------------------------------------------
+// aux accessors of the reference layout
+TAG_DEV double cov_A(const double* a, int r, int c) { return a[c * 3 + r]; }
+TAG_DEV double cov_Acon(const double* a, int r, int c) { return a[6 + c * 2 + r]; }
+TAG_DEV double cov_agc(const double* a, int i, int j) {
+  return (i == 0 && j == 0) ? a[16] : (i == 1 && j == 1) ? a[18] : a[17];
+}
+
+// state of another node in the contravariant basis of `to`
+TAG_DEV void cov_transform(const double* u, const double* from, const double* to, double* s) {
+  double gl[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) gl[r] = cov_A(from, r, 0) * u[1] + cov_A(from, r, 1) * u[2];
+  s[0] = u[0];
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+    s[1 + r] = cov_Acon(to, r, 0) * gl[0] + cov_Acon(to, r, 1) * gl[1] + cov_Acon(to, r, 2) * gl[2];
+}
+
+// contravariant flux from reference-layout aux (surface version of cov_flux)
+TAG_DEV void cov_flux_aux(const CovParams& P, const double* u, const double* a, int o, double* f) {
+  const double J = a[12];
+  const double m = J * u[1 + o];
+  if (P.split) {
+    f[0] = m;
+    f[1] = m * (u[1] / u[0]);
+    f[2] = m * (u[2] / u[0]);
+    return;
+  }
+  const double vo = u[1 + o] / u[0];
+  const double gt = 0.5 * P.g * u[0] * u[0];
+  f[0] = m;
+  f[1] = J * (u[1] * vo + cov_agc(a, 0, o) * gt);
+  f[2] = J * (u[2] * vo + cov_agc(a, 1, o) * gt);
+}
+
+// surface flux (+ 0.5 nonconservative) of left state a, right state c, both
+// sides' geometry that of `own`
+TAG_DEV void cov_surface(const CovParams& P, const double* a, const double* c, const double* own,
+                         int o, double* F) {
+  const double J = own[12];
+  if (P.surf_sym == 1) {
+    const double m = 0.5 * (J * a[1 + o] + J * c[1 + o]);
+    F[0] = m;
+    F[1] = 0.5 * (a[1] / a[0] + c[1] / c[0]) * m;
+    F[2] = 0.5 * (a[2] / a[0] + c[2] / c[0]) * m;
+  } else {
+    double fa[3], fc[3];
+    cov_flux_aux(P, a, own, o, fa);
+    cov_flux_aux(P, c, own, o, fc);
+#pragma unroll
+    for (int v = 0; v < 3; ++v) F[v] = 0.5 * (fa[v] + fc[v]);
+  }
+  if (P.surf_diss) {
+    const double goo = cov_agc(own, o, o);
+    const double lam = fmax(fabs(a[1 + o] / a[0]) + sqrt(goo * a[0] * P.g),
+                            fabs(c[1 + o] / c[0]) + sqrt(goo * c[0] * P.g));
+#pragma unroll
+    for (int v = 0; v < 3; ++v) F[v] += -0.5 * J * lam * (c[v] - a[v]);
+  }
+  if (P.surf_nc == 1) {
+    // flux_nonconservative_ec with both geometries `own` (no topography jump)
+    const double vb0 = c[1] / c[0], vb1 = c[2] / c[0];
+    const double vc0 = own[13] * vb0 + own[14] * vb1;
+    const double vc1 = own[14] * vb0 + own[15] * vb1;
+    const double half_m = 0.5 * a[1 + o];
+    const double ph = P.g * a[0] * c[0];
+    const double g0 = J * (half_m * (own[16] * vc0 + own[17] * vc1 - vb0) + cov_agc(own, 0, o) * ph);
+    const double g1 = J * (half_m * (own[17] * vc0 + own[18] * vc1 - vb1) + cov_agc(own, 1, o) * ph);
+    F[1] += 0.5 * g0;
+    F[2] += 0.5 * g1;
+  } else if (P.surf_nc == 2) {
+    const double ph = P.g * a[0] * c[0];
+    F[1] += 0.5 * (J * (cov_agc(own, 0, o) * ph));
+    F[2] += 0.5 * (J * (cov_agc(own, 1, o) * ph));
+  }
+}
+
+// outward flux of one side (face f of its element)
+TAG_DEV void cov_side_flux(const CovParams& P, const double* mine, const double* other_in_mine,
+                           const double* own, int f, double* F) {
+  const int o = f >> 1;
+  if ((f & 1) == 0) {
+    cov_surface(P, other_in_mine, mine, own, o, F);
+    F[0] = -F[0];
+    F[1] = -F[1];
+    F[2] = -F[2];
+  } else {
+    cov_surface(P, mine, other_in_mine, own, o, F);
+  }
+}
+
+template <int n>
+TAG_DEV void cov_interface_body(const CovParams& P, const CovGroup& G, int lblk, const double* u,
+                                const double* aux, const int* if_e, const int* if_f,
+                                const int* if_flip, double* sfv) {
+  const int t = lblk * blockDim.x + threadIdx.x;
+  const int k = t / n, l = t % n;
+  if (k >= G.nif) return;
+  const int kk = G.if0 + k;
+  const int e0 = if_e[2 * kk], e1 = if_e[2 * kk + 1];
+  const int f0 = if_f[2 * kk], f1 = if_f[2 * kk + 1];
+  const int l1 = if_flip[kk] ? n - 1 - l : l;
+  int i0, j0, i1, j1;
+  face_node(f0, l, n, i0, j0);
+  face_node(f1, l1, n, i1, j1);
+  const long q0 = G.node0 + (long)(e0 - G.e0) * n * n + j0 * n + i0;
+  const long q1 = G.node0 + (long)(e1 - G.e0) * n * n + j1 * n + i1;
+  double ul[3], ur[3], al[26], ar[26];
+#pragma unroll
+  for (int v = 0; v < 3; ++v) {
+    ul[v] = u[q0 * 3 + v];
+    ur[v] = u[q1 * 3 + v];
+  }
+#pragma unroll
+  for (int v = 0; v < 26; ++v) {
+    al[v] = aux[q0 * 26 + v];
+    ar[v] = aux[q1 * 26 + v];
+  }
+  double rt[3], lt[3], Fp[3], Fs[3];
+  cov_transform(ur, ar, al, rt);
+  cov_transform(ul, al, ar, lt);
+  cov_side_flux(P, ul, rt, al, f0, Fp);
+  cov_side_flux(P, ur, lt, ar, f1, Fs);
+  double* s0 = sfv + G.sf0 + ((long)(e0 - G.e0) * 4 + f0) * n * 3 + l * 3;
+  double* s1 = sfv + G.sf0 + ((long)(e1 - G.e0) * 4 + f1) * n * 3 + l1 * 3;
+#pragma unroll
+  for (int v = 0; v < 3; ++v) {
+    s0[v] = Fp[v];
+    s1[v] = Fs[v];
+  }
+}
+
+__global__ void __launch_bounds__(256) k_cov_interface(CovParams P, const CovGroups* __restrict__ GG,
+                                                       const double* __restrict__ u,
+                                                       const double* __restrict__ aux,
+                                                       const int* __restrict__ if_e,
+                                                       const int* __restrict__ if_f,
+                                                       const int* __restrict__ if_flip,
+                                                       double* __restrict__ sfv) {
+  const int gi = cov_find_group(*GG, blockIdx.x, true);
+  const CovGroup& G = GG->g[gi];
+  const int lblk = blockIdx.x - G.iblk0;
+  switch (G.n) {
+    case 4: cov_interface_body<4>(P, G, lblk, u, aux, if_e, if_f, if_flip, sfv); break;
+    case 6: cov_interface_body<6>(P, G, lblk, u, aux, if_e, if_f, if_flip, sfv); break;
+    case 8: cov_interface_body<8>(P, G, lblk, u, aux, if_e, if_f, if_flip, sfv); break;
+    case 2: cov_interface_body<2>(P, G, lblk, u, aux, if_e, if_f, if_flip, sfv); break;
+    case 3: cov_interface_body<3>(P, G, lblk, u, aux, if_e, if_f, if_flip, sfv); break;
+    case 5: cov_interface_body<5>(P, G, lblk, u, aux, if_e, if_f, if_flip, sfv); break;
+    case 7: cov_interface_body<7>(P, G, lblk, u, aux, if_e, if_f, if_flip, sfv); break;
+    default: break;
+  }
+}
+
+// ---- element kernel --------------------------------------------------------------
+// shared memory per element (doubles): u [nn][3], pk [nn][16], weak-form
+// fluxes [2][nn][3]
+__host__ __device__ constexpr int cov_elem_doubles(int n) { return n * n * (3 + kPack + 6); }
+
+template <int n, int MODE>
+TAG_DEV void cov_element_body(const CovParams& P, const CovGroup& G, int lblk,
+                              const BasisDev* __restrict__ bases, double* __restrict__ u,
+                              double* __restrict__ du, double* __restrict__ kreg,
+                              const double* __restrict__ pk, const double* __restrict__ sfv,
+                              StageArgs st, double* smem, unsigned& bad) {
+  constexpr int nn = n * n, per = cov_elem_doubles(n);
+  BasisDev* sb = reinterpret_cast<BasisDev*>(smem);
+  double* base = smem + sizeof(BasisDev) / sizeof(double);
+  const int nthr = blockDim.x;
+  const int el_first = lblk * G.epb;
+  const int ne = min(G.epb, G.ne - el_first);
+  if (ne <= 0) return;
+  for (int t = threadIdx.x; t < (int)(sizeof(BasisDev) / sizeof(double)); t += nthr)
+    smem[t] = reinterpret_cast<const double*>(bases + G.basis)[t];
+  const long q_first = G.node0 + (long)el_first * nn;
+  for (int t = threadIdx.x; t < ne * nn * 3; t += nthr) {
+    const int el = t / (nn * 3), r = t % (nn * 3);
+    base[el * per + r] = u[q_first * 3 + t];
+  }
+  for (int t = threadIdx.x; t < ne * nn * kPack; t += nthr) {
+    const int el = t / (nn * kPack), r = t % (nn * kPack);
+    base[el * per + nn * 3 + r] = pk[q_first * kPack + t];
+  }
+  __syncthreads();
+  if (P.volume == 0) {
+    for (int t = threadIdx.x; t < ne * nn; t += nthr) {
+      const int el = t / nn, node = t % nn;
+      double* eb = base + el * per;
+      cov_flux(P, eb + node * 3, eb + nn * 3 + node * kPack, 0, eb + nn * (3 + kPack) + node * 3);
+      cov_flux(P, eb + node * 3, eb + nn * 3 + node * kPack, 1,
+               eb + nn * (3 + kPack) + nn * 3 + node * 3);
+    }
+    __syncthreads();
+  }
+  // one thread per node: volume, surface, Jacobian, sources, stage update
+  for (int t = threadIdx.x; t < ne * nn; t += nthr) {
+    const int el = t / nn, node = t % nn;
+    const int i = node % n, j = node / n;
+    double* eb = base + el * per;
+    const double* ui = eb + node * 3;
+    const double* pi = eb + nn * 3 + node * kPack;
+    double acc[3] = {0.0, 0.0, 0.0};
+    if (P.volume == 0) {
+      const double* F1 = eb + nn * (3 + kPack);
+      const double* F2 = F1 + nn * 3;
+#pragma unroll
+      for (int b = 0; b < n; ++b) {
+        const double d1 = sb->Dh[i * n + b], d2 = sb->Dh[j * n + b];
+#pragma unroll
+        for (int v = 0; v < 3; ++v) {
+          acc[v] = fma(d1, F1[(j * n + b) * 3 + v], acc[v]);
+          acc[v] = fma(d2, F2[(b * n + i) * 3 + v], acc[v]);
+        }
+      }
+    } else {
+      double nc1 = 0.0, nc2 = 0.0;
+#pragma unroll
+      for (int d = 0; d < 2; ++d) {
+#pragma unroll
+        for (int b = 0; b < n; ++b) {
+          const int nb = d == 0 ? j * n + b : b * n + i;
+          const int a = d == 0 ? i : j;
+          const double Dab = sb->Ds[a * n + b];
+          const double* ub = eb + nb * 3;
+          const double* pb = eb + nn * 3 + nb * kPack;
+          if (b != a) {
+            double f[3];
+            cov_vol_sym(P, ui, pi, ub, pb, d, f);
+#pragma unroll
+            for (int v = 0; v < 3; ++v) acc[v] = fma(Dab, f[v], acc[v]);
+          }
+          if (P.vol_nc) {
+            double g2[2];
+            cov_noncons_ec(P, ui, pi, ub, pb, pb[kPHs] - pi[kPHs], d, g2);
+            nc1 = fma(Dab, g2[0], nc1);
+            nc2 = fma(Dab, g2[1], nc2);
+          }
+        }
+      }
+      acc[1] += 0.5 * nc1;
+      acc[2] += 0.5 * nc2;
+    }
+    const double* se = sfv + G.sf0 + (long)(el_first + el) * 4 * n * 3;
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+      if (i == 0) acc[v] += se[(0 * n + j) * 3 + v] * sb->winv0;
+      if (i == n - 1) acc[v] += se[(1 * n + j) * 3 + v] * sb->winvN;
+      if (j == 0) acc[v] += se[(2 * n + i) * 3 + v] * sb->winv0;
+      if (j == n - 1) acc[v] += se[(3 * n + i) * 3 + v] * sb->winvN;
+    }
+    double s[3];
+    cov_source(P, ui, pi, s);
+    const double fac = -1.0 / pi[kPJ];
+    const long gq = q_first + (long)el * nn + node;
+    const int e = G.e0 + el_first + el;
+    double dv[3];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+      dv[v] = acc[v] * fac + s[v];
+      if (!isfinite(dv[v])) bad |= TAG_S_NAN;
+    }
+    if (!(ui[0] > 0.0)) bad |= TAG_S_NEG_DENSITY;
+    if (MODE == kModeRhs) {
+#pragma unroll
+      for (int v = 0; v < 3; ++v) du[gq * 3 + v] = dv[v];
+    } else {
+      const double dt = st.dt[st.member ? st.member[e] : 0];
+#pragma unroll
+      for (int v = 0; v < 3; ++v) {
+        const double kn = st.A * kreg[gq * 3 + v] + dt * dv[v];
+        kreg[gq * 3 + v] = kn;
+        u[gq * 3 + v] = ui[v] + st.B * kn;
+      }
+    }
+  }
+  if (MODE == kModeStage && st.max_speed != nullptr) {
+    // CFL speeds of the updated state, scaled by n: dt = cfl 2 / (n max_e(l1 + l2))
+    __syncthreads();
+    for (int t = threadIdx.x; t < ne * nn; t += nthr) {
+      const int el = t / nn, node = t % nn;
+      double* eb = base + el * per;
+      const long gq = q_first + (long)el * nn + node;
+      const double* pi = eb + nn * 3 + node * kPack;
+      const double h = u[gq * 3];
+      const double l1 = fabs(u[gq * 3 + 1] / h) + sqrt(pi[kPGc11] * h * P.g);
+      const double l2 = fabs(u[gq * 3 + 2] / h) + sqrt(pi[kPGc22] * h * P.g);
+      eb[node * 3] = l1;  // the state slots are free now
+      eb[node * 3 + 1] = l2;
+    }
+    __syncthreads();
+    for (int el = threadIdx.x; el < ne; el += nthr) {
+      const double* eb = base + el * per;
+      double m1 = 0.0, m2 = 0.0;
+      for (int node = 0; node < nn; ++node) {
+        m1 = fmax(m1, eb[node * 3]);
+        m2 = fmax(m2, eb[node * 3 + 1]);
+      }
+      const int e = G.e0 + el_first + el;
+      atomic_max_nonneg(st.max_speed + (st.member ? st.member[e] : 0), n * (m1 + m2));
+    }
+  }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_cov_element(CovParams P, const CovGroups* __restrict__ GG,
+                                                     const BasisDev* __restrict__ bases,
+                                                     double* __restrict__ u,
+                                                     double* __restrict__ du,
+                                                     double* __restrict__ kreg,
+                                                     const double* __restrict__ pk,
+                                                     const double* __restrict__ sfv, StageArgs st,
+                                                     unsigned* __restrict__ status) {
+  extern __shared__ double smem[];
+  const int gi = cov_find_group(*GG, blockIdx.x, false);
+  const CovGroup& G = GG->g[gi];
+  const int lblk = blockIdx.x - G.blk0;
+  unsigned bad = 0;
+  switch (G.n) {
+    case 4: cov_element_body<4, MODE>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
+    case 6: cov_element_body<6, MODE>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
+    case 8: cov_element_body<8, MODE>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
+    case 2: cov_element_body<2, MODE>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
+    case 3: cov_element_body<3, MODE>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
+    case 5: cov_element_body<5, MODE>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
+    case 7: cov_element_body<7, MODE>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
+    default: break;
+  }
+  if (bad) atomicOr(status, bad);
+}
+
+// scaled CFL speed n max_e(l1 + l2) of a host-set state, per member
+__global__ void k_cov_max_speed(CovParams P, const CovGroups* __restrict__ GG,
+                                const double* __restrict__ u, const double* __restrict__ pk,
+                                const int* __restrict__ member, double* __restrict__ max_speed,
+                                int nelem) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nelem) return;
+  int gi = 0;
+  for (int k = 1; k < GG->count; ++k)
+    if (GG->g[k].e0 <= e) gi = k;
+  const CovGroup& G = GG->g[gi];
+  const int n = G.n, nn = n * n;
+  const long q0 = G.node0 + (long)(e - G.e0) * nn;
+  double m1 = 0.0, m2 = 0.0;
+  for (int node = 0; node < nn; ++node) {
+    const double* uq = u + (q0 + node) * 3;
+    const double* p = pk + (q0 + node) * kPack;
+    m1 = fmax(m1, fabs(uq[1] / uq[0]) + sqrt(p[kPGc11] * uq[0] * P.g));
+    m2 = fmax(m2, fabs(uq[2] / uq[0]) + sqrt(p[kPGc22] * uq[0] * P.g));
+  }
+  atomic_max_nonneg(max_speed + (member ? member[e] : 0), n * (m1 + m2));
+}
+
+}  // namespace tag

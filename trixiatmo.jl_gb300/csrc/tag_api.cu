@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "dg2d_kernels.cuh"
+#include "cov_kernels.cuh"
 #include "dg3d_kernels.cuh"
 #include "newton_rainy.cuh"
 #include "phys_euler_energy_2d.cuh"
@@ -44,6 +45,17 @@ void tag::set_last_error(const std::string& msg) { g_last_error = msg; }
 struct tag_handle_s {
   int eq = 0, n = 0, nelem = 0, nif = 0, nbd = 0, nv = 0, na = 0;
   int dim = 2, npe = 0, nface = 4, jpn = 4;  // nodes per element, faces, Ja doubles per node
+  long nodes = 0;                            // solution nodes (all elements)
+  int dt_n = 0;                              // n in dt = cfl 2 / (n max_speed); 1 when
+                                             // the kernels reduce n-scaled speeds
+  // covariant equations: element groups, geometry, packed element data
+  CovParams p_cov{};
+  CovGroups h_groups{};
+  CovGroups* d_groups = nullptr;
+  BasisDev* d_bases = nullptr;
+  double *d_aux = nullptr, *d_pk = nullptr;
+  int cov_blocks = 0, cov_iblocks = 0, cov_threads = 0;
+  size_t cov_smem = 0;
   PhysEnergy2D::Params p_energy{};
   PhysEnergy3D::Params p_energy3d{};
   PhysRainy2D::Params p_rainy{};
@@ -318,7 +330,7 @@ MemberScalars member_scalars(tag_handle h) {
 
 int begin_step(tag_handle h) {
   k_begin_step<<<(h->nmembers + 127) / 128, 128, 0, h->stream>>>(member_scalars(h), h->d_ctl,
-                                                                  h->nmembers, h->n);
+                                                                  h->nmembers, h->dt_n);
   TAG_CUDA(cudaGetLastError());
   return TAG_OK;
 }
@@ -342,7 +354,7 @@ int stage_sequence(tag_handle h) {
     if (rc) return rc;
     if (h->has_limiter) {
       // stage limiter: saturation Newton solve on every node (warm start)
-      const long nodes = (long)h->nelem * h->npe;
+      const long nodes = (long)h->nodes;
       NewtonArgs a = h->newton;
       a.learned = 0;
       a.iters = nullptr;
@@ -386,7 +398,7 @@ int autotune(tag_handle h, const double* u) {
   TAG_CUDA(cudaGetDevice(&dev));
   int max_smem = 0;
   TAG_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  if (!h->d_tmp_du) TAG_CUDA(cudaMalloc(&h->d_tmp_du, sizeof(double) * h->nelem * h->npe * h->nv));
+  if (!h->d_tmp_du) TAG_CUDA(cudaMalloc(&h->d_tmp_du, sizeof(double) * h->nodes * h->nv));
   cudaEvent_t a, b;
   TAG_CUDA(cudaEventCreate(&a));
   TAG_CUDA(cudaEventCreate(&b));
@@ -431,6 +443,245 @@ __global__ void k_fp64_probe(double* out, int iters, double seed) {
     a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
   }
   out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+// ---- covariant equations (element groups of possibly different degree) ------
+int cov_interface(tag_handle h, const double* u) {
+  if (h->cov_iblocks == 0) return TAG_OK;
+  k_cov_interface<<<h->cov_iblocks, 256, 0, h->stream>>>(h->p_cov, h->d_groups, u, h->d_aux,
+                                                         h->d_if_e, h->d_if_f, h->d_if_flip,
+                                                         h->d_sfv);
+  TAG_CUDA(cudaGetLastError());
+  return TAG_OK;
+}
+
+int cov_element(tag_handle h, int mode, double* u, double* du, int stage, bool last, double) {
+  const CK2N54 ck = ck2n54();
+  StageArgs st{};
+  st.member = h->d_member;
+  if (mode == kModeStage) {
+    st.A = ck.A[stage];
+    st.B = ck.B[stage];
+    st.c_stage = ck.c[stage];
+    st.t_member = h->d_mscal;
+    st.dt = h->d_mscal + h->nmembers;
+    st.max_speed = last ? h->d_mscal + 2 * h->nmembers : nullptr;
+    k_cov_element<kModeStage><<<h->cov_blocks, h->cov_threads, h->cov_smem, h->stream>>>(
+        h->p_cov, h->d_groups, h->d_bases, u, du, h->d_k, h->d_pk, h->d_sfv, st, h->d_status);
+  } else {
+    k_cov_element<kModeRhs><<<h->cov_blocks, h->cov_threads, h->cov_smem, h->stream>>>(
+        h->p_cov, h->d_groups, h->d_bases, u, du, h->d_k, h->d_pk, h->d_sfv, st, h->d_status);
+  }
+  TAG_CUDA(cudaGetLastError());
+  return TAG_OK;
+}
+
+int cov_max_speed(tag_handle h, const double* u) {
+  k_cov_max_speed<<<(h->nelem + 127) / 128, 128, 0, h->stream>>>(
+      h->p_cov, h->d_groups, u, h->d_pk, h->d_member, h->d_mscal + 2 * h->nmembers, h->nelem);
+  TAG_CUDA(cudaGetLastError());
+  return TAG_OK;
+}
+
+int cov_init(int max_smem) {
+  TAG_CUDA(cudaFuncSetAttribute(k_cov_element<kModeStage>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  TAG_CUDA(cudaFuncSetAttribute(k_cov_element<kModeRhs>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  return TAG_OK;
+}
+
+size_t cov_smem_bytes(int) { return 0; }
+int cov_max_threads() { return 256; }
+
+const Ops kCovOps{&cov_interface, &cov_element, &cov_max_speed, &cov_init, &cov_smem_bytes, 256,
+                  &cov_max_threads};
+
+// Flux options of a covariant member configuration; returns the reason it is
+// rejected, or null.
+const char* cov_params(const tag_config* c, CovParams& P, double& omega) {
+  if (c->equations != TAG_EQ_COVARIANT_SWE) return "every member must use the covariant equations";
+  P = CovParams{};
+  P.g = c->params[0];
+  omega = c->params[1];
+  P.split = c->params[2] != 0.0;
+  P.vol_nc = (int)c->params[3];
+  P.surf_nc = (int)c->params[4];
+  switch (c->volume_flux) {
+    case TAG_VF_WEAK_FORM: P.volume = 0; break;
+    case TAG_VF_COV_CENTRAL: P.volume = 1; P.vol_sym = 0; break;
+    case TAG_VF_COV_EC: P.volume = 1; P.vol_sym = 1; break;
+    default: return "unsupported volume flux for the covariant equations";
+  }
+  switch (c->surface_flux) {
+    case TAG_SF_LAX_FRIEDRICHS: P.surf_sym = 0; P.surf_diss = 1; break;
+    case TAG_SF_COV_CENTRAL: P.surf_sym = 0; P.surf_diss = 0; break;
+    case TAG_SF_COV_EC: P.surf_sym = 1; P.surf_diss = 0; break;
+    case TAG_SF_COV_EC_LLF: P.surf_sym = 1; P.surf_diss = 1; break;
+    default: return "unsupported surface flux for the covariant equations";
+  }
+  if (P.vol_nc < 0 || P.vol_nc > 1 || P.surf_nc < 0 || P.surf_nc > 2)
+    return "unsupported nonconservative flux id";
+  if ((P.vol_nc || P.surf_nc || P.vol_sym) && !P.split)
+    return "flux_ec and the nonconservative fluxes need the split form";
+  if (P.volume == 0 && P.vol_nc) return "the weak form has no nonconservative volume term";
+  if (!(P.g > 0.0)) return "gravity must be positive";
+  return nullptr;
+}
+
+int create_cov(const tag_config* cfgs, int m, tag_handle* out) {
+  if (m < 1) return fail(TAG_E_INVALID, "no members");
+  CovParams P;
+  double omega = 0.0;
+  if (const char* why = cov_params(&cfgs[0], P, omega)) return fail(TAG_E_INVALID, why);
+  for (int k = 1; k < m; ++k) {
+    CovParams Q;
+    double om2;
+    if (const char* why = cov_params(&cfgs[k], Q, om2)) return fail(TAG_E_INVALID, why);
+    if (std::memcmp(&Q, &P, sizeof(P)) != 0 || om2 != omega)
+      return fail(TAG_E_INVALID, "members must share equations and fluxes");
+  }
+  long nodes = 0, sf = 0;
+  int nelem = 0, nif = 0, max_n = 0;
+  for (int k = 0; k < m; ++k) {
+    const tag_config* c = &cfgs[k];
+    const int n = c->polydeg + 1;
+    if (n < 2 || n > kMaxNodes) return fail(TAG_E_INVALID, "polydeg out of range 1..7");
+    if (c->nelements <= 0 || c->ninterfaces < 0 || c->nboundaries != 0)
+      return fail(TAG_E_INVALID, "bad mesh sizes (the covariant solver has no boundaries)");
+    if (!c->derivative_split || !c->weights || !c->aux_node_vars || !c->node_coordinates)
+      return fail(TAG_E_INVALID, "missing basis, aux_node_vars or node_coordinates");
+    for (int i = 0; i < c->ninterfaces; ++i) {
+      for (int sd = 0; sd < 2; ++sd) {
+        const int e = c->interface_elements[2 * i + sd], f = c->interface_faces[2 * i + sd];
+        if (e < 0 || e >= c->nelements || f < 0 || f > 3)
+          return fail(TAG_E_INVALID, "interface index out of range");
+      }
+      const int o = c->interface_flip ? c->interface_flip[i] : 0;
+      if (o < 0 || o > 1) return fail(TAG_E_INVALID, "interface orientation out of range");
+    }
+    nodes += (long)c->nelements * n * n;
+    sf += (long)c->nelements * 4 * n * 3;
+    nelem += c->nelements;
+    nif += c->ninterfaces;
+    max_n = std::max(max_n, n);
+  }
+  // groups: runs of members with the same degree
+  CovGroups G{};
+  std::vector<BasisDev> bases;
+  std::vector<double> aux((size_t)nodes * 26), xyz((size_t)nodes * 3);
+  std::vector<int> ie((size_t)2 * nif), ifc((size_t)2 * nif), ifl((size_t)nif), member(nelem);
+  long node_off = 0, sf_off = 0;
+  int e_off = 0, if_off = 0, blk = 0, iblk = 0;
+  size_t smem = 0;
+  for (int k = 0; k < m; ++k) {
+    const tag_config* c = &cfgs[k];
+    const int n = c->polydeg + 1, nn = n * n;
+    if (G.count == 0 || G.g[G.count - 1].n != n) {
+      if (G.count == kCovMaxGroups) return fail(TAG_E_INVALID, "too many degree runs (max 64)");
+      CovGroup& g = G.g[G.count++];
+      g.n = n;
+      g.e0 = e_off;
+      g.ne = 0;
+      g.node0 = node_off;
+      g.sf0 = sf_off;
+      g.if0 = if_off;
+      g.nif = 0;
+      g.epb = std::max(1, 256 / nn);
+      g.basis = (int)bases.size();
+      BasisDev b;
+      load_basis(b, c->derivative_split, c->weights, n);
+      bases.push_back(b);
+    }
+    CovGroup& g = G.g[G.count - 1];
+    const size_t q0 = (size_t)node_off;
+    std::memcpy(&aux[q0 * 26], c->aux_node_vars, sizeof(double) * (size_t)c->nelements * nn * 26);
+    std::memcpy(&xyz[q0 * 3], c->node_coordinates, sizeof(double) * (size_t)c->nelements * nn * 3);
+    for (int i = 0; i < c->ninterfaces; ++i) {
+      ie[2 * (if_off + i)] = c->interface_elements[2 * i] + e_off;
+      ie[2 * (if_off + i) + 1] = c->interface_elements[2 * i + 1] + e_off;
+      ifc[2 * (if_off + i)] = c->interface_faces[2 * i];
+      ifc[2 * (if_off + i) + 1] = c->interface_faces[2 * i + 1];
+      ifl[if_off + i] = c->interface_flip ? c->interface_flip[i] : 0;
+    }
+    for (int e = 0; e < c->nelements; ++e) member[e_off + e] = k;
+    g.ne += c->nelements;
+    g.nif += c->ninterfaces;
+    node_off += (long)c->nelements * nn;
+    sf_off += (long)c->nelements * 4 * n * 3;
+    e_off += c->nelements;
+    if_off += c->ninterfaces;
+  }
+  for (int k = 0; k < G.count; ++k) {
+    CovGroup& g = G.g[k];
+    g.blk0 = blk;
+    blk += (g.ne + g.epb - 1) / g.epb;
+    g.iblk0 = iblk;
+    iblk += (g.nif * g.n + 255) / 256;
+    smem = std::max(smem, sizeof(double) * (size_t)g.epb * cov_elem_doubles(g.n));
+  }
+  tag_handle h = new tag_handle_s();
+  h->eq = TAG_EQ_COVARIANT_SWE;
+  h->n = max_n;
+  h->nelem = nelem;
+  h->nif = nif;
+  h->nbd = 0;
+  h->nmembers = m;
+  h->dim = 2;
+  h->nface = 4;
+  h->npe = max_n * max_n;
+  h->jpn = 0;
+  h->nodes = nodes;
+  h->dt_n = 1;  // the kernels reduce n-scaled speeds
+  h->nv = 3;
+  h->na = 3;
+  h->p_cov = P;
+  h->h_groups = G;
+  h->cov_blocks = blk;
+  h->cov_iblocks = iblk;
+  h->cov_threads = 256;
+  h->cov_smem = smem + sizeof(BasisDev);
+  h->epb = 1;  // tiling is per group; no autotuning
+  h->ops = &kCovOps;
+  auto cleanup = [&](int rc) {
+    tag_destroy(h);
+    return rc;
+  };
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return cleanup(fail(TAG_E_CUDA, "stream create failed"));
+  int rc = TAG_OK;
+  if ((rc = upload(&h->d_u, (const double*)nullptr, (size_t)nodes * 3, h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_k, (const double*)nullptr, (size_t)nodes * 3, h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_aux, aux.data(), aux.size(), h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_xy, xyz.data(), xyz.size(), h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_pk, (const double*)nullptr, (size_t)nodes * kPack, h->stream)))
+    return cleanup(rc);
+  if ((rc = upload(&h->d_sfv, (const double*)nullptr, (size_t)sf, h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_if_e, ie.data(), ie.size(), h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_if_f, ifc.data(), ifc.size(), h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_if_flip, ifl.data(), ifl.size(), h->stream))) return cleanup(rc);
+  if (m > 1)
+    if ((rc = upload(&h->d_member, member.data(), member.size(), h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_groups, &h->h_groups, 1, h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_bases, bases.data(), bases.size(), h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_mscal, (const double*)nullptr, (size_t)3 * m, h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_ctl, (const StepCtl*)nullptr, 1, h->stream))) return cleanup(rc);
+  if ((rc = upload(&h->d_status, (const unsigned*)nullptr, 1, h->stream))) return cleanup(rc);
+  if (cudaMallocHost(&h->h_pin, sizeof(double) * (3 * m + 2)) != cudaSuccess)
+    return cleanup(fail(TAG_E_CUDA, "pinned alloc failed"));
+  k_cov_pack<<<(unsigned)((nodes + 255) / 256), 256, 0, h->stream>>>(h->d_aux, h->d_xy, nodes,
+                                                                      omega, h->d_pk);
+  if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(h->stream) != cudaSuccess)
+    return cleanup(fail(TAG_E_CUDA, "upload failed"));
+  {
+    int dev = 0, max_smem = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (h->cov_smem > (size_t)max_smem) return cleanup(fail(TAG_E_INVALID, "tile too large"));
+    if ((rc = h->ops->init(max_smem))) return cleanup(rc);
+  }
+  *out = h;
+  return TAG_OK;
 }
 
 // Supported (equations, volume flux, surface flux, source) combinations;
@@ -495,6 +746,7 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
     return fail(TAG_E_NO_DEVICE, "no CUDA device visible");
+  if (cfg->equations == TAG_EQ_COVARIANT_SWE) return create_cov(cfg, 1, out);
   const char* why = check_equations(cfg);
   if (why) return fail(TAG_E_INVALID, why);
   const int dim = cfg->equations == TAG_EQ_EULER_ENERGY_3D ? 3 : 2;
@@ -547,6 +799,8 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
   h->dim = dim;
   h->nface = nface;
   h->npe = dim == 3 ? n * n * n : n * n;
+  h->nodes = (long)h->nelem * h->npe;
+  h->dt_n = n;
   h->jpn = dim * dim;
   if (rainy) {
     h->nv = PhysRainy2D::NV;
@@ -580,7 +834,7 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
   };
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
     return cleanup(fail(TAG_E_CUDA, "stream create failed"));
-  const size_t nodes = (size_t)h->nelem * h->npe;
+  const size_t nodes = (size_t)h->nodes;
   const size_t face_nodes = (size_t)h->nelem * nface * (dim == 3 ? n * n : n);
   int rc = TAG_OK;
   if ((rc = upload(&h->d_u, (const double*)nullptr, nodes * h->nv, h->stream))) return cleanup(rc);
@@ -625,6 +879,16 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
   return TAG_OK;
 }
 
+int tag_create_ensemble(const tag_config* members, int32_t nmembers, tag_handle* out) {
+  if (!members || !out || nmembers < 1) return fail(TAG_E_INVALID, "bad argument");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(TAG_E_NO_DEVICE, "no CUDA device visible");
+  if (members[0].equations != TAG_EQ_COVARIANT_SWE)
+    return fail(TAG_E_INVALID, "tag_create_ensemble supports the covariant equations");
+  return create_cov(members, nmembers, out);
+}
+
 int tag_destroy(tag_handle h) {
   if (!h) return TAG_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
@@ -636,6 +900,10 @@ int tag_destroy(tag_handle h) {
   for (int* p : ip)
     if (p) cudaFree(p);
   if (h->d_member) cudaFree(h->d_member);
+  if (h->d_aux) cudaFree(h->d_aux);
+  if (h->d_pk) cudaFree(h->d_pk);
+  if (h->d_groups) cudaFree(h->d_groups);
+  if (h->d_bases) cudaFree(h->d_bases);
   if (h->d_mlp) cudaFree(h->d_mlp);
   if (h->d_counters) cudaFree(h->d_counters);
   if (h->d_iters) cudaFree(h->d_iters);
@@ -649,7 +917,7 @@ int tag_destroy(tag_handle h) {
 }
 
 int64_t tag_ndofs_total(tag_handle h) {
-  return h ? (int64_t)h->nelem * h->npe * h->nv : -1;
+  return h ? (int64_t)h->nodes * h->nv : -1;
 }
 
 int tag_rhs(tag_handle h, const double* u, double* du, double t, int32_t on_device) {
@@ -679,7 +947,7 @@ int tag_set_state(tag_handle h, const double* u_host) {
   if (!h || !u_host) return fail(TAG_E_INVALID, "null argument");
   TAG_CUDA(cudaMemcpyAsync(h->d_u, u_host, sizeof(double) * (size_t)tag_ndofs_total(h),
                            cudaMemcpyHostToDevice, h->stream));
-  TAG_CUDA(cudaMemsetAsync(h->d_k, 0, sizeof(double) * (size_t)h->nelem * h->npe * h->na,
+  TAG_CUDA(cudaMemsetAsync(h->d_k, 0, sizeof(double) * (size_t)h->nodes * h->na,
                            h->stream));
   TAG_CUDA(cudaStreamSynchronize(h->stream));
   h->speed_valid = false;
@@ -711,7 +979,7 @@ int tag_max_dt_members(tag_handle h, double* out) {
   for (int m = 0; m < h->nmembers; ++m) {
     double ms = h->h_pin[m];
     if (!(ms > 0.0)) ms = 4.9406564584124654e-324;
-    out[m] = 2.0 / (h->n * ms);
+    out[m] = 2.0 / (h->dt_n * ms);
   }
   h->speed_valid = true;
   return TAG_OK;
@@ -818,7 +1086,7 @@ int tag_set_mlp(tag_handle h, const float* params) {
 int tag_newton_solve(tag_handle h, int32_t use_learned, int32_t* iters, tag_newton_stats* stats) {
   if (!h || !h->has_limiter) return fail(TAG_E_INVALID, "not a rainy handle");
   if (use_learned && !h->d_mlp) return fail(TAG_E_INVALID, "no MLP parameters set");
-  const long nodes = (long)h->nelem * h->npe;
+  const long nodes = (long)h->nodes;
   NewtonArgs a = h->newton;
   a.learned = use_learned ? 1 : 0;
   a.mlp = h->d_mlp;

@@ -231,6 +231,14 @@ class _Handle:
 
 
 class SemidiscretizationHyperbolic:
+    def __new__(cls, *args, **kwargs):
+        # covariant equations take the covariant constructor (aux variables)
+        eq = args[1] if len(args) > 1 else kwargs.get("equations")
+        from .covariant import CovariantShallowWaterEquations2D
+        if cls is SemidiscretizationHyperbolic and isinstance(eq, CovariantShallowWaterEquations2D):
+            return object.__new__(SemidiscretizationCovariant)
+        return object.__new__(cls)
+
     def __init__(self, mesh, equations, initial_condition, solver, *, boundary_conditions=None,
                  source_terms=None):
         self.mesh = mesh
@@ -409,3 +417,187 @@ def fp64_peak():
     v = ctypes.c_double()
     _lib.check(_lib.load().tag_fp64_peak(ctypes.byref(v)))
     return v.value
+
+
+# ---- covariant equations on the cubed sphere -----------------------------------------
+def _cov_flux_ids(equations, solver):
+    """(volume id, surface id, volume nonconservative, surface nonconservative)
+    of a covariant solver (dg_2d_manifold_in_3d_covariant.jl:98-432)."""
+    from . import covariant as cv
+    vi = solver.volume_integral
+    vnc = 0
+    if isinstance(vi, VolumeIntegralWeakForm):
+        vid = _lib.TAG_VF_WEAK_FORM
+    else:
+        vf = vi.volume_flux
+        sym, nc = (vf if isinstance(vf, tuple) else (vf, None))
+        vid = {id(cv.flux_central): _lib.TAG_VF_COV_CENTRAL,
+               id(cv.flux_ec): _lib.TAG_VF_COV_EC}.get(id(sym))
+        if vid is None:
+            raise ValueError(f"unsupported covariant volume flux {sym}")
+        if nc is not None:
+            if nc is not cv.flux_nonconservative_ec:
+                raise ValueError(f"unsupported nonconservative volume flux {nc}")
+            vnc = 1
+    sf = solver.surface_flux
+    sym, nc = (sf if isinstance(sf, tuple) else (sf, None))
+    if sym is flux_lax_friedrichs:
+        sid = _lib.TAG_SF_LAX_FRIEDRICHS
+    elif sym is cv.flux_central:
+        sid = _lib.TAG_SF_COV_CENTRAL
+    elif sym is cv.flux_ec:
+        sid = _lib.TAG_SF_COV_EC
+    elif isinstance(sym, cv.FluxPlusDissipation) and isinstance(sym.dissipation,
+                                                               cv.DissipationLocalLaxFriedrichs):
+        if sym.numerical_flux is cv.flux_ec:
+            sid = _lib.TAG_SF_COV_EC_LLF
+        elif sym.numerical_flux is cv.flux_central:
+            sid = _lib.TAG_SF_LAX_FRIEDRICHS
+        else:
+            raise ValueError(f"unsupported covariant surface flux {sym.numerical_flux}")
+    else:
+        raise ValueError(f"unsupported covariant surface flux {sym}")
+    snc = 0
+    if nc is cv.flux_nonconservative_ec:
+        snc = 1
+    elif nc is cv.flux_nonconservative_surface_simplified:
+        snc = 2
+    elif nc is not None:
+        raise ValueError(f"unsupported nonconservative surface flux {nc}")
+    return vid, sid, vnc, snc
+
+
+class _CovHandle:
+    """One tag_handle for one or more covariant members (mesh, solver,
+    bottom topography) of possibly different polynomial degree."""
+
+    def __init__(self, members, equations, source_terms, metric_terms):
+        from . import covariant as cv
+        if source_terms is not cv.source_terms_geometric_coriolis:
+            raise ValueError("the covariant path applies source_terms_geometric_coriolis")
+        L = _lib.load()
+        m = len(members)
+        cfgs = (_lib.TagConfig * m)()
+        self.keep = []
+        self.aux, self.xyz, self.ns, self.member_nelements = [], [], [], []
+        for k, (mesh, solver, topo) in enumerate(members):
+            basis = solver.basis
+            aux, xyz = cv.compute_aux_vars(mesh, basis, equations, metric_terms, topo)
+            conn = mesh.connectivity(basis)
+            ie, ifc, fl, _, _ = conn.arrays()
+            vid, sid, vnc, snc = _cov_flux_ids(equations, solver)
+            ds = np.asfortranarray(basis.derivative_split)
+            w = np.ascontiguousarray(basis.weights)
+            self.keep += [aux, xyz, ie, ifc, fl, ds, w]
+            c = cfgs[k]
+            c.equations = _lib.TAG_EQ_COVARIANT_SWE
+            c.volume_flux, c.surface_flux = vid, sid
+            c.polydeg = solver.polydeg
+            c.nelements = mesh.nelements
+            c.ninterfaces = ie.shape[0]
+            c.nboundaries = 0
+            c.nmembers = 1
+            c.derivative_split = ds.ctypes.data_as(_dp)
+            c.weights = _ptr(w)
+            c.node_coordinates = _ptr(xyz)
+            c.aux_node_vars = _ptr(aux)
+            c.interface_elements = _ptr(ie, _ip)
+            c.interface_faces = _ptr(ifc, _ip)
+            c.interface_flip = _ptr(fl, _ip)
+            for i, p in enumerate([equations.gravity, equations.rotation_rate,
+                                   1.0 if equations.split else 0.0, vnc, snc]):
+                c.params[i] = p
+            self.aux.append(aux)
+            self.xyz.append(xyz)
+            self.ns.append(basis.n)
+            self.member_nelements.append(mesh.nelements)
+        h = ctypes.c_void_p()
+        if m == 1:
+            _lib.check(L.tag_create(ctypes.byref(cfgs[0]), ctypes.byref(h)))
+        else:
+            _lib.check(L.tag_create_ensemble(cfgs, m, ctypes.byref(h)))
+        self.h, self.L = h, L
+        self.ndims = 2
+        self.nmembers = m
+        self.nelements = sum(self.member_nelements)
+        self.member_nodes = [e * n * n for e, n in zip(self.member_nelements, self.ns)]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.tag_destroy(self.h)
+            self.h = None
+
+
+class SemidiscretizationCovariant(SemidiscretizationHyperbolic):
+    """`SemidiscretizationHyperbolic` for the covariant shallow-water equations
+    on P4estMeshCubedSphere2D (the reference's constructor with `auxiliary_field`
+    and `metric_terms`, src/semidiscretization/semidiscretization_hyperbolic_2d_manifold_in_3d.jl:78-111).
+    The initial condition takes (x, t, aux, equations), as returned by
+    `transform_initial_condition`."""
+
+    def __init__(self, mesh, equations, initial_condition, solver, *, source_terms=None,
+                 boundary_conditions=None, auxiliary_field=None, metric_terms=None):
+        self.mesh = mesh
+        self.equations = equations
+        self.solver = solver
+        self.initial_condition = initial_condition
+        self.source_terms = source_terms
+        self._H = _CovHandle([(mesh, solver, auxiliary_field)], equations, source_terms,
+                             metric_terms)
+        self.n = solver.basis.n
+        self.nelements = mesh.nelements
+        self.nmembers = 1
+        self.aux_node_vars = self._H.aux[0]
+        self.node_coordinates = self._H.xyz[0]
+        self.contravariant_vectors = None
+        self.inverse_jacobian = None
+        self._h = self._H.h
+        self._L = self._H.L
+
+    def compute_coefficients(self, t=0.0, initial_condition=None):
+        ic = initial_condition or self.initial_condition
+        return np.ascontiguousarray(ic(self.node_coordinates, t, self.aux_node_vars),
+                                    dtype=np.float64)
+
+
+class SemidiscretizationCovariantEnsemble(SemidiscretizationHyperbolic):
+    """Independent covariant members — each its own cubed-sphere mesh, solver
+    (polynomial degree), bottom topography and initial condition — in one handle
+    (tag_create_ensemble).  The state is the members' states flattened and
+    concatenated; member_state(u, m) views member m as [E, n, n, 3]."""
+
+    def __init__(self, meshes, equations, initial_conditions, solvers, *, source_terms=None,
+                 auxiliary_fields=None, metric_terms=None):
+        m = len(meshes)
+        if not isinstance(solvers, (list, tuple)):
+            solvers = [solvers] * m
+        auxiliary_fields = auxiliary_fields or [None] * m
+        self.meshes, self.solvers = list(meshes), list(solvers)
+        self.equations = equations
+        self.initial_conditions = list(initial_conditions)
+        self._H = _CovHandle(list(zip(self.meshes, self.solvers, auxiliary_fields)), equations,
+                             source_terms, metric_terms)
+        self.nmembers = m
+        self.nelements = self._H.nelements
+        self.member_node_offsets = np.concatenate([[0], np.cumsum(self._H.member_nodes)])
+        self.n = max(self._H.ns)
+        self._h = self._H.h
+        self._L = self._H.L
+
+    @property
+    def shape(self):
+        return (int(self.member_node_offsets[-1]) * 3,)
+
+    @property
+    def ndofs(self):
+        return int(self.member_node_offsets[-1])
+
+    def member_state(self, u, m):
+        a, b = self.member_node_offsets[m] * 3, self.member_node_offsets[m + 1] * 3
+        n = self._H.ns[m]
+        return u[a:b].reshape(self._H.member_nelements[m], n, n, 3)
+
+    def compute_coefficients(self, t=0.0, initial_condition=None):
+        parts = [np.asarray(ic(self._H.xyz[k], t, self._H.aux[k]), dtype=np.float64).ravel()
+                 for k, ic in enumerate(self.initial_conditions)]
+        return np.ascontiguousarray(np.concatenate(parts))
