@@ -68,6 +68,10 @@ def perturbed(u, seed, amp=1e-2):
 @pytest.mark.parametrize("name", ["geostrophic_balance", "unsteady_solid_body_rotation",
                                   "isolated_mountain"])
 def test_cov_rhs_matches_oracle(tg, orc, gpu_lib, name, polydeg):
+    if name == "geostrophic_balance" and polydeg % 2 == 0:
+        # an even degree on 3 trees per face edge puts a node on a pole, where
+        # the spherical global coordinates of this case are singular
+        pytest.skip("pole node in spherical coordinates")
     eq, mesh, semi, fluxes, _ = make_semi(tg, name, k=3, polydeg=polydeg)
     u = perturbed(semi.compute_coefficients(), seed=polydeg)
     du = semi.rhs(u)
