@@ -172,6 +172,192 @@ def sequential_member_rate(tg, steps):
     return rate
 
 
+def swe_member_specs(nmembers, seed=5):
+    """Seeded uneven members: trees per face edge U{8..32}, polydeg from
+    {3, 5, 7}, Gaussian height bumps of 1-5 % on the geostrophic balance."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    specs = []
+    for m in range(nmembers):
+        k = int(rng.integers(8, 33))
+        N = int(rng.choice([3, 5, 7]))
+        amp = float(rng.uniform(0.01, 0.05))
+        z = rng.uniform(-1, 1)
+        lon = rng.uniform(-np.pi, np.pi)
+        c = np.array([np.sqrt(1 - z * z) * np.cos(lon), np.sqrt(1 - z * z) * np.sin(lon), z])
+        specs.append((k, N, amp, c))
+    return specs
+
+
+def make_swe_ensemble(tg, nmembers=64, variant="weak", seed=5, members=None):
+    """64 covariant shallow-water members of uneven size and degree on the
+    cubed sphere: weak form + flux_lax_friedrichs (elixir_geostrophic_balance)
+    or the split entropy-conservative form; Cartesian global coordinates."""
+    cv = tg.covariant
+    from trixiatmo_gb300.initial_conditions import (EARTH_GRAVITATIONAL_ACCELERATION as G,
+                                                    EARTH_RADIUS, EARTH_ROTATION_RATE as OM)
+    if variant == "ec":
+        eq = cv.SplitCovariantShallowWaterEquations2D(G, OM)
+    else:
+        eq = cv.CovariantShallowWaterEquations2D(G, OM)
+    specs = swe_member_specs(nmembers, seed)
+    if members is not None:
+        specs = [specs[m] for m in members]
+    meshes, solvers, ics = [], [], []
+    for k, N, amp, c in specs:
+        meshes.append(cv.P4estMeshCubedSphere2D(k, EARTH_RADIUS, polydeg=N))
+        if variant == "ec":
+            solvers.append(tg.DGSEM(N, (cv.FluxPlusDissipation(cv.flux_ec,
+                                                               cv.DissipationLocalLaxFriedrichs()),
+                                        cv.flux_nonconservative_surface_simplified),
+                                    tg.VolumeIntegralFluxDifferencing(
+                                        (cv.flux_ec, cv.flux_nonconservative_ec))))
+        else:
+            solvers.append(tg.DGSEM(N, tg.flux_lax_friedrichs, tg.VolumeIntegralWeakForm()))
+
+        def ic(x, t, e, amp=amp, c=c):
+            p = cv.initial_condition_geostrophic_balance(x, t, e)
+            r = x / np.sqrt((x ** 2).sum(-1, keepdims=True))
+            d2 = ((r - c) ** 2).sum(-1)
+            p[..., 0] *= 1 + amp * np.exp(-d2 / 0.05)
+            return p
+        ics.append(cv.transform_initial_condition(ic, eq))
+    ens = tg.SemidiscretizationCovariantEnsemble(meshes, eq, ics, solvers,
+                                                 source_terms=cv.source_terms_geometric_coriolis)
+    return eq, ens, specs, (meshes, solvers, ics)
+
+
+def run_swe(args):
+    """Uneven covariant shallow-water ensemble: whole-ensemble DOF·stage/s,
+    the same members run one by one, p50/p99 step latency."""
+    import torch
+    tg = entry.load_package()
+    torch.cuda.set_device(0)
+    t_build = time.perf_counter()
+    eq, ens, specs, parts = make_swe_ensemble(tg, args.swe_members, args.swe_variant)
+    t_build = time.perf_counter() - t_build
+    u0 = ens.compute_coefficients()
+    ens.set_state(u0)
+    M = ens.nmembers
+    dofs = ens.ndofs
+    stream = torch.cuda.ExternalStream(ens.stream())
+    t = ens.rk_steps(max(args.warmup, 1), cfl=0.4, t=np.zeros(M))
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    t = ens.rk_steps(args.steps, cfl=0.4, t=t)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clock_info = clocks.stop()
+    value = dofs * 5 * args.steps / (ms * 1e-3)
+    # per-step latency through the API (host-observed, one step per call)
+    lat = []
+    for _ in range(max(args.steps, 20)):
+        a = time.perf_counter()
+        t = ens.rk_steps(1, cfl=0.4, t=t)
+        lat.append((time.perf_counter() - a) * 1e3)
+    ms_if, ms_el = ens.time_kernels(reps=10)
+    # the same members one by one, each in its own handle
+    meshes, solvers, ics = parts
+    seq_time = 0.0
+    for m in range(M):
+        alone = tg.SemidiscretizationHyperbolic(meshes[m], eq, ics[m], solvers[m],
+                                                source_terms=tg.covariant.source_terms_geometric_coriolis)
+        alone.set_state(np.ascontiguousarray(ens.member_state(u0, m)))
+        tm = alone.rk_steps(max(args.warmup, 1), cfl=0.4, t=0.0)
+        s = torch.cuda.ExternalStream(alone.stream())
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a0.record(s)
+        alone.rk_steps(args.steps, cfl=0.4, t=tm)
+        a1.record(s)
+        torch.cuda.synchronize()
+        seq_time += a0.elapsed_time(a1)
+        alone.close()
+    seq_value = dofs * 5 * args.steps / (seq_time * 1e-3)
+    # end to end through the C ABI: H2D of the state, one step, D2H
+    u_pin = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True).numpy()
+    u_pin[...] = u0
+    t_e = np.zeros(M)
+    a = time.perf_counter()
+    for _ in range(args.steps):
+        ens.set_state(u_pin)
+        t_e = ens.rk_steps(1, cfl=0.4, t=t_e)
+        ens.get_state(u_pin)
+    e2e = dofs * 5 * args.steps / (time.perf_counter() - a)
+    # bytes per element launch (stage mode): u, k read + written, packed
+    # metric data (16 doubles) read per node, outward surface fluxes read
+    nodes = dofs
+    face_doubles = sum(6 * k * k * 4 * (N + 1) * 3 for k, N, _, _ in specs)
+    by = 8 * (nodes * (3 + 3 + 16 + 3 + 3) + face_doubles)
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        hbm_peak, hbm_src = float(peaks["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        hbm_peak, hbm_src = 6800.0, "fallback"
+    gbs = by / (ms_el * 1e-3) / 1e9
+    cpu = None
+    if not args.no_cpu:
+        orc = entry.load_oracle()
+        orc.build()
+        sample = list(range(min(4, M)))
+        _, ens_s, specs_s, _ = make_swe_ensemble(tg, args.swe_members, args.swe_variant,
+                                                 members=sample)
+        cov_ids = dict(volume=0, surf_sym=0, surf_diss=1) if args.swe_variant == "weak" else \
+            dict(volume=1, vol_sym=1, vol_nc=1, surf_sym=1, surf_diss=1, surf_nc=2)
+        a = time.perf_counter()
+        cdofs = 0
+        for i, m in enumerate(sample):
+            mesh = ens_s.meshes[i]
+            basis = ens_s.solvers[i].basis
+            conn = mesh.connectivity(basis)
+            ie, ifc, fl, _, _ = conn.arrays()
+            c = orc.CovSWE(basis.n - 1, ens_s._H.aux[i], ens_s._H.xyz[i], ie, ifc, fl,
+                           eq.gravity, eq.rotation_rate, eq.split, cov_ids)
+            um = np.ascontiguousarray(ens_s.member_state(ens_s.compute_coefficients(), i))
+            c.ck_steps(um, np.zeros_like(um), 0.0, 0.4, args.cpu_steps)
+            cdofs += um.size // 3
+        cel = time.perf_counter() - a
+        ens_s.close()
+        cpu = {"value": cdofs * 5 * args.cpu_steps / cel, "unit": UNIT,
+               "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
+               "kind": "port",
+               "sample": f"{len(sample)} of the members x {args.cpu_steps} CK2N54 steps, oracle/ "
+                         f"C++ OpenMP ({cel:.1f} s)"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": f"{M} covariant shallow-water members on the cubed sphere, trees "
+                               f"per face edge U{{8..32}}, polydeg in {{3, 5, 7}}, geostrophic "
+                               f"balance + 1-5 % height bumps, "
+                               f"{'weak form + LLF' if args.swe_variant == 'weak' else 'split EC'}"
+                               f", CK2N54 CFL 0.4, per-member dt",
+                   "dofs": dofs, "elements": ens.nelements, "members": M,
+                   "degree_runs": int(ens._H.nmembers), "build_seconds": t_build,
+                   "l2": "inputs larger than L2 (u + k + packed metric data)"},
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": gbs / hbm_peak, "traffic": None,
+                     "kernel": "k_cov_element (volume + surface + Jacobian + sources + RK stage)",
+                     "peak_source": hbm_src, "ms_element": ms_el, "ms_interface": ms_if,
+                     "bytes_per_launch": by},
+        "ensemble_vs_sequential": {"sequential_rate": seq_value, "speedup": value / seq_value},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                       "steps": len(lat)},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(u0.nbytes),
+                "d2h_bytes_per_step": int(u0.nbytes)},
+        "gpu_launches": args.steps * 11,
+        "clocks": clock_info,
+        "status": ens.status(),
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line))
+    ens.close()
+
+
 def flops_per_element_launch_3d(n, nelem):
     """FP64 flops of one 3D element-kernel launch, counted from the reference
     formulas: per symmetric pair 120 (flux_ranocha 3D with its two logarithmic
@@ -518,7 +704,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="shell", choices=["shell", "ensemble"])
+    ap.add_argument("--workload", default="shell", choices=["shell", "ensemble", "swe"])
+    ap.add_argument("--swe-members", type=int, default=64)
+    ap.add_argument("--swe-variant", default="weak", choices=["weak", "ec"])
     ap.add_argument("--cpu-steps-shell", type=int, default=2)
     ap.add_argument("--members", type=int, default=256)
     ap.add_argument("--cpu-members", type=int, default=64)
@@ -529,6 +717,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "swe":
+        run_swe(args)
     else:
         run_ours(args)
 

@@ -358,6 +358,16 @@ def compute_aux_vars(mesh, basis, equations, metric_terms=None, bottom_topograph
     (containers_2d_manifold_in_3d_covariant.jl:247-295, 379-441, 455-490)."""
     metric_terms = metric_terms or MetricTermsCovariantSphere()
     spherical = isinstance(equations.global_coordinate_system, GlobalSphericalCoordinates)
+    key = (basis.n, spherical, type(metric_terms.christoffel_symbols).__name__,
+           id(bottom_topography))
+    cache = mesh.__dict__.setdefault("_aux_cache", {})
+    if key in cache:
+        return cache[key]
+    cache[key] = _compute_aux_vars(mesh, basis, metric_terms, spherical, bottom_topography)
+    return cache[key]
+
+
+def _compute_aux_vars(mesh, basis, metric_terms, spherical, bottom_topography):
     n = basis.n
     E = mesh.nelements
     X1, X2 = np.meshgrid(basis.nodes, basis.nodes, indexing="xy")  # [j, i]
