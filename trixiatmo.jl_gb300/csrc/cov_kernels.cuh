@@ -168,94 +168,95 @@ TAG_DEV void cov_source(const CovParams& P, const double* u, const double* p, do
 }
 
 // ---- interface fluxes ------------------------------------------------------------
-// aux accessors of the reference layout
-TAG_DEV double cov_A(const double* a, int r, int c) { return a[c * 3 + r]; }
-TAG_DEV double cov_Acon(const double* a, int r, int c) { return a[6 + c * 2 + r]; }
-TAG_DEV double cov_agc(const double* a, int i, int j) {
-  return (i == 0 && j == 0) ? a[16] : (i == 1 && j == 1) ? a[18] : a[17];
+// Geometry of one side of an interface node (the reference's aux layout: A
+// column-major at 0..5, the contravariant basis column-major at 6..11, J at
+// 12, G_11 G_12 G_22 at 13..15, G^11 G^12 G^22 at 16..18).
+struct CovSide {
+  double A[6], Ac[6], J, gv11, gv12, gv22, gc11, gc12, gc22;
+};
+
+TAG_DEV void cov_load_side(const double* __restrict__ a, CovSide& s) {
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    s.A[k] = a[k];
+    s.Ac[k] = a[6 + k];
+  }
+  s.J = a[12];
+  s.gv11 = a[13]; s.gv12 = a[14]; s.gv22 = a[15];
+  s.gc11 = a[16]; s.gc12 = a[17]; s.gc22 = a[18];
 }
 
 // state of another node in the contravariant basis of `to`
-TAG_DEV void cov_transform(const double* u, const double* from, const double* to, double* s) {
+TAG_DEV void cov_transform(const double* u, const CovSide& from, const CovSide& to, double* s) {
   double gl[3];
 #pragma unroll
-  for (int r = 0; r < 3; ++r) gl[r] = cov_A(from, r, 0) * u[1] + cov_A(from, r, 1) * u[2];
+  for (int r = 0; r < 3; ++r) gl[r] = from.A[r] * u[1] + from.A[3 + r] * u[2];
   s[0] = u[0];
 #pragma unroll
-  for (int r = 0; r < 2; ++r)
-    s[1 + r] = cov_Acon(to, r, 0) * gl[0] + cov_Acon(to, r, 1) * gl[1] + cov_Acon(to, r, 2) * gl[2];
+  for (int r = 0; r < 2; ++r) s[1 + r] = to.Ac[r] * gl[0] + to.Ac[2 + r] * gl[1] + to.Ac[4 + r] * gl[2];
 }
 
-// contravariant flux from reference-layout aux (surface version of cov_flux)
-TAG_DEV void cov_flux_aux(const CovParams& P, const double* u, const double* a, int o, double* f) {
-  const double J = a[12];
-  const double m = J * u[1 + o];
-  if (P.split) {
-    f[0] = m;
-    f[1] = m * (u[1] / u[0]);
-    f[2] = m * (u[2] / u[0]);
-    return;
-  }
-  const double vo = u[1 + o] / u[0];
-  const double gt = 0.5 * P.g * u[0] * u[0];
-  f[0] = m;
-  f[1] = J * (u[1] * vo + cov_agc(a, 0, o) * gt);
-  f[2] = J * (u[2] * vo + cov_agc(a, 1, o) * gt);
-}
-
-// surface flux (+ 0.5 nonconservative) of left state a, right state c, both
-// sides' geometry that of `own`
-TAG_DEV void cov_surface(const CovParams& P, const double* a, const double* c, const double* own,
+// surface flux (+ 0.5 nonconservative) along o of left state a and right
+// state c, both sides' geometry `w` (the reference passes aux_vars_ll twice)
+TAG_DEV void cov_surface(const CovParams& P, const double* a, const double* c, const CovSide& w,
                          int o, double* F) {
-  const double J = own[12];
+  const double J = w.J;
+  const double gco0 = o ? w.gc12 : w.gc11;  // G^{1o}
+  const double gco1 = o ? w.gc22 : w.gc12;  // G^{2o}
+  const double ao = o ? a[2] : a[1], co = o ? c[2] : c[1];
   if (P.surf_sym == 1) {
-    const double m = 0.5 * (J * a[1 + o] + J * c[1 + o]);
+    const double m = 0.5 * (J * ao + J * co);
     F[0] = m;
     F[1] = 0.5 * (a[1] / a[0] + c[1] / c[0]) * m;
     F[2] = 0.5 * (a[2] / a[0] + c[2] / c[0]) * m;
+  } else if (P.split) {
+    const double ma = J * ao, mc = J * co;
+    F[0] = 0.5 * (ma + mc);
+    F[1] = 0.5 * (ma * (a[1] / a[0]) + mc * (c[1] / c[0]));
+    F[2] = 0.5 * (ma * (a[2] / a[0]) + mc * (c[2] / c[0]));
   } else {
-    double fa[3], fc[3];
-    cov_flux_aux(P, a, own, o, fa);
-    cov_flux_aux(P, c, own, o, fc);
-#pragma unroll
-    for (int v = 0; v < 3; ++v) F[v] = 0.5 * (fa[v] + fc[v]);
+    const double va = ao / a[0], vc = co / c[0];
+    const double ga = 0.5 * P.g * a[0] * a[0], gc = 0.5 * P.g * c[0] * c[0];
+    F[0] = 0.5 * (J * ao + J * co);
+    F[1] = 0.5 * (J * (a[1] * va + gco0 * ga) + J * (c[1] * vc + gco0 * gc));
+    F[2] = 0.5 * (J * (a[2] * va + gco1 * ga) + J * (c[2] * vc + gco1 * gc));
   }
   if (P.surf_diss) {
-    const double goo = cov_agc(own, o, o);
-    const double lam = fmax(fabs(a[1 + o] / a[0]) + sqrt(goo * a[0] * P.g),
-                            fabs(c[1 + o] / c[0]) + sqrt(goo * c[0] * P.g));
-#pragma unroll
-    for (int v = 0; v < 3; ++v) F[v] += -0.5 * J * lam * (c[v] - a[v]);
+    const double goo = o ? w.gc22 : w.gc11;
+    const double lam = fmax(fabs(ao / a[0]) + sqrt(goo * a[0] * P.g),
+                            fabs(co / c[0]) + sqrt(goo * c[0] * P.g));
+    const double s = -0.5 * J * lam;
+    F[0] += s * (c[0] - a[0]);
+    F[1] += s * (c[1] - a[1]);
+    F[2] += s * (c[2] - a[2]);
   }
   if (P.surf_nc == 1) {
-    // flux_nonconservative_ec with both geometries `own` (no topography jump)
+    // flux_nonconservative_ec with both geometries `w` (no topography jump)
     const double vb0 = c[1] / c[0], vb1 = c[2] / c[0];
-    const double vc0 = own[13] * vb0 + own[14] * vb1;
-    const double vc1 = own[14] * vb0 + own[15] * vb1;
-    const double half_m = 0.5 * a[1 + o];
+    const double vc0 = w.gv11 * vb0 + w.gv12 * vb1;
+    const double vc1 = w.gv12 * vb0 + w.gv22 * vb1;
+    const double half_m = 0.5 * ao;
     const double ph = P.g * a[0] * c[0];
-    const double g0 = J * (half_m * (own[16] * vc0 + own[17] * vc1 - vb0) + cov_agc(own, 0, o) * ph);
-    const double g1 = J * (half_m * (own[17] * vc0 + own[18] * vc1 - vb1) + cov_agc(own, 1, o) * ph);
-    F[1] += 0.5 * g0;
-    F[2] += 0.5 * g1;
+    F[1] += 0.5 * (J * (half_m * (w.gc11 * vc0 + w.gc12 * vc1 - vb0) + gco0 * ph));
+    F[2] += 0.5 * (J * (half_m * (w.gc12 * vc0 + w.gc22 * vc1 - vb1) + gco1 * ph));
   } else if (P.surf_nc == 2) {
     const double ph = P.g * a[0] * c[0];
-    F[1] += 0.5 * (J * (cov_agc(own, 0, o) * ph));
-    F[2] += 0.5 * (J * (cov_agc(own, 1, o) * ph));
+    F[1] += 0.5 * (J * (gco0 * ph));
+    F[2] += 0.5 * (J * (gco1 * ph));
   }
 }
 
 // outward flux of one side (face f of its element)
 TAG_DEV void cov_side_flux(const CovParams& P, const double* mine, const double* other_in_mine,
-                           const double* own, int f, double* F) {
+                           const CovSide& w, int f, double* F) {
   const int o = f >> 1;
   if ((f & 1) == 0) {
-    cov_surface(P, other_in_mine, mine, own, o, F);
+    cov_surface(P, other_in_mine, mine, w, o, F);
     F[0] = -F[0];
     F[1] = -F[1];
     F[2] = -F[2];
   } else {
-    cov_surface(P, mine, other_in_mine, own, o, F);
+    cov_surface(P, mine, other_in_mine, w, o, F);
   }
 }
 
@@ -275,17 +276,15 @@ TAG_DEV void cov_interface_body(const CovParams& P, const CovGroup& G, int lblk,
   face_node(f1, l1, n, i1, j1);
   const long q0 = G.node0 + (long)(e0 - G.e0) * n * n + j0 * n + i0;
   const long q1 = G.node0 + (long)(e1 - G.e0) * n * n + j1 * n + i1;
-  double ul[3], ur[3], al[26], ar[26];
+  double ul[3], ur[3];
 #pragma unroll
   for (int v = 0; v < 3; ++v) {
     ul[v] = u[q0 * 3 + v];
     ur[v] = u[q1 * 3 + v];
   }
-#pragma unroll
-  for (int v = 0; v < 26; ++v) {
-    al[v] = aux[q0 * 26 + v];
-    ar[v] = aux[q1 * 26 + v];
-  }
+  CovSide al, ar;
+  cov_load_side(aux + q0 * 26, al);
+  cov_load_side(aux + q1 * 26, ar);
   double rt[3], lt[3], Fp[3], Fs[3];
   cov_transform(ur, ar, al, rt);
   cov_transform(ul, al, ar, lt);
@@ -323,9 +322,12 @@ __global__ void __launch_bounds__(256) k_cov_interface(CovParams P, const CovGro
 }
 
 // ---- element kernel --------------------------------------------------------------
-// shared memory per element (doubles): u [nn][3], pk [nn][16], weak-form
-// fluxes [2][nn][3]
-__host__ __device__ constexpr int cov_elem_doubles(int n) { return n * n * (3 + kPack + 6); }
+// One thread per node (epb * n^2 <= 256 threads).  Shared memory per node:
+// flux differencing: v1, v2, (G_cov v)_1, (G_cov v)_2, J hv^1, J hv^2, h, h_s, J,
+// G^11, G^12, G^22, g h^2 / 2 (13 doubles, an odd stride); weak form: the two
+// contravariant fluxes.
+constexpr int kCovQ = 13;
+__host__ __device__ constexpr int cov_elem_doubles(int n) { return n * n * kCovQ; }
 
 template <int n, int MODE>
 TAG_DEV void cov_element_body(const CovParams& P, const CovGroup& G, int lblk,
@@ -333,77 +335,104 @@ TAG_DEV void cov_element_body(const CovParams& P, const CovGroup& G, int lblk,
                               double* __restrict__ du, double* __restrict__ kreg,
                               const double* __restrict__ pk, const double* __restrict__ sfv,
                               StageArgs st, double* smem, unsigned& bad) {
-  constexpr int nn = n * n, per = cov_elem_doubles(n);
+  constexpr int nn = n * n;
   BasisDev* sb = reinterpret_cast<BasisDev*>(smem);
-  double* base = smem + sizeof(BasisDev) / sizeof(double);
-  const int nthr = blockDim.x;
+  double* q = smem + sizeof(BasisDev) / sizeof(double);
   const int el_first = lblk * G.epb;
   const int ne = min(G.epb, G.ne - el_first);
   if (ne <= 0) return;
-  for (int t = threadIdx.x; t < (int)(sizeof(BasisDev) / sizeof(double)); t += nthr)
+  for (int t = threadIdx.x; t < (int)(sizeof(BasisDev) / sizeof(double)); t += blockDim.x)
     smem[t] = reinterpret_cast<const double*>(bases + G.basis)[t];
-  const long q_first = G.node0 + (long)el_first * nn;
-  for (int t = threadIdx.x; t < ne * nn * 3; t += nthr) {
-    const int el = t / (nn * 3), r = t % (nn * 3);
-    base[el * per + r] = u[q_first * 3 + t];
-  }
-  for (int t = threadIdx.x; t < ne * nn * kPack; t += nthr) {
-    const int el = t / (nn * kPack), r = t % (nn * kPack);
-    base[el * per + nn * 3 + r] = pk[q_first * kPack + t];
+  const int el = threadIdx.x / nn, node = threadIdx.x % nn;
+  const bool act = el < ne;
+  const int i = node % n, j = node / n;
+  const long gq = G.node0 + (long)(el_first + el) * nn + node;
+  double ui[3];
+  double* qn = q + threadIdx.x * kCovQ;
+  const double* __restrict__ pg = pk + gq * kPack;  // re-read where needed (L1 hit)
+  if (act) {
+#pragma unroll
+    for (int v = 0; v < 3; ++v) ui[v] = u[gq * 3 + v];
+    double p[kPack];
+#pragma unroll
+    for (int k = 0; k < kPack; ++k) p[k] = __ldg(pg + k);
+    if (P.volume == 0) {
+      cov_flux(P, ui, p, 0, qn);
+      cov_flux(P, ui, p, 1, qn + 3);
+    } else {
+      const double v1 = ui[1] / ui[0], v2 = ui[2] / ui[0];
+      qn[0] = v1;
+      qn[1] = v2;
+      qn[2] = p[kPGv11] * v1 + p[kPGv12] * v2;
+      qn[3] = p[kPGv12] * v1 + p[kPGv22] * v2;
+      qn[4] = p[kPJ] * ui[1];
+      qn[5] = p[kPJ] * ui[2];
+      qn[6] = ui[0];
+      qn[7] = p[kPHs];
+      qn[8] = p[kPJ];
+      qn[9] = p[kPGc11];
+      qn[10] = p[kPGc12];
+      qn[11] = p[kPGc22];
+      qn[12] = 0.5 * P.g * ui[0] * ui[0];
+    }
   }
   __syncthreads();
-  if (P.volume == 0) {
-    for (int t = threadIdx.x; t < ne * nn; t += nthr) {
-      const int el = t / nn, node = t % nn;
-      double* eb = base + el * per;
-      cov_flux(P, eb + node * 3, eb + nn * 3 + node * kPack, 0, eb + nn * (3 + kPack) + node * 3);
-      cov_flux(P, eb + node * 3, eb + nn * 3 + node * kPack, 1,
-               eb + nn * (3 + kPack) + nn * 3 + node * 3);
-    }
-    __syncthreads();
-  }
-  // one thread per node: volume, surface, Jacobian, sources, stage update
-  for (int t = threadIdx.x; t < ne * nn; t += nthr) {
-    const int el = t / nn, node = t % nn;
-    const int i = node % n, j = node / n;
-    double* eb = base + el * per;
-    const double* ui = eb + node * 3;
-    const double* pi = eb + nn * 3 + node * kPack;
+  double un[3] = {0.0, 0.0, 0.0};
+  if (act) {
+    const double* eq = q + el * nn * kCovQ;
     double acc[3] = {0.0, 0.0, 0.0};
     if (P.volume == 0) {
-      const double* F1 = eb + nn * (3 + kPack);
-      const double* F2 = F1 + nn * 3;
 #pragma unroll
       for (int b = 0; b < n; ++b) {
         const double d1 = sb->Dh[i * n + b], d2 = sb->Dh[j * n + b];
+        const double* F1 = eq + (j * n + b) * kCovQ;
+        const double* F2 = eq + (b * n + i) * kCovQ + 3;
 #pragma unroll
-        for (int v = 0; v < 3; ++v) {
-          acc[v] = fma(d1, F1[(j * n + b) * 3 + v], acc[v]);
-          acc[v] = fma(d2, F2[(b * n + i) * 3 + v], acc[v]);
-        }
+        for (int v = 0; v < 3; ++v) acc[v] = fma(d2, F2[v], fma(d1, F1[v], acc[v]));
       }
     } else {
+      const double* qa = qn;
+      const double h_a = ui[0], hs_a = qa[7], J_a = qa[8];
       double nc1 = 0.0, nc2 = 0.0;
 #pragma unroll
       for (int d = 0; d < 2; ++d) {
+        const double hvo_a = d ? ui[2] : ui[1];
+        const double Jhvo_a = d ? qa[5] : qa[4];
+        const double gco0 = d ? qa[10] : qa[9], gco1 = d ? qa[11] : qa[10];
+        const int a = d ? j : i;
 #pragma unroll
         for (int b = 0; b < n; ++b) {
-          const int nb = d == 0 ? j * n + b : b * n + i;
-          const int a = d == 0 ? i : j;
+          const double* qb = eq + (d ? b * n + i : j * n + b) * kCovQ;
           const double Dab = sb->Ds[a * n + b];
-          const double* ub = eb + nb * 3;
-          const double* pb = eb + nn * 3 + nb * kPack;
           if (b != a) {
-            double f[3];
-            cov_vol_sym(P, ui, pi, ub, pb, d, f);
-#pragma unroll
-            for (int v = 0; v < 3; ++v) acc[v] = fma(Dab, f[v], acc[v]);
+            const double Jhvo_b = d ? qb[5] : qb[4];
+            double f0, f1, f2;
+            if (P.vol_sym == 1) {
+              const double m = 0.5 * (Jhvo_a + Jhvo_b);
+              f0 = m;
+              f1 = 0.5 * (qa[0] + qb[0]) * m;
+              f2 = 0.5 * (qa[1] + qb[1]) * m;
+            } else if (P.split) {
+              f0 = 0.5 * (Jhvo_a + Jhvo_b);
+              f1 = 0.5 * (Jhvo_a * qa[0] + Jhvo_b * qb[0]);
+              f2 = 0.5 * (Jhvo_a * qa[1] + Jhvo_b * qb[1]);
+            } else {
+              const double gb0 = d ? qb[10] : qb[9], gb1 = d ? qb[11] : qb[10];
+              f0 = 0.5 * (Jhvo_a + Jhvo_b);
+              f1 = 0.5 * ((Jhvo_a * qa[0] + J_a * gco0 * qa[12]) + (Jhvo_b * qb[0] + qb[8] * gb0 * qb[12]));
+              f2 = 0.5 * ((Jhvo_a * qa[1] + J_a * gco1 * qa[12]) + (Jhvo_b * qb[1] + qb[8] * gb1 * qb[12]));
+            }
+            acc[0] = fma(Dab, f0, acc[0]);
+            acc[1] = fma(Dab, f1, acc[1]);
+            acc[2] = fma(Dab, f2, acc[2]);
           }
           if (P.vol_nc) {
-            double g2[2];
-            cov_noncons_ec(P, ui, pi, ub, pb, pb[kPHs] - pi[kPHs], d, g2);
-            nc1 = fma(Dab, g2[0], nc1);
-            nc2 = fma(Dab, g2[1], nc2);
+            const double half_m = 0.5 * hvo_a;
+            const double ph = P.g * h_a * (qb[6] + (qb[7] - hs_a));
+            const double g0 = J_a * (half_m * (qa[9] * qb[2] + qa[10] * qb[3] - qb[0]) + gco0 * ph);
+            const double g1 = J_a * (half_m * (qa[10] * qb[2] + qa[11] * qb[3] - qb[1]) + gco1 * ph);
+            nc1 = fma(Dab, g0, nc1);
+            nc2 = fma(Dab, g1, nc2);
           }
         }
       }
@@ -419,9 +448,13 @@ TAG_DEV void cov_element_body(const CovParams& P, const CovGroup& G, int lblk,
       if (j == n - 1) acc[v] += se[(3 * n + i) * 3 + v] * sb->winvN;
     }
     double s[3];
-    cov_source(P, ui, pi, s);
-    const double fac = -1.0 / pi[kPJ];
-    const long gq = q_first + (long)el * nn + node;
+    {
+      double p[kPack];
+#pragma unroll
+      for (int k = 0; k < kPack; ++k) p[k] = __ldg(pg + k);
+      cov_source(P, ui, p, s);
+    }
+    const double fac = -1.0 / __ldg(pg + kPJ);
     const int e = G.e0 + el_first + el;
     double dv[3];
 #pragma unroll
@@ -439,33 +472,27 @@ TAG_DEV void cov_element_body(const CovParams& P, const CovGroup& G, int lblk,
       for (int v = 0; v < 3; ++v) {
         const double kn = st.A * kreg[gq * 3 + v] + dt * dv[v];
         kreg[gq * 3 + v] = kn;
-        u[gq * 3 + v] = ui[v] + st.B * kn;
+        un[v] = ui[v] + st.B * kn;
+        u[gq * 3 + v] = un[v];
       }
     }
   }
   if (MODE == kModeStage && st.max_speed != nullptr) {
     // CFL speeds of the updated state, scaled by n: dt = cfl 2 / (n max_e(l1 + l2))
     __syncthreads();
-    for (int t = threadIdx.x; t < ne * nn; t += nthr) {
-      const int el = t / nn, node = t % nn;
-      double* eb = base + el * per;
-      const long gq = q_first + (long)el * nn + node;
-      const double* pi = eb + nn * 3 + node * kPack;
-      const double h = u[gq * 3];
-      const double l1 = fabs(u[gq * 3 + 1] / h) + sqrt(pi[kPGc11] * h * P.g);
-      const double l2 = fabs(u[gq * 3 + 2] / h) + sqrt(pi[kPGc22] * h * P.g);
-      eb[node * 3] = l1;  // the state slots are free now
-      eb[node * 3 + 1] = l2;
+    if (act) {
+      qn[0] = fabs(un[1] / un[0]) + sqrt(__ldg(pg + kPGc11) * un[0] * P.g);
+      qn[1] = fabs(un[2] / un[0]) + sqrt(__ldg(pg + kPGc22) * un[0] * P.g);
     }
     __syncthreads();
-    for (int el = threadIdx.x; el < ne; el += nthr) {
-      const double* eb = base + el * per;
+    if (threadIdx.x < ne) {
+      const double* eq = q + threadIdx.x * nn * kCovQ;
       double m1 = 0.0, m2 = 0.0;
-      for (int node = 0; node < nn; ++node) {
-        m1 = fmax(m1, eb[node * 3]);
-        m2 = fmax(m2, eb[node * 3 + 1]);
+      for (int k = 0; k < nn; ++k) {
+        m1 = fmax(m1, eq[k * kCovQ]);
+        m2 = fmax(m2, eq[k * kCovQ + 1]);
       }
-      const int e = G.e0 + el_first + el;
+      const int e = G.e0 + el_first + threadIdx.x;
       atomic_max_nonneg(st.max_speed + (st.member ? st.member[e] : 0), n * (m1 + m2));
     }
   }
