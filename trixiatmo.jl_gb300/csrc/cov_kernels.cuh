@@ -25,7 +25,7 @@ namespace tag {
 // packed per-node element data
 enum CovPack : int {
   kPJ = 0, kPGc11, kPGc12, kPGc22, kPGv11, kPGv12, kPGv22, kPHs,
-  kPC111, kPC112, kPC122, kPC211, kPC212, kPC222, kPF, kPPad, kPack = 16
+  kPC111, kPC112, kPC122, kPC211, kPC212, kPC222, kPF, kPInvJ, kPack = 16
 };
 
 struct CovParams {
@@ -65,7 +65,7 @@ TAG_DEV int cov_find_group(const CovGroups& G, int blk, bool iface) {
   return lo;
 }
 
-// packs aux (26) and the Coriolis parameter f = 2 Omega z / |x| per node
+// packs aux (26), the Coriolis parameter f = 2 Omega z / |x| and 1/J per node
 __global__ void k_cov_pack(const double* __restrict__ aux, const double* __restrict__ xyz,
                            long nodes, double omega, double* __restrict__ pk) {
   const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -80,7 +80,7 @@ __global__ void k_cov_pack(const double* __restrict__ aux, const double* __restr
   for (int k = 0; k < 6; ++k) p[kPC111 + k] = a[20 + k];
   const double* x = xyz + q * 3;
   p[kPF] = 2.0 * omega * x[2] / sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
-  p[kPPad] = 0.0;
+  p[kPInvJ] = 1.0 / a[12];
 }
 
 // ---- pointwise physics on packed data -----------------------------------------
@@ -88,59 +88,28 @@ TAG_DEV double cov_gcon(const double* p, int i, int j) {
   return (i == 0 && j == 0) ? p[kPGc11] : (i == 1 && j == 1) ? p[kPGc22] : p[kPGc12];
 }
 
-// contravariant flux component o of one node (standard or split form)
-TAG_DEV void cov_flux(const CovParams& P, const double* u, const double* p, int o, double* f) {
+// contravariant flux component o of one node (standard or split form); ih = 1/h
+TAG_DEV void cov_flux(const CovParams& P, const double* u, double ih, const double* p, int o,
+                      double* f) {
   const double J = p[kPJ];
   const double m = J * u[1 + o];
   if (P.split) {
-    const double ih = 1.0 / u[0];
     f[0] = m;
     f[1] = m * (u[1] * ih);
     f[2] = m * (u[2] * ih);
     return;
   }
-  const double vo = u[1 + o] / u[0];
+  const double vo = u[1 + o] * ih;
   const double gt = 0.5 * P.g * u[0] * u[0];
   f[0] = m;
   f[1] = J * (u[1] * vo + cov_gcon(p, 0, o) * gt);
   f[2] = J * (u[2] * vo + cov_gcon(p, 1, o) * gt);
 }
 
-// symmetric two-point volume flux of nodes a and b along o
-TAG_DEV void cov_vol_sym(const CovParams& P, const double* ua, const double* pa, const double* ub,
-                         const double* pb, int o, double* f) {
-  if (P.vol_sym == 1) {
-    const double m = 0.5 * (pa[kPJ] * ua[1 + o] + pb[kPJ] * ub[1 + o]);
-    f[0] = m;
-    f[1] = 0.5 * (ua[1] / ua[0] + ub[1] / ub[0]) * m;
-    f[2] = 0.5 * (ua[2] / ua[0] + ub[2] / ub[0]) * m;
-    return;
-  }
-  double fa[3], fb[3];
-  cov_flux(P, ua, pa, o, fa);
-  cov_flux(P, ub, pb, o, fb);
-#pragma unroll
-  for (int v = 0; v < 3; ++v) f[v] = 0.5 * (fa[v] + fb[v]);
-}
-
-// flux_nonconservative_ec of (a, b) along o: momentum components only
-TAG_DEV void cov_noncons_ec(const CovParams& P, const double* ua, const double* pa, const double* ub,
-                            const double* pb, double hs_jump, int o, double* g2) {
-  const double vb0 = ub[1] / ub[0], vb1 = ub[2] / ub[0];
-  const double vc0 = pb[kPGv11] * vb0 + pb[kPGv12] * vb1;
-  const double vc1 = pb[kPGv12] * vb0 + pb[kPGv22] * vb1;
-  const double half_m = 0.5 * ua[1 + o];
-  const double ph = P.g * ua[0] * (ub[0] + hs_jump);
-  const double geo0 = half_m * (pa[kPGc11] * vc0 + pa[kPGc12] * vc1 - vb0);
-  const double geo1 = half_m * (pa[kPGc12] * vc0 + pa[kPGc22] * vc1 - vb1);
-  g2[0] = pa[kPJ] * (geo0 + cov_gcon(pa, 0, o) * ph);
-  g2[1] = pa[kPJ] * (geo1 + cov_gcon(pa, 1, o) * ph);
-}
-
 // source_terms_geometric_coriolis (standard or split), after apply_jacobian
-TAG_DEV void cov_source(const CovParams& P, const double* u, const double* p, double* s) {
+TAG_DEV void cov_source(const CovParams& P, const double* u, double ih, const double* p,
+                        double* s) {
   const double hv0 = u[1], hv1 = u[2];
-  const double ih = 1.0 / u[0];
   const double v0 = hv0 * ih, v1 = hv1 * ih;
   const double T00 = hv0 * v0, T01 = hv0 * v1, T10 = hv1 * v0, T11 = hv1 * v1;
   double sg0, sg1;
@@ -201,30 +170,31 @@ TAG_DEV void cov_transform(const double* u, const CovSide& from, const CovSide& 
 TAG_DEV void cov_surface(const CovParams& P, const double* a, const double* c, const CovSide& w,
                          int o, double* F) {
   const double J = w.J;
+  const double iha = 1.0 / a[0], ihc = 1.0 / c[0];
   const double gco0 = o ? w.gc12 : w.gc11;  // G^{1o}
   const double gco1 = o ? w.gc22 : w.gc12;  // G^{2o}
   const double ao = o ? a[2] : a[1], co = o ? c[2] : c[1];
+  const double va1 = a[1] * iha, va2 = a[2] * iha, vc1 = c[1] * ihc, vc2 = c[2] * ihc;
+  const double vao = o ? va2 : va1, vco = o ? vc2 : vc1;
   if (P.surf_sym == 1) {
     const double m = 0.5 * (J * ao + J * co);
     F[0] = m;
-    F[1] = 0.5 * (a[1] / a[0] + c[1] / c[0]) * m;
-    F[2] = 0.5 * (a[2] / a[0] + c[2] / c[0]) * m;
+    F[1] = 0.5 * (va1 + vc1) * m;
+    F[2] = 0.5 * (va2 + vc2) * m;
   } else if (P.split) {
     const double ma = J * ao, mc = J * co;
     F[0] = 0.5 * (ma + mc);
-    F[1] = 0.5 * (ma * (a[1] / a[0]) + mc * (c[1] / c[0]));
-    F[2] = 0.5 * (ma * (a[2] / a[0]) + mc * (c[2] / c[0]));
+    F[1] = 0.5 * (ma * va1 + mc * vc1);
+    F[2] = 0.5 * (ma * va2 + mc * vc2);
   } else {
-    const double va = ao / a[0], vc = co / c[0];
     const double ga = 0.5 * P.g * a[0] * a[0], gc = 0.5 * P.g * c[0] * c[0];
     F[0] = 0.5 * (J * ao + J * co);
-    F[1] = 0.5 * (J * (a[1] * va + gco0 * ga) + J * (c[1] * vc + gco0 * gc));
-    F[2] = 0.5 * (J * (a[2] * va + gco1 * ga) + J * (c[2] * vc + gco1 * gc));
+    F[1] = 0.5 * (J * (a[1] * vao + gco0 * ga) + J * (c[1] * vco + gco0 * gc));
+    F[2] = 0.5 * (J * (a[2] * vao + gco1 * ga) + J * (c[2] * vco + gco1 * gc));
   }
   if (P.surf_diss) {
     const double goo = o ? w.gc22 : w.gc11;
-    const double lam = fmax(fabs(ao / a[0]) + sqrt(goo * a[0] * P.g),
-                            fabs(co / c[0]) + sqrt(goo * c[0] * P.g));
+    const double lam = fmax(fabs(vao) + sqrt(goo * a[0] * P.g), fabs(vco) + sqrt(goo * c[0] * P.g));
     const double s = -0.5 * J * lam;
     F[0] += s * (c[0] - a[0]);
     F[1] += s * (c[1] - a[1]);
@@ -232,13 +202,12 @@ TAG_DEV void cov_surface(const CovParams& P, const double* a, const double* c, c
   }
   if (P.surf_nc == 1) {
     // flux_nonconservative_ec with both geometries `w` (no topography jump)
-    const double vb0 = c[1] / c[0], vb1 = c[2] / c[0];
-    const double vc0 = w.gv11 * vb0 + w.gv12 * vb1;
-    const double vc1 = w.gv12 * vb0 + w.gv22 * vb1;
+    const double vcv0 = w.gv11 * vc1 + w.gv12 * vc2;
+    const double vcv1 = w.gv12 * vc1 + w.gv22 * vc2;
     const double half_m = 0.5 * ao;
     const double ph = P.g * a[0] * c[0];
-    F[1] += 0.5 * (J * (half_m * (w.gc11 * vc0 + w.gc12 * vc1 - vb0) + gco0 * ph));
-    F[2] += 0.5 * (J * (half_m * (w.gc12 * vc0 + w.gc22 * vc1 - vb1) + gco1 * ph));
+    F[1] += 0.5 * (J * (half_m * (w.gc11 * vcv0 + w.gc12 * vcv1 - vc1) + gco0 * ph));
+    F[2] += 0.5 * (J * (half_m * (w.gc12 * vcv0 + w.gc22 * vcv1 - vc2) + gco1 * ph));
   } else if (P.surf_nc == 2) {
     const double ph = P.g * a[0] * c[0];
     F[1] += 0.5 * (J * (gco0 * ph));
@@ -356,11 +325,12 @@ TAG_DEV void cov_element_body(const CovParams& P, const CovGroup& G, int lblk,
     double p[kPack];
 #pragma unroll
     for (int k = 0; k < kPack; ++k) p[k] = __ldg(pg + k);
+    const double ih = 1.0 / ui[0];
     if (P.volume == 0) {
-      cov_flux(P, ui, p, 0, qn);
-      cov_flux(P, ui, p, 1, qn + 3);
+      cov_flux(P, ui, ih, p, 0, qn);
+      cov_flux(P, ui, ih, p, 1, qn + 3);
     } else {
-      const double v1 = ui[1] / ui[0], v2 = ui[2] / ui[0];
+      const double v1 = ui[1] * ih, v2 = ui[2] * ih;
       qn[0] = v1;
       qn[1] = v2;
       qn[2] = p[kPGv11] * v1 + p[kPGv12] * v2;
@@ -452,9 +422,9 @@ TAG_DEV void cov_element_body(const CovParams& P, const CovGroup& G, int lblk,
       double p[kPack];
 #pragma unroll
       for (int k = 0; k < kPack; ++k) p[k] = __ldg(pg + k);
-      cov_source(P, ui, p, s);
+      cov_source(P, ui, 1.0 / ui[0], p, s);
     }
-    const double fac = -1.0 / __ldg(pg + kPJ);
+    const double fac = -__ldg(pg + kPInvJ);
     const int e = G.e0 + el_first + el;
     double dv[3];
 #pragma unroll
@@ -481,8 +451,9 @@ TAG_DEV void cov_element_body(const CovParams& P, const CovGroup& G, int lblk,
     // CFL speeds of the updated state, scaled by n: dt = cfl 2 / (n max_e(l1 + l2))
     __syncthreads();
     if (act) {
-      qn[0] = fabs(un[1] / un[0]) + sqrt(__ldg(pg + kPGc11) * un[0] * P.g);
-      qn[1] = fabs(un[2] / un[0]) + sqrt(__ldg(pg + kPGc22) * un[0] * P.g);
+      const double ihn = 1.0 / un[0];
+      qn[0] = fabs(un[1] * ihn) + sqrt(__ldg(pg + kPGc11) * un[0] * P.g);
+      qn[1] = fabs(un[2] * ihn) + sqrt(__ldg(pg + kPGc22) * un[0] * P.g);
     }
     __syncthreads();
     if (threadIdx.x < ne) {
