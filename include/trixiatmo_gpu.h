@@ -58,6 +58,7 @@ extern "C" {
 #define TAG_EQ_RAINY_2D 3        /* CompressibleRainyEulerEquations2D (+ Newton stage limiter) */
 #define TAG_EQ_MOIST_EULER_2D 4  /* CompressibleMoistEulerEquations2D                             */
 #define TAG_EQ_COVARIANT_SWE 5   /* (Split)CovariantShallowWaterEquations2D on a 2D manifold     */
+#define TAG_EQ_POTENTIAL_TEMPERATURE_2D 6 /* CompressibleEulerPotentialTemperatureEquationsWithGravity2D */
 
 #define TAG_VF_RANOCHA_WARUSZEWSKI 1 /* (flux_ranocha, flux_nonconservative_waruszewski_etal) */
 #define TAG_VF_EC_RAIN 2             /* VolumeIntegralFluxDifferencing(flux_ec_rain)    */
@@ -65,6 +66,9 @@ extern "C" {
 #define TAG_VF_CHANDRASHEKAR 4       /* VolumeIntegralFluxDifferencing(flux_chandrashekar), moist */
 #define TAG_VF_COV_CENTRAL 5         /* covariant: flux differencing with flux_central  */
 #define TAG_VF_COV_EC 6              /* covariant: flux differencing with flux_ec (split form) */
+#define TAG_VF_PT_TEC 7              /* potential temperature: (flux_tec, nonconservative gravity term) */
+#define TAG_VF_PT_EC 8               /* potential temperature: (flux_ec, nonconservative gravity term)  */
+#define TAG_VF_PT_ETEC 9             /* potential temperature: (flux_etec, nonconservative gravity term) */
 #define TAG_SF_LMARS 1               /* (FluxLMARS(c), flux_zero)                       */
 #define TAG_SF_LAX_FRIEDRICHS 2      /* flux_lax_friedrichs (max_abs_speed_naive)       */
 #define TAG_SF_CHANDRASHEKAR 3       /* flux_chandrashekar as surface flux (moist)      */
@@ -118,6 +122,10 @@ typedef struct {
                         RAINY_2D: params[0] = TAG_SRC_* source kind;
                         MOIST_EULER_2D: c_pd, c_vd, c_pv, c_vv, gravity, LMARS
                         speed of sound, TAG_SRC_* source kind (0: none);
+                        POTENTIAL_TEMPERATURE_2D: c_p, c_v, gravity, LMARS speed
+                        of sound, nonconservative gravity term (0
+                        flux_nonconservative_waruszewski_etal, 1 _artiano_etal,
+                        2 _souza_etal);
                         COVARIANT_SWE: gravity, rotation rate, split form (0/1),
                         volume nonconservative flux (0 none, 1
                         flux_nonconservative_ec), surface nonconservative flux

@@ -82,6 +82,23 @@ def lib():
         L.orc_cov_ck_steps.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double,
                                        ctypes.c_double, ctypes.c_int, ctypes.c_double,
                                        ctypes.c_double]
+        L.orc_pt_create.restype = ctypes.c_void_p
+        L.orc_pt_create.argtypes = ([ctypes.c_int] * 3 + [ctypes.c_double] * 4 + [ctypes.c_int] * 5 +
+                                    [ctypes.c_double] * 4)
+        L.orc_pt_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_pt_initial_condition_gravity_waves.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_pt_errors_gravity_waves.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+        L.orc_pt_rhs.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double]
+        L.orc_pt_max_dt.restype = ctypes.c_double
+        L.orc_pt_max_dt.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_pt_ssprk43_run.restype = ctypes.c_int
+        L.orc_pt_ssprk43_run.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_double]
+        L.orc_pt_ck_steps.restype = ctypes.c_double
+        L.orc_pt_ck_steps.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_int]
+        L.orc_pt_stolarsky.restype = ctypes.c_double
+        L.orc_pt_stolarsky.argtypes = [ctypes.c_double] * 3
         L.orc_moist_create.restype = ctypes.c_void_p
         L.orc_moist_create.argtypes = ([ctypes.c_int] * 3 + [ctypes.c_double] * 4 +
                                        [ctypes.c_int] * 6 + [ctypes.c_double] * 2 + [ctypes.c_int])
@@ -275,6 +292,55 @@ class CovSWE:
         if getattr(self, "h", None):
             lib().orc_cov_destroy(self.h)
             self.h = None
+
+
+class PotTemp2D:
+    """Potential-temperature Euler with gravity on a StructuredMesh rectangle.
+    volume 0 flux_tec, 1 flux_ec, 2 flux_etec; nc 0 waruszewski, 1 artiano,
+    2 souza; wall_kind 1 StructuredMesh slip wall, 2 outward normal."""
+
+    nv = 5
+
+    def __init__(self, polydeg, nx, ny, x0, x1, y0, y1, periodic_x=True, periodic_y=False,
+                 volume=0, nc=0, wall_kind=1, c_p=1004.0, c_v=717.0, g=9.80616, c_lmars=340.0):
+        self.n = polydeg + 1
+        self.nelem = nx * ny
+        self.h = lib().orc_pt_create(polydeg, nx, ny, x0, x1, y0, y1, int(periodic_x),
+                                     int(periodic_y), volume, nc, wall_kind, c_p, c_v, g, c_lmars)
+
+    def initial_condition_gravity_waves(self):
+        u = np.zeros((self.nelem, self.n, self.n, 5))
+        lib().orc_pt_initial_condition_gravity_waves(self.h, _p(u))
+        return u
+
+    def errors_gravity_waves(self, u):
+        l2, linf = np.zeros(5), np.zeros(5)
+        lib().orc_pt_errors_gravity_waves(self.h, _p(np.ascontiguousarray(u)), _p(l2), _p(linf))
+        return l2, linf
+
+    def rhs(self, u, t=0.0):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        du = np.zeros_like(u)
+        lib().orc_pt_rhs(self.h, _p(u), _p(du), t)
+        return du
+
+    def max_dt(self, u):
+        return lib().orc_pt_max_dt(self.h, _p(np.ascontiguousarray(u)))
+
+    def ssprk43_run(self, u, t0, t_end, cfl):
+        return lib().orc_pt_ssprk43_run(self.h, _p(u), t0, t_end, cfl)
+
+    def ck_steps(self, u, k, t, cfl, nsteps):
+        return lib().orc_pt_ck_steps(self.h, _p(u), _p(k), t, cfl, nsteps)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_pt_destroy(self.h)
+            self.h = None
+
+
+def stolarsky(x, y, gamma):
+    return lib().orc_pt_stolarsky(x, y, gamma)
 
 
 class Moist2D:

@@ -19,6 +19,7 @@
 #include "orc_euler_energy_2d.hpp"
 #include "orc_euler_energy_3d.hpp"
 #include "orc_moist_2d.hpp"
+#include "orc_pt_2d.hpp"
 #include "orc_cov_swe.hpp"
 #include "orc_rainy_2d.hpp"
 #include "orc_time.hpp"
@@ -438,7 +439,63 @@ void errors_2d(const Basis& b, const Mesh2D& mesh, const double* u, Exact&& exac
   for (int v = 0; v < NVAR; ++v) l2[v] = std::sqrt(l2[v] / vol);
 }
 
+// CompressibleEulerPotentialTemperatureEquationsWithGravity2D on a
+// StructuredMesh: volume (flux_tec | flux_ec | flux_etec, nonconservative
+// gravity term), surface (FluxLMARS(c), flux_zero).
+struct PTPhys {
+  using State = PotTemp2D::State;
+  static constexpr int nv = 5;
+  static constexpr bool has_noncons = true;
+  static constexpr bool has_sources = false;
+  PotTemp2D eq;
+  double c_lmars = 340.0;
+  State volume_flux(const State& a, const State& b, const double* n) const {
+    return eq.volume_flux(a, b, n);
+  }
+  State volume_noncons(const State& a, const State& b, const double* n) const {
+    return eq.noncons(a, b, n);
+  }
+  State surface_flux(const State& a, const State& b, const double* n) const {
+    return eq.flux_lmars(a, b, n, c_lmars);
+  }
+  State surface_noncons(const State&, const State&, const double*) const { return State{}; }
+  State bc_structured(const State& ui, const double* n, int direction) const {
+    return eq.slip_wall_structured(ui, n, direction, c_lmars);
+  }
+  State bc_normal(const State& ui, const double* n) const {
+    return eq.slip_wall_normal(ui, n, c_lmars);
+  }
+  State flux(const State& u, const double* n) const { return eq.flux(u, n); }
+  State source(const State&, const double*, double) const { return State{}; }
+  void max_abs_speeds(const State& u, double& l1, double& l2) const { eq.max_abs_speeds(u, l1, l2); }
+};
+
+struct PTCase {
+  PTPhys phys;
+  Basis basis;
+  Mesh2D mesh;
+  std::unique_ptr<DG2D<PTPhys>> dg;
+  size_t ndofs() const { return (size_t)mesh.nelem * basis.n * basis.n; }
+};
+
+// initial_condition_gravity_waves (src/equations/initial_condition_compressible_euler_2d.jl:11-35)
+// for the potential-temperature equations (their prim2cons)
+inline PotTemp2D::State ic_gravity_waves_pt(const PotTemp2D& eq, const double* x) {
+  const double g = eq.g, R = eq.R, T0 = 250.0;
+  const double x_c = 100000.0, a = 5000.0, H = 10000.0;
+  const double delta = g / (R * T0);
+  const double pi = 3.14159265358979323846;
+  const double Tb = 0.001 * std::sin(pi * x[1] / H) * std::exp(-(x[0] - x_c) * (x[0] - x_c) / (a * a));
+  const double ps = 100000.0;
+  const double rhos = ps / (T0 * R);
+  const double rho_b = rhos * (-Tb / T0);
+  const double p = ps * std::exp(-delta * x[1]);
+  const double rho = rhos * std::exp(-delta * x[1]) + rho_b * std::exp(-0.5 * delta * x[1]);
+  return eq.prim2cons(rho, 20.0, 0.0, p, g * x[1]);
+}
+
 }  // namespace orc
+
 
 
 using namespace orc;
@@ -977,6 +1034,84 @@ double orc_cov_ck_steps(void* h, double* u, double* k, double t, double cfl, int
     t += dt;
   }
   return t;
+}
+
+// ---- 2D potential temperature with gravity --------------------------------
+// volume: 0 flux_tec, 1 flux_ec, 2 flux_etec; nc: 0 waruszewski, 1 artiano,
+// 2 souza; wall_kind: 1 StructuredMesh, 2 outward normal.
+void* orc_pt_create(int polydeg, int nx, int ny, double x0, double x1, double y0, double y1,
+                    int periodic_x, int periodic_y, int volume, int nc, int wall_kind,
+                    double c_p, double c_v, double g, double c_lmars) {
+  auto* c = new PTCase();
+  c->phys.eq.init(c_p, c_v, g);
+  c->phys.eq.volume = volume;
+  c->phys.eq.nc_kind = nc;
+  c->phys.c_lmars = c_lmars;
+  c->basis = make_lgl_basis(polydeg);
+  c->mesh = structured_rectangle(c->basis, nx, ny, x0, x1, y0, y1, periodic_x != 0,
+                                 periodic_y != 0, wall_kind);
+  c->dg.reset(new DG2D<PTPhys>(c->phys, c->basis, c->mesh));
+  return c;
+}
+
+void orc_pt_destroy(void* h) { delete static_cast<PTCase*>(h); }
+
+void orc_pt_initial_condition_gravity_waves(void* h, double* u) {
+  auto* c = static_cast<PTCase*>(h);
+  for (size_t q = 0; q < c->ndofs(); ++q) {
+    const auto s = ic_gravity_waves_pt(c->phys.eq, &c->mesh.xy[q * 2]);
+    for (int v = 0; v < 5; ++v) u[q * 5 + v] = s[v];
+  }
+}
+
+void orc_pt_errors_gravity_waves(void* h, const double* u, double* l2, double* linf) {
+  auto* c = static_cast<PTCase*>(h);
+  errors_2d<5>(c->basis, c->mesh, u,
+               [&](const double* x) { return ic_gravity_waves_pt(c->phys.eq, x); }, l2, linf);
+}
+
+void orc_pt_rhs(void* h, const double* u, double* du, double t) {
+  static_cast<PTCase*>(h)->dg->rhs(u, du, t);
+}
+
+double orc_pt_max_dt(void* h, const double* u) { return static_cast<PTCase*>(h)->dg->max_dt(u); }
+
+// SSPRK43 at a fixed CFL (adaptive = false), the last step shortened to t_end
+int orc_pt_ssprk43_run(void* h, double* u, double t0, double t_end, double cfl) {
+  auto* c = static_cast<PTCase*>(h);
+  const size_t N = c->ndofs() * 5;
+  std::vector<double> tmp(N), du(N), u0(N);
+  double t = t0;
+  int steps = 0;
+  while (t < t_end) {
+    double dt = cfl * c->dg->max_dt(u);
+    if (t + dt > t_end) dt = t_end - t;
+    ssprk43_step([&](const double* uu, double* dd, double tt) { c->dg->rhs(uu, dd, tt); }, u,
+                 tmp.data(), du.data(), u0.data(), N, t, dt);
+    t += dt;
+    ++steps;
+  }
+  return steps;
+}
+
+double orc_pt_ck_steps(void* h, double* u, double* k, double t, double cfl, int nsteps) {
+  auto* c = static_cast<PTCase*>(h);
+  const size_t N = c->ndofs() * 5;
+  std::vector<double> du(N);
+  for (int s = 0; s < nsteps; ++s) {
+    const double dt = cfl * c->dg->max_dt(u);
+    ck2n54_step([&](const double* uu, double* dd, double tt) { c->dg->rhs(uu, dd, tt); }, u, k,
+                du.data(), N, t, dt);
+    t += dt;
+  }
+  return t;
+}
+
+double orc_pt_stolarsky(double x, double y, double gamma) {
+  PotTemp2D eq;
+  eq.gamma = gamma;
+  stolarsky_coefficients(gamma, eq.sc);
+  return eq.stolarsky(x, y);
 }
 
 }  // extern "C"

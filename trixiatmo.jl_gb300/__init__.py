@@ -19,7 +19,10 @@ from .equations import (CompressibleEulerEnergyEquationsWithGravity2D,
                         flux_ranocha, flux_zero, speed_of_sound_isothermal,
                         CompressibleMoistEulerEquations2D, flux_chandrashekar,
                         source_terms_geopotential, source_terms_moist_bubble,
-                        source_terms_convergence_test_dry, source_terms_convergence_test_moist)
+                        source_terms_convergence_test_dry, source_terms_convergence_test_moist,
+                        CompressibleEulerPotentialTemperatureEquationsWithGravity2D, flux_ec,
+                        flux_tec, flux_etec, flux_nonconservative_artiano_etal,
+                        flux_nonconservative_souza_etal)
 from .initial_conditions import (EARTH_GRAVITATIONAL_ACCELERATION, EARTH_RADIUS,
                                  EARTH_ROTATION_RATE, IsothermalShell, MoistBubbleRainy,
                                  WarmBubble, initial_condition_convergence_test_rainy,
@@ -53,4 +56,6 @@ __all__ = [
     "initial_condition_convergence_test_dry", "initial_condition_convergence_test_moist",
     "P4estMesh", "covariant", "SemidiscretizationCovariant",
     "SemidiscretizationCovariantEnsemble",
+    "CompressibleEulerPotentialTemperatureEquationsWithGravity2D", "flux_ec", "flux_tec",
+    "flux_etec", "flux_nonconservative_artiano_etal", "flux_nonconservative_souza_etal",
 ]

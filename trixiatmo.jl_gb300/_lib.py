@@ -39,6 +39,10 @@ TAG_SRC_MOIST_BUBBLE = 4
 TAG_SRC_MOIST_CONVERGENCE_DRY = 5
 TAG_SRC_MOIST_CONVERGENCE = 6
 TAG_EQ_COVARIANT_SWE = 5
+TAG_EQ_POTENTIAL_TEMPERATURE_2D = 6
+TAG_VF_PT_TEC = 7
+TAG_VF_PT_EC = 8
+TAG_VF_PT_ETEC = 9
 TAG_VF_COV_CENTRAL = 5
 TAG_VF_COV_EC = 6
 TAG_SF_COV_EC = 4

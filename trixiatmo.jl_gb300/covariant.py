@@ -88,7 +88,7 @@ class _NamedFlux:
 
 
 flux_central = _NamedFlux("flux_central")
-flux_ec = _NamedFlux("flux_ec")
+from .equations import flux_ec  # noqa: E402  (one name for both equation families)
 flux_nonconservative_ec = _NamedFlux("flux_nonconservative_ec")
 flux_nonconservative_surface_simplified = _NamedFlux("flux_nonconservative_surface_simplified")
 

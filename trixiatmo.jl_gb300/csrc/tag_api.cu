@@ -16,6 +16,7 @@
 #include "phys_euler_energy_2d.cuh"
 #include "phys_euler_energy_3d.cuh"
 #include "phys_moist_2d.cuh"
+#include "phys_pt_2d.cuh"
 #include "phys_rainy_2d.cuh"
 
 using namespace tag;
@@ -60,6 +61,7 @@ struct tag_handle_s {
   PhysEnergy3D::Params p_energy3d{};
   PhysRainy2D::Params p_rainy{};
   PhysMoist2D::Params p_moist{};
+  PhysPT2D::Params p_pt{};
   // rainy: Newton stage limiter settings, MLP parameters, statistics counters
   bool has_limiter = false;
   NewtonArgs newton{0, 20, 0, 0, 8, 1e-9, nullptr, nullptr, nullptr};
@@ -126,6 +128,10 @@ const PhysRainy2D::Params& params_of<PhysRainy2D>(tag_handle h) {
 template <>
 const PhysMoist2D::Params& params_of<PhysMoist2D>(tag_handle h) {
   return h->p_moist;
+}
+template <>
+const PhysPT2D::Params& params_of<PhysPT2D>(tag_handle h) {
+  return h->p_pt;
 }
 
 template <class Phys, int n, int VOL = kVolFluxDiff>
@@ -719,6 +725,14 @@ const char* check_equations(const tag_config* cfg) {
         return "FluxLMARS needs a positive speed of sound";
       return nullptr;
     }
+    case TAG_EQ_POTENTIAL_TEMPERATURE_2D: {
+      if ((vf != TAG_VF_PT_TEC && vf != TAG_VF_PT_EC && vf != TAG_VF_PT_ETEC) || sf != TAG_SF_LMARS)
+        return "unsupported flux combination for the potential-temperature equations";
+      const double k = cfg->params[4];
+      if (k != 0 && k != 1 && k != 2) return "unsupported nonconservative gravity term";
+      if (!(cfg->params[3] > 0.0)) return "FluxLMARS needs a positive speed of sound";
+      return nullptr;
+    }
     default:
       return "unsupported equations id";
   }
@@ -728,6 +742,7 @@ bool boundary_kind_ok(int eq, int kind) {
   switch (eq) {
     case TAG_EQ_EULER_ENERGY_2D:
     case TAG_EQ_MOIST_EULER_2D:
+    case TAG_EQ_POTENTIAL_TEMPERATURE_2D:
       return kind == TAG_BC_SLIP_WALL_STRUCTURED || kind == TAG_BC_SLIP_WALL_NORMAL;
     case TAG_EQ_EULER_ENERGY_3D: return kind == TAG_BC_SLIP_WALL_NORMAL;
     case TAG_EQ_RAINY_2D: return kind == TAG_BC_SIMPLE_SLIP_WALL;
@@ -809,6 +824,14 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
     h->ops = cfg->volume_flux == TAG_VF_WEAK_FORM ? ops_for_n<PhysRainy2D, kVolWeak>(n)
                                                   : ops_for_n<PhysRainy2D, kVolFluxDiff>(n);
     h->has_limiter = true;
+  } else if (cfg->equations == TAG_EQ_POTENTIAL_TEMPERATURE_2D) {
+    h->nv = PhysPT2D::NV;
+    h->na = PhysPT2D::NA;
+    double pp[8];
+    for (int k = 0; k < 8; ++k) pp[k] = cfg->params[k];
+    pp[5] = cfg->volume_flux == TAG_VF_PT_TEC ? 0 : cfg->volume_flux == TAG_VF_PT_EC ? 1 : 2;
+    h->p_pt = PhysPT2D::make_params(pp);
+    h->ops = ops_for_n<PhysPT2D, kVolFluxDiff>(n);
   } else if (moist) {
     h->nv = PhysMoist2D::NV;
     h->na = PhysMoist2D::NA;

@@ -47,6 +47,35 @@ class CompressibleEulerEnergyEquationsWithGravity2D:
         return rho, v1, v2, p, u[..., 4]
 
 
+class CompressibleEulerPotentialTemperatureEquationsWithGravity2D:
+    """State (rho, rho_v1, rho_v2, rho_theta, phi), p = K rho_theta^gamma
+    (src/equations/compressible_euler_potential_temperature_gravity_2d.jl:5-33)."""
+
+    nvariables = 5
+    ndims = 2
+    eq_id = _lib.TAG_EQ_POTENTIAL_TEMPERATURE_2D
+
+    def __init__(self, *, c_p, c_v, gravity):
+        self.c_p = float(c_p)
+        self.c_v = float(c_v)
+        self.g = float(gravity)
+        self.p_0 = 100000.0
+        self.R = self.c_p - self.c_v
+        self.gamma = self.c_p / self.c_v
+        self.inv_gamma_minus_one = 1.0 / (self.gamma - 1.0)
+        self.K = self.p_0 * (self.R / self.p_0) ** self.gamma
+
+    def prim2cons(self, rho, v1, v2, p, phi):
+        one = np.ones_like(p)
+        rho_theta = (p / self.p_0) ** (1 / self.gamma) * self.p_0 / self.R
+        return np.stack([rho * one, rho * v1 * one, rho * v2 * one, rho_theta * one, phi * one],
+                        axis=-1)
+
+    def cons2prim(self, u):
+        rho = u[..., 0]
+        return rho, u[..., 1] / rho, u[..., 2] / rho, self.K * u[..., 3] ** self.gamma, u[..., 4]
+
+
 class CompressibleEulerEnergyEquationsWithGravity3D:
     """State (rho, rho_v1, rho_v2, rho_v3, rho_e, phi)
     (src/equations/compressible_euler_energy_with_gravity_3d.jl:45-65)."""
@@ -145,6 +174,14 @@ flux_zero = _NamedFlux("flux_zero")
 flux_ec_rain = _NamedFlux("flux_ec_rain")
 flux_lax_friedrichs = _NamedFlux("flux_lax_friedrichs")
 flux_chandrashekar = _NamedFlux("flux_chandrashekar")
+# entropy / total-energy conservative fluxes; flux_ec is shared with the
+# covariant shallow-water equations (the reference dispatches one name on the
+# equation type)
+flux_ec = _NamedFlux("flux_ec")
+flux_tec = _NamedFlux("flux_tec")
+flux_etec = _NamedFlux("flux_etec")
+flux_nonconservative_artiano_etal = _NamedFlux("flux_nonconservative_artiano_etal")
+flux_nonconservative_souza_etal = _NamedFlux("flux_nonconservative_souza_etal")
 
 
 class FluxLMARS:

@@ -25,7 +25,10 @@ import numpy as np
 
 from . import _lib
 from .basis import LobattoLegendreBasis
-from .equations import (CompressibleEulerEnergyEquationsWithGravity2D,
+from .equations import (CompressibleEulerPotentialTemperatureEquationsWithGravity2D,
+                        flux_etec, flux_nonconservative_artiano_etal,
+                        flux_nonconservative_souza_etal, flux_tec,
+                        CompressibleEulerEnergyEquationsWithGravity2D,
                         CompressibleEulerEnergyEquationsWithGravity3D,
                         CompressibleMoistEulerEquations2D, CompressibleRainyEulerEquations2D,
                         FluxLMARS, VolumeIntegralWeakForm, _Source,
@@ -108,6 +111,24 @@ def _flux_ids(equations, solver, source_terms=None):
             raise ValueError(f"{source_terms} is not a source of the moist equations")
         eq = equations
         return vid, sid, [eq.c_pd, eq.c_vd, eq.c_pv, eq.c_vv, eq.g, c_lmars, float(src)]
+    if isinstance(equations, CompressibleEulerPotentialTemperatureEquationsWithGravity2D):
+        from .equations import flux_ec
+        if not isinstance(vf, tuple):
+            raise ValueError("volume flux must be (flux_tec | flux_ec | flux_etec, a "
+                             "nonconservative gravity term)")
+        vid = {id(flux_tec): _lib.TAG_VF_PT_TEC, id(flux_ec): _lib.TAG_VF_PT_EC,
+               id(flux_etec): _lib.TAG_VF_PT_ETEC}.get(id(vf[0]))
+        nc = {id(flux_nonconservative_waruszewski_etal): 0,
+              id(flux_nonconservative_artiano_etal): 1,
+              id(flux_nonconservative_souza_etal): 2}.get(id(vf[1]))
+        if vid is None or nc is None:
+            raise ValueError(f"unsupported potential-temperature volume flux {vf}")
+        if not (isinstance(sf, tuple) and isinstance(sf[0], FluxLMARS) and sf[1] is flux_zero):
+            raise ValueError("surface flux must be (FluxLMARS(c), flux_zero)")
+        if source_terms is not None:
+            raise ValueError("source terms are not supported for this equation set")
+        return vid, _lib.TAG_SF_LMARS, [equations.c_p, equations.c_v, equations.g,
+                                        sf[0].speed_of_sound, float(nc)]
     if isinstance(equations, CompressibleEulerEnergyEquationsWithGravity3D):
         if not (isinstance(vf, tuple) and vf[0] is flux_ranocha
                 and vf[1] is flux_nonconservative_waruszewski_etal):
