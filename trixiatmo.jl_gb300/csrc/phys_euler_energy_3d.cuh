@@ -60,15 +60,16 @@ struct PhysEnergy3D {
     const double v1 = qa[1] + qb[1], v2 = qa[2] + qb[2], v3 = qa[3] + qb[3];
     const double p_avg = qa[4] + qb[4];
     const double vsq = 2.0 * (qa[1] * qb[1] + qa[2] * qb[2] + qa[3] * qb[3]);
-    const double vn = v1 * n1 + v2 * n2 + v3 * n3;
+    // halved normal velocities of both nodes: vn = 0.5 (vn_a + vn_b) and
+    // 0.5 (p_a vn_b + p_b vn_a) = 2 (q_a[4] vnb + q_b[4] vna)
+    const double vna = qa[1] * n1 + qa[2] * n2 + qa[3] * n3;
+    const double vnb = qb[1] * n1 + qb[2] * n2 + qb[3] * n3;
+    const double vn = vna + vnb;
     const double f1 = rho_mean * vn;
     const double f2 = f1 * v1 + p_avg * n1;
     const double f3 = f1 * v2 + p_avg * n2;
     const double f4 = f1 * v3 + p_avg * n3;
-    const double c1 = qa[4] * qb[1] + qb[4] * qa[1];
-    const double c2 = qa[4] * qb[2] + qb[4] * qa[2];
-    const double c3 = qa[4] * qb[3] + qb[4] * qa[3];
-    const double f5 = f1 * (vsq + inv_rho_p_mean * P.inv_gm1) + 2.0 * (n1 * c1 + n2 * c2 + n3 * c3);
+    const double f5 = f1 * (vsq + inv_rho_p_mean * P.inv_gm1) + 2.0 * (qa[4] * vnb + qb[4] * vna);
     const double h = rho_mean * (qb[5] - qa[5]);
     const double g2 = n1 * h, g3 = n2 * h, g4 = n3 * h, g5 = h * vn;
     Fa[0] = f1;      Fb[0] = f1;

@@ -55,15 +55,30 @@ constexpr double kSeriesF2 = 1.0e-2;
 // bound never leaves the series range (margin for rounding of f2).
 constexpr double kLogMeanRange = 0.9e-2;
 
+// The eight-term series R(f2) and Q(f2) described above
+TAG_DEV double ln_series_R(double f2) {
+  return 1.0 + f2 * (-1.0 / 3.0 + f2 * (-4.0 / 45.0 + f2 * (-44.0 / 945.0 +
+         f2 * (-428.0 / 14175.0 + f2 * (-10196.0 / 467775.0 +
+         f2 * (-10719068.0 / 638512875.0 + f2 * (-25865068.0 / 1915538625.0)))))));
+}
+TAG_DEV double ln_series_Q(double f2) {
+  return 1.0 + f2 * (1.0 / 3.0 + f2 * (1.0 / 5.0 + f2 * (1.0 / 7.0 +
+         f2 * (1.0 / 9.0 + f2 * (1.0 / 11.0 + f2 * (1.0 / 13.0 + f2 * (1.0 / 15.0)))))));
+}
+// Below kShortF2 the first four terms are exact to < 2e-17 relative.
+constexpr double kShortF2 = 1.0e-4;
+
 // The rare branch, kept out of line so that the common path is not predicated
-// with its extra reciprocal.
-static __device__ __noinline__ void ln_mean_pair_log(double sx, double dx, double sy, double dy, double R,
-                                              double Q, bool lx, bool ly, double Lxa, double Lxb,
-                                              double Lya, double Lyb, double& rho_mean,
-                                              double& inv_beta_mean) {
-  const double nx = lx ? dx : 0.5 * sx * R;
+// with its extra reciprocal; the series are evaluated only for a mean that is
+// still in range.
+static __device__ __noinline__ void ln_mean_pair_log(double sx, double dx, double sy, double dy,
+                                                     double f2x, double f2y, double Lxa,
+                                                     double Lxb, double Lya, double Lyb,
+                                                     double& rho_mean, double& inv_beta_mean) {
+  const bool lx = f2x >= kSeriesF2, ly = f2y >= kSeriesF2;
+  const double nx = lx ? dx : 0.5 * sx * ln_series_R(f2x);
   const double ex = lx ? Lxb - Lxa : 1.0;
-  const double ny = ly ? Lyb - Lya : 2.0 * Q;
+  const double ny = ly ? Lyb - Lya : 2.0 * ln_series_Q(f2y);
   const double ey = ly ? dy : sy;
   const double r2 = 1.0 / (ex * ey);
   rho_mean = nx * ey * r2;
@@ -73,7 +88,10 @@ static __device__ __noinline__ void ln_mean_pair_log(double sx, double dx, doubl
 // kNodeLogs: true when the caller supplies per-node logarithms (elements
 // whose pairs often leave the series range, e.g. tall 3D elements); false to
 // take the logarithms inside the rare branch (2D elements rarely need them).
-template <bool kNodeLogs>
+// kShort: take the four-term series below kShortF2.  Worth it only where a
+// warp's pairs share one direction (the 3D kernel); in the 2D kernel a warp
+// mixes horizontal and vertical pairs and the extra branch diverges.
+template <bool kNodeLogs, bool kShort = kNodeLogs>
 TAG_DEV void ln_mean_pair(double xa, double xb, double ya, double yb, double Lxa, double Lxb,
                           double Lya, double Lyb, double& rho_mean, double& inv_beta_mean) {
   const double sx = xa + xb, dx = xb - xa;
@@ -82,40 +100,19 @@ TAG_DEV void ln_mean_pair(double xa, double xb, double ya, double yb, double Lxa
   const double isx = sy * r, isy = sx * r;
   const double tx = dx * isx, ty = dy * isy;
   const double f2x = tx * tx, f2y = ty * ty;
-  if constexpr (kNodeLogs) {
-    // the series are needed by both branches: evaluate them once
-    const double R = 1.0 + f2x * (-1.0 / 3.0 + f2x * (-4.0 / 45.0 + f2x * (-44.0 / 945.0 +
-                     f2x * (-428.0 / 14175.0 + f2x * (-10196.0 / 467775.0 +
-                     f2x * (-10719068.0 / 638512875.0 + f2x * (-25865068.0 / 1915538625.0)))))));
-    const double Q = 1.0 + f2y * (1.0 / 3.0 + f2y * (1.0 / 5.0 + f2y * (1.0 / 7.0 +
-                     f2y * (1.0 / 9.0 + f2y * (1.0 / 11.0 + f2y * (1.0 / 13.0 + f2y * (1.0 / 15.0)))))));
-    if (f2x < kSeriesF2 && f2y < kSeriesF2) {
-      rho_mean = 0.5 * sx * R;
-      inv_beta_mean = 2.0 * isy * Q;
-    } else {
-      // rho_mean = nx / ex, inv_beta_mean = ny / ey, one more reciprocal
-      ln_mean_pair_log(sx, dx, sy, dy, R, Q, f2x >= kSeriesF2, f2y >= kSeriesF2, Lxa, Lxb, Lya,
-                       Lyb, rho_mean, inv_beta_mean);
-    }
+  const double fm = fmax(f2x, f2y);
+  if (kShort && fm < kShortF2) {
+    // nearly equal values (e.g. horizontal pairs of a smooth atmosphere)
+    rho_mean = 0.5 * sx * (1.0 + f2x * (-1.0 / 3.0 + f2x * (-4.0 / 45.0 + f2x * (-44.0 / 945.0))));
+    inv_beta_mean = 2.0 * isy * (1.0 + f2y * (1.0 / 3.0 + f2y * (1.0 / 5.0 + f2y * (1.0 / 7.0))));
+  } else if (fm < kSeriesF2) {
+    rho_mean = 0.5 * sx * ln_series_R(f2x);
+    inv_beta_mean = 2.0 * isy * ln_series_Q(f2y);
+  } else if constexpr (kNodeLogs) {
+    ln_mean_pair_log(sx, dx, sy, dy, f2x, f2y, Lxa, Lxb, Lya, Lyb, rho_mean, inv_beta_mean);
   } else {
-    if (f2x < kSeriesF2 && f2y < kSeriesF2) {
-      const double R = 1.0 + f2x * (-1.0 / 3.0 + f2x * (-4.0 / 45.0 + f2x * (-44.0 / 945.0 +
-                       f2x * (-428.0 / 14175.0 + f2x * (-10196.0 / 467775.0 +
-                       f2x * (-10719068.0 / 638512875.0 + f2x * (-25865068.0 / 1915538625.0)))))));
-      const double Q = 1.0 + f2y * (1.0 / 3.0 + f2y * (1.0 / 5.0 + f2y * (1.0 / 7.0 +
-                       f2y * (1.0 / 9.0 + f2y * (1.0 / 11.0 + f2y * (1.0 / 13.0 + f2y * (1.0 / 15.0)))))));
-      rho_mean = 0.5 * sx * R;
-      inv_beta_mean = 2.0 * isy * Q;
-    } else {
-      rho_mean = f2x < kSeriesF2 ? 0.5 * sx * (1.0 / (1.0 + f2x * (1.0 / 3.0 + f2x * (1.0 / 5.0 +
-                                   f2x * (1.0 / 7.0 + f2x * (1.0 / 9.0 + f2x * (1.0 / 11.0 +
-                                   f2x * (1.0 / 13.0 + f2x * (1.0 / 15.0)))))))))
-                                 : dx / log(xb / xa);
-      inv_beta_mean = f2y < kSeriesF2 ? 2.0 * isy * (1.0 + f2y * (1.0 / 3.0 + f2y * (1.0 / 5.0 +
-                                        f2y * (1.0 / 7.0 + f2y * (1.0 / 9.0 + f2y * (1.0 / 11.0 +
-                                        f2y * (1.0 / 13.0 + f2y * (1.0 / 15.0))))))))
-                                      : log(yb / ya) / dy;
-    }
+    rho_mean = f2x < kSeriesF2 ? 0.5 * sx * ln_series_R(f2x) : dx / log(xb / xa);
+    inv_beta_mean = f2y < kSeriesF2 ? 2.0 * isy * ln_series_Q(f2y) : log(yb / ya) / dy;
   }
 }
 
