@@ -177,13 +177,31 @@ int tag_state_device_ptr(tag_handle h, double** u_dev);
  * pattern src/callbacks_step/stepsize_dg2d.jl:5-44. */
 int tag_max_dt(tag_handle h, double* out);
 
-/* Advances the resident state by `nsteps` CarpenterKennedy2N54 steps.  With
+/* Advances the resident state by `nsteps` steps of the handle's time
+ * integrator (CarpenterKennedy2N54 unless tag_set_time_integrator chose an
+ * SSP scheme).  With
  * fixed_dt > 0 every step uses it, otherwise dt = cfl * max_dt(u) before each
  * step (StepsizeCallback), per ensemble member.  t points to nmembers doubles
  * (one when there is a single mesh): the members' times, read and updated.
- * Each step is one CUDA-graph replay of a dt kernel and
- * 5 x (interface kernel + element kernel). */
+ * Each step is one CUDA-graph replay of a dt kernel and one
+ * (interface kernel + element kernel) pair per stage (5, 4 or 3 stages). */
 int tag_rk_steps(tag_handle h, int32_t nsteps, double cfl, double fixed_dt, double* t);
+
+/* Time integrator of tag_rk_steps.  The reference picks it by the algorithm
+ * passed to `solve(ode, alg; dt, callback = StepsizeCallback(cfl))`:
+ *   TAG_RK_CK2N54   CarpenterKennedy2N54(williamson_condition = false), the default
+ *                   (e.g. examples/euler/moist_air/buoyancy/elixir_gemein_bubble.jl)
+ *   TAG_RK_SSPRK43  SSPRK43() with the step size of the StepsizeCallback,
+ *                   adaptive = false (examples/euler/dry_air/buoyancy/
+ *                   elixir_energy_inertia_gravity_waves.jl,
+ *                   elixir_potential_temperature_inertia_gravity_waves.jl)
+ *   TAG_RK_SSPRK33  SSPRK33() (elixir_gemein_nonhydrostatic_gravity_waves.jl)
+ * Applies to the following tag_rk_steps calls (the captured step graph is
+ * rebuilt); stage limiters run after every stage of any scheme. */
+#define TAG_RK_CK2N54 0
+#define TAG_RK_SSPRK43 1
+#define TAG_RK_SSPRK33 2
+int tag_set_time_integrator(tag_handle h, int32_t scheme);
 
 /* Per-member max_dt of the resident state (out: nmembers doubles). */
 int tag_max_dt_members(tag_handle h, double* out);

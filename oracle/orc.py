@@ -94,6 +94,12 @@ def lib():
         L.orc_pt_ssprk43_run.restype = ctypes.c_int
         L.orc_pt_ssprk43_run.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_double,
                                          ctypes.c_double]
+        for name in ("orc_euler2d_ssp_steps", "orc_moist_ssp_steps", "orc_pt_ssp_steps",
+                     "orc_cov_ssp_steps", "orc_euler3d_ssp_steps"):
+            f = getattr(L, name)
+            f.restype = ctypes.c_double
+            f.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                          ctypes.c_int, ctypes.c_double, ctypes.c_double]
         L.orc_pt_ck_steps.restype = ctypes.c_double
         L.orc_pt_ck_steps.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_int]
@@ -131,6 +137,11 @@ def lib():
         L.orc_rainy_newton_states.argtypes = [_dp, ctypes.c_long, ctypes.c_int, ctypes.c_double,
                                               ctypes.c_int, ctypes.c_int, _dp, _ip,
                                               ctypes.POINTER(ctypes.c_long)]
+        L.orc_rainy_ssp_steps.restype = ctypes.c_double
+        L.orc_rainy_ssp_steps.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                          ctypes.c_int]
         L.orc_rainy_ck_steps.restype = ctypes.c_double
         L.orc_rainy_ck_steps.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double,
                                          ctypes.c_double, ctypes.c_int, ctypes.c_double,
@@ -207,6 +218,10 @@ class Euler2D:
     def ck_steps(self, u, k, t, cfl, nsteps, fixed_dt=0.0):
         return lib().orc_euler2d_ck_steps(self.h, _p(u), _p(k), t, cfl, nsteps, fixed_dt)
 
+    def ssp_steps(self, u, t, cfl, nsteps, scheme, fixed_dt=0.0, t_end=0.0):
+        """SSPRK43 (scheme 1) or SSPRK33 (scheme 2) steps; returns the new time."""
+        return lib().orc_euler2d_ssp_steps(self.h, _p(u), t, cfl, nsteps, scheme, fixed_dt, t_end)
+
     def ssprk43_run(self, u, t0, t_end, cfl):
         return lib().orc_euler2d_ssprk43_run(self.h, _p(u), t0, t_end, cfl)
 
@@ -253,6 +268,10 @@ class Euler3D:
     def ck_steps(self, u, k, t, cfl, nsteps, fixed_dt=0.0):
         return lib().orc_euler3d_ck_steps(self.h, _p(u), _p(k), t, cfl, nsteps, fixed_dt)
 
+    def ssp_steps(self, u, t, cfl, nsteps, scheme, fixed_dt=0.0, t_end=0.0):
+        """SSPRK43 (scheme 1) or SSPRK33 (scheme 2) steps; returns the new time."""
+        return lib().orc_euler3d_ssp_steps(self.h, _p(u), t, cfl, nsteps, scheme, fixed_dt, t_end)
+
 
 class CovSWE:
     """Covariant shallow water on the cubed sphere; geometry (aux, xyz) and
@@ -287,6 +306,10 @@ class CovSWE:
 
     def ck_steps(self, u, k, t, cfl, nsteps, fixed_dt=0.0, t_end=0.0):
         return lib().orc_cov_ck_steps(self.h, _p(u), _p(k), t, cfl, nsteps, fixed_dt, t_end)
+
+    def ssp_steps(self, u, t, cfl, nsteps, scheme, fixed_dt=0.0, t_end=0.0):
+        """SSPRK43 (scheme 1) or SSPRK33 (scheme 2) steps; returns the new time."""
+        return lib().orc_cov_ssp_steps(self.h, _p(u), t, cfl, nsteps, scheme, fixed_dt, t_end)
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -332,6 +355,10 @@ class PotTemp2D:
 
     def ck_steps(self, u, k, t, cfl, nsteps):
         return lib().orc_pt_ck_steps(self.h, _p(u), _p(k), t, cfl, nsteps)
+
+    def ssp_steps(self, u, t, cfl, nsteps, scheme, fixed_dt=0.0, t_end=0.0):
+        """SSPRK43 (scheme 1) or SSPRK33 (scheme 2) steps; returns the new time."""
+        return lib().orc_pt_ssp_steps(self.h, _p(u), t, cfl, nsteps, scheme, fixed_dt, t_end)
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -384,6 +411,10 @@ class Moist2D:
 
     def ck_steps(self, u, k, t, cfl, nsteps, fixed_dt=0.0, t_end=0.0):
         return lib().orc_moist_ck_steps(self.h, _p(u), _p(k), t, cfl, nsteps, fixed_dt, t_end)
+
+    def ssp_steps(self, u, t, cfl, nsteps, scheme, fixed_dt=0.0, t_end=0.0):
+        """SSPRK43 (scheme 1) or SSPRK33 (scheme 2) steps; returns the new time."""
+        return lib().orc_moist_ssp_steps(self.h, _p(u), t, cfl, nsteps, scheme, fixed_dt, t_end)
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -462,6 +493,13 @@ class Rainy2D:
                  t_end=0.0):
         return lib().orc_rainy_ck_steps(self.h, _p(u), _p(k), t, cfl, nsteps, fixed_dt, mode, tol,
                                         maxit, t_end)
+
+    def ssp_steps(self, u, t, cfl, nsteps, scheme, fixed_dt=0.0, mode=0, tol=1e-9, maxit=20,
+                  t_end=0.0):
+        """SSPRK43 (scheme 1) or SSPRK33 (scheme 2) steps with the Newton stage
+        limiter after every stage; returns the new time."""
+        return lib().orc_rainy_ssp_steps(self.h, _p(u), t, cfl, nsteps, scheme, fixed_dt, t_end,
+                                         mode, tol, maxit)
 
 
 def rainy_newton_states(u, mode=1, tol=1e-12, maxit=20, polish=0, guesses=None):

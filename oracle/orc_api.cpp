@@ -727,6 +727,14 @@ double orc_euler3d_ck_steps(void* h, double* u, double* k, double t, double cfl,
 }
 
 
+double orc_euler3d_ssp_steps(void* h, double* u, double t, double cfl, int nsteps, int scheme,
+                             double fixed_dt, double t_end) {
+  auto* c = static_cast<Euler3DCase*>(h);
+  return ssp_steps([&](const double* uu, double* dd, double tt) { c->dg->rhs(uu, dd, tt); },
+                   [&](const double* uu) { return c->dg->max_dt(uu); }, [](double*) {}, u,
+                   c->ndofs() * 6, t, cfl, nsteps, scheme, fixed_dt, t_end);
+}
+
 // ---- 2D rainy Euler (flux_ec_rain / flux_lax_friedrichs, source_terms_rainy,
 //      simple slip walls) on a StructuredMesh rectangle
 // weak_form: VolumeIntegralWeakForm (else flux differencing with flux_ec_rain);
@@ -887,6 +895,19 @@ double orc_rainy_ck_steps(void* h, double* u, double* k, double t, double cfl, i
   return t;
 }
 
+// SSPRK43 / SSPRK33 steps with the Newton stage limiter after every stage.
+double orc_rainy_ssp_steps(void* h, double* u, double t, double cfl, int nsteps, int scheme,
+                           double fixed_dt, double t_end, int mode, double tol, int maxit) {
+  auto* c = static_cast<RainyCase*>(h);
+  return ssp_steps([&](const double* uu, double* dd, double tt) { c->dg->rhs(uu, dd, tt); },
+                   [&](const double* uu) { return c->dg->max_dt(uu); },
+                   [&](double* v) {
+                     long nf;
+                     orc_rainy_newton(h, v, mode, tol, maxit, 0, nullptr, nullptr, &nf);
+                   },
+                   u, c->ndofs() * 9, t, cfl, nsteps, scheme, fixed_dt, t_end);
+}
+
 // Pointwise helpers for tests: flux_ec_rain, flux_llf, residual, Jacobian.
 void orc_rainy_flux_ec(const double* ul, const double* ur, const double* n, double* f) {
   RainyEuler2D eq;
@@ -1036,6 +1057,14 @@ double orc_cov_ck_steps(void* h, double* u, double* k, double t, double cfl, int
   return t;
 }
 
+double orc_cov_ssp_steps(void* h, double* u, double t, double cfl, int nsteps, int scheme,
+                         double fixed_dt, double t_end) {
+  auto* c = static_cast<CovDG*>(h);
+  return ssp_steps([&](const double* uu, double* dd, double) { c->rhs(uu, dd); },
+                   [&](const double* uu) { return c->max_dt(uu); }, [](double*) {}, u,
+                   (size_t)c->nelem * c->n * c->n * 3, t, cfl, nsteps, scheme, fixed_dt, t_end);
+}
+
 // ---- 2D potential temperature with gravity --------------------------------
 // volume: 0 flux_tec, 1 flux_ec, 2 flux_etec; nc: 0 waruszewski, 1 artiano,
 // 2 souza; wall_kind: 1 StructuredMesh, 2 outward normal.
@@ -1105,6 +1134,35 @@ double orc_pt_ck_steps(void* h, double* u, double* k, double t, double cfl, int 
     t += dt;
   }
   return t;
+}
+
+// SSPRK43 (scheme 1) / SSPRK33 (scheme 2) steps of the energy 2D, moist,
+// potential-temperature and covariant cases (orc::ssp_steps).
+double orc_euler2d_ssp_steps(void* h, double* u, double t, double cfl, int nsteps, int scheme,
+                             double fixed_dt, double t_end) {
+  auto* c = static_cast<Euler2DCase*>(h);
+  return ssp_steps([&](const double* uu, double* dd, double tt) { c->dg->rhs(uu, dd, tt); },
+                   [&](const double* uu) { return c->dg->max_dt(uu); }, [](double*) {}, u,
+                   c->ndofs() * 5, t,
+                   cfl, nsteps, scheme, fixed_dt, t_end);
+}
+
+double orc_moist_ssp_steps(void* h, double* u, double t, double cfl, int nsteps, int scheme,
+                           double fixed_dt, double t_end) {
+  auto* c = static_cast<MoistCase*>(h);
+  return ssp_steps([&](const double* uu, double* dd, double tt) { c->dg->rhs(uu, dd, tt); },
+                   [&](const double* uu) { return c->dg->max_dt(uu); }, [](double*) {}, u,
+                   c->ndofs() * 6, t,
+                   cfl, nsteps, scheme, fixed_dt, t_end);
+}
+
+double orc_pt_ssp_steps(void* h, double* u, double t, double cfl, int nsteps, int scheme,
+                        double fixed_dt, double t_end) {
+  auto* c = static_cast<PTCase*>(h);
+  return ssp_steps([&](const double* uu, double* dd, double tt) { c->dg->rhs(uu, dd, tt); },
+                   [&](const double* uu) { return c->dg->max_dt(uu); }, [](double*) {}, u,
+                   c->ndofs() * 5, t,
+                   cfl, nsteps, scheme, fixed_dt, t_end);
 }
 
 double orc_pt_stolarsky(double x, double y, double gamma) {

@@ -51,19 +51,67 @@ void ck2n54_step(Rhs&& rhs, double* u, double* k, double* du, size_t N, double t
   }
 }
 
-template <class Rhs>
-void ssprk43_step(Rhs&& rhs, double* u, double* tmp, double* du, double* u0, size_t N, double t,
-                  double dt) {
+// One SSPRK43 step (Kraaijevanger 1991, Shu-Osher form); `lim(v)` is the
+// stage limiter applied to every stage value (a no-op without one).
+template <class Rhs, class Lim>
+void ssprk43_step(Rhs&& rhs, Lim&& lim, double* u, double* tmp, double* du, double* u0, size_t N,
+                  double t, double dt) {
   const double h = 0.5 * dt;
   for (size_t q = 0; q < N; ++q) u0[q] = u[q];
   rhs(u, du, t);
   for (size_t q = 0; q < N; ++q) tmp[q] = u[q] + h * du[q];
+  lim(tmp);
   rhs(tmp, du, t + h);
   for (size_t q = 0; q < N; ++q) tmp[q] = tmp[q] + h * du[q];
+  lim(tmp);
   rhs(tmp, du, t + dt);
   for (size_t q = 0; q < N; ++q) tmp[q] = (2.0 / 3.0) * u0[q] + (1.0 / 3.0) * (tmp[q] + h * du[q]);
+  lim(tmp);
   rhs(tmp, du, t + h);
   for (size_t q = 0; q < N; ++q) u[q] = tmp[q] + h * du[q];
+  lim(u);
+}
+
+template <class Rhs>
+void ssprk43_step(Rhs&& rhs, double* u, double* tmp, double* du, double* u0, size_t N, double t,
+                  double dt) {
+  ssprk43_step(rhs, [](double*) {}, u, tmp, du, u0, N, t, dt);
+}
+
+// One SSPRK33 step (Shu & Osher 1988, Shu-Osher form), stage limiter `lim`.
+template <class Rhs, class Lim>
+void ssprk33_step(Rhs&& rhs, Lim&& lim, double* u, double* tmp, double* du, double* u0, size_t N,
+                  double t, double dt) {
+  for (size_t q = 0; q < N; ++q) u0[q] = u[q];
+  rhs(u, du, t);
+  for (size_t q = 0; q < N; ++q) tmp[q] = u[q] + dt * du[q];
+  lim(tmp);
+  rhs(tmp, du, t + dt);
+  for (size_t q = 0; q < N; ++q) tmp[q] = 0.75 * u0[q] + 0.25 * (tmp[q] + dt * du[q]);
+  lim(tmp);
+  rhs(tmp, du, t + 0.5 * dt);
+  for (size_t q = 0; q < N; ++q) u[q] = (1.0 / 3.0) * u0[q] + (2.0 / 3.0) * (tmp[q] + dt * du[q]);
+  lim(u);
+}
+
+// `nsteps` steps of SSPRK43 (scheme 1) or SSPRK33 (scheme 2), adaptive = false:
+// dt = cfl * max_dt(u) before each step (or fixed_dt > 0), the last one
+// shortened to land on t_end (> 0).  Returns the new time.
+template <class Rhs, class MaxDt, class Lim>
+double ssp_steps(Rhs&& rhs, MaxDt&& max_dt, Lim&& lim, double* u, size_t N, double t, double cfl,
+                 int nsteps, int scheme, double fixed_dt, double t_end) {
+  std::vector<double> tmp(N), du(N), u0(N);
+  for (int s = 0; s < nsteps; ++s) {
+    if (t_end > 0 && t >= t_end) break;
+    double dt = fixed_dt > 0 ? fixed_dt : cfl * max_dt(u);
+    if (t_end > 0 && t + dt > t_end) dt = t_end - t;
+    if (scheme == 2)
+      ssprk33_step(rhs, lim, u, tmp.data(), du.data(), u0.data(), N, t, dt);
+    else
+      ssprk43_step(rhs, lim, u, tmp.data(), du.data(), u0.data(), N, t, dt);
+    t += dt;
+  }
+  return t;
 }
 
 }  // namespace orc

@@ -48,6 +48,9 @@ TAG_VF_COV_EC = 6
 TAG_SF_COV_EC = 4
 TAG_SF_COV_EC_LLF = 5
 TAG_SF_COV_CENTRAL = 6
+TAG_RK_CK2N54 = 0
+TAG_RK_SSPRK43 = 1
+TAG_RK_SSPRK33 = 2
 MLP_PARAMS = 1293
 MLP_TRAINABLE = 1281
 TAG_VF_RANOCHA_WARUSZEWSKI = 1
@@ -109,6 +112,7 @@ SIGNATURES = {
     "tag_time_kernels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp, _dp]),
     "tag_rk_steps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double,
                                     ctypes.c_double, _dp]),
+    "tag_set_time_integrator": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "tag_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32),
                                   ctypes.c_int32]),
     "tag_stream": (ctypes.c_void_p, [ctypes.c_void_p]),

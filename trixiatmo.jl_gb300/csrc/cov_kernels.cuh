@@ -440,9 +440,7 @@ TAG_DEV void cov_element_body(const CovParams& P, const CovGroup& G, int lblk,
       const double dt = st.dt[st.member ? st.member[e] : 0];
 #pragma unroll
       for (int v = 0; v < 3; ++v) {
-        const double kn = st.A * kreg[gq * 3 + v] + dt * dv[v];
-        kreg[gq * 3 + v] = kn;
-        un[v] = ui[v] + st.B * kn;
+        un[v] = stage_value(st, ui[v], kreg + gq * 3 + v, dt, dv[v]);
         u[gq * 3 + v] = un[v];
       }
     }

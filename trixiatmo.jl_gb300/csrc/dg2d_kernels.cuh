@@ -27,7 +27,8 @@ enum VolumeKind : int { kVolFluxDiff = 0, kVolWeak = 1 };
 enum ElementMode : int { kModeRhs = 0, kModeStage = 1 };
 
 struct StageArgs {
-  double A, B;                    // 2N coefficients of this stage
+  double A, B, C;                 // stage coefficients (StageCoef)
+  int ssp, save;                  // SSP (Shu-Osher) form; keep u in k at this stage
   const double* dt;               // per-member dt (device)
   double* max_speed;              // per-member CFL speed accumulator, or null
   const int* member;              // member of each element, or null (one member)
@@ -36,6 +37,33 @@ struct StageArgs {
   double t_rhs;                   // time of an rhs evaluation (rhs mode)
   const double* xy;               // node coordinates (sources), or null
 };
+
+inline void set_stage(StageArgs& st, int scheme, int stage) {
+  const StageCoef c = rk_stage(scheme, stage);
+  st.A = c.A;
+  st.B = c.B;
+  st.C = c.C;
+  st.ssp = c.ssp;
+  st.save = c.save;
+  st.c_stage = c.c;
+}
+
+// New value of one stage variable from its old value uo and time derivative
+// dv; updates the variable's k register (StageCoef's two forms).
+TAG_DEV double stage_value(const StageArgs& st, double uo, double* __restrict__ kp, double dt,
+                           double dv) {
+  if (!st.ssp) {
+    const double kn = st.A * *kp + dt * dv;
+    *kp = kn;
+    return uo + st.B * kn;
+  }
+  const double w = uo + (st.B * dt) * dv;
+  if (st.save) {
+    *kp = uo;
+    return w;
+  }
+  return st.A == 0.0 ? w : st.A * *kp + st.C * w;
+}
 
 // ---------------------------------------------------------------------------
 // Interface + boundary fluxes
@@ -315,9 +343,7 @@ __global__ void k_element(typename Phys::Params Pp, const BasisDev basis, double
     } else {
       const size_t kq = gq * NA + v;
       const double dt = st.dt[st.member ? st.member[e] : 0];
-      const double kn = st.A * kreg[kq] + dt * dv;
-      kreg[kq] = kn;
-      const double un = eb[S::oU + node * NV + v] + st.B * kn;
+      const double un = stage_value(st, eb[S::oU + node * NV + v], kreg + kq, dt, dv);
       eb[S::oU + node * NV + v] = un;
       u[gq * NV + v] = un;
     }

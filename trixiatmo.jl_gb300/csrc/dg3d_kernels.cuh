@@ -272,9 +272,7 @@ __global__ void k_element3d(typename Phys::Params Pp, const BasisDev basis, doub
     } else {
       const size_t kq = gq * NA + v;
       const double dt = st.dt[st.member ? st.member[e] : 0];
-      const double kn = st.A * kreg[kq] + dt * dv;
-      kreg[kq] = kn;
-      const double un = eb[S::oU + node * NV + v] + st.B * kn;
+      const double un = stage_value(st, eb[S::oU + node * NV + v], kreg + kq, dt, dv);
       // all reads of this node's old state (the Coriolis source) precede the
       // barrier below; write the new value to global memory now and to
       // shared memory after it

@@ -64,6 +64,7 @@ struct tag_handle_s {
   PhysPT2D::Params p_pt{};
   // rainy: Newton stage limiter settings, MLP parameters, statistics counters
   bool has_limiter = false;
+  int scheme = TAG_RK_CK2N54;  // time integrator of tag_rk_steps
   NewtonArgs newton{0, 20, 0, 0, 8, 1e-9, nullptr, nullptr, nullptr};
   float* d_mlp = nullptr;
   unsigned long long* d_counters = nullptr;
@@ -153,15 +154,12 @@ struct OpsImpl {
     const int blocks = (h->nelem + epb - 1) / epb;
     const int threads = std::min(cap(), epb * S::TPE);
     const size_t smem = S::bytes(epb);
-    const CK2N54 ck = ck2n54();
     StageArgs st{};
     st.member = h->d_member;
     st.xy = h->d_xy;
     st.t_rhs = t;
     if (mode == kModeStage) {
-      st.A = ck.A[stage];
-      st.B = ck.B[stage];
-      st.c_stage = ck.c[stage];
+      set_stage(st, h->scheme, stage);
       st.t_member = h->d_mscal;
       st.dt = h->d_mscal + h->nmembers;
       st.max_speed = last ? h->d_mscal + 2 * h->nmembers : nullptr;
@@ -239,12 +237,10 @@ struct OpsImpl3D {
     const int blocks = (h->nelem + epb - 1) / epb;
     const int threads = std::min(cap(), ((epb * S::TPE + 31) / 32) * 32);
     const size_t smem = S::bytes(epb);
-    const CK2N54 ck = ck2n54();
     StageArgs st{};
     st.member = h->d_member;
     if (mode == kModeStage) {
-      st.A = ck.A[stage];
-      st.B = ck.B[stage];
+      set_stage(st, h->scheme, stage);
       st.dt = h->d_mscal + h->nmembers;
       st.max_speed = last ? h->d_mscal + 2 * h->nmembers : nullptr;
       k_element3d<Phys, n, kModeStage><<<blocks, threads, smem, h->stream>>>(
@@ -348,15 +344,16 @@ int reset_and_reduce_speeds(tag_handle h) {
 }
 
 int stage_sequence(tag_handle h) {
-  // one RK step: begin-step scalars, then 5 x (interface, element)
+  // one RK step: begin-step scalars, then one (interface, element) pair per stage
   int rc0 = begin_step(h);
   if (rc0) return rc0;
-  for (int s = 0; s < 5; ++s) {
+  const int ns = rk_stages(h->scheme);
+  for (int s = 0; s < ns; ++s) {
     int rc = h->ops->interface(h, h->d_u);
     if (rc) return rc;
     // with a stage limiter the next step's CFL speed is taken from the
     // limited state, after the last Newton solve, not inside the element kernel
-    rc = h->ops->element(h, kModeStage, h->d_u, nullptr, s, s == 4 && !h->has_limiter, 0.0);
+    rc = h->ops->element(h, kModeStage, h->d_u, nullptr, s, s == ns - 1 && !h->has_limiter, 0.0);
     if (rc) return rc;
     if (h->has_limiter) {
       // stage limiter: saturation Newton solve on every node (warm start)
@@ -368,7 +365,7 @@ int stage_sequence(tag_handle h) {
       k_newton_rainy<<<(unsigned)((nodes + 255) / 256), 256, 0, h->stream>>>(h->d_u, nodes, a,
                                                                               h->d_status);
       TAG_CUDA(cudaGetLastError());
-      if (s == 4) {
+      if (s == ns - 1) {
         rc = h->ops->max_speed(h, h->d_u);
         if (rc) return rc;
       }
@@ -462,13 +459,10 @@ int cov_interface(tag_handle h, const double* u) {
 }
 
 int cov_element(tag_handle h, int mode, double* u, double* du, int stage, bool last, double) {
-  const CK2N54 ck = ck2n54();
   StageArgs st{};
   st.member = h->d_member;
   if (mode == kModeStage) {
-    st.A = ck.A[stage];
-    st.B = ck.B[stage];
-    st.c_stage = ck.c[stage];
+    set_stage(st, h->scheme, stage);
     st.t_member = h->d_mscal;
     st.dt = h->d_mscal + h->nmembers;
     st.max_speed = last ? h->d_mscal + 2 * h->nmembers : nullptr;
@@ -1081,6 +1075,17 @@ int tag_time_kernels(tag_handle h, int32_t reps, double* ms_interface, double* m
   *ms_interface = si / reps;
   *ms_element = se / reps;
   h->speed_valid = false;
+  return TAG_OK;
+}
+
+int tag_set_time_integrator(tag_handle h, int32_t scheme) {
+  if (!h) return fail(TAG_E_INVALID, "bad argument");
+  if (scheme != TAG_RK_CK2N54 && scheme != TAG_RK_SSPRK43 && scheme != TAG_RK_SSPRK33)
+    return fail(TAG_E_INVALID, "unknown time integrator");
+  if (scheme != h->scheme) {
+    h->scheme = scheme;
+    h->graph_epb = -2;  // the stage sequence is baked into the captured graph
+  }
   return TAG_OK;
 }
 

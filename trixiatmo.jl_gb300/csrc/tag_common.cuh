@@ -180,6 +180,39 @@ __host__ __device__ inline CK2N54 ck2n54() {
                  2006345519317.0 / 3224310063776.0, 2802321613138.0 / 2924317926251.0}};
 }
 
+// One stage of a time integrator in the form the element kernels apply:
+//   2N (ssp = 0):  k = A k + dt du,  u = u + B k
+//   SSP (ssp = 1): w = u + (B dt) du,  u = A k + C w  (u = w where A = 0),
+//                  k = u at the first stage (save), the step's starting state.
+// The SSP schemes are the Shu-Osher forms of SSPRK43 (Kraaijevanger 1991;
+// h = dt/2: u1 = u + h L(u), u2 = u1 + h L(u1), u3 = 2/3 u + 1/3 (u2 + h L(u2)),
+// u_new = u3 + h L(u3)) and SSPRK33 (Shu & Osher 1988: u1 = u + dt L(u),
+// u2 = 3/4 u + 1/4 (u1 + dt L(u1)), u_new = 1/3 u + 2/3 (u2 + dt L(u2))).
+struct StageCoef {
+  double A, B, C, c;  // c: stage time fraction
+  int ssp, save;
+};
+
+inline int rk_stages(int scheme) {
+  return scheme == TAG_RK_SSPRK43 ? 4 : scheme == TAG_RK_SSPRK33 ? 3 : 5;
+}
+
+inline StageCoef rk_stage(int scheme, int s) {
+  if (scheme == TAG_RK_SSPRK43) {
+    static const double c[4] = {0.0, 0.5, 1.0, 0.5};
+    if (s == 2) return StageCoef{2.0 / 3.0, 0.5, 1.0 / 3.0, c[s], 1, 0};
+    return StageCoef{0.0, 0.5, 1.0, c[s], 1, s == 0};
+  }
+  if (scheme == TAG_RK_SSPRK33) {
+    static const double c[3] = {0.0, 1.0, 0.5};
+    if (s == 1) return StageCoef{0.75, 1.0, 0.25, c[s], 1, 0};
+    if (s == 2) return StageCoef{1.0 / 3.0, 1.0, 2.0 / 3.0, c[s], 1, 0};
+    return StageCoef{0.0, 1.0, 1.0, c[s], 1, 1};
+  }
+  const CK2N54 ck = ck2n54();
+  return StageCoef{ck.A[s], ck.B[s], 0.0, ck.c[s], 0, 0};
+}
+
 // Step control shared by all ensemble members (device memory, so a captured
 // graph picks up new values without re-instantiation).
 struct StepCtl {

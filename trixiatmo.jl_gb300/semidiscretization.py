@@ -251,6 +251,10 @@ class _Handle:
             self.h = None
 
 
+_RK_METHODS = {"CarpenterKennedy2N54": _lib.TAG_RK_CK2N54, "SSPRK43": _lib.TAG_RK_SSPRK43,
+               "SSPRK33": _lib.TAG_RK_SSPRK33}
+
+
 class SemidiscretizationHyperbolic:
     def __new__(cls, *args, **kwargs):
         # covariant equations take the covariant constructor (aux variables)
@@ -345,9 +349,14 @@ class SemidiscretizationHyperbolic:
         _lib.check(self._L.tag_max_dt_members(self._h, _ptr(out)))
         return out
 
-    def rk_steps(self, nsteps, cfl=1.0, t=0.0, fixed_dt=0.0):
-        """CarpenterKennedy2N54 steps; t is a scalar (single mesh) or one time
-        per ensemble member.  Returns the new time(s)."""
+    def rk_steps(self, nsteps, cfl=1.0, t=0.0, fixed_dt=0.0, method="CarpenterKennedy2N54"):
+        """Steps of `method` (CarpenterKennedy2N54, SSPRK43 or SSPRK33, the
+        reference's `solve(ode, alg; callback = StepsizeCallback(cfl))` with
+        adaptive = false); t is a scalar (single mesh) or one time per ensemble
+        member.  Returns the new time(s)."""
+        if method not in _RK_METHODS:
+            raise ValueError(f"unknown time integrator {method!r}")
+        _lib.check(self._L.tag_set_time_integrator(self._h, _RK_METHODS[method]))
         tt = np.ascontiguousarray(np.broadcast_to(np.asarray(t, dtype=np.float64),
                                                   (self.nmembers,)).copy())
         _lib.check(self._L.tag_rk_steps(self._h, int(nsteps), float(cfl), float(fixed_dt),
