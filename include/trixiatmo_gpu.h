@@ -203,6 +203,50 @@ int tag_rk_steps(tag_handle h, int32_t nsteps, double cfl, double fixed_dt, doub
 #define TAG_RK_SSPRK33 2
 int tag_set_time_integrator(tag_handle h, int32_t scheme);
 
+/* ---- analysis of the resident state (AnalysisCallback) ------------------ */
+/* Integrals over each member's domain, computed on the device in a fixed
+ * summation order (repeated calls return the same bits):
+ *   TAG_AQ_STATE          every conserved variable (nv values; the basis of
+ *                         :conservation_error, Trixi `integrate(u_ode, semi)`)
+ *   TAG_AQ_ENTROPY        the equations' `entropy` (extra_analysis_integrals =
+ *                         (entropy,)); not defined for the rainy equations
+ *   TAG_AQ_ENERGY_TOTAL   `energy_total` (energy, moist and potential-
+ *                         temperature equations)
+ *   TAG_AQ_ENTROPY_TIMEDERIVATIVE  the integral of cons2entropy(u) . du/dt with
+ *                         du/dt = rhs(u, t) evaluated on the device (the
+ *                         AnalysisCallback's default `entropy_timederivative`)
+ * Quadrature: LGL weights times |J| (Cartesian meshes: 1/inverse_jacobian;
+ * covariant equations: the area element of aux_node_vars, reference
+ * src/callbacks_step/analysis_covariant.jl:53-105).  out: nmembers x values
+ * doubles, divided by the member's volume when normalize != 0 (Trixi's
+ * default).  Members of an ensemble must occupy contiguous element ranges. */
+#define TAG_AQ_STATE 0
+#define TAG_AQ_ENTROPY 1
+#define TAG_AQ_ENERGY_TOTAL 2
+#define TAG_AQ_ENTROPY_TIMEDERIVATIVE 3
+int tag_analyze_integral(tag_handle h, int32_t quantity, int32_t normalize, double t, double* out);
+
+/* Analysis nodes for tag_analyze_errors.  Cartesian meshes: *m = 2N + 1
+ * nodes per direction (the LGL nodes of degree 2N, Trixi's default analysis
+ * polydeg); x (may be null) receives their coordinates [E][m^d][d],
+ * interpolated from node_coordinates (which tag_create must have been given).
+ * Covariant equations: *m = 0, the analysis nodes are the solution nodes and
+ * x receives their Cartesian coordinates [nodes][3]. */
+int tag_analysis_nodes(tag_handle h, int32_t* m, double* x);
+
+/* l2 and linf errors of the resident state against u_exact (host array, the
+ * caller's initial_condition(x, t) at the analysis nodes: [E][m^d][nv] on
+ * Cartesian meshes, [nodes][nv] for covariant equations in the contravariant
+ * components).  l2 = sqrt(sum wJ d^2 / sum wJ), linf = max |d| per variable,
+ * d = u_exact - u, with the solution and J interpolated to the analysis nodes
+ * on Cartesian meshes (Trixi's calc_error_norms; covariant
+ * src/callbacks_step/analysis_covariant.jl:143-189).  l2, linf: nmembers x nv. */
+int tag_analyze_errors(tag_handle h, const double* u_exact, double* l2, double* linf);
+
+/* Legendre-Gauss-Lobatto nodes and weights of degree polydeg on [-1, 1]
+ * (Trixi's LobattoLegendreBasis(polydeg).nodes / .weights); host only. */
+int tag_lgl_basis(int32_t polydeg, double* nodes, double* weights);
+
 /* Per-member max_dt of the resident state (out: nmembers doubles). */
 int tag_max_dt_members(tag_handle h, double* out);
 

@@ -51,6 +51,10 @@ TAG_SF_COV_CENTRAL = 6
 TAG_RK_CK2N54 = 0
 TAG_RK_SSPRK43 = 1
 TAG_RK_SSPRK33 = 2
+TAG_AQ_STATE = 0
+TAG_AQ_ENTROPY = 1
+TAG_AQ_ENERGY_TOTAL = 2
+TAG_AQ_ENTROPY_TIMEDERIVATIVE = 3
 MLP_PARAMS = 1293
 MLP_TRAINABLE = 1281
 TAG_VF_RANOCHA_WARUSZEWSKI = 1
@@ -113,6 +117,11 @@ SIGNATURES = {
     "tag_rk_steps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double,
                                     ctypes.c_double, _dp]),
     "tag_set_time_integrator": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "tag_analyze_integral": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                            ctypes.c_double, _dp]),
+    "tag_analysis_nodes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), _dp]),
+    "tag_analyze_errors": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp]),
+    "tag_lgl_basis": (ctypes.c_int, [ctypes.c_int32, _dp, _dp]),
     "tag_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32),
                                   ctypes.c_int32]),
     "tag_stream": (ctypes.c_void_p, [ctypes.c_void_p]),

@@ -18,6 +18,7 @@
 // nodes of each element contiguous; aux[node][26] is the reference's
 // aux_node_vars; pk[node][16] a packed copy of what the element kernel reads.
 #pragma once
+#include "cov_params.cuh"
 #include "dg2d_kernels.cuh"
 
 namespace tag {
@@ -26,17 +27,6 @@ namespace tag {
 enum CovPack : int {
   kPJ = 0, kPGc11, kPGc12, kPGc22, kPGv11, kPGv12, kPGv22, kPHs,
   kPC111, kPC112, kPC122, kPC211, kPC212, kPC222, kPF, kPInvJ, kPack = 16
-};
-
-struct CovParams {
-  double g;
-  int split;     // SplitCovariantShallowWaterEquations2D
-  int volume;    // 0 weak form, 1 flux differencing
-  int vol_sym;   // 0 flux_central, 1 flux_ec
-  int vol_nc;    // 0 none, 1 flux_nonconservative_ec
-  int surf_sym;  // 0 flux_central, 1 flux_ec
-  int surf_diss; // 0 none, 1 local Lax-Friedrichs
-  int surf_nc;   // 0 none, 1 flux_nonconservative_ec, 2 flux_nonconservative_surface_simplified
 };
 
 struct CovGroup {

@@ -18,6 +18,7 @@
 #include "phys_moist_2d.cuh"
 #include "phys_pt_2d.cuh"
 #include "phys_rainy_2d.cuh"
+#include "tag_analysis.cuh"
 
 using namespace tag;
 
@@ -86,6 +87,14 @@ struct tag_handle_s {
   bool speed_valid = false;
   int epb = 0;
   const Ops* ops = nullptr;
+  // analysis (allocated by the first analysis call)
+  bool an_ready = false;
+  int an_m = 0, an_chunks = 0;
+  long an_chunk = 0;
+  double *d_an_wj = nullptr, *d_an_V = nullptr, *d_an_wa = nullptr, *d_an_rows = nullptr,
+         *d_an_erows = nullptr, *d_an_out = nullptr, *d_an_uex = nullptr, *d_an_x = nullptr;
+  long* d_an_rng = nullptr;  // [4][nmembers]: node begin, node end, element begin, element end
+  size_t an_uex_cap = 0;
 };
 
 namespace {
@@ -744,6 +753,139 @@ bool boundary_kind_ok(int eq, int kind) {
   }
 }
 
+// ---- analysis ---------------------------------------------------------------
+int analysis_phys(tag_handle h) {
+  switch (h->eq) {
+    case TAG_EQ_EULER_ENERGY_2D: return kAnEnergy2D;
+    case TAG_EQ_EULER_ENERGY_3D: return kAnEnergy3D;
+    case TAG_EQ_RAINY_2D: return kAnRainy2D;
+    case TAG_EQ_MOIST_EULER_2D: return kAnMoist2D;
+    case TAG_EQ_POTENTIAL_TEMPERATURE_2D: return kAnPT2D;
+    default: return kAnCov;
+  }
+}
+
+const void* analysis_params(tag_handle h) {
+  switch (h->eq) {
+    case TAG_EQ_EULER_ENERGY_2D: return &h->p_energy;
+    case TAG_EQ_EULER_ENERGY_3D: return &h->p_energy3d;
+    case TAG_EQ_RAINY_2D: return &h->p_rainy;
+    case TAG_EQ_MOIST_EULER_2D: return &h->p_moist;
+    case TAG_EQ_POTENTIAL_TEMPERATURE_2D: return &h->p_pt;
+    default: return &h->p_cov;
+  }
+}
+
+// Member node / element ranges, quadrature weights x |J| per node, the
+// analysis interpolation (Cartesian meshes) and reduction scratch; once per
+// handle.
+int analysis_setup(tag_handle h) {
+  if (h->an_ready) return TAG_OK;
+  const bool cov = h->eq == TAG_EQ_COVARIANT_SWE;
+  const int M = h->nmembers, E = h->nelem;
+  std::vector<int> member(E, 0);
+  if (h->d_member) {
+    TAG_CUDA(cudaMemcpyAsync(member.data(), h->d_member, sizeof(int) * E, cudaMemcpyDeviceToHost,
+                             h->stream));
+    TAG_CUDA(cudaStreamSynchronize(h->stream));
+  }
+  std::vector<long> enode(E + 1);
+  if (cov) {
+    for (int k = 0; k < h->h_groups.count; ++k) {
+      const CovGroup& g = h->h_groups.g[k];
+      for (int e = g.e0; e < g.e0 + g.ne; ++e) enode[e] = g.node0 + (long)(e - g.e0) * g.n * g.n;
+    }
+  } else {
+    for (int e = 0; e < E; ++e) enode[e] = (long)e * h->npe;
+  }
+  enode[E] = h->nodes;
+  std::vector<long> rng(4 * (size_t)M, -1);
+  long *nb = rng.data(), *ne_ = nb + M, *eb = nb + 2 * M, *ee = nb + 3 * M;
+  for (int e = 0; e < E; ++e) {
+    const int m = member[e];
+    if (m < 0 || m >= M) return fail(TAG_E_INVALID, "element member out of range");
+    if (eb[m] < 0)
+      eb[m] = e;
+    else if (ee[m] != e)
+      return fail(TAG_E_INVALID, "analysis needs each member in one contiguous element range");
+    ee[m] = e + 1;
+  }
+  long lmax = 1;
+  for (int m = 0; m < M; ++m) {
+    if (eb[m] < 0) return fail(TAG_E_INVALID, "a member has no elements");
+    nb[m] = enode[eb[m]];
+    ne_[m] = enode[ee[m]];
+    lmax = std::max(lmax, ne_[m] - nb[m]);
+  }
+  int rc = upload(&h->d_an_rng, rng.data(), rng.size(), h->stream);
+  if (rc) return rc;
+  TAG_CUDA(cudaMalloc(&h->d_an_wj, sizeof(double) * h->nodes));
+  std::vector<double*> tmp;
+  auto solution_weights = [&](int n, double** dw) {
+    std::vector<double> x(n), w(n);
+    lgl_nodes_weights(n - 1, x.data(), w.data());
+    *dw = nullptr;
+    const int r = upload(dw, w.data(), (size_t)n, h->stream);
+    tmp.push_back(*dw);
+    return r;
+  };
+  if (cov) {
+    for (int k = 0; k < h->h_groups.count && !rc; ++k) {
+      const CovGroup& g = h->h_groups.g[k];
+      double* dw;
+      if ((rc = solution_weights(g.n, &dw))) break;
+      rc = analysis_weights_covariant(h->d_aux, dw, g.n, g.node0, (long)g.ne * g.n * g.n,
+                                      h->d_an_wj, h->stream);
+    }
+  } else {
+    double* dw;
+    if (!(rc = solution_weights(h->n, &dw)))
+      rc = analysis_weights_cartesian(h->d_invJ, dw, h->n, h->dim, h->nodes, h->d_an_wj,
+                                      h->stream);
+    if (!rc) {
+      const int n = h->n, m = 2 * n - 1;
+      std::vector<double> xn(n), wn(n), xm(m), wm(m), V((size_t)m * n);
+      lgl_nodes_weights(n - 1, xn.data(), wn.data());
+      lgl_nodes_weights(m - 1, xm.data(), wm.data());
+      interpolation_matrix(xn.data(), n, xm.data(), m, V.data());
+      h->an_m = m;
+      rc = upload(&h->d_an_V, V.data(), V.size(), h->stream);
+      if (!rc) rc = upload(&h->d_an_wa, wm.data(), wm.size(), h->stream);
+      if (!rc)
+        rc = upload(&h->d_an_erows, (const double*)nullptr, (size_t)E * (2 * h->nv + 1),
+                    h->stream);
+    }
+  }
+  TAG_CUDA(cudaStreamSynchronize(h->stream));
+  for (double* p : tmp)
+    if (p) cudaFree(p);
+  if (rc) return rc;
+  h->an_chunk = 8192;
+  h->an_chunks = (int)((lmax + h->an_chunk - 1) / h->an_chunk);
+  const size_t width = 2 * (size_t)h->nv + 1;
+  if ((rc = upload(&h->d_an_rows, (const double*)nullptr, (size_t)M * h->an_chunks * width,
+                   h->stream)))
+    return rc;
+  if ((rc = upload(&h->d_an_out, (const double*)nullptr, (size_t)M * width, h->stream))) return rc;
+  h->an_ready = true;
+  return TAG_OK;
+}
+
+AnalysisArgs analysis_args(tag_handle h, int quantity, const double* du) {
+  AnalysisArgs a{};
+  a.phys = analysis_phys(h);
+  a.params = analysis_params(h);
+  a.quantity = quantity;
+  a.nmembers = h->nmembers;
+  a.u = h->d_u;
+  a.du = du;
+  a.aux = h->eq == TAG_EQ_COVARIANT_SWE ? h->d_aux : nullptr;
+  a.wj = h->d_an_wj;
+  a.mbeg = h->d_an_rng;
+  a.mend = h->d_an_rng + h->nmembers;
+  return a;
+}
+
 }  // namespace
 
 extern "C" {
@@ -910,13 +1052,17 @@ int tag_destroy(tag_handle h) {
   if (!h) return TAG_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->graph) cudaGraphExecDestroy(h->graph);
-  double* dp[] = {h->d_u, h->d_k, h->d_Ja, h->d_invJ, h->d_xy, h->d_sfv, h->d_tmp_u, h->d_tmp_du};
+  double* dp[] = {h->d_u,       h->d_k,       h->d_Ja,         h->d_invJ,    h->d_xy,
+                  h->d_sfv,     h->d_tmp_u,   h->d_tmp_du,     h->d_an_wj,   h->d_an_V,
+                  h->d_an_wa,   h->d_an_rows, h->d_an_erows,   h->d_an_out,  h->d_an_uex,
+                  h->d_an_x};
   for (double* p : dp)
     if (p) cudaFree(p);
   int* ip[] = {h->d_if_e, h->d_if_f, h->d_if_flip, h->d_bd_e, h->d_bd_f, h->d_bd_kind};
   for (int* p : ip)
     if (p) cudaFree(p);
   if (h->d_member) cudaFree(h->d_member);
+  if (h->d_an_rng) cudaFree(h->d_an_rng);
   if (h->d_aux) cudaFree(h->d_aux);
   if (h->d_pk) cudaFree(h->d_pk);
   if (h->d_groups) cudaFree(h->d_groups);
@@ -1198,6 +1344,122 @@ int tag_fp64_peak(double* flops_per_s) {
   cudaEventDestroy(b);
   cudaFree(out);
   *flops_per_s = 2.0 * 8.0 * iters * (double)threads * blocks / (best * 1e-3);
+  return TAG_OK;
+}
+
+int tag_analyze_integral(tag_handle h, int32_t quantity, int32_t normalize, double t,
+                         double* out) {
+  if (!h || !out) return fail(TAG_E_INVALID, "bad argument");
+  const int nq = analysis_values(analysis_phys(h), quantity);
+  if (nq < 0) return fail(TAG_E_INVALID, "quantity not defined for these equations");
+  int rc = analysis_setup(h);
+  if (rc) return rc;
+  const double* du = nullptr;
+  if (quantity == TAG_AQ_ENTROPY_TIMEDERIVATIVE) {
+    if (!h->d_tmp_du) TAG_CUDA(cudaMalloc(&h->d_tmp_du, sizeof(double) * h->nodes * h->nv));
+    if ((rc = h->ops->interface(h, h->d_u))) return rc;
+    if ((rc = h->ops->element(h, kModeRhs, h->d_u, h->d_tmp_du, 0, false, t))) return rc;
+    du = h->d_tmp_du;
+  }
+  const AnalysisArgs a = analysis_args(h, quantity, du);
+  if ((rc = analysis_node_rows(a, h->an_chunks, h->an_chunk, h->d_an_rows, h->stream)))
+    return fail(rc, "analysis launch failed");
+  if ((rc = analysis_reduce_rows(h->d_an_rows, nq + 1, 0, 0, nullptr, nullptr, h->an_chunks,
+                                 h->nmembers, h->d_an_out, h->stream)))
+    return fail(rc, "analysis reduction failed");
+  const int M = h->nmembers;
+  std::vector<double> v((size_t)M * (nq + 1));
+  TAG_CUDA(cudaMemcpyAsync(v.data(), h->d_an_out, sizeof(double) * v.size(),
+                           cudaMemcpyDeviceToHost, h->stream));
+  TAG_CUDA(cudaStreamSynchronize(h->stream));
+  for (int m = 0; m < M; ++m) {
+    const double* r = &v[(size_t)m * (nq + 1)];
+    for (int q = 0; q < nq; ++q) out[(size_t)m * nq + q] = normalize ? r[q] / r[nq] : r[q];
+  }
+  return TAG_OK;
+}
+
+int tag_analysis_nodes(tag_handle h, int32_t* m, double* x) {
+  if (!h || !m) return fail(TAG_E_INVALID, "bad argument");
+  int rc = analysis_setup(h);
+  if (rc) return rc;
+  if (h->eq == TAG_EQ_COVARIANT_SWE) {
+    *m = 0;
+    if (x) {
+      TAG_CUDA(cudaMemcpyAsync(x, h->d_xy, sizeof(double) * h->nodes * 3, cudaMemcpyDeviceToHost,
+                               h->stream));
+      TAG_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    return TAG_OK;
+  }
+  *m = h->an_m;
+  if (!x) return TAG_OK;
+  if (!h->d_xy) return fail(TAG_E_INVALID, "tag_create was given no node_coordinates");
+  const size_t ma = h->dim == 3 ? (size_t)h->an_m * h->an_m * h->an_m : (size_t)h->an_m * h->an_m;
+  const size_t count = (size_t)h->nelem * ma * h->dim;
+  if (!h->d_an_x) TAG_CUDA(cudaMalloc(&h->d_an_x, sizeof(double) * count));
+  if ((rc = analysis_coordinates(h->dim, h->n, h->an_m, h->nelem, h->d_xy, h->d_an_V, h->d_an_x,
+                                 h->stream)))
+    return fail(rc, "analysis launch failed");
+  TAG_CUDA(cudaMemcpyAsync(x, h->d_an_x, sizeof(double) * count, cudaMemcpyDeviceToHost,
+                           h->stream));
+  TAG_CUDA(cudaStreamSynchronize(h->stream));
+  return TAG_OK;
+}
+
+int tag_analyze_errors(tag_handle h, const double* u_exact, double* l2, double* linf) {
+  if (!h || !u_exact || !l2 || !linf) return fail(TAG_E_INVALID, "bad argument");
+  int rc = analysis_setup(h);
+  if (rc) return rc;
+  const bool cov = h->eq == TAG_EQ_COVARIANT_SWE;
+  const int nv = h->nv, nq = 2 * nv + 1, M = h->nmembers;
+  const size_t ma =
+      cov ? 0
+          : (h->dim == 3 ? (size_t)h->an_m * h->an_m * h->an_m : (size_t)h->an_m * h->an_m);
+  const size_t count = cov ? (size_t)h->nodes * nv : (size_t)h->nelem * ma * nv;
+  if (h->an_uex_cap < count) {
+    if (h->d_an_uex) cudaFree(h->d_an_uex);
+    h->d_an_uex = nullptr;
+    h->an_uex_cap = 0;
+    TAG_CUDA(cudaMalloc(&h->d_an_uex, sizeof(double) * count));
+    h->an_uex_cap = count;
+  }
+  TAG_CUDA(cudaMemcpyAsync(h->d_an_uex, u_exact, sizeof(double) * count, cudaMemcpyHostToDevice,
+                           h->stream));
+  if (cov) {
+    const AnalysisArgs a = analysis_args(h, TAG_AQ_STATE, nullptr);
+    if ((rc = analysis_node_error_rows(a, h->d_an_uex, h->an_chunks, h->an_chunk, h->d_an_rows,
+                                       h->stream)))
+      return fail(rc, "analysis launch failed");
+    rc = analysis_reduce_rows(h->d_an_rows, nq, nv, 2 * nv, nullptr, nullptr, h->an_chunks, M,
+                              h->d_an_out, h->stream);
+  } else {
+    if ((rc = analysis_element_error_rows(analysis_phys(h), h->dim, h->n, h->an_m, h->nelem,
+                                          h->d_u, h->d_invJ, h->d_an_V, h->d_an_wa, h->d_an_uex,
+                                          h->d_an_erows, h->stream)))
+      return fail(rc, "analysis launch failed");
+    rc = analysis_reduce_rows(h->d_an_erows, nq, nv, 2 * nv, h->d_an_rng + 2 * M,
+                              h->d_an_rng + 3 * M, 0, M, h->d_an_out, h->stream);
+  }
+  if (rc) return fail(rc, "analysis reduction failed");
+  std::vector<double> v((size_t)M * nq);
+  TAG_CUDA(cudaMemcpyAsync(v.data(), h->d_an_out, sizeof(double) * v.size(),
+                           cudaMemcpyDeviceToHost, h->stream));
+  TAG_CUDA(cudaStreamSynchronize(h->stream));
+  for (int m = 0; m < M; ++m) {
+    const double* r = &v[(size_t)m * nq];
+    for (int q = 0; q < nv; ++q) {
+      l2[(size_t)m * nv + q] = std::sqrt(r[q] / r[2 * nv]);
+      linf[(size_t)m * nv + q] = r[nv + q];
+    }
+  }
+  return TAG_OK;
+}
+
+int tag_lgl_basis(int32_t polydeg, double* nodes, double* weights) {
+  if (polydeg < 1 || polydeg > 64 || !nodes || !weights)
+    return fail(TAG_E_INVALID, "bad argument");
+  lgl_nodes_weights(polydeg, nodes, weights);
   return TAG_OK;
 }
 

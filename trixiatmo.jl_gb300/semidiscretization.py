@@ -363,6 +363,65 @@ class SemidiscretizationHyperbolic:
                                         _ptr(tt)))
         return float(tt[0]) if self.nmembers == 1 and np.ndim(t) == 0 else tt
 
+    # ---- analysis (AnalysisCallback), on the resident state ---------------------
+    def integrate(self, func="cons2cons", normalize=True):
+        """Trixi's `integrate(func, u_ode, semi; normalize)` of the resident state,
+        func one of "cons2cons" (every conserved variable), "entropy",
+        "energy_total".  Returns one array (or value) per member; a single mesh
+        returns its own."""
+        q = {"cons2cons": _lib.TAG_AQ_STATE, "entropy": _lib.TAG_AQ_ENTROPY,
+             "energy_total": _lib.TAG_AQ_ENERGY_TOTAL}[func]
+        return self._integral(q, normalize, 0.0)
+
+    def entropy_timederivative(self, t=0.0, normalize=True):
+        """The AnalysisCallback's entropy_timederivative: the integral of
+        cons2entropy(u) . rhs(u, t) over the domain (rhs evaluated on the device)."""
+        return self._integral(_lib.TAG_AQ_ENTROPY_TIMEDERIVATIVE, normalize, t)
+
+    def _integral(self, q, normalize, t):
+        nq = self.equations.nvariables if q == _lib.TAG_AQ_STATE else 1
+        out = np.zeros(self.nmembers * nq)
+        _lib.check(self._L.tag_analyze_integral(self._h, int(q), int(bool(normalize)), float(t),
+                                                _ptr(out)))
+        out = out.reshape(self.nmembers, nq)
+        if nq == 1:
+            out = out[:, 0]
+        return out[0] if self.nmembers == 1 else out
+
+    def analysis_nodes(self):
+        """(m, x): m analysis nodes per direction (0: the solution nodes) and
+        their coordinates."""
+        m = ctypes.c_int32()
+        _lib.check(self._L.tag_analysis_nodes(self._h, ctypes.byref(m), None))
+        m = m.value
+        if m == 0:
+            shape = (self.ndofs, 3)
+        else:
+            shape = (self.nelements,) + (m,) * self.ndims + (self.ndims,)
+        x = np.zeros(int(np.prod(shape)))
+        _lib.check(self._L.tag_analysis_nodes(self._h, ctypes.byref(ctypes.c_int32()), _ptr(x)))
+        return m, x.reshape(shape)
+
+    def exact_at_analysis_nodes(self, t=0.0, initial_condition=None):
+        ic = initial_condition or self.initial_condition
+        m, x = self.analysis_nodes()
+        if m == 0:
+            return self.compute_coefficients(t, initial_condition)
+        return np.ascontiguousarray(ic(x, t, self.equations), dtype=np.float64)
+
+    def calc_error_norms(self, t=0.0, initial_condition=None, u_exact=None):
+        """l2 and linf errors of the resident state against the exact solution
+        (the initial condition at time t on the analysis nodes, or u_exact)."""
+        if u_exact is None:
+            u_exact = self.exact_at_analysis_nodes(t, initial_condition)
+        u_exact = np.ascontiguousarray(u_exact, dtype=np.float64)
+        nv = self.equations.nvariables
+        l2 = np.zeros(self.nmembers * nv)
+        linf = np.zeros(self.nmembers * nv)
+        _lib.check(self._L.tag_analyze_errors(self._h, _ptr(u_exact), _ptr(l2), _ptr(linf)))
+        l2, linf = l2.reshape(self.nmembers, nv), linf.reshape(self.nmembers, nv)
+        return (l2[0], linf[0]) if self.nmembers == 1 else (l2, linf)
+
     def time_kernels(self, reps=10):
         a, b = ctypes.c_double(), ctypes.c_double()
         _lib.check(self._L.tag_time_kernels(self._h, int(reps), ctypes.byref(a), ctypes.byref(b)))
@@ -441,6 +500,14 @@ class SemidiscretizationEnsemble(SemidiscretizationHyperbolic):
 
     def member_slice(self, m):
         return slice(int(self.member_offsets[m]), int(self.member_offsets[m + 1]))
+
+    def exact_at_analysis_nodes(self, t=0.0, initial_condition=None):
+        m, x = self.analysis_nodes()
+        parts = []
+        for k, ic in enumerate(self.initial_conditions):
+            ic = initial_condition or ic
+            parts.append(ic(x[self.member_slice(k)], t, self.equations))
+        return np.ascontiguousarray(np.concatenate(parts), dtype=np.float64)
 
 
 def fp64_peak():
