@@ -298,6 +298,11 @@ def run_swe(args):
     except (OSError, KeyError, ValueError):
         hbm_peak, hbm_src = 6800.0, "fallback"
     gbs = by / (ms_el * 1e-3) / 1e9
+    fl = sum(6 * k * k * flops_per_node_covariant(N + 1, args.swe_variant) * (N + 1) ** 2
+             for k, N, _, _ in specs)
+    peak_fp64 = tg.fp64_peak()
+    achieved_tf = fl / (ms_el * 1e-3) / 1e12
+    traffic = TRAFFIC_PER_DOF.get("swe") if args.swe_variant == "weak" else None
     cpu = None
     if not args.no_cpu:
         orc = entry.load_oracle()
@@ -338,11 +343,17 @@ def run_swe(args):
                    "dofs": dofs, "elements": ens.nelements, "members": M,
                    "degree_runs": int(ens._H.nmembers), "build_seconds": t_build,
                    "l2": "inputs larger than L2 (u + k + packed metric data)"},
-        "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": gbs / hbm_peak, "traffic": None,
+        "roofline": {"bound": "fp64", "achieved": achieved_tf, "peak": peak_fp64 / 1e12,
+                     "unit": "TFLOP/s", "frac": achieved_tf / (peak_fp64 / 1e12),
+                     "traffic": (traffic * dofs) if traffic else None,
+                     "traffic_source": "ncu dram__bytes_read+write per DOF of a capture, "
+                                       "scaled by DOF" if traffic else None,
                      "kernel": "k_cov_element (volume + surface + Jacobian + sources + RK stage)",
-                     "peak_source": hbm_src, "ms_element": ms_el, "ms_interface": ms_if,
-                     "bytes_per_launch": by},
+                     "peak_source": "FP64 FMA probe in this run (tag_fp64_peak), of measured",
+                     "hbm_achieved_gbs": gbs, "hbm_peak_gbs": hbm_peak,
+                     "hbm_frac": gbs / hbm_peak, "hbm_peak_source": hbm_src,
+                     "ms_element": ms_el, "ms_interface": ms_if,
+                     "flops_per_launch": fl, "bytes_per_launch": by},
         "ensemble_vs_sequential": {"sequential_rate": seq_value, "speedup": value / seq_value},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                        "steps": len(lat)},
@@ -356,6 +367,20 @@ def run_swe(args):
         line["cpu_baseline"] = cpu
     print(json.dumps(line))
     ens.close()
+
+
+def flops_per_node_covariant(n, variant):
+    """FP64 flops per node of one covariant element-kernel launch, counted from
+    the reference formulas (covariant_shallow_water.jl, _split.jl) with a
+    division as one flop.  Weak form: both contravariant fluxes 23, the D_hat
+    contraction 12 n, the surface terms 24 / n, Jacobian and source sum 6, the
+    geometric + Coriolis source 49, the stage update 15.  Split EC form: per
+    direction flux_ec over the symmetric pairs 10 (n - 1) and the
+    nonconservative flux_ec over all n partners 26 n, per-node velocities 13,
+    surface 24 / n, Jacobian 10, the split source 67, the stage update 15."""
+    if variant == "weak":
+        return 93 + 12 * n + 24.0 / n
+    return 2 * (10 * (n - 1) + 26 * n) + 13 + 10 + 67 + 15 + 24.0 / n
 
 
 def flops_per_element_launch_3d(n, nelem):
@@ -695,7 +720,8 @@ def run_ours(args):
 # DRAM bytes per DOF of the element kernel from ncu captures (read + write),
 # used to report `traffic` for the full-size launch.
 TRAFFIC_PER_DOF = {"shell": 282.45,      # k_element3d, stage mode, full shell
-                   "ensemble": 205.27}    # k_element 2D, stage mode, 128-member ensemble
+                   "ensemble": 205.27,    # k_element 2D, stage mode, 128-member ensemble
+                   "swe": 214.71}         # k_cov_element weak form, 8 of the SWE members
 
 
 def main():

@@ -243,6 +243,24 @@ int tag_analysis_nodes(tag_handle h, int32_t* m, double* x);
  * src/callbacks_step/analysis_covariant.jl:143-189).  l2, linf: nmembers x nv. */
 int tag_analyze_errors(tag_handle h, const double* u_exact, double* l2, double* linf);
 
+/* Covariant metric terms of a cubed-sphere mesh, computed on the device
+ * (the reference's cache construction, init_auxiliary_node_variables!,
+ * src/solvers/dgsem_p4est/containers_2d_manifold_in_3d_covariant.jl:232-489,
+ * with the element-local mapping of src/meshes/p4est_cubed_sphere.jl).
+ * vertices [E][4][3]: each element's corners (counter-clockwise, outward
+ * normal); nodes [n]: dg.basis.nodes; derivative_matrix [n, n] column-major
+ * (dg.basis.derivative_matrix, needed when collocation != 0).  spherical != 0:
+ * GlobalSphericalCoordinates, else GlobalCartesianCoordinates; collocation
+ * != 0: ChristoffelSymbolsCollocationDerivative, else the exact derivatives
+ * (ChristoffelSymbolsAutodiff).  Outputs (host): aux [E][n][n][26] in the
+ * aux_node_vars order with the bottom topography (slot 19) set to 0 for the
+ * caller to fill, and the node coordinates xyz [E][n][n][3].  Returns
+ * TAG_E_INVALID when a metric term is not finite (spherical components at a
+ * pole). */
+int tag_cov_metric_terms(const double* vertices, int32_t nelements, int32_t polydeg, double radius,
+                         int32_t spherical, int32_t collocation, const double* nodes,
+                         const double* derivative_matrix, double* aux, double* xyz);
+
 /* Legendre-Gauss-Lobatto nodes and weights of degree polydeg on [-1, 1]
  * (Trixi's LobattoLegendreBasis(polydeg).nodes / .weights); host only. */
 int tag_lgl_basis(int32_t polydeg, double* nodes, double* weights);

@@ -1,0 +1,51 @@
+"""Covariant metric terms computed on the device (tag_cov_metric_terms)
+against the host NumPy construction of the same 26 auxiliary variables and
+node coordinates: Cartesian and spherical global components, exact (dual
+number) and collocation Christoffel symbols, degrees 1-7.  Tolerance: every
+slot within 1e-12 of its largest magnitude over the mesh (the Christoffel
+symbols, derivatives of the metric, within 1e-10 of the largest of them).  A pole node in spherical
+components is reported as an error, as on the host."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(tg, k, N, spherical, collocation, topo=None):
+    cv = tg.covariant
+    from trixiatmo_gb300.initial_conditions import EARTH_RADIUS
+    coords = cv.GlobalSphericalCoordinates() if spherical else cv.GlobalCartesianCoordinates()
+    eq = cv.CovariantShallowWaterEquations2D(9.80616, 7.292e-5, coords)
+    mesh = cv.P4estMeshCubedSphere2D(k, EARTH_RADIUS, polydeg=N)
+    basis = tg.LobattoLegendreBasis(N)
+    metric = cv.MetricTermsCovariantSphere(cv.ChristoffelSymbolsCollocationDerivative()
+                                           if collocation else cv.ChristoffelSymbolsAutodiff())
+    return cv, mesh, basis, eq, metric
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 5, 7])
+@pytest.mark.parametrize("spherical,collocation", [(False, False), (False, True), (True, False)])
+def test_device_metric_terms_match_host(tg, gpu_lib, N, spherical, collocation):
+    if spherical and N % 2 == 0:
+        # an even degree puts a node on a pole (the centre node of the middle
+        # element for odd k, element corners for even k)
+        pytest.skip("pole node in spherical components")
+    cv, mesh, basis, eq, metric = _setup(tg, 3, N, spherical, collocation)
+    topo = cv.bottom_topography_isolated_mountain
+    aux_h, xyz_h = cv.compute_aux_vars(mesh, basis, eq, metric, topo)
+    aux_d, xyz_d = cv.compute_aux_vars(mesh, basis, eq, metric, topo, device=True)
+    assert np.abs(xyz_d - xyz_h).max() <= 1e-12 * np.abs(xyz_h).max()
+    chris = np.abs(aux_h[..., 20:26]).max()
+    for s in range(26):
+        # the Christoffel symbols against the largest of them: some vanish
+        # analytically and are rounding noise of either construction
+        scale = chris if s >= 20 else max(np.abs(aux_h[..., s]).max(), 1e-300)
+        tol = 1e-10 if s >= 20 else 1e-12
+        err = np.abs(aux_d[..., s] - aux_h[..., s]).max()
+        assert err <= tol * scale, (s, err / scale)
+
+
+def test_device_metric_terms_report_pole_singularity(tg, gpu_lib):
+    cv, mesh, basis, eq, metric = _setup(tg, 3, 2, True, False)
+    with pytest.raises(Exception):
+        cv.compute_aux_vars(mesh, basis, eq, metric, None, device=True)

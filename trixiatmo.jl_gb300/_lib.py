@@ -122,6 +122,8 @@ SIGNATURES = {
     "tag_analysis_nodes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), _dp]),
     "tag_analyze_errors": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp]),
     "tag_lgl_basis": (ctypes.c_int, [ctypes.c_int32, _dp, _dp]),
+    "tag_cov_metric_terms": (ctypes.c_int, [_dp, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                            ctypes.c_int32, ctypes.c_int32, _dp, _dp, _dp, _dp]),
     "tag_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32),
                                   ctypes.c_int32]),
     "tag_stream": (ctypes.c_void_p, [ctypes.c_void_p]),

@@ -19,6 +19,7 @@ and uploaded by tag_create.
 """
 from __future__ import annotations
 
+import ctypes
 import math
 
 import numpy as np
@@ -158,18 +159,17 @@ class P4estMeshCubedSphere2D:
         self.polydeg = int(polydeg)
         k = self.k
         d = 2.0 / k
-        verts = np.empty((6 * k * k, 4, 3))
+        verts = np.empty((6, k, k, 4, 3))          # [face, cy, cx, corner, xyz]
+        c = np.arange(k, dtype=np.float64)
+        xo = (-1 + c * d + d / 2)[None, :]           # [1, cx]
+        yo = (-1 + c * d + d / 2)[:, None]           # [cy, 1]
         for direction in range(1, 7):
-            for cy in range(k):
-                for cx in range(k):
-                    e = cx + k * (cy + k * (direction - 1))
-                    xo = -1 + cx * d + d / 2
-                    yo = -1 + cy * d + d / 2
-                    for c, (sx, sy) in enumerate(((-1, -1), (1, -1), (1, 1), (-1, 1))):
-                        verts[e, c] = cubed_sphere_face_point(np.float64(xo + sx * d / 2),
-                                                              np.float64(yo + sy * d / 2),
-                                                              self.radius, direction)
-        self.vertices = verts
+            for corner, (sx, sy) in enumerate(((-1, -1), (1, -1), (1, 1), (-1, 1))):
+                xi = np.broadcast_to(xo + sx * d / 2, (k, k))
+                eta = np.broadcast_to(yo + sy * d / 2, (k, k))
+                verts[direction - 1, :, :, corner] = cubed_sphere_face_point(xi, eta, self.radius,
+                                                                             direction)
+        self.vertices = verts.reshape(6 * k * k, 4, 3)
 
     @property
     def nelements(self):
@@ -197,25 +197,22 @@ class P4estMeshCubedSphere2D:
         order = np.lexsort((q[:, 2], q[:, 1], q[:, 0]))
         flat = q[order]
         same = np.all(flat[1:] == flat[:-1], axis=1)
-        c = Connectivity()
-        paired = np.zeros(E * 4, dtype=bool)
-        for t in np.nonzero(same)[0]:
-            a, b = int(order[t]), int(order[t + 1])
-            if paired[a] or paired[b]:
-                continue
-            paired[a] = paired[b] = True
-            e0, f0 = divmod(a, 4)
-            e1, f1 = divmod(b, 4)
-            P, S = allf[e0, f0], allf[e1, f1]
-            fwd = np.abs(S - P).max()
-            bwd = np.abs(S[::-1] - P).max()
-            if min(fwd, bwd) > 1e-6 * scale:
-                raise RuntimeError("edges with equal midpoints do not match node by node")
-            c.if_elements.append((e0, e1))
-            c.if_faces.append((f0, f1))
-            c.if_flip.append(int(bwd < fwd))
-        if not paired.all():
+        t = np.nonzero(same)[0]
+        a, b = order[t], order[t + 1]
+        # every edge is shared by exactly two elements
+        if len(t) * 2 != E * 4 or np.unique(np.concatenate([a, b])).size != E * 4:
             raise RuntimeError("unmatched element edge on the cubed sphere")
+        e0, f0 = np.divmod(a, 4)
+        e1, f1 = np.divmod(b, 4)
+        P, S = allf[e0, f0], allf[e1, f1]              # [I, n, 3]
+        fwd = np.abs(S - P).max(axis=(1, 2))
+        bwd = np.abs(S[:, ::-1] - P).max(axis=(1, 2))
+        if (np.minimum(fwd, bwd) > 1e-6 * scale).any():
+            raise RuntimeError("edges with equal midpoints do not match node by node")
+        c = Connectivity()
+        c.if_elements = np.stack([e0, e1], axis=1)
+        c.if_faces = np.stack([f0, f1], axis=1)
+        c.if_flip = (bwd < fwd).astype(np.int32)
         return c
 
 
@@ -353,18 +350,44 @@ def _metric_covariant(A):
     return g11, g12, g22
 
 
-def compute_aux_vars(mesh, basis, equations, metric_terms=None, bottom_topography=None):
-    """aux[e, j, i, 26] of the reference's covariant cache
-    (containers_2d_manifold_in_3d_covariant.jl:247-295, 379-441, 455-490)."""
+def compute_aux_vars(mesh, basis, equations, metric_terms=None, bottom_topography=None,
+                     device=False):
+    """aux[e, j, i, 26] and node coordinates xyz[e, j, i, 3] of the reference's
+    covariant cache (containers_2d_manifold_in_3d_covariant.jl:247-295,
+    379-441, 455-490).  device=True computes them with tag_cov_metric_terms
+    on the GPU (what the semidiscretizations use); otherwise in NumPy on the
+    host."""
     metric_terms = metric_terms or MetricTermsCovariantSphere()
     spherical = isinstance(equations.global_coordinate_system, GlobalSphericalCoordinates)
     key = (basis.n, spherical, type(metric_terms.christoffel_symbols).__name__,
-           id(bottom_topography))
+           id(bottom_topography), bool(device))
     cache = mesh.__dict__.setdefault("_aux_cache", {})
     if key in cache:
         return cache[key]
-    cache[key] = _compute_aux_vars(mesh, basis, metric_terms, spherical, bottom_topography)
+    f = _compute_aux_vars_device if device else _compute_aux_vars
+    cache[key] = f(mesh, basis, metric_terms, spherical, bottom_topography)
     return cache[key]
+
+
+def _compute_aux_vars_device(mesh, basis, metric_terms, spherical, bottom_topography):
+    n, E = basis.n, mesh.nelements
+    collocation = isinstance(metric_terms.christoffel_symbols,
+                             ChristoffelSymbolsCollocationDerivative)
+    v = np.ascontiguousarray(mesh.vertices, dtype=np.float64)
+    x = np.ascontiguousarray(basis.nodes, dtype=np.float64)
+    D = np.asfortranarray(basis.derivative_matrix, dtype=np.float64)
+    aux = np.zeros((E, n, n, N_AUX))
+    xyz = np.zeros((E, n, n, 3))
+    dp = ctypes.POINTER(ctypes.c_double)
+    _lib.check(_lib.load().tag_cov_metric_terms(
+        v.ctypes.data_as(dp), E, n - 1, mesh.radius, int(spherical), int(collocation),
+        x.ctypes.data_as(dp), D.ctypes.data_as(dp), aux.ctypes.data_as(dp),
+        xyz.ctypes.data_as(dp)))
+    if bottom_topography is not None:
+        aux[..., 19] = bottom_topography(xyz)
+        if not np.isfinite(aux[..., 19]).all():
+            raise ValueError("the bottom topography is not finite at a node")
+    return aux, xyz
 
 
 def _compute_aux_vars(mesh, basis, metric_terms, spherical, bottom_topography):

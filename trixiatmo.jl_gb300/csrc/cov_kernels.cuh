@@ -306,7 +306,7 @@ TAG_DEV void cov_element_body(const CovParams& P, const CovGroup& G, int lblk,
   const bool act = el < ne;
   const int i = node % n, j = node / n;
   const long gq = G.node0 + (long)(el_first + el) * nn + node;
-  double ui[3];
+  double ui[3], ih = 0.0;  // ih = 1/h, shared by the fluxes and the source
   double* qn = q + threadIdx.x * kCovQ;
   const double* __restrict__ pg = pk + gq * kPack;  // re-read where needed (L1 hit)
   if (act) {
@@ -315,7 +315,7 @@ TAG_DEV void cov_element_body(const CovParams& P, const CovGroup& G, int lblk,
     double p[kPack];
 #pragma unroll
     for (int k = 0; k < kPack; ++k) p[k] = __ldg(pg + k);
-    const double ih = 1.0 / ui[0];
+    ih = 1.0 / ui[0];
     if (P.volume == 0) {
       cov_flux(P, ui, ih, p, 0, qn);
       cov_flux(P, ui, ih, p, 1, qn + 3);
@@ -412,7 +412,7 @@ TAG_DEV void cov_element_body(const CovParams& P, const CovGroup& G, int lblk,
       double p[kPack];
 #pragma unroll
       for (int k = 0; k < kPack; ++k) p[k] = __ldg(pg + k);
-      cov_source(P, ui, 1.0 / ui[0], p, s);
+      cov_source(P, ui, ih, p, s);
     }
     const double fac = -__ldg(pg + kPInvJ);
     const int e = G.e0 + el_first + el;

@@ -579,7 +579,8 @@ class _CovHandle:
         self.aux, self.xyz, self.ns, self.member_nelements = [], [], [], []
         for k, (mesh, solver, topo) in enumerate(members):
             basis = solver.basis
-            aux, xyz = cv.compute_aux_vars(mesh, basis, equations, metric_terms, topo)
+            aux, xyz = cv.compute_aux_vars(mesh, basis, equations, metric_terms, topo,
+                                           device=True)
             conn = mesh.connectivity(basis)
             ie, ifc, fl, _, _ = conn.arrays()
             vid, sid, vnc, snc = _cov_flux_ids(equations, solver)
