@@ -59,6 +59,7 @@ extern "C" {
 #define TAG_EQ_MOIST_EULER_2D 4  /* CompressibleMoistEulerEquations2D                             */
 #define TAG_EQ_COVARIANT_SWE 5   /* (Split)CovariantShallowWaterEquations2D on a 2D manifold     */
 #define TAG_EQ_POTENTIAL_TEMPERATURE_2D 6 /* CompressibleEulerPotentialTemperatureEquationsWithGravity2D */
+#define TAG_EQ_POTENTIAL_TEMPERATURE_3D 7 /* CompressibleEulerPotentialTemperatureEquationsWithGravity3D + source_terms_coriolis */
 
 #define TAG_VF_RANOCHA_WARUSZEWSKI 1 /* (flux_ranocha, flux_nonconservative_waruszewski_etal) */
 #define TAG_VF_EC_RAIN 2             /* VolumeIntegralFluxDifferencing(flux_ec_rain)    */

@@ -137,6 +137,23 @@ def lib():
         L.orc_rainy_newton_states.argtypes = [_dp, ctypes.c_long, ctypes.c_int, ctypes.c_double,
                                               ctypes.c_int, ctypes.c_int, _dp, _ip,
                                               ctypes.POINTER(ctypes.c_long)]
+        L.orc_pt3d_create.restype = ctypes.c_void_p
+        L.orc_pt3d_create.argtypes = ([ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int,
+                                       _ip, _ip, _ip, ctypes.c_int, _ip, _ip] +
+                                      [ctypes.c_double] * 5 + [ctypes.c_int] * 2)
+        L.orc_pt3d_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_pt3d_rhs.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double]
+        L.orc_pt3d_max_dt.restype = ctypes.c_double
+        L.orc_pt3d_max_dt.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_pt3d_ck_steps.restype = ctypes.c_double
+        L.orc_pt3d_ck_steps.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_int, ctypes.c_double]
+        L.orc_pt3d_ssp_steps.restype = ctypes.c_double
+        L.orc_pt3d_ssp_steps.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                         ctypes.c_double]
+        for name in ("orc_pt3d_pointwise", "orc_pt2d_pointwise"):
+            getattr(L, name).argtypes = [ctypes.c_int] * 3 + [ctypes.c_double, _dp, _dp, _dp, _dp]
         L.orc_rainy_ssp_steps.restype = ctypes.c_double
         L.orc_rainy_ssp_steps.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_double,
                                           ctypes.c_int, ctypes.c_int, ctypes.c_double,
@@ -271,6 +288,60 @@ class Euler3D:
     def ssp_steps(self, u, t, cfl, nsteps, scheme, fixed_dt=0.0, t_end=0.0):
         """SSPRK43 (scheme 1) or SSPRK33 (scheme 2) steps; returns the new time."""
         return lib().orc_euler3d_ssp_steps(self.h, _p(u), t, cfl, nsteps, scheme, fixed_dt, t_end)
+
+
+class PotTemp3D:
+    """Potential-temperature Euler with gravity in 3D (shell geometry and
+    connectivity are the host mirror's arrays).  volume 0 flux_tec, 1 flux_ec,
+    2 flux_etec; nc 0 waruszewski, 1 artiano, 2 souza."""
+
+    nv = 6
+
+    def __init__(self, polydeg, Ja, invJ, xyz, if_elements, if_faces, if_orient, bd_elements,
+                 bd_faces, c_p=1004.0, c_v=717.0, g=9.80616, c_lmars=340.0, omega=0.0,
+                 volume=0, nc=0):
+        self.n = polydeg + 1
+        self.nelem = invJ.shape[0]
+        self._keep = [np.ascontiguousarray(a) for a in (Ja, invJ, xyz)]
+        ints = [np.ascontiguousarray(a, dtype=np.int32) for a in
+                (if_elements, if_faces, if_orient, bd_elements, bd_faces)]
+        self._keep += ints
+        self.h = lib().orc_pt3d_create(polydeg, self.nelem, _p(self._keep[0]), _p(self._keep[1]),
+                                       _p(self._keep[2]), len(ints[2]), _ip(ints[0]),
+                                       _ip(ints[1]), _ip(ints[2]), len(ints[3]), _ip(ints[3]),
+                                       _ip(ints[4]), c_p, c_v, g, c_lmars, omega, volume, nc)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_pt3d_destroy(self.h)
+            self.h = None
+
+    def rhs(self, u, t=0.0):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        du = np.zeros_like(u)
+        lib().orc_pt3d_rhs(self.h, _p(u), _p(du), t)
+        return du
+
+    def max_dt(self, u):
+        return lib().orc_pt3d_max_dt(self.h, _p(np.ascontiguousarray(u)))
+
+    def ck_steps(self, u, k, t, cfl, nsteps, fixed_dt=0.0):
+        return lib().orc_pt3d_ck_steps(self.h, _p(u), _p(k), t, cfl, nsteps, fixed_dt)
+
+    def ssp_steps(self, u, t, cfl, nsteps, scheme, fixed_dt=0.0, t_end=0.0):
+        return lib().orc_pt3d_ssp_steps(self.h, _p(u), t, cfl, nsteps, scheme, fixed_dt, t_end)
+
+
+def pt_pointwise(ndims, kind, ul, ur, n, volume=0, nc=0, c=340.0):
+    """Pointwise potential-temperature fluxes (kind 0 flux, 1 volume flux,
+    2 nonconservative gravity term, 3 LMARS) of the 2D or 3D equations."""
+    nv = ndims + 3
+    f = np.zeros(nv)
+    fn = lib().orc_pt3d_pointwise if ndims == 3 else lib().orc_pt2d_pointwise
+    fn(kind, volume, nc, c, _p(np.ascontiguousarray(ul, dtype=np.float64)),
+       _p(np.ascontiguousarray(ur, dtype=np.float64)),
+       _p(np.ascontiguousarray(n, dtype=np.float64)), _p(f))
+    return f
 
 
 class CovSWE:

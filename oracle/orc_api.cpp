@@ -20,6 +20,7 @@
 #include "orc_euler_energy_3d.hpp"
 #include "orc_moist_2d.hpp"
 #include "orc_pt_2d.hpp"
+#include "orc_pt_3d.hpp"
 #include "orc_cov_swe.hpp"
 #include "orc_rainy_2d.hpp"
 #include "orc_time.hpp"
@@ -733,6 +734,144 @@ double orc_euler3d_ssp_steps(void* h, double* u, double t, double cfl, int nstep
   return ssp_steps([&](const double* uu, double* dd, double tt) { c->dg->rhs(uu, dd, tt); },
                    [&](const double* uu) { return c->dg->max_dt(uu); }, [](double*) {}, u,
                    c->ndofs() * 6, t, cfl, nsteps, scheme, fixed_dt, t_end);
+}
+
+// ---- 3D potential temperature with gravity ----------------------------------
+// CompressibleEulerPotentialTemperatureEquationsWithGravity3D: volume
+// (flux_tec | flux_ec | flux_etec, nonconservative gravity term), surface
+// (FluxLMARS(c), flux_zero), slip walls with the outward normal, Coriolis.
+struct PTPhys3D {
+  using State = PotTemp3D::State;
+  static constexpr int nv = 6;
+  static constexpr bool has_noncons = true;
+  static constexpr bool has_sources = true;
+  PotTemp3D eq;
+  double c_lmars = 340.0, omega = 0.0;
+  State volume_flux(const State& a, const State& b, const double* n) const {
+    return eq.volume_flux(a, b, n);
+  }
+  State volume_noncons(const State& a, const State& b, const double* n) const {
+    return eq.noncons(a, b, n);
+  }
+  State surface_flux(const State& a, const State& b, const double* n) const {
+    return eq.flux_lmars(a, b, n, c_lmars);
+  }
+  State surface_noncons(const State&, const State&, const double*) const { return State{}; }
+  State bc_normal(const State& ui, const double* n) const {
+    return eq.slip_wall_normal(ui, n, c_lmars);
+  }
+  State source(const State& u, const double*, double) const { return eq.coriolis(u, omega); }
+  void max_abs_speeds(const State& u, double* l) const { eq.max_abs_speeds(u, l); }
+};
+
+struct PT3DCase {
+  PTPhys3D phys;
+  Basis basis;
+  std::vector<double> Ja, invJ, xyz;
+  Mesh3D mesh;
+  std::unique_ptr<DG3D<PTPhys3D>> dg;
+  size_t ndofs() const { return (size_t)mesh.nelem * basis.n * basis.n * basis.n; }
+};
+
+void* orc_pt3d_create(int polydeg, int nelem, const double* Ja, const double* invJ,
+                      const double* xyz, int nif, const int* if_e, const int* if_f,
+                      const int* if_orient, int nbd, const int* bd_e, const int* bd_f, double c_p,
+                      double c_v, double g, double c_lmars, double omega, int volume, int nc) {
+  auto* c = new PT3DCase();
+  c->phys.eq.init(c_p, c_v, g);
+  c->phys.eq.volume = volume;
+  c->phys.eq.nc_kind = nc;
+  c->phys.c_lmars = c_lmars;
+  c->phys.omega = omega;
+  c->basis = make_lgl_basis(polydeg);
+  const int n = c->basis.n;
+  const size_t nodes = (size_t)nelem * n * n * n;
+  c->Ja.assign(Ja, Ja + nodes * 9);
+  c->invJ.assign(invJ, invJ + nodes);
+  if (xyz) c->xyz.assign(xyz, xyz + nodes * 3);
+  c->mesh.n = n;
+  c->mesh.nelem = nelem;
+  c->mesh.Ja = c->Ja.data();
+  c->mesh.invJ = c->invJ.data();
+  c->mesh.xyz = xyz ? c->xyz.data() : nullptr;
+  for (int k = 0; k < nif; ++k) {
+    c->mesh.if_e0.push_back(if_e[2 * k]);
+    c->mesh.if_e1.push_back(if_e[2 * k + 1]);
+    c->mesh.if_f0.push_back(if_f[2 * k]);
+    c->mesh.if_f1.push_back(if_f[2 * k + 1]);
+    c->mesh.if_orient.push_back(if_orient[k]);
+  }
+  for (int k = 0; k < nbd; ++k) {
+    c->mesh.bd_e.push_back(bd_e[k]);
+    c->mesh.bd_f.push_back(bd_f[k]);
+  }
+  c->dg.reset(new DG3D<PTPhys3D>(c->phys, c->basis, c->mesh));
+  return c;
+}
+
+void orc_pt3d_destroy(void* h) { delete static_cast<PT3DCase*>(h); }
+
+void orc_pt3d_rhs(void* h, const double* u, double* du, double t) {
+  static_cast<PT3DCase*>(h)->dg->rhs(u, du, t);
+}
+
+double orc_pt3d_max_dt(void* h, const double* u) {
+  return static_cast<PT3DCase*>(h)->dg->max_dt(u);
+}
+
+double orc_pt3d_ck_steps(void* h, double* u, double* k, double t, double cfl, int nsteps,
+                         double fixed_dt) {
+  auto* c = static_cast<PT3DCase*>(h);
+  const size_t N = c->ndofs() * 6;
+  std::vector<double> du(N);
+  for (int s = 0; s < nsteps; ++s) {
+    const double dt = fixed_dt > 0 ? fixed_dt : cfl * c->dg->max_dt(u);
+    ck2n54_step([&](const double* uu, double* dd, double tt) { c->dg->rhs(uu, dd, tt); }, u, k,
+                du.data(), N, t, dt);
+    t += dt;
+  }
+  return t;
+}
+
+double orc_pt3d_ssp_steps(void* h, double* u, double t, double cfl, int nsteps, int scheme,
+                          double fixed_dt, double t_end) {
+  auto* c = static_cast<PT3DCase*>(h);
+  return ssp_steps([&](const double* uu, double* dd, double tt) { c->dg->rhs(uu, dd, tt); },
+                   [&](const double* uu) { return c->dg->max_dt(uu); }, [](double*) {}, u,
+                   c->ndofs() * 6, t, cfl, nsteps, scheme, fixed_dt, t_end);
+}
+
+// pointwise 3D fluxes for the consistency tests: kind 0 flux, 1 volume flux
+// (tec / ec / etec by `volume`), 2 nonconservative term (by `nc`), 3 LMARS(c)
+void orc_pt3d_pointwise(int kind, int volume, int nc, double c, const double* ul,
+                        const double* ur, const double* n, double* f) {
+  PotTemp3D eq;
+  eq.init(1004.0, 717.0, 9.80616);
+  eq.volume = volume;
+  eq.nc_kind = nc;
+  PotTemp3D::State a, b;
+  for (int v = 0; v < 6; ++v) { a[v] = ul[v]; b[v] = ur[v]; }
+  PotTemp3D::State r = kind == 0 ? eq.flux(a, n)
+                     : kind == 1 ? eq.volume_flux(a, b, n)
+                     : kind == 2 ? eq.noncons(a, b, n)
+                                 : eq.flux_lmars(a, b, n, c);
+  for (int v = 0; v < 6; ++v) f[v] = r[v];
+}
+
+// the same for the 2D equations (5 variables)
+void orc_pt2d_pointwise(int kind, int volume, int nc, double c, const double* ul,
+                        const double* ur, const double* n, double* f) {
+  PotTemp2D eq;
+  eq.init(1004.0, 717.0, 9.80616);
+  eq.volume = volume;
+  eq.nc_kind = nc;
+  PotTemp2D::State a, b;
+  for (int v = 0; v < 5; ++v) { a[v] = ul[v]; b[v] = ur[v]; }
+  PotTemp2D::State r = kind == 0 ? eq.flux(a, n)
+                     : kind == 1 ? eq.volume_flux(a, b, n)
+                     : kind == 2 ? eq.noncons(a, b, n)
+                                 : eq.flux_lmars(a, b, n, c);
+  for (int v = 0; v < 5; ++v) f[v] = r[v];
 }
 
 // ---- 2D rainy Euler (flux_ec_rain / flux_lax_friedrichs, source_terms_rainy,

@@ -20,7 +20,8 @@ from .equations import (CompressibleEulerEnergyEquationsWithGravity2D,
                         CompressibleMoistEulerEquations2D, flux_chandrashekar,
                         source_terms_geopotential, source_terms_moist_bubble,
                         source_terms_convergence_test_dry, source_terms_convergence_test_moist,
-                        CompressibleEulerPotentialTemperatureEquationsWithGravity2D, flux_ec,
+                        CompressibleEulerPotentialTemperatureEquationsWithGravity2D,
+                        CompressibleEulerPotentialTemperatureEquationsWithGravity3D, flux_ec,
                         flux_tec, flux_etec, flux_nonconservative_artiano_etal,
                         flux_nonconservative_souza_etal)
 from .initial_conditions import (EARTH_GRAVITATIONAL_ACCELERATION, EARTH_RADIUS,
@@ -56,6 +57,7 @@ __all__ = [
     "initial_condition_convergence_test_dry", "initial_condition_convergence_test_moist",
     "P4estMesh", "covariant", "SemidiscretizationCovariant",
     "SemidiscretizationCovariantEnsemble",
-    "CompressibleEulerPotentialTemperatureEquationsWithGravity2D", "flux_ec", "flux_tec",
+    "CompressibleEulerPotentialTemperatureEquationsWithGravity2D",
+    "CompressibleEulerPotentialTemperatureEquationsWithGravity3D", "flux_ec", "flux_tec",
     "flux_etec", "flux_nonconservative_artiano_etal", "flux_nonconservative_souza_etal",
 ]

@@ -40,6 +40,7 @@ TAG_SRC_MOIST_CONVERGENCE_DRY = 5
 TAG_SRC_MOIST_CONVERGENCE = 6
 TAG_EQ_COVARIANT_SWE = 5
 TAG_EQ_POTENTIAL_TEMPERATURE_2D = 6
+TAG_EQ_POTENTIAL_TEMPERATURE_3D = 7
 TAG_VF_PT_TEC = 7
 TAG_VF_PT_EC = 8
 TAG_VF_PT_ETEC = 9

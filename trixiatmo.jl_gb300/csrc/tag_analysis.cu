@@ -9,6 +9,7 @@
 #include "phys_euler_energy_3d.cuh"
 #include "phys_moist_2d.cuh"
 #include "phys_pt_2d.cuh"
+#include "phys_pt_3d.cuh"
 #include "phys_rainy_2d.cuh"
 
 namespace tag {
@@ -97,6 +98,29 @@ struct An<PhysPT2D> {
     const double w1 = log(q.K * pow(u[3] / u[0], q.gamma)) - q.gamma;
     const double w4 = u[0] / u[3] * q.gamma;
     return w1 * du[0] + w4 * du[3];
+  }
+};
+
+// compressible_euler_potential_temperature_gravity_3d.jl: cons2entropy
+// :560-569, entropy :571-578, energy_total :593-603
+template <>
+struct An<PhysPT3D> {
+  using P = PhysPT3D::Params;
+  static constexpr int NV = 6;
+  static constexpr bool kEntropy = true, kEnergy = true;
+  TAG_DEV static double entropy(const P& q, const double* u, const double*) {
+    const double p = q.pt.K * pow(u[4], q.pt.gamma);
+    const double s = log(p) - q.pt.gamma * log(u[0]);
+    return -s * u[0] / (q.pt.gamma - 1.0);
+  }
+  TAG_DEV static double energy_total(const P& q, const double* u, const double*) {
+    const double p = q.pt.K * pow(u[4], q.pt.gamma);
+    return p / (q.pt.gamma - 1.0) + 0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0];
+  }
+  TAG_DEV static double dsdt(const P& q, const double* u, const double* du, const double*) {
+    const double w1 = log(q.pt.K * pow(u[4] / u[0], q.pt.gamma)) - q.pt.gamma;
+    const double w5 = u[0] / u[4] * q.pt.gamma;
+    return w1 * du[0] + w5 * du[4];
   }
 };
 
@@ -434,6 +458,8 @@ int dispatch_node_rows(const AnalysisArgs& a, const double* uex, int quantity, i
       return launch_node_rows<An<PhysPT2D>>(a, uex, quantity, nchunks, chunk, rows, s);
     case kAnCov:
       return launch_node_rows<An<PhysCovAn>>(a, uex, quantity, nchunks, chunk, rows, s);
+    case kAnPT3D:
+      return launch_node_rows<An<PhysPT3D>>(a, uex, quantity, nchunks, chunk, rows, s);
   }
   return TAG_E_INVALID;
 }
@@ -477,8 +503,8 @@ void legendre(int N, double x, double& L, double& dL) {
 }  // namespace
 
 int analysis_values(int phys, int quantity) {
-  static const int nv[] = {5, 6, 9, 6, 5, 3};
-  if (phys < 0 || phys > kAnCov) return -1;
+  static const int nv[] = {5, 6, 9, 6, 5, 3, 6};
+  if (phys < 0 || phys > kAnPT3D) return -1;
   switch (quantity) {
     case TAG_AQ_STATE: return nv[phys];
     case TAG_AQ_ENTROPY: return phys == kAnRainy2D ? -1 : 1;
@@ -516,6 +542,9 @@ int analysis_element_error_rows(int phys, int dim, int n, int m, int nelem, cons
                                                     rows, s);
     case kAnPT2D:
       return launch_element_errors<An<PhysPT2D>>(dim, n, m, nelem, u, invJ, V, wa, u_exact,
+                                                 rows, s);
+    case kAnPT3D:
+      return launch_element_errors<An<PhysPT3D>>(dim, n, m, nelem, u, invJ, V, wa, u_exact,
                                                  rows, s);
   }
   return TAG_E_INVALID;

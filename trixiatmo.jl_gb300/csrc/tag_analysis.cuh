@@ -18,7 +18,7 @@
 namespace tag {
 
 enum AnalysisPhys : int {
-  kAnEnergy2D = 0, kAnEnergy3D, kAnRainy2D, kAnMoist2D, kAnPT2D, kAnCov
+  kAnEnergy2D = 0, kAnEnergy3D, kAnRainy2D, kAnMoist2D, kAnPT2D, kAnCov, kAnPT3D
 };
 
 // One analysis call.  Node ranges of the members are [mbeg[m], mend[m])

@@ -17,6 +17,7 @@
 #include "phys_euler_energy_3d.cuh"
 #include "phys_moist_2d.cuh"
 #include "phys_pt_2d.cuh"
+#include "phys_pt_3d.cuh"
 #include "phys_rainy_2d.cuh"
 #include "tag_analysis.cuh"
 
@@ -63,6 +64,7 @@ struct tag_handle_s {
   PhysRainy2D::Params p_rainy{};
   PhysMoist2D::Params p_moist{};
   PhysPT2D::Params p_pt{};
+  PhysPT3D::Params p_pt3d{};
   // rainy: Newton stage limiter settings, MLP parameters, statistics counters
   bool has_limiter = false;
   int scheme = TAG_RK_CK2N54;  // time integrator of tag_rk_steps
@@ -142,6 +144,10 @@ const PhysMoist2D::Params& params_of<PhysMoist2D>(tag_handle h) {
 template <>
 const PhysPT2D::Params& params_of<PhysPT2D>(tag_handle h) {
   return h->p_pt;
+}
+template <>
+const PhysPT3D::Params& params_of<PhysPT3D>(tag_handle h) {
+  return h->p_pt3d;
 }
 
 template <class Phys, int n, int VOL = kVolFluxDiff>
@@ -728,7 +734,8 @@ const char* check_equations(const tag_config* cfg) {
         return "FluxLMARS needs a positive speed of sound";
       return nullptr;
     }
-    case TAG_EQ_POTENTIAL_TEMPERATURE_2D: {
+    case TAG_EQ_POTENTIAL_TEMPERATURE_2D:
+    case TAG_EQ_POTENTIAL_TEMPERATURE_3D: {
       if ((vf != TAG_VF_PT_TEC && vf != TAG_VF_PT_EC && vf != TAG_VF_PT_ETEC) || sf != TAG_SF_LMARS)
         return "unsupported flux combination for the potential-temperature equations";
       const double k = cfg->params[4];
@@ -747,7 +754,8 @@ bool boundary_kind_ok(int eq, int kind) {
     case TAG_EQ_MOIST_EULER_2D:
     case TAG_EQ_POTENTIAL_TEMPERATURE_2D:
       return kind == TAG_BC_SLIP_WALL_STRUCTURED || kind == TAG_BC_SLIP_WALL_NORMAL;
-    case TAG_EQ_EULER_ENERGY_3D: return kind == TAG_BC_SLIP_WALL_NORMAL;
+    case TAG_EQ_EULER_ENERGY_3D:
+    case TAG_EQ_POTENTIAL_TEMPERATURE_3D: return kind == TAG_BC_SLIP_WALL_NORMAL;
     case TAG_EQ_RAINY_2D: return kind == TAG_BC_SIMPLE_SLIP_WALL;
     default: return false;
   }
@@ -761,6 +769,7 @@ int analysis_phys(tag_handle h) {
     case TAG_EQ_RAINY_2D: return kAnRainy2D;
     case TAG_EQ_MOIST_EULER_2D: return kAnMoist2D;
     case TAG_EQ_POTENTIAL_TEMPERATURE_2D: return kAnPT2D;
+    case TAG_EQ_POTENTIAL_TEMPERATURE_3D: return kAnPT3D;
     default: return kAnCov;
   }
 }
@@ -772,6 +781,7 @@ const void* analysis_params(tag_handle h) {
     case TAG_EQ_RAINY_2D: return &h->p_rainy;
     case TAG_EQ_MOIST_EULER_2D: return &h->p_moist;
     case TAG_EQ_POTENTIAL_TEMPERATURE_2D: return &h->p_pt;
+    case TAG_EQ_POTENTIAL_TEMPERATURE_3D: return &h->p_pt3d;
     default: return &h->p_cov;
   }
 }
@@ -900,7 +910,8 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
   if (cfg->equations == TAG_EQ_COVARIANT_SWE) return create_cov(cfg, 1, out);
   const char* why = check_equations(cfg);
   if (why) return fail(TAG_E_INVALID, why);
-  const int dim = cfg->equations == TAG_EQ_EULER_ENERGY_3D ? 3 : 2;
+  const int dim = (cfg->equations == TAG_EQ_EULER_ENERGY_3D ||
+                   cfg->equations == TAG_EQ_POTENTIAL_TEMPERATURE_3D) ? 3 : 2;
   const int nface = 2 * dim;
   const bool rainy = cfg->equations == TAG_EQ_RAINY_2D;
   const bool moist = cfg->equations == TAG_EQ_MOIST_EULER_2D;
@@ -975,6 +986,14 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
     h->p_moist.surface = cfg->surface_flux;
     h->ops = cfg->volume_flux == TAG_VF_WEAK_FORM ? ops_for_n<PhysMoist2D, kVolWeak>(n)
                                                   : ops_for_n<PhysMoist2D, kVolFluxDiff>(n);
+  } else if (cfg->equations == TAG_EQ_POTENTIAL_TEMPERATURE_3D) {
+    h->nv = PhysPT3D::NV;
+    h->na = PhysPT3D::NA;
+    double pp[8];
+    for (int k = 0; k < 8; ++k) pp[k] = cfg->params[k];
+    pp[5] = cfg->volume_flux == TAG_VF_PT_TEC ? 0 : cfg->volume_flux == TAG_VF_PT_EC ? 1 : 2;
+    h->p_pt3d = PhysPT3D::make_params(pp);
+    h->ops = ops3d_for_n<PhysPT3D>(n);
   } else if (dim == 3) {
     h->nv = PhysEnergy3D::NV;
     h->na = PhysEnergy3D::NA;

@@ -76,6 +76,37 @@ class CompressibleEulerPotentialTemperatureEquationsWithGravity2D:
         return rho, u[..., 1] / rho, u[..., 2] / rho, self.K * u[..., 3] ** self.gamma, u[..., 4]
 
 
+class CompressibleEulerPotentialTemperatureEquationsWithGravity3D:
+    """State (rho, rho_v1, rho_v2, rho_v3, rho_theta, phi), p = K rho_theta^gamma
+    (src/equations/compressible_euler_potential_temperature_gravity_3d.jl:42-66)."""
+
+    nvariables = 6
+    ndims = 3
+    eq_id = _lib.TAG_EQ_POTENTIAL_TEMPERATURE_3D
+
+    def __init__(self, *, c_p, c_v, gravity):
+        self.c_p = float(c_p)
+        self.c_v = float(c_v)
+        self.g = float(gravity)
+        self.p_0 = 100000.0
+        self.R = self.c_p - self.c_v
+        self.gamma = self.c_p / self.c_v
+        self.inv_gamma_minus_one = 1.0 / (self.gamma - 1.0)
+        self.K = self.p_0 * (self.R / self.p_0) ** self.gamma
+
+    def prim2cons(self, rho, v1, v2, v3, p, phi):
+        """:535-543: rho_theta = (p / K)^(1 / gamma)."""
+        one = np.ones_like(p)
+        rho_theta = (p / self.K) ** (1 / self.gamma)
+        return np.stack([rho * one, rho * v1 * one, rho * v2 * one, rho * v3 * one,
+                         rho_theta * one, phi * one], axis=-1)
+
+    def cons2prim(self, u):
+        rho = u[..., 0]
+        return (rho, u[..., 1] / rho, u[..., 2] / rho, u[..., 3] / rho,
+                self.K * u[..., 4] ** self.gamma, u[..., 5])
+
+
 class CompressibleEulerEnergyEquationsWithGravity3D:
     """State (rho, rho_v1, rho_v2, rho_v3, rho_e, phi)
     (src/equations/compressible_euler_energy_with_gravity_3d.jl:45-65)."""

@@ -26,6 +26,7 @@ import numpy as np
 from . import _lib
 from .basis import LobattoLegendreBasis
 from .equations import (CompressibleEulerPotentialTemperatureEquationsWithGravity2D,
+                        CompressibleEulerPotentialTemperatureEquationsWithGravity3D,
                         flux_etec, flux_nonconservative_artiano_etal,
                         flux_nonconservative_souza_etal, flux_tec,
                         CompressibleEulerEnergyEquationsWithGravity2D,
@@ -111,7 +112,8 @@ def _flux_ids(equations, solver, source_terms=None):
             raise ValueError(f"{source_terms} is not a source of the moist equations")
         eq = equations
         return vid, sid, [eq.c_pd, eq.c_vd, eq.c_pv, eq.c_vv, eq.g, c_lmars, float(src)]
-    if isinstance(equations, CompressibleEulerPotentialTemperatureEquationsWithGravity2D):
+    if isinstance(equations, (CompressibleEulerPotentialTemperatureEquationsWithGravity2D,
+                              CompressibleEulerPotentialTemperatureEquationsWithGravity3D)):
         from .equations import flux_ec
         if not isinstance(vf, tuple):
             raise ValueError("volume flux must be (flux_tec | flux_ec | flux_etec, a "
@@ -125,10 +127,15 @@ def _flux_ids(equations, solver, source_terms=None):
             raise ValueError(f"unsupported potential-temperature volume flux {vf}")
         if not (isinstance(sf, tuple) and isinstance(sf[0], FluxLMARS) and sf[1] is flux_zero):
             raise ValueError("surface flux must be (FluxLMARS(c), flux_zero)")
+        params = [equations.c_p, equations.c_v, equations.g, sf[0].speed_of_sound, float(nc)]
+        if equations.ndims == 3:
+            if source_terms not in (None, source_terms_coriolis):
+                raise ValueError(f"unsupported source terms {source_terms}")
+            omega = EARTH_ROTATION_RATE if source_terms is source_terms_coriolis else 0.0
+            return vid, _lib.TAG_SF_LMARS, params + [0.0, omega]
         if source_terms is not None:
             raise ValueError("source terms are not supported for this equation set")
-        return vid, _lib.TAG_SF_LMARS, [equations.c_p, equations.c_v, equations.g,
-                                        sf[0].speed_of_sound, float(nc)]
+        return vid, _lib.TAG_SF_LMARS, params
     if isinstance(equations, CompressibleEulerEnergyEquationsWithGravity3D):
         if not (isinstance(vf, tuple) and vf[0] is flux_ranocha
                 and vf[1] is flux_nonconservative_waruszewski_etal):
