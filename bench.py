@@ -527,6 +527,24 @@ def cpu_oracle_rate_shell(steps):
     return invJ.size * 5 * steps / el, threads, el
 
 
+def max_over_ranks(x, world, device="cuda"):
+    """Largest value of x over all ranks (x itself on one rank): the timing
+    rule of the replicas-only multi-GPU run."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(world, dofs, stages, seconds):
+    """Whole-job DOF·stage/s of `world` replicas that each advanced `dofs`
+    by `stages` stages, timed by the slowest rank."""
+    return world * dofs * stages / seconds
+
+
 def dist_init():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -619,12 +637,10 @@ def run_ours(args):
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
     clock_info = clocks.stop()
+    ms = max_over_ranks(ms, world)
     if world > 1:
-        tt = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         torch.distributed.barrier()
-        ms = float(tt.item())
-    value = world * dofs * 5 * args.steps / (ms * 1e-3)
+    value = replica_rate(world, dofs, 5 * args.steps, ms * 1e-3)
     status = semi.status()
 
     # kernel timing for the roofline (same stream, CUDA events, stage mode)
@@ -657,12 +673,8 @@ def run_ours(args):
         semi.set_state(u_pin)
         t_e = semi.rk_steps(1, cfl=1.0, t=t_e)
         semi.get_state(u_pin)
-    el = time.perf_counter() - t0
-    if world > 1:
-        tt = torch.tensor([el], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        el = float(tt.item())
-    e2e = world * dofs * 5 * e2e_steps / el
+    el = max_over_ranks(time.perf_counter() - t0, world)
+    e2e = replica_rate(world, dofs, 5 * e2e_steps, el)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
