@@ -152,6 +152,8 @@ def test_error_norms_reproduce_energy_golden(tg, orc, analysis, gpu_lib):
     assert _norms_close(linf, linfo, u), (linf, linfo)
     m, x = semi.analysis_nodes()
     assert m == 7 and x.shape == (480, 7, 7, 2)
+    xh = semi.analysis_coordinates_host()
+    assert np.abs(x - xh).max() <= 1e-14 * np.abs(xh).max()
     semi.close()
 
 
@@ -169,6 +171,9 @@ def test_error_norms_3d_match_oracle(tg, orc, analysis, gpu_lib):
         lambda x: tg.initial_condition_baroclinic_instability(x, 0.0, eq), 3)
     assert _norms_close(l2, l2o, u), (l2, l2o)
     assert _norms_close(linf, linfo, u), (linf, linfo)
+    m, x = semi.analysis_nodes()  # device interpolation of the coordinates
+    xh = semi.analysis_coordinates_host()
+    assert m == 7 and np.abs(x - xh).max() <= 1e-14 * np.abs(xh).max()
     semi.close()
 
 

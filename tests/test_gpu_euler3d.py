@@ -110,4 +110,7 @@ def test_gpu_reproduces_reference_golden_3d(tg, orc, gpu_lib):
         ug, semi.node_coordinates, semi.inverse_jacobian, solver_basis(semi).nodes,
         lambda x: tg.initial_condition_baroclinic_instability(x, 0.0, eq), 3)
     check_golden(l2, linf)
+    # and with the error norms computed on the device (tag_analyze_errors)
+    l2d, linfd = semi.calc_error_norms(0.0)
+    check_golden(l2d, linfd)
     semi.close()
