@@ -60,6 +60,7 @@ extern "C" {
 #define TAG_EQ_COVARIANT_SWE 5   /* (Split)CovariantShallowWaterEquations2D on a 2D manifold     */
 #define TAG_EQ_POTENTIAL_TEMPERATURE_2D 6 /* CompressibleEulerPotentialTemperatureEquationsWithGravity2D */
 #define TAG_EQ_POTENTIAL_TEMPERATURE_3D 7 /* CompressibleEulerPotentialTemperatureEquationsWithGravity3D + source_terms_coriolis */
+#define TAG_EQ_INTERNAL_ENERGY_2D 8 /* CompressibleEulerInternalEnergyEquationsWithGravity2D */
 
 #define TAG_VF_RANOCHA_WARUSZEWSKI 1 /* (flux_ranocha, flux_nonconservative_waruszewski_etal) */
 #define TAG_VF_EC_RAIN 2             /* VolumeIntegralFluxDifferencing(flux_ec_rain)    */
@@ -70,12 +71,14 @@ extern "C" {
 #define TAG_VF_PT_TEC 7              /* potential temperature: (flux_tec, nonconservative gravity term) */
 #define TAG_VF_PT_EC 8               /* potential temperature: (flux_ec, nonconservative gravity term)  */
 #define TAG_VF_PT_ETEC 9             /* potential temperature: (flux_etec, nonconservative gravity term) */
+#define TAG_VF_IE_ETEC 10            /* internal energy: (flux_conservative_etec, flux_nonconservative_etec) */
 #define TAG_SF_LMARS 1               /* (FluxLMARS(c), flux_zero)                       */
 #define TAG_SF_LAX_FRIEDRICHS 2      /* flux_lax_friedrichs (max_abs_speed_naive)       */
 #define TAG_SF_CHANDRASHEKAR 3       /* flux_chandrashekar as surface flux (moist)      */
 #define TAG_SF_COV_EC 4              /* covariant: flux_ec                              */
 #define TAG_SF_COV_EC_LLF 5          /* covariant: FluxPlusDissipation(flux_ec, DissipationLocalLaxFriedrichs()) */
 #define TAG_SF_COV_CENTRAL 6         /* covariant: flux_central (no dissipation)        */
+#define TAG_SF_IE_ES 7               /* internal energy: (flux_conservative_es, flux_nonconservative_es) */
 
 #define TAG_SRC_RAINY 1              /* source_terms_rainy (microphysics + gravity)     */
 #define TAG_SRC_RAINY_CONVERGENCE 2  /* manufactured source of the rainy convergence test */

@@ -154,6 +154,18 @@ def lib():
                                          ctypes.c_double]
         for name in ("orc_pt3d_pointwise", "orc_pt2d_pointwise"):
             getattr(L, name).argtypes = [ctypes.c_int] * 3 + [ctypes.c_double, _dp, _dp, _dp, _dp]
+        L.orc_ie_create.restype = ctypes.c_void_p
+        L.orc_ie_create.argtypes = ([ctypes.c_int] * 3 + [ctypes.c_double] * 4 +
+                                    [ctypes.c_int] * 2 + [ctypes.c_double] * 3 + [ctypes.c_int])
+        L.orc_ie_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_ie_rhs.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double]
+        L.orc_ie_max_dt.restype = ctypes.c_double
+        L.orc_ie_max_dt.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_ie_ssp_steps.restype = ctypes.c_double
+        L.orc_ie_ssp_steps.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                       ctypes.c_double]
+        L.orc_ie_pointwise.argtypes = [ctypes.c_int, _dp, _dp, _dp, _dp]
         L.orc_rainy_ssp_steps.restype = ctypes.c_double
         L.orc_rainy_ssp_steps.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_double,
                                           ctypes.c_int, ctypes.c_int, ctypes.c_double,
@@ -341,6 +353,48 @@ def pt_pointwise(ndims, kind, ul, ur, n, volume=0, nc=0, c=340.0):
     fn(kind, volume, nc, c, _p(np.ascontiguousarray(ul, dtype=np.float64)),
        _p(np.ascontiguousarray(ur, dtype=np.float64)),
        _p(np.ascontiguousarray(n, dtype=np.float64)), _p(f))
+    return f
+
+
+class InternalEnergy2D:
+    """Internal-energy Euler with gravity on a rectangle with outward-normal
+    slip walls: (flux_conservative_etec, flux_nonconservative_etec) volume,
+    (flux_conservative_es, flux_nonconservative_es) surface flux."""
+
+    nv = 5
+
+    def __init__(self, polydeg, nx, ny, x0, x1, y0, y1, periodic_x=True, periodic_y=False,
+                 c_p=1004.0, c_v=717.0, g=9.81, surface_etec=False):
+        self.n = polydeg + 1
+        self.nelem = nx * ny
+        self.h = lib().orc_ie_create(polydeg, nx, ny, x0, x1, y0, y1, int(periodic_x),
+                                     int(periodic_y), c_p, c_v, g, int(surface_etec))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_ie_destroy(self.h)
+            self.h = None
+
+    def rhs(self, u, t=0.0):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        du = np.zeros_like(u)
+        lib().orc_ie_rhs(self.h, _p(u), _p(du), t)
+        return du
+
+    def max_dt(self, u):
+        return lib().orc_ie_max_dt(self.h, _p(np.ascontiguousarray(u)))
+
+    def ssp_steps(self, u, t, cfl, nsteps, scheme, fixed_dt=0.0, t_end=0.0):
+        return lib().orc_ie_ssp_steps(self.h, _p(u), t, cfl, nsteps, scheme, fixed_dt, t_end)
+
+
+def ie_pointwise(kind, ul, ur, n):
+    """kind 0 flux, 1 flux_conservative_etec, 2 flux_nonconservative_etec,
+    3 flux_conservative_es, 4 flux_nonconservative_es."""
+    f = np.zeros(5)
+    lib().orc_ie_pointwise(kind, _p(np.ascontiguousarray(ul, dtype=np.float64)),
+                           _p(np.ascontiguousarray(ur, dtype=np.float64)),
+                           _p(np.ascontiguousarray(n, dtype=np.float64)), _p(f))
     return f
 
 

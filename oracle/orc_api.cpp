@@ -21,6 +21,7 @@
 #include "orc_moist_2d.hpp"
 #include "orc_pt_2d.hpp"
 #include "orc_pt_3d.hpp"
+#include "orc_ie_2d.hpp"
 #include "orc_cov_swe.hpp"
 #include "orc_rainy_2d.hpp"
 #include "orc_time.hpp"
@@ -1032,6 +1033,93 @@ double orc_rainy_ck_steps(void* h, double* u, double* k, double t, double cfl, i
     t += dt;
   }
   return t;
+}
+
+// ---- 2D internal energy with gravity ------------------------------------------
+// CompressibleEulerInternalEnergyEquationsWithGravity2D: volume
+// (flux_conservative_etec, flux_nonconservative_etec), surface
+// (flux_conservative_es, flux_nonconservative_es), slip walls with the
+// outward normal (the reference's P4estMesh elixir).
+struct IEPhys {
+  using State = InternalEnergy2D::State;
+  static constexpr int nv = 5;
+  static constexpr bool has_noncons = true;
+  static constexpr bool has_sources = false;
+  InternalEnergy2D eq;
+  State flux(const State& u, const double* n) const { return eq.flux(u, n); }
+  State volume_flux(const State& a, const State& b, const double* n) const {
+    return eq.flux_etec(a, b, n);
+  }
+  State volume_noncons(const State& a, const State& b, const double* n) const {
+    return eq.noncons_etec(a, b, n);
+  }
+  int surface = 0;  // 0: the es pair (the elixir's), 1: the etec pair (entropy conservative)
+  State surface_flux(const State& a, const State& b, const double* n) const {
+    return surface ? eq.flux_etec(a, b, n) : eq.flux_es(a, b, n);
+  }
+  State surface_noncons(const State& a, const State& b, const double* n) const {
+    return surface ? eq.noncons_etec(a, b, n) : eq.noncons_es(a, b, n);
+  }
+  State bc_structured(const State& ui, const double* n, int) const {
+    return eq.slip_wall_normal(ui, n);
+  }
+  State bc_normal(const State& ui, const double* n) const { return eq.slip_wall_normal(ui, n); }
+  State source(const State&, const double*, double) const { return State{}; }
+  void max_abs_speeds(const State& u, double& l1, double& l2) const {
+    eq.max_abs_speeds(u, l1, l2);
+  }
+};
+
+struct IECase {
+  IEPhys phys;
+  Basis basis;
+  Mesh2D mesh;
+  std::unique_ptr<DG2D<IEPhys>> dg;
+  size_t ndofs() const { return (size_t)mesh.nelem * basis.n * basis.n; }
+};
+
+void* orc_ie_create(int polydeg, int nx, int ny, double x0, double x1, double y0, double y1,
+                    int periodic_x, int periodic_y, double c_p, double c_v, double g,
+                    int surface) {
+  auto* c = new IECase();
+  c->phys.eq.init(c_p, c_v, g);
+  c->phys.surface = surface;
+  c->basis = make_lgl_basis(polydeg);
+  c->mesh = structured_rectangle(c->basis, nx, ny, x0, x1, y0, y1, periodic_x != 0,
+                                 periodic_y != 0, 2);
+  c->dg.reset(new DG2D<IEPhys>(c->phys, c->basis, c->mesh));
+  return c;
+}
+
+void orc_ie_destroy(void* h) { delete static_cast<IECase*>(h); }
+
+void orc_ie_rhs(void* h, const double* u, double* du, double t) {
+  static_cast<IECase*>(h)->dg->rhs(u, du, t);
+}
+
+double orc_ie_max_dt(void* h, const double* u) { return static_cast<IECase*>(h)->dg->max_dt(u); }
+
+double orc_ie_ssp_steps(void* h, double* u, double t, double cfl, int nsteps, int scheme,
+                        double fixed_dt, double t_end) {
+  auto* c = static_cast<IECase*>(h);
+  return ssp_steps([&](const double* uu, double* dd, double tt) { c->dg->rhs(uu, dd, tt); },
+                   [&](const double* uu) { return c->dg->max_dt(uu); }, [](double*) {}, u,
+                   c->ndofs() * 5, t, cfl, nsteps, scheme, fixed_dt, t_end);
+}
+
+// pointwise fluxes for the consistency tests: kind 0 flux, 1 conservative
+// etec, 2 nonconservative etec, 3 conservative es, 4 nonconservative es
+void orc_ie_pointwise(int kind, const double* ul, const double* ur, const double* n, double* f) {
+  InternalEnergy2D eq;
+  eq.init(1004.0, 717.0, 9.81);
+  InternalEnergy2D::State a, b;
+  for (int v = 0; v < 5; ++v) { a[v] = ul[v]; b[v] = ur[v]; }
+  const InternalEnergy2D::State r = kind == 0 ? eq.flux(a, n)
+                                  : kind == 1 ? eq.flux_etec(a, b, n)
+                                  : kind == 2 ? eq.noncons_etec(a, b, n)
+                                  : kind == 3 ? eq.flux_es(a, b, n)
+                                              : eq.noncons_es(a, b, n);
+  for (int v = 0; v < 5; ++v) f[v] = r[v];
 }
 
 // SSPRK43 / SSPRK33 steps with the Newton stage limiter after every stage.

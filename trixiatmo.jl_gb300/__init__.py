@@ -21,7 +21,10 @@ from .equations import (CompressibleEulerEnergyEquationsWithGravity2D,
                         source_terms_geopotential, source_terms_moist_bubble,
                         source_terms_convergence_test_dry, source_terms_convergence_test_moist,
                         CompressibleEulerPotentialTemperatureEquationsWithGravity2D,
-                        CompressibleEulerPotentialTemperatureEquationsWithGravity3D, flux_ec,
+                        CompressibleEulerPotentialTemperatureEquationsWithGravity3D,
+                        CompressibleEulerInternalEnergyEquationsWithGravity2D,
+                        flux_conservative_etec, flux_nonconservative_etec,
+                        flux_conservative_es, flux_nonconservative_es, flux_ec,
                         flux_tec, flux_etec, flux_nonconservative_artiano_etal,
                         flux_nonconservative_souza_etal)
 from .initial_conditions import (EARTH_GRAVITATIONAL_ACCELERATION, EARTH_RADIUS,
@@ -58,6 +61,9 @@ __all__ = [
     "P4estMesh", "covariant", "SemidiscretizationCovariant",
     "SemidiscretizationCovariantEnsemble",
     "CompressibleEulerPotentialTemperatureEquationsWithGravity2D",
-    "CompressibleEulerPotentialTemperatureEquationsWithGravity3D", "flux_ec", "flux_tec",
+    "CompressibleEulerPotentialTemperatureEquationsWithGravity3D",
+    "CompressibleEulerInternalEnergyEquationsWithGravity2D", "flux_conservative_etec",
+    "flux_nonconservative_etec", "flux_conservative_es", "flux_nonconservative_es",
+    "flux_ec", "flux_tec",
     "flux_etec", "flux_nonconservative_artiano_etal", "flux_nonconservative_souza_etal",
 ]

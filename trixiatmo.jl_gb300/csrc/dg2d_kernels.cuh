@@ -100,10 +100,23 @@ __global__ void __launch_bounds__(256) k_interface(
     Phys::surface_flux(P, ul, ur, n1, n2, F);
     double* s0 = sfv + (((size_t)e0 * 4 + f0) * n + l) * NA;
     double* s1 = sfv + (((size_t)e1 * 4 + f1) * n + l1) * NA;
+    if constexpr (Phys::kSurfaceNoncons) {
+      // nonconservative surface terms, each side with its own state first:
+      // primary F + G(ul, ur)/2, secondary -(F + G(ur, ul)/2)
+      double G0[NA], G1[NA];
+      Phys::surface_noncons(P, ul, ur, n1, n2, G0);
+      Phys::surface_noncons(P, ur, ul, n1, n2, G1);
 #pragma unroll
-    for (int v = 0; v < NA; ++v) {
-      s0[v] = F[v];
-      s1[v] = -F[v];
+      for (int v = 0; v < NA; ++v) {
+        s0[v] = F[v] + 0.5 * G0[v];
+        s1[v] = -(F[v] + 0.5 * G1[v]);
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < NA; ++v) {
+        s0[v] = F[v];
+        s1[v] = -F[v];
+      }
     }
     return;
   }

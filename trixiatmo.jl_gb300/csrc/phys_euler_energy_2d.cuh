@@ -16,6 +16,7 @@ struct PhysEnergy2D {
   static constexpr int kRho = 0, kBeta = 5, kLogRho = 6, kLogBeta = 7;
   static constexpr bool kNodeLogs = false;  // 2D elements rarely leave the series range
   static constexpr bool kHasSources = false;
+  static constexpr bool kSurfaceNoncons = false;  // surface flux only (flux_zero)
 
   struct Params {
     double gamma, gm1, inv_gm1, c_lmars, inv_2c;

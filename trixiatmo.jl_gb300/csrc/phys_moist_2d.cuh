@@ -15,6 +15,7 @@ struct PhysMoist2D {
   static constexpr int kRho = 0, kBeta = 0, kLogRho = 0, kLogBeta = 0;
   static constexpr bool kNodeLogs = false;
   static constexpr bool kHasSources = true;
+  static constexpr bool kSurfaceNoncons = false;  // surface flux only (flux_zero)
 
   struct Params {
     double c_pd, c_vd, c_pv, c_vv, c_pl, R_d, R_v, L_00, g, c_lmars;

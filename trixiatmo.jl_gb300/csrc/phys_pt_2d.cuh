@@ -24,6 +24,7 @@ struct PhysPT2D {
   static constexpr int kRho = 0, kBeta = 0, kLogRho = 0, kLogBeta = 0;
   static constexpr bool kNodeLogs = false;
   static constexpr bool kHasSources = false;
+  static constexpr bool kSurfaceNoncons = false;  // surface flux only (flux_zero)
 
   struct Params {
     double gamma, K, c_lmars, stol_fac;  // stol_fac = (gamma - 1) / gamma

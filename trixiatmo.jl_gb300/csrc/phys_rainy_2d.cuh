@@ -53,6 +53,7 @@ struct PhysRainy2D {
   static constexpr int kRho = 0, kBeta = 0, kLogRho = 0, kLogBeta = 0;
   static constexpr bool kNodeLogs = false;
   static constexpr bool kHasSources = true;
+  static constexpr bool kSurfaceNoncons = false;  // surface flux only (flux_zero)
 
   struct Params {
     int source_kind;  // TAG_SRC_RAINY or TAG_SRC_RAINY_CONVERGENCE

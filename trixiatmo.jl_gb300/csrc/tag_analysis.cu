@@ -10,6 +10,7 @@
 #include "phys_moist_2d.cuh"
 #include "phys_pt_2d.cuh"
 #include "phys_pt_3d.cuh"
+#include "phys_ie_2d.cuh"
 #include "phys_rainy_2d.cuh"
 
 namespace tag {
@@ -121,6 +122,26 @@ struct An<PhysPT3D> {
     const double w1 = log(q.pt.K * pow(u[4] / u[0], q.pt.gamma)) - q.pt.gamma;
     const double w5 = u[0] / u[4] * q.pt.gamma;
     return w1 * du[0] + w5 * du[4];
+  }
+};
+
+// compressible_euler_internal_energy_with_gravity_2d.jl: cons2entropy
+// :271-280 and entropy :282-289 as defined there (no energy_total)
+template <>
+struct An<PhysIE2D> {
+  using P = PhysIE2D::Params;
+  static constexpr int NV = 5;
+  static constexpr bool kEntropy = true, kEnergy = false;
+  TAG_DEV static double entropy(const P& q, const double* u, const double*) {
+    const double p = q.gm1 * u[3];
+    const double s = log(p) - q.gamma * log(u[0]);
+    return -s * u[0] / q.gm1;
+  }
+  TAG_DEV static double energy_total(const P&, const double*, const double*) { return 0.0; }
+  TAG_DEV static double dsdt(const P& q, const double* u, const double* du, const double*) {
+    const double w1 = log(u[3] * q.gm1 / pow(u[0], q.gamma)) - q.gamma;
+    const double w4 = u[0] / (u[3] * q.gm1);
+    return w1 * du[0] + w4 * du[3];
   }
 };
 
@@ -460,6 +481,8 @@ int dispatch_node_rows(const AnalysisArgs& a, const double* uex, int quantity, i
       return launch_node_rows<An<PhysCovAn>>(a, uex, quantity, nchunks, chunk, rows, s);
     case kAnPT3D:
       return launch_node_rows<An<PhysPT3D>>(a, uex, quantity, nchunks, chunk, rows, s);
+    case kAnIE2D:
+      return launch_node_rows<An<PhysIE2D>>(a, uex, quantity, nchunks, chunk, rows, s);
   }
   return TAG_E_INVALID;
 }
@@ -503,12 +526,13 @@ void legendre(int N, double x, double& L, double& dL) {
 }  // namespace
 
 int analysis_values(int phys, int quantity) {
-  static const int nv[] = {5, 6, 9, 6, 5, 3, 6};
-  if (phys < 0 || phys > kAnPT3D) return -1;
+  static const int nv[] = {5, 6, 9, 6, 5, 3, 6, 5};
+  if (phys < 0 || phys > kAnIE2D) return -1;
   switch (quantity) {
     case TAG_AQ_STATE: return nv[phys];
     case TAG_AQ_ENTROPY: return phys == kAnRainy2D ? -1 : 1;
-    case TAG_AQ_ENERGY_TOTAL: return (phys == kAnRainy2D || phys == kAnCov) ? -1 : 1;
+    case TAG_AQ_ENERGY_TOTAL:
+      return (phys == kAnRainy2D || phys == kAnCov || phys == kAnIE2D) ? -1 : 1;
     case TAG_AQ_ENTROPY_TIMEDERIVATIVE: return 1;
   }
   return -1;
@@ -545,6 +569,9 @@ int analysis_element_error_rows(int phys, int dim, int n, int m, int nelem, cons
                                                  rows, s);
     case kAnPT3D:
       return launch_element_errors<An<PhysPT3D>>(dim, n, m, nelem, u, invJ, V, wa, u_exact,
+                                                 rows, s);
+    case kAnIE2D:
+      return launch_element_errors<An<PhysIE2D>>(dim, n, m, nelem, u, invJ, V, wa, u_exact,
                                                  rows, s);
   }
   return TAG_E_INVALID;

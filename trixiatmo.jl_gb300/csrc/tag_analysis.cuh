@@ -18,7 +18,8 @@
 namespace tag {
 
 enum AnalysisPhys : int {
-  kAnEnergy2D = 0, kAnEnergy3D, kAnRainy2D, kAnMoist2D, kAnPT2D, kAnCov, kAnPT3D
+  kAnEnergy2D = 0, kAnEnergy3D, kAnRainy2D, kAnMoist2D, kAnPT2D, kAnCov, kAnPT3D,
+  kAnIE2D
 };
 
 // One analysis call.  Node ranges of the members are [mbeg[m], mend[m])

@@ -18,6 +18,7 @@
 #include "phys_moist_2d.cuh"
 #include "phys_pt_2d.cuh"
 #include "phys_pt_3d.cuh"
+#include "phys_ie_2d.cuh"
 #include "phys_rainy_2d.cuh"
 #include "tag_analysis.cuh"
 
@@ -65,6 +66,7 @@ struct tag_handle_s {
   PhysMoist2D::Params p_moist{};
   PhysPT2D::Params p_pt{};
   PhysPT3D::Params p_pt3d{};
+  PhysIE2D::Params p_ie{};
   // rainy: Newton stage limiter settings, MLP parameters, statistics counters
   bool has_limiter = false;
   int scheme = TAG_RK_CK2N54;  // time integrator of tag_rk_steps
@@ -148,6 +150,10 @@ const PhysPT2D::Params& params_of<PhysPT2D>(tag_handle h) {
 template <>
 const PhysPT3D::Params& params_of<PhysPT3D>(tag_handle h) {
   return h->p_pt3d;
+}
+template <>
+const PhysIE2D::Params& params_of<PhysIE2D>(tag_handle h) {
+  return h->p_ie;
 }
 
 template <class Phys, int n, int VOL = kVolFluxDiff>
@@ -743,6 +749,10 @@ const char* check_equations(const tag_config* cfg) {
       if (!(cfg->params[3] > 0.0)) return "FluxLMARS needs a positive speed of sound";
       return nullptr;
     }
+    case TAG_EQ_INTERNAL_ENERGY_2D:
+      if (vf != TAG_VF_IE_ETEC || sf != TAG_SF_IE_ES)
+        return "unsupported flux combination for the internal-energy equations";
+      return nullptr;
     default:
       return "unsupported equations id";
   }
@@ -757,6 +767,7 @@ bool boundary_kind_ok(int eq, int kind) {
     case TAG_EQ_EULER_ENERGY_3D:
     case TAG_EQ_POTENTIAL_TEMPERATURE_3D: return kind == TAG_BC_SLIP_WALL_NORMAL;
     case TAG_EQ_RAINY_2D: return kind == TAG_BC_SIMPLE_SLIP_WALL;
+    case TAG_EQ_INTERNAL_ENERGY_2D: return kind == TAG_BC_SLIP_WALL_NORMAL;
     default: return false;
   }
 }
@@ -770,6 +781,7 @@ int analysis_phys(tag_handle h) {
     case TAG_EQ_MOIST_EULER_2D: return kAnMoist2D;
     case TAG_EQ_POTENTIAL_TEMPERATURE_2D: return kAnPT2D;
     case TAG_EQ_POTENTIAL_TEMPERATURE_3D: return kAnPT3D;
+    case TAG_EQ_INTERNAL_ENERGY_2D: return kAnIE2D;
     default: return kAnCov;
   }
 }
@@ -782,6 +794,7 @@ const void* analysis_params(tag_handle h) {
     case TAG_EQ_MOIST_EULER_2D: return &h->p_moist;
     case TAG_EQ_POTENTIAL_TEMPERATURE_2D: return &h->p_pt;
     case TAG_EQ_POTENTIAL_TEMPERATURE_3D: return &h->p_pt3d;
+    case TAG_EQ_INTERNAL_ENERGY_2D: return &h->p_ie;
     default: return &h->p_cov;
   }
 }
@@ -986,6 +999,11 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
     h->p_moist.surface = cfg->surface_flux;
     h->ops = cfg->volume_flux == TAG_VF_WEAK_FORM ? ops_for_n<PhysMoist2D, kVolWeak>(n)
                                                   : ops_for_n<PhysMoist2D, kVolFluxDiff>(n);
+  } else if (cfg->equations == TAG_EQ_INTERNAL_ENERGY_2D) {
+    h->nv = PhysIE2D::NV;
+    h->na = PhysIE2D::NA;
+    h->p_ie = PhysIE2D::make_params(cfg->params);
+    h->ops = ops_for_n<PhysIE2D, kVolFluxDiff>(n);
   } else if (cfg->equations == TAG_EQ_POTENTIAL_TEMPERATURE_3D) {
     h->nv = PhysPT3D::NV;
     h->na = PhysPT3D::NA;

@@ -107,6 +107,34 @@ class CompressibleEulerPotentialTemperatureEquationsWithGravity3D:
                 self.K * u[..., 4] ** self.gamma, u[..., 5])
 
 
+class CompressibleEulerInternalEnergyEquationsWithGravity2D:
+    """State (rho, rho_v1, rho_v2, rho_e_internal, phi), p = (gamma - 1) rho_e_internal
+    (src/equations/compressible_euler_internal_energy_with_gravity_2d.jl:42-62)."""
+
+    nvariables = 5
+    ndims = 2
+    eq_id = _lib.TAG_EQ_INTERNAL_ENERGY_2D
+
+    def __init__(self, *, c_p, c_v, gravity):
+        self.c_p = float(c_p)
+        self.c_v = float(c_v)
+        self.g = float(gravity)
+        self.p_0 = 100000.0
+        self.R = self.c_p - self.c_v
+        self.gamma = self.c_p / self.c_v
+        self.inv_gamma_minus_one = 1.0 / (self.gamma - 1.0)
+
+    def prim2cons(self, rho, v1, v2, p, phi):
+        """:248-255."""
+        one = np.ones_like(p)
+        return np.stack([rho * one, rho * v1 * one, rho * v2 * one,
+                         p * self.inv_gamma_minus_one * one, phi * one], axis=-1)
+
+    def cons2prim(self, u):
+        rho = u[..., 0]
+        return rho, u[..., 1] / rho, u[..., 2] / rho, (self.gamma - 1.0) * u[..., 3], u[..., 4]
+
+
 class CompressibleEulerEnergyEquationsWithGravity3D:
     """State (rho, rho_v1, rho_v2, rho_v3, rho_e, phi)
     (src/equations/compressible_euler_energy_with_gravity_3d.jl:45-65)."""
@@ -210,6 +238,11 @@ flux_chandrashekar = _NamedFlux("flux_chandrashekar")
 # equation type)
 flux_ec = _NamedFlux("flux_ec")
 flux_tec = _NamedFlux("flux_tec")
+# CompressibleEulerInternalEnergyEquationsWithGravity2D (:110-246)
+flux_conservative_etec = _NamedFlux("flux_conservative_etec")
+flux_nonconservative_etec = _NamedFlux("flux_nonconservative_etec")
+flux_conservative_es = _NamedFlux("flux_conservative_es")
+flux_nonconservative_es = _NamedFlux("flux_nonconservative_es")
 flux_etec = _NamedFlux("flux_etec")
 flux_nonconservative_artiano_etal = _NamedFlux("flux_nonconservative_artiano_etal")
 flux_nonconservative_souza_etal = _NamedFlux("flux_nonconservative_souza_etal")

@@ -25,7 +25,10 @@ import numpy as np
 
 from . import _lib
 from .basis import LobattoLegendreBasis
-from .equations import (CompressibleEulerPotentialTemperatureEquationsWithGravity2D,
+from .equations import (CompressibleEulerInternalEnergyEquationsWithGravity2D,
+                        flux_conservative_es, flux_conservative_etec, flux_nonconservative_es,
+                        flux_nonconservative_etec,
+                        CompressibleEulerPotentialTemperatureEquationsWithGravity2D,
                         CompressibleEulerPotentialTemperatureEquationsWithGravity3D,
                         flux_etec, flux_nonconservative_artiano_etal,
                         flux_nonconservative_souza_etal, flux_tec,
@@ -112,6 +115,17 @@ def _flux_ids(equations, solver, source_terms=None):
             raise ValueError(f"{source_terms} is not a source of the moist equations")
         eq = equations
         return vid, sid, [eq.c_pd, eq.c_vd, eq.c_pv, eq.c_vv, eq.g, c_lmars, float(src)]
+    if isinstance(equations, CompressibleEulerInternalEnergyEquationsWithGravity2D):
+        if not (isinstance(vf, tuple) and vf[0] is flux_conservative_etec
+                and vf[1] is flux_nonconservative_etec):
+            raise ValueError("volume flux must be (flux_conservative_etec, "
+                             "flux_nonconservative_etec)")
+        if not (isinstance(sf, tuple) and sf[0] is flux_conservative_es
+                and sf[1] is flux_nonconservative_es):
+            raise ValueError("surface flux must be (flux_conservative_es, flux_nonconservative_es)")
+        if source_terms is not None:
+            raise ValueError("source terms are not supported for this equation set")
+        return _lib.TAG_VF_IE_ETEC, _lib.TAG_SF_IE_ES, [equations.c_p, equations.c_v, equations.g]
     if isinstance(equations, (CompressibleEulerPotentialTemperatureEquationsWithGravity2D,
                               CompressibleEulerPotentialTemperatureEquationsWithGravity3D)):
         from .equations import flux_ec
