@@ -79,6 +79,8 @@ extern "C" {
 #define TAG_SF_COV_EC_LLF 5          /* covariant: FluxPlusDissipation(flux_ec, DissipationLocalLaxFriedrichs()) */
 #define TAG_SF_COV_CENTRAL 6         /* covariant: flux_central (no dissipation)        */
 #define TAG_SF_IE_ES 7               /* internal energy: (flux_conservative_es, flux_nonconservative_es) */
+#define TAG_SF_PT_EC 8               /* potential temperature 2D: (flux_ec, params[7]: 0 flux_zero,
+                                        1 waruszewski, 2 artiano, 3 souza gravity term) */
 
 #define TAG_SRC_RAINY 1              /* source_terms_rainy (microphysics + gravity)     */
 #define TAG_SRC_RAINY_CONVERGENCE 2  /* manufactured source of the rainy convergence test */

@@ -84,7 +84,11 @@ def lib():
                                        ctypes.c_double]
         L.orc_pt_create.restype = ctypes.c_void_p
         L.orc_pt_create.argtypes = ([ctypes.c_int] * 3 + [ctypes.c_double] * 4 + [ctypes.c_int] * 5 +
-                                    [ctypes.c_double] * 4)
+                                    [ctypes.c_double] * 4 + [ctypes.c_int] * 2)
+        L.orc_pt_create_mesh.restype = ctypes.c_void_p
+        L.orc_pt_create_mesh.argtypes = ([ctypes.c_int] * 2 + [_dp] * 3 + [ctypes.c_int] +
+                                         [_ip] * 3 + [ctypes.c_int] + [_ip] * 3 +
+                                         [ctypes.c_int] * 4 + [ctypes.c_double] * 4)
         L.orc_pt_destroy.argtypes = [ctypes.c_void_p]
         L.orc_pt_initial_condition_gravity_waves.argtypes = [ctypes.c_void_p, _dp]
         L.orc_pt_errors_gravity_waves.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
@@ -450,11 +454,27 @@ class PotTemp2D:
     nv = 5
 
     def __init__(self, polydeg, nx, ny, x0, x1, y0, y1, periodic_x=True, periodic_y=False,
-                 volume=0, nc=0, wall_kind=1, c_p=1004.0, c_v=717.0, g=9.80616, c_lmars=340.0):
+                 volume=0, nc=0, wall_kind=1, c_p=1004.0, c_v=717.0, g=9.80616, c_lmars=340.0,
+                 surface=0, snc=-1, mesh=None):
+        """surface 0 (FluxLMARS(c), surface term snc) or 1 (flux_ec, surface term
+        snc); snc -1 flux_zero, else a gravity-term kind as nc.  mesh: (xy, Ja,
+        invJ, if_e, if_f, if_flip, bd_e, bd_f, bd_kind) arrays of the host
+        mirror instead of the rectangle."""
         self.n = polydeg + 1
+        if mesh is not None:
+            self._keep = [np.ascontiguousarray(a, dtype=np.float64) for a in mesh[:3]]
+            self._keep += [np.ascontiguousarray(a, dtype=np.int32) for a in mesh[3:]]
+            xy, Ja, invJ, ie, ifc, fl, be, bf, bk = self._keep
+            self.nelem = invJ.shape[0]
+            self.h = lib().orc_pt_create_mesh(polydeg, self.nelem, _p(xy), _p(Ja), _p(invJ),
+                                              len(fl), _ip(ie), _ip(ifc), _ip(fl), len(be),
+                                              _ip(be), _ip(bf), _ip(bk), volume, nc, surface,
+                                              snc, c_p, c_v, g, c_lmars)
+            return
         self.nelem = nx * ny
         self.h = lib().orc_pt_create(polydeg, nx, ny, x0, x1, y0, y1, int(periodic_x),
-                                     int(periodic_y), volume, nc, wall_kind, c_p, c_v, g, c_lmars)
+                                     int(periodic_y), volume, nc, wall_kind, c_p, c_v, g, c_lmars,
+                                     surface, snc)
 
     def initial_condition_gravity_waves(self):
         u = np.zeros((self.nelem, self.n, self.n, 5))

@@ -458,9 +458,11 @@ struct PTPhys {
     return eq.noncons(a, b, n);
   }
   State surface_flux(const State& a, const State& b, const double* n) const {
-    return eq.flux_lmars(a, b, n, c_lmars);
+    return eq.surface_flux(a, b, n, c_lmars);
   }
-  State surface_noncons(const State&, const State&, const double*) const { return State{}; }
+  State surface_noncons(const State& a, const State& b, const double* n) const {
+    return eq.surface_noncons(a, b, n);
+  }
   State bc_structured(const State& ui, const double* n, int direction) const {
     return eq.slip_wall_structured(ui, n, direction, c_lmars);
   }
@@ -1297,15 +1299,57 @@ double orc_cov_ssp_steps(void* h, double* u, double t, double cfl, int nsteps, i
 // 2 souza; wall_kind: 1 StructuredMesh, 2 outward normal.
 void* orc_pt_create(int polydeg, int nx, int ny, double x0, double x1, double y0, double y1,
                     int periodic_x, int periodic_y, int volume, int nc, int wall_kind,
-                    double c_p, double c_v, double g, double c_lmars) {
+                    double c_p, double c_v, double g, double c_lmars, int surface, int snc) {
   auto* c = new PTCase();
   c->phys.eq.init(c_p, c_v, g);
   c->phys.eq.volume = volume;
   c->phys.eq.nc_kind = nc;
+  c->phys.eq.surface = surface;
+  c->phys.eq.snc_kind = snc;
   c->phys.c_lmars = c_lmars;
   c->basis = make_lgl_basis(polydeg);
   c->mesh = structured_rectangle(c->basis, nx, ny, x0, x1, y0, y1, periodic_x != 0,
                                  periodic_y != 0, wall_kind);
+  c->dg.reset(new DG2D<PTPhys>(c->phys, c->basis, c->mesh));
+  return c;
+}
+
+// the same on a mesh given by the host mirror's arrays (curvilinear P4estMesh):
+// node coordinates [E][n][n][2], contravariant vectors [E][n][n][2][2],
+// inverse Jacobian [E][n][n], interfaces and boundary faces as for the C ABI
+void* orc_pt_create_mesh(int polydeg, int nelem, const double* xy, const double* Ja,
+                         const double* invJ, int nif, const int* if_e, const int* if_f,
+                         const int* if_flip, int nbd, const int* bd_e, const int* bd_f,
+                         const int* bd_kind, int volume, int nc, int surface, int snc, double c_p,
+                         double c_v, double g, double c_lmars) {
+  auto* c = new PTCase();
+  c->phys.eq.init(c_p, c_v, g);
+  c->phys.eq.volume = volume;
+  c->phys.eq.nc_kind = nc;
+  c->phys.eq.surface = surface;
+  c->phys.eq.snc_kind = snc;
+  c->phys.c_lmars = c_lmars;
+  c->basis = make_lgl_basis(polydeg);
+  const int n = c->basis.n;
+  const size_t nodes = (size_t)nelem * n * n;
+  Mesh2D& m = c->mesh;
+  m.n = n;
+  m.nelem = nelem;
+  m.xy.assign(xy, xy + nodes * 2);
+  m.Ja.assign(Ja, Ja + nodes * 4);
+  m.invJ.assign(invJ, invJ + nodes);
+  for (int k = 0; k < nif; ++k) {
+    m.if_e0.push_back(if_e[2 * k]);
+    m.if_e1.push_back(if_e[2 * k + 1]);
+    m.if_f0.push_back(if_f[2 * k]);
+    m.if_f1.push_back(if_f[2 * k + 1]);
+    m.if_flip.push_back(if_flip[k]);
+  }
+  for (int k = 0; k < nbd; ++k) {
+    m.bd_e.push_back(bd_e[k]);
+    m.bd_f.push_back(bd_f[k]);
+    m.bd_kind.push_back(bd_kind[k]);
+  }
   c->dg.reset(new DG2D<PTPhys>(c->phys, c->basis, c->mesh));
   return c;
 }

@@ -43,6 +43,8 @@ struct PotTemp2D {
   double R = 287.0, gamma = 1004.0 / 717.0, K = 0.0, sc[8];
   int volume = 0;  // 0 flux_tec, 1 flux_ec, 2 flux_etec
   int nc_kind = 0;  // 0 waruszewski (ln_mean rho), 1 artiano (stolarsky rho), 2 souza (average)
+  int surface = 0;  // surface flux: 0 FluxLMARS(c), 1 flux_ec
+  int snc_kind = -1;  // surface nonconservative term: -1 flux_zero, else as nc_kind
 
   void init(double cp, double cv, double grav) {
     c_p = cp; c_v = cv; g = grav;
@@ -108,13 +110,37 @@ struct PotTemp2D {
   }
 
   // flux_nonconservative_{waruszewski_etal, artiano_etal, souza_etal} (:111-170)
-  State noncons(const State& ul, const State& ur, const double* n) const {
+  State noncons_of(const State& ul, const State& ur, const double* n, int kind) const {
     double ra;
-    if (nc_kind == 0) ra = ln_mean(ul[0], ur[0]);
-    else if (nc_kind == 1) ra = stolarsky(ul[0], ur[0]);
+    if (kind == 0) ra = ln_mean(ul[0], ur[0]);
+    else if (kind == 1) ra = stolarsky(ul[0], ur[0]);
     else ra = 0.5 * (ul[0] + ur[0]);
     const double jump = ur[4] - ul[4];
     return {0.0, n[0] * ra * jump, n[1] * ra * jump, 0.0, 0.0};
+  }
+  State noncons(const State& ul, const State& ur, const double* n) const {
+    return noncons_of(ul, ur, n, nc_kind);
+  }
+
+  // flux_ec (:290-321) whatever the volume flux is
+  State flux_ec(const State& ul, const State& ur, const double* n) const {
+    double rl, v1l, v2l, pl, rr, v1r, v2r, pr;
+    cons2prim(ul, rl, v1l, v2l, pl);
+    cons2prim(ur, rr, v1r, v2r, pr);
+    const double vnl = v1l * n[0] + v2l * n[1], vnr = v1r * n[0] + v2r * n[1];
+    const double v1a = 0.5 * (v1l + v1r), v2a = 0.5 * (v2l + v2r), pa = 0.5 * (pl + pr);
+    const double f1 = ln_mean(rl, rr) * 0.5 * (vnl + vnr);
+    const double f4 = f1 * inv_ln_mean(rl / ul[3], rr / ur[3]);
+    return {f1, f1 * v1a + pa * n[0], f1 * v2a + pa * n[1], f4, 0.0};
+  }
+
+  // the configured surface flux and nonconservative surface term
+  State surface_flux(const State& ul, const State& ur, const double* n, double a) const {
+    return surface ? flux_ec(ul, ur, n) : flux_lmars(ul, ur, n, a);
+  }
+  State surface_noncons(const State& ul, const State& ur, const double* n) const {
+    if (snc_kind < 0) return State{};
+    return noncons_of(ul, ur, n, snc_kind);
   }
 
   // FluxLMARS (:171-193)
@@ -142,15 +168,20 @@ struct PotTemp2D {
   State slip_wall_structured(const State& ui, const double* n, int direction, double a) const {
     State ub = ui;
     ub[2] = -ui[2];
-    if (direction % 2 == 0) return flux_lmars(ui, ub, n, a);
-    return flux_lmars(ub, ui, n, a);
+    if (direction % 2 == 0) return surface_flux(ui, ub, n, a);
+    return surface_flux(ub, ui, n, a);
   }
+  // the surface flux plus half the nonconservative term of the inner and the
+  // mirrored state (zero: both carry the same phi)
   State slip_wall_normal(const State& ui, const double* n, double a) const {
     const double nrm = std::sqrt(n[0] * n[0] + n[1] * n[1]);
     const double nx = n[0] / nrm, ny = n[1] / nrm;
     const double un = nx * ui[1] + ny * ui[2];
     const State ub = {ui[0], ui[1] - 2.0 * un * nx, ui[2] - 2.0 * un * ny, ui[3], ui[4]};
-    return flux_lmars(ui, ub, n, a);
+    State f = surface_flux(ui, ub, n, a);
+    const State g = surface_noncons(ui, ub, n);
+    for (int v = 0; v < 5; ++v) f[v] += 0.5 * g[v];
+    return f;
   }
 
   void max_abs_speeds(const State& u, double& l1, double& l2) const {

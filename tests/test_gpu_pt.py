@@ -100,3 +100,62 @@ def test_gpu_reproduces_pt_gravity_waves_golden(tg, orc, gpu_lib):
     for v in range(4):
         assert abs(l2[v] / GOLDEN_L2[v] - 1) < 2e-3, v
     semi.close()
+
+
+def test_pt_ec_surface_rhs_matches_oracle(tg, orc, gpu_lib):
+    """(flux_etec, Souza) volume flux with the entropy-conservative surface flux
+    (flux_ec, flux_nonconservative_waruszewski_etal): the surface gravity term
+    differs on the two sides of an interface; StructuredMesh and P4estMesh walls."""
+    for normal_walls in (False, True):
+        eq, mesh, semi = make_pt(tg, 8, 8, 3, "etec", "souza", normal_walls)
+        semi.close()
+        solver = tg.DGSEM(3, (tg.flux_ec, tg.flux_nonconservative_waruszewski_etal),
+                          tg.VolumeIntegralFluxDifferencing((tg.flux_etec,
+                                                             tg.flux_nonconservative_souza_etal)))
+        bcs = {"y_neg": tg.boundary_condition_slip_wall, "y_pos": tg.boundary_condition_slip_wall}
+        semi = tg.SemidiscretizationHyperbolic(mesh, eq, tg.initial_condition_gravity_waves, solver,
+                                               boundary_conditions=bcs)
+        u = perturbed(semi.compute_coefficients(), 13)
+        du = semi.rhs(u)
+        c = orc.PotTemp2D(3, 8, 8, 0.0, 300000.0, 0.0, 10000.0, True, False, volume=2, nc=2,
+                          wall_kind=2 if normal_walls else 1, surface=1, snc=0)
+        inv = mesh.inv if normal_walls else np.arange(u.shape[0])
+        du_ref = c.rhs(u[inv])
+        assert np.abs(du[inv] - du_ref).max() <= 1e-12 * np.abs(du_ref).max(), normal_walls
+        for v in range(4):
+            s = np.abs(du_ref[..., v]).max()
+            assert np.abs(du[inv][..., v] - du_ref[..., v]).max() <= 1e-11 * s, (normal_walls, v)
+        semi.close()
+
+
+@pytest.mark.parametrize("name", ["default", "ec_surface"])
+def test_gpu_reproduces_well_balanced_curvilinear_golden(tg, orc, gpu_lib, name):
+    """elixir_potential_temperature_well_balanced_curvilinear
+    (test/test_2d_potential_temperature.jl:100-144) on the curvilinear
+    P4estMesh: the rhs against the oracle on the same arrays, then SSPRK43 at
+    dt = 0.01 to t = 0.4 and the error norms, all on the GPU."""
+    from test_oracle_pt import (WELL_BALANCED, check_well_balanced, well_balanced_arrays,
+                                well_balanced_mesh)
+    kw, g2, gi = WELL_BALANCED[name]
+    eq = tg.CompressibleEulerPotentialTemperatureEquationsWithGravity2D(c_p=1004, c_v=717,
+                                                                         gravity=9.81)
+    mesh = well_balanced_mesh(tg)
+    vf = (tg.flux_etec, tg.flux_nonconservative_souza_etal) if name == "ec_surface" else \
+        (tg.flux_tec, tg.flux_nonconservative_artiano_etal)
+    sf = (tg.flux_ec, tg.flux_nonconservative_waruszewski_etal) if name == "ec_surface" else \
+        (tg.FluxLMARS(340.0), tg.flux_zero)
+    solver = tg.DGSEM(2, sf, tg.VolumeIntegralFluxDifferencing(vf))
+    bcs = {k: tg.boundary_condition_slip_wall for k in ("x_neg", "x_pos", "y_neg", "y_pos")}
+    semi = tg.SemidiscretizationHyperbolic(mesh, eq, tg.initial_condition_adiabatic, solver,
+                                           boundary_conditions=bcs)
+    basis, xy, Ja, invJ, arrays = well_balanced_arrays(tg, mesh)
+    c = orc.PotTemp2D(2, 0, 0, 0, 0, 0, 0, g=9.81, c_lmars=340.0, mesh=arrays, **kw)
+    u = perturbed(semi.compute_coefficients(), 3)
+    du, du_ref = semi.rhs(u), c.rhs(u)
+    assert np.abs(du - du_ref).max() <= 1e-12 * np.abs(du_ref).max()
+    semi.set_state(semi.compute_coefficients())
+    t = semi.rk_steps(40, fixed_dt=0.01, t=0.0, method="SSPRK43")
+    assert abs(t - 0.4) < 1e-12
+    l2, linf = semi.calc_error_norms(0.4)
+    check_well_balanced(l2, linf, g2, gi)
+    semi.close()

@@ -46,3 +46,68 @@ def test_stolarsky_mean_against_definition(orc):
             continue
         ex = (g - 1) / g * (mp.mpf(y) ** g - mp.mpf(x) ** g) / (mp.mpf(y) ** (g - 1) - mp.mpf(x) ** (g - 1))
         assert abs(got - float(ex)) <= 2e-15 * float(ex), (x, y)
+
+
+# test/test_2d_potential_temperature.jl:100-144: elixir_potential_temperature_
+# well_balanced_curvilinear (P4estMesh of 16 x 16 trees with a sine mapping,
+# N = 2, slip walls, adiabatic atmosphere at rest, SSPRK43 at dt = 0.01 to
+# t = 0.4), checked there with atol = 1e-5: the default fluxes and the entropy-
+# conservative surface flux with a nonconservative surface gravity term.
+WELL_BALANCED = {
+    "default": (dict(volume=0, nc=1, surface=0, snc=-1),
+                [1.9638272579852512e-8, 9.794074039239054e-13, 9.90302138162671e-13,
+                 5.891481774330958e-6, 6.256813355477567e-13],
+                [5.575406336610911e-8, 1.5959531831834447e-11, 1.575602141459924e-11,
+                 1.6726218973417417e-5, 3.637978807091713e-12]),
+    "ec_surface": (dict(volume=2, nc=2, surface=1, snc=0),
+                   [1.9676517857526736e-8, 1.5583712851610544e-7, 1.9956396607024943e-7,
+                    5.902955362653274e-6, 6.256813355477567e-13],
+                   [5.695755511681e-8, 9.548396023850076e-7, 1.3602645625916122e-6,
+                    1.708726631477475e-5, 3.637978807091713e-12]),
+}
+
+
+def well_balanced_mesh(tg):
+    def mapping(xi, eta):
+        x = xi + 0.1 * np.sin(np.pi * xi) * np.sin(np.pi * eta)
+        y = eta + 0.1 * np.sin(np.pi * xi) * np.sin(np.pi * eta)
+        return 1000 * 0.5 * (1 + x), 1000 * 0.5 * (1 + y)
+    return tg.P4estMesh((16, 16), polydeg=2, mapping=mapping, periodicity=(False, False))
+
+
+def well_balanced_arrays(tg, mesh):
+    basis = tg.LobattoLegendreBasis(2)
+    xy, Ja, invJ = mesh.geometry(basis)
+    conn = mesh.connectivity()
+    ie, ifc, fl, be, bf = conn.arrays()
+    bk = np.full(len(be), 2, dtype=np.int32)  # outward-normal slip walls
+    return basis, xy, Ja, invJ, (xy, Ja, invJ, ie, ifc, fl, be, bf, bk)
+
+
+@pytest.mark.parametrize("name", list(WELL_BALANCED))
+def test_oracle_pt_well_balanced_curvilinear_golden(tg, orc, name):
+    import analysis
+    kw, g2, gi = WELL_BALANCED[name]
+    eq = tg.CompressibleEulerPotentialTemperatureEquationsWithGravity2D(c_p=1004, c_v=717,
+                                                                         gravity=9.81)
+    mesh = well_balanced_mesh(tg)
+    basis, xy, Ja, invJ, arrays = well_balanced_arrays(tg, mesh)
+    c = orc.PotTemp2D(2, 0, 0, 0, 0, 0, 0, g=9.81, c_lmars=340.0, mesh=arrays, **kw)
+    u = np.ascontiguousarray(tg.initial_condition_adiabatic(xy, 0.0, eq))
+    t = c.ssp_steps(u, 0.0, 1.0, 10 ** 6, 1, fixed_dt=0.01, t_end=0.4)
+    assert abs(t - 0.4) < 1e-14
+    l2, linf = analysis.error_norms(u, xy, invJ, basis.nodes,
+                                    lambda x: tg.initial_condition_adiabatic(x, 0.0, eq), 2)
+    check_well_balanced(l2, linf, g2, gi)
+
+
+def check_well_balanced(l2, linf, g2, gi):
+    """Much tighter than the reference test's atol = 1e-5: norms above 1e-10
+    within 1e-6 relative (measured: 1e-11 .. 6e-7), the rounding-noise norms
+    (momenta of the default fluxes, phi) within 1e-11 absolute."""
+    for got, gold in ((l2, g2), (linf, gi)):
+        for v in range(5):
+            if gold[v] > 1e-10:
+                assert abs(got[v] / gold[v] - 1) <= 1e-6, (v, got[v], gold[v])
+            else:
+                assert abs(got[v] - gold[v]) <= 1e-11, (v, got[v], gold[v])

@@ -32,6 +32,7 @@ from .initial_conditions import (EARTH_GRAVITATIONAL_ACCELERATION, EARTH_RADIUS,
                                  WarmBubble, initial_condition_convergence_test_rainy,
                                  initial_condition_baroclinic_instability,
                                  initial_condition_gravity_waves, seeded_perturbation,
+                                 initial_condition_adiabatic,
                                  initial_condition_gemein_bubble,
                                  initial_condition_convergence_test_dry,
                                  initial_condition_convergence_test_moist)
@@ -58,7 +59,7 @@ __all__ = [
     "source_terms_moist_bubble", "source_terms_convergence_test_dry",
     "source_terms_convergence_test_moist", "initial_condition_gemein_bubble",
     "initial_condition_convergence_test_dry", "initial_condition_convergence_test_moist",
-    "P4estMesh", "covariant", "SemidiscretizationCovariant",
+    "P4estMesh", "covariant", "SemidiscretizationCovariant", "initial_condition_adiabatic",
     "SemidiscretizationCovariantEnsemble",
     "CompressibleEulerPotentialTemperatureEquationsWithGravity2D",
     "CompressibleEulerPotentialTemperatureEquationsWithGravity3D",

@@ -44,6 +44,7 @@ TAG_EQ_POTENTIAL_TEMPERATURE_3D = 7
 TAG_EQ_INTERNAL_ENERGY_2D = 8
 TAG_VF_IE_ETEC = 10
 TAG_SF_IE_ES = 7
+TAG_SF_PT_EC = 8
 TAG_VF_PT_TEC = 7
 TAG_VF_PT_EC = 8
 TAG_VF_PT_ETEC = 9

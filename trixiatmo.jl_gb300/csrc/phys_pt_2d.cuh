@@ -24,16 +24,21 @@ struct PhysPT2D {
   static constexpr int kRho = 0, kBeta = 0, kLogRho = 0, kLogBeta = 0;
   static constexpr bool kNodeLogs = false;
   static constexpr bool kHasSources = false;
-  static constexpr bool kSurfaceNoncons = false;  // surface flux only (flux_zero)
+  // surface flux (FluxLMARS(c), flux_zero) or (flux_ec, a nonconservative
+  // gravity term); the interface kernel adds the per-side term when snc >= 0
+  static constexpr bool kSurfaceNoncons = true;
 
   struct Params {
     double gamma, K, c_lmars, stol_fac;  // stol_fac = (gamma - 1) / gamma
     double sc[8];                        // Stolarsky series coefficients
     int volume;                          // 0 flux_tec, 1 flux_ec, 2 flux_etec
     int nc;                              // 0 waruszewski, 1 artiano, 2 souza
+    int surface;                         // 0 FluxLMARS(c), 1 flux_ec
+    int snc;                             // surface gravity term: -1 none (flux_zero), else as nc
   };
 
-  // params = (c_p, c_v, g, LMARS c, nonconservative kind, volume kind)
+  // params = (c_p, c_v, g, LMARS c, nonconservative kind, volume kind,
+  // surface kind, surface nonconservative kind + 1)
   static Params make_params(const double* p) {
     Params q;
     const double c_p = p[0], c_v = p[1], R = c_p - c_v;
@@ -43,6 +48,8 @@ struct PhysPT2D {
     q.stol_fac = (q.gamma - 1.0) / q.gamma;
     q.nc = (int)p[4];
     q.volume = (int)p[5];
+    q.surface = (int)p[6];
+    q.snc = (int)p[7] - 1;
     double a[8], b[8];
     for (int j = 0; j < 8; ++j) {
       double ra = 1.0, rb = 1.0;
@@ -166,9 +173,50 @@ struct PhysPT2D {
     F[3] = us[3] * v_int;
   }
 
+  // flux_ec (:290-321) of full states
+  TAG_DEV static void flux_ec(const Params& P, const double* ul, const double* ur, double n1,
+                              double n2, double* F) {
+    const double irl = 1.0 / ul[0], irr = 1.0 / ur[0];
+    const double v1l = ul[1] * irl, v2l = ul[2] * irl, v1r = ur[1] * irr, v2r = ur[2] * irr;
+    const double pl = P.K * pow(ul[3], P.gamma), pr = P.K * pow(ur[3], P.gamma);
+    const double vn = 0.5 * ((v1l * n1 + v2l * n2) + (v1r * n1 + v2r * n2));
+    const double pa = 0.5 * (pl + pr);
+    double rho_ln, inv_sig;
+    ln_mean_pair<false>(ul[0], ur[0], ul[0] / ul[3], ur[0] / ur[3], 0.0, 0.0, 0.0, 0.0, rho_ln,
+                        inv_sig);
+    const double f1 = rho_ln * vn;
+    F[0] = f1;
+    F[1] = f1 * 0.5 * (v1l + v1r) + pa * n1;
+    F[2] = f1 * 0.5 * (v2l + v2r) + pa * n2;
+    F[3] = f1 * inv_sig;
+  }
+
   TAG_DEV static void surface_flux(const Params& P, const double* ul, const double* ur, double n1,
                                    double n2, double* F) {
-    lmars(P, ul, ur, n1, n2, F);
+    if (P.surface == 1)
+      flux_ec(P, ul, ur, n1, n2, F);
+    else
+      lmars(P, ul, ur, n1, n2, F);
+  }
+
+  // the nonconservative gravity term of the surface flux, G(ul, ur) along the
+  // primary's normal (zero for flux_zero)
+  TAG_DEV static void surface_noncons(const Params& P, const double* ul, const double* ur,
+                                      double n1, double n2, double* G) {
+    G[0] = G[1] = G[2] = G[3] = 0.0;
+    if (P.snc < 0) return;
+    double ra;
+    if (P.snc == 0) {
+      ra = ln_mean_single(ul[0], ur[0]);
+    } else if (P.snc == 1) {
+      const double xg = pow(ul[0], P.gamma), yg = pow(ur[0], P.gamma);
+      ra = stolarsky(P, ul[0], ur[0], xg, xg / ul[0], yg, yg / ur[0]);
+    } else {
+      ra = 0.5 * (ul[0] + ur[0]);
+    }
+    const double jump = ur[4] - ul[4];
+    G[1] = n1 * ra * jump;
+    G[2] = n2 * ra * jump;
   }
 
   // Slip walls.  TAG_BC_SLIP_WALL_STRUCTURED (:62-83): reached with the normal
@@ -177,12 +225,13 @@ struct PhysPT2D {
   // is mirrored about the outward normal (n1, n2).
   TAG_DEV static void boundary_flux(const Params& P, const double* ui, double n1, double n2,
                                     int face, int kind, double* F) {
+    // (the wall's nonconservative term vanishes: both states carry the same phi)
     if (kind == TAG_BC_SLIP_WALL_STRUCTURED) {
       const double ub[5] = {ui[0], ui[1], -ui[2], ui[3], ui[4]};
       if (face & 1) {
-        lmars(P, ui, ub, n1, n2, F);
+        surface_flux(P, ui, ub, n1, n2, F);
       } else {
-        lmars(P, ub, ui, n1, n2, F);
+        surface_flux(P, ub, ui, n1, n2, F);
         F[0] = -F[0]; F[1] = -F[1]; F[2] = -F[2]; F[3] = -F[3];
       }
     } else {
@@ -190,7 +239,7 @@ struct PhysPT2D {
       const double nx = n1 / nn, ny = n2 / nn;
       const double un = nx * ui[1] + ny * ui[2];
       const double ub[5] = {ui[0], ui[1] - 2.0 * un * nx, ui[2] - 2.0 * un * ny, ui[3], ui[4]};
-      lmars(P, ui, ub, n1, n2, F);
+      surface_flux(P, ui, ub, n1, n2, F);
     }
   }
 

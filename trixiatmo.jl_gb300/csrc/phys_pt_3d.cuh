@@ -30,8 +30,12 @@ struct PhysPT3D {
 
   // params = (c_p, c_v, g, LMARS c, nonconservative kind, volume kind, Omega)
   static Params make_params(const double* p) {
+    double p2[8];
+    for (int k = 0; k < 8; ++k) p2[k] = p[k];
+    p2[6] = 0.0;  // surface (FluxLMARS(c), flux_zero)
+    p2[7] = 0.0;
     Params q;
-    q.pt = PhysPT2D::make_params(p);
+    q.pt = PhysPT2D::make_params(p2);
     q.omega = p[6];
     return q;
   }

@@ -742,11 +742,19 @@ const char* check_equations(const tag_config* cfg) {
     }
     case TAG_EQ_POTENTIAL_TEMPERATURE_2D:
     case TAG_EQ_POTENTIAL_TEMPERATURE_3D: {
-      if ((vf != TAG_VF_PT_TEC && vf != TAG_VF_PT_EC && vf != TAG_VF_PT_ETEC) || sf != TAG_SF_LMARS)
+      const bool ec_surface =
+          sf == TAG_SF_PT_EC && cfg->equations == TAG_EQ_POTENTIAL_TEMPERATURE_2D;
+      if ((vf != TAG_VF_PT_TEC && vf != TAG_VF_PT_EC && vf != TAG_VF_PT_ETEC) ||
+          (sf != TAG_SF_LMARS && !ec_surface))
         return "unsupported flux combination for the potential-temperature equations";
       const double k = cfg->params[4];
       if (k != 0 && k != 1 && k != 2) return "unsupported nonconservative gravity term";
-      if (!(cfg->params[3] > 0.0)) return "FluxLMARS needs a positive speed of sound";
+      if (ec_surface) {
+        const double s = cfg->params[7];
+        if (s != 0 && s != 1 && s != 2 && s != 3) return "unsupported surface gravity term";
+      } else if (!(cfg->params[3] > 0.0)) {
+        return "FluxLMARS needs a positive speed of sound";
+      }
       return nullptr;
     }
     case TAG_EQ_INTERNAL_ENERGY_2D:
@@ -990,6 +998,8 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
     double pp[8];
     for (int k = 0; k < 8; ++k) pp[k] = cfg->params[k];
     pp[5] = cfg->volume_flux == TAG_VF_PT_TEC ? 0 : cfg->volume_flux == TAG_VF_PT_EC ? 1 : 2;
+    pp[6] = cfg->surface_flux == TAG_SF_PT_EC ? 1 : 0;
+    if (cfg->surface_flux != TAG_SF_PT_EC) pp[7] = 0;  // flux_zero
     h->p_pt = PhysPT2D::make_params(pp);
     h->ops = ops_for_n<PhysPT2D, kVolFluxDiff>(n);
   } else if (moist) {

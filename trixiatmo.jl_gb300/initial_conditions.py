@@ -26,6 +26,21 @@ def initial_condition_gravity_waves(x, t, equations):
     return equations.prim2cons(rho, 20.0, 0.0, p, g * x[..., 1])
 
 
+def initial_condition_adiabatic(x, t, equations):
+    """src/equations/initial_condition_compressible_euler_2d.jl:44-67: an
+    adiabatic atmosphere at rest (potential temperature 300 K) in hydrostatic
+    balance."""
+    g, c_p, c_v = equations.g, equations.c_p, equations.c_v
+    p0 = 100_000.0
+    R = c_p - c_v
+    theta = 300.0
+    exner = 1.0 - g / (c_p * theta) * x[..., 1]
+    p = p0 * exner ** (c_p / R)
+    T = theta * exner
+    rho = p / (R * T)
+    return equations.prim2cons(rho, 0.0, 0.0, p, g * x[..., 1])
+
+
 class WarmBubble:
     """Dry warm bubble (Wicker & Skamarock 1998) of
     examples/euler/dry_air/buoyancy/elixir_gemein_bubble.jl:20-51 for the

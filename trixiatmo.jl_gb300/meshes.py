@@ -141,18 +141,26 @@ class P4estMesh:
     ndims = 2
     normal_walls = True
 
-    def __init__(self, trees_per_dimension, *, polydeg=1, coordinates_min, coordinates_max,
-                 initial_refinement_level=0, periodicity=True):
+    def __init__(self, trees_per_dimension, *, polydeg=1, coordinates_min=None,
+                 coordinates_max=None, mapping=None, initial_refinement_level=0,
+                 periodicity=True):
+        """mapping(xi, eta) -> (x, y) of the global reference square [-1, 1]^2
+        (the `mapping` keyword of the reference's P4estMesh, e.g.
+        examples/euler/dry_air/tests/elixir_potential_temperature_well_balanced_curvilinear.jl);
+        otherwise the affine map of coordinates_min / coordinates_max.  Trees
+        are not refined when a mapping is given."""
         tx, ty = map(int, trees_per_dimension)
         if isinstance(periodicity, bool):
             periodicity = (periodicity, periodicity)
         L = int(initial_refinement_level)
+        if mapping is not None and L != 0:
+            raise ValueError("a mapped P4estMesh is supported at initial_refinement_level = 0")
         k = 1 << L
         self.trees_per_dimension = (tx, ty)
         self.level = L
         self.polydeg = int(polydeg)
         self._grid = StructuredMesh((tx * k, ty * k), coordinates_min, coordinates_max,
-                                    periodicity)
+                                    periodicity, mapping=mapping)
         nx = tx * k
         perm = np.empty(tx * ty * k * k, dtype=np.int64)
         for tyi in range(ty):

@@ -139,8 +139,19 @@ def _flux_ids(equations, solver, source_terms=None):
               id(flux_nonconservative_souza_etal): 2}.get(id(vf[1]))
         if vid is None or nc is None:
             raise ValueError(f"unsupported potential-temperature volume flux {vf}")
+        nc_ids = {id(flux_nonconservative_waruszewski_etal): 1,
+                  id(flux_nonconservative_artiano_etal): 2, id(flux_nonconservative_souza_etal): 3}
+        if (equations.ndims == 2 and isinstance(sf, tuple) and sf[0] is flux_ec
+                and (sf[1] is flux_zero or id(sf[1]) in nc_ids)):
+            # (flux_ec, flux_zero | a nonconservative gravity term) at the surface
+            snc = 0 if sf[1] is flux_zero else nc_ids[id(sf[1])]
+            if source_terms is not None:
+                raise ValueError("source terms are not supported for this equation set")
+            return vid, _lib.TAG_SF_PT_EC, [equations.c_p, equations.c_v, equations.g, 0.0,
+                                            float(nc), 0.0, 0.0, float(snc)]
         if not (isinstance(sf, tuple) and isinstance(sf[0], FluxLMARS) and sf[1] is flux_zero):
-            raise ValueError("surface flux must be (FluxLMARS(c), flux_zero)")
+            raise ValueError("surface flux must be (FluxLMARS(c), flux_zero)"
+                             + (" or (flux_ec, a gravity term)" if equations.ndims == 2 else ""))
         params = [equations.c_p, equations.c_v, equations.g, sf[0].speed_of_sound, float(nc)]
         if equations.ndims == 3:
             if source_terms not in (None, source_terms_coriolis):
