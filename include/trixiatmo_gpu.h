@@ -88,6 +88,8 @@ extern "C" {
 #define TAG_SRC_MOIST_BUBBLE 4       /* source_terms_moist_bubble: geopotential + phase change */
 #define TAG_SRC_MOIST_CONVERGENCE_DRY 5 /* source_terms_convergence_test_dry (moist equations) */
 #define TAG_SRC_MOIST_CONVERGENCE 6  /* source_terms_convergence_test_moist            */
+#define TAG_SRC_MOIST_GRAVITY_WAVE 7 /* geopotential + phase change +
+                                        source_terms_nonhydrostatic_rayleigh_sponge     */
 
 #define TAG_BC_SLIP_WALL_STRUCTURED 1 /* boundary_condition_slip_wall reached from a StructuredMesh */
 #define TAG_BC_SLIP_WALL_NORMAL 2     /* boundary_condition_slip_wall reached from a P4estMesh      */

@@ -109,6 +109,11 @@ def lib():
                                       ctypes.c_int]
         L.orc_pt_stolarsky.restype = ctypes.c_double
         L.orc_pt_stolarsky.argtypes = [ctypes.c_double] * 3
+        L.orc_moist_create_mesh.restype = ctypes.c_void_p
+        L.orc_moist_create_mesh.argtypes = ([ctypes.c_int] * 2 + [_dp] * 3 + [ctypes.c_int] +
+                                            [_ip] * 3 + [ctypes.c_int] + [_ip] * 3 +
+                                            [ctypes.c_int] * 3 + [ctypes.c_double] * 2 +
+                                            [ctypes.c_int])
         L.orc_moist_create.restype = ctypes.c_void_p
         L.orc_moist_create.argtypes = ([ctypes.c_int] * 3 + [ctypes.c_double] * 4 +
                                        [ctypes.c_int] * 6 + [ctypes.c_double] * 2 + [ctypes.c_int])
@@ -519,16 +524,30 @@ class Moist2D:
     """Moist Euler on a StructuredMesh rectangle.  surface_kind 0: FluxLMARS(c),
     1: flux_lax_friedrichs, 2: flux_chandrashekar; source_kind 0: none,
     1: geopotential, 2: moist bubble (geopotential + phase change), 3 / 4: the
-    dry / moist convergence tests; wall_kind 1: StructuredMesh slip wall,
-    2: outward normal (P4estMesh); ic_kind 0: gemein bubble (dry, v1 = 20),
-    1 / 2: dry / moist convergence test."""
+    dry / moist convergence tests, 5: moist bubble + Rayleigh sponge;
+    wall_kind 1: StructuredMesh slip wall, 2: outward normal (P4estMesh);
+    ic_kind 0: gemein bubble (dry, v1 = 20), 1 / 2: dry / moist convergence
+    test, 3: nonhydrostatic gravity wave.  mesh: (xy, Ja, invJ, if_e, if_f,
+    if_flip, bd_e, bd_f, bd_kind) arrays of the host mirror instead of the
+    rectangle."""
 
     nv = 6
 
     def __init__(self, polydeg, nx, ny, x0, x1, y0, y1, periodic_x=True, periodic_y=False,
                  weak_form=False, surface_kind=0, source_kind=1, wall_kind=1, c_lmars=360.0,
-                 gravity=9.80616, ic_kind=0):
+                 gravity=9.80616, ic_kind=0, mesh=None):
         self.n = polydeg + 1
+        if mesh is not None:
+            self._keep = [np.ascontiguousarray(a, dtype=np.float64) for a in mesh[:3]]
+            self._keep += [np.ascontiguousarray(a, dtype=np.int32) for a in mesh[3:]]
+            xy, Ja, invJ, ie, ifc, fl, be, bf, bk = self._keep
+            self.nelem = invJ.shape[0]
+            self.h = lib().orc_moist_create_mesh(polydeg, self.nelem, _p(xy), _p(Ja), _p(invJ),
+                                                 len(fl), _ip(ie), _ip(ifc), _ip(fl), len(be),
+                                                 _ip(be), _ip(bf), _ip(bk), int(weak_form),
+                                                 int(surface_kind), int(source_kind), c_lmars,
+                                                 gravity, int(ic_kind))
+            return
         self.nelem = nx * ny
         self.h = lib().orc_moist_create(polydeg, nx, ny, x0, x1, y0, y1, int(periodic_x),
                                         int(periodic_y), int(weak_form), int(surface_kind),

@@ -350,11 +350,41 @@ struct MoistPhys {
       case 2: return eq.source_moist_bubble(u);
       case 3: return eq.source_convergence_dry(u, x, t);
       case 4: return eq.source_convergence_moist(u, x, t);
+      case 5: return eq.source_gravity_wave(u, x);
       default: return State{};
     }
   }
   void max_abs_speeds(const State& u, double& l1, double& l2) const { eq.max_abs_speeds(u, l1, l2); }
 };
+
+// A 2D mesh given by the host mirror's arrays (curvilinear P4estMesh, or a
+// StructuredMesh with curved faces): node coordinates [E][n][n][2],
+// contravariant vectors [E][n][n][2][2], inverse Jacobian [E][n][n],
+// interfaces and boundary faces as for the C ABI.
+Mesh2D mesh_from_arrays(int n, int nelem, const double* xy, const double* Ja, const double* invJ,
+                        int nif, const int* if_e, const int* if_f, const int* if_flip, int nbd,
+                        const int* bd_e, const int* bd_f, const int* bd_kind) {
+  const size_t nodes = (size_t)nelem * n * n;
+  Mesh2D m;
+  m.n = n;
+  m.nelem = nelem;
+  m.xy.assign(xy, xy + nodes * 2);
+  m.Ja.assign(Ja, Ja + nodes * 4);
+  m.invJ.assign(invJ, invJ + nodes);
+  for (int k = 0; k < nif; ++k) {
+    m.if_e0.push_back(if_e[2 * k]);
+    m.if_e1.push_back(if_e[2 * k + 1]);
+    m.if_f0.push_back(if_f[2 * k]);
+    m.if_f1.push_back(if_f[2 * k + 1]);
+    m.if_flip.push_back(if_flip[k]);
+  }
+  for (int k = 0; k < nbd; ++k) {
+    m.bd_e.push_back(bd_e[k]);
+    m.bd_f.push_back(bd_f[k]);
+    m.bd_kind.push_back(bd_kind[k]);
+  }
+  return m;
+}
 
 struct MoistCase {
   MoistPhys phys;
@@ -367,10 +397,26 @@ struct MoistCase {
 
 // Initial states of the moist tests.  kind 0: the warm bubble of
 // examples/euler/dry_air/buoyancy/elixir_gemein_bubble.jl:20-51 (v1 = 20,
-// no moisture); 1 / 2: the dry / moist convergence tests (:173-200, :244-272).
+// no moisture); 1 / 2: the dry / moist convergence tests (:173-200, :244-272);
+// 3: the mountain-triggered gravity wave of
+// examples/euler/dry_air/buoyancy/elixir_gemein_nonhydrostatic_gravity_waves.jl:15-39
+// (constant Brunt-Vaisala frequency N = 0.01 over theta_0 = T_0 = 280 K,
+// v1 = 10, no moisture).
 inline MoistEuler2D::State ic_moist(const MoistEuler2D& eq, int kind, const double* x, double t) {
   if (kind == 1) return eq.ic_convergence_dry(x, t);
   if (kind == 2) return eq.ic_convergence_moist(x, t);
+  if (kind == 3) {
+    const double z = x[1], theta_0 = 280.0, N = 0.01;
+    const double theta = theta_0 * std::exp(N * N * z / eq.g);
+    const double p = eq.p_0 * std::pow(1.0 + eq.g * eq.g * (1.0 / (eq.c_pd * theta_0 * (N * N))) *
+                                                 (std::exp(-z * (N * N) / eq.g) - 1.0),
+                                       1.0 / eq.kappa);
+    const double rho = p / (std::pow(p / eq.p_0, eq.kappa) * eq.R_d * theta);
+    const double T = p / (eq.R_d * rho);
+    const double v1 = 10.0, v2 = 0.0;
+    return {rho, rho * v1, rho * v2, rho * eq.c_vd * T + 0.5 * rho * (v1 * v1 + v2 * v2), 0.0,
+            0.0};
+  }
   const double xc = 10000.0, zc = 2000.0, rc = 2000.0, theta_ref = 300.0;
   const double r = std::sqrt((x[0] - xc) * (x[0] - xc) + (x[1] - zc) * (x[1] - zc));
   double dth = 0.0;
@@ -1176,6 +1222,26 @@ void* orc_moist_create(int polydeg, int nx, int ny, double x0, double x1, double
   return c;
 }
 
+// the same on a mesh given by the host mirror's arrays (see mesh_from_arrays)
+void* orc_moist_create_mesh(int polydeg, int nelem, const double* xy, const double* Ja,
+                            const double* invJ, int nif, const int* if_e, const int* if_f,
+                            const int* if_flip, int nbd, const int* bd_e, const int* bd_f,
+                            const int* bd_kind, int weak_form, int surface_kind, int source_kind,
+                            double c_lmars, double gravity, int ic_kind) {
+  auto* c = new MoistCase();
+  c->phys.eq.init(1004.0, 717.0, 1885.0, 1424.0, gravity);
+  c->phys.surface_kind = surface_kind;
+  c->phys.source_kind = source_kind;
+  c->phys.c_lmars = c_lmars;
+  c->ic_kind = ic_kind;
+  c->basis = make_lgl_basis(polydeg);
+  c->mesh = mesh_from_arrays(c->basis.n, nelem, xy, Ja, invJ, nif, if_e, if_f, if_flip, nbd, bd_e,
+                             bd_f, bd_kind);
+  c->dg.reset(new DG2D<MoistPhys>(c->phys, c->basis, c->mesh));
+  c->dg->weak_form = weak_form != 0;
+  return c;
+}
+
 void orc_moist_destroy(void* h) { delete static_cast<MoistCase*>(h); }
 
 void orc_moist_initial_condition(void* h, double t, double* u) {
@@ -1314,7 +1380,7 @@ void* orc_pt_create(int polydeg, int nx, int ny, double x0, double x1, double y0
   return c;
 }
 
-// the same on a mesh given by the host mirror's arrays (curvilinear P4estMesh):
+// potential temperature on such a mesh:
 // node coordinates [E][n][n][2], contravariant vectors [E][n][n][2][2],
 // inverse Jacobian [E][n][n], interfaces and boundary faces as for the C ABI
 void* orc_pt_create_mesh(int polydeg, int nelem, const double* xy, const double* Ja,
@@ -1330,26 +1396,8 @@ void* orc_pt_create_mesh(int polydeg, int nelem, const double* xy, const double*
   c->phys.eq.snc_kind = snc;
   c->phys.c_lmars = c_lmars;
   c->basis = make_lgl_basis(polydeg);
-  const int n = c->basis.n;
-  const size_t nodes = (size_t)nelem * n * n;
-  Mesh2D& m = c->mesh;
-  m.n = n;
-  m.nelem = nelem;
-  m.xy.assign(xy, xy + nodes * 2);
-  m.Ja.assign(Ja, Ja + nodes * 4);
-  m.invJ.assign(invJ, invJ + nodes);
-  for (int k = 0; k < nif; ++k) {
-    m.if_e0.push_back(if_e[2 * k]);
-    m.if_e1.push_back(if_e[2 * k + 1]);
-    m.if_f0.push_back(if_f[2 * k]);
-    m.if_f1.push_back(if_f[2 * k + 1]);
-    m.if_flip.push_back(if_flip[k]);
-  }
-  for (int k = 0; k < nbd; ++k) {
-    m.bd_e.push_back(bd_e[k]);
-    m.bd_f.push_back(bd_f[k]);
-    m.bd_kind.push_back(bd_kind[k]);
-  }
+  c->mesh = mesh_from_arrays(c->basis.n, nelem, xy, Ja, invJ, nif, if_e, if_f, if_flip, nbd, bd_e,
+                             bd_f, bd_kind);
   c->dg.reset(new DG2D<PTPhys>(c->phys, c->basis, c->mesh));
   return c;
 }

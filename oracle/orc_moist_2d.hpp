@@ -194,6 +194,28 @@ struct MoistEuler2D {
     return s;
   }
 
+  // source_terms_nonhydrostatic_rayleigh_sponge, :346-373: damping of the
+  // velocity towards (10, 0) in the layer z_s = 9000 < z < z_top = 16000
+  State source_rayleigh_sponge(const State& u, const double* x) const {
+    const double v1 = u[1] / u[0], v2 = u[2] / u[0];
+    const double z = x[1], z_s = 9000.0, z_top = 16000.0, alpha = 0.5;
+    double tau = 0.0;
+    if (z > z_s) {
+      const double s = std::sin(0.5 * (z - z_s) * (1.0 / (z_top - z_s)));
+      tau = alpha * (s * s);
+    }
+    return {0.0, -tau * u[0] * (v1 - 10.0), -tau * u[0] * (v2 - 0.0), 0.0, 0.0, 0.0};
+  }
+
+  // the source of examples/euler/dry_air/buoyancy/elixir_gemein_nonhydrostatic_gravity_waves.jl:50-56:
+  // (geopotential + phase change) + Rayleigh sponge
+  State source_gravity_wave(const State& u, const double* x) const {
+    State s = source_moist_bubble(u);
+    const State r = source_rayleigh_sponge(u, x);
+    for (int v = 0; v < 6; ++v) s[v] += r[v];
+    return s;
+  }
+
   // max_abs_speeds, :921-930
   void max_abs_speeds(const State& u, double& l1, double& l2) const {
     double p, T;

@@ -102,7 +102,7 @@ def test_cov_rk_steps_match_oracle(tg, orc, gpu_lib):
 
 
 @pytest.mark.parametrize("name", ["geostrophic_balance", "isolated_mountain", "well_balanced",
-                                  "unsteady_solid_body_rotation"])
+                                  "unsteady_solid_body_rotation", "barotropic_instability"])
 def test_gpu_reproduces_covariant_golden(tg, orc, gpu_lib, name):
     cv = tg.covariant
     eq, mesh, semi, fluxes, cfl = make_semi(tg, name)

@@ -169,3 +169,65 @@ def test_gpu_reproduces_moist_golden(tg, orc, gpu_lib, name):
     l2d, linfd = semi.calc_error_norms(t)
     check_golden(l2d, linfd, golden, rtol)
     semi.close()
+
+
+def gravity_wave_semi(tg, polydeg=3, cells=(10, 8)):
+    from test_oracle_moist import gravity_wave_faces
+    eq = tg.CompressibleMoistEulerEquations2D(**CP, gravity=9.80616)
+    mesh = tg.StructuredMesh(cells, periodicity=(True, False), faces=gravity_wave_faces())
+    solver = tg.DGSEM(polydeg, tg.FluxLMARS(360.0),
+                      tg.VolumeIntegralFluxDifferencing(tg.flux_chandrashekar))
+    semi = tg.SemidiscretizationHyperbolic(
+        mesh, eq, tg.initial_condition_nonhydrostatic_gravity_wave, solver,
+        boundary_conditions={"y_neg": tg.boundary_condition_slip_wall,
+                             "y_pos": tg.boundary_condition_slip_wall},
+        source_terms=tg.source_terms_nonhydrostatic_gravity_wave)
+    return eq, mesh, semi
+
+
+@pytest.mark.parametrize("polydeg", [2, 3, 4, 5])
+def test_moist_rhs_curved_mesh_with_sponge(tg, orc, gpu_lib, polydeg):
+    """The witch-of-Agnesi StructuredMesh (transfinite mapping, curved bottom
+    slip wall) with geopotential + phase change + Rayleigh sponge sources, on a
+    moist state with random velocities (the sponge acts above 9 km)."""
+    from test_oracle_moist import gravity_wave_mesh
+    eq, mesh, semi = gravity_wave_semi(tg, polydeg, (8, 6))
+    *_, arrays = gravity_wave_mesh(tg, (8, 6), polydeg)
+    u = moist_state(eq, semi.compute_coefficients(), seed=40 + polydeg)
+    du = semi.rhs(u)
+    c = orc.Moist2D(polydeg, 0, 0, 0, 0, 0, 0, surface_kind=0, source_kind=5, c_lmars=360.0,
+                    gravity=9.80616, ic_kind=3, mesh=arrays)
+    du_ref = c.rhs(u)
+    assert max_norm_rel(du, du_ref) <= RTOL, max_norm_rel(du, du_ref)
+    for v in range(6):
+        s = np.abs(du_ref[..., v]).max()
+        assert np.abs(du[..., v] - du_ref[..., v]).max() <= 1e-11 * s, v
+    semi.close()
+
+
+def test_gpu_reproduces_nonhydrostatic_gravity_waves_golden(tg, orc, gpu_lib):
+    """test/test_2d_moist_euler.jl:59-84 with every SSPRK33 stage on the GPU
+    (CFL 0.2, t = 0.1); error norms by the oracle and on the device."""
+    from test_oracle_moist import NONHYDROSTATIC_GRAVITY_WAVES, gravity_wave_mesh
+    eq, mesh, semi = gravity_wave_semi(tg)
+    *_, arrays = gravity_wave_mesh(tg)
+    semi.set_state(semi.compute_coefficients())
+    t, t_end = 0.0, 0.1
+    while t < t_end - 1e-15:
+        dt = 0.2 * semi.max_dt()
+        if t + dt >= t_end:
+            t = semi.rk_steps(1, fixed_dt=t_end - t, t=t, method="SSPRK33")
+        else:
+            t = semi.rk_steps(1, cfl=0.2, t=t, method="SSPRK33")
+    assert abs(t - t_end) < 1e-13
+    u = semi.get_state()
+    c = orc.Moist2D(3, 0, 0, 0, 0, 0, 0, surface_kind=0, source_kind=5, c_lmars=360.0,
+                    gravity=9.80616, ic_kind=3, mesh=arrays)
+    l2, linf = c.errors(u, t)
+    check_golden(l2, linf, NONHYDROSTATIC_GRAVITY_WAVES)
+    l2d, linfd = semi.calc_error_norms(t)
+    check_golden(l2d, linfd, NONHYDROSTATIC_GRAVITY_WAVES)
+    uo = np.ascontiguousarray(semi.compute_coefficients())
+    assert c.ssp_steps(uo, 0.0, 0.2, 10 ** 6, 2, t_end=0.1) == 0.1
+    assert max_norm_rel(u, uo) <= 1e-13
+    semi.close()

@@ -16,9 +16,13 @@ polydeg 3, element_local_mapping = true) run to t = 1 day with CK2N54:
     collocation-derivative Christoffel symbols;
   * elixir_isolated_mountain (:42-54): as Rossby-Haurwitz, dual-number
     Christoffel symbols, bottom topography;
-  * elixir_well_balanced (:90-101): l2 = linf = 0 at atol 1e-11, CFL 0.1.
+  * elixir_well_balanced (:90-101): l2 = linf = 0 at atol 1e-11, CFL 0.1;
+  * elixir_barotropic_instability (:78-89): Galewsky et al.'s jet, as
+    Rossby-Haurwitz but with dual-number Christoffel symbols; its height
+    integral by composite Gauss-Legendre quadrature instead of QuadGK.
 Tolerance: Trixi's @test_trixi_include defaults (atol 500 eps, rtol sqrt(eps)).
-Geostrophic balance, isolated mountain and well-balanced agree to 2.5e-9.  The
+Geostrophic balance, isolated mountain, well-balanced and barotropic
+instability agree to 3.8e-9.  The
 two cases with meridional flow, unsteady solid-body rotation and Rossby-Haurwitz,
 deviate systematically by 5.8e-8 and 5.5e-8 (1e-14 noise in the geometry moves
 them by < 2e-12, so this is not rounding); the cause is not found, and they are
@@ -45,6 +49,8 @@ GOLDEN = {
     "isolated_mountain": ([13.18894432799001, 0.005698447961168719, 0.007624217062402512],
                           [116.645494528163, 0.052086295524203324, 0.07855675891709994]),
     "well_balanced": ([0.0, 0.0, 0.0], [0.0, 0.0, 0.0]),
+    "barotropic_instability": ([21.08826693663232, 0.03006187671520436, 0.023421745045307123],
+                               [122.9994523425994, 0.17997299389835533, 0.16659612583251238]),
 }
 
 
@@ -70,6 +76,8 @@ def case(tg, name):
     if name == "isolated_mountain":
         return (split, cv.initial_condition_isolated_mountain, ec, 0.4, None,
                 cv.bottom_topography_isolated_mountain)
+    if name == "barotropic_instability":
+        return (split, cv.initial_condition_barotropic_instability, ec, 0.4, None, None)
     return (split, cv.initial_condition_well_balanced(), dict(ec, surf_nc=1), 0.1, None,
             cv.bottom_topography_isolated_mountain)
 
@@ -136,3 +144,29 @@ def test_cubed_sphere_mesh_and_metric(tg):
             mesh, basis, eq, cv.MetricTermsCovariantSphere(cv.ChristoffelSymbolsCollocationDerivative()))
         scale = np.abs(aux[..., 20:26]).max()
         assert np.abs(aux_c[..., 20:26] - aux[..., 20:26]).max() < 0.05 * scale
+
+
+def test_galewsky_height_is_in_gradient_wind_balance(tg):
+    """The Galewsky height (reference_data.jl:427-474) solves
+    dh/dlat = -(a/g) u (2 Omega sin + u tan / a) with h = 10158 m at the pole:
+    checked by a sixth-order central difference of the quadrature, away from
+    the perturbation (which lives near lon = 0)."""
+    cv = tg.covariant
+    from trixiatmo_gb300.initial_conditions import (EARTH_GRAVITATIONAL_ACCELERATION as G,
+                                                    EARTH_RADIUS as A, EARTH_ROTATION_RATE as OM)
+    eq = cv.SplitCovariantShallowWaterEquations2D(G, OM, cv.GlobalSphericalCoordinates())
+    lat = np.linspace(0.3, 1.3, 41)
+    lon = np.pi - 0.01
+
+    def height(la):
+        x = A * np.stack([np.cos(la) * np.cos(lon), np.cos(la) * np.sin(lon), np.sin(la)], -1)
+        return cv.initial_condition_barotropic_instability(x, 0.0, eq)[..., 0]
+
+    d = 1e-3
+    c = np.array([-1, 9, -45, 0, 45, -9, 1]) / 60.0
+    dh = sum(ck * height(lat + (k - 3) * d) for k, ck in enumerate(c)) / d
+    u = cv.galewsky_velocity(lat)
+    rhs = -(A / G) * u * (2 * OM * np.sin(lat) + u * np.tan(lat) / A)
+    assert np.abs(dh - rhs).max() <= 1e-6 * np.abs(rhs).max()
+    assert abs(height(np.array([np.pi / 2 - 1e-9]))[0] - 10158.0) < 1e-9
+    assert np.all(u[(lat <= np.pi / 7) | (lat >= np.pi / 2 - np.pi / 7)] == 0)

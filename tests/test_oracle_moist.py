@@ -10,7 +10,13 @@ test/test_2d_moist_euler.jl:
     elixir_gemein_source_terms.jl with polydeg 3 and 10x8 cells, flux_chandrashekar
     as volume and surface flux, the moist convergence source (phase change);
   * "elixir_gemein_source_terms dry" (:126-150): examples/euler/dry_air/tests/
-    elixir_gemein_source_terms.jl, weak form, flux_lax_friedrichs, gravity 0.
+    elixir_gemein_source_terms.jl, weak form, flux_lax_friedrichs, gravity 0;
+  * "elixir_gemein_nonhydrostatic_gravity_waves" (:59-84):
+    examples/euler/dry_air/buoyancy/elixir_gemein_nonhydrostatic_gravity_waves.jl
+    with polydeg 3 and 10x8 cells: a StructuredMesh whose bottom face is a
+    witch-of-Agnesi hill (transfinite mapping of four face curves),
+    flux_chandrashekar / FluxLMARS(360), geopotential + phase change + Rayleigh
+    sponge sources, slip walls, SSPRK33 at CFL 0.2 to t = 0.1.
 Tolerances are Trixi's @test_trixi_include defaults (atol 500 eps, rtol sqrt(eps)).
 The P4estMesh of the first test is affine, so the StructuredMesh of the same
 64x64 elements with outward-normal wall semantics has the same nodes, metric
@@ -74,6 +80,96 @@ def test_oracle_moist_golden(orc, name):
     assert abs(t - 0.1) < 1e-15
     l2, linf = c.errors(u, t)
     check_golden(l2, linf, golden, 5e-8 if name == "dry_bubble" else RTOL)
+
+
+NONHYDROSTATIC_GRAVITY_WAVES = (
+    [3.54205348345642e-5, 0.00212660009365362, 0.011728423281347147, 9.898615652683135, 0.0, 0.0],
+    [0.0017602402189631494, 0.1494206825191764, 0.5945421207691134, 489.9007739148801, 0.0, 0.0])
+
+
+def gravity_wave_faces():
+    """The elixir's four face curves (:81-92): periodic sides at x = +-20 km, the
+    hill h a^2 / (x^2 + a^2) (h = 400 m, a = 1 km, shifted to 0 at the sides)
+    at the bottom, a flat top at 16 km."""
+    def f1(s):
+        return -20000.0 + 0.0 * s, 8000 * s + 8000
+
+    def f2(s):
+        return 20000.0 + 0.0 * s, 8000 * s + 8000
+
+    def f3(s):
+        return (20000 * s, 400 * 1000.0 ** 2 * (1.0 / ((20000 * s) ** 2 + 1000 ** 2)) -
+                400 * 1000.0 ** 2 * (1.0 / (20000 ** 2 + 1000 ** 2)))
+
+    def f4(s):
+        return 20000 * s, 16000.0 + 0.0 * s
+    return f1, f2, f3, f4
+
+
+def gravity_wave_mesh(tg, cells=(10, 8), polydeg=3):
+    """(mesh, basis, node coordinates, contravariant vectors, inverse Jacobian,
+    oracle mesh arrays) with StructuredMesh slip walls at the bottom and top."""
+    mesh = tg.StructuredMesh(cells, periodicity=(True, False), faces=gravity_wave_faces())
+    basis = tg.LobattoLegendreBasis(polydeg)
+    xy, Ja, invJ = mesh.geometry(basis)
+    ie, ifc, fl, be, bf = mesh.connectivity().arrays()
+    bk = np.full(len(be), 1, dtype=np.int32)
+    return mesh, basis, xy, Ja, invJ, (xy, Ja, invJ, ie, ifc, fl, be, bf, bk)
+
+
+def test_transfinite_mapping_reproduces_faces_and_rectangles(tg):
+    """The Coons patch of four straight faces of a rectangle is the affine map;
+    of the gravity-wave faces it reproduces each face curve on its side."""
+    from trixiatmo_gb300.meshes import transfinite_mapping
+    m = transfinite_mapping((lambda s: (0.0 * s - 3.0, 2.0 * s + 1.0),
+                             lambda s: (0.0 * s + 5.0, 2.0 * s + 1.0),
+                             lambda s: (4.0 * s + 1.0, 0.0 * s - 1.0),
+                             lambda s: (4.0 * s + 1.0, 0.0 * s + 3.0)))
+    xi, eta = np.meshgrid(np.linspace(-1, 1, 7), np.linspace(-1, 1, 5))
+    x, y = m(xi, eta)
+    assert np.allclose(x, 1.0 + 4.0 * xi, atol=1e-14) and np.allclose(y, 1.0 + 2.0 * eta, atol=1e-14)
+    faces = gravity_wave_faces()
+    m = transfinite_mapping(faces)
+    s = np.linspace(-1, 1, 33)
+    for f, (a, b) in zip(faces, ((-1.0, s), (1.0, s), (s, -1.0), (s, 1.0))):
+        a, b = np.broadcast_arrays(a, b)
+        assert np.allclose(np.stack(m(a, b)), np.stack(np.broadcast_arrays(*f(s))), rtol=0,
+                           atol=1e-11)
+
+
+def test_oracle_nonhydrostatic_gravity_waves_golden(tg, orc):
+    mesh, basis, xy, Ja, invJ, arrays = gravity_wave_mesh(tg)
+    assert abs(xy[..., 1].min()) < 1e-9 and (invJ > 0).all()
+    c = orc.Moist2D(3, 0, 0, 0, 0, 0, 0, surface_kind=0, source_kind=5, c_lmars=360.0,
+                    gravity=9.80616, ic_kind=3, mesh=arrays)
+    eq = tg.CompressibleMoistEulerEquations2D(c_pd=1004, c_vd=717, c_pv=1885, c_vv=1424,
+                                              gravity=9.80616)
+    u = np.ascontiguousarray(tg.initial_condition_nonhydrostatic_gravity_wave(xy, 0.0, eq))
+    assert np.abs(u - c.initial_condition()).max() <= 1e-14 * np.abs(u).max()
+    t = c.ssp_steps(u, 0.0, 0.2, 10 ** 6, 2, t_end=0.1)
+    assert abs(t - 0.1) < 1e-15
+    l2, linf = c.errors(u, t)
+    check_golden(l2, linf, NONHYDROSTATIC_GRAVITY_WAVES)
+
+
+def test_rayleigh_sponge(orc, tg):
+    """source_terms_nonhydrostatic_rayleigh_sponge (compressible_moist_euler_2d.jl:346-373)
+    through the oracle's rhs: zero below z_s = 9 km, relaxing (v1, v2) to (10, 0)
+    with tau = sin^2((z - z_s) / (2 (z_top - z_s))) / 2 above it."""
+    mesh, basis, xy, Ja, invJ, arrays = gravity_wave_mesh(tg, cells=(4, 4), polydeg=2)
+    kw = dict(surface_kind=0, c_lmars=360.0, gravity=9.80616, ic_kind=3, mesh=arrays)
+    with_sponge = orc.Moist2D(2, 0, 0, 0, 0, 0, 0, source_kind=5, **kw)
+    without = orc.Moist2D(2, 0, 0, 0, 0, 0, 0, source_kind=2, **kw)
+    u = with_sponge.initial_condition()
+    u[..., 1] *= 1.3
+    u[..., 2] = 0.2 * u[..., 0]
+    d = with_sponge.rhs(u) - without.rhs(u)
+    z = xy[..., 1]
+    tau = np.where(z > 9000.0, 0.5 * np.sin(0.5 * (z - 9000.0) / 7000.0) ** 2, 0.0)
+    assert np.allclose(d[..., 1], -tau * u[..., 0] * (u[..., 1] / u[..., 0] - 10.0), rtol=1e-9,
+                       atol=1e-9)
+    assert np.allclose(d[..., 2], -tau * u[..., 0] * 0.2, rtol=1e-9, atol=1e-9)
+    assert np.all(d[..., [0, 3, 4, 5]] == 0) and np.all(d[z <= 9000.0] == 0)
 
 
 def test_chandrashekar_consistency(orc):

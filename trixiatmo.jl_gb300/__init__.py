@@ -20,6 +20,7 @@ from .equations import (CompressibleEulerEnergyEquationsWithGravity2D,
                         CompressibleMoistEulerEquations2D, flux_chandrashekar,
                         source_terms_geopotential, source_terms_moist_bubble,
                         source_terms_convergence_test_dry, source_terms_convergence_test_moist,
+                        source_terms_nonhydrostatic_gravity_wave,
                         CompressibleEulerPotentialTemperatureEquationsWithGravity2D,
                         CompressibleEulerPotentialTemperatureEquationsWithGravity3D,
                         CompressibleEulerInternalEnergyEquationsWithGravity2D,
@@ -35,7 +36,8 @@ from .initial_conditions import (EARTH_GRAVITATIONAL_ACCELERATION, EARTH_RADIUS,
                                  initial_condition_adiabatic,
                                  initial_condition_gemein_bubble,
                                  initial_condition_convergence_test_dry,
-                                 initial_condition_convergence_test_moist)
+                                 initial_condition_convergence_test_moist,
+                                 initial_condition_nonhydrostatic_gravity_wave)
 from .meshes import P4estMesh, StructuredMesh
 from .meshes3d import P4estMeshCubedSphereTopography
 from .semidiscretization import (DGSEM, SemidiscretizationCovariant,
@@ -60,7 +62,8 @@ __all__ = [
     "source_terms_convergence_test_moist", "initial_condition_gemein_bubble",
     "initial_condition_convergence_test_dry", "initial_condition_convergence_test_moist",
     "P4estMesh", "covariant", "SemidiscretizationCovariant", "initial_condition_adiabatic",
-    "SemidiscretizationCovariantEnsemble",
+    "SemidiscretizationCovariantEnsemble", "source_terms_nonhydrostatic_gravity_wave",
+    "initial_condition_nonhydrostatic_gravity_wave",
     "CompressibleEulerPotentialTemperatureEquationsWithGravity2D",
     "CompressibleEulerPotentialTemperatureEquationsWithGravity3D",
     "CompressibleEulerInternalEnergyEquationsWithGravity2D", "flux_conservative_etec",

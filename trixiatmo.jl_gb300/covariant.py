@@ -560,6 +560,58 @@ def initial_condition_unsteady_solid_body_rotation(x, t, equations):
     return np.stack([H, v[..., 0], v[..., 1], v[..., 2], b], -1)
 
 
+def galewsky_velocity(lat, u0=80.0, lat0=np.pi / 7, lat1=np.pi / 2 - np.pi / 7):
+    """Zonal jet of Galewsky et al. (2004) (reference_data.jl:461-469): a
+    C-infinity bump supported on (lat0, lat1)."""
+    lat = np.asarray(lat, dtype=np.float64)
+    inside = (lat0 < lat) & (lat < lat1)
+    lc = np.where(inside, lat, 0.5 * (lat0 + lat1))
+    u = u0 / math.exp(-4.0 / (lat1 - lat0) ** 2) * np.exp(1.0 / (lc - lat0) * 1.0 / (lc - lat1))
+    return np.where(inside, u, 0.0)
+
+
+def _galewsky_height_integrals(lat, panels=64, order=16):
+    """(I1, I2) with the integral of galewsky_integrand (reference_data.jl:471-474)
+    from pi/2 to lat equal to I1 + I2 / a:
+    I1 = int u 2 Omega sin, I2 = int u^2 tan.  The reference integrates
+    adaptively (QuadGK); here a composite Gauss-Legendre rule (`panels` panels
+    of `order` points) over [max(lat, lat0), lat1], the jet's support, which
+    is exact to rounding for this smooth integrand (doubling the panels moves
+    the result by < 1e-15 relative)."""
+    lat0, lat1 = np.pi / 7, np.pi / 2 - np.pi / 7
+    xg, wg = np.polynomial.legendre.leggauss(order)
+    s = ((np.arange(panels)[:, None] + 0.5 * (xg[None, :] + 1.0)) / panels).ravel()
+    ws = (np.broadcast_to(wg, (panels, order)) / (2.0 * panels)).ravel()
+    flat = np.asarray(lat, dtype=np.float64).ravel()
+    I1 = np.zeros_like(flat)
+    I2 = np.zeros_like(flat)
+    for c0 in range(0, flat.size, 4096):
+        lo = np.clip(flat[c0:c0 + 4096], lat0, lat1)
+        length = lat1 - lo
+        q = lo[:, None] + length[:, None] * s[None, :]
+        u = galewsky_velocity(q)
+        I1[c0:c0 + 4096] = -(u * 2 * EARTH_ROTATION_RATE * np.sin(q)) @ ws * length
+        I2[c0:c0 + 4096] = -(u * u * np.tan(q)) @ ws * length
+    shape = np.shape(lat)
+    return I1.reshape(shape), I2.reshape(shape)
+
+
+def initial_condition_barotropic_instability(x, t, equations):
+    """Galewsky et al. (2004) barotropic instability (reference_data.jl:427-459):
+    the balanced zonal jet with the height
+    h_0 = 10158 - a/g int_{pi/2}^{lat} u (2 Omega sin + u tan / a), a the
+    node's radius, plus the 120 m perturbation at lat_2 = pi/4 for
+    -pi < lon < pi."""
+    lon, lat, a = _lonlat(x)
+    vlon = galewsky_velocity(lat)
+    I1, I2 = _galewsky_height_integrals(lat)
+    h = 10158.0 - a / EARTH_GRAVITATIONAL_ACCELERATION * (I1 + I2 / a)
+    alpha, beta, lat2 = 1.0 / 3.0, 1.0 / 15.0, np.pi / 4
+    pert = 120.0 * np.cos(lat) * np.exp(-((lon / alpha) ** 2)) * np.exp(-((lat2 - lat) / beta) ** 2)
+    h = np.where((-np.pi < lon) & (lon < np.pi), h + pert, h)
+    return _spherical_out(h, vlon, np.zeros_like(h), np.zeros_like(h), x, equations)
+
+
 def initial_condition_well_balanced(H=5960.0):
     """The constant total height at rest of examples/shallow_water/covariant/elixir_well_balanced.jl."""
     def ic(x, t, equations):

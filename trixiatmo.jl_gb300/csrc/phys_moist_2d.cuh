@@ -242,6 +242,22 @@ struct PhysMoist2D {
       bubble_source(P, u, P.source == TAG_SRC_MOIST_BUBBLE, s);
       return;
     }
+    if (P.source == TAG_SRC_MOIST_GRAVITY_WAVE) {
+      // + source_terms_nonhydrostatic_rayleigh_sponge (:346-373): relax the
+      // velocity to (10, 0) above z_s = 9 km with
+      // tau = 1/2 sin^2((z - z_s) / (2 (z_top - z_s))), z_top = 16 km
+      bubble_source(P, u, true, s);
+      const double z = x[1];
+      double tau = 0.0;
+      if (z > 9000.0) {
+        const double sn = sin(0.5 * (z - 9000.0) * (1.0 / (16000.0 - 9000.0)));
+        tau = 0.5 * (sn * sn);
+      }
+      const double v1 = u[1] / u[0], v2 = u[2] / u[0];
+      s[1] += -tau * u[0] * (v1 - 10.0);
+      s[2] += -tau * u[0] * (v2 - 0.0);
+      return;
+    }
     if (P.source != TAG_SRC_MOIST_CONVERGENCE_DRY && P.source != TAG_SRC_MOIST_CONVERGENCE) {
 #pragma unroll
       for (int v = 0; v < 6; ++v) s[v] = 0.0;

@@ -731,11 +731,12 @@ const char* check_equations(const tag_config* cfg) {
         return "unsupported flux combination for the moist equations";
       const double k = cfg->params[6];
       if (k != 0 && k != TAG_SRC_GEOPOTENTIAL && k != TAG_SRC_MOIST_BUBBLE &&
-          k != TAG_SRC_MOIST_CONVERGENCE_DRY && k != TAG_SRC_MOIST_CONVERGENCE)
+          k != TAG_SRC_MOIST_CONVERGENCE_DRY && k != TAG_SRC_MOIST_CONVERGENCE &&
+          k != TAG_SRC_MOIST_GRAVITY_WAVE)
         return "unsupported source kind for the moist equations";
-      if ((k == TAG_SRC_MOIST_CONVERGENCE_DRY || k == TAG_SRC_MOIST_CONVERGENCE) &&
-          !cfg->node_coordinates)
-        return "the convergence-test source needs node coordinates";
+      if ((k == TAG_SRC_MOIST_CONVERGENCE_DRY || k == TAG_SRC_MOIST_CONVERGENCE ||
+           k == TAG_SRC_MOIST_GRAVITY_WAVE) && !cfg->node_coordinates)
+        return "this source needs node coordinates";
       if (sf == TAG_SF_LMARS && !(cfg->params[5] > 0.0))
         return "FluxLMARS needs a positive speed of sound";
       return nullptr;

@@ -300,6 +300,12 @@ source_terms_convergence_test_dry = _Source("source_terms_convergence_test_dry",
                                             _lib.TAG_SRC_MOIST_CONVERGENCE_DRY)
 source_terms_convergence_test_moist = _Source("source_terms_convergence_test_moist",
                                               _lib.TAG_SRC_MOIST_CONVERGENCE)
+# source_terms_geopotential + source_terms_phase_change +
+# source_terms_nonhydrostatic_rayleigh_sponge (:346-373), the sum the
+# nonhydrostatic gravity-wave elixir defines
+# (examples/euler/dry_air/buoyancy/elixir_gemein_nonhydrostatic_gravity_waves.jl:50-56)
+source_terms_nonhydrostatic_gravity_wave = _Source("source_terms_nonhydrostatic_gravity_wave",
+                                                   _lib.TAG_SRC_MOIST_GRAVITY_WAVE)
 
 
 def speed_of_sound_isothermal(equations, T0):

@@ -272,6 +272,26 @@ def initial_condition_gemein_bubble(x, t, equations):
                     axis=-1)
 
 
+def initial_condition_nonhydrostatic_gravity_wave(x, t, equations):
+    """Mountain-triggered gravity wave (Gallus & Klemp 2000) of
+    examples/euler/dry_air/buoyancy/elixir_gemein_nonhydrostatic_gravity_waves.jl:15-39
+    for the moist equations without moisture: constant Brunt-Vaisala frequency
+    N = 0.01 over theta_0 = T_0 = 280 K, hydrostatic pressure, uniform
+    v1 = 10 m/s."""
+    eq = equations
+    z = x[..., 1]
+    theta_0, N = 280.0, 0.01
+    theta = theta_0 * np.exp(N * N * z / eq.g)
+    p = eq.p_0 * (1.0 + eq.g * eq.g * (1.0 / (eq.c_pd * theta_0 * (N * N))) *
+                  (np.exp(-z * (N * N) / eq.g) - 1.0)) ** (1.0 / eq.kappa)
+    rho = p / ((p / eq.p_0) ** eq.kappa * eq.R_d * theta)
+    T = p / (eq.R_d * rho)
+    v1, v2 = 10.0, 0.0
+    z0 = np.zeros_like(rho)
+    return np.stack([rho, rho * v1, rho * v2, rho * eq.c_vd * T + 0.5 * rho * (v1 * v1 + v2 * v2),
+                     z0, z0], axis=-1)
+
+
 def initial_condition_convergence_test_dry(x, t, equations):
     """src/equations/compressible_moist_euler_2d.jl:173-200."""
     eq = equations

@@ -39,15 +39,49 @@ class Connectivity:
         return ie, ifc, fl, be, bf
 
 
+def transfinite_mapping(faces):
+    """The Coons patch (transfinite interpolation) of four boundary curves, as
+    `Trixi.StructuredMesh(cells_per_dimension, faces)` builds its mapping:
+    faces = (xi = -1, xi = +1, eta = -1, eta = +1) curves, each s -> (x, y)
+    for s in [-1, 1], meeting at the corners.  The mapping is the sum of the
+    linear blends between opposite faces minus the bilinear blend of the four
+    corners, so that it reproduces every face exactly."""
+    f1, f2, f3, f4 = faces
+
+    def pt(f, s):
+        x, y = f(s)
+        return np.asarray(x, dtype=np.float64), np.asarray(y, dtype=np.float64)
+
+    c00, c10 = pt(f1, -1.0), pt(f2, -1.0)  # bottom left / right
+    c01, c11 = pt(f1, 1.0), pt(f2, 1.0)    # top left / right
+
+    def mapping(xi, eta):
+        out = []
+        a1, a2, b3, b4 = pt(f1, eta), pt(f2, eta), pt(f3, xi), pt(f4, xi)
+        for d in range(2):
+            lin_xi = 0.5 * ((1.0 - xi) * a1[d] + (1.0 + xi) * a2[d])
+            lin_eta = 0.5 * ((1.0 - eta) * b3[d] + (1.0 + eta) * b4[d])
+            bil = 0.25 * (c00[d] * (1.0 - xi) * (1.0 - eta) + c10[d] * (1.0 + xi) * (1.0 - eta) +
+                          c01[d] * (1.0 - xi) * (1.0 + eta) + c11[d] * (1.0 + xi) * (1.0 + eta))
+            out.append(lin_xi + lin_eta - bil)
+        return tuple(out)
+
+    return mapping
+
+
 class StructuredMesh:
-    """2D StructuredMesh on [xmin, xmax] x [ymin, ymax] (or a mapping)."""
+    """2D StructuredMesh on [xmin, xmax] x [ymin, ymax], or of a mapping
+    (xi, eta) in [-1, 1]^2 -> (x, y), or of four boundary curves `faces`
+    (transfinite_mapping)."""
 
     ndims = 2
 
     def __init__(self, cells_per_dimension, coordinates_min=None, coordinates_max=None,
-                 periodicity=(True, True), mapping=None):
+                 periodicity=(True, True), mapping=None, faces=None):
         self.nx, self.ny = map(int, cells_per_dimension)
         self.periodicity = tuple(bool(p) for p in periodicity)
+        if faces is not None:
+            mapping = transfinite_mapping(faces)
         if mapping is None:
             x0, y0 = map(float, coordinates_min)
             x1, y1 = map(float, coordinates_max)

@@ -111,7 +111,8 @@ def _flux_ids(equations, solver, source_terms=None):
             raise ValueError(f"unsupported source terms {source_terms}")
         src = 0 if source_terms is None else source_terms.kind
         if src not in (0, _lib.TAG_SRC_GEOPOTENTIAL, _lib.TAG_SRC_MOIST_BUBBLE,
-                       _lib.TAG_SRC_MOIST_CONVERGENCE_DRY, _lib.TAG_SRC_MOIST_CONVERGENCE):
+                       _lib.TAG_SRC_MOIST_CONVERGENCE_DRY, _lib.TAG_SRC_MOIST_CONVERGENCE,
+                       _lib.TAG_SRC_MOIST_GRAVITY_WAVE):
             raise ValueError(f"{source_terms} is not a source of the moist equations")
         eq = equations
         return vid, sid, [eq.c_pd, eq.c_vd, eq.c_pv, eq.c_vv, eq.g, c_lmars, float(src)]
