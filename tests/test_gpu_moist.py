@@ -231,3 +231,32 @@ def test_gpu_reproduces_nonhydrostatic_gravity_waves_golden(tg, orc, gpu_lib):
     assert c.ssp_steps(uo, 0.0, 0.2, 10 ** 6, 2, t_end=0.1) == 0.1
     assert max_norm_rel(u, uo) <= 1e-13
     semi.close()
+
+
+def test_gpu_reproduces_moist_bubble_golden(tg, orc, gpu_lib):
+    """test/test_2d_moist_euler.jl:32-57 (Bryan & Fritsch moist bubble on the
+    saturated AtmosphereLayers background, 16x8 StructuredMesh, N = 3, slip
+    walls all round) with every CK2N54 stage on the GPU; norms by NumPy and on
+    the device; the state against the oracle's run."""
+    import analysis
+    from test_oracle_moist import check_moist_bubble, moist_bubble_ic, moist_bubble_mesh
+    eq = tg.CompressibleMoistEulerEquations2D(**CP, gravity=9.80616)
+    ic = moist_bubble_ic(tg, eq)
+    mesh, basis, xy, Ja, invJ, arrays = moist_bubble_mesh(tg)
+    solver = tg.DGSEM(3, tg.FluxLMARS(360.0),
+                      tg.VolumeIntegralFluxDifferencing(tg.flux_chandrashekar))
+    wall = tg.boundary_condition_slip_wall
+    semi = tg.SemidiscretizationHyperbolic(
+        mesh, eq, ic, solver, source_terms=tg.source_terms_moist_bubble,
+        boundary_conditions={"x_neg": wall, "x_pos": wall, "y_neg": wall, "y_pos": wall})
+    u, t = _gpu_golden_run(tg, semi, 0.2, 0.1)
+    l2, linf = analysis.error_norms(u, xy, invJ, basis.nodes, lambda x: ic(x, 0.0, eq), 2)
+    check_moist_bubble(l2, linf)
+    l2d, linfd = semi.calc_error_norms(t)
+    check_moist_bubble(l2d, linfd)
+    c = orc.Moist2D(3, 0, 0, 0, 0, 0, 0, surface_kind=0, source_kind=2, c_lmars=360.0,
+                    gravity=9.80616, mesh=arrays)
+    uo = np.ascontiguousarray(ic(xy, 0.0, eq))
+    c.ck_steps(uo, np.zeros_like(uo), 0.0, 0.2, 100000, 0.0, 0.1)
+    assert max_norm_rel(u, uo) <= 1e-13
+    semi.close()

@@ -16,7 +16,17 @@ test/test_2d_moist_euler.jl:
     with polydeg 3 and 10x8 cells: a StructuredMesh whose bottom face is a
     witch-of-Agnesi hill (transfinite mapping of four face curves),
     flux_chandrashekar / FluxLMARS(360), geopotential + phase change + Rayleigh
-    sponge sources, slip walls, SSPRK33 at CFL 0.2 to t = 0.1.
+    sponge sources, slip walls, SSPRK33 at CFL 0.2 to t = 0.1;
+  * "elixir_gemein_bubble moist" (:32-57): examples/euler/moist_air/buoyancy/
+    elixir_gemein_bubble.jl with polydeg 3 and 16x8 cells: Bryan & Fritsch's
+    moist bubble on a saturated background (AtmosphereLayers: a nonlinear solve
+    per 10 m layer), slip walls on all four sides, source_terms_moist_bubble,
+    CK2N54 at CFL 0.2 to t = 0.1.  The reference solves the layers with NLsolve
+    (residual tolerance 1e-8), the host mirror by Newton to the last bits; all
+    norms agree to 3e-9 relative except the linf of rho_v1, a 1.2e-6 quantity
+    at t = 0.1 (noise of the at-rest state), which deviates by 1.7e-13
+    absolute (3e-11 of max|rho_v2|), above Trixi's atol of 500 eps: that
+    entry is checked at atol 2e-13.
 Tolerances are Trixi's @test_trixi_include defaults (atol 500 eps, rtol sqrt(eps)).
 The P4estMesh of the first test is affine, so the StructuredMesh of the same
 64x64 elements with outward-normal wall semantics has the same nodes, metric
@@ -170,6 +180,83 @@ def test_rayleigh_sponge(orc, tg):
                        atol=1e-9)
     assert np.allclose(d[..., 2], -tau * u[..., 0] * 0.2, rtol=1e-9, atol=1e-9)
     assert np.all(d[..., [0, 3, 4, 5]] == 0) and np.all(d[z <= 9000.0] == 0)
+
+
+MOIST_BUBBLE = (
+    [7.3515680983123215e-6, 1.1067008939664827e-7, 0.0006971968385493199, 1.715939603224655,
+     8.832720252288771e-7, 1.025736269959355e-6],
+    [8.056395313560394e-5, 1.1981461033088162e-6, 0.0058959697735631155, 19.248694115842227,
+     1.0043632092967755e-5, 1.1439573103299433e-5])
+
+
+def check_moist_bubble(l2, linf):
+    g2, gi = MOIST_BUBBLE
+    for v in range(6):
+        assert close(l2[v], g2[v]), ("l2", v, l2[v], g2[v])
+        if v == 1:
+            assert abs(linf[v] - gi[v]) <= 2e-13, ("linf", v, linf[v], gi[v])
+        else:
+            assert close(linf[v], gi[v]), ("linf", v, linf[v], gi[v])
+
+
+_LAYERS = {}
+
+
+def moist_bubble_ic(tg, eq):
+    """initial_condition_moist_bubble on the elixir's AtmosphereLayers (built once)."""
+    from trixiatmo_gb300.initial_conditions import AtmosphereLayers, initial_condition_moist_bubble
+    if "layers" not in _LAYERS:
+        _LAYERS["layers"] = AtmosphereLayers(eq)
+    return initial_condition_moist_bubble(_LAYERS["layers"])
+
+
+def moist_bubble_mesh(tg, polydeg=3, cells=(16, 8)):
+    mesh = tg.StructuredMesh(cells, (0.0, 0.0), (20000.0, 10000.0), periodicity=(False, False))
+    basis = tg.LobattoLegendreBasis(polydeg)
+    xy, Ja, invJ = mesh.geometry(basis)
+    ie, ifc, fl, be, bf = mesh.connectivity().arrays()
+    bk = np.full(len(be), 1, dtype=np.int32)
+    return mesh, basis, xy, Ja, invJ, (xy, Ja, invJ, ie, ifc, fl, be, bf, bk)
+
+
+def test_atmosphere_layers_solve_the_layer_equations(tg):
+    """Every tabulated layer is a root of the reference's seven layer equations
+    (moist_state, compressible_moist_euler_2d.jl:1009-1034) to rounding, is
+    saturated with liquid water present, and the table is hydrostatic."""
+    from trixiatmo_gb300.initial_conditions import AtmosphereLayers
+    eq = tg.CompressibleMoistEulerEquations2D(c_pd=1004, c_vd=717, c_pv=1885, c_vv=1424,
+                                              gravity=9.80616)
+    y0 = np.array([1e5, 1.4, 320.0, 0.02, 0.02, 0.028, 320.0])
+    y = y0
+    for dz in (0.01, 10.0, 10.0):
+        y_next = AtmosphereLayers._solve(eq, y, dz, 0.02, 320.0)
+        F = AtmosphereLayers._residual(eq, y_next, y[0], dz, 0.02, 320.0)
+        # F1 = (p - p_below) / dz + g rho: rounding of p divided by dz
+        scale = np.array([y_next[0] / dz, y_next[0], 320.0, 0.02, y_next[5], 320.0, y_next[5]])
+        assert np.all(np.abs(F) <= 1e-13 * scale), F
+        y = y_next
+    if "layers" not in _LAYERS:
+        _LAYERS["layers"] = AtmosphereLayers(eq)
+    data = _LAYERS["layers"]
+    rho, rho_qv, rho_ql = data.layer_data[:, 0], data.layer_data[:, 2], data.layer_data[:, 3]
+    assert data.layer_data.shape == (1002, 4)
+    assert np.all(rho_ql > 0) and np.all(np.diff(rho) < 0)
+    assert np.allclose((rho_qv + rho_ql) / (rho - rho_qv - rho_ql), 0.02, rtol=1e-12)
+
+
+def test_oracle_moist_bubble_golden(tg, orc):
+    import analysis
+    eq = tg.CompressibleMoistEulerEquations2D(c_pd=1004, c_vd=717, c_pv=1885, c_vv=1424,
+                                              gravity=9.80616)
+    ic = moist_bubble_ic(tg, eq)
+    mesh, basis, xy, Ja, invJ, arrays = moist_bubble_mesh(tg)
+    c = orc.Moist2D(3, 0, 0, 0, 0, 0, 0, surface_kind=0, source_kind=2, c_lmars=360.0,
+                    gravity=9.80616, mesh=arrays)
+    u = np.ascontiguousarray(ic(xy, 0.0, eq))
+    t = c.ck_steps(u, np.zeros_like(u), 0.0, 0.2, 100000, 0.0, 0.1)
+    assert abs(t - 0.1) < 1e-15
+    l2, linf = analysis.error_norms(u, xy, invJ, basis.nodes, lambda x: ic(x, 0.0, eq), 2)
+    check_moist_bubble(l2, linf)
 
 
 def test_chandrashekar_consistency(orc):

@@ -37,7 +37,8 @@ from .initial_conditions import (EARTH_GRAVITATIONAL_ACCELERATION, EARTH_RADIUS,
                                  initial_condition_gemein_bubble,
                                  initial_condition_convergence_test_dry,
                                  initial_condition_convergence_test_moist,
-                                 initial_condition_nonhydrostatic_gravity_wave)
+                                 initial_condition_nonhydrostatic_gravity_wave,
+                                 AtmosphereLayers, initial_condition_moist_bubble)
 from .meshes import P4estMesh, StructuredMesh
 from .meshes3d import P4estMeshCubedSphereTopography
 from .semidiscretization import (DGSEM, SemidiscretizationCovariant,
@@ -63,7 +64,8 @@ __all__ = [
     "initial_condition_convergence_test_dry", "initial_condition_convergence_test_moist",
     "P4estMesh", "covariant", "SemidiscretizationCovariant", "initial_condition_adiabatic",
     "SemidiscretizationCovariantEnsemble", "source_terms_nonhydrostatic_gravity_wave",
-    "initial_condition_nonhydrostatic_gravity_wave",
+    "initial_condition_nonhydrostatic_gravity_wave", "AtmosphereLayers",
+    "initial_condition_moist_bubble",
     "CompressibleEulerPotentialTemperatureEquationsWithGravity2D",
     "CompressibleEulerPotentialTemperatureEquationsWithGravity3D",
     "CompressibleEulerInternalEnergyEquationsWithGravity2D", "flux_conservative_etec",

@@ -312,3 +312,170 @@ def initial_condition_convergence_test_moist(x, t, equations):
     T = (ini - 1.0) / mu + 10.0 / eq.c_vd + 40.0
     E = mu * T + qv * eq.L_00 + 1.0
     return np.stack([ini, ini, ini, E * ini, qv * ini, ql * ini], axis=-1)
+
+
+class AtmosphereLayers:
+    """Saturated moist background atmosphere of constant equivalent potential
+    temperature and total water (src/equations/compressible_moist_euler_2d.jl:1009-1104),
+    tabulated every `preciseness` metres up to `total_height`.
+
+    Each layer solves the seven equations of the reference's `moist_state`
+    (:1009-1034) for y = (p, rho, T, r_t, r_v, rho_qv, theta_e): the discrete
+    hydrostatic balance (p - p_below) / dz + g rho = 0, the gas law, the
+    definition of theta_e (H = 1), r_t = r_t0, rho_qv = rho_d r_v,
+    theta_e = theta_e0, and saturation in the form a + b - sqrt(a^2 + b^2) = 0
+    (a the vapour deficit, b the liquid).  The surface layer is solved with
+    dz = 0.01 from the guess (p0, rho0, theta_e0, r_t0, r_v0, rho0 r_v0,
+    theta_e0); each next layer from the one below.  The reference calls NLsolve
+    (trust region, tolerance 1e-8 on the residual); here a damped Newton
+    iteration with a complex-step Jacobian (exact to rounding) runs to the
+    root's last bits.  layer_data[i] = (rho, rho_theta, rho_qv, rho_ql) at
+    z = i * preciseness."""
+
+    def __init__(self, equations, total_height=10010, preciseness=10, ground_state=(1.4, 100000),
+                 equivalent_potential_temperature=320, mixing_ratios=(0.02, 0.02)):
+        eq = equations
+        self.total_height = float(total_height)
+        self.preciseness = int(preciseness)
+        rho0, p0 = map(float, ground_state)
+        r_t0, r_v0 = map(float, mixing_ratios)
+        theta_e0 = float(equivalent_potential_temperature)
+        n = int(round(total_height / preciseness))
+        y = np.array([p0, rho0, theta_e0, r_t0, r_v0, rho0 * r_v0, theta_e0])
+        data = np.zeros((n + 1, 4))
+        for i in range(n + 1):
+            dz = 0.01 if i == 0 else float(preciseness)
+            y = self._solve(eq, y, dz, r_t0, theta_e0)
+            p, rho, T, r_t, r_v, rho_qv, _ = y
+            rho_d = rho / (1.0 + r_t)
+            rho_ql = rho - rho_d - rho_qv
+            kappa_M = (eq.R_d * rho_d + eq.R_v * rho_qv) / (
+                eq.c_pd * rho_d + eq.c_pv * rho_qv + eq.c_pl * rho_ql)
+            rho_theta = (rho * (p0 / p) ** kappa_M * T * (1.0 + (eq.R_v / eq.R_d) * r_v) /
+                         (1.0 + r_t))
+            data[i] = (rho, rho_theta, rho_qv, rho_ql)
+        self.layer_data = data
+
+    @staticmethod
+    def _residual(eq, y, p_below, dz, r_t0, theta_e0):
+        p, rho, T, r_t, r_v, rho_qv, theta_e = y
+        rho_d = rho / (1.0 + r_t)
+        p_d = eq.R_d * rho_d * T
+        T_C = T - 273.15
+        p_vs = 611.2 * np.exp(17.62 * T_C / (243.12 + T_C))
+        L = eq.L_00 - (eq.c_pl - eq.c_pv) * T
+        cm = eq.c_pd + eq.c_pl * r_t
+        a = p_vs / (eq.R_v * T) - rho_qv
+        b = rho - rho_qv - rho_d
+        return np.stack([(p - p_below) / dz + eq.g * rho,
+                         p - (eq.R_d * rho_d + eq.R_v * rho_qv) * T,
+                         theta_e - T * (p_d / eq.p_0) ** (-eq.R_d / cm) * np.exp(L * r_v / (cm * T)),
+                         r_t - r_t0 + 0.0 * p,
+                         rho_qv - rho_d * r_v,
+                         theta_e - theta_e0 + 0.0 * p,
+                         a + b - np.sqrt(a * a + b * b)])
+
+    @classmethod
+    def _solve(cls, eq, y0, dz, r_t0, theta_e0):
+        y = y0.copy()
+        p_below = y0[0]
+        scale = np.abs(y0) + 1e-3
+        h = 1e-30
+        for _ in range(100):
+            F = cls._residual(eq, y, p_below, dz, r_t0, theta_e0)
+            Yc = y[:, None] + 1j * h * scale[:, None] * np.eye(7)
+            J = cls._residual(eq, Yc, p_below, dz, r_t0, theta_e0).imag / (h * scale[None, :])
+            step = np.linalg.solve(J, -F)
+            nF = np.abs(F).max()
+            lam = 1.0
+            while lam > 1e-4:
+                yn = y + lam * step
+                if np.all(np.isfinite(cls._residual(eq, yn, p_below, dz, r_t0, theta_e0))) and (
+                        np.abs(cls._residual(eq, yn, p_below, dz, r_t0, theta_e0)).max() < nF
+                        or nF < 1e-9):
+                    break
+                lam *= 0.5
+            y = yn
+            if np.all(np.abs(lam * step) <= 4e-16 * np.abs(y)):
+                break
+        return y
+
+
+def _perturb_moist_profile(x, rho, rho_theta, rho_qv, rho_ql, eq):
+    """perturb_moist_profile! (compressible_moist_euler_2d.jl:1148-1206): the
+    Bryan-Fritsch bubble (2 K of density potential temperature, radius 2 km at
+    (10 km, 2 km)) at constant pressure, with the saturation adjustment by
+    fixed-point iteration to 1e-12."""
+    xc, zc, rc, dtheta = 10000.0, 2000.0, 2000.0, 2.0
+    r = np.sqrt((x[0] - xc) ** 2 + (x[1] - zc) ** 2)
+    rho_d = rho - rho_qv - rho_ql
+    kappa_M = (eq.R_d * rho_d + eq.R_v * rho_qv) / (eq.c_pd * rho_d + eq.c_pv * rho_qv +
+                                                   eq.c_pl * rho_ql)
+    p_loc = eq.p_0 * (eq.R_d * rho_theta / eq.p_0) ** (1.0 / (1.0 - kappa_M))
+    T_loc = p_loc / (eq.R_d * rho_d + eq.R_v * rho_qv)
+    rho_e = (eq.c_vd * rho_d + eq.c_vv * rho_qv + eq.c_pl * rho_ql) * T_loc + eq.L_00 * rho_qv
+    if r < rc:
+        th_dens = rho_theta / rho * (p_loc / eq.p_0) ** (kappa_M - eq.kappa)
+        th_dens_new = th_dens * (1.0 + dtheta * np.cos(np.pi * (0.5 * r / rc)) ** 2 / 300.0)
+        rt = (rho_qv + rho_ql) / rho_d
+        rv = rho_qv / rho_d
+        th_loc = th_dens_new * (1.0 + rt) / (1.0 + (eq.R_v / eq.R_d) * rv)
+        if rt > 0:
+            for _ in range(1000):
+                T_loc = th_loc * (p_loc / eq.p_0) ** eq.kappa
+                T_C = T_loc - 273.15
+                pvs = 611.2 * np.exp(17.62 * T_C / (243.12 + T_C))
+                rho_d_new = (p_loc - pvs) / (eq.R_d * T_loc)
+                rvs = pvs / (eq.R_v * rho_d_new * T_loc)
+                th_new = th_dens_new * (1.0 + rt) / (1.0 + (eq.R_v / eq.R_d) * rvs)
+                if abs(th_new - th_loc) <= th_loc * 1.0e-12:
+                    break
+                th_loc = th_new
+            else:
+                raise RuntimeError("moist bubble: saturation adjustment did not converge")
+        else:
+            rvs = 0.0
+            T_loc = th_loc * (p_loc / eq.p_0) ** eq.kappa
+            rho_d_new = p_loc / (eq.R_d * T_loc)
+        rho_qv = rvs * rho_d_new
+        rho_ql = (rt - rvs) * rho_d_new
+        rho = rho_d_new * (1.0 + rt)
+        rho_d = rho - rho_qv - rho_ql
+        rho_e = (eq.c_vd * rho_d + eq.c_vv * rho_qv + eq.c_pl * rho_ql) * T_loc + eq.L_00 * rho_qv
+    return rho, rho_e, rho_qv, rho_ql
+
+
+def initial_condition_moist_bubble(atmosphere_layers):
+    """Moist bubble of Bryan & Fritsch (2002)
+    (compressible_moist_euler_2d.jl:1106-1146): the layer data interpolated
+    linearly in z (rho; rho_theta, rho_qv, rho_ql per unit rho), then the
+    perturbation; at rest.  Returns the initial condition (x, t, equations)."""
+    layers = atmosphere_layers
+
+    def ic(x, t, equations):
+        eq = equations
+        data, dz, H = layers.layer_data, float(layers.preciseness), layers.total_height
+        flat = np.asarray(x, dtype=np.float64).reshape(-1, 2)
+        out = np.zeros((flat.shape[0], 6))
+        for k, xk in enumerate(flat):
+            z = xk[1]
+            if z > H and not np.isclose(z, H, rtol=np.sqrt(np.finfo(float).eps), atol=0.0):
+                raise ValueError("the atmosphere does not match the simulation domain")
+            n = int(np.floor((z + np.finfo(float).eps) / dz))  # 0-based layer below z
+            z_l = n * dz
+            z_r = (n + 1) * dz
+            if z_l == H:
+                z_r = z_l + dz
+                n -= 1
+            rl, thl, qvl, qll = data[n]
+            rr, thr, qvr, qlr = data[n + 1]
+            rho = (rr * (z - z_l) + rl * (z_r - z)) / dz
+            rho_theta = rho * (thr / rr * (z - z_l) + thl / rl * (z_r - z)) / dz
+            rho_qv = rho * (qvr / rr * (z - z_l) + qvl / rl * (z_r - z)) / dz
+            rho_ql = rho * (qlr / rr * (z - z_l) + qll / rl * (z_r - z)) / dz
+            rho, rho_e, rho_qv, rho_ql = _perturb_moist_profile(xk, rho, rho_theta, rho_qv,
+                                                                rho_ql, eq)
+            out[k] = (rho, 0.0, 0.0, rho_e, rho_qv, rho_ql)
+        return out.reshape(np.shape(x)[:-1] + (6,))
+
+    return ic
