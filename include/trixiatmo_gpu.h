@@ -90,6 +90,7 @@ extern "C" {
 #define TAG_SRC_MOIST_CONVERGENCE 6  /* source_terms_convergence_test_moist            */
 #define TAG_SRC_MOIST_GRAVITY_WAVE 7 /* geopotential + phase change +
                                         source_terms_nonhydrostatic_rayleigh_sponge     */
+#define TAG_SRC_RAINY_NO_PHASE_CHANGE 8 /* source_terms_no_phase_change (rainy: gravity only) */
 
 #define TAG_BC_SLIP_WALL_STRUCTURED 1 /* boundary_condition_slip_wall reached from a StructuredMesh */
 #define TAG_BC_SLIP_WALL_NORMAL 2     /* boundary_condition_slip_wall reached from a P4estMesh      */
@@ -127,7 +128,8 @@ typedef struct {
   double params[8];  /* EULER_ENERGY_2D: c_p, c_v, gravity, LMARS speed of sound;
                         EULER_ENERGY_3D: the same, then the Coriolis angular
                         velocity (0 disables the source);
-                        RAINY_2D: params[0] = TAG_SRC_* source kind;
+                        RAINY_2D: params[0] = TAG_SRC_* source kind (surface flux
+                        TAG_SF_LAX_FRIEDRICHS or TAG_SF_LMARS = flux_LMARS, c = 360);
                         MOIST_EULER_2D: c_pd, c_vd, c_pv, c_vv, gravity, LMARS
                         speed of sound, TAG_SRC_* source kind (0: none);
                         POTENTIAL_TEMPERATURE_2D: c_p, c_v, gravity, LMARS speed

@@ -129,6 +129,12 @@ def lib():
                                          ctypes.c_double]
         L.orc_moist_flux_chandrashekar.argtypes = [_dp, _dp, _dp, _dp]
         L.orc_moist_flux.argtypes = [_dp, _dp, _dp]
+        L.orc_rainy_flux_lmars.argtypes = [_dp, _dp, _dp, _dp]
+        L.orc_rainy_slip_wall.argtypes = [_dp, _dp, _dp]
+        L.orc_rainy_create_mesh.restype = ctypes.c_void_p
+        L.orc_rainy_create_mesh.argtypes = ([ctypes.c_int] * 2 + [_dp] * 3 + [ctypes.c_int] +
+                                            [_ip] * 3 + [ctypes.c_int] + [_ip] * 3 +
+                                            [ctypes.c_int] * 4)
         L.orc_rainy_create.restype = ctypes.c_void_p
         L.orc_rainy_create.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] * 4 + [ctypes.c_int] * 4
         L.orc_rainy_geometry.argtypes = [ctypes.c_void_p, _dp]
@@ -586,6 +592,21 @@ class Moist2D:
             self.h = None
 
 
+def rainy_flux_lmars(ul, ur, n):
+    f = np.zeros(9)
+    lib().orc_rainy_flux_lmars(_p(np.ascontiguousarray(ul, dtype=np.float64)),
+                               _p(np.ascontiguousarray(ur, dtype=np.float64)),
+                               _p(np.ascontiguousarray(n, dtype=np.float64)), _p(f))
+    return f
+
+
+def rainy_slip_wall(u, n):
+    f = np.zeros(9)
+    lib().orc_rainy_slip_wall(_p(np.ascontiguousarray(u, dtype=np.float64)),
+                              _p(np.ascontiguousarray(n, dtype=np.float64)), _p(f))
+    return f
+
+
 def moist_flux_chandrashekar(ul, ur, n):
     f = np.zeros(6)
     lib().orc_moist_flux_chandrashekar(_p(np.ascontiguousarray(ul, dtype=np.float64)),
@@ -604,13 +625,27 @@ def moist_flux(u, n):
 class Rainy2D:
     """Rainy Euler (flux_ec_rain / flux_lax_friedrichs, source_terms_rainy,
     simple slip walls) on a StructuredMesh rectangle, with the Newton stage
-    limiter."""
+    limiter.  source_kind 0 source_terms_rainy, 1 convergence test, 2 none,
+    3 source_terms_no_phase_change.  mesh: (xy, Ja, invJ, if_e, if_f, if_flip,
+    bd_e, bd_f, bd_kind) arrays of the host mirror instead of the rectangle,
+    with surface 0 flux_lax_friedrichs / 1 flux_LMARS and wall 0 simple /
+    1 pressure-Riemann slip walls."""
 
     nv = 9
 
     def __init__(self, polydeg, nx, ny, x0, x1, y0, y1, periodic_x=True, periodic_y=False,
-                 weak_form=False, source_kind=0):
+                 weak_form=False, source_kind=0, mesh=None, surface=0, wall=0):
         self.n = polydeg + 1
+        if mesh is not None:
+            self._keep = [np.ascontiguousarray(a, dtype=np.float64) for a in mesh[:3]]
+            self._keep += [np.ascontiguousarray(a, dtype=np.int32) for a in mesh[3:]]
+            xy, Ja, invJ, ie, ifc, fl, be, bf, bk = self._keep
+            self.nelem = invJ.shape[0]
+            self.h = lib().orc_rainy_create_mesh(polydeg, self.nelem, _p(xy), _p(Ja), _p(invJ),
+                                                 len(fl), _ip(ie), _ip(ifc), _ip(fl), len(be),
+                                                 _ip(be), _ip(bf), _ip(bk), int(weak_form),
+                                                 int(source_kind), int(surface), int(wall))
+            return
         self.nelem = nx * ny
         self.h = lib().orc_rainy_create(polydeg, nx, ny, x0, x1, y0, y1, int(periodic_x),
                                         int(periodic_y), int(weak_form), int(source_kind))

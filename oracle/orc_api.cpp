@@ -152,21 +152,32 @@ struct RainyPhys {
     return eq.flux_ec_rain(a, b, n);
   }
   State volume_noncons(const State&, const State&, const double*) const { return State{}; }
+  // surface 0: flux_lax_friedrichs, 1: flux_LMARS
+  int surface = 0;
+  // StructuredMesh walls (kind 1): 0 boundary_condition_simple_slip_wall,
+  // 1 boundary_condition_slip_wall (pressure Riemann problem)
+  int wall = 0;
   State surface_flux(const State& a, const State& b, const double* n) const {
-    return eq.flux_llf(a, b, n);
+    return surface == 1 ? eq.flux_lmars(a, b, n) : eq.flux_llf(a, b, n);
   }
   State surface_noncons(const State&, const State&, const double*) const { return State{}; }
   State bc_structured(const State& ui, const double* n, int direction) const {
-    return eq.slip_wall_structured(ui, n, direction);
+    if (wall == 1) return eq.slip_wall_pressure_structured(ui, n, direction);
+    State ub = ui;
+    ub[4] = -ui[4];
+    return direction % 2 == 0 ? surface_flux(ui, ub, n) : surface_flux(ub, ui, n);
   }
   State bc_normal(const State& ui, const double* n) const {
+    if (wall == 1) return eq.slip_wall(ui, n);
     return eq.slip_wall_structured(ui, n, 2);
   }
-  // 0: source_terms_rainy; 1: convergence-test manufactured source; 2: none
+  // 0: source_terms_rainy; 1: convergence-test manufactured source; 2: none;
+  // 3: source_terms_no_phase_change
   int source_kind = 0;
   State flux(const State& u, const double* n) const { return eq.flux(u, n); }
   State source(const State& u, const double* x, double t) const {
     if (source_kind == 2) return State{};
+    if (source_kind == 3) return eq.source_no_phase_change(u);
     return source_kind == 0 ? eq.source_rainy(u) : source_convergence(x, t);
   }
   void max_abs_speeds(const State& u, double& l1, double& l2) const { eq.max_abs_speeds(u, l1, l2); }
@@ -937,6 +948,42 @@ void* orc_rainy_create(int polydeg, int nx, int ny, double x0, double x1, double
   c->dg.reset(new DG2D<RainyPhys>(c->phys, c->basis, c->mesh));
   c->dg->weak_form = weak_form != 0;
   return c;
+}
+
+// on a mesh given by the host mirror's arrays (see mesh_from_arrays);
+// surface 0 flux_lax_friedrichs / 1 flux_LMARS, wall 0 simple / 1 pressure
+// Riemann slip wall on the boundary faces of kind 1
+void* orc_rainy_create_mesh(int polydeg, int nelem, const double* xy, const double* Ja,
+                            const double* invJ, int nif, const int* if_e, const int* if_f,
+                            const int* if_flip, int nbd, const int* bd_e, const int* bd_f,
+                            const int* bd_kind, int weak_form, int source_kind, int surface,
+                            int wall) {
+  auto* c = new RainyCase();
+  c->phys.source_kind = source_kind;
+  c->phys.surface = surface;
+  c->phys.wall = wall;
+  c->basis = make_lgl_basis(polydeg);
+  c->mesh = mesh_from_arrays(c->basis.n, nelem, xy, Ja, invJ, nif, if_e, if_f, if_flip, nbd, bd_e,
+                             bd_f, bd_kind);
+  c->dg.reset(new DG2D<RainyPhys>(c->phys, c->basis, c->mesh));
+  c->dg->weak_form = weak_form != 0;
+  return c;
+}
+
+void orc_rainy_flux_lmars(const double* ul, const double* ur, const double* n, double* f) {
+  RainyEuler2D eq;
+  RainyEuler2D::State a, b;
+  for (int v = 0; v < 9; ++v) { a[v] = ul[v]; b[v] = ur[v]; }
+  const auto r = eq.flux_lmars(a, b, n);
+  for (int v = 0; v < 9; ++v) f[v] = r[v];
+}
+
+void orc_rainy_slip_wall(const double* u, const double* n, double* f) {
+  RainyEuler2D eq;
+  RainyEuler2D::State a;
+  for (int v = 0; v < 9; ++v) a[v] = u[v];
+  const auto r = eq.slip_wall(a, n);
+  for (int v = 0; v < 9; ++v) f[v] = r[v];
 }
 
 void orc_rainy_geometry(void* h, double* xy) {

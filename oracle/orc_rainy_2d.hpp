@@ -41,7 +41,7 @@ struct RainyEuler2D {
     if (rc < 0.0 && std::fabs(rc) <= 1e-15) rc = 0.0;
   }
 
-  // pressure, :317-330
+  // pressure, :328-341
   double pressure(const State& u) const {
     double rv, rc, T;
     nlsol(u, rv, rc, T);
@@ -177,6 +177,70 @@ struct RainyEuler2D {
     ub[4] = -ui[4];
     if (direction % 2 == 0) return flux_llf(ui, ub, n);
     return flux_llf(ub, ui, n);
+  }
+
+  // flux_LMARS, :817-861 (a = 360, beta = 1): the upwind state times the
+  // interface velocity plus the interface pressure
+  State flux_lmars(const State& ul, const State& ur, const double* n) const {
+    const double a = 360.0, beta = 1.0;
+    const double rho_l = ul[0] + ul[1] + ul[2], rho_r = ur[0] + ur[1] + ur[2];
+    const double ri_l = 1.0 / rho_l, ri_r = 1.0 / rho_r;
+    const double p_l = pressure(ul), p_r = pressure(ur);
+    const double v_l = (ul[3] * ri_l) * n[0] + (ul[4] * ri_l) * n[1];
+    const double v_r = (ur[3] * ri_r) * n[0] + (ur[4] * ri_r) * n[1];
+    const double nrm = std::sqrt(n[0] * n[0] + n[1] * n[1]);
+    const double rho = 0.5 * (rho_l + rho_r);
+    const double p_int = 0.5 * (p_l + p_r) - beta * 0.5 * a * rho * (v_r - v_l) / nrm;
+    const double v_int = 0.5 * (v_l + v_r) - beta * 1.0 / (2.0 * a * rho) * (p_r - p_l) * nrm;
+    const State& us = v_int > 0 ? ul : ur;
+    const double ps = v_int > 0 ? p_l : p_r;
+    return {us[0] * v_int, us[1] * v_int, 0.0, us[3] * v_int + p_int * n[0],
+            us[4] * v_int + p_int * n[1], us[5] * v_int + ps * v_int, 0.0, 0.0, 0.0};
+  }
+
+  // boundary_condition_slip_wall with an outward normal, :639-686: the wall
+  // pressure of the normal Riemann problem (Toro 2009, section 6.3.3)
+  State slip_wall(const State& ui, const double* n) const {
+    const double nrm = std::sqrt(n[0] * n[0] + n[1] * n[1]);
+    const double c = n[0] / nrm, s = n[1] / nrm;
+    const double rho = ui[0] + ui[1] + ui[2];
+    const double rinv = 1.0 / rho;
+    const double v_normal = (c * ui[3] + s * ui[4]) * rinv;
+    double rv, rc, T;
+    nlsol(ui, rv, rc, T);
+    const double p = (R_d * ui[0] + R_v * rv) * T;
+    const double q_v = rv / ui[0], q_l = (rc + ui[2]) / ui[0];
+    const double gamma = 1.0 + (R_d + R_v * q_v) / (c_vd + c_vv * q_v + c_l * q_l);
+    double p_star;
+    if (v_normal <= 0.0) {
+      const double v_sound = std::sqrt(gamma * p * rinv);
+      p_star = p * std::pow(1.0 + 0.5 * (gamma - 1.0) * v_normal / v_sound,
+                            2.0 * gamma * (1.0 / (gamma - 1.0)));
+    } else {
+      const double A = 2.0 / ((gamma + 1.0) * rho);
+      const double B = p * (gamma - 1.0) / (gamma + 1.0);
+      p_star = p + 0.5 * v_normal / A *
+                       (v_normal + std::sqrt(v_normal * v_normal + 4.0 * A * (p + B)));
+    }
+    return {0.0, 0.0, 0.0, p_star * c * nrm, p_star * s * nrm, 0.0, 0.0, 0.0, 0.0};
+  }
+
+  // its StructuredMesh method, :689-705: on the negative faces (odd 1-based
+  // direction) the outward-normal wall of -n, sign flipped back
+  State slip_wall_pressure_structured(const State& ui, const double* n, int direction) const {
+    if (direction % 2 == 1) {
+      const double m[2] = {-n[0], -n[1]};
+      State f = slip_wall(ui, m);
+      for (double& x : f) x = -x;
+      return f;
+    }
+    return slip_wall(ui, n);
+  }
+
+  // source_terms_no_phase_change, :580-593: gravity only
+  State source_no_phase_change(const State& u) const {
+    const double rho = u[0] + u[1] + u[2];
+    return {0.0, 0.0, 0.0, 0.0, -g * rho, -g * u[4], 0.0, 0.0, 0.0};
   }
 
   // source_terms_rainy, :548-577

@@ -202,3 +202,61 @@ def test_learned_guess_trains_and_reduces_newton_iterations(tg, orc, gpu_lib):
     for v in (6, 7, 8):
         assert np.abs(u_plain[..., v] - uo[..., v]).max() <= 1e-11 * np.abs(uo[..., v]).max()
     semi.close()
+
+
+def hoeck_semi(tg, ic, cells=(64, 32), polydeg=3):
+    """examples/euler/moist_air/buoyancy/elixir_hoeck_bubble.jl: flux_ec_rain /
+    flux_LMARS, source_terms_no_phase_change, pressure-Riemann slip walls."""
+    eq = tg.CompressibleRainyEulerEquations2D()
+    solver = tg.DGSEM(polydeg, tg.flux_LMARS, tg.VolumeIntegralFluxDifferencing(tg.flux_ec_rain))
+    mesh = tg.StructuredMesh(cells, (0.0, 0.0), (20000.0, 10000.0), periodicity=(True, False))
+    bcs = {"y_neg": tg.boundary_condition_slip_wall, "y_pos": tg.boundary_condition_slip_wall}
+    return eq, tg.SemidiscretizationHyperbolic(mesh, eq, ic, solver,
+                                               source_terms=tg.source_terms_no_phase_change,
+                                               boundary_conditions=bcs)
+
+
+@pytest.mark.parametrize("polydeg", [2, 3, 4])
+def test_rainy_lmars_pressure_walls_match_oracle(tg, orc, gpu_lib, polydeg):
+    """flux_LMARS, the pressure-Riemann slip wall and the gravity-only source
+    on a moving, saturation-consistent rainy state (with rain)."""
+    from test_oracle_rainy import hoeck_moist_setup
+    _, ic, _, _, _, _, arrays = hoeck_moist_setup(tg, (8, 4), polydeg)
+    eq, semi = hoeck_semi(tg, ic, (8, 4), polydeg)
+    u = semi.compute_coefficients()
+    u[..., 2] = 1e-4 * u[..., 0]
+    u = solved_state(orc, moving(u, seed=20 + polydeg))
+    du = semi.rhs(u)
+    c = orc.Rainy2D(polydeg, 0, 0, 0, 0, 0, 0, source_kind=3, mesh=arrays, surface=1, wall=1)
+    du_ref = c.rhs(u)
+    assert max_norm_rel(du, du_ref) <= RTOL, max_norm_rel(du, du_ref)
+    for v in (1, 2):
+        s = np.abs(du_ref[..., v]).max()
+        assert np.abs(du[..., v] - du_ref[..., v]).max() <= 1e-10 * s
+    semi.close()
+
+
+def test_gpu_reproduces_hoeck_moist_bubble_golden(tg, orc, gpu_lib):
+    """test/test_2d_rainy_euler.jl:42-77 with every CK2N54 stage, the Newton
+    stage limiter (default tolerance 1e-9) and the CFL reduction on the GPU;
+    norms by NumPy and on the device."""
+    import analysis
+    from test_oracle_rainy import check_hoeck_moist, hoeck_moist_setup
+    eqr, ic, mesh, basis, xy, invJ, arrays = hoeck_moist_setup(tg)
+    eq, semi = hoeck_semi(tg, ic)
+    semi.set_state(semi.compute_coefficients())
+    semi.set_newton(mode=0, tol=1e-9, max_iterations=20)
+    t, t_end = 0.0, 10.0
+    while t < t_end - 1e-13:
+        dt = semi.max_dt()
+        if t + dt >= t_end:
+            t = semi.rk_steps(1, fixed_dt=t_end - t, t=t)
+        else:
+            t = semi.rk_steps(1, cfl=1.0, t=t)
+    assert abs(t - t_end) < 1e-12
+    u = semi.get_state()
+    l2, linf = analysis.error_norms(u, xy, invJ, basis.nodes, lambda x: ic(x, 0.0, eq), 2)
+    check_hoeck_moist(l2, linf)
+    l2d, linfd = semi.calc_error_norms(t_end)
+    check_hoeck_moist(l2d, linfd)
+    semi.close()

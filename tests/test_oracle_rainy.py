@@ -66,3 +66,69 @@ def test_rainy_newton_recovers_saturation_state(orc):
     rv_sat = np.minimum(e_s / (461.0 * u[..., 8]), u[..., 1])
     assert np.allclose(u[..., 6], rv_sat, rtol=1e-10)
     assert np.allclose(u[..., 6] + u[..., 7], u[..., 1], rtol=1e-12)
+
+
+# test/test_2d_rainy_euler.jl:42-77: examples/euler/moist_air/buoyancy/elixir_hoeck_bubble.jl
+# (the moist bubble on the AtmosphereLayers background as a rainy state,
+# 64x32 StructuredMesh over 20 km x 10 km, periodic in x, pressure-Riemann slip
+# walls, N = 3, flux_ec_rain / flux_LMARS, source_terms_no_phase_change,
+# CK2N54 at CFL 1 with the Newton stage limiter at its default tolerance 1e-9)
+# to t = 10 s.  The oracle agrees with the golden to 8e-11 relative.
+HOECK_MOIST = (
+    [0.0031469268543095233, 6.293853704548511e-5, 0.0, 0.030085941482251792, 1.2721823851437415,
+     1040.2702923456666, 0.0011556742959893704, 0.0011991088277167412, 2.080063951506559],
+    [0.010772626708125621, 0.00021545552388836306, 0.0, 0.17969745708245988, 2.469797669783883,
+     3725.8780578381848, 0.0030306571979925243, 0.0032258070568836963, 3.242378389076862])
+
+
+def check_hoeck_moist(l2, linf):
+    for v in range(9):
+        for a, g in ((l2[v], HOECK_MOIST[0][v]), (linf[v], HOECK_MOIST[1][v])):
+            assert abs(a - g) <= max(500 * np.finfo(np.float64).eps, RTOL * abs(g)), (v, a, g)
+
+
+def hoeck_moist_setup(tg, cells=(64, 32), polydeg=3):
+    """(rainy equations, initial condition, basis, xy, invJ, oracle mesh arrays)."""
+    from test_oracle_moist import _LAYERS
+    from trixiatmo_gb300.initial_conditions import (AtmosphereLayers,
+                                                    initial_condition_moist_bubble_rainy)
+    eqm = tg.CompressibleMoistEulerEquations2D(c_pd=1004, c_vd=717, c_pv=1885, c_vv=1424,
+                                               gravity=9.80616)
+    if "layers" not in _LAYERS:
+        _LAYERS["layers"] = AtmosphereLayers(eqm)
+    ic = initial_condition_moist_bubble_rainy(_LAYERS["layers"], eqm)
+    mesh = tg.StructuredMesh(cells, (0.0, 0.0), (20000.0, 10000.0), periodicity=(True, False))
+    basis = tg.LobattoLegendreBasis(polydeg)
+    xy, Ja, invJ = mesh.geometry(basis)
+    ie, ifc, fl, be, bf = mesh.connectivity().arrays()
+    bk = np.full(len(be), 1, dtype=np.int32)
+    return (tg.CompressibleRainyEulerEquations2D(), ic, mesh, basis, xy, invJ,
+            (xy, Ja, invJ, ie, ifc, fl, be, bf, bk))
+
+
+def test_oracle_hoeck_moist_bubble_golden(tg, orc):
+    import analysis
+    eq, ic, mesh, basis, xy, invJ, arrays = hoeck_moist_setup(tg)
+    c = orc.Rainy2D(3, 0, 0, 0, 0, 0, 0, source_kind=3, mesh=arrays, surface=1, wall=1)
+    u = np.ascontiguousarray(ic(xy, 0.0, eq))
+    t = c.ck_steps(u, np.zeros_like(u), 0.0, 1.0, 10 ** 6, 0.0, 0, 1e-9, 20, 10.0)
+    assert abs(t - 10.0) < 1e-13
+    l2, linf = analysis.error_norms(u, xy, invJ, basis.nodes, lambda x: ic(x, 0.0, eq), 2)
+    check_hoeck_moist(l2, linf)
+
+
+def test_rainy_lmars_and_pressure_wall(orc):
+    """flux_LMARS (compressible_rainy_euler_2d.jl:817-861) is consistent for a
+    state at rest (pressure only), and the pressure-Riemann slip wall gives the
+    state's own pressure for zero normal velocity."""
+    rng = np.random.default_rng(5)
+    for _ in range(10):
+        u = np.array([rng.uniform(0.8, 1.2), 0.02, 0.0, 0.0, 0.0, 0.0, 0.015, 0.005,
+                      rng.uniform(270, 300)])
+        u[5] = 717.0 * u[0] * u[8]
+        n = rng.uniform(-1, 1, 2)
+        p = (287.0 * u[0] + 461.0 * u[6]) * u[8]
+        f = orc.rainy_flux_lmars(u, u, n)
+        assert np.allclose(f, [0, 0, 0, p * n[0], p * n[1], 0, 0, 0, 0], rtol=1e-14, atol=1e-12)
+        w = orc.rainy_slip_wall(u, n)
+        assert np.allclose(w, [0, 0, 0, p * n[0], p * n[1], 0, 0, 0, 0], rtol=1e-14, atol=1e-12)

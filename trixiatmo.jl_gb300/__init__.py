@@ -20,7 +20,8 @@ from .equations import (CompressibleEulerEnergyEquationsWithGravity2D,
                         CompressibleMoistEulerEquations2D, flux_chandrashekar,
                         source_terms_geopotential, source_terms_moist_bubble,
                         source_terms_convergence_test_dry, source_terms_convergence_test_moist,
-                        source_terms_nonhydrostatic_gravity_wave,
+                        source_terms_nonhydrostatic_gravity_wave, flux_LMARS,
+                        source_terms_no_phase_change,
                         CompressibleEulerPotentialTemperatureEquationsWithGravity2D,
                         CompressibleEulerPotentialTemperatureEquationsWithGravity3D,
                         CompressibleEulerInternalEnergyEquationsWithGravity2D,
@@ -65,7 +66,7 @@ __all__ = [
     "P4estMesh", "covariant", "SemidiscretizationCovariant", "initial_condition_adiabatic",
     "SemidiscretizationCovariantEnsemble", "source_terms_nonhydrostatic_gravity_wave",
     "initial_condition_nonhydrostatic_gravity_wave", "AtmosphereLayers",
-    "initial_condition_moist_bubble",
+    "initial_condition_moist_bubble", "flux_LMARS", "source_terms_no_phase_change",
     "CompressibleEulerPotentialTemperatureEquationsWithGravity2D",
     "CompressibleEulerPotentialTemperatureEquationsWithGravity3D",
     "CompressibleEulerInternalEnergyEquationsWithGravity2D", "flux_conservative_etec",

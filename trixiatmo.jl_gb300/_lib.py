@@ -39,6 +39,7 @@ TAG_SRC_MOIST_BUBBLE = 4
 TAG_SRC_MOIST_CONVERGENCE_DRY = 5
 TAG_SRC_MOIST_CONVERGENCE = 6
 TAG_SRC_MOIST_GRAVITY_WAVE = 7
+TAG_SRC_RAINY_NO_PHASE_CHANGE = 8
 TAG_EQ_COVARIANT_SWE = 5
 TAG_EQ_POTENTIAL_TEMPERATURE_2D = 6
 TAG_EQ_POTENTIAL_TEMPERATURE_3D = 7

@@ -56,14 +56,15 @@ struct PhysRainy2D {
   static constexpr bool kSurfaceNoncons = false;  // surface flux only (flux_zero)
 
   struct Params {
-    int source_kind;  // TAG_SRC_RAINY or TAG_SRC_RAINY_CONVERGENCE
-    int pad;
+    int source_kind;  // TAG_SRC_RAINY, TAG_SRC_RAINY_CONVERGENCE or TAG_SRC_RAINY_NO_PHASE_CHANGE
+    int lmars;        // surface flux: 0 flux_lax_friedrichs, 1 flux_LMARS
   };
 
-  static Params make_params(const double* p) {
+  // params = (source kind); the surface flux is set from the configuration
+  static Params make_params(const double* p, int surface_flux = TAG_SF_LAX_FRIEDRICHS) {
     Params q;
     q.source_kind = (int)p[0];
-    q.pad = 0;
+    q.lmars = surface_flux == TAG_SF_LMARS;
     return q;
   }
 
@@ -178,9 +179,76 @@ struct PhysRainy2D {
     return sqrt(gm * p * ri);
   }
 
-  // flux_lax_friedrichs: central flux + 0.5 max_abs_speed_naive (u_rr - u_ll)
+  // pressure(u), :328-341
+  TAG_DEV static double pressure(const double* u) {
+    using C = RainyConst;
+    double rv, rc, T;
+    nlsol(u, rv, rc, T);
+    return (C::R_d * u[0] + C::R_v * rv) * T;
+  }
+
+  // flux_LMARS, :817-861 (speed of sound a = 360, beta = 1): upwinded
+  // transport of the whole state plus the interface pressure
+  TAG_DEV static void lmars(const double* ul, const double* ur, double n1, double n2, double* F) {
+    const double a = 360.0;
+    const double rl = ul[0] + ul[1] + ul[2], rr = ur[0] + ur[1] + ur[2];
+    const double ril = 1.0 / rl, rir = 1.0 / rr;
+    const double pl = pressure(ul), pr = pressure(ur);
+    const double vl = (ul[3] * ril) * n1 + (ul[4] * ril) * n2;
+    const double vr = (ur[3] * rir) * n1 + (ur[4] * rir) * n2;
+    const double nrm = sqrt(n1 * n1 + n2 * n2);
+    const double rho = 0.5 * (rl + rr);
+    const double p_int = 0.5 * (pl + pr) - 0.5 * a * rho * (vr - vl) / nrm;
+    const double v_int = 0.5 * (vl + vr) - 1.0 / (2.0 * a * rho) * (pr - pl) * nrm;
+    const double* us = v_int > 0.0 ? ul : ur;
+    const double ps = v_int > 0.0 ? pl : pr;
+    F[0] = us[0] * v_int;
+    F[1] = us[1] * v_int;
+    F[2] = 0.0;
+    F[3] = us[3] * v_int + p_int * n1;
+    F[4] = us[4] * v_int + p_int * n2;
+    F[5] = us[5] * v_int + ps * v_int;
+    F[6] = F[7] = F[8] = 0.0;
+  }
+
+  // boundary_condition_slip_wall with an outward normal (:639-686): the
+  // pressure of the Riemann problem against the wall (Toro 2009, 6.3.3)
+  TAG_DEV static void slip_wall(const double* ui, double n1, double n2, double* F) {
+    using C = RainyConst;
+    const double nrm = sqrt(n1 * n1 + n2 * n2);
+    const double c = n1 / nrm, s = n2 / nrm;
+    const double rho = ui[0] + ui[1] + ui[2];
+    const double ri = 1.0 / rho;
+    const double vn = (c * ui[3] + s * ui[4]) * ri;
+    double rv, rc, T;
+    nlsol(ui, rv, rc, T);
+    const double p = (C::R_d * ui[0] + C::R_v * rv) * T;
+    const double q_v = rv / ui[0];
+    const double q_l = (rc + ui[2]) / ui[0];
+    const double gm = 1.0 + (C::R_d + C::R_v * q_v) / (C::c_vd + C::c_vv * q_v + C::c_l * q_l);
+    double p_star;
+    if (vn <= 0.0) {
+      const double cs = sqrt(gm * p * ri);
+      p_star = p * pow(1.0 + 0.5 * (gm - 1.0) * vn / cs, 2.0 * gm * (1.0 / (gm - 1.0)));
+    } else {
+      const double A = 2.0 / ((gm + 1.0) * rho);
+      const double B = p * (gm - 1.0) / (gm + 1.0);
+      p_star = p + 0.5 * vn / A * (vn + sqrt(vn * vn + 4.0 * A * (p + B)));
+    }
+    F[0] = F[1] = F[2] = 0.0;
+    F[3] = p_star * c * nrm;
+    F[4] = p_star * s * nrm;
+    F[5] = F[6] = F[7] = F[8] = 0.0;
+  }
+
+  // flux_lax_friedrichs: central flux + 0.5 max_abs_speed_naive (u_rr - u_ll);
+  // or flux_LMARS
   TAG_DEV static void surface_flux(const Params& P, const double* ul, const double* ur, double n1,
                                    double n2, double* F) {
+    if (P.lmars) {
+      lmars(ul, ur, n1, n2, F);
+      return;
+    }
     double fl[9], fr[9];
     flux(P, ul, n1, n2, fl);
     flux(P, ur, n1, n2, fr);
@@ -192,11 +260,21 @@ struct PhysRainy2D {
     for (int v = 0; v < 9; ++v) F[v] = 0.5 * (fl[v] + fr[v]) - 0.5 * lam * (ur[v] - ul[v]);
   }
 
-  // boundary_condition_simple_slip_wall reached from a StructuredMesh
-  // (:973-994): rho_v2 mirrored, states ordered by the face parity; OUTWARD flux.
+  // kind TAG_BC_SIMPLE_SLIP_WALL: boundary_condition_simple_slip_wall reached
+  // from a StructuredMesh (:973-994): rho_v2 mirrored, states ordered by the
+  // face parity.  TAG_BC_SLIP_WALL_STRUCTURED: boundary_condition_slip_wall's
+  // StructuredMesh method (:689-705), the outward-normal wall evaluated with
+  // the outward normal (-n on the negative faces).  Both return the OUTWARD flux.
   TAG_DEV static void boundary_flux(const Params& P, const double* ui, double n1, double n2,
                                     int face, int kind, double* F) {
-    (void)kind;
+    if (kind == TAG_BC_SLIP_WALL_STRUCTURED || kind == TAG_BC_SLIP_WALL_NORMAL) {
+      if (kind == TAG_BC_SLIP_WALL_STRUCTURED && !(face & 1)) {
+        n1 = -n1;
+        n2 = -n2;
+      }
+      slip_wall(ui, n1, n2, F);
+      return;
+    }
     double ub[9];
 #pragma unroll
     for (int v = 0; v < 9; ++v) ub[v] = ui[v];
@@ -210,11 +288,20 @@ struct PhysRainy2D {
     }
   }
 
-  // source_terms_rainy (:548-577) or the manufactured source of
+  // source_terms_rainy (:548-577), source_terms_no_phase_change (:580-593)
+  // or the manufactured source of
   // examples/euler/precipitation/tests/convergence_test.jl:42-124; s[9]
   TAG_DEV static void source(const Params& P, const double* u, const double* x, double t,
                              double* s) {
     using C = RainyConst;
+    if (P.source_kind == TAG_SRC_RAINY_NO_PHASE_CHANGE) {
+      const double rho = u[0] + u[1] + u[2];
+#pragma unroll
+      for (int v = 0; v < 9; ++v) s[v] = 0.0;
+      s[4] = -C::g * rho;
+      s[5] = -C::g * u[4];
+      return;
+    }
     if (P.source_kind == TAG_SRC_RAINY) {
       double rv, rc, T;
       nlsol(u, rv, rc, T);

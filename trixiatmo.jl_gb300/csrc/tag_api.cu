@@ -716,10 +716,11 @@ const char* check_equations(const tag_config* cfg) {
         return "unsupported flux combination";
       return nullptr;
     case TAG_EQ_RAINY_2D: {
-      if ((vf != TAG_VF_EC_RAIN && vf != TAG_VF_WEAK_FORM) || sf != TAG_SF_LAX_FRIEDRICHS)
+      if ((vf != TAG_VF_EC_RAIN && vf != TAG_VF_WEAK_FORM) ||
+          (sf != TAG_SF_LAX_FRIEDRICHS && sf != TAG_SF_LMARS))
         return "unsupported flux combination for the rainy equations";
       const double k = cfg->params[0];
-      if (k != TAG_SRC_RAINY && k != TAG_SRC_RAINY_CONVERGENCE)
+      if (k != TAG_SRC_RAINY && k != TAG_SRC_RAINY_CONVERGENCE && k != TAG_SRC_RAINY_NO_PHASE_CHANGE)
         return "unsupported source kind for the rainy equations";
       if (k == TAG_SRC_RAINY_CONVERGENCE && !cfg->node_coordinates)
         return "the convergence-test source needs node coordinates";
@@ -775,7 +776,9 @@ bool boundary_kind_ok(int eq, int kind) {
       return kind == TAG_BC_SLIP_WALL_STRUCTURED || kind == TAG_BC_SLIP_WALL_NORMAL;
     case TAG_EQ_EULER_ENERGY_3D:
     case TAG_EQ_POTENTIAL_TEMPERATURE_3D: return kind == TAG_BC_SLIP_WALL_NORMAL;
-    case TAG_EQ_RAINY_2D: return kind == TAG_BC_SIMPLE_SLIP_WALL;
+    case TAG_EQ_RAINY_2D:
+      return kind == TAG_BC_SIMPLE_SLIP_WALL || kind == TAG_BC_SLIP_WALL_STRUCTURED ||
+             kind == TAG_BC_SLIP_WALL_NORMAL;
     case TAG_EQ_INTERNAL_ENERGY_2D: return kind == TAG_BC_SLIP_WALL_NORMAL;
     default: return false;
   }
@@ -989,7 +992,7 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
   if (rainy) {
     h->nv = PhysRainy2D::NV;
     h->na = PhysRainy2D::NA;
-    h->p_rainy = PhysRainy2D::make_params(cfg->params);
+    h->p_rainy = PhysRainy2D::make_params(cfg->params, cfg->surface_flux);
     h->ops = cfg->volume_flux == TAG_VF_WEAK_FORM ? ops_for_n<PhysRainy2D, kVolWeak>(n)
                                                   : ops_for_n<PhysRainy2D, kVolFluxDiff>(n);
     h->has_limiter = true;

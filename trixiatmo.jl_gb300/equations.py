@@ -232,6 +232,9 @@ flux_nonconservative_waruszewski_etal = _NamedFlux("flux_nonconservative_warusze
 flux_zero = _NamedFlux("flux_zero")
 flux_ec_rain = _NamedFlux("flux_ec_rain")
 flux_lax_friedrichs = _NamedFlux("flux_lax_friedrichs")
+# the rainy equations' own LMARS (src/equations/compressible_rainy_euler_2d.jl:817-861,
+# speed of sound 360)
+flux_LMARS = _NamedFlux("flux_LMARS")
 flux_chandrashekar = _NamedFlux("flux_chandrashekar")
 # entropy / total-energy conservative fluxes; flux_ec is shared with the
 # covariant shallow-water equations (the reference dispatches one name on the
@@ -292,6 +295,9 @@ class _Source:
 source_terms_rainy = _Source("source_terms_rainy", _lib.TAG_SRC_RAINY)
 source_terms_convergence_test_rainy = _Source("source_terms_convergence_test_rainy",
                                               _lib.TAG_SRC_RAINY_CONVERGENCE)
+# rainy equations, gravity only (compressible_rainy_euler_2d.jl:580-593)
+source_terms_no_phase_change = _Source("source_terms_no_phase_change",
+                                       _lib.TAG_SRC_RAINY_NO_PHASE_CHANGE)
 # moist equations, src/equations/compressible_moist_euler_2d.jl:320-340, :376-380,
 # :203-241, :275-317
 source_terms_geopotential = _Source("source_terms_geopotential", _lib.TAG_SRC_GEOPOTENTIAL)

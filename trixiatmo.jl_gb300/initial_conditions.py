@@ -402,47 +402,85 @@ class AtmosphereLayers:
 
 
 def _perturb_moist_profile(x, rho, rho_theta, rho_qv, rho_ql, eq):
-    """perturb_moist_profile! (compressible_moist_euler_2d.jl:1148-1206): the
-    Bryan-Fritsch bubble (2 K of density potential temperature, radius 2 km at
-    (10 km, 2 km)) at constant pressure, with the saturation adjustment by
-    fixed-point iteration to 1e-12."""
+    """perturb_moist_profile! (compressible_moist_euler_2d.jl:1148-1206), per
+    node over arrays: the Bryan-Fritsch bubble (2 K of density potential
+    temperature, radius 2 km at (10 km, 2 km)) at constant pressure, with the
+    saturation adjustment by fixed-point iteration to 1e-12 (each node stops
+    at its own first converged iterate).  Returns rho, rho_e, rho_qv, rho_ql, T."""
     xc, zc, rc, dtheta = 10000.0, 2000.0, 2000.0, 2.0
-    r = np.sqrt((x[0] - xc) ** 2 + (x[1] - zc) ** 2)
+    r = np.sqrt((x[..., 0] - xc) ** 2 + (x[..., 1] - zc) ** 2)
     rho_d = rho - rho_qv - rho_ql
     kappa_M = (eq.R_d * rho_d + eq.R_v * rho_qv) / (eq.c_pd * rho_d + eq.c_pv * rho_qv +
                                                    eq.c_pl * rho_ql)
     p_loc = eq.p_0 * (eq.R_d * rho_theta / eq.p_0) ** (1.0 / (1.0 - kappa_M))
     T_loc = p_loc / (eq.R_d * rho_d + eq.R_v * rho_qv)
     rho_e = (eq.c_vd * rho_d + eq.c_vv * rho_qv + eq.c_pl * rho_ql) * T_loc + eq.L_00 * rho_qv
-    if r < rc:
-        th_dens = rho_theta / rho * (p_loc / eq.p_0) ** (kappa_M - eq.kappa)
-        th_dens_new = th_dens * (1.0 + dtheta * np.cos(np.pi * (0.5 * r / rc)) ** 2 / 300.0)
-        rt = (rho_qv + rho_ql) / rho_d
-        rv = rho_qv / rho_d
-        th_loc = th_dens_new * (1.0 + rt) / (1.0 + (eq.R_v / eq.R_d) * rv)
-        if rt > 0:
-            for _ in range(1000):
-                T_loc = th_loc * (p_loc / eq.p_0) ** eq.kappa
-                T_C = T_loc - 273.15
-                pvs = 611.2 * np.exp(17.62 * T_C / (243.12 + T_C))
-                rho_d_new = (p_loc - pvs) / (eq.R_d * T_loc)
-                rvs = pvs / (eq.R_v * rho_d_new * T_loc)
-                th_new = th_dens_new * (1.0 + rt) / (1.0 + (eq.R_v / eq.R_d) * rvs)
-                if abs(th_new - th_loc) <= th_loc * 1.0e-12:
-                    break
-                th_loc = th_new
-            else:
-                raise RuntimeError("moist bubble: saturation adjustment did not converge")
-        else:
-            rvs = 0.0
-            T_loc = th_loc * (p_loc / eq.p_0) ** eq.kappa
-            rho_d_new = p_loc / (eq.R_d * T_loc)
-        rho_qv = rvs * rho_d_new
-        rho_ql = (rt - rvs) * rho_d_new
-        rho = rho_d_new * (1.0 + rt)
-        rho_d = rho - rho_qv - rho_ql
-        rho_e = (eq.c_vd * rho_d + eq.c_vv * rho_qv + eq.c_pl * rho_ql) * T_loc + eq.L_00 * rho_qv
-    return rho, rho_e, rho_qv, rho_ql
+    b = np.nonzero(r < rc)[0]
+    if b.size == 0:
+        return rho, rho_e, rho_qv, rho_ql, T_loc
+    rho, rho_e, rho_qv, rho_ql, T_loc = (a.copy() for a in (rho, rho_e, rho_qv, rho_ql, T_loc))
+    th_dens = rho_theta[b] / rho[b] * (p_loc[b] / eq.p_0) ** (kappa_M[b] - eq.kappa)
+    th_dens_new = th_dens * (1.0 + dtheta * np.cos(np.pi * (0.5 * r[b] / rc)) ** 2 / 300.0)
+    rt = (rho_qv[b] + rho_ql[b]) / rho_d[b]
+    rv = rho_qv[b] / rho_d[b]
+    th_loc = th_dens_new * (1.0 + rt) / (1.0 + (eq.R_v / eq.R_d) * rv)
+    pl = p_loc[b]
+    T_b = np.zeros_like(th_loc)
+    rvs = np.zeros_like(th_loc)
+    rho_d_new = np.zeros_like(th_loc)
+    dry = rt <= 0
+    T_b[dry] = th_loc[dry] * (pl[dry] / eq.p_0) ** eq.kappa
+    rho_d_new[dry] = pl[dry] / (eq.R_d * T_b[dry])
+    act = np.nonzero(~dry)[0]
+    for _ in range(1000):
+        if act.size == 0:
+            break
+        T_a = th_loc[act] * (pl[act] / eq.p_0) ** eq.kappa
+        T_C = T_a - 273.15
+        pvs = 611.2 * np.exp(17.62 * T_C / (243.12 + T_C))
+        rdn = (pl[act] - pvs) / (eq.R_d * T_a)
+        rvs_a = pvs / (eq.R_v * rdn * T_a)
+        th_new = th_dens_new[act] * (1.0 + rt[act]) / (1.0 + (eq.R_v / eq.R_d) * rvs_a)
+        done = np.abs(th_new - th_loc[act]) <= th_loc[act] * 1.0e-12
+        T_b[act], rvs[act], rho_d_new[act] = T_a, rvs_a, rdn
+        th_loc[act[~done]] = th_new[~done]
+        act = act[~done]
+    else:
+        raise RuntimeError("moist bubble: saturation adjustment did not converge")
+    qv = rvs * rho_d_new
+    ql = (rt - rvs) * rho_d_new
+    rr = rho_d_new * (1.0 + rt)
+    rd = rr - qv - ql
+    rho[b], rho_qv[b], rho_ql[b], T_loc[b] = rr, qv, ql, T_b
+    rho_e[b] = (eq.c_vd * rd + eq.c_vv * qv + eq.c_pl * ql) * T_b + eq.L_00 * qv
+    return rho, rho_e, rho_qv, rho_ql, T_loc
+
+
+def _moist_bubble_states(layers, x, eq):
+    """initial_condition_moist_bubble (compressible_moist_euler_2d.jl:1106-1146)
+    at nodes x[..., 2]: (rho, rho_v1, rho_v2, rho_E, rho_qv, rho_ql, T)."""
+    data, dz, H = layers.layer_data, float(layers.preciseness), layers.total_height
+    flat = np.asarray(x, dtype=np.float64).reshape(-1, 2)
+    z = flat[:, 1]
+    if np.any((z > H) & ~np.isclose(z, H, rtol=np.sqrt(np.finfo(float).eps), atol=0.0)):
+        raise ValueError("the atmosphere does not match the simulation domain")
+    n = np.floor((z + np.finfo(float).eps) / dz).astype(np.int64)  # 0-based layer below z
+    z_l = n * dz
+    z_r = (n + 1) * dz
+    top = z_l == H
+    z_r = np.where(top, z_l + dz, z_r)
+    n = np.where(top, n - 1, n)
+    rl, thl, qvl, qll = data[n].T
+    rr, thr, qvr, qlr = data[n + 1].T
+    rho = (rr * (z - z_l) + rl * (z_r - z)) / dz
+    rho_theta = rho * (thr / rr * (z - z_l) + thl / rl * (z_r - z)) / dz
+    rho_qv = rho * (qvr / rr * (z - z_l) + qvl / rl * (z_r - z)) / dz
+    rho_ql = rho * (qlr / rr * (z - z_l) + qll / rl * (z_r - z)) / dz
+    rho, rho_e, rho_qv, rho_ql, T = _perturb_moist_profile(flat, rho, rho_theta, rho_qv, rho_ql,
+                                                           eq)
+    z0 = np.zeros_like(rho)
+    out = np.stack([rho, z0, z0, rho_e + 0.5 * rho * 0.0, rho_qv, rho_ql, T], axis=-1)
+    return out.reshape(np.shape(x)[:-1] + (7,))
 
 
 def initial_condition_moist_bubble(atmosphere_layers):
@@ -450,32 +488,23 @@ def initial_condition_moist_bubble(atmosphere_layers):
     (compressible_moist_euler_2d.jl:1106-1146): the layer data interpolated
     linearly in z (rho; rho_theta, rho_qv, rho_ql per unit rho), then the
     perturbation; at rest.  Returns the initial condition (x, t, equations)."""
-    layers = atmosphere_layers
-
     def ic(x, t, equations):
-        eq = equations
-        data, dz, H = layers.layer_data, float(layers.preciseness), layers.total_height
-        flat = np.asarray(x, dtype=np.float64).reshape(-1, 2)
-        out = np.zeros((flat.shape[0], 6))
-        for k, xk in enumerate(flat):
-            z = xk[1]
-            if z > H and not np.isclose(z, H, rtol=np.sqrt(np.finfo(float).eps), atol=0.0):
-                raise ValueError("the atmosphere does not match the simulation domain")
-            n = int(np.floor((z + np.finfo(float).eps) / dz))  # 0-based layer below z
-            z_l = n * dz
-            z_r = (n + 1) * dz
-            if z_l == H:
-                z_r = z_l + dz
-                n -= 1
-            rl, thl, qvl, qll = data[n]
-            rr, thr, qvr, qlr = data[n + 1]
-            rho = (rr * (z - z_l) + rl * (z_r - z)) / dz
-            rho_theta = rho * (thr / rr * (z - z_l) + thl / rl * (z_r - z)) / dz
-            rho_qv = rho * (qvr / rr * (z - z_l) + qvl / rl * (z_r - z)) / dz
-            rho_ql = rho * (qlr / rr * (z - z_l) + qll / rl * (z_r - z)) / dz
-            rho, rho_e, rho_qv, rho_ql = _perturb_moist_profile(xk, rho, rho_theta, rho_qv,
-                                                                rho_ql, eq)
-            out[k] = (rho, 0.0, 0.0, rho_e, rho_qv, rho_ql)
-        return out.reshape(np.shape(x)[:-1] + (6,))
+        return _moist_bubble_states(atmosphere_layers, x, equations)[..., :6]
+
+    return ic
+
+
+def initial_condition_moist_bubble_rainy(atmosphere_layers, moist_equations):
+    """The moist bubble as a state of the rainy equations
+    (examples/euler/moist_air/buoyancy/elixir_hoeck_bubble.jl:16-25):
+    (rho_dry, rho_vapour + rho_cloud, rho_rain = 0, rho_v1, rho_v2, energy,
+    rho_vapour, rho_cloud, T), the bubble computed with the moist equations'
+    constants."""
+    def ic(x, t, equations):
+        s = _moist_bubble_states(atmosphere_layers, x, moist_equations)
+        rho, qv, ql = s[..., 0], s[..., 4], s[..., 5]
+        z0 = np.zeros_like(rho)
+        return np.stack([rho - qv - ql, qv + ql, z0, s[..., 1], s[..., 2], s[..., 3], qv, ql,
+                         s[..., 6]], axis=-1)
 
     return ic

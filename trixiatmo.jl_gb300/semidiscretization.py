@@ -37,7 +37,7 @@ from .equations import (CompressibleEulerInternalEnergyEquationsWithGravity2D,
                         CompressibleMoistEulerEquations2D, CompressibleRainyEulerEquations2D,
                         FluxLMARS, VolumeIntegralWeakForm, _Source,
                         boundary_condition_simple_slip_wall, boundary_condition_slip_wall,
-                        flux_chandrashekar, flux_ec_rain, flux_lax_friedrichs,
+                        flux_chandrashekar, flux_ec_rain, flux_lax_friedrichs, flux_LMARS,
                         flux_nonconservative_waruszewski_etal, flux_ranocha, flux_zero)
 from .initial_conditions import EARTH_ROTATION_RATE
 
@@ -84,11 +84,18 @@ def _flux_ids(equations, solver, source_terms=None):
         else:
             raise ValueError("volume integral must be weak form or flux differencing with "
                              "flux_ec_rain")
-        if sf is not flux_lax_friedrichs:
-            raise ValueError("surface flux must be flux_lax_friedrichs")
-        if not isinstance(source_terms, _Source):
-            raise ValueError("rainy equations need source_terms_rainy or the convergence-test source")
-        return vid, _lib.TAG_SF_LAX_FRIEDRICHS, [float(source_terms.kind)]
+        if sf is flux_lax_friedrichs:
+            sid = _lib.TAG_SF_LAX_FRIEDRICHS
+        elif sf is flux_LMARS:
+            sid = _lib.TAG_SF_LMARS
+        else:
+            raise ValueError("surface flux must be flux_lax_friedrichs or flux_LMARS")
+        if not isinstance(source_terms, _Source) or source_terms.kind not in (
+                _lib.TAG_SRC_RAINY, _lib.TAG_SRC_RAINY_CONVERGENCE,
+                _lib.TAG_SRC_RAINY_NO_PHASE_CHANGE):
+            raise ValueError("rainy equations need source_terms_rainy, "
+                             "source_terms_no_phase_change or the convergence-test source")
+        return vid, sid, [float(source_terms.kind)]
     if isinstance(equations, CompressibleMoistEulerEquations2D):
         if isinstance(vi, VolumeIntegralWeakForm):
             vid = _lib.TAG_VF_WEAK_FORM
