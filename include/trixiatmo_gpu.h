@@ -91,10 +91,15 @@ extern "C" {
 #define TAG_SRC_MOIST_GRAVITY_WAVE 7 /* geopotential + phase change +
                                         source_terms_nonhydrostatic_rayleigh_sponge     */
 #define TAG_SRC_RAINY_NO_PHASE_CHANGE 8 /* source_terms_no_phase_change (rainy: gravity only) */
+#define TAG_SRC_MOUNTAIN_WAVE 9      /* MountainWaveSetup as source terms (potential temperature
+                                        2D), set by tag_set_source                          */
 
 #define TAG_BC_SLIP_WALL_STRUCTURED 1 /* boundary_condition_slip_wall reached from a StructuredMesh */
 #define TAG_BC_SLIP_WALL_NORMAL 2     /* boundary_condition_slip_wall reached from a P4estMesh      */
 #define TAG_BC_SIMPLE_SLIP_WALL 3     /* boundary_condition_simple_slip_wall (rainy, StructuredMesh) */
+#define TAG_BC_DIRICHLET 4            /* BoundaryConditionDirichlet reached from a P4estMesh: the
+                                         surface flux of the inner and a given state, the states
+                                         set by tag_set_boundary_values (2D equations)          */
 
 typedef struct tag_handle_s* tag_handle;
 
@@ -212,6 +217,22 @@ int tag_rk_steps(tag_handle h, int32_t nsteps, double cfl, double fixed_dt, doub
 #define TAG_RK_SSPRK43 1
 #define TAG_RK_SSPRK33 2
 int tag_set_time_integrator(tag_handle h, int32_t scheme);
+
+/* States [B, n, nv] of the boundary faces of kind TAG_BC_DIRICHLET (entries of
+ * other faces are ignored): the values of Trixi's
+ * BoundaryConditionDirichlet(boundary_value_function) at the face nodes
+ * (reference: BoundaryConditionDirichlet(setup) in
+ * examples/euler/dry_air/mountain_flow/elixir_potential_temperature_linear_hydrostatic.jl:26-31).
+ * Required before the first rhs or step of a mesh with such faces; the states
+ * may be replaced between steps (time-dependent data). */
+int tag_set_boundary_values(tag_handle h, const double* values);
+
+/* Source terms that need more constants than tag_config.params holds:
+ *   POTENTIAL_TEMPERATURE_2D, TAG_SRC_MOUNTAIN_WAVE, 8 params (theta_0, u0,
+ *   Brunt-Vaisala frequency, z_damping_start, z_damping_end, x_damping_start,
+ *   x_damping_end, damping_rate): MountainWaveSetup passed as source_terms
+ *   (src/equations/initial_condition_compressible_euler_2d.jl:174-200). */
+int tag_set_source(tag_handle h, int32_t kind, const double* params, int32_t nparams);
 
 /* ---- analysis of the resident state (AnalysisCallback) ------------------ */
 /* Integrals over each member's domain, computed on the device in a fixed

@@ -85,6 +85,7 @@ def lib():
         L.orc_pt_create.restype = ctypes.c_void_p
         L.orc_pt_create.argtypes = ([ctypes.c_int] * 3 + [ctypes.c_double] * 4 + [ctypes.c_int] * 5 +
                                     [ctypes.c_double] * 4 + [ctypes.c_int] * 2)
+        L.orc_pt_set_mountain.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.orc_pt_create_mesh.restype = ctypes.c_void_p
         L.orc_pt_create_mesh.argtypes = ([ctypes.c_int] * 2 + [_dp] * 3 + [ctypes.c_int] +
                                          [_ip] * 3 + [ctypes.c_int] + [_ip] * 3 +
@@ -486,6 +487,15 @@ class PotTemp2D:
         self.h = lib().orc_pt_create(polydeg, nx, ny, x0, x1, y0, y1, int(periodic_x),
                                      int(periodic_y), volume, nc, wall_kind, c_p, c_v, g, c_lmars,
                                      surface, snc)
+
+    def set_mountain(self, mw=None, bd_values=None):
+        """MountainWaveSetup's damping source, mw = (theta_0, u0, N, z_damping_start,
+        z_damping_end, x_damping_start, x_damping_end, damping_rate), and the
+        states [B, n, 5] of the Dirichlet boundary faces (kind 4)."""
+        self._mw = None if mw is None else np.ascontiguousarray(mw, dtype=np.float64)
+        self._bv = None if bd_values is None else np.ascontiguousarray(bd_values, dtype=np.float64)
+        lib().orc_pt_set_mountain(self.h, None if self._mw is None else _p(self._mw),
+                                  None if self._bv is None else _p(self._bv))
 
     def initial_condition_gravity_waves(self):
         u = np.zeros((self.nelem, self.n, self.n, 5))

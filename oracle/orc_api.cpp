@@ -501,13 +501,39 @@ void errors_2d(const Basis& b, const Mesh2D& mesh, const double* u, Exact&& exac
 // CompressibleEulerPotentialTemperatureEquationsWithGravity2D on a
 // StructuredMesh: volume (flux_tec | flux_ec | flux_etec, nonconservative
 // gravity term), surface (FluxLMARS(c), flux_zero).
+// rayleigh_damping_coefficient (src/equations/initial_condition_compressible_euler_2d.jl:80-106):
+// sin^2 ramps of the vertical layer above z_s and of the lateral layers beyond +-x_s
+inline double rayleigh_damping(const double* x, double rate, double zs, double ze, double xs,
+                               double xe) {
+  const double pi = 3.14159265358979323846;
+  double dv = 0.0, dr = 0.0, dl = 0.0;
+  if (x[1] > zs) {
+    const double s = std::sin(pi * (0.5 * (x[1] - zs) / (ze - zs)));
+    dv = rate * (s * s);
+  }
+  if (!(x[0] < xs)) {
+    const double s = std::sin(pi * (0.5 * (x[0] - xs) / (xe - xs)));
+    dr = rate * (s * s);
+  }
+  if (!(x[0] > -xs)) {
+    const double s = std::sin(pi * (0.5 * (x[0] + xs) / (-xe + xs)));
+    dl = rate * (s * s);
+  }
+  return dv + dr + dl;
+}
+
 struct PTPhys {
   using State = PotTemp2D::State;
   static constexpr int nv = 5;
   static constexpr bool has_noncons = true;
-  static constexpr bool has_sources = false;
+  static constexpr bool has_sources = true;
   PotTemp2D eq;
   double c_lmars = 340.0;
+  // MountainWaveSetup's source (initial_condition_compressible_euler_2d.jl:174-200):
+  // mw = (theta_0, u0, N, z_damping_start, z_damping_end, x_damping_start,
+  // x_damping_end, damping_rate); off when mountain == 0
+  int mountain = 0;
+  double mw[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   State volume_flux(const State& a, const State& b, const double* n) const {
     return eq.volume_flux(a, b, n);
   }
@@ -527,7 +553,14 @@ struct PTPhys {
     return eq.slip_wall_normal(ui, n, c_lmars);
   }
   State flux(const State& u, const double* n) const { return eq.flux(u, n); }
-  State source(const State&, const double*, double) const { return State{}; }
+  State source(const State& u, const double* x, double) const {
+    if (!mountain) return State{};
+    const double v1 = u[1] / u[0], theta = u[3] / u[0];
+    const double damping = -rayleigh_damping(x, mw[7], mw[3], mw[4], mw[5], mw[6]);
+    const double theta_b = mw[0] * std::exp(mw[2] * mw[2] / eq.g * x[1]);
+    return {0.0, u[0] * (v1 - mw[1]) * damping, u[2] * damping,
+            u[0] * (theta - theta_b) * damping, 0.0};
+  }
   void max_abs_speeds(const State& u, double& l1, double& l2) const { eq.max_abs_speeds(u, l1, l2); }
 };
 
@@ -1447,6 +1480,20 @@ void* orc_pt_create_mesh(int polydeg, int nelem, const double* xy, const double*
                              bd_f, bd_kind);
   c->dg.reset(new DG2D<PTPhys>(c->phys, c->basis, c->mesh));
   return c;
+}
+
+// MountainWaveSetup's damping source (params as PTPhys::mw) and the states of
+// the Dirichlet boundary faces (kind 4) [B][n][5]
+void orc_pt_set_mountain(void* h, const double* mw, const double* bd_values) {
+  auto* c = static_cast<PTCase*>(h);
+  c->phys.mountain = mw != nullptr;
+  if (mw)
+    for (int k = 0; k < 8; ++k) c->phys.mw[k] = mw[k];
+  if (bd_values) {
+    const size_t nb = c->mesh.bd_e.size() * c->basis.n * 5;
+    c->mesh.bd_values.assign(bd_values, bd_values + nb);
+  }
+  c->dg.reset(new DG2D<PTPhys>(c->phys, c->basis, c->mesh));
 }
 
 void orc_pt_destroy(void* h) { delete static_cast<PTCase*>(h); }

@@ -34,8 +34,11 @@ struct Mesh2D {
   // secondary's face-node order
   std::vector<int> if_e0, if_f0, if_e1, if_f1, if_flip;
   // boundary faces: elem, face, kind (1 = slip wall, StructuredMesh semantics;
-  // 2 = slip wall, P4estMesh semantics)
+  // 2 = slip wall, P4estMesh semantics; 4 = Dirichlet, P4estMesh semantics)
   std::vector<int> bd_e, bd_f, bd_kind;
+  // Dirichlet states [B][n][nv] of the kind-4 faces (Trixi's
+  // BoundaryConditionDirichlet: surface flux of the inner and the given state)
+  std::vector<double> bd_values;
 };
 
 // Face node (i, j) of face f at face index l.
@@ -269,6 +272,18 @@ struct DG2D {
         fl = phys.bc_structured(ui, nrm, f + 1);
         const double s = sj * ((f % 2) ? 1.0 : -1.0);  // to outward
         for (int v = 0; v < nv; ++v) sf(e, f, l, v) = s * fl[v];
+      } else if (m.bd_kind[k] == 4) {
+        // BoundaryConditionDirichlet, P4estMesh method: surface flux (plus half
+        // the nonconservative surface flux) of the inner and the boundary state
+        outward_normal(e, f, l, nrm);
+        State ub;
+        for (int v = 0; v < nv; ++v) ub[v] = m.bd_values[((size_t)k * n + l) * nv + v];
+        fl = phys.surface_flux(ui, ub, nrm);
+        if (Phys::has_noncons) {
+          const State g = phys.surface_noncons(ui, ub, nrm);
+          for (int v = 0; v < nv; ++v) fl[v] += 0.5 * g[v];
+        }
+        for (int v = 0; v < nv; ++v) sf(e, f, l, v) = fl[v];
       } else {
         outward_normal(e, f, l, nrm);
         fl = phys.bc_normal(ui, nrm);

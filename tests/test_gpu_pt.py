@@ -159,3 +159,71 @@ def test_gpu_reproduces_well_balanced_curvilinear_golden(tg, orc, gpu_lib, name)
     l2, linf = semi.calc_error_norms(0.4)
     check_well_balanced(l2, linf, g2, gi)
     semi.close()
+
+
+def mountain_semi(tg, name, trees=(20, 12), polydeg=3):
+    from test_oracle_pt import mountain_case
+    eq, setup, mesh, basis, xy, invJ, arrays, bv, okw, solver = mountain_case(tg, name, trees,
+                                                                            polydeg)
+    bc = tg.BoundaryConditionDirichlet(setup)
+    semi = tg.SemidiscretizationHyperbolic(
+        mesh, eq, setup, solver, source_terms=setup,
+        boundary_conditions={"x_neg": bc, "x_pos": bc, "y_neg": tg.boundary_condition_slip_wall,
+                             "y_pos": bc})
+    return eq, setup, mesh, basis, xy, invJ, arrays, bv, okw, semi
+
+
+@pytest.mark.parametrize("polydeg", [2, 3, 4])
+@pytest.mark.parametrize("name", ["linear_hydrostatic", "schaer_mountain"])
+def test_pt_mountain_rhs_matches_oracle(tg, orc, gpu_lib, name, polydeg):
+    """Terrain-following P4estMesh, Dirichlet boundary states (left, right, top),
+    slip wall at the ground, MountainWaveSetup's damping source, on a perturbed
+    state (the damping acts in the absorbing layers)."""
+    eq, setup, mesh, basis, xy, invJ, arrays, bv, okw, semi = mountain_semi(tg, name, (8, 6),
+                                                                           polydeg)
+    # the host mirror's Dirichlet states are the setup at the boundary face nodes
+    dirichlet = arrays[-1] == 4
+    assert np.abs(semi._H.boundary_values[dirichlet] - bv[dirichlet]).max() == 0.0
+    u = perturbed(semi.compute_coefficients(), 30 + polydeg)
+    du = semi.rhs(u)
+    c = orc.PotTemp2D(polydeg, 0, 0, 0, 0, 0, 0, mesh=arrays, **okw)
+    c.set_mountain(setup.params(), bv)
+    du_ref = c.rhs(u)
+    assert np.abs(du - du_ref).max() <= 1e-12 * np.abs(du_ref).max(), (
+        np.abs(du - du_ref).max() / np.abs(du_ref).max())
+    for v in range(4):
+        s = np.abs(du_ref[..., v]).max()
+        assert np.abs(du[..., v] - du_ref[..., v]).max() <= 1e-11 * s, v
+    semi.close()
+
+
+@pytest.mark.parametrize("name", ["linear_hydrostatic", "linear_nonhydrostatic",
+                                  "schaer_mountain"])
+def test_gpu_reproduces_mountain_wave_golden(tg, orc, gpu_lib, name):
+    """test/test_2d_potential_temperature.jl:29-98 with every SSPRK43 stage on the
+    GPU at CFL 0.5 (standing in for the reference's adaptive steps), norms by
+    NumPy and on the device, at the tests' own tolerance (atol 1e-5); the state
+    against the oracle's run."""
+    import analysis
+    from test_oracle_pt import MOUNTAIN_CFL, check_mountain
+    eq, setup, mesh, basis, xy, invJ, arrays, bv, okw, semi = mountain_semi(tg, name)
+    semi.set_state(semi.compute_coefficients())
+    t, t_end = 0.0, 360.0
+    while t < t_end - 1e-9:
+        dt = MOUNTAIN_CFL * semi.max_dt()
+        if t + dt >= t_end:
+            t = semi.rk_steps(1, fixed_dt=t_end - t, t=t, method="SSPRK43")
+        else:
+            t = semi.rk_steps(1, cfl=MOUNTAIN_CFL, t=t, method="SSPRK43")
+    assert abs(t - t_end) < 1e-9
+    u = semi.get_state()
+    l2, linf = analysis.error_norms(u, xy, invJ, basis.nodes, lambda x: setup(x, 0.0, eq), 2)
+    check_mountain(name, l2, linf)
+    l2d, linfd = semi.calc_error_norms(t_end)
+    check_mountain(name, l2d, linfd)
+    c = orc.PotTemp2D(3, 0, 0, 0, 0, 0, 0, mesh=arrays, **okw)
+    c.set_mountain(setup.params(), bv)
+    uo = np.ascontiguousarray(semi.compute_coefficients())
+    c.ssp_steps(uo, 0.0, MOUNTAIN_CFL, 10 ** 7, 1, t_end=360.0)
+    assert np.abs(u[..., :4] - uo[..., :4]).max() <= 1e-10 * np.abs(uo[..., :4]).max()
+    semi.close()

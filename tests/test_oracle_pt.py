@@ -111,3 +111,133 @@ def check_well_balanced(l2, linf, g2, gi):
                 assert abs(got[v] / gold[v] - 1) <= 1e-6, (v, got[v], gold[v])
             else:
                 assert abs(got[v] - gold[v]) <= 1e-11, (v, got[v], gold[v])
+
+
+# test/test_2d_potential_temperature.jl:29-98: examples/euler/dry_air/mountain_flow/
+# elixir_potential_temperature_{linear_hydrostatic, linear_nonhydrostatic,
+# schaer_mountain}.jl with 20x12 trees of polydeg 3 to t = 360 s: a
+# terrain-following P4estMesh (transfinite mapping of terrain_following_faces),
+# MountainWaveSetup as initial condition, Dirichlet boundary data (left, right,
+# top) and Rayleigh-damping source, slip wall at the ground.  The reference
+# integrates with adaptive (error-controlled) SSPRK43; SSPRK43 at fixed CFL 0.5
+# stands in for it, and the tests' own tolerance (atol 1e-5) holds: the largest
+# deviations are 6.7e-6 (hydrostatic), 8.8e-6 (nonhydrostatic) and 4.7e-6 (Schaer).
+G_EARTH = 9.80616
+MOUNTAIN = {
+    "linear_hydrostatic": dict(
+        setup=dict(theta_0=250, u0=20, brunt_vaisala_frequency=G_EARTH / math.sqrt(1004.0 * 250),
+                   z_damping_start=15000, z_damping_end=30000, x_damping_start=60000,
+                   x_damping_end=120000, damping_rate=0.035),
+        topo=("witch", dict(height=1, half_width=10000)), L=240000, H=30000,
+        volume="tec", nc="waruszewski", c="isothermal250",
+        golden=([2.669332229493225e-6, 0.0006518362209690377, 0.00011039658133803138,
+                 0.00022353351014161769, 2.647509013539741e-11],
+                [2.7590006774769193e-5, 0.017497225180171938, 0.0018056117333556639,
+                 0.001078532265978538, 1.7462298274040222e-10])),
+    "linear_nonhydrostatic": dict(
+        setup=dict(theta_0=280, u0=10, brunt_vaisala_frequency=0.01, z_damping_start=15000,
+                   z_damping_end=30000, x_damping_start=40000, x_damping_end=72000,
+                   damping_rate=0.03),
+        topo=("witch", dict(height=1, half_width=1000)), L=144000, H=30000,
+        volume="etec", nc="artiano", c=340.0,
+        golden=([4.345825921806206e-7, 0.00018887049967917287, 0.00012755555800319474,
+                 8.576762747892351e-5, 2.7230966512302478e-11],
+                [1.0334839461112466e-5, 0.013797647921778733, 0.007887457557781355,
+                 0.0003272987411264694, 1.4551915228366852e-10])),
+    "schaer_mountain": dict(
+        setup=dict(theta_0=280, u0=10, brunt_vaisala_frequency=0.01, z_damping_start=13000,
+                   z_damping_end=21000, x_damping_start=20000, x_damping_end=25000,
+                   damping_rate=0.03),
+        topo=("schaer", dict(height=250, half_width=5000, wavelength=4000)), L=50000, H=21000,
+        volume="etec", nc="artiano", c=340.0,
+        golden=([0.00010948264917453087, 0.09903481134935169, 0.09822804596320808,
+                 0.004246742748260301, 1.8456576434476605e-11],
+                [0.0017570540164735249, 2.3792558995181707, 2.354152711825134,
+                 0.0764797692902448, 8.731149137020111e-11])),
+}
+MOUNTAIN_CFL = 0.5
+
+
+def mountain_case(tg, name, trees=(20, 12), polydeg=3):
+    """(equations, setup, mesh, basis, xy, invJ, oracle mesh arrays, Dirichlet
+    states [B, n, 5], oracle keyword arguments, solver) of one elixir."""
+    C = MOUNTAIN[name]
+    eq = tg.CompressibleEulerPotentialTemperatureEquationsWithGravity2D(c_p=1004, c_v=717,
+                                                                         gravity=G_EARTH)
+    setup = tg.MountainWaveSetup(**C["setup"])
+    kind, kw = C["topo"]
+    topo = tg.WitchOfAgnesi(**kw) if kind == "witch" else tg.SchaerMountain(**kw)
+    faces = tg.terrain_following_faces(topo, -C["L"] / 2, C["L"] / 2, C["H"])
+    mesh = tg.P4estMesh(trees, polydeg=polydeg, faces=faces, periodicity=(False, False))
+    basis = tg.LobattoLegendreBasis(polydeg)
+    xy, Ja, invJ = mesh.geometry(basis)
+    conn = mesh.connectivity()
+    ie, ifc, fl, be, bf = conn.arrays()
+    bk = np.array([2 if nm == "y_neg" else 4 for nm in conn.bd_names], dtype=np.int32)
+    n = polydeg + 1
+    li = np.arange(n)
+    bv = np.zeros((len(be), n, 5))
+    for k, (e, f) in enumerate(zip(be, bf)):
+        i = {0: 0 * li, 1: 0 * li + n - 1, 2: li, 3: li}[int(f)]
+        j = {0: li, 1: li, 2: 0 * li, 3: 0 * li + n - 1}[int(f)]
+        bv[k] = setup(xy[e, j, i], 0.0, eq)
+    c = (math.sqrt(eq.gamma * eq.R * 250.0) if C["c"] == "isothermal250" else C["c"])
+    okw = dict(volume={"tec": 0, "etec": 2}[C["volume"]],
+               nc={"waruszewski": 0, "artiano": 1}[C["nc"]], g=G_EARTH, c_lmars=c, surface=0,
+               snc=-1)
+    vf = {"tec": tg.flux_tec, "etec": tg.flux_etec}[C["volume"]]
+    ncf = {"waruszewski": tg.flux_nonconservative_waruszewski_etal,
+           "artiano": tg.flux_nonconservative_artiano_etal}[C["nc"]]
+    solver = tg.DGSEM(polydeg, (tg.FluxLMARS(c), tg.flux_zero),
+                      tg.VolumeIntegralFluxDifferencing((vf, ncf)))
+    return (eq, setup, mesh, basis, xy, invJ, (xy, Ja, invJ, ie, ifc, fl, be, bf, bk), bv, okw,
+            solver)
+
+
+def check_mountain(name, l2, linf, atol=1e-5):
+    g2, gi = MOUNTAIN[name]["golden"]
+    for v in range(5):
+        assert abs(l2[v] - g2[v]) <= atol, ("l2", v, l2[v], g2[v])
+        assert abs(linf[v] - gi[v]) <= atol, ("linf", v, linf[v], gi[v])
+
+
+@pytest.mark.parametrize("name", list(MOUNTAIN))
+def test_oracle_mountain_wave_golden(tg, orc, name):
+    import analysis
+    eq, setup, mesh, basis, xy, invJ, arrays, bv, okw, _ = mountain_case(tg, name)
+    c = orc.PotTemp2D(3, 0, 0, 0, 0, 0, 0, mesh=arrays, **okw)
+    c.set_mountain(setup.params(), bv)
+    u = np.ascontiguousarray(setup(xy, 0.0, eq))
+    t = c.ssp_steps(u, 0.0, MOUNTAIN_CFL, 10 ** 7, 1, t_end=360.0)
+    assert abs(t - 360.0) < 1e-9
+    l2, linf = analysis.error_norms(u, xy, invJ, basis.nodes, lambda x: setup(x, 0.0, eq), 2)
+    check_mountain(name, l2, linf)
+
+
+def test_terrain_following_mesh_and_damping(tg, orc):
+    """terrain_following_faces + the transfinite mapping put the bottom nodes on
+    the topography and the top nodes at z_top; MountainWaveSetup is at rest
+    relative to u0 where there is no damping, and its damping source is zero
+    inside the domain and relaxes towards the setup in the absorbing layers."""
+    eq, setup, mesh, basis, xy, invJ, arrays, bv, okw, _ = mountain_case(tg, "schaer_mountain",
+                                                                       (10, 6))
+    topo = tg.SchaerMountain(height=250, half_width=5000, wavelength=4000)
+    assert np.allclose(xy[:10, 0, :, 1], topo(xy[:10, 0, :, 0]), rtol=0, atol=1e-9)
+    assert np.allclose(xy[-10:, -1, :, 1], 21000.0, rtol=0, atol=1e-9)
+    assert (invJ > 0).all()
+    kw = dict(okw)
+    c_src = orc.PotTemp2D(3, 0, 0, 0, 0, 0, 0, mesh=arrays, **kw)
+    c_src.set_mountain(setup.params(), bv)
+    c_nos = orc.PotTemp2D(3, 0, 0, 0, 0, 0, 0, mesh=arrays, **kw)
+    c_nos.set_mountain(None, bv)
+    u = np.ascontiguousarray(setup(xy, 0.0, eq))
+    u[..., 1] *= 1.1
+    d = c_src.rhs(u) - c_nos.rhs(u)
+    x, z = xy[..., 0], xy[..., 1]
+    inside = (z <= 13000.0) & (np.abs(x) < 20000.0)
+    assert np.all(d[inside] == 0)
+    rate = np.zeros_like(z)
+    rate += np.where(z > 13000.0, 0.03 * np.sin(np.pi * 0.5 * (z - 13000.0) / 8000.0) ** 2, 0.0)
+    rate += np.where(x >= 20000.0, 0.03 * np.sin(np.pi * 0.5 * (x - 20000.0) / 5000.0) ** 2, 0.0)
+    rate += np.where(x <= -20000.0, 0.03 * np.sin(np.pi * 0.5 * (x + 20000.0) / -5000.0) ** 2, 0.0)
+    assert np.allclose(d[..., 1], -rate * (u[..., 1] - u[..., 0] * 10.0), rtol=1e-9, atol=1e-12)

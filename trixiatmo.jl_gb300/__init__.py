@@ -40,7 +40,10 @@ from .initial_conditions import (EARTH_GRAVITATIONAL_ACCELERATION, EARTH_RADIUS,
                                  initial_condition_convergence_test_moist,
                                  initial_condition_nonhydrostatic_gravity_wave,
                                  AtmosphereLayers, initial_condition_moist_bubble)
-from .meshes import P4estMesh, StructuredMesh
+from .meshes import (P4estMesh, SchaerMountain, SchärMountain, StructuredMesh, WitchOfAgnesi,
+                     terrain_following_faces)
+from .equations import BoundaryConditionDirichlet
+from .initial_conditions import MountainWaveSetup
 from .meshes3d import P4estMeshCubedSphereTopography
 from .semidiscretization import (DGSEM, SemidiscretizationCovariant,
                                  SemidiscretizationCovariantEnsemble, SemidiscretizationEnsemble,
@@ -67,6 +70,8 @@ __all__ = [
     "SemidiscretizationCovariantEnsemble", "source_terms_nonhydrostatic_gravity_wave",
     "initial_condition_nonhydrostatic_gravity_wave", "AtmosphereLayers",
     "initial_condition_moist_bubble", "flux_LMARS", "source_terms_no_phase_change",
+    "SchaerMountain", "SchärMountain", "WitchOfAgnesi", "terrain_following_faces",
+    "BoundaryConditionDirichlet", "MountainWaveSetup",
     "CompressibleEulerPotentialTemperatureEquationsWithGravity2D",
     "CompressibleEulerPotentialTemperatureEquationsWithGravity3D",
     "CompressibleEulerInternalEnergyEquationsWithGravity2D", "flux_conservative_etec",

@@ -31,6 +31,7 @@ TAG_SF_LAX_FRIEDRICHS = 2
 TAG_SRC_RAINY = 1
 TAG_SRC_RAINY_CONVERGENCE = 2
 TAG_BC_SIMPLE_SLIP_WALL = 3
+TAG_BC_DIRICHLET = 4
 TAG_EQ_MOIST_EULER_2D = 4
 TAG_VF_CHANDRASHEKAR = 4
 TAG_SF_CHANDRASHEKAR = 3
@@ -40,6 +41,7 @@ TAG_SRC_MOIST_CONVERGENCE_DRY = 5
 TAG_SRC_MOIST_CONVERGENCE = 6
 TAG_SRC_MOIST_GRAVITY_WAVE = 7
 TAG_SRC_RAINY_NO_PHASE_CHANGE = 8
+TAG_SRC_MOUNTAIN_WAVE = 9
 TAG_EQ_COVARIANT_SWE = 5
 TAG_EQ_POTENTIAL_TEMPERATURE_2D = 6
 TAG_EQ_POTENTIAL_TEMPERATURE_3D = 7
@@ -124,6 +126,8 @@ SIGNATURES = {
     "tag_rk_steps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double,
                                     ctypes.c_double, _dp]),
     "tag_set_time_integrator": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "tag_set_boundary_values": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "tag_set_source": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp, ctypes.c_int32]),
     "tag_analyze_integral": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                             ctypes.c_double, _dp]),
     "tag_analysis_nodes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), _dp]),

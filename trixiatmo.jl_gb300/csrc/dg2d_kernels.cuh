@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(256) k_interface(
     const double* __restrict__ invJ, const int* __restrict__ if_e, const int* __restrict__ if_f,
     const int* __restrict__ if_flip, int nif, const int* __restrict__ bd_e,
     const int* __restrict__ bd_f, const int* __restrict__ bd_kind, int nbd,
-    double* __restrict__ sfv) {
+    double* __restrict__ sfv, const double* __restrict__ bvals = nullptr) {
   constexpr int NV = Phys::NV, NA = Phys::NA;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int k = tid / n, l = tid % n;
@@ -139,6 +139,21 @@ __global__ void __launch_bounds__(256) k_interface(
       Phys::boundary_flux(P, ui, n1, n2, f, kind, F);
 #pragma unroll
       for (int v = 0; v < NA; ++v) F[v] *= sj;
+    } else if (kind == TAG_BC_DIRICHLET) {
+      // BoundaryConditionDirichlet (P4estMesh method): the surface flux of the
+      // inner and the given state along the outward normal, plus half the
+      // nonconservative surface flux
+      const double so = (f & 1) ? 1.0 : -1.0;
+      double ub[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) ub[v] = bvals[((size_t)kb * n + l) * NV + v];
+      Phys::surface_flux(P, ui, ub, so * n1, so * n2, F);
+      if constexpr (Phys::kSurfaceNoncons) {
+        double G[NA];
+        Phys::surface_noncons(P, ui, ub, so * n1, so * n2, G);
+#pragma unroll
+        for (int v = 0; v < NA; ++v) F[v] += 0.5 * G[v];
+      }
     } else {
       const double so = (f & 1) ? 1.0 : -1.0;
       Phys::boundary_flux(P, ui, so * n1, so * n2, f, kind, F);

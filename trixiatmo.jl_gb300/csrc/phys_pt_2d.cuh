@@ -23,7 +23,8 @@ struct PhysPT2D {
   static constexpr int NQ = 11;
   static constexpr int kRho = 0, kBeta = 0, kLogRho = 0, kLogBeta = 0;
   static constexpr bool kNodeLogs = false;
-  static constexpr bool kHasSources = false;
+  // MountainWaveSetup's Rayleigh damping when set (Params::mountain)
+  static constexpr bool kHasSources = true;
   // surface flux (FluxLMARS(c), flux_zero) or (flux_ec, a nonconservative
   // gravity term); the interface kernel adds the per-side term when snc >= 0
   static constexpr bool kSurfaceNoncons = true;
@@ -35,6 +36,10 @@ struct PhysPT2D {
     int nc;                              // 0 waruszewski, 1 artiano, 2 souza
     int surface;                         // 0 FluxLMARS(c), 1 flux_ec
     int snc;                             // surface gravity term: -1 none (flux_zero), else as nc
+    int mountain;                        // 1: MountainWaveSetup's damping source
+    double g;                            // gravity
+    double mw[8];  // theta_0, u0, N, z_damping_start, z_damping_end, x_damping_start,
+                   // x_damping_end, damping_rate
   };
 
   // params = (c_p, c_v, g, LMARS c, nonconservative kind, volume kind,
@@ -50,6 +55,9 @@ struct PhysPT2D {
     q.volume = (int)p[5];
     q.surface = (int)p[6];
     q.snc = (int)p[7] - 1;
+    q.mountain = 0;
+    q.g = p[2];
+    for (int k = 0; k < 8; ++k) q.mw[k] = 0.0;
     double a[8], b[8];
     for (int j = 0; j < 8; ++j) {
       double ra = 1.0, rb = 1.0;
@@ -201,6 +209,36 @@ struct PhysPT2D {
 
   // the nonconservative gravity term of the surface flux, G(ul, ur) along the
   // primary's normal (zero for flux_zero)
+  // MountainWaveSetup as source terms (src/equations/initial_condition_compressible_euler_2d.jl:174-200):
+  // relaxation of v1 to u0, of v2 to 0 and of theta to theta_0 exp(N^2 z / g)
+  // at the rate of rayleigh_damping_coefficient (:80-106), a sum of sin^2
+  // ramps above z_damping_start and beyond +-x_damping_start
+  TAG_DEV static void source(const Params& P, const double* u, const double* x, double,
+                             double* s) {
+    s[0] = s[1] = s[2] = s[3] = 0.0;
+    if (!P.mountain) return;
+    const double rate = P.mw[7], zs = P.mw[3], ze = P.mw[4], xs = P.mw[5], xe = P.mw[6];
+    double dv = 0.0, dr = 0.0, dl = 0.0;
+    if (x[1] > zs) {
+      const double r = sinpi(0.5 * (x[1] - zs) / (ze - zs));
+      dv = rate * (r * r);
+    }
+    if (!(x[0] < xs)) {
+      const double r = sinpi(0.5 * (x[0] - xs) / (xe - xs));
+      dr = rate * (r * r);
+    }
+    if (!(x[0] > -xs)) {
+      const double r = sinpi(0.5 * (x[0] + xs) / (-xe + xs));
+      dl = rate * (r * r);
+    }
+    const double damping = -(dv + dr + dl);
+    const double v1 = u[1] / u[0], theta = u[3] / u[0];
+    const double theta_b = P.mw[0] * exp(P.mw[2] * P.mw[2] / P.g * x[1]);
+    s[1] = u[0] * (v1 - P.mw[1]) * damping;
+    s[2] = u[2] * damping;
+    s[3] = u[0] * (theta - theta_b) * damping;
+  }
+
   TAG_DEV static void surface_noncons(const Params& P, const double* ul, const double* ur,
                                       double n1, double n2, double* G) {
     G[0] = G[1] = G[2] = G[3] = 0.0;

@@ -80,6 +80,10 @@ struct tag_handle_s {
          *d_sfv = nullptr, *d_tmp_u = nullptr, *d_tmp_du = nullptr;
   int *d_if_e = nullptr, *d_if_f = nullptr, *d_if_flip = nullptr, *d_bd_e = nullptr,
       *d_bd_f = nullptr, *d_bd_kind = nullptr;
+  // states of the TAG_BC_DIRICHLET faces [B][n][nv] (allocated when the mesh has
+  // such faces; the interface kernel reads them)
+  double* d_bvals = nullptr;
+  bool need_bvals = false, bvals_set = false;
   int nmembers = 1;
   int* d_member = nullptr;        // [E] or null
   double* d_mscal = nullptr;      // [3 * nmembers]: t, dt, max_speed
@@ -163,9 +167,11 @@ struct OpsImpl {
     const int total = (h->nif + h->nbd) * n;
     if (total == 0) return TAG_OK;
     const int threads = 256;
+    if (h->need_bvals && !h->bvals_set)
+      return fail(TAG_E_INVALID, "Dirichlet boundary faces without states (tag_set_boundary_values)");
     k_interface<Phys, n><<<(total + threads - 1) / threads, threads, 0, h->stream>>>(
         params_of<Phys>(h), u, h->d_Ja, h->d_invJ, h->d_if_e, h->d_if_f, h->d_if_flip, h->nif,
-        h->d_bd_e, h->d_bd_f, h->d_bd_kind, h->nbd, h->d_sfv);
+        h->d_bd_e, h->d_bd_f, h->d_bd_kind, h->nbd, h->d_sfv, h->d_bvals);
     TAG_CUDA(cudaGetLastError());
     return TAG_OK;
   }
@@ -773,13 +779,15 @@ bool boundary_kind_ok(int eq, int kind) {
     case TAG_EQ_EULER_ENERGY_2D:
     case TAG_EQ_MOIST_EULER_2D:
     case TAG_EQ_POTENTIAL_TEMPERATURE_2D:
-      return kind == TAG_BC_SLIP_WALL_STRUCTURED || kind == TAG_BC_SLIP_WALL_NORMAL;
+      return kind == TAG_BC_SLIP_WALL_STRUCTURED || kind == TAG_BC_SLIP_WALL_NORMAL ||
+             kind == TAG_BC_DIRICHLET;
     case TAG_EQ_EULER_ENERGY_3D:
     case TAG_EQ_POTENTIAL_TEMPERATURE_3D: return kind == TAG_BC_SLIP_WALL_NORMAL;
     case TAG_EQ_RAINY_2D:
       return kind == TAG_BC_SIMPLE_SLIP_WALL || kind == TAG_BC_SLIP_WALL_STRUCTURED ||
-             kind == TAG_BC_SLIP_WALL_NORMAL;
-    case TAG_EQ_INTERNAL_ENERGY_2D: return kind == TAG_BC_SLIP_WALL_NORMAL;
+             kind == TAG_BC_SLIP_WALL_NORMAL || kind == TAG_BC_DIRICHLET;
+    case TAG_EQ_INTERNAL_ENERGY_2D:
+      return kind == TAG_BC_SLIP_WALL_NORMAL || kind == TAG_BC_DIRICHLET;
     default: return false;
   }
 }
@@ -1063,6 +1071,11 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
   if (cfg->boundary_kinds)
     if ((rc = upload(&h->d_bd_kind, cfg->boundary_kinds, (size_t)h->nbd, h->stream)))
       return cleanup(rc);
+  for (int k = 0; cfg->boundary_kinds && k < h->nbd; ++k)
+    h->need_bvals = h->need_bvals || cfg->boundary_kinds[k] == TAG_BC_DIRICHLET;
+  if (h->need_bvals)
+    if ((rc = upload(&h->d_bvals, (const double*)nullptr, (size_t)h->nbd * n * h->nv, h->stream)))
+      return cleanup(rc);
   if (cfg->nmembers > 1)
     if ((rc = upload(&h->d_member, cfg->element_member, (size_t)h->nelem, h->stream)))
       return cleanup(rc);
@@ -1106,7 +1119,7 @@ int tag_destroy(tag_handle h) {
   double* dp[] = {h->d_u,       h->d_k,       h->d_Ja,         h->d_invJ,    h->d_xy,
                   h->d_sfv,     h->d_tmp_u,   h->d_tmp_du,     h->d_an_wj,   h->d_an_V,
                   h->d_an_wa,   h->d_an_rows, h->d_an_erows,   h->d_an_out,  h->d_an_uex,
-                  h->d_an_x};
+                  h->d_an_x,    h->d_bvals};
   for (double* p : dp)
     if (p) cudaFree(p);
   int* ip[] = {h->d_if_e, h->d_if_f, h->d_if_flip, h->d_bd_e, h->d_bd_f, h->d_bd_kind};
@@ -1272,6 +1285,30 @@ int tag_time_kernels(tag_handle h, int32_t reps, double* ms_interface, double* m
   *ms_interface = si / reps;
   *ms_element = se / reps;
   h->speed_valid = false;
+  return TAG_OK;
+}
+
+int tag_set_boundary_values(tag_handle h, const double* values) {
+  if (!h || !values) return fail(TAG_E_INVALID, "bad argument");
+  if (!h->need_bvals) return fail(TAG_E_INVALID, "the mesh has no Dirichlet boundary faces");
+  const size_t bytes = (size_t)h->nbd * h->n * h->nv * sizeof(double);
+  TAG_CUDA(cudaMemcpyAsync(h->d_bvals, values, bytes, cudaMemcpyHostToDevice, h->stream));
+  TAG_CUDA(cudaStreamSynchronize(h->stream));
+  h->bvals_set = true;
+  return TAG_OK;
+}
+
+int tag_set_source(tag_handle h, int32_t kind, const double* params, int32_t nparams) {
+  if (!h) return fail(TAG_E_INVALID, "bad argument");
+  if (h->eq != TAG_EQ_POTENTIAL_TEMPERATURE_2D || kind != TAG_SRC_MOUNTAIN_WAVE)
+    return fail(TAG_E_INVALID, "unsupported source for these equations");
+  if (!params || nparams != 8) return fail(TAG_E_INVALID, "MountainWaveSetup needs 8 parameters");
+  if (!h->d_xy) return fail(TAG_E_INVALID, "this source needs node coordinates");
+  if (!(params[4] > params[3]) || !(params[6] > params[5]) || !(params[7] >= 0.0))
+    return fail(TAG_E_INVALID, "bad damping layers");
+  h->p_pt.mountain = 1;
+  for (int k = 0; k < 8; ++k) h->p_pt.mw[k] = params[k];
+  h->graph_epb = -2;  // the parameters are baked into the captured graph
   return TAG_OK;
 }
 

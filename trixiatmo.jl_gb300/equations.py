@@ -279,6 +279,21 @@ class _BC:
 
 
 boundary_condition_slip_wall = _BC("boundary_condition_slip_wall")
+
+
+class BoundaryConditionDirichlet:
+    """Trixi's BoundaryConditionDirichlet(boundary_value_function): the
+    surface flux (plus half the nonconservative surface flux) of the inner
+    state and boundary_value_function(x, t, equations) at the boundary node.
+    The boundary states are evaluated on the host at the boundary nodes when
+    the semidiscretization is built (the function is taken as
+    time-independent, as MountainWaveSetup is) and uploaded to the device."""
+
+    def __init__(self, boundary_value_function):
+        self.boundary_value_function = boundary_value_function
+
+    def __repr__(self):
+        return f"BoundaryConditionDirichlet({self.boundary_value_function})"
 boundary_condition_periodic = _BC("boundary_condition_periodic")
 boundary_condition_simple_slip_wall = _BC("boundary_condition_simple_slip_wall")
 

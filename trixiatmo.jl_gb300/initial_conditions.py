@@ -252,6 +252,46 @@ class MoistBubbleRainy:
         return np.stack([rd, rm, rr, z0, z0, e, rv, rc, T], axis=-1)
 
 
+class MountainWaveSetup:
+    """Uniform flow u0 over a stratification of constant Brunt-Vaisala
+    frequency N and surface potential temperature theta_0
+    (src/equations/initial_condition_compressible_euler_2d.jl:107-200): called
+    with (x, t, equations) it is the initial (and Dirichlet boundary) state,
+    theta = theta_0 exp(N^2 z / g), Exner pressure
+    1 + g^2 / (c_p theta_0 N^2) (exp(-N^2 z / g) - 1); passed as source_terms
+    it is the Rayleigh damping towards that state in the absorbing layers
+    (above z_damping_start, beyond +-x_damping_start)."""
+
+    def __init__(self, *, theta_0, u0, brunt_vaisala_frequency, z_damping_start, z_damping_end,
+                 x_damping_start, x_damping_end, damping_rate):
+        self.theta_0, self.u0 = float(theta_0), float(u0)
+        self.brunt_vaisala_frequency = float(brunt_vaisala_frequency)
+        self.z_damping_start, self.z_damping_end = float(z_damping_start), float(z_damping_end)
+        self.x_damping_start, self.x_damping_end = float(x_damping_start), float(x_damping_end)
+        self.damping_rate = float(damping_rate)
+
+    def params(self):
+        """(theta_0, u0, N, z_damping_start, z_damping_end, x_damping_start,
+        x_damping_end, damping_rate), the device source's parameters."""
+        return [self.theta_0, self.u0, self.brunt_vaisala_frequency, self.z_damping_start,
+                self.z_damping_end, self.x_damping_start, self.x_damping_end, self.damping_rate]
+
+    def __call__(self, x, t, equations):
+        eq = equations
+        g, c_p, R = eq.g, eq.c_p, eq.R
+        Nf = self.brunt_vaisala_frequency
+        z = x[..., 1]
+        exner = 1.0 + g * g / (c_p * self.theta_0 * (Nf * Nf)) * (np.exp(-(Nf * Nf) / g * z) - 1.0)
+        p = eq.p_0 * exner ** (c_p / R)
+        theta = self.theta_0 * np.exp((Nf * Nf) / g * z)
+        T = theta * exner
+        rho = p / (R * T)
+        return eq.prim2cons(rho, self.u0 + 0.0 * rho, 0.0 * rho, p, g * z)
+
+    def __repr__(self):
+        return "MountainWaveSetup"
+
+
 # ---- CompressibleMoistEulerEquations2D ------------------------------------
 def initial_condition_gemein_bubble(x, t, equations):
     """Warm bubble of examples/euler/dry_air/buoyancy/elixir_gemein_bubble.jl:20-51

@@ -69,6 +69,61 @@ def transfinite_mapping(faces):
     return mapping
 
 
+class WitchOfAgnesi:
+    """Bell-shaped ridge h(x) = height / (1 + (x / half_width)^2)
+    (src/equations/initial_condition_compressible_euler_2d.jl:229-258)."""
+
+    def __init__(self, *, height, half_width):
+        self.height, self.half_width = float(height), float(half_width)
+
+    def __call__(self, x):
+        return self.height / (1.0 + (x / self.half_width) ** 2)
+
+
+class SchaerMountain:
+    """Schaer et al.'s ridges h(x) = height exp(-(x / half_width)^2)
+    cos^2(pi x / wavelength) (initial_condition_compressible_euler_2d.jl:202-227)."""
+
+    def __init__(self, *, height, half_width, wavelength):
+        self.height, self.half_width = float(height), float(half_width)
+        self.wavelength = float(wavelength)
+
+    def __call__(self, x):
+        return (self.height * np.exp(-(x / self.half_width) ** 2) *
+                np.cos(np.pi * (x / self.wavelength)) ** 2)
+
+
+SchärMountain = SchaerMountain
+
+
+def terrain_following_faces(topography, x_min, x_max, z_top):
+    """(left, right, bottom, top) boundary curves of a terrain-following
+    domain [x_min, x_max] x [topography(x), z_top]
+    (initial_condition_compressible_euler_2d.jl:260-285); each s in [-1, 1] ->
+    (x, z)."""
+    x_min, x_max, z_top = float(x_min), float(x_max), float(z_top)
+    x_mid = 0.5 * (x_min + x_max)
+    x_half = 0.5 * (x_max - x_min)
+    z_left, z_right = float(topography(x_min)), float(topography(x_max))
+
+    def x_of(s):
+        return x_mid + x_half * s
+
+    def f_left(s):
+        return x_min + 0.0 * s, z_left + (z_top - z_left) * 0.5 * (s + 1)
+
+    def f_right(s):
+        return x_max + 0.0 * s, z_right + (z_top - z_right) * 0.5 * (s + 1)
+
+    def f_bottom(s):
+        return x_of(s), topography(x_of(s))
+
+    def f_top(s):
+        return x_of(s), z_top + 0.0 * s
+
+    return f_left, f_right, f_bottom, f_top
+
+
 class StructuredMesh:
     """2D StructuredMesh on [xmin, xmax] x [ymin, ymax], or of a mapping
     (xi, eta) in [-1, 1]^2 -> (x, y), or of four boundary curves `faces`
@@ -176,13 +231,17 @@ class P4estMesh:
     normal_walls = True
 
     def __init__(self, trees_per_dimension, *, polydeg=1, coordinates_min=None,
-                 coordinates_max=None, mapping=None, initial_refinement_level=0,
+                 coordinates_max=None, mapping=None, faces=None, initial_refinement_level=0,
                  periodicity=True):
         """mapping(xi, eta) -> (x, y) of the global reference square [-1, 1]^2
         (the `mapping` keyword of the reference's P4estMesh, e.g.
-        examples/euler/dry_air/tests/elixir_potential_temperature_well_balanced_curvilinear.jl);
+        examples/euler/dry_air/tests/elixir_potential_temperature_well_balanced_curvilinear.jl),
+        or the transfinite mapping of four boundary curves `faces` (e.g.
+        terrain_following_faces, examples/euler/dry_air/mountain_flow/*.jl);
         otherwise the affine map of coordinates_min / coordinates_max.  Trees
         are not refined when a mapping is given."""
+        if faces is not None:
+            mapping = transfinite_mapping(faces)
         tx, ty = map(int, trees_per_dimension)
         if isinstance(periodicity, bool):
             periodicity = (periodicity, periodicity)

@@ -39,7 +39,8 @@ from .equations import (CompressibleEulerInternalEnergyEquationsWithGravity2D,
                         boundary_condition_simple_slip_wall, boundary_condition_slip_wall,
                         flux_chandrashekar, flux_ec_rain, flux_lax_friedrichs, flux_LMARS,
                         flux_nonconservative_waruszewski_etal, flux_ranocha, flux_zero)
-from .initial_conditions import EARTH_ROTATION_RATE
+from .equations import BoundaryConditionDirichlet
+from .initial_conditions import EARTH_ROTATION_RATE, MountainWaveSetup
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)
@@ -153,8 +154,8 @@ def _flux_ids(equations, solver, source_terms=None):
                 and (sf[1] is flux_zero or id(sf[1]) in nc_ids)):
             # (flux_ec, flux_zero | a nonconservative gravity term) at the surface
             snc = 0 if sf[1] is flux_zero else nc_ids[id(sf[1])]
-            if source_terms is not None:
-                raise ValueError("source terms are not supported for this equation set")
+            if source_terms is not None and not isinstance(source_terms, MountainWaveSetup):
+                raise ValueError(f"unsupported source terms {source_terms}")
             return vid, _lib.TAG_SF_PT_EC, [equations.c_p, equations.c_v, equations.g, 0.0,
                                             float(nc), 0.0, 0.0, float(snc)]
         if not (isinstance(sf, tuple) and isinstance(sf[0], FluxLMARS) and sf[1] is flux_zero):
@@ -166,8 +167,8 @@ def _flux_ids(equations, solver, source_terms=None):
                 raise ValueError(f"unsupported source terms {source_terms}")
             omega = EARTH_ROTATION_RATE if source_terms is source_terms_coriolis else 0.0
             return vid, _lib.TAG_SF_LMARS, params + [0.0, omega]
-        if source_terms is not None:
-            raise ValueError("source terms are not supported for this equation set")
+        if source_terms is not None and not isinstance(source_terms, MountainWaveSetup):
+            raise ValueError(f"unsupported source terms {source_terms}")
         return vid, _lib.TAG_SF_LMARS, params
     if isinstance(equations, CompressibleEulerEnergyEquationsWithGravity3D):
         if not (isinstance(vf, tuple) and vf[0] is flux_ranocha
@@ -200,6 +201,8 @@ def _bc_kinds(names, boundary_conditions, ndims, normal_walls=False):
         bc = bcs.get(name)
         if bc is boundary_condition_simple_slip_wall:
             kinds.append(_lib.TAG_BC_SIMPLE_SLIP_WALL)
+        elif isinstance(bc, BoundaryConditionDirichlet) and ndims == 2 and normal_walls:
+            kinds.append(_lib.TAG_BC_DIRICHLET)
         elif bc is boundary_condition_slip_wall:
             # StructuredMesh (2D) reaches the reference's orientation-argument
             # method; P4estMesh (the 3D shell) the normal-vector method
@@ -222,6 +225,7 @@ class _Handle:
             raise ValueError("mesh and equations dimensions differ")
         coords, Ja, invJ = [], [], []
         ie, ifc, fl, be, bf, bk, member = [], [], [], [], [], [], []
+        self._bd_names = []
         cache = {}
         offset = 0
         for m, mesh in enumerate(meshes):
@@ -235,6 +239,7 @@ class _Handle:
             coords.append(xy); Ja.append(ja); invJ.append(ij)
             ie.append(a_ie + offset); ifc.append(a_ifc); fl.append(a_fl)
             be.append(a_be + offset); bf.append(a_bf)
+            self._bd_names.append(list(conn.bd_names))
             bk.append(np.asarray(_bc_kinds(conn.bd_names, boundary_conditions, self.ndims,
                                            getattr(mesh, "normal_walls", False)),
                                  dtype=np.int32))
@@ -284,6 +289,32 @@ class _Handle:
         _lib.check(L.tag_create(ctypes.byref(cfg), ctypes.byref(h)))
         self.h = h
         self.L = L
+        if isinstance(source_terms, MountainWaveSetup):
+            mw = np.ascontiguousarray(source_terms.params(), dtype=np.float64)
+            _lib.check(L.tag_set_source(h, _lib.TAG_SRC_MOUNTAIN_WAVE, _ptr(mw), 8))
+        if np.any(bk == _lib.TAG_BC_DIRICHLET):
+            self.boundary_values = self._dirichlet_states(be, bf, bk, boundary_conditions)
+            _lib.check(L.tag_set_boundary_values(h, _ptr(self.boundary_values)))
+
+    def _dirichlet_states(self, be, bf, bk, boundary_conditions):
+        """[B, n, nv] states of BoundaryConditionDirichlet at the boundary face
+        nodes (Trixi evaluates boundary_value_function(x, t, equations) there;
+        the state is taken at t = 0)."""
+        n, nv = self.n, self.equations.nvariables
+        names = []
+        for mesh_conn_names in self._bd_names:
+            names.extend(mesh_conn_names)
+        out = np.zeros((len(be), n, nv))
+        li = np.arange(n)
+        for k, (e, f) in enumerate(zip(be, bf)):
+            if bk[k] != _lib.TAG_BC_DIRICHLET:
+                continue
+            i = {0: 0 * li, 1: 0 * li + n - 1, 2: li, 3: li}[int(f)]
+            j = {0: li, 1: li, 2: 0 * li, 3: 0 * li + n - 1}[int(f)]
+            x = self.node_coordinates[e, j, i]
+            fn = boundary_conditions[names[k]].boundary_value_function
+            out[k] = fn(x, 0.0, self.equations)
+        return out
 
     def close(self):
         if getattr(self, "h", None):
