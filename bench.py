@@ -374,13 +374,15 @@ def flops_per_node_covariant(n, variant):
     the reference formulas (covariant_shallow_water.jl, _split.jl) with a
     division as one flop.  Weak form: both contravariant fluxes 23, the D_hat
     contraction 12 n, the surface terms 24 / n, Jacobian and source sum 6, the
-    geometric + Coriolis source 49, the stage update 15.  Split EC form: per
-    direction flux_ec over the symmetric pairs 10 (n - 1) and the
-    nonconservative flux_ec over all n partners 26 n, per-node velocities 13,
-    surface 24 / n, Jacobian 10, the split source 67, the stage update 15."""
+    geometric + Coriolis source 49, the stage update 15.  Split EC form, as
+    the kernel evaluates it (the pair fluxes regrouped into contractions of
+    node quantities): per direction 13 per symmetric partner (n - 1), 7 per
+    nonconservative partner (n), 47 to combine the sums; 2 to add the
+    nonconservative part, per-node velocities 13, surface 24 / n, Jacobian
+    10, the split source 67, the stage update 15."""
     if variant == "weak":
         return 93 + 12 * n + 24.0 / n
-    return 2 * (10 * (n - 1) + 26 * n) + 13 + 10 + 67 + 15 + 24.0 / n
+    return 2 * (13 * (n - 1) + 7 * n + 47) + 2 + 13 + 10 + 67 + 15 + 24.0 / n
 
 
 def flops_per_element_launch_3d(n, nelem):

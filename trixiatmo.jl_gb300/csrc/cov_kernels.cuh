@@ -350,6 +350,68 @@ TAG_DEV void cov_element_body(const CovParams& P, const CovGroup& G, int lblk,
 #pragma unroll
         for (int v = 0; v < 3; ++v) acc[v] = fma(d2, F2[v], fma(d1, F1[v], acc[v]));
       }
+    } else if (P.split && P.vol_sym <= 1) {
+      // Split form with flux_central or flux_ec (and flux_nonconservative_ec):
+      // every pair flux is a sum of products of a node-a factor and a node-b
+      // factor, so each line sum sum_b D_ab f(a, b) is formed from a few
+      // contractions sum_b D_ab x_b of node-b quantities (the pair terms of
+      // covariant_shallow_water_split.jl:100-215 regrouped; 10 instead of
+      // ~33 FP64 operations per partner node).  b = a is left out of the
+      // symmetric part and kept in the nonconservative part, as in the
+      // pairwise form.
+      const double* qa = qn;
+      const double h_a = ui[0], hs_a = qa[7], J_a = qa[8];
+      const double gh = P.g * h_a;
+      double nc1 = 0.0, nc2 = 0.0;
+#pragma unroll
+      for (int d = 0; d < 2; ++d) {
+        const double hvo_a = d ? ui[2] : ui[1];
+        const double Jhvo_a = d ? qa[5] : qa[4];
+        const double gco0 = d ? qa[10] : qa[9], gco1 = d ? qa[11] : qa[10];
+        const int a = d ? j : i;
+        double SD = 0.0, A1 = 0.0, A2 = 0.0, A3 = 0.0, A4 = 0.0, A5 = 0.0;
+        double B2 = 0.0, B3 = 0.0, BH = 0.0;
+#pragma unroll
+        for (int b = 0; b < n; ++b) {
+          const double* qb = eq + (d ? b * n + i : j * n + b) * kCovQ;
+          const double Dab = sb->Ds[a * n + b];
+          if (b != a) {
+            const double Jb = d ? qb[5] : qb[4];
+            SD += Dab;
+            A1 = fma(Dab, Jb, A1);
+            A2 = fma(Dab, qb[0], A2);
+            A3 = fma(Dab, qb[0] * Jb, A3);
+            A4 = fma(Dab, qb[1], A4);
+            A5 = fma(Dab, qb[1] * Jb, A5);
+          }
+          if (P.vol_nc) {
+            B2 = fma(Dab, qb[2], B2);
+            B3 = fma(Dab, qb[3], B3);
+            BH = fma(Dab, qb[6] + qb[7], BH);
+          }
+        }
+        acc[0] += 0.5 * (Jhvo_a * SD + A1);
+        if (P.vol_sym == 1) {
+          // flux_ec: f = m (1, (v_a + v_b) / 2), m = (J hv_a + J hv_b) / 2
+          acc[1] += 0.25 * ((qa[0] * Jhvo_a) * SD + qa[0] * A1 + Jhvo_a * A2 + A3);
+          acc[2] += 0.25 * ((qa[1] * Jhvo_a) * SD + qa[1] * A1 + Jhvo_a * A4 + A5);
+        } else {
+          // flux_central of the split fluxes: (J hv v_a + J hv v_b) / 2
+          acc[1] += 0.5 * ((Jhvo_a * qa[0]) * SD + A3);
+          acc[2] += 0.5 * ((Jhvo_a * qa[1]) * SD + A5);
+        }
+        if (P.vol_nc) {
+          const double Daa = sb->Ds[a * n + a];
+          const double Sall = SD + Daa;
+          const double B0 = fma(Daa, qa[0], A2), B1 = fma(Daa, qa[1], A4);
+          const double half_m = 0.5 * hvo_a;
+          const double ph = gh * (BH - hs_a * Sall);
+          nc1 += J_a * (half_m * (qa[9] * B2 + qa[10] * B3 - B0) + gco0 * ph);
+          nc2 += J_a * (half_m * (qa[10] * B2 + qa[11] * B3 - B1) + gco1 * ph);
+        }
+      }
+      acc[1] += 0.5 * nc1;
+      acc[2] += 0.5 * nc2;
     } else {
       const double* qa = qn;
       const double h_a = ui[0], hs_a = qa[7], J_a = qa[8];
