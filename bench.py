@@ -318,8 +318,8 @@ def run_swe(args):
             mesh = ens_s.meshes[i]
             basis = ens_s.solvers[i].basis
             conn = mesh.connectivity(basis)
-            ie, ifc, fl, _, _ = conn.arrays()
-            c = orc.CovSWE(basis.n - 1, ens_s._H.aux[i], ens_s._H.xyz[i], ie, ifc, fl,
+            ie, ifc, flip, _, _ = conn.arrays()
+            c = orc.CovSWE(basis.n - 1, ens_s._H.aux[i], ens_s._H.xyz[i], ie, ifc, flip,
                            eq.gravity, eq.rotation_rate, eq.split, cov_ids)
             um = np.ascontiguousarray(ens_s.member_state(ens_s.compute_coefficients(), i))
             c.ck_steps(um, np.zeros_like(um), 0.0, 0.4, args.cpu_steps)

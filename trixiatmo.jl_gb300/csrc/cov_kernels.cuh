@@ -288,7 +288,9 @@ __global__ void __launch_bounds__(256) k_cov_interface(CovParams P, const CovGro
 constexpr int kCovQ = 13;
 __host__ __device__ constexpr int cov_elem_doubles(int n) { return n * n * kCovQ; }
 
-template <int n, int MODE>
+// VK: 0 weak form (VolumeIntegralWeakForm), 1 flux differencing; a template
+// parameter so that each volume kind gets its own register allocation
+template <int n, int MODE, int VK>
 TAG_DEV void cov_element_body(const CovParams& P, const CovGroup& G, int lblk,
                               const BasisDev* __restrict__ bases, double* __restrict__ u,
                               double* __restrict__ du, double* __restrict__ kreg,
@@ -316,7 +318,7 @@ TAG_DEV void cov_element_body(const CovParams& P, const CovGroup& G, int lblk,
 #pragma unroll
     for (int k = 0; k < kPack; ++k) p[k] = __ldg(pg + k);
     ih = 1.0 / ui[0];
-    if (P.volume == 0) {
+    if constexpr (VK == 0) {
       cov_flux(P, ui, ih, p, 0, qn);
       cov_flux(P, ui, ih, p, 1, qn + 3);
     } else {
@@ -341,7 +343,7 @@ TAG_DEV void cov_element_body(const CovParams& P, const CovGroup& G, int lblk,
   if (act) {
     const double* eq = q + el * nn * kCovQ;
     double acc[3] = {0.0, 0.0, 0.0};
-    if (P.volume == 0) {
+    if constexpr (VK == 0) {
 #pragma unroll
       for (int b = 0; b < n; ++b) {
         const double d1 = sb->Dh[i * n + b], d2 = sb->Dh[j * n + b];
@@ -519,8 +521,10 @@ TAG_DEV void cov_element_body(const CovParams& P, const CovGroup& G, int lblk,
   }
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(256) k_cov_element(CovParams P, const CovGroups* __restrict__ GG,
+// 256 threads and at least three CTAs per SM: up to 85 registers, which the
+// FP64-latency-bound body uses for independent operations in flight
+template <int MODE, int VK>
+__global__ void __launch_bounds__(256, 3) k_cov_element(CovParams P, const CovGroups* __restrict__ GG,
                                                      const BasisDev* __restrict__ bases,
                                                      double* __restrict__ u,
                                                      double* __restrict__ du,
@@ -534,13 +538,13 @@ __global__ void __launch_bounds__(256) k_cov_element(CovParams P, const CovGroup
   const int lblk = blockIdx.x - G.blk0;
   unsigned bad = 0;
   switch (G.n) {
-    case 4: cov_element_body<4, MODE>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
-    case 6: cov_element_body<6, MODE>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
-    case 8: cov_element_body<8, MODE>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
-    case 2: cov_element_body<2, MODE>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
-    case 3: cov_element_body<3, MODE>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
-    case 5: cov_element_body<5, MODE>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
-    case 7: cov_element_body<7, MODE>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
+    case 4: cov_element_body<4, MODE, VK>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
+    case 6: cov_element_body<6, MODE, VK>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
+    case 8: cov_element_body<8, MODE, VK>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
+    case 2: cov_element_body<2, MODE, VK>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
+    case 3: cov_element_body<3, MODE, VK>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
+    case 5: cov_element_body<5, MODE, VK>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
+    case 7: cov_element_body<7, MODE, VK>(P, G, lblk, bases, u, du, kreg, pk, sfv, st, smem, bad); break;
     default: break;
   }
   if (bad) atomicOr(status, bad);

@@ -493,10 +493,12 @@ int cov_element(tag_handle h, int mode, double* u, double* du, int stage, bool l
     st.t_member = h->d_mscal;
     st.dt = h->d_mscal + h->nmembers;
     st.max_speed = last ? h->d_mscal + 2 * h->nmembers : nullptr;
-    k_cov_element<kModeStage><<<h->cov_blocks, h->cov_threads, h->cov_smem, h->stream>>>(
+    auto kern = h->p_cov.volume == 0 ? k_cov_element<kModeStage, 0> : k_cov_element<kModeStage, 1>;
+    kern<<<h->cov_blocks, h->cov_threads, h->cov_smem, h->stream>>>(
         h->p_cov, h->d_groups, h->d_bases, u, du, h->d_k, h->d_pk, h->d_sfv, st, h->d_status);
   } else {
-    k_cov_element<kModeRhs><<<h->cov_blocks, h->cov_threads, h->cov_smem, h->stream>>>(
+    auto kern = h->p_cov.volume == 0 ? k_cov_element<kModeRhs, 0> : k_cov_element<kModeRhs, 1>;
+    kern<<<h->cov_blocks, h->cov_threads, h->cov_smem, h->stream>>>(
         h->p_cov, h->d_groups, h->d_bases, u, du, h->d_k, h->d_pk, h->d_sfv, st, h->d_status);
   }
   TAG_CUDA(cudaGetLastError());
@@ -511,9 +513,13 @@ int cov_max_speed(tag_handle h, const double* u) {
 }
 
 int cov_init(int max_smem) {
-  TAG_CUDA(cudaFuncSetAttribute(k_cov_element<kModeStage>,
+  TAG_CUDA(cudaFuncSetAttribute(k_cov_element<kModeStage, 0>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-  TAG_CUDA(cudaFuncSetAttribute(k_cov_element<kModeRhs>,
+  TAG_CUDA(cudaFuncSetAttribute(k_cov_element<kModeRhs, 0>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  TAG_CUDA(cudaFuncSetAttribute(k_cov_element<kModeStage, 1>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+  TAG_CUDA(cudaFuncSetAttribute(k_cov_element<kModeRhs, 1>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
   return TAG_OK;
 }
