@@ -227,3 +227,32 @@ def test_gpu_reproduces_mountain_wave_golden(tg, orc, gpu_lib, name):
     c.ssp_steps(uo, 0.0, MOUNTAIN_CFL, 10 ** 7, 1, t_end=360.0)
     assert np.abs(u[..., :4] - uo[..., :4]).max() <= 1e-10 * np.abs(uo[..., :4]).max()
     semi.close()
+
+
+def test_pt_time_dependent_dirichlet_states(tg, orc, gpu_lib):
+    """set_boundary_time(t) re-evaluates BoundaryConditionDirichlet's function
+    at the boundary nodes; the rhs then equals the oracle's with those states."""
+    from test_oracle_pt import mountain_case
+    eq, setup, mesh, basis, xy, invJ, arrays, bv, okw, solver = mountain_case(
+        tg, "linear_hydrostatic", (6, 4), 3)
+
+    def boundary_value(x, t, equations):
+        s = setup(x, t, equations)
+        s[..., 1] *= 1.0 + 0.01 * t  # a time-dependent inflow velocity
+        return s
+
+    bc = tg.BoundaryConditionDirichlet(boundary_value)
+    semi = tg.SemidiscretizationHyperbolic(
+        mesh, eq, setup, solver, source_terms=setup,
+        boundary_conditions={"x_neg": bc, "x_pos": bc, "y_neg": tg.boundary_condition_slip_wall,
+                             "y_pos": bc})
+    u = perturbed(semi.compute_coefficients(), 77)
+    c = orc.PotTemp2D(3, 0, 0, 0, 0, 0, 0, mesh=arrays, **okw)
+    for t in (0.0, 5.0):
+        semi.set_boundary_time(t)
+        bvt = bv.copy()
+        bvt[..., 1] *= 1.0 + 0.01 * t
+        c.set_mountain(setup.params(), bvt)
+        du, du_ref = semi.rhs(u, t), c.rhs(u, t)
+        assert np.abs(du - du_ref).max() <= 1e-12 * np.abs(du_ref).max(), t
+    semi.close()

@@ -286,8 +286,9 @@ class BoundaryConditionDirichlet:
     surface flux (plus half the nonconservative surface flux) of the inner
     state and boundary_value_function(x, t, equations) at the boundary node.
     The boundary states are evaluated on the host at the boundary nodes when
-    the semidiscretization is built (the function is taken as
-    time-independent, as MountainWaveSetup is) and uploaded to the device."""
+    the semidiscretization is built (at t = 0) and uploaded to the device;
+    SemidiscretizationHyperbolic.set_boundary_time(t) re-evaluates them for
+    time-dependent data."""
 
     def __init__(self, boundary_value_function):
         self.boundary_value_function = boundary_value_function

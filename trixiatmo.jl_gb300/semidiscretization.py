@@ -292,14 +292,22 @@ class _Handle:
         if isinstance(source_terms, MountainWaveSetup):
             mw = np.ascontiguousarray(source_terms.params(), dtype=np.float64)
             _lib.check(L.tag_set_source(h, _lib.TAG_SRC_MOUNTAIN_WAVE, _ptr(mw), 8))
+        self._dirichlet = None
         if np.any(bk == _lib.TAG_BC_DIRICHLET):
-            self.boundary_values = self._dirichlet_states(be, bf, bk, boundary_conditions)
-            _lib.check(L.tag_set_boundary_values(h, _ptr(self.boundary_values)))
+            self._dirichlet = (be, bf, bk, boundary_conditions)
+            self.set_boundary_time(0.0)
 
-    def _dirichlet_states(self, be, bf, bk, boundary_conditions):
+    def set_boundary_time(self, t):
+        """Evaluates the Dirichlet states at time t and uploads them (the states
+        stay fixed until the next call; a time-independent function needs none)."""
+        if self._dirichlet is None:
+            return
+        self.boundary_values = self._dirichlet_states(*self._dirichlet, t=t)
+        _lib.check(self.L.tag_set_boundary_values(self.h, _ptr(self.boundary_values)))
+
+    def _dirichlet_states(self, be, bf, bk, boundary_conditions, t=0.0):
         """[B, n, nv] states of BoundaryConditionDirichlet at the boundary face
-        nodes (Trixi evaluates boundary_value_function(x, t, equations) there;
-        the state is taken at t = 0)."""
+        nodes (Trixi evaluates boundary_value_function(x, t, equations) there)."""
         n, nv = self.n, self.equations.nvariables
         names = []
         for mesh_conn_names in self._bd_names:
@@ -313,7 +321,7 @@ class _Handle:
             j = {0: li, 1: li, 2: 0 * li, 3: 0 * li + n - 1}[int(f)]
             x = self.node_coordinates[e, j, i]
             fn = boundary_conditions[names[k]].boundary_value_function
-            out[k] = fn(x, 0.0, self.equations)
+            out[k] = fn(x, t, self.equations)
         return out
 
     def close(self):
@@ -397,6 +405,11 @@ class SemidiscretizationHyperbolic:
     def rhs_device(self, u_ptr: int, du_ptr: int, t=0.0):
         _lib.check(self._L.tag_rhs(self._h, ctypes.cast(u_ptr, _dp), ctypes.cast(du_ptr, _dp),
                                    float(t), 1))
+
+    def set_boundary_time(self, t):
+        """Re-evaluates BoundaryConditionDirichlet states at time t (for
+        time-dependent boundary data; call between steps)."""
+        self._H.set_boundary_time(float(t))
 
     def set_state(self, u):
         u = np.ascontiguousarray(u, dtype=np.float64)
