@@ -29,11 +29,12 @@ def per_var(a, b):
     return out
 
 
-def make_semi(tg, trees, layers, polydeg, coriolis=True):
+def make_semi(tg, trees, layers, polydeg, coriolis=True, topography=None, adapt=None):
     eq = tg.CompressibleEulerEnergyEquationsWithGravity3D(
         c_p=1004, c_v=717, gravity=tg.EARTH_GRAVITATIONAL_ACCELERATION)
     mesh = tg.P4estMeshCubedSphereTopography(trees, layers, tg.EARTH_RADIUS, 30000.0,
-                                             polydeg=polydeg)
+                                             polydeg=polydeg, initial_topography=topography,
+                                             adapt_vertical_grid=adapt)
     solver = tg.DGSEM(polydeg, (tg.FluxLMARS(340.0), tg.flux_zero),
                       tg.VolumeIntegralFluxDifferencing(
                           (tg.flux_ranocha, tg.flux_nonconservative_waruszewski_etal)))
@@ -113,4 +114,27 @@ def test_gpu_reproduces_reference_golden_3d(tg, orc, gpu_lib):
     # and with the error norms computed on the device (tag_analyze_errors)
     l2d, linfd = semi.calc_error_norms(0.0)
     check_golden(l2d, linfd)
+    semi.close()
+
+
+@pytest.mark.parametrize("vertical", ["galchen", "sleve"])
+def test_rhs3d_with_topography_matches_oracle(tg, orc, gpu_lib, vertical):
+    """A shell whose ground carries a 2 km Gaussian mountain (GalChen or
+    Sleve(0.7, 0.8) vertical coordinates): curved, non-radial element faces
+    and slip walls on the terrain."""
+    from trixiatmo_gb300.meshes3d import GalChen, Sleve
+
+    def mountain(lat, lon):
+        return 2000.0 * np.exp(-((lat - 0.4) ** 2 + (lon - 0.3) ** 2) / 0.05)
+
+    adapt = GalChen() if vertical == "galchen" else Sleve(0.7, 0.8)
+    eq, mesh, semi = make_semi(tg, 3, 2, 4, topography=mountain, adapt=adapt)
+    u = perturb3d(semi.compute_coefficients(), eq, seed=321)
+    du = semi.rhs(u)
+    o = oracle_3d(orc, tg, 4, semi.contravariant_vectors, semi.inverse_jacobian,
+                  semi.node_coordinates, mesh.connectivity(solver_basis(semi)))
+    du_ref = o.rhs(u)
+    assert max_norm_rel(du, du_ref) <= RTOL, max_norm_rel(du, du_ref)
+    assert per_var(du, du_ref) <= RTOL_VAR, per_var(du, du_ref)
+    assert semi.status() == 0
     semi.close()

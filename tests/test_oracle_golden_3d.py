@@ -108,3 +108,54 @@ def perturb3d(u, eq, seed, amplitude=1e-2, velocity=5.0):
                         v1 + velocity * rng.uniform(-1, 1, s), v2 + velocity * rng.uniform(-1, 1, s),
                         v3 + velocity * rng.uniform(-1, 1, s),
                         p * (1 + amplitude * rng.uniform(-1, 1, s)), phi)
+
+
+@pytest.mark.parametrize("vertical", ["galchen", "sleve"])
+def test_shell_mesh_with_topography(tg, vertical):
+    """P4estMeshCubedSphereTopography with an initial topography
+    (src/meshes/p4est_cubed_sphere_topography.jl:596-620) and GalChen or
+    Sleve(0.7, 0.8) vertical coordinates: the ground follows the topography,
+    the top stays at inner_radius + thickness, interfaces still match node
+    for node and the curl-form metric terms keep the discrete metric
+    identities; zero topography gives the perfect sphere's nodes exactly."""
+    from trixiatmo_gb300.meshes3d import GalChen, Sleve
+    a, H = 6.371e6, 30000.0
+
+    def mountain(lat, lon):
+        return 2000.0 * np.exp(-((lat - 0.4) ** 2 + (lon - 0.3) ** 2) / 0.05)
+
+    adapt = GalChen() if vertical == "galchen" else Sleve(0.7, 0.8)
+    basis = tg.LobattoLegendreBasis(3)
+    flat = tg.P4estMeshCubedSphereTopography(3, 2, a, H, polydeg=3)
+    zero = tg.P4estMeshCubedSphereTopography(3, 2, a, H, polydeg=3,
+                                             initial_topography=lambda lat, lon: 0.0 * lat,
+                                             adapt_vertical_grid=adapt)
+    x0, x1 = flat.geometry(basis)[0], zero.geometry(basis)[0]
+    if vertical == "galchen":
+        assert np.array_equal(x0, x1)
+    else:  # eta H = (z_ref / H) H: the last bit of z_ref
+        assert np.abs(x0 - x1).max() <= 1e-8
+    mesh = tg.P4estMeshCubedSphereTopography(3, 2, a, H, polydeg=3, initial_topography=mountain,
+                                             adapt_vertical_grid=adapt)
+    xyz, Ja, invJ = mesh.geometry(basis)
+    r = np.sqrt((xyz ** 2).sum(-1))
+    top = r[:, -1][np.arange(mesh.nelements) % 2 == 1]   # layer 1, k = n - 1
+    assert np.allclose(top, a + H, rtol=0, atol=1e-7)
+    ground = r[:, 0][np.arange(mesh.nelements) % 2 == 0]  # layer 0, k = 0
+    assert ground.max() - a > 1500.0 and ground.min() >= a - 1e-7
+    # the reference's latitude: asin of the unit vector's z divided by the cube
+    # point's radius 1 / max|unit_i|
+    p = xyz[:, 0][np.arange(mesh.nelements) % 2 == 0]
+    unit = p / np.sqrt((p ** 2).sum(-1))[..., None]
+    lat_ref = np.arcsin(unit[..., 2] * np.abs(unit).max(-1))
+    lon = np.arctan2(unit[..., 1], unit[..., 0])
+    assert np.allclose(ground, a + mountain(lat_ref, lon), rtol=0, atol=1e-6)
+    assert np.all(invJ > 0)
+    conn = mesh.connectivity(basis)
+    ie, ifc, io, be, bf = conn.arrays()
+    assert len(be) == 2 * 6 * 9 and len(io) == (6 * mesh.nelements - len(be)) // 2
+    D = basis.derivative_matrix
+    div = (np.einsum("ia,ekja...->ekji...", D, Ja[..., 0, :]) +
+           np.einsum("ja,ekai...->ekji...", D, Ja[..., 1, :]) +
+           np.einsum("ka,eaji...->ekji...", D, Ja[..., 2, :]))
+    assert np.abs(div).max() <= 1e-13 * np.abs(Ja).max()

@@ -44,7 +44,7 @@ from .meshes import (P4estMesh, SchaerMountain, SchärMountain, StructuredMesh, 
                      terrain_following_faces)
 from .equations import BoundaryConditionDirichlet
 from .initial_conditions import MountainWaveSetup
-from .meshes3d import P4estMeshCubedSphereTopography
+from .meshes3d import GalChen, P4estMeshCubedSphereTopography, Sleve
 from .semidiscretization import (DGSEM, SemidiscretizationCovariant,
                                  SemidiscretizationCovariantEnsemble, SemidiscretizationEnsemble,
                                  SemidiscretizationHyperbolic, fp64_peak, source_terms_coriolis)
@@ -71,7 +71,7 @@ __all__ = [
     "initial_condition_nonhydrostatic_gravity_wave", "AtmosphereLayers",
     "initial_condition_moist_bubble", "flux_LMARS", "source_terms_no_phase_change",
     "SchaerMountain", "SchärMountain", "WitchOfAgnesi", "terrain_following_faces",
-    "BoundaryConditionDirichlet", "MountainWaveSetup",
+    "BoundaryConditionDirichlet", "MountainWaveSetup", "GalChen", "Sleve",
     "CompressibleEulerPotentialTemperatureEquationsWithGravity2D",
     "CompressibleEulerPotentialTemperatureEquationsWithGravity3D",
     "CompressibleEulerInternalEnergyEquationsWithGravity2D", "flux_conservative_etec",

@@ -1,9 +1,10 @@
 """Host-side 3D hexahedral meshes: the cubed-sphere shell.
 
 `P4estMeshCubedSphereTopography` mirrors TrixiAtmo's constructor of the same
-name (src/meshes/p4est_cubed_sphere_topography.jl:114-167) for a perfect
-sphere (zero topography, so every vertical coordinate transform reduces to
-z = z_reference): 6 faces x trees_per_face^2 x layers hexahedra, the
+name (src/meshes/p4est_cubed_sphere_topography.jl:114-167), by default for a
+perfect sphere, optionally with an initial topography spread over the column
+by GalChen or Sleve vertical coordinates: 6 faces x trees_per_face^2 x layers
+hexahedra, the
 equiangular cubed-sphere map of :596-620, boundaries `inside` (zeta-) and
 `outside` (zeta+).  Elements are numbered column first (layer fastest), then
 cell x, cell y, cube face; the reference orders the cells of a face along a
@@ -31,9 +32,40 @@ import numpy as np
 from .basis import LobattoLegendreBasis
 
 
-def cubed_sphere_mapping(xi, eta, zeta, inner_radius, thickness, direction):
+class GalChen:
+    """Gal-Chen & Somerville's terrain-following coordinate
+    (src/meshes/p4est_cubed_sphere_topography.jl:54-79): the topography's
+    influence decays linearly from the ground to the top H,
+    z = z_ref + (H - z_ref) z_s / H."""
+
+    def __call__(self, z_reference, z_topography, H):
+        return z_reference + (H - z_reference) * z_topography / H
+
+
+class Sleve:
+    """SLEVE coordinate of Schaer et al. (2002) (p4est_cubed_sphere_topography.jl:7-52):
+    with eta = z_ref / H, z = eta H + z_s sinh((eta_H - eta) / s / eta_H) / sinh(1 / s)
+    for eta <= eta_H and z = eta H above."""
+
+    def __init__(self, eta_H, s):
+        self.eta_H, self.s = float(eta_H), float(s)
+
+    def __call__(self, z_reference, z_topography, H):
+        eta = z_reference / H
+        low = eta <= self.eta_H
+        decay = np.sinh((self.eta_H - eta) / self.s / self.eta_H) / np.sinh(1.0 / self.s)
+        return np.where(low, eta * H + z_topography * decay, eta * H)
+
+
+def cubed_sphere_mapping(xi, eta, zeta, inner_radius, thickness, direction, topography=None,
+                         adapt_vertical_grid=None):
     """Equiangular cubed-sphere shell map of one cube face (1-based direction
-    1..6 as in the reference: -z, +x, +y, -x, -y, +z)."""
+    1..6 as in the reference: -z, +x, +y, -x, -y, +z).  With a topography
+    (a function of latitude and longitude, p4est_cubed_sphere_topography.jl:596-620)
+    the reference height z_ref = thickness (zeta + 1) / 2 is moved by
+    adapt_vertical_grid (GalChen or Sleve); the latitude is taken as the
+    reference takes it, asin of the unit vector's z component divided once
+    more by r."""
     alpha = xi * np.pi / 4
     beta = eta * np.pi / 4
     x = np.tan(alpha)
@@ -49,6 +81,11 @@ def cubed_sphere_mapping(xi, eta, zeta, inner_radius, thickness, direction):
     }[direction]
     r = np.sqrt(1 + x * x + y * y)
     z = thickness * 0.5 * (zeta + 1)
+    if topography is not None:
+        ux, uy, uz = cube[0] / r, cube[1] / r, cube[2] / r
+        lat = np.arcsin(uz / r)
+        lon = np.arctan2(uy, ux)
+        z = (adapt_vertical_grid or GalChen())(z, topography(lat, lon), thickness)
     s = (inner_radius + z) / r
     return s * cube[0], s * cube[1], s * cube[2]
 
@@ -173,12 +210,17 @@ def match_faces(xyz, n, boundary_face_names):
 
 
 class P4estMeshCubedSphereTopography:
-    """Cubed-sphere shell of 6 * trees_per_face_dimension^2 * layers hexahedra
-    (zero topography)."""
+    """Cubed-sphere shell of 6 * trees_per_face_dimension^2 * layers hexahedra;
+    initial_topography(lat, lon) (default: none, a perfect sphere) raises the
+    ground, adapt_vertical_grid (GalChen() by default, or Sleve(eta_H, s))
+    spreads it over the column."""
 
     ndims = 3
 
-    def __init__(self, trees_per_face_dimension, layers, inner_radius, thickness, *, polydeg):
+    def __init__(self, trees_per_face_dimension, layers, inner_radius, thickness, *, polydeg,
+                 initial_topography=None, adapt_vertical_grid=None):
+        self.initial_topography = initial_topography
+        self.adapt_vertical_grid = adapt_vertical_grid or GalChen()
         self.nc = int(trees_per_face_dimension)
         self.nz = int(layers)
         self.inner_radius = float(inner_radius)
@@ -207,7 +249,8 @@ class P4estMeshCubedSphereTopography:
             (dz / 2 * nodes)[None, None, None, :, None, None]
         XI, ETA, ZETA = np.broadcast_arrays(XI, ETA, ZETA)  # [cy, cx, cz, k, j, i]
         for d in range(6):
-            X, Y, Z = cubed_sphere_mapping(XI, ETA, ZETA, self.inner_radius, self.thickness, d + 1)
+            X, Y, Z = cubed_sphere_mapping(XI, ETA, ZETA, self.inner_radius, self.thickness, d + 1,
+                                           self.initial_topography, self.adapt_vertical_grid)
             out[d, ..., 0], out[d, ..., 1], out[d, ..., 2] = X, Y, Z
         # element e = cz + nz * (cx + nc * (cy + nc * dir))
         out = out.transpose(0, 1, 2, 3, 4, 5, 6, 7).reshape(6, nc, nc, nz, n, n, n, 3)
