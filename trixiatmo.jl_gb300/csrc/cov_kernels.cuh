@@ -156,11 +156,11 @@ TAG_DEV void cov_transform(const double* u, const CovSide& from, const CovSide& 
 }
 
 // surface flux (+ 0.5 nonconservative) along o of left state a and right
-// state c, both sides' geometry `w` (the reference passes aux_vars_ll twice)
-TAG_DEV void cov_surface(const CovParams& P, const double* a, const double* c, const CovSide& w,
-                         int o, double* F) {
+// state c, both sides' geometry `w` (the reference passes aux_vars_ll twice);
+// iha = 1 / a[0], ihc = 1 / c[0]
+TAG_DEV void cov_surface(const CovParams& P, const double* a, const double* c, double iha,
+                         double ihc, const CovSide& w, int o, double* F) {
   const double J = w.J;
-  const double iha = 1.0 / a[0], ihc = 1.0 / c[0];
   const double gco0 = o ? w.gc12 : w.gc11;  // G^{1o}
   const double gco1 = o ? w.gc22 : w.gc12;  // G^{2o}
   const double ao = o ? a[2] : a[1], co = o ? c[2] : c[1];
@@ -206,16 +206,18 @@ TAG_DEV void cov_surface(const CovParams& P, const double* a, const double* c, c
 }
 
 // outward flux of one side (face f of its element)
+// ih_mine = 1 / mine[0], ih_other = 1 / other_in_mine[0] (the transformation
+// keeps h), each computed once per interface node
 TAG_DEV void cov_side_flux(const CovParams& P, const double* mine, const double* other_in_mine,
-                           const CovSide& w, int f, double* F) {
+                           double ih_mine, double ih_other, const CovSide& w, int f, double* F) {
   const int o = f >> 1;
   if ((f & 1) == 0) {
-    cov_surface(P, other_in_mine, mine, w, o, F);
+    cov_surface(P, other_in_mine, mine, ih_other, ih_mine, w, o, F);
     F[0] = -F[0];
     F[1] = -F[1];
     F[2] = -F[2];
   } else {
-    cov_surface(P, mine, other_in_mine, w, o, F);
+    cov_surface(P, mine, other_in_mine, ih_mine, ih_other, w, o, F);
   }
 }
 
@@ -247,8 +249,9 @@ TAG_DEV void cov_interface_body(const CovParams& P, const CovGroup& G, int lblk,
   double rt[3], lt[3], Fp[3], Fs[3];
   cov_transform(ur, ar, al, rt);
   cov_transform(ul, al, ar, lt);
-  cov_side_flux(P, ul, rt, al, f0, Fp);
-  cov_side_flux(P, ur, lt, ar, f1, Fs);
+  const double ihl = 1.0 / ul[0], ihr = 1.0 / ur[0];
+  cov_side_flux(P, ul, rt, ihl, ihr, al, f0, Fp);
+  cov_side_flux(P, ur, lt, ihr, ihl, ar, f1, Fs);
   double* s0 = sfv + G.sf0 + ((long)(e0 - G.e0) * 4 + f0) * n * 3 + l * 3;
   double* s1 = sfv + G.sf0 + ((long)(e1 - G.e0) * 4 + f1) * n * 3 + l1 * 3;
 #pragma unroll
