@@ -88,8 +88,9 @@ struct PhysEnergy2D {
   TAG_DEV static void lmars(const Params& P, const double* ul, const double* ur, double n1,
                             double n2, double* F) {
     const double rho_ll = ul[0], rho_rr = ur[0];
-    const double v1_ll = ul[1] / rho_ll, v2_ll = ul[2] / rho_ll;
-    const double v1_rr = ur[1] / rho_rr, v2_rr = ur[2] / rho_rr;
+    const double irl = 1.0 / rho_ll, irr = 1.0 / rho_rr;  // one reciprocal per state
+    const double v1_ll = ul[1] * irl, v2_ll = ul[2] * irl;
+    const double v1_rr = ur[1] * irr, v2_rr = ur[2] * irr;
     const double p_ll = P.gm1 * (ul[3] - 0.5 * (ul[1] * v1_ll + ul[2] * v2_ll));
     const double p_rr = P.gm1 * (ur[3] - 0.5 * (ur[1] * v1_rr + ur[2] * v2_rr));
     const double v_ll = v1_ll * n1 + v2_ll * n2;
