@@ -302,7 +302,7 @@ def run_swe(args):
              for k, N, _, _ in specs)
     peak_fp64 = tg.fp64_peak()
     achieved_tf = fl / (ms_el * 1e-3) / 1e12
-    traffic = TRAFFIC_PER_DOF.get("swe") if args.swe_variant == "weak" else None
+    traffic = TRAFFIC_PER_DOF.get("swe" if args.swe_variant == "weak" else "swe_ec")
     cpu = None
     if not args.no_cpu:
         orc = entry.load_oracle()
@@ -735,7 +735,8 @@ def run_ours(args):
 # used to report `traffic` for the full-size launch.
 TRAFFIC_PER_DOF = {"shell": 282.45,      # k_element3d, stage mode, full shell
                    "ensemble": 205.27,    # k_element 2D, stage mode, 128-member ensemble
-                   "swe": 214.71}         # k_cov_element weak form, 8 of the SWE members
+                   "swe": 214.71,         # k_cov_element weak form, 8 of the SWE members
+                   "swe_ec": 215.20}      # k_cov_element split EC form, the same 8 members
 
 
 def main():
