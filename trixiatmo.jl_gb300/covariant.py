@@ -493,14 +493,16 @@ def initial_condition_rossby_haurwitz(x, t, equations):
     products of those alone are rounded to single precision before they meet
     double-precision values; the same promotion is kept here."""
     lon, lat, a = _lonlat(x)
-    f32 = np.float32
+    f32, f64 = np.float32, np.float64
     h0, omega, K, R = f32(8.0e3), f32(7.848e-6), f32(7.848e-6), f32(4.0)
     cl = np.cos(lat)
-    Om = EARTH_ROTATION_RATE
-    A = (f32(0.5) * omega * (2 * Om + omega) * cl ** 2 +
+    # EARTH_ROTATION_RATE is a double, so every sum with it is a double; NumPy
+    # would round a Python float plus a float32 scalar to float32.
+    Om = f64(EARTH_ROTATION_RATE)
+    A = (f32(0.5) * omega * (2 * Om + f64(omega)) * cl ** 2 +
          f32(0.25) * K ** 2 * cl ** (2 * R) * ((R + 1) * cl ** 2 + (2 * R ** 2 - R - 2) -
                                                2 * R ** 2 / cl ** 2))
-    B = (2 * (Om + omega) * K / ((R + 1) * (R + 2)) * cl ** R *
+    B = (2 * (Om + f64(omega)) * f64(K) / ((R + 1) * (R + 2)) * cl ** R *
          ((R ** 2 + 2 * R + 2) - (R + 1) ** 2 * cl ** 2))
     C = f32(0.25) * K ** 2 * cl ** (2 * R) * ((R + 1) * cl ** 2 - (R + 2))
     h = h0 + (1 / EARTH_GRAVITATIONAL_ACCELERATION) * (

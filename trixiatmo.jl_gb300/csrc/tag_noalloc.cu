@@ -12,8 +12,15 @@
 // on one device share it, so two calls whose kernels overlap in time on the
 // same GPU (different streams, different host threads) race on it and give
 // wrong results; callers must order such calls.
+//
+// The array's device address is looked up once per device and kept.  It
+// belongs to the device's primary context (the one the CUDA runtime, PyTorch
+// and Julia's CUDA.jl use): calls made under another context of the same
+// device, or after cudaDeviceReset destroyed the primary context, would use a
+// stale address and are not supported.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <mutex>
 #include <string>
 
@@ -40,6 +47,54 @@ unsigned* g_status_dev[kMaxDevices] = {};
 int nfail(int code, const std::string& msg) {
   tag::set_last_error(msg);  // reported by tag_last_error()
   return code;
+}
+
+// Boundary kinds this entry point evaluates: the slip walls need nothing but
+// the inner state; a Dirichlet face would need the per-face boundary states
+// that only a tag_create handle owns (tag_set_boundary_values).
+bool supported_boundary_kind(int32_t k) {
+  return k == TAG_BC_SLIP_WALL_STRUCTURED || k == TAG_BC_SLIP_WALL_NORMAL;
+}
+
+// Reads the caller's boundary_kinds (device memory) in fixed-size pieces into
+// a stack buffer, ordered on `s` after the caller's own work, and rejects any
+// kind the kernels cannot evaluate without more data.
+int check_boundary_kinds(const int32_t* kinds, int nbd, cudaStream_t s) {
+  constexpr int kChunk = 1024;
+  int32_t buf[kChunk];
+  for (int off = 0; off < nbd; off += kChunk) {
+    const int m = nbd - off < kChunk ? nbd - off : kChunk;
+    cudaError_t e = cudaMemcpyAsync(buf, kinds + off, sizeof(int32_t) * m, cudaMemcpyDefault, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess)
+      return nfail(TAG_E_CUDA, std::string("reading boundary_kinds: ") + cudaGetErrorString(e));
+    for (int k = 0; k < m; ++k)
+      if (!supported_boundary_kind(buf[k]))
+        return nfail(TAG_E_INVALID,
+                     "tag_rhs_noalloc evaluates slip walls only (TAG_BC_SLIP_WALL_STRUCTURED, "
+                     "TAG_BC_SLIP_WALL_NORMAL); boundary face " + std::to_string(off + k) +
+                         " has kind " + std::to_string(buf[k]));
+  }
+  return TAG_OK;
+}
+
+// Widest launch the element kernel allows (its register use bounds the
+// threads per block); the kernel strides over its block, so a narrower
+// block computes the same result.
+template <int n>
+int element_thread_cap(int& cap) {
+  static int c = 0;
+  static std::once_flag once;
+  static cudaError_t err = cudaSuccess;
+  std::call_once(once, [] {
+    cudaFuncAttributes a;
+    err = cudaFuncGetAttributes(&a, k_element<PhysEnergy2D, n, kModeRhs>);
+    if (err == cudaSuccess) c = (a.maxThreadsPerBlock / 32) * 32;
+  });
+  if (err != cudaSuccess)
+    return nfail(TAG_E_CUDA, std::string("cudaFuncGetAttributes: ") + cudaGetErrorString(err));
+  cap = c;
+  return TAG_OK;
 }
 
 int setup_device(int dev, double** sfv, unsigned** status) {
@@ -77,9 +132,12 @@ int launch_noalloc(const tag_config* cfg, const PhysEnergy2D::Params& P, const B
   }
   // elements per CTA: the largest count whose shared memory fits the default
   // 48 KB window (no attribute change needed)
+  int cap = 0;
+  int rc = element_thread_cap<n>(cap);
+  if (rc) return rc;
   int epb = 1;
   while (epb < 16 && S::bytes(epb + 1) <= 48 * 1024 && (epb + 1) * S::TPE <= 1024) ++epb;
-  const int threads = epb * S::TPE;
+  const int threads = std::min(cap, epb * S::TPE);
   StageArgs st{};
   k_element<Phys, n, kModeRhs><<<(nelem + epb - 1) / epb, threads, S::bytes(epb), s>>>(
       P, basis, const_cast<double*>(u), du, nullptr, cfg->contravariant_vectors,
@@ -126,7 +184,12 @@ int tag_rhs_noalloc(const tag_config* cfg, const double* u, double* du, void* st
   int rc = setup_device(dev, &sfv, &status);
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  // the shared scratch keeps the previous call's contents: clear it
+  if (cfg->nboundaries > 0 && (rc = check_boundary_kinds(cfg->boundary_kinds, cfg->nboundaries, s)))
+    return rc;
+  // the shared scratch keeps the previous call's contents: clear it (a well-
+  // formed mesh lists every face as an interface side or a boundary face and
+  // overwrites all of it; a face listed nowhere then reads zero flux rather
+  // than another call's data; at most 8 MiB of writes, about 1 us)
   e = cudaMemsetAsync(sfv, 0, need * sizeof(double), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(status, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return nfail(TAG_E_CUDA, cudaGetErrorString(e));

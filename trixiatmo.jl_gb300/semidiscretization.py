@@ -447,6 +447,52 @@ class SemidiscretizationHyperbolic:
                                         _ptr(tt)))
         return float(tt[0]) if self.nmembers == 1 and np.ndim(t) == 0 else tt
 
+    def solve(self, tspan, cfl=1.0, method="CarpenterKennedy2N54", save_dt=None, fixed_dt=0.0):
+        """Integrates the resident state over tspan = (t0, t_end), as the
+        reference's `solve(ode, alg; adaptive = false, callback =
+        CallbackSet(StepsizeCallback(cfl), SaveSolutionCallback(dt = save_dt)))`
+        does: every step takes dt = cfl * max_dt of the state it starts from (or
+        fixed_dt), and a step that would pass the next stop is shortened to land
+        on it, the time then set to the stop itself.  The stops are t_end and,
+        with save_dt, t0 + k * save_dt: Trixi's SaveSolutionCallback(dt = ...)
+        is a PeriodicCallback that adds those tstops, and the shortened steps
+        change the solution (the covariant elixirs save every tspan / 10).
+        Whole runs of steps that end before a stop are one `tag_rk_steps` call
+        (graph replays); only the step that meets a stop is decided on the host.
+        Returns t_end."""
+        if self.nmembers != 1:
+            raise ValueError("solve integrates a single mesh; step ensembles with rk_steps")
+        t0, t_end = float(tspan[0]), float(tspan[1])
+        stops = []
+        if save_dt:
+            k = 1
+            while t0 + k * save_dt < t_end:
+                stops.append(t0 + k * save_dt)
+                k += 1
+        stops.append(t_end)
+        t = t0
+        for stop in stops:
+            while t < stop:
+                dt = fixed_dt if fixed_dt > 0 else cfl * self.max_dt()
+                if not dt > 0:
+                    raise RuntimeError(f"non-positive time step {dt!r} at t = {t!r}")
+                # whole steps that certainly end before the stop (dt may drift
+                # by a few percent over them), in one call
+                n_safe = int(0.9 * (stop - t) / dt) - 1
+                if n_safe > 0:
+                    t = self.rk_steps(n_safe, cfl=cfl, t=t, fixed_dt=fixed_dt, method=method)
+                    if t > stop:
+                        raise RuntimeError(f"time step grew past the stop {stop!r} (t = {t!r})")
+                    continue
+                # OrdinaryDiffEq: dt = min(dt, tstop - t); a time within 100 ulp
+                # of the stop is the stop
+                if t + dt >= stop - 100 * np.spacing(stop):
+                    self.rk_steps(1, t=t, fixed_dt=stop - t, method=method)
+                    t = stop
+                else:
+                    t = self.rk_steps(1, cfl=cfl, t=t, fixed_dt=fixed_dt, method=method)
+        return t
+
     # ---- analysis (AnalysisCallback), on the resident state ---------------------
     def integrate(self, func="cons2cons", normalize=True):
         """Trixi's `integrate(func, u_ode, semi; normalize)` of the resident state,
