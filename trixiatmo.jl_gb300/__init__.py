@@ -7,7 +7,7 @@ The directory name is not a Python identifier; load it with
 ``load_package()`` from ``__graft_entry__`` (or importlib) under the name
 ``trixiatmo_gb300``.
 """
-from . import _lib, covariant, learned_guess
+from . import _lib, covariant, learned_guess, trixi_connectivity
 from .basis import LobattoLegendreBasis
 from .equations import (CompressibleEulerEnergyEquationsWithGravity2D,
                         CompressibleEulerEnergyEquationsWithGravity3D,
@@ -78,4 +78,5 @@ __all__ = [
     "flux_nonconservative_etec", "flux_conservative_es", "flux_nonconservative_es",
     "flux_ec", "flux_tec",
     "flux_etec", "flux_nonconservative_artiano_etal", "flux_nonconservative_souza_etal",
+    "trixi_connectivity",
 ]
