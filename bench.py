@@ -117,12 +117,13 @@ def rainy_newton_section(tg, train_states=1_000_000, epochs=40):
     t0 = time.perf_counter()
     params, gen, losses = lg.train_guess(n=train_states, epochs=epochs, seed=11, batch=2048)
     t_train = time.perf_counter() - t0
+    in_run = rainy_stage_section(tg, params)
     eq, semi = make_rainy(tg)
     u0 = semi.compute_coefficients()
     semi.set_mlp(params)
     semi.set_newton(mode=1, tol=1e-12, max_iterations=30, polish=1)
     res = {}
-    for name, learned in (("plain", False), ("learned", True)):
+    for name, learned in (("plain", 0), ("closed_form", 2), ("learned", 1)):
         best = 1e30
         for _ in range(3):
             semi.set_state(u0)
@@ -138,7 +139,9 @@ def rainy_newton_section(tg, train_states=1_000_000, epochs=40):
         "workload": "rainy moist bubble 128x64 elements, polydeg 3, 131072 nodes; "
                     "tolerance 1e-12 relative; canonical finish (snap + 1 update) on both",
         "iters_per_node_plain": ip, "iters_per_node_learned": il, "reduction": ip / il,
+        "iters_per_node_closed_form": float(res["closed_form"][1].mean()),
         "iters_saturated_nodes": {"plain": float(res["plain"][1][sat].mean()),
+                                  "closed_form": float(res["closed_form"][1][sat].mean()),
                                   "learned": float(res["learned"][1][sat].mean()),
                                   "fraction": float(sat.mean())},
         "bitwise_equal_fraction": float(same.mean()),
@@ -148,8 +151,62 @@ def rainy_newton_section(tg, train_states=1_000_000, epochs=40):
         "training": {"states": train_states, "epochs": epochs,
                      "seconds_incl_generation": t_train, "loss_first": float(losses[0]),
                      "loss_last": float(losses[-1])},
+        "in_run": in_run,
     }
     semi.close()
+    return out
+
+
+def rainy_stage_section(tg, params, steps=20):
+    """The learned guess where the reference uses the solve: config 2 (the
+    128 x 64, polydeg 3 moist bubble) run for `steps` CK2N54 steps at CFL 1
+    with the Newton stage limiter after every stage
+    (src/callbacks_stage/nonlinear_solve_dg2d.jl:6-44, as
+    examples/euler/moist_air/buoyancy/elixir_hoeck_bubble.jl:87-94 passes it),
+    at tolerance 1e-12 relative with the canonical finish, from three starts:
+    the warm start of the reference (slots 7-9 of the previous stage), the
+    closed-form unsaturated branch alone (warm start on saturated nodes), and
+    closed form + MLP.  Newton updates per node solve over the run, the run's
+    DOF·stage/s (CUDA events on the library's stream), and whether the three
+    runs end in the same bits."""
+    import torch
+    lg = tg.learned_guess
+    out, finals = {}, {}
+    for name, start in (("warm", 0), ("closed_form", 2), ("learned", 1)):
+        eq, semi = make_rainy(tg)
+        semi.set_mlp(params)
+        semi.set_newton(mode=1, tol=1e-12, max_iterations=30, polish=1)
+        semi.set_newton_start(start)
+        semi.set_state(semi.compute_coefficients())
+        t = semi.rk_steps(1, cfl=1.0, t=0.0)  # warm-up: graph capture
+        semi.newton_counters(reset=True)
+        stream = torch.cuda.ExternalStream(semi.stream())
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        t = semi.rk_steps(steps, cfl=1.0, t=t)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        sec = ev0.elapsed_time(ev1) * 1e-3
+        c = semi.newton_counters(reset=True)
+        finals[name] = semi.get_state()
+        sat = lg.saturated(finals[name].reshape(-1, 9))
+        out[name] = {"updates_per_node_solve": c["updates"] / c["node_solves"],
+                     "fallbacks": c["fallbacks"], "not_converged": c["not_converged"],
+                     "node_solves": c["node_solves"],
+                     "dof_stage_per_s": semi.ndofs * 5 * steps / sec,
+                     "saturated_fraction_final": float(sat.mean())}
+        semi.close()
+    w, f, l = (out[k]["updates_per_node_solve"] for k in ("warm", "closed_form", "learned"))
+    out["reduction_vs_warm"] = w / l if l > 0 else None
+    out["reduction_vs_closed_form"] = f / l if l > 0 else None
+    same = [np.all(finals["warm"].reshape(-1, 9) == finals[k].reshape(-1, 9), axis=1).mean()
+            for k in ("closed_form", "learned")]
+    out["bitwise_equal_final_fraction"] = {"closed_form": float(same[0]), "learned": float(same[1])}
+    out["workload"] = (f"rainy moist bubble 128x64, polydeg 3, {steps} CK2N54 steps at CFL 1, "
+                       "Newton limiter after every stage, tolerance 1e-12 relative, canonical "
+                       "finish")
     return out
 
 
@@ -298,9 +355,9 @@ def run_swe(args):
     except (OSError, KeyError, ValueError):
         hbm_peak, hbm_src = 6800.0, "fallback"
     gbs = by / (ms_el * 1e-3) / 1e9
-    fl = sum(6 * k * k * flops_per_node_covariant(N + 1, args.swe_variant) * (N + 1) ** 2
+    fl = sum(6 * k * k * (N + 1) ** 2 * ALGORITHMIC_OPS[f"swe_{args.swe_variant}_{N}"]["element"]
              for k, N, _, _ in specs)
-    peak_fp64 = tg.fp64_peak()
+    peak_fp64, peak_src, probe_fp64 = fp64_roofline_peak(tg, clock_info)
     achieved_tf = fl / (ms_el * 1e-3) / 1e12
     traffic = TRAFFIC_PER_DOF.get("swe" if args.swe_variant == "weak" else "swe_ec")
     cpu = None
@@ -349,11 +406,13 @@ def run_swe(args):
                      "traffic_source": "ncu dram__bytes_read+write per DOF of a capture, "
                                        "scaled by DOF" if traffic else None,
                      "kernel": "k_cov_element (volume + surface + Jacobian + sources + RK stage)",
-                     "peak_source": "FP64 FMA probe in this run (tag_fp64_peak), of measured",
+                     "peak_source": peak_src, "fma_stream_tflops": probe_fp64 / 1e12,
+                     "frac_of_fma_stream": achieved_tf / (probe_fp64 / 1e12),
                      "hbm_achieved_gbs": gbs, "hbm_peak_gbs": hbm_peak,
                      "hbm_frac": gbs / hbm_peak, "hbm_peak_source": hbm_src,
                      "ms_element": ms_el, "ms_interface": ms_if,
-                     "flops_per_launch": fl, "bytes_per_launch": by},
+                     "flops_per_launch": fl, "flops_source": FLOPS_SOURCE,
+                     "bytes_per_launch": by},
         "ensemble_vs_sequential": {"sequential_rate": seq_value, "speedup": value / seq_value},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                        "steps": len(lat)},
@@ -369,33 +428,34 @@ def run_swe(args):
     ens.close()
 
 
-def flops_per_node_covariant(n, variant):
-    """FP64 flops per node of one covariant element-kernel launch, counted from
-    the reference formulas (covariant_shallow_water.jl, _split.jl) with a
-    division as one flop.  Weak form: both contravariant fluxes 23, the D_hat
-    contraction 12 n, the surface terms 24 / n, Jacobian and source sum 6, the
-    geometric + Coriolis source 49, the stage update 15.  Split EC form, as
-    the kernel evaluates it (the pair fluxes regrouped into contractions of
-    node quantities): per direction 13 per symmetric partner (n - 1), 7 per
-    nonconservative partner (n), 47 to combine the sums; 2 to add the
-    nonconservative part, per-node velocities 13, surface 24 / n, Jacobian
-    10, the split source 67, the stage update 15."""
-    if variant == "weak":
-        return 93 + 12 * n + 24.0 / n
-    return 2 * (13 * (n - 1) + 7 * n + 47) + 2 + 13 + 10 + 67 + 15 + 24.0 / n
-
-
-def flops_per_element_launch_3d(n, nelem):
-    """FP64 flops of one 3D element-kernel launch, counted from the reference
-    formulas: per symmetric pair 120 (flux_ranocha 3D with its two logarithmic
-    means in the 4-term form, half the Waruszewski term, both D_split
-    products), per node 11 (cons2prim), per (node, active variable)
-    3(n-1) direction sums + Jacobian + Coriolis + 5 for the stage update, plus
-    2 per face-node surface term."""
-    pairs = 3 * n * n * n * (n - 1) // 2
-    nodes = n ** 3
-    per_elem = pairs * 120 + nodes * 11 + nodes * 5 * (3 * (n - 1) + 1 + 1 + 5) + 6 * n * n * 5 * 2
-    return per_elem * nelem
+# ---- algorithmic work per DOF·stage ------------------------------------------
+# Operation counts of the oracle's formulas (a restatement of the reference's
+# flux_ranocha, flux_nonconservative_waruszewski_etal, FluxLMARS, covariant
+# fluxes and sources, CK2N54 stage update and max_dt), obtained by running one
+# CK2N54 step of the oracle compiled with a counting scalar on each workload's
+# synthetic state (`python oracle/flop_counts.py`, which prints this table;
+# tests/test_flop_counts.py recomputes the cheap rows).  add, sub, mul, div,
+# sqrt, log, exp and pow count one operation each; "element" is the element
+# kernel's share (volume integral, surface integral, apply_jacobian, sources,
+# stage update, and the CFL reduction of the last stage spread over the five
+# stages), "total" adds the interface and boundary fluxes; "transcendental"
+# (log, exp, pow) and "div" are contained in the totals.  These count the
+# reference's formulas as written, which recompute primitive variables in
+# every two-point flux and evaluate the nonconservative term against every
+# node of a line; the kernels compute per-node quantities once, so the
+# algorithmic rate can exceed what the FP64 pipe executes.
+FLOPS_SOURCE = ("operation count of the oracle's formulas per DOF·stage (counting scalar, "
+                "oracle/flop_counts.py), element-kernel share, x DOF")
+ALGORITHMIC_OPS = {
+    "shell": {"total": 2381.223, "element": 2329.702, "transcendental": 7.500, "div": 232.592},
+    "bubble": {"total": 874.958, "element": 835.060, "transcendental": 1.871, "div": 78.517},
+    "swe_weak_3": {"total": 247.013, "element": 171.013, "transcendental": 0.000, "div": 11.400},
+    "swe_weak_5": {"total": 243.339, "element": 192.672, "transcendental": 0.000, "div": 9.733},
+    "swe_weak_7": {"total": 253.503, "element": 215.503, "transcendental": 0.000, "div": 8.900},
+    "swe_ec_3": {"total": 578.013, "element": 506.013, "transcendental": 0.000, "div": 39.400},
+    "swe_ec_5": {"total": 759.672, "element": 711.672, "transcendental": 0.000, "div": 53.067},
+    "swe_ec_7": {"total": 954.503, "element": 918.503, "transcendental": 0.000, "div": 67.900},
+}
 
 
 def bytes_per_element_launch_3d(n, nelem):
@@ -406,23 +466,32 @@ def bytes_per_element_launch_3d(n, nelem):
     return 8 * (nodes * (6 + 9 + 1 + 5 + 5 + 5) + nelem * 6 * n * n * 5)
 
 
-# ---- algorithmic work per DOF·stage (counted from the formulas) ---------------
-def flops_per_element_launch(n, nelem):
-    """FP64 flops of one element-kernel launch: per symmetric pair 101 (flux_ranocha
-    with shared means, half the Waruszewski term, both D_split products), per
-    node 8 (cons2prim), per (node, active variable) 2(n-1)+1 slot sums, Jacobian
-    1 and stage update 5, plus 2 per face-node surface term."""
-    P = n * n * (n - 1)
-    per_elem = P * 101 + n * n * 8 + n * n * 4 * (2 * (n - 1) + 1 + 1 + 5) + 4 * n * 4 * 2
-    return per_elem * nelem
-
-
 def bytes_per_element_launch(n, nelem):
     """Compulsory DRAM bytes of one element-kernel (stage mode) launch: read u
     (5 vars), Ja (4), invJ (1), sfv (4 faces x n x 4 vars per element), k (4);
     write u (4 active vars) and k (4)."""
     nodes = n * n * nelem
     return 8 * (nodes * (5 + 4 + 1 + 4 + 4 + 4) + nelem * 4 * n * 4)
+
+
+# ---- FP64 roofline denominator ---------------------------------------------
+# GB300's FP64 pipe executes at most 2 DFMA (4 flops) per clock per SM: ncu on
+# the FMA probe of tag_fp64_peak (profiles/fp64_pipe_gb300.md) counts 3.36
+# flops per clock per SM at 84.2 % sm__pipe_fp64_cycles_active, i.e. a pipe
+# peak of 4.0.  The denominator is that peak at the SM clock sampled during
+# the timed region (1.259 TFLOP/s at 2070 MHz); the probe's own rate, the
+# best a stream of independent FMAs reaches, is reported beside it.
+FP64_FLOPS_PER_CLK_SM = 4.0
+
+
+def fp64_roofline_peak(tg, clock_info):
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = clock_info.get("sm_mhz") or clock_info.get("sm_max_mhz") or 2070.0
+    peak = FP64_FLOPS_PER_CLK_SM * sms * mhz * 1e6
+    src = (f"FP64 pipe peak 4 flop/clk/SM (ncu, profiles/fp64_pipe_gb300.md) x {sms} SMs x "
+           f"{mhz:.0f} MHz sampled in the timed region, of measured")
+    return peak, src, tg.fp64_peak()
 
 
 # ---- clocks during the timed region ----------------------------------------
@@ -554,9 +623,29 @@ def dist_init():
     return world, rank, local
 
 
+def julia_probe():
+    """Looks for a Julia installation with Trixi and TrixiAtmo on this machine
+    (the reference's own CPU rhs! would be timed there); returns a one-line
+    finding."""
+    import shutil
+    exe = shutil.which("julia")
+    if exe is None:
+        return "julia: not found on PATH"
+    try:
+        r = subprocess.run([exe, "--startup-file=no", "-e", "using Trixi, TrixiAtmo; print(1)"],
+                           capture_output=True, text=True, timeout=300)
+    except (OSError, subprocess.TimeoutExpired) as e:
+        return f"julia at {exe}: probe failed ({e})"
+    if r.returncode != 0:
+        return f"julia at {exe}: `using Trixi, TrixiAtmo` failed"
+    return f"julia at {exe} with Trixi and TrixiAtmo"
+
+
 def _note():
-    return ("Julia/Trixi are not installed on this box; the reference CPU rhs! is the C++ OpenMP "
-            "restatement in oracle/ (pinned to the reference's golden l2/linf)")
+    probe = julia_probe()
+    state = "not timed by this bench" if "with Trixi" in probe else "unavailable on this box"
+    return (f"reference Julia rhs! baseline: {state} ({probe}); the reference CPU rhs! is the "
+            "C++ OpenMP restatement in oracle/ (pinned to the reference's golden l2/linf)")
 
 
 def run_reference(args):
@@ -601,18 +690,18 @@ def run_ours(args):
         torch.cuda.set_device(0)
     tg = entry.load_package()
     if args.workload == "shell":
-        eq, semi = make_shell(tg)
+        eq, semi = make_shell(tg, args.trees, args.layers)
         n = semi.n
-        fl = flops_per_element_launch_3d(n, semi.nelements)
+        fl = ALGORITHMIC_OPS["shell"]["element"] * semi.ndofs
         by = bytes_per_element_launch_3d(n, semi.nelements)
-        workload = ("3D dry Euler on a cubed-sphere shell, 6 panels x 16x16 elements x 8 layers, "
-                    "polydeg 5, isothermal 250 K + seeded density bumps, gravity + Coriolis, "
-                    "CK2N54 CFL 1")
+        workload = (f"3D dry Euler on a cubed-sphere shell, 6 panels x {args.trees}x{args.trees} "
+                    f"elements x {args.layers} layers, polydeg 5, isothermal 250 K + seeded "
+                    "density bumps, gravity + Coriolis, CK2N54 CFL 1")
         l2_note = "inputs larger than L2 (u 127 MB, Ja 191 MB, k 106 MB)"
     else:
         eq, semi = make_ensemble(tg, args.members)
         n = semi.n
-        fl = flops_per_element_launch(n, semi.nelements)
+        fl = ALGORITHMIC_OPS["bubble"]["element"] * semi.ndofs
         by = bytes_per_element_launch(n, semi.nelements)
         workload = (f"ensemble of {args.members} dry warm-bubble members, 64x32 StructuredMesh, "
                     "polydeg 3, CK2N54 CFL 1, per-member dt")
@@ -647,7 +736,7 @@ def run_ours(args):
 
     # kernel timing for the roofline (same stream, CUDA events, stage mode)
     ms_if, ms_el = semi.time_kernels(reps=10)
-    peak_fp64 = tg.fp64_peak()
+    peak_fp64, peak_src, probe_fp64 = fp64_roofline_peak(tg, clock_info)
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
         hbm_peak, hbm_src = float(peaks["hbm_gbs"]), "measured"
@@ -706,11 +795,13 @@ def run_ours(args):
                                            "scaled by DOF" if traffic else None,
                          "kernel": "element kernel (volume + surface + Jacobian + sources + "
                                    "RK stage)",
-                         "peak_source": "FP64 FMA probe in this run (tag_fp64_peak), of measured",
+                         "peak_source": peak_src, "fma_stream_tflops": probe_fp64 / 1e12,
+                         "frac_of_fma_stream": achieved_tf / (probe_fp64 / 1e12),
                          "hbm_achieved_gbs": achieved_gbs, "hbm_peak_gbs": hbm_peak,
                          "hbm_frac": achieved_gbs / hbm_peak, "hbm_peak_source": hbm_src,
                          "ms_element": ms_el, "ms_interface": ms_if,
-                         "flops_per_launch": fl, "bytes_per_launch": by},
+                         "flops_per_launch": fl, "flops_source": FLOPS_SOURCE,
+                         "bytes_per_launch": by},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(u0.nbytes),
                     "d2h_bytes_per_step": int(u0.nbytes)},
             "gpu_launches": args.steps * 11,
@@ -755,6 +846,10 @@ def main():
     ap.add_argument("--ref-members", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-rainy", action="store_true")
+    ap.add_argument("--trees", type=int, default=16,
+                    help="shell: trees per cube-face edge (16 = the benchmark configuration)")
+    ap.add_argument("--layers", type=int, default=8,
+                    help="shell: radial layers (8 = the benchmark configuration)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

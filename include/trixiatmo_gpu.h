@@ -319,6 +319,22 @@ int tag_time_kernels(tag_handle h, int32_t reps, double* ms_interface, double* m
 int tag_set_newton(tag_handle h, int32_t mode, double tol, int32_t max_iterations,
                    int32_t polish);
 
+/* Start of the Newton solve inside tag_rk_steps' stage limiter (no counterpart
+ * in the reference, whose NonlinearSolveDG always starts from the previous
+ * values of slots 7-9): 0 that warm start (default); 1 the learned guess (the
+ * closed-form unsaturated equilibrium where it is valid, else the MLP set by
+ * tag_set_mlp); 2 the closed-form branch alone, with the warm start on
+ * saturated nodes.  A guessed start not converged after 8 updates falls back
+ * to the warm start; with the canonical finish (tag_set_newton polish = 1) all
+ * three starts give the same bits. */
+int tag_set_newton_start(tag_handle h, int32_t start);
+
+/* Newton work of the stage limiter summed over tag_rk_steps calls:
+ * out[0] updates, out[1] fallbacks to the warm start, out[2] node solves that
+ * missed the tolerance, out[3] node solves (nodes x stages); reset != 0 zeroes
+ * the sums after reading. */
+int tag_newton_counters(tag_handle h, int64_t* out, int32_t reset);
+
 typedef struct {
   int64_t nodes;            /* nodes solved                                    */
   int64_t updates;          /* Newton updates until convergence, summed        */
@@ -328,8 +344,9 @@ typedef struct {
 
 /* One Newton solve of the saturation system on every node of the resident
  * state (the stage limiter's work once, nonlinear_solve_dg2d.jl:6-44).
- * use_learned != 0 starts from the learned guess and falls back to the warm
- * start (slots 7-9) when it has not converged after 8 updates.  The learned
+ * use_learned 1 starts from the learned guess, 2 from its closed-form branch
+ * alone (the warm start on saturated nodes), and both fall back to the warm
+ * start (slots 7-9) when not converged after 8 updates; 0 starts warm.  The learned
  * guess is the closed-form unsaturated equilibrium T_unsat = (e_int - rho_m L)
  * / (c_vd rho_d + c_vv rho_m + c_l rho_r) where e_s(T_unsat)/(R_v T_unsat) >=
  * rho_m (exact there), else T_unsat plus the offset predicted by the MLP set
@@ -367,9 +384,38 @@ void* tag_stream(tag_handle h);
 int tag_set_elements_per_block(tag_handle h, int32_t epb);
 int tag_get_elements_per_block(tag_handle h, int32_t* epb);
 
+/* Geometry of the cubed-sphere shell built on the device: what TrixiAtmo's
+ * P4estMeshCubedSphereTopography(trees, layers, inner_radius, thickness;
+ * polydeg) and Trixi's curved P4estMesh{3} cache hold
+ * (src/meshes/p4est_cubed_sphere_topography.jl:596-670): node coordinates of
+ * the equiangular cubed-sphere map, the contravariant vectors in the
+ * invariant curl form (Kopriva 2006) from collocation derivatives, and the
+ * inverse Jacobian.  nodes / derivative_matrix: the LGL basis (host);
+ * ground_height (host, may be null): [E, n, n] heights of each element's
+ * column nodes (j, i) above the sphere, spread over the column by Gal-Chen
+ * (vertical 0) or Sleve(eta_H, s) (vertical 1).  Elements
+ * e = cz + layers (cx + trees (cy + trees face)); outputs (host)
+ * xyz[3, n, n, n, E], Ja[3, 3, n, n, n, E], invJ[n, n, n, E] column-major. */
+int tag_shell_geometry(int32_t trees, int32_t layers, double inner_radius, double thickness,
+                       int32_t polydeg, const double* nodes, const double* derivative_matrix,
+                       const double* ground_height, int32_t vertical, double sleve_eta_h,
+                       double sleve_s, double* xyz, double* Ja, double* invJ);
+
 /* FP64 FMA throughput probe (FLOP/s, FMA = 2) on the current device; the
  * denominator of the FP64 roofline. */
 int tag_fp64_peak(double* flops_per_s);
+
+/* Diagnostics, no counterpart in the reference (whose ln_mean, inv_ln_mean
+ * and stolarsky_mean come from Trixi, imported at src/TrixiAtmo.jl:37):
+ * evaluates the device forms of those means on n host value pairs (x[q],
+ * y[q]) in one kernel.  kind 0: the 2D kernels' pair form (eight-term series,
+ * logarithms beyond f2 = 1e-2); 1: the same with per-node logarithms and the
+ * four-term form below f2 = 1e-4; 2: the 3D energy kernel's halved form
+ * (sixteen-term series up to f2 = 0.09); 3: the single means; 4: the
+ * potential-temperature kernels' Stolarsky mean with gamma = cp / cv.
+ * out1 = ln_mean (kind 4: the Stolarsky mean), out2 = inv_ln_mean. */
+int tag_eval_means(int32_t kind, int64_t n, double cp, double cv, const double* x,
+                   const double* y, double* out1, double* out2);
 
 /* tag_rhs_noalloc — no counterpart in the reference.
  * du = rhs(u) for TAG_EQ_EULER_ENERGY_2D (TAG_VF_RANOCHA_WARUSZEWSKI,

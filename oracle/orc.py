@@ -15,7 +15,9 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_FLOPS_PATH = os.path.join(_HERE, "_build", "liborcflops.so")
 _lib = None
+_flops = None
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip_t = ctypes.POINTER(ctypes.c_int32)
@@ -110,6 +112,9 @@ def lib():
                                       ctypes.c_int]
         L.orc_pt_stolarsky.restype = ctypes.c_double
         L.orc_pt_stolarsky.argtypes = [ctypes.c_double] * 3
+        for name in ("orc_ln_mean", "orc_inv_ln_mean"):
+            getattr(L, name).restype = ctypes.c_double
+            getattr(L, name).argtypes = [ctypes.c_double] * 2
         L.orc_moist_create_mesh.restype = ctypes.c_void_p
         L.orc_moist_create_mesh.argtypes = ([ctypes.c_int] * 2 + [_dp] * 3 + [ctypes.c_int] +
                                             [_ip] * 3 + [ctypes.c_int] + [_ip] * 3 +
@@ -536,6 +541,14 @@ def stolarsky(x, y, gamma):
     return lib().orc_pt_stolarsky(x, y, gamma)
 
 
+def ln_mean(x, y):
+    return lib().orc_ln_mean(x, y)
+
+
+def inv_ln_mean(x, y):
+    return lib().orc_inv_ln_mean(x, y)
+
+
 class Moist2D:
     """Moist Euler on a StructuredMesh rectangle.  surface_kind 0: FluxLMARS(c),
     1: flux_lax_friedrichs, 2: flux_chandrashekar; source_kind 0: none,
@@ -736,4 +749,76 @@ def rainy_flux(u, n):
     f = np.zeros(9)
     lib().orc_rainy_flux(_p(np.ascontiguousarray(u, dtype=np.float64)),
                          _p(np.ascontiguousarray(n, dtype=np.float64)), _p(f))
+    return f
+
+
+# ---- operation counts of the oracle's formulas (orc_flopcount.cpp) ----------
+COUNT_NAMES = ("add", "mul", "div", "sqrt", "log", "exp", "pow")
+
+
+def _flops_lib():
+    global _flops
+    if _flops is None:
+        if not os.path.exists(_FLOPS_PATH):
+            build()
+        L = ctypes.CDLL(_FLOPS_PATH)
+        _ll = ctypes.POINTER(ctypes.c_longlong)
+        L.orc_count_euler3d_step.argtypes = (
+            [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, _ip_t, _ip_t, _ip_t,
+             ctypes.c_int, _ip_t, _ip_t] + [ctypes.c_double] * 6 + [_dp, _ll])
+        L.orc_count_euler2d_step.argtypes = (
+            [ctypes.c_int] * 3 + [ctypes.c_double] * 9 + [_dp, _ll])
+        L.orc_count_cov_step.argtypes = (
+            [ctypes.c_int, ctypes.c_int, _dp, _dp, ctypes.c_int, _ip_t, _ip_t, _ip_t,
+             ctypes.c_double, ctypes.c_double] + [ctypes.c_int] * 7 + [ctypes.c_double, _dp, _ll])
+        _flops = L
+    return _flops
+
+
+PHASES = ("volume", "interface", "boundary", "surface_jacobian_sources", "stage_update",
+          "max_dt")
+
+
+def _counts(call):
+    """{phase: {operation: count}} over one CK2N54 step (max_dt: once)."""
+    out = np.zeros((len(PHASES), 7), dtype=np.int64)
+    call(out.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)))
+    return {ph: dict(zip(COUNT_NAMES, (int(v) for v in out[i]))) for i, ph in enumerate(PHASES)}
+
+
+def count_euler3d_step(polydeg, Ja, invJ, xyz, if_e, if_f, if_o, bd_e, bd_f, u0, c_p=1004.0,
+                       c_v=717.0, g=9.80616, c_lmars=340.0, omega=7.292e-5, cfl=1.0):
+    """Operation counts of one CK2N54 step of the 3D dry-Euler oracle on u0."""
+    c = np.ascontiguousarray
+    ie, ifc, io = (c(a, dtype=np.int32) for a in (if_e, if_f, if_o))
+    be, bf = c(bd_e, dtype=np.int32), c(bd_f, dtype=np.int32)
+    Ja, invJ, xyz, u0 = (c(a, dtype=np.float64) for a in (Ja, invJ, xyz, u0))
+    return _counts(lambda o: _flops_lib().orc_count_euler3d_step(
+        polydeg, invJ.size // (polydeg + 1) ** 3, _p(Ja), _p(invJ), _p(xyz), io.size, _ip(ie),
+        _ip(ifc), _ip(io), be.size, _ip(be), _ip(bf), c_p, c_v, g, c_lmars, omega, cfl, _p(u0), o))
+
+
+def count_euler2d_step(polydeg, nx, ny, x0, x1, y0, y1, u0, c_p=1004.0, c_v=717.0, g=9.81,
+                       c_lmars=340.0, cfl=1.0):
+    """Operation counts of one CK2N54 step of one 2D dry-Euler member."""
+    u0 = np.ascontiguousarray(u0, dtype=np.float64)
+    return _counts(lambda o: _flops_lib().orc_count_euler2d_step(
+        polydeg, nx, ny, x0, x1, y0, y1, c_p, c_v, g, c_lmars, cfl, _p(u0), o))
+
+
+def count_cov_step(polydeg, aux, xyz, if_e, if_f, if_flip, g, omega, split, fluxes, u0, cfl=0.4):
+    """Operation counts of one CK2N54 step of one covariant shallow-water mesh."""
+    c = np.ascontiguousarray
+    ie, ifc, fl = (c(a, dtype=np.int32) for a in (if_e, if_f, if_flip))
+    aux, xyz, u0 = (c(a, dtype=np.float64) for a in (aux, xyz, u0))
+    f = _cov_flux_ids(fluxes)
+    return _counts(lambda o: _flops_lib().orc_count_cov_step(
+        polydeg, aux.size // (26 * (polydeg + 1) ** 2), _p(aux), _p(xyz), fl.size, _ip(ie),
+        _ip(ifc), _ip(fl), g, omega, int(split), f["volume"], f["vol_sym"], f["vol_nc"],
+        f["surf_sym"], f["surf_diss"], f["surf_nc"], cfl, _p(u0), o))
+
+
+def _cov_flux_ids(fluxes):
+    f = dict(volume=0, vol_sym=0, vol_nc=0, surf_sym=0, surf_diss=1, surf_nc=0)
+    f.update(fluxes)
     return f

@@ -25,43 +25,9 @@
 #include "orc_cov_swe.hpp"
 #include "orc_rainy_2d.hpp"
 #include "orc_time.hpp"
+#include "orc_energy_phys.hpp"
 
 namespace orc {
-
-struct EnergyPhys {
-  using State = EulerEnergy2D::State;
-  static constexpr int nv = 5;
-  static constexpr bool has_noncons = true;
-  static constexpr bool has_sources = false;
-  EulerEnergy2D eq;
-  double c_lmars = 340.0;
-  State volume_flux(const State& a, const State& b, const double* n) const {
-    return eq.flux_ranocha(a, b, n);
-  }
-  State volume_noncons(const State& a, const State& b, const double* n) const {
-    return eq.noncons_waruszewski(a, b, n);
-  }
-  State surface_flux(const State& a, const State& b, const double* n) const {
-    return eq.flux_lmars(a, b, n, c_lmars);
-  }
-  State surface_noncons(const State&, const State&, const double*) const { return State{}; }
-  State bc_structured(const State& ui, const double* n, int direction) const {
-    return eq.slip_wall_structured(ui, n, direction, c_lmars);
-  }
-  State bc_normal(const State& ui, const double* n) const {
-    return eq.slip_wall_normal(ui, n, c_lmars);
-  }
-  State source(const State&, const double*, double) const { return State{}; }
-  void max_abs_speeds(const State& u, double& l1, double& l2) const { eq.max_abs_speeds(u, l1, l2); }
-  // flux(u, normal_direction), compressible_euler_energy_with_gravity_2d.jl:154-166
-  State flux(const State& u, const double* n) const {
-    double rho, v1, v2, p;
-    eq.cons2prim(u, rho, v1, v2, p);
-    const double vn = v1 * n[0] + v2 * n[1];
-    const double rvn = rho * vn;
-    return {rvn, rvn * v1 + p * n[0], rvn * v2 + p * n[1], (u[3] + p) * vn, 0.0};
-  }
-};
 
 struct Euler2DCase {
   EnergyPhys phys;
@@ -108,28 +74,6 @@ inline EulerEnergy2D::State ic_warm_bubble(const EulerEnergy2D& eq, const double
   const double rho_e = rho * eq.c_v * T + 0.5 * rho * v1 * v1;
   return {rho, rho * v1, 0.0, rho_e, eq.g * x[1]};
 }
-
-struct EnergyPhys3D {
-  using State = EulerEnergy3D::State;
-  static constexpr int nv = 6;
-  static constexpr bool has_noncons = true;
-  static constexpr bool has_sources = true;
-  EulerEnergy3D eq;
-  double c_lmars = 340.0, omega = 0.0;
-  State volume_flux(const State& a, const State& b, const double* n) const {
-    return eq.flux_ranocha(a, b, n);
-  }
-  State volume_noncons(const State& a, const State& b, const double* n) const {
-    return eq.noncons_waruszewski(a, b, n);
-  }
-  State surface_flux(const State& a, const State& b, const double* n) const {
-    return eq.flux_lmars(a, b, n, c_lmars);
-  }
-  State surface_noncons(const State&, const State&, const double*) const { return State{}; }
-  State bc_normal(const State& ui, const double* n) const { return eq.slip_wall_normal(ui, n, c_lmars); }
-  State source(const State& u, const double*, double) const { return eq.coriolis(u, omega); }
-  void max_abs_speeds(const State& u, double* l) const { eq.max_abs_speeds(u, l); }
-};
 
 // 3D case: geometry and connectivity are copied from the caller's arrays
 // (built by the host mirror exactly as passed to the C ABI).
@@ -1577,6 +1521,10 @@ double orc_pt_ssp_steps(void* h, double* u, double t, double cfl, int nsteps, in
                    c->ndofs() * 5, t,
                    cfl, nsteps, scheme, fixed_dt, t_end);
 }
+
+// the logarithmic mean and its inverse of orc_means.hpp (Trixi's definitions)
+double orc_ln_mean(double x, double y) { return ln_mean(x, y); }
+double orc_inv_ln_mean(double x, double y) { return inv_ln_mean(x, y); }
 
 double orc_pt_stolarsky(double x, double y, double gamma) {
   PotTemp2D eq;

@@ -2,7 +2,7 @@
 reference_goldens.json (run once where the reference sources are available;
 the tests read only the JSON).
 
-    python tests/golden/extract_goldens.py /root/reference/test
+    python tests/golden/extract_goldens.py <reference>/test
 
 Each `@trixi_testset "name"` block of test/*.jl contributes an entry keyed
 "<file>:<line> <name>" with its `l2=[...]` and `linf=[...]` arrays (numbers as

@@ -49,3 +49,25 @@ def test_device_metric_terms_report_pole_singularity(tg, gpu_lib):
     cv, mesh, basis, eq, metric = _setup(tg, 3, 2, True, False)
     with pytest.raises(Exception):
         cv.compute_aux_vars(mesh, basis, eq, metric, None, device=True)
+
+
+@pytest.mark.parametrize("topo", [None, "galchen", "sleve"])
+def test_shell_geometry_on_device_matches_host(tg, gpu_lib, topo):
+    """tag_shell_geometry (node coordinates, curl-form contravariant vectors,
+    inverse Jacobian of the cubed-sphere shell) against the host mirror's NumPy
+    construction, on a perfect sphere and over a mountain spread by Gal-Chen
+    or Sleve vertical coordinates."""
+    def mountain(lat, lon):
+        return 2000.0 * np.exp(-((lat - 0.5) ** 2 + (lon - 1.0) ** 2) / 0.05)
+    kw = {}
+    if topo:
+        kw = dict(initial_topography=mountain,
+                  adapt_vertical_grid=tg.GalChen() if topo == "galchen" else tg.Sleve(0.7, 0.8))
+    for N in (2, 5):
+        basis = tg.LobattoLegendreBasis(N)
+        host = tg.P4estMeshCubedSphereTopography(3, 2, 6.371e6, 30000.0, polydeg=N, **kw)
+        dev = tg.P4estMeshCubedSphereTopography(3, 2, 6.371e6, 30000.0, polydeg=N,
+                                                geometry_on_device=True, **kw)
+        for a, b in zip(host.geometry(basis), dev.geometry(basis)):
+            assert a.shape == b.shape
+            assert np.abs(a - b).max() <= 1e-13 * np.abs(a).max(), np.abs(a - b).max()

@@ -260,3 +260,62 @@ def test_gpu_reproduces_hoeck_moist_bubble_golden(tg, orc, gpu_lib):
     l2d, linfd = semi.calc_error_norms(t_end)
     check_hoeck_moist(l2d, linfd)
     semi.close()
+
+
+def test_newton_maxit_status_set_when_the_limit_is_hit(tg, orc, gpu_lib):
+    """TAG_S_NEWTON_MAXIT is the ABI's form of the reference's
+    `@warn "Newton method: tolerance not met"`
+    (src/callbacks_stage/nonlinear_solve_dg2d.jl:33-35).  Made to fire from the
+    host: max_iterations = 1 on the bubble's constructed vapour / cloud /
+    temperature slots, which are off the saturation equilibrium, leaves nodes
+    outside the tolerance; the oracle's solve with the same limit counts the
+    same nodes.  The bit marks nodes whose residual still misses the tolerance
+    after max_iterations updates (the reference warns whenever the last allowed
+    update was taken, a superset).  With the default 20 iterations the solve
+    converges everywhere and the bit stays clear."""
+    eq, semi = make_rainy(tg, 8, 4)
+    u0 = semi.compute_coefficients()
+    n = u0.size // 9
+    semi.set_state(u0)
+    semi.status(clear=True)
+    semi.set_newton(mode=0, tol=1e-9, max_iterations=1)
+    st, _ = semi.newton_solve()
+    assert semi.status() & tg._lib.TAG_S_NEWTON_MAXIT
+    assert st["not_converged"] > n // 10
+    v = np.ascontiguousarray(u0).copy()
+    _, _, nf = orc.rainy_newton_states(v, mode=0, tol=1e-9, maxit=1)
+    assert abs(st["not_converged"] - nf) <= max(1, n // 100), (st["not_converged"], nf)
+    semi.set_state(u0)
+    semi.set_newton(mode=0, tol=1e-9, max_iterations=20)
+    st, _ = semi.newton_solve()
+    assert st["not_converged"] == 0
+    assert not semi.status() & tg._lib.TAG_S_NEWTON_MAXIT
+    semi.close()
+
+
+def test_learned_guess_in_run_beats_its_closed_form_branch(tg, orc, gpu_lib):
+    """The stage limiter inside the RK run (as the reference applies it after
+    every stage, src/callbacks_stage/nonlinear_solve_dg2d.jl:6-44), started
+    three ways: warm (the reference's), the closed-form unsaturated branch alone
+    (warm start on saturated nodes), and closed form + MLP.  Unsaturated nodes
+    take the same closed form in the last two, so their difference is the
+    network's gain on saturated nodes, which must be positive; with the
+    canonical finish the three runs give the same states."""
+    lg = tg.learned_guess
+    p, _, _ = lg.train_guess(n=200_000, epochs=8, seed=3)
+    res = {}
+    for start in (0, 2, 1):
+        eq, semi = make_rainy(tg, 32, 16, 3)
+        semi.set_mlp(p)
+        semi.set_newton(mode=1, tol=1e-12, max_iterations=30, polish=1)
+        semi.set_newton_start(start)
+        semi.set_state(semi.compute_coefficients())
+        semi.rk_steps(3, cfl=1.0, t=0.0)
+        res[start] = (semi.newton_counters(), semi.get_state())
+        semi.close()
+    for start in (0, 1, 2):
+        assert res[start][0]["not_converged"] == 0
+        assert res[start][0]["node_solves"] == 3 * 5 * 32 * 16 * 16
+    assert res[1][0]["updates"] < res[2][0]["updates"] <= res[0][0]["updates"], res
+    for start in (1, 2):
+        assert max_norm_rel(res[start][1], res[0][1]) <= 1e-10

@@ -141,6 +141,12 @@ SIGNATURES = {
     "tag_set_elements_per_block": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "tag_get_elements_per_block": (ctypes.c_int, [ctypes.c_void_p, _ip]),
     "tag_fp64_peak": (ctypes.c_int, [_dp]),
+    "tag_shell_geometry": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_int32, _dp, _dp, _dp,
+                                          ctypes.c_int32, ctypes.c_double, ctypes.c_double, _dp,
+                                          _dp, _dp]),
+    "tag_eval_means": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, ctypes.c_double,
+                                      ctypes.c_double, _dp, _dp, _dp, _dp]),
     "tag_last_error": (ctypes.c_char_p, []),
     "tag_set_newton": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double,
                                       ctypes.c_int32, ctypes.c_int32]),
@@ -150,6 +156,9 @@ SIGNATURES = {
                                                ctypes.c_double, ctypes.c_int32, ctypes.c_int32,
                                                _fp, _ip, ctypes.POINTER(NewtonStats)]),
     "tag_set_mlp": (ctypes.c_int, [ctypes.c_void_p, _fp]),
+    "tag_set_newton_start": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "tag_newton_counters": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
+                                           ctypes.c_int32]),
     "tag_mlp_forward": (ctypes.c_int, [_fp, _fp, ctypes.c_int64, _fp]),
     "tag_mlp_loss_grad": (ctypes.c_int, [_fp, _fp, _fp, ctypes.c_int64, _fp, _fp]),
     "tag_mlp_train": (ctypes.c_int, [_fp, _fp, _fp, ctypes.c_int64, ctypes.c_int32,

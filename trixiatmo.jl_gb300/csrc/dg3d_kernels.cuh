@@ -119,7 +119,7 @@ struct ElemSmem3D {
   static constexpr int TPE = (P > nnn) ? P : nnn;  // threads per element
   static constexpr int oU = 0;
   static constexpr int oQ = oU + nnn * NV;
-  static constexpr int oJa = oQ + nnn * NQ;       // halved
+  static constexpr int oJa = oQ + nnn * NQ;       // contravariant vectors as stored
   static constexpr int oA = oJa + nnn * 9;        // accumulators [3][nnn][NA]
   static constexpr int oL = oA + 3 * nnn * NA;    // CFL speeds [3][nnn]
   static constexpr int per_elem = oL + 3 * nnn;
@@ -143,8 +143,13 @@ __global__ void k_element3d(typename Phys::Params Pp, const BasisDev basis, doub
   const int nthr = blockDim.x;
   unsigned bad = 0;
 
-  for (int t = threadIdx.x; t < (int)(sizeof(BasisDev) / sizeof(double)); t += nthr)
-    smem[t] = reinterpret_cast<const double*>(&basis)[t];
+  // The pair normal is ja_a + ja_b, twice the average the two-point fluxes
+  // take; every volume pair flux is linear in the normal, so D_split is halved
+  // instead (both scalings by 2 are exact: the same bits as averaging).
+  for (int t = threadIdx.x; t < (int)(sizeof(BasisDev) / sizeof(double)); t += nthr) {
+    const double b = reinterpret_cast<const double*>(&basis)[t];
+    smem[t] = t < kMaxNodes * kMaxNodes ? 0.5 * b : b;
+  }
   {
     const double* ug = u + (size_t)e_first * nnn * NV;
     for (int t = threadIdx.x; t < ne * nnn * NV; t += nthr) {
@@ -154,7 +159,7 @@ __global__ void k_element3d(typename Phys::Params Pp, const BasisDev basis, doub
     const double* jg = Ja + (size_t)e_first * nnn * 9;
     for (int t = threadIdx.x; t < ne * nnn * 9; t += nthr) {
       const int el = t / (nnn * 9), r = t % (nnn * 9);
-      base[el * S::per_elem + S::oJa + r] = 0.5 * jg[t];
+      base[el * S::per_elem + S::oJa + r] = jg[t];
     }
   }
   __syncthreads();
@@ -191,7 +196,8 @@ __global__ void k_element3d(typename Phys::Params Pp, const BasisDev basis, doub
         b1 = fmax(b1, __shfl_xor_sync(0xffffffffu, b1, o));
       }
       if (lane == 0)
-        base[el * S::per_elem + S::oL] = (needs_logs(r0, r1) || needs_logs(b0, b1)) ? 1.0 : 0.0;
+        base[el * S::per_elem + S::oL] =
+            (needs_logs(r0, r1, Phys::kLogRange) || needs_logs(b0, b1, Phys::kLogRange)) ? 1.0 : 0.0;
     }
     __syncthreads();
   }
@@ -299,8 +305,8 @@ __global__ void k_element3d(typename Phys::Params Pp, const BasisDev basis, doub
       for (int v = NA; v < NV; ++v) un[v] = eb[S::oU + node * NV + v];
       double lam[3];
       Phys::max_speeds(Pp, un, lam);
-      const double* ja = eb + S::oJa + node * 9;  // halved
-      const double ij = 2.0 * fabs(invJ[(size_t)(e_first + el) * nnn + node]);
+      const double* ja = eb + S::oJa + node * 9;
+      const double ij = fabs(invJ[(size_t)(e_first + el) * nnn + node]);
 #pragma unroll
       for (int d = 0; d < 3; ++d)
         eb[S::oL + d * nnn + node] =

@@ -69,7 +69,10 @@ struct NewtonArgs {
   int maxit;         // Newton updates allowed
   int polish;        // canonical finish: Newton updates from the converged iterate snapped
                      // to a fixed grid (0: stop at the criterion, as the reference does)
-  int learned;       // start from the MLP guess (fallback to the warm start after maxit_learned)
+  int learned;       // start: 0 the warm start (slots 7-9, as the reference); 1 the closed-form
+                     // unsaturated equilibrium where valid, else the MLP guess; 2 the closed
+                     // form where valid, else the warm start.  A guessed start that has not
+                     // converged after maxit_learned updates falls back to the warm start.
   int maxit_learned; // 8
   double tol;
   const float* mlp;  // device parameters (kMlpParams floats) or null
@@ -179,19 +182,28 @@ TAG_DEV int rainy_newton_run(const double* u, double* x, int mode, double tol, i
   return it;
 }
 
+// The closed-form unsaturated equilibrium (all moisture as vapour at T_unsat)
+// when it is valid, i.e. when the vapour fits under the saturation density;
+// returns false for a saturated node.
+TAG_DEV bool rainy_closed_form_guess(const double* u, double* x, double& tu, double& e_int) {
+  using C = RainyConst;
+  tu = rainy_t_unsat(u, e_int);
+  if (tu > 0.0 && rainy_e_s(tu) / (C::R_v * tu) >= u[1]) {
+    x[0] = u[1];
+    x[1] = 0.0;
+    x[2] = tu;
+    return true;
+  }
+  return false;
+}
+
 // Learned start: the closed-form unsaturated equilibrium where it is valid,
 // else T_unsat plus the network's latent-heat offset, with vapour and cloud
 // from the saturation relation at that temperature.
 TAG_DEV void rainy_learned_guess(const float* __restrict__ P, const double* u, double* x) {
   using C = RainyConst;
-  double e_int;
-  const double tu = rainy_t_unsat(u, e_int);
-  if (tu > 0.0 && rainy_e_s(tu) / (C::R_v * tu) >= u[1]) {
-    x[0] = u[1];
-    x[1] = 0.0;
-    x[2] = tu;
-    return;
-  }
+  double e_int, tu;
+  if (rainy_closed_form_guess(u, x, tu, e_int)) return;
   float xin[kMlpIn];
   mlp_inputs(u, e_int, tu, xin);
   const double T = tu + fmax((double)mlp_forward(P, xin), 0.0);
@@ -203,7 +215,7 @@ TAG_DEV void rainy_learned_guess(const float* __restrict__ P, const double* u, d
 static __global__ void __launch_bounds__(256) k_newton_rainy(double* __restrict__ u, long nodes,
                                                       NewtonArgs a, unsigned* __restrict__ status) {
   __shared__ float sp[kMlpParams];
-  if (a.learned && a.mlp) {
+  if (a.learned == 1 && a.mlp) {
     for (int t = threadIdx.x; t < kMlpParams; t += blockDim.x) sp[t] = a.mlp[t];
     __syncthreads();
   }
@@ -217,9 +229,16 @@ static __global__ void __launch_bounds__(256) k_newton_rainy(double* __restrict_
   double x[3] = {s[6], s[7], s[8]};
   bool conv = false;
   int its = 0, fallback = 0;
-  if (a.learned && a.mlp) {
-    double xg[3];
+  double xg[3];
+  bool guessed = false;
+  if (a.learned == 1 && a.mlp) {
     rainy_learned_guess(sp, s, xg);
+    guessed = true;
+  } else if (a.learned == 2) {
+    double tu, e_int;
+    guessed = rainy_closed_form_guess(s, xg, tu, e_int);
+  }
+  if (guessed) {
     its = rainy_newton_run(s, xg, a.mode, a.tol, a.maxit_learned, a.polish, conv);
     if (conv && isfinite(xg[2])) {
       x[0] = xg[0];

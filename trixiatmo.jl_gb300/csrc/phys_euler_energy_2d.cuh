@@ -11,7 +11,8 @@ struct PhysEnergy2D {
   static constexpr int NV = 5;  // stored variables per node
   static constexpr int NA = 4;  // variables with nonzero du
   // per-node quantities kept in shared memory (odd stride: no bank conflicts):
-  // rho, v1/2, v2/2, p/2, phi/2, beta = rho/p, log rho, log beta, (pad)
+  // rho/2, v1/2, v2/2, p/2, phi/2, beta/2 = rho/(2p), log(rho/2), log(beta/2),
+  // (pad); the halved rho and beta feed ln_mean_pair_halved
   static constexpr int NQ = 9;
   static constexpr int kRho = 0, kBeta = 5, kLogRho = 6, kLogBeta = 7;
   static constexpr bool kNodeLogs = false;  // 2D elements rarely leave the series range
@@ -19,7 +20,7 @@ struct PhysEnergy2D {
   static constexpr bool kSurfaceNoncons = false;  // surface flux only (flux_zero)
 
   struct Params {
-    double gamma, gm1, inv_gm1, c_lmars, inv_2c;
+    double gamma, gm1, inv_gm1, c_lmars, inv_2c, half_inv_gm1;
   };
 
   static Params make_params(const double* p) {
@@ -30,22 +31,23 @@ struct PhysEnergy2D {
     q.inv_gm1 = 1.0 / (q.gamma - 1.0);
     q.c_lmars = p[3];
     q.inv_2c = 0.5 / p[3];
+    q.half_inv_gm1 = 0.5 * q.inv_gm1;
     return q;
   }
 
   // cons2prim (:527-536), once per node:
-  //   q = (rho, v1/2, v2/2, p/2, phi/2, beta = rho/p); flags bad states.
+  //   q = (rho/2, v1/2, v2/2, p/2, phi/2, beta/2 = rho/(2p)); flags bad states.
   TAG_DEV static void node_prims(const Params& P, const double* u, double* q, unsigned& bad) {
     const double rho = u[0];
     const double irho = 1.0 / rho;
     const double v1 = u[1] * irho, v2 = u[2] * irho;
     const double p = P.gm1 * (u[3] - 0.5 * (u[1] * v1 + u[2] * v2));
-    q[0] = rho;
+    q[0] = 0.5 * rho;
     q[1] = 0.5 * v1;
     q[2] = 0.5 * v2;
     q[3] = 0.5 * p;
     q[4] = 0.5 * u[4];
-    q[5] = rho / p;
+    q[5] = 0.5 * rho / p;
     q[8] = 0.0;
     if (!(rho > 0.0)) bad |= TAG_S_NEG_DENSITY;
     if (!(p > 0.0)) bad |= TAG_S_NEG_PRESSURE;
@@ -57,31 +59,38 @@ struct PhysEnergy2D {
   // node a, weighted by Dsplit[a,b]) and Fb = F - G/2 (to node b, Dsplit[b,a]);
   // G(b,a) = -G(a,b).  Written on the half-valued node quantities of
   // node_prims; p_ll p_rr inv_ln_mean(rho_ll p_rr, rho_rr p_ll) is evaluated as
-  // the equal inv_ln_mean(rho_ll/p_ll, rho_rr/p_rr).
+  // the equal inv_ln_mean(rho_ll/p_ll, rho_rr/p_rr).  With h the gravity term
+  // rho_mean (phi_b - phi_a) / 2, the momentum fluxes of the two sides are
+  // f1 v + n (p_avg +- h) and the energy fluxes 2 E +- h vn, E being half of
+  // flux_ranocha's energy flux.
   TAG_DEV static void volume_pair(const Params& P, const double* qa, const double* qb,
                                   double n1, double n2, double* Fa, double* Fb) {
     double rho_mean, inv_rho_p_mean;
-    ln_mean_pair<kNodeLogs>(qa[0], qb[0], qa[5], qb[5], qa[6], qb[6], qa[7], qb[7], rho_mean,
-                            inv_rho_p_mean);
-    const double v1_avg = qa[1] + qb[1];
-    const double v2_avg = qa[2] + qb[2];
-    const double p_avg = qa[3] + qb[3];
-    const double vsq_avg = 2.0 * (qa[1] * qb[1] + qa[2] * qb[2]);
-    const double vn = v1_avg * n1 + v2_avg * n2;  // 0.5 (vn_a + vn_b)
+    ln_mean_pair_halved<false, 8, true>(qa[0], qb[0], qa[5], qb[5], 0.0, 0.0, 0.0, 0.0,
+                                        rho_mean, inv_rho_p_mean);
+    const double v1 = qa[1] + qb[1];
+    const double v2 = qa[2] + qb[2];
+    const double vn = fma(v2, n2, v1 * n1);  // 0.5 (vn_a + vn_b)
     const double f1 = rho_mean * vn;
-    const double f2 = f1 * v1_avg + p_avg * n1;
-    const double f3 = f1 * v2_avg + p_avg * n2;
-    // 0.5 (p_a vn_b + p_b vn_a)
-    const double c1 = qa[3] * qb[1] + qb[3] * qa[1];
-    const double c2 = qa[3] * qb[2] + qb[3] * qa[2];
-    const double f4 = f1 * (vsq_avg + inv_rho_p_mean * P.inv_gm1) + 2.0 * (n1 * c1 + n2 * c2);
-    // half of waruszewski: 0.5 ln_mean(rho) (phi_b - phi_a) * (0, n1, n2, n . v_avg)
     const double h = rho_mean * (qb[4] - qa[4]);
-    const double g2 = n1 * h, g3 = n2 * h, g4 = h * vn;
-    Fa[0] = f1;      Fb[0] = f1;
-    Fa[1] = f2 + g2; Fb[1] = f2 - g2;
-    Fa[2] = f3 + g3; Fb[2] = f3 - g3;
-    Fa[3] = f4 + g4; Fb[3] = f4 - g4;
+    const double p_avg = qa[3] + qb[3];
+    const double pp = p_avg + h, pm = p_avg - h;
+    const double t1 = f1 * v1, t2 = f1 * v2;
+    Fa[0] = f1;
+    Fb[0] = f1;
+    Fa[1] = fma(n1, pp, t1);
+    Fb[1] = fma(n1, pm, t1);
+    Fa[2] = fma(n2, pp, t2);
+    Fb[2] = fma(n2, pm, t2);
+    // E = f1 (v_a.v_b / 4 + inv_beta_mean / (2 (gamma - 1))) + (p_a vn_b + p_b vn_a) / 4
+    const double vv = fma(qa[2], qb[2], qa[1] * qb[1]);
+    const double x = fma(inv_rho_p_mean, P.half_inv_gm1, vv);
+    const double c1 = fma(qa[3], qb[1], qb[3] * qa[1]);
+    const double c2 = fma(qa[3], qb[2], qb[3] * qa[2]);
+    const double e = fma(f1, x, fma(n2, c2, n1 * c1));
+    const double hv = h * vn;
+    Fa[3] = fma(2.0, e, hv);
+    Fb[3] = fma(2.0, e, -hv);
   }
 
   // FluxLMARS (:397-430) between states ul, ur for the (unnormalised) normal n.

@@ -11,16 +11,19 @@ namespace tag {
 struct PhysEnergy3D {
   static constexpr int NV = 6;
   static constexpr int NA = 5;
-  // rho, v1/2, v2/2, v3/2, p/2, phi/2, beta = rho/p, log rho, log beta (odd stride)
+  // rho/2, v1/2, v2/2, v3/2, p/2, phi/2, beta/2 = rho/(2p), log(rho/2),
+  // log(beta/2) (odd stride); the halved rho and beta feed ln_mean_pair_halved
   static constexpr int NQ = 9;
   static constexpr int kRho = 0, kBeta = 6, kLogRho = 7, kLogBeta = 8;
-  // tall shell elements (km-sized vertical node spacing) put many vertical
-  // pairs out of the series range: logarithms once per node
+  // the sixteen-term series keeps every pair of a tall shell element (km-sized
+  // vertical node spacing) out of the logarithms; only elements whose values
+  // spread further take logarithms, once per node
   static constexpr bool kNodeLogs = true;
+  static constexpr double kLogRange = kLongLogRange;
   static constexpr bool kHasSources = true;  // Coriolis, added per (node, variable)
 
   struct Params {
-    double gamma, gm1, inv_gm1, c_lmars, omega;
+    double gamma, gm1, inv_gm1, c_lmars, omega, half_inv_gm1;
   };
 
   static Params make_params(const double* p) {
@@ -28,6 +31,7 @@ struct PhysEnergy3D {
     q.gamma = p[0] / p[1];
     q.gm1 = q.gamma - 1.0;
     q.inv_gm1 = 1.0 / (q.gamma - 1.0);
+    q.half_inv_gm1 = 0.5 * q.inv_gm1;
     q.c_lmars = p[3];
     q.omega = p[4];
     return q;
@@ -38,45 +42,54 @@ struct PhysEnergy3D {
     const double irho = 1.0 / rho;
     const double v1 = u[1] * irho, v2 = u[2] * irho, v3 = u[3] * irho;
     const double p = P.gm1 * (u[4] - 0.5 * (u[1] * v1 + u[2] * v2 + u[3] * v3));
-    q[0] = rho;
+    q[0] = 0.5 * rho;
     q[1] = 0.5 * v1;
     q[2] = 0.5 * v2;
     q[3] = 0.5 * v3;
     q[4] = 0.5 * p;
     q[5] = 0.5 * u[5];
-    q[6] = rho / p;
+    q[6] = 0.5 * rho / p;
     if (!(rho > 0.0)) bad |= TAG_S_NEG_DENSITY;
     if (!(p > 0.0)) bad |= TAG_S_NEG_PRESSURE;
   }
 
   // flux_ranocha (3D, :382-415) + half of flux_nonconservative_waruszewski_etal
   // (3D, :135-159) for one symmetric pair; see PhysEnergy2D::volume_pair.
+  // nrm is the average of the two nodes' contravariant vectors.  With h the
+  // gravity term rho_mean (phi_b - phi_a) / 2, the momentum fluxes of the two
+  // sides are f1 v + n (p_avg +- h), and the energy fluxes 2 E +- h vn with
+  // E = f1 (v_a.v_b / 4 + inv_beta_mean / (2 (gamma - 1))) + (p_a vn_b + p_b vn_a) / 4
+  // (node values halved, so E is half of flux_ranocha's energy flux).
   TAG_DEV static void volume_pair(const Params& P, const double* qa, const double* qb,
                                   const double* nrm, double* Fa, double* Fb) {
     double rho_mean, inv_rho_p_mean;
-    ln_mean_pair<kNodeLogs>(qa[0], qb[0], qa[6], qb[6], qa[7], qb[7], qa[8], qb[8], rho_mean,
-                            inv_rho_p_mean);
+    ln_mean_pair_halved(qa[0], qb[0], qa[6], qb[6], qa[7], qb[7], qa[8], qb[8], rho_mean,
+                        inv_rho_p_mean);
     const double n1 = nrm[0], n2 = nrm[1], n3 = nrm[2];
     const double v1 = qa[1] + qb[1], v2 = qa[2] + qb[2], v3 = qa[3] + qb[3];
-    const double p_avg = qa[4] + qb[4];
-    const double vsq = 2.0 * (qa[1] * qb[1] + qa[2] * qb[2] + qa[3] * qb[3]);
-    // halved normal velocities of both nodes: vn = 0.5 (vn_a + vn_b) and
-    // 0.5 (p_a vn_b + p_b vn_a) = 2 (q_a[4] vnb + q_b[4] vna)
-    const double vna = qa[1] * n1 + qa[2] * n2 + qa[3] * n3;
-    const double vnb = qb[1] * n1 + qb[2] * n2 + qb[3] * n3;
+    // halved normal velocities of both nodes: vn = 0.5 (vn_a + vn_b)
+    const double vna = fma(qa[3], n3, fma(qa[2], n2, qa[1] * n1));
+    const double vnb = fma(qb[3], n3, fma(qb[2], n2, qb[1] * n1));
     const double vn = vna + vnb;
     const double f1 = rho_mean * vn;
-    const double f2 = f1 * v1 + p_avg * n1;
-    const double f3 = f1 * v2 + p_avg * n2;
-    const double f4 = f1 * v3 + p_avg * n3;
-    const double f5 = f1 * (vsq + inv_rho_p_mean * P.inv_gm1) + 2.0 * (qa[4] * vnb + qb[4] * vna);
     const double h = rho_mean * (qb[5] - qa[5]);
-    const double g2 = n1 * h, g3 = n2 * h, g4 = n3 * h, g5 = h * vn;
-    Fa[0] = f1;      Fb[0] = f1;
-    Fa[1] = f2 + g2; Fb[1] = f2 - g2;
-    Fa[2] = f3 + g3; Fb[2] = f3 - g3;
-    Fa[3] = f4 + g4; Fb[3] = f4 - g4;
-    Fa[4] = f5 + g5; Fb[4] = f5 - g5;
+    const double p_avg = qa[4] + qb[4];
+    const double pp = p_avg + h, pm = p_avg - h;
+    const double t1 = f1 * v1, t2 = f1 * v2, t3 = f1 * v3;
+    Fa[0] = f1;
+    Fb[0] = f1;
+    Fa[1] = fma(n1, pp, t1);
+    Fb[1] = fma(n1, pm, t1);
+    Fa[2] = fma(n2, pp, t2);
+    Fb[2] = fma(n2, pm, t2);
+    Fa[3] = fma(n3, pp, t3);
+    Fb[3] = fma(n3, pm, t3);
+    const double vv = fma(qa[3], qb[3], fma(qa[2], qb[2], qa[1] * qb[1]));
+    const double x = fma(inv_rho_p_mean, P.half_inv_gm1, vv);
+    const double e = fma(f1, x, fma(qa[4], vnb, qb[4] * vna));
+    const double hv = h * vn;
+    Fa[4] = fma(2.0, e, hv);
+    Fb[4] = fma(2.0, e, -hv);
   }
 
   // FluxLMARS (3D, :430-466)

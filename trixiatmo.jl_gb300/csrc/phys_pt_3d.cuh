@@ -21,6 +21,7 @@ struct PhysPT3D {
   static constexpr int NQ = 13;
   static constexpr int kRho = 0, kBeta = 0, kLogRho = 0, kLogBeta = 0;
   static constexpr bool kNodeLogs = false;
+  static constexpr double kLogRange = kLogMeanRange;
   static constexpr bool kHasSources = true;  // Coriolis, per (node, variable)
 
   struct Params {

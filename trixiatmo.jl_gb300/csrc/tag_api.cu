@@ -9,6 +9,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "dg2d_kernels.cuh"
 #include "cov_kernels.cuh"
 #include "dg3d_kernels.cuh"
@@ -23,6 +25,21 @@
 #include "tag_analysis.cuh"
 
 using namespace tag;
+
+// NVTX ranges named after the reference's timer sections of rhs_hyperbolic!
+// (src/solvers/dgsem_p4est/dg_2d_manifold_in_3d_covariant.jl:16-67) and the
+// stage limiter (src/callbacks_stage/nonlinear_solve_dg.jl:38), joined where
+// one kernel does several of them.  Header-only NVTX: inert unless a profiler
+// attaches.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+constexpr const char* kNvtxInterface = "prolong2interfaces + interface flux + boundary flux";
+constexpr const char* kNvtxElement =
+    "volume integral + surface integral + Jacobian + source terms";
 
 namespace {
 
@@ -74,6 +91,12 @@ struct tag_handle_s {
   float* d_mlp = nullptr;
   unsigned long long* d_counters = nullptr;
   int* d_iters = nullptr;
+  // the stage limiter inside tag_rk_steps: its start (NewtonArgs::learned)
+  // and counters accumulated over the run ([0] updates, [1] fallbacks,
+  // [2] not converged), with the number of node solves they cover
+  int newton_start = 0;
+  unsigned long long* d_run_counters = nullptr;
+  long long run_node_solves = 0;
   BasisDev basis{};
   cudaStream_t stream = nullptr;
   double *d_u = nullptr, *d_k = nullptr, *d_Ja = nullptr, *d_invJ = nullptr, *d_xy = nullptr,
@@ -386,9 +409,10 @@ int stage_sequence(tag_handle h) {
       // stage limiter: saturation Newton solve on every node (warm start)
       const long nodes = (long)h->nodes;
       NewtonArgs a = h->newton;
-      a.learned = 0;
+      a.learned = h->newton_start;
+      a.mlp = h->d_mlp;
       a.iters = nullptr;
-      a.counters = nullptr;
+      a.counters = h->d_run_counters;
       k_newton_rainy<<<(unsigned)((nodes + 255) / 256), 256, 0, h->stream>>>(h->d_u, nodes, a,
                                                                               h->d_status);
       TAG_CUDA(cudaGetLastError());
@@ -1090,6 +1114,8 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
   if ((rc = upload(&h->d_ctl, (const StepCtl*)nullptr, 1, h->stream))) return cleanup(rc);
   if ((rc = upload(&h->d_status, (const unsigned*)nullptr, 1, h->stream))) return cleanup(rc);
   if (rainy) {
+    if ((rc = upload(&h->d_run_counters, (const unsigned long long*)nullptr, 4, h->stream)))
+      return cleanup(rc);
     if ((rc = upload(&h->d_counters, (const unsigned long long*)nullptr, 4, h->stream)))
       return cleanup(rc);
     if ((rc = upload(&h->d_iters, (const int*)nullptr, nodes, h->stream))) return cleanup(rc);
@@ -1139,6 +1165,7 @@ int tag_destroy(tag_handle h) {
   if (h->d_bases) cudaFree(h->d_bases);
   if (h->d_mlp) cudaFree(h->d_mlp);
   if (h->d_counters) cudaFree(h->d_counters);
+  if (h->d_run_counters) cudaFree(h->d_run_counters);
   if (h->d_iters) cudaFree(h->d_iters);
   if (h->d_mscal) cudaFree(h->d_mscal);
   if (h->d_ctl) cudaFree(h->d_ctl);
@@ -1165,11 +1192,18 @@ int tag_rhs(tag_handle h, const double* u, double* du, double t, int32_t on_devi
     ud = h->d_tmp_u;
     dud = h->d_tmp_du;
   }
+  NvtxRange r_rhs("rhs!");
   int rc = autotune(h, ud);
   if (rc) return rc;
-  rc = h->ops->interface(h, ud);
+  {
+    NvtxRange r(kNvtxInterface);
+    rc = h->ops->interface(h, ud);
+  }
   if (rc) return rc;
-  rc = h->ops->element(h, kModeRhs, const_cast<double*>(ud), dud, 0, false, t);
+  {
+    NvtxRange r(kNvtxElement);
+    rc = h->ops->element(h, kModeRhs, const_cast<double*>(ud), dud, 0, false, t);
+  }
   if (rc) return rc;
   if (!on_device) TAG_CUDA(cudaMemcpyAsync(du, dud, bytes, cudaMemcpyDeviceToHost, h->stream));
   TAG_CUDA(cudaStreamSynchronize(h->stream));
@@ -1248,7 +1282,9 @@ int tag_rk_steps(tag_handle h, int32_t nsteps, double cfl, double fixed_dt, doub
   TAG_CUDA(cudaMemcpyAsync(h->d_ctl, h->h_pin + 3 * M, sizeof(StepCtl), cudaMemcpyHostToDevice,
                            h->stream));
   if ((rc = build_graph(h))) return rc;
+  NvtxRange r_steps(h->has_limiter ? "RK steps (stages + nonlinear system solver)" : "RK steps");
   for (int s = 0; s < nsteps; ++s) TAG_CUDA(cudaGraphLaunch(h->graph, h->stream));
+  if (h->has_limiter) h->run_node_solves += (long long)nsteps * rk_stages(h->scheme) * h->nodes;
   TAG_CUDA(cudaMemcpyAsync(h->h_pin, h->d_mscal, sizeof(double) * 2 * M, cudaMemcpyDeviceToHost,
                            h->stream));
   TAG_CUDA(cudaStreamSynchronize(h->stream));
@@ -1342,6 +1378,32 @@ int tag_set_newton(tag_handle h, int32_t mode, double tol, int32_t max_iteration
   return TAG_OK;
 }
 
+int tag_set_newton_start(tag_handle h, int32_t start) {
+  if (!h || !h->has_limiter) return fail(TAG_E_INVALID, "not a rainy handle");
+  if (start < 0 || start > 2) return fail(TAG_E_INVALID, "start must be 0, 1 or 2");
+  if (start == 1 && !h->d_mlp) return fail(TAG_E_INVALID, "no MLP parameters set");
+  h->newton_start = start;
+  h->graph_epb = -2;  // the limiter's arguments are baked into the captured graph
+  return TAG_OK;
+}
+
+int tag_newton_counters(tag_handle h, int64_t* out, int32_t reset) {
+  if (!h || !h->has_limiter || !out) return fail(TAG_E_INVALID, "bad argument");
+  unsigned long long c[4];
+  TAG_CUDA(cudaMemcpyAsync(c, h->d_run_counters, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+  TAG_CUDA(cudaStreamSynchronize(h->stream));
+  out[0] = (int64_t)c[0];
+  out[1] = (int64_t)c[1];
+  out[2] = (int64_t)c[2];
+  out[3] = h->run_node_solves;
+  if (reset) {
+    TAG_CUDA(cudaMemsetAsync(h->d_run_counters, 0, sizeof(c), h->stream));
+    TAG_CUDA(cudaStreamSynchronize(h->stream));
+    h->run_node_solves = 0;
+  }
+  return TAG_OK;
+}
+
 int tag_set_mlp(tag_handle h, const float* params) {
   if (!h || !h->has_limiter || !params) return fail(TAG_E_INVALID, "bad argument");
   if (!h->d_mlp) TAG_CUDA(cudaMalloc(&h->d_mlp, sizeof(float) * kMlpParams));
@@ -1353,10 +1415,12 @@ int tag_set_mlp(tag_handle h, const float* params) {
 
 int tag_newton_solve(tag_handle h, int32_t use_learned, int32_t* iters, tag_newton_stats* stats) {
   if (!h || !h->has_limiter) return fail(TAG_E_INVALID, "not a rainy handle");
-  if (use_learned && !h->d_mlp) return fail(TAG_E_INVALID, "no MLP parameters set");
+  if (use_learned < 0 || use_learned > 2) return fail(TAG_E_INVALID, "start must be 0, 1 or 2");
+  NvtxRange r_solve("nonlinear system solver");
+  if (use_learned == 1 && !h->d_mlp) return fail(TAG_E_INVALID, "no MLP parameters set");
   const long nodes = (long)h->nodes;
   NewtonArgs a = h->newton;
-  a.learned = use_learned ? 1 : 0;
+  a.learned = use_learned;
   a.mlp = h->d_mlp;
   a.iters = h->d_iters;
   a.counters = h->d_counters;

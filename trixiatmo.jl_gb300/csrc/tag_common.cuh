@@ -116,6 +116,113 @@ TAG_DEV void ln_mean_pair(double xa, double xb, double ya, double yb, double Lxa
   }
 }
 
+// The same series R and Q to sixteen terms: exact to < 1e-18 relative for
+// f2 < kLongF2 = 0.09 (node values within a factor 1.86 of each other), which
+// covers every pair of a tall atmospheric element without logarithms (a 3.75 km
+// layer of an isothermal 250 K atmosphere reaches f2 = 0.064).  Coefficients:
+// Q_k = 1/(2k+1); R = 1/Q by exact series inversion, correctly rounded.
+constexpr double kLongF2 = 0.09;
+// An element whose node values satisfy ((max-min)/(max+min))^2 below this bound
+// keeps every pair inside kLongF2 (margin for the rounding of f2).
+constexpr double kLongLogRange = 0.08;
+
+TAG_DEV double ln_series_R16(double f2) {
+  double r = -0.004746430692874202;
+  r = fma(r, f2, -0.005208475658374312);
+  r = fma(r, f2, -0.005756954446288888);
+  r = fma(r, f2, -0.006417063031397296);
+  r = fma(r, f2, -0.007224464737393906);
+  r = fma(r, f2, -0.008231206567350501);
+  r = fma(r, f2, -0.009516073194527899);
+  r = fma(r, f2, -0.011203745637718733);
+  r = fma(r, f2, -0.013502765051265932);
+  r = fma(r, f2, -0.016787551856334924);
+  r = fma(r, f2, -0.021796804019026242);
+  r = fma(r, f2, -0.030194003527336862);
+  r = fma(r, f2, -0.04656084656084656);
+  r = fma(r, f2, -0.08888888888888889);
+  r = fma(r, f2, -0.3333333333333333);
+  return fma(r, f2, 1.0);
+}
+TAG_DEV double ln_series_Q16(double f2) {
+  double r = 1.0 / 31.0;
+  r = fma(r, f2, 1.0 / 29.0);
+  r = fma(r, f2, 1.0 / 27.0);
+  r = fma(r, f2, 1.0 / 25.0);
+  r = fma(r, f2, 1.0 / 23.0);
+  r = fma(r, f2, 1.0 / 21.0);
+  r = fma(r, f2, 1.0 / 19.0);
+  r = fma(r, f2, 1.0 / 17.0);
+  r = fma(r, f2, 1.0 / 15.0);
+  r = fma(r, f2, 1.0 / 13.0);
+  r = fma(r, f2, 1.0 / 11.0);
+  r = fma(r, f2, 1.0 / 9.0);
+  r = fma(r, f2, 1.0 / 7.0);
+  r = fma(r, f2, 1.0 / 5.0);
+  r = fma(r, f2, 1.0 / 3.0);
+  return fma(r, f2, 1.0);
+}
+
+// Out-of-line branch of ln_mean_pair_halved for a pair with f2 at or above
+// the series range `lim` in either mean (elements flagged by needs_logs give
+// per-node logarithms Lxa = log(xa/2) ...; kLogsInline takes log(y/x)
+// here instead, for kernels whose elements rarely need them; differences of
+// logarithms do not see the halving).  One reciprocal serves both means:
+// rho_mean = nx/ex and inv_beta_mean = ny/ey.
+template <int kTerms, bool kLogsInline>
+static __device__ __noinline__ void ln_mean_pair_halved_log(double sx, double dx, double sy,
+                                                            double dy, double f2x, double f2y,
+                                                            double Lxa, double Lxb, double Lya,
+                                                            double Lyb, double& rho_mean,
+                                                            double& inv_beta_mean) {
+  constexpr double lim = kTerms == 16 ? kLongF2 : kSeriesF2;
+  const bool lx = f2x >= lim, ly = f2y >= lim;
+  const double Rx = kTerms == 16 ? ln_series_R16(f2x) : ln_series_R(f2x);
+  const double Qy = kTerms == 16 ? ln_series_Q16(f2y) : ln_series_Q(f2y);
+  const double nx = lx ? 2.0 * dx : sx * Rx;
+  const double ny = ly ? (kLogsInline ? log((sy + dy) / (sy - dy)) : Lyb - Lya) : Qy;
+  const double ex = lx ? (kLogsInline ? log((sx + dx) / (sx - dx)) : Lxb - Lxa) : 1.0;
+  const double ey = ly ? 2.0 * dy : sy;
+  const double r2 = 1.0 / (ex * ey);
+  rho_mean = nx * ey * r2;
+  inv_beta_mean = ny * ex * r2;
+}
+
+// ln_mean(x_a, x_b) and inv_ln_mean(y_a, y_b) from HALVED node values
+// (hx = x/2, hy = y/2, which saves the factors 1/2 and 2 of the series forms:
+// ln_mean = (hx_a + hx_b) R(f2x), inv_ln_mean = Q(f2y) / (hy_a + hy_b)), one
+// reciprocal per pair.  The number of series terms follows the pair's own f2
+// (four below kShortF2 when kShort, else kTerms = 8 below kSeriesF2 or 16
+// below kLongF2, logarithms beyond), so a pair's result does not depend on
+// which pairs share its warp; the branch tests compare the bit patterns of
+// the non-negative f2 on the integer pipe.  kShort pays where a warp's pairs
+// share one direction (the 3D kernel); in the 2D kernel a warp mixes
+// horizontal and vertical pairs, and the extra branch would diverge.
+template <bool kShort = true, int kTerms = 16, bool kLogsInline = false>
+TAG_DEV void ln_mean_pair_halved(double hxa, double hxb, double hya, double hyb, double Lxa,
+                                 double Lxb, double Lya, double Lyb, double& rho_mean,
+                                 double& inv_beta_mean) {
+  static_assert(kTerms == 8 || kTerms == 16, "eight or sixteen series terms");
+  constexpr double lim = kTerms == 16 ? kLongF2 : kSeriesF2;
+  const double sx = hxa + hxb, dx = hxb - hxa;
+  const double sy = hya + hyb, dy = hyb - hya;
+  const double r = 1.0 / (sx * sy);
+  const double isx = sy * r, isy = sx * r;
+  const double tx = dx * isx, ty = dy * isy;
+  const double f2x = tx * tx, f2y = ty * ty;
+  const long long fb = max(__double_as_longlong(f2x), __double_as_longlong(f2y));
+  if (kShort && fb < __double_as_longlong(kShortF2)) {
+    rho_mean = sx * fma(f2x, fma(f2x, fma(f2x, -44.0 / 945.0, -4.0 / 45.0), -1.0 / 3.0), 1.0);
+    inv_beta_mean = isy * fma(f2y, fma(f2y, fma(f2y, 1.0 / 7.0, 1.0 / 5.0), 1.0 / 3.0), 1.0);
+  } else if (fb < __double_as_longlong(lim)) {
+    rho_mean = sx * (kTerms == 16 ? ln_series_R16(f2x) : ln_series_R(f2x));
+    inv_beta_mean = isy * (kTerms == 16 ? ln_series_Q16(f2y) : ln_series_Q(f2y));
+  } else {
+    ln_mean_pair_halved_log<kTerms, kLogsInline>(sx, dx, sy, dy, f2x, f2y, Lxa, Lxb, Lya, Lyb,
+                                                 rho_mean, inv_beta_mean);
+  }
+}
+
 // One logarithmic mean (or its inverse) with its own reciprocal: the series of
 // ln_mean_pair in the common range, the reference's (y-x)/log(y/x) outside.
 TAG_DEV double ln_mean_single(double x, double y) {
@@ -143,9 +250,9 @@ TAG_DEV double inv_ln_mean_single(double x, double y) {
 
 // Whether the values of one element can push a node pair out of the series
 // range of ln_mean_pair.
-TAG_DEV bool needs_logs(double vmin, double vmax) {
+TAG_DEV bool needs_logs(double vmin, double vmax, double range = kLogMeanRange) {
   const double t = (vmax - vmin) / (vmax + vmin);
-  return t * t >= kLogMeanRange;
+  return t * t >= range;
 }
 
 // Face node (i, j) of face f (0 = xi-, 1 = xi+, 2 = eta-, 3 = eta+) at index l.

@@ -218,7 +218,11 @@ class P4estMeshCubedSphereTopography:
     ndims = 3
 
     def __init__(self, trees_per_face_dimension, layers, inner_radius, thickness, *, polydeg,
-                 initial_topography=None, adapt_vertical_grid=None):
+                 initial_topography=None, adapt_vertical_grid=None, geometry_on_device=False):
+        """geometry_on_device: build node coordinates and metric terms with
+        the library's kernel (tag_shell_geometry) instead of NumPy; the two
+        agree to rounding (1e-15 relative)."""
+        self.geometry_on_device = bool(geometry_on_device)
         self.initial_topography = initial_topography
         self.adapt_vertical_grid = adapt_vertical_grid or GalChen()
         self.nc = int(trees_per_face_dimension)
@@ -256,8 +260,58 @@ class P4estMeshCubedSphereTopography:
         out = out.transpose(0, 1, 2, 3, 4, 5, 6, 7).reshape(6, nc, nc, nz, n, n, n, 3)
         return np.ascontiguousarray(out.reshape(-1, n, n, n, 3))
 
+    def ground_heights(self, basis: LobattoLegendreBasis):
+        """Ground height of every column node [E, n(j), n(i)] (zero without a
+        topography): the topography function at the latitude and longitude the
+        reference takes for the node's column (cubed_sphere_mapping)."""
+        nc, nz, n = self.nc, self.nz, basis.n
+        E = self.nelements
+        if self.initial_topography is None:
+            return np.zeros((E, n, n))
+        nodes = basis.nodes
+        dx = 2.0 / nc
+        c = -1 + np.arange(nc) * dx + dx / 2
+        XI = c[None, :, None, None] + (dx / 2 * nodes)[None, None, None, :]   # [cy, cx, j, i]
+        ETA = c[:, None, None, None] + (dx / 2 * nodes)[None, None, :, None]
+        XI, ETA = np.broadcast_arrays(XI, ETA)
+        out = np.empty((6, nc, nc, nz, n, n))
+        for d in range(6):
+            x, y = np.tan(XI * np.pi / 4), np.tan(ETA * np.pi / 4)
+            one = np.ones_like(x)
+            cube = {1: (-y, -x, -one), 2: (one, x, y), 3: (-x, one, y), 4: (-one, -x, y),
+                    5: (x, -one, y), 6: (x, y, one)}[d + 1]
+            r = np.sqrt(1 + x * x + y * y)
+            ux, uy, uz = cube[0] / r, cube[1] / r, cube[2] / r
+            zs = self.initial_topography(np.arcsin(uz / r), np.arctan2(uy, ux))
+            out[d] = np.broadcast_to(zs[:, :, None], (nc, nc, nz, n, n))
+        return np.ascontiguousarray(out.reshape(E, n, n))
+
+    def geometry_device(self, basis: LobattoLegendreBasis):
+        """(node coordinates, contravariant vectors, inverse Jacobian) built by
+        the library's kernel, in the layouts of geometry()."""
+        import ctypes
+        from . import _lib
+        L = _lib.load()
+        n, E = basis.n, self.nelements
+        xyz = np.empty((E, n, n, n, 3))
+        Ja = np.empty((E, n, n, n, 3, 3))
+        invJ = np.empty((E, n, n, n))
+        dp = lambda a: a.ctypes.data_as(_lib._dp)  # noqa: E731
+        nodes = np.ascontiguousarray(basis.nodes, dtype=np.float64)
+        D = np.ascontiguousarray(basis.derivative_matrix, dtype=np.float64)
+        zs = None if self.initial_topography is None else self.ground_heights(basis)
+        vg = self.adapt_vertical_grid
+        sleve = isinstance(vg, Sleve)
+        _lib.check(L.tag_shell_geometry(
+            self.nc, self.nz, self.inner_radius, self.thickness, basis.polydeg, dp(nodes), dp(D),
+            dp(zs) if zs is not None else None, 1 if sleve else 0,
+            vg.eta_H if sleve else 0.0, vg.s if sleve else 0.0, dp(xyz), dp(Ja), dp(invJ)))
+        return xyz, Ja, invJ
+
     def geometry(self, basis: LobattoLegendreBasis):
         key = basis.polydeg
+        if key not in self._geom and self.geometry_on_device:
+            self._geom[key] = self.geometry_device(basis)
         if key not in self._geom:
             xyz = self.node_coordinates(basis)
             det, Ja = metric_terms_3d(xyz, basis.derivative_matrix)

@@ -586,13 +586,27 @@ class SemidiscretizationHyperbolic:
 
     def newton_solve(self, learned=False):
         """One Newton solve on every node of the resident state; returns
-        (stats dict, per-node update counts)."""
+        (stats dict, per-node update counts).  learned: False / 0 the warm
+        start, True / 1 the learned guess, 2 its closed-form branch alone."""
         iters = np.zeros(self.ndofs, dtype=np.int32)
         st = _lib.NewtonStats()
-        _lib.check(self._L.tag_newton_solve(self._h, int(bool(learned)), _ptr(iters, _ip),
+        _lib.check(self._L.tag_newton_solve(self._h, int(learned), _ptr(iters, _ip),
                                             ctypes.byref(st)))
         return ({"nodes": st.nodes, "updates": st.updates, "fallbacks": st.fallbacks,
                  "not_converged": st.not_converged}, iters)
+
+    def set_newton_start(self, start):
+        """Start of the stage limiter's Newton solve inside rk_steps: 0 the
+        warm start (the reference's), 1 the learned guess, 2 its closed-form
+        branch alone."""
+        _lib.check(self._L.tag_set_newton_start(self._h, int(start)))
+
+    def newton_counters(self, reset=True):
+        """The stage limiter's work summed over rk_steps calls: updates,
+        fallbacks, not_converged, node_solves."""
+        out = (ctypes.c_int64 * 4)()
+        _lib.check(self._L.tag_newton_counters(self._h, out, int(bool(reset))))
+        return dict(zip(("updates", "fallbacks", "not_converged", "node_solves"), list(out)))
 
     def status(self, clear=True):
         v = ctypes.c_uint32()
