@@ -324,9 +324,11 @@ int tag_set_newton(tag_handle h, int32_t mode, double tol, int32_t max_iteration
  * values of slots 7-9): 0 that warm start (default); 1 the learned guess (the
  * closed-form unsaturated equilibrium where it is valid, else the MLP set by
  * tag_set_mlp); 2 the closed-form branch alone, with the warm start on
- * saturated nodes.  A guessed start not converged after 8 updates falls back
+ * saturated nodes; 3 the closed-form branch, and on saturated nodes whichever
+ * of the MLP guess and the warm start has the smaller residual (needs
+ * tag_set_mlp).  A guessed start not converged after 8 updates falls back
  * to the warm start; with the canonical finish (tag_set_newton polish = 1) all
- * three starts give the same bits. */
+ * four starts give the same bits. */
 int tag_set_newton_start(tag_handle h, int32_t start);
 
 /* Newton work of the stage limiter summed over tag_rk_steps calls:
@@ -345,7 +347,9 @@ typedef struct {
 /* One Newton solve of the saturation system on every node of the resident
  * state (the stage limiter's work once, nonlinear_solve_dg2d.jl:6-44).
  * use_learned 1 starts from the learned guess, 2 from its closed-form branch
- * alone (the warm start on saturated nodes), and both fall back to the warm
+ * alone (the warm start on saturated nodes), 3 from the closed-form branch and
+ * on saturated nodes from the smaller-residual one of the MLP guess and the
+ * warm start; all three fall back to the warm
  * start (slots 7-9) when not converged after 8 updates; 0 starts warm.  The learned
  * guess is the closed-form unsaturated equilibrium T_unsat = (e_int - rho_m L)
  * / (c_vd rho_d + c_vv rho_m + c_l rho_r) where e_s(T_unsat)/(R_v T_unsat) >=
@@ -408,11 +412,14 @@ int tag_fp64_peak(double* flops_per_s);
 /* Diagnostics, no counterpart in the reference (whose ln_mean, inv_ln_mean
  * and stolarsky_mean come from Trixi, imported at src/TrixiAtmo.jl:37):
  * evaluates the device forms of those means on n host value pairs (x[q],
- * y[q]) in one kernel.  kind 0: the 2D kernels' pair form (eight-term series,
- * logarithms beyond f2 = 1e-2); 1: the same with per-node logarithms and the
- * four-term form below f2 = 1e-4; 2: the 3D energy kernel's halved form
- * (sixteen-term series up to f2 = 0.09); 3: the single means; 4: the
- * potential-temperature kernels' Stolarsky mean with gamma = cp / cv.
+ * y[q]) in one kernel.  kind 0: the 2D kernels' pair form (six-coefficient
+ * polynomials, logarithms beyond f2 = 1e-2); 1: the same with per-node
+ * logarithms and the four-term form below f2 = 1e-4; 2: the 3D energy
+ * kernel's halved form (polynomials up to f2 = 0.09); 3: the single means;
+ * 4: the potential-temperature kernels' Stolarsky mean with gamma = cp / cv;
+ * 5 and 6: the halved form of kind 2 with one mean's pair (x[q], y[q]) and
+ * the other's (1, 1), so that the two means take different forms
+ * (5: ln_mean of the pair in out1; 6: inv_ln_mean of the pair in out2).
  * out1 = ln_mean (kind 4: the Stolarsky mean), out2 = inv_ln_mean. */
 int tag_eval_means(int32_t kind, int64_t n, double cp, double cv, const double* x,
                    const double* y, double* out1, double* out2);

@@ -56,7 +56,12 @@ def test_shell_geometry_on_device_matches_host(tg, gpu_lib, topo):
     """tag_shell_geometry (node coordinates, curl-form contravariant vectors,
     inverse Jacobian of the cubed-sphere shell) against the host mirror's NumPy
     construction, on a perfect sphere and over a mountain spread by Gal-Chen
-    or Sleve vertical coordinates."""
+    or Sleve vertical coordinates.  Coordinates agree to 1e-13 of their
+    size.  The contravariant vectors and the inverse Jacobian agree to 1e-11:
+    the curl form differences products X_l grad X_m of size R^2 ~ 4e13 m^2
+    down to entries of size R times an element's width, and the device's fma
+    sums round differently from NumPy's matrix products, so the cancellation
+    amplifies the rounding by about R over the element's thickness (~1e3)."""
     def mountain(lat, lon):
         return 2000.0 * np.exp(-((lat - 0.5) ** 2 + (lon - 1.0) ** 2) / 0.05)
     kw = {}
@@ -68,6 +73,6 @@ def test_shell_geometry_on_device_matches_host(tg, gpu_lib, topo):
         host = tg.P4estMeshCubedSphereTopography(3, 2, 6.371e6, 30000.0, polydeg=N, **kw)
         dev = tg.P4estMeshCubedSphereTopography(3, 2, 6.371e6, 30000.0, polydeg=N,
                                                 geometry_on_device=True, **kw)
-        for a, b in zip(host.geometry(basis), dev.geometry(basis)):
+        for a, b, tol in zip(host.geometry(basis), dev.geometry(basis), (1e-13, 1e-11, 1e-11)):
             assert a.shape == b.shape
-            assert np.abs(a - b).max() <= 1e-13 * np.abs(a).max(), np.abs(a - b).max()
+            assert np.abs(a - b).max() <= tol * np.abs(a).max(), np.abs(a - b).max()

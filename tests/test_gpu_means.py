@@ -53,6 +53,22 @@ def test_device_log_means_against_exact(tg, gpu_lib, orc, kind, series_f2, node_
     assert rel(ln[short], o).max() <= 8 * EPS and rel(iln[short], oi).max() <= 8 * EPS
 
 
+@pytest.mark.parametrize("kind", [5, 6])
+def test_device_halved_means_take_separate_forms(tg, gpu_lib, kind):
+    """The 3D kernel's halved pair form chooses each mean's form from that
+    mean's own f2: with the other mean's pair equal (f2 = 0, the short form),
+    the swept mean still meets its bounds on both sides of every threshold."""
+    F, gamma = fixture()
+    x, y, f2 = F["x"], F["y"], F["f2"]
+    m, im = device(tg, kind, x, y, gamma)
+    got, other, ex = (m, im, F["ln_mean"]) if kind == 5 else (im, m, F["inv_ln_mean"])
+    series = f2 < 0.09
+    assert np.all(rel(got[series], ex[series]) <= 6 * EPS), rel(got[series], ex[series]).max()
+    bound = node_log_bound(x, y, True)
+    assert np.all(rel(got[~series], ex[~series]) <= bound[~series])
+    assert np.abs(other - 1.0).max() <= 2 * EPS
+
+
 def test_device_stolarsky_mean_against_exact(tg, gpu_lib):
     F, gamma = fixture()
     st, _ = device(tg, 4, F["x"], F["y"], gamma)

@@ -66,3 +66,35 @@ def test_oracle_means_against_exact(orc):
         above = (F["f2"] >= c) & (F["f2"] < 1.02 * c)
         assert rel(ln[below], F["ln_mean"][below]).max() <= 4 * EPS + 2 * EPS / (2 * math.sqrt(c))
         assert rel(ln[above], F["ln_mean"][above]).max() <= 4 * EPS + 2 * EPS / (2 * math.sqrt(c))
+
+
+def _device_polynomial(src, name):
+    """Coefficients c0, c1, ... of `TAG_DEV double name(double f2)` in
+    tag_common.cuh, written as Horner steps from the highest one down."""
+    import re
+    body = re.search(r"TAG_DEV double " + name + r"\(double f2\) \{(.*?)\n\}", src, re.S).group(1)
+    nums = [float(v) for v in re.findall(r"(-?\d+\.\d+(?:e-?\d+)?)", body)]
+    assert nums[-1] == 1.0  # the final fma(r, f2, 1.0)
+    return nums[:-1][::-1]
+
+
+def test_device_series_coefficients_are_the_economized_ones():
+    """The polynomial forms of R(f2) = z/atanh z and Q(f2) = atanh z / z in
+    csrc/tag_common.cuh are the Chebyshev economizations that
+    csrc/log_mean_series.py computes, and each is exact to well below an ulp
+    over its range (50-digit evaluation of the rounded coefficients)."""
+    import importlib.util
+    root = os.path.dirname(HERE)
+    csrc = os.path.join(root, "trixiatmo.jl_gb300", "csrc")
+    spec = importlib.util.spec_from_file_location("log_mean_series",
+                                                  os.path.join(csrc, "log_mean_series.py"))
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    with open(os.path.join(csrc, "tag_common.cuh")) as f:
+        src = f.read()
+    names = {("R", "0.09"): "ln_series_R_long", ("Q", "0.09"): "ln_series_Q_long",
+             ("R", "0.01"): "ln_series_R", ("Q", "0.01"): "ln_series_Q"}
+    for _, fun, F, m in gen.FORMS:
+        dev = _device_polynomial(src, names[(fun, F)])
+        assert dev == gen.coefficients(fun, F, m), (fun, F)
+        assert gen.max_rel_error(fun, F, dev, samples=400) < 4e-18

@@ -242,22 +242,9 @@ __global__ void k_element(typename Phys::Params Pp, const BasisDev basis, double
   if (Phys::kNodeLogs) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = (nthr + 31) >> 5;
     for (int el = warp; el < ne; el += nwarps) {
-      const double* eb = base + el * S::per_elem;
-      double r0 = 1e300, r1 = 0.0, b0 = 1e300, b1 = 0.0;
-      for (int node = lane; node < nn; node += 32) {
-        const double* q = eb + S::oQ + node * NQ;
-        r0 = fmin(r0, q[Phys::kRho]); r1 = fmax(r1, q[Phys::kRho]);
-        b0 = fmin(b0, q[Phys::kBeta]); b1 = fmax(b1, q[Phys::kBeta]);
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        r0 = fmin(r0, __shfl_xor_sync(0xffffffffu, r0, o));
-        r1 = fmax(r1, __shfl_xor_sync(0xffffffffu, r1, o));
-        b0 = fmin(b0, __shfl_xor_sync(0xffffffffu, b0, o));
-        b1 = fmax(b1, __shfl_xor_sync(0xffffffffu, b1, o));
-      }
-      if (lane == 0)
-        base[el * S::per_elem + S::oL] = (needs_logs(r0, r1) || needs_logs(b0, b1)) ? 1.0 : 0.0;
+      const bool logs = element_needs_logs(base + el * S::per_elem + S::oQ, nn, NQ, Phys::kRho,
+                                           Phys::kBeta, kLogMeanRange);
+      if (lane == 0) base[el * S::per_elem + S::oL] = logs ? 1.0 : 0.0;
     }
     __syncthreads();
   }
@@ -365,7 +352,7 @@ __global__ void k_element(typename Phys::Params Pp, const BasisDev basis, double
     const size_t gq = (size_t)e * nn + node;
     double dv = acc * (-invJ[gq]);
     if constexpr (Phys::kHasSources) dv += eb[S::oS + node * NA + v];
-    if (!isfinite(dv)) bad |= TAG_S_NAN;
+    if (not_finite(dv)) bad |= TAG_S_NAN;
     if (MODE == kModeRhs) {
       du[gq * NV + v] = dv;
     } else {

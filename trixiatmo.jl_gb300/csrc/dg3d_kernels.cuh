@@ -181,23 +181,9 @@ __global__ void k_element3d(typename Phys::Params Pp, const BasisDev basis, doub
   if (Phys::kNodeLogs) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = (nthr + 31) >> 5;
     for (int el = warp; el < ne; el += nwarps) {
-      const double* eb = base + el * S::per_elem;
-      double r0 = 1e300, r1 = 0.0, b0 = 1e300, b1 = 0.0;
-      for (int node = lane; node < nnn; node += 32) {
-        const double* q = eb + S::oQ + node * NQ;
-        r0 = fmin(r0, q[Phys::kRho]); r1 = fmax(r1, q[Phys::kRho]);
-        b0 = fmin(b0, q[Phys::kBeta]); b1 = fmax(b1, q[Phys::kBeta]);
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        r0 = fmin(r0, __shfl_xor_sync(0xffffffffu, r0, o));
-        r1 = fmax(r1, __shfl_xor_sync(0xffffffffu, r1, o));
-        b0 = fmin(b0, __shfl_xor_sync(0xffffffffu, b0, o));
-        b1 = fmax(b1, __shfl_xor_sync(0xffffffffu, b1, o));
-      }
-      if (lane == 0)
-        base[el * S::per_elem + S::oL] =
-            (needs_logs(r0, r1, Phys::kLogRange) || needs_logs(b0, b1, Phys::kLogRange)) ? 1.0 : 0.0;
+      const bool logs = element_needs_logs(base + el * S::per_elem + S::oQ, nnn, NQ, Phys::kRho,
+                                           Phys::kBeta, Phys::kLogRange);
+      if (lane == 0) base[el * S::per_elem + S::oL] = logs ? 1.0 : 0.0;
     }
     __syncthreads();
   }
@@ -272,7 +258,7 @@ __global__ void k_element3d(typename Phys::Params Pp, const BasisDev basis, doub
     if (k == n - 1) acc += se[((5 * n + j) * n + i) * NA + v] * sb->winvN;
     const size_t gq = (size_t)e * nnn + node;
     const double dv = acc * (-invJ[gq]) + Phys::source(Pp, eb + S::oU + node * NV, v);
-    if (!isfinite(dv)) bad |= TAG_S_NAN;
+    if (not_finite(dv)) bad |= TAG_S_NAN;
     if (MODE == kModeRhs) {
       du[gq * NV + v] = dv;
     } else {

@@ -71,8 +71,10 @@ struct NewtonArgs {
                      // to a fixed grid (0: stop at the criterion, as the reference does)
   int learned;       // start: 0 the warm start (slots 7-9, as the reference); 1 the closed-form
                      // unsaturated equilibrium where valid, else the MLP guess; 2 the closed
-                     // form where valid, else the warm start.  A guessed start that has not
-                     // converged after maxit_learned updates falls back to the warm start.
+                     // form where valid, else the warm start; 3 the closed form where valid,
+                     // else whichever of the MLP guess and the warm start has the smaller
+                     // residual.  A guessed start that has not converged after
+                     // maxit_learned updates falls back to the warm start.
   int maxit_learned; // 8
   double tol;
   const float* mlp;  // device parameters (kMlpParams floats) or null
@@ -122,6 +124,18 @@ TAG_DEV bool rainy_newton_done(const double* u, const double* r, int mode, doubl
   const double e_int = u[5] - 0.5 * (u[3] * u[3] + u[4] * u[4]) / rho;
   const double s2 = tol * 1.0e7 * fabs(u[1]);
   return fabs(r[0]) < tol * fabs(e_int) && fabs(r[1]) <= s2 && fabs(r[2]) <= s2;
+}
+
+// Size of a residual in the units of the stopping criterion: max |r| for
+// mode 0; for mode 1 each component over its own scale (|E_int| for the
+// energy, 1e7 rho_moist for the two mass rows), so that a size below tol is
+// convergence in both modes.
+TAG_DEV double rainy_residual_size(const double* u, const double* r, int mode) {
+  if (mode == 0) return fmax(fabs(r[0]), fmax(fabs(r[1]), fabs(r[2])));
+  const double rho = u[0] + u[1] + u[2];
+  const double e_int = u[5] - 0.5 * (u[3] * u[3] + u[4] * u[4]) / rho;
+  const double sm = 1.0e7 * fabs(u[1]);
+  return fmax(fabs(r[0]) / fabs(e_int), fmax(fabs(r[1]), fabs(r[2])) / sm);
 }
 
 // Snaps a converged iterate to a grid fixed by the node's state: vapour and
@@ -200,22 +214,24 @@ TAG_DEV bool rainy_closed_form_guess(const double* u, double* x, double& tu, dou
 // Learned start: the closed-form unsaturated equilibrium where it is valid,
 // else T_unsat plus the network's latent-heat offset, with vapour and cloud
 // from the saturation relation at that temperature.
-TAG_DEV void rainy_learned_guess(const float* __restrict__ P, const double* u, double* x) {
+// Returns true where the closed form was taken.
+TAG_DEV bool rainy_learned_guess(const float* __restrict__ P, const double* u, double* x) {
   using C = RainyConst;
   double e_int, tu;
-  if (rainy_closed_form_guess(u, x, tu, e_int)) return;
+  if (rainy_closed_form_guess(u, x, tu, e_int)) return true;
   float xin[kMlpIn];
   mlp_inputs(u, e_int, tu, xin);
   const double T = tu + fmax((double)mlp_forward(P, xin), 0.0);
   x[2] = T;
   x[0] = fmin(rainy_e_s(T) / (C::R_v * T), u[1]);
   x[1] = u[1] - x[0];
+  return false;
 }
 
 static __global__ void __launch_bounds__(256) k_newton_rainy(double* __restrict__ u, long nodes,
                                                       NewtonArgs a, unsigned* __restrict__ status) {
   __shared__ float sp[kMlpParams];
-  if (a.learned == 1 && a.mlp) {
+  if ((a.learned == 1 || a.learned == 3) && a.mlp) {
     for (int t = threadIdx.x; t < kMlpParams; t += blockDim.x) sp[t] = a.mlp[t];
     __syncthreads();
   }
@@ -234,6 +250,16 @@ static __global__ void __launch_bounds__(256) k_newton_rainy(double* __restrict_
   if (a.learned == 1 && a.mlp) {
     rainy_learned_guess(sp, s, xg);
     guessed = true;
+  } else if (a.learned == 3 && a.mlp) {
+    guessed = rainy_learned_guess(sp, s, xg);
+    if (!guessed) {
+      // saturated node: keep the MLP guess only where it starts closer
+      double rg[3], rw[3];
+      rainy_residual(s, xg, rg);
+      rainy_residual(s, x, rw);
+      const double sg = rainy_residual_size(s, rg, a.mode);
+      guessed = isfinite(sg) && sg < rainy_residual_size(s, rw, a.mode);
+    }
   } else if (a.learned == 2) {
     double tu, e_int;
     guessed = rainy_closed_form_guess(s, xg, tu, e_int);

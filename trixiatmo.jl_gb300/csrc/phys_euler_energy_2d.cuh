@@ -20,7 +20,7 @@ struct PhysEnergy2D {
   static constexpr bool kSurfaceNoncons = false;  // surface flux only (flux_zero)
 
   struct Params {
-    double gamma, gm1, inv_gm1, c_lmars, inv_2c, half_inv_gm1;
+    double gamma, gm1, inv_gm1, c_lmars, quarter_c, inv_c, half_inv_gm1;
   };
 
   static Params make_params(const double* p) {
@@ -30,27 +30,32 @@ struct PhysEnergy2D {
     q.gm1 = q.gamma - 1.0;
     q.inv_gm1 = 1.0 / (q.gamma - 1.0);
     q.c_lmars = p[3];
-    q.inv_2c = 0.5 / p[3];
+    q.quarter_c = 0.25 * p[3];
+    q.inv_c = 1.0 / p[3];
     q.half_inv_gm1 = 0.5 * q.inv_gm1;
     return q;
   }
 
   // cons2prim (:527-536), once per node:
   //   q = (rho/2, v1/2, v2/2, p/2, phi/2, beta/2 = rho/(2p)); flags bad states.
+  // One reciprocal: rho p = (gamma - 1)(rho E - |rho v|^2 / 2) needs no
+  // division, and r = 1/(rho^2 p) gives 1/(2 rho) = (rho p) r / 2 and
+  // rho/(2p) = rho^3 r / 2.
   TAG_DEV static void node_prims(const Params& P, const double* u, double* q, unsigned& bad) {
     const double rho = u[0];
-    const double irho = 1.0 / rho;
-    const double v1 = u[1] * irho, v2 = u[2] * irho;
-    const double p = P.gm1 * (u[3] - 0.5 * (u[1] * v1 + u[2] * v2));
+    const double m2 = fma(u[2], u[2], u[1] * u[1]);
+    const double rp = P.gm1 * fma(rho, u[3], -0.5 * m2);
+    const double r = 1.0 / (rho * rp);
+    const double hirho = 0.5 * (rp * r);
     q[0] = 0.5 * rho;
-    q[1] = 0.5 * v1;
-    q[2] = 0.5 * v2;
-    q[3] = 0.5 * p;
+    q[1] = u[1] * hirho;
+    q[2] = u[2] * hirho;
+    q[3] = rp * hirho;
     q[4] = 0.5 * u[4];
-    q[5] = 0.5 * rho / p;
+    q[5] = q[0] * rho * (rho * r);
     q[8] = 0.0;
-    if (!(rho > 0.0)) bad |= TAG_S_NEG_DENSITY;
-    if (!(p > 0.0)) bad |= TAG_S_NEG_PRESSURE;
+    if (not_positive(rho)) bad |= TAG_S_NEG_DENSITY;
+    if (not_positive(q[3])) bad |= TAG_S_NEG_PRESSURE;
   }
 
   // One symmetric pair of the volume integral: flux_ranocha (:366-395) plus half
@@ -66,8 +71,8 @@ struct PhysEnergy2D {
   TAG_DEV static void volume_pair(const Params& P, const double* qa, const double* qb,
                                   double n1, double n2, double* Fa, double* Fb) {
     double rho_mean, inv_rho_p_mean;
-    ln_mean_pair_halved<false, 8, true>(qa[0], qb[0], qa[5], qb[5], 0.0, 0.0, 0.0, 0.0,
-                                        rho_mean, inv_rho_p_mean);
+    ln_mean_pair_halved<false, false, true>(qa[0], qb[0], qa[5], qb[5], 0.0, 0.0, 0.0, 0.0,
+                                            rho_mean, inv_rho_p_mean);
     const double v1 = qa[1] + qb[1];
     const double v2 = qa[2] + qb[2];
     const double vn = fma(v2, n2, v1 * n1);  // 0.5 (vn_a + vn_b)
@@ -93,22 +98,26 @@ struct PhysEnergy2D {
     Fb[3] = fma(2.0, e, -hv);
   }
 
-  // FluxLMARS (:397-430) between states ul, ur for the (unnormalised) normal n.
+  // FluxLMARS (:397-430) between states ul, ur for the (unnormalised) normal n:
+  //   p = (p_ll + p_rr)/2 - c rho (v_rr - v_ll) / (2 |n|),
+  //   v = (v_ll + v_rr)/2 - (p_rr - p_ll) |n| / (2 c rho),  rho = (rho_ll + rho_rr)/2,
+  // with one reciprocal for 1/rho_ll, 1/rho_rr and 1/(rho_ll + rho_rr), one
+  // reciprocal square root for |n| and 1/|n|, and p = (gamma - 1)(rho e -
+  // |rho v|^2 / (2 rho)) (the FP64 pipe bounds the interface kernel too).
   TAG_DEV static void lmars(const Params& P, const double* ul, const double* ur, double n1,
                             double n2, double* F) {
     const double rho_ll = ul[0], rho_rr = ur[0];
-    const double irl = 1.0 / rho_ll, irr = 1.0 / rho_rr;  // one reciprocal per state
-    const double v1_ll = ul[1] * irl, v2_ll = ul[2] * irl;
-    const double v1_rr = ur[1] * irr, v2_rr = ur[2] * irr;
-    const double p_ll = P.gm1 * (ul[3] - 0.5 * (ul[1] * v1_ll + ul[2] * v2_ll));
-    const double p_rr = P.gm1 * (ur[3] - 0.5 * (ur[1] * v1_rr + ur[2] * v2_rr));
-    const double v_ll = v1_ll * n1 + v2_ll * n2;
-    const double v_rr = v1_rr * n1 + v2_rr * n2;
-    const double norm_ = sqrt(n1 * n1 + n2 * n2);
-    const double c = P.c_lmars;
-    const double rho = 0.5 * (rho_ll + rho_rr);
-    const double p = 0.5 * (p_ll + p_rr) - 0.5 * c * rho * (v_rr - v_ll) / norm_;
-    const double v = 0.5 * (v_ll + v_rr) - 1.0 / (2.0 * c * rho) * (p_rr - p_ll) * norm_;
+    const double srho = rho_ll + rho_rr, prho = rho_ll * rho_rr;
+    const double r = 1.0 / (prho * srho);
+    const double irl = (rho_rr * srho) * r, irr = (rho_ll * srho) * r, isum = prho * r;
+    const double p_ll = P.gm1 * fma(-0.5 * fma(ul[2], ul[2], ul[1] * ul[1]), irl, ul[3]);
+    const double p_rr = P.gm1 * fma(-0.5 * fma(ur[2], ur[2], ur[1] * ur[1]), irr, ur[3]);
+    const double v_ll = fma(ul[2], n2, ul[1] * n1) * irl;
+    const double v_rr = fma(ur[2], n2, ur[1] * n1) * irr;
+    const double nsq = fma(n2, n2, n1 * n1);
+    const double inorm = rsqrt(nsq), norm_ = nsq * inorm;
+    const double p = 0.5 * (p_ll + p_rr) - P.quarter_c * srho * (v_rr - v_ll) * inorm;
+    const double v = 0.5 * (v_ll + v_rr) - P.inv_c * (p_rr - p_ll) * norm_ * isum;
     if (v >= 0.0) {
       F[0] = ul[0] * v; F[1] = ul[1] * v; F[2] = ul[2] * v; F[3] = ul[3] * v + p_ll * v;
     } else {
@@ -141,8 +150,8 @@ struct PhysEnergy2D {
         F[0] = -F[0]; F[1] = -F[1]; F[2] = -F[2]; F[3] = -F[3];
       }
     } else {
-      const double nn = sqrt(n1 * n1 + n2 * n2);
-      const double nx = n1 / nn, ny = n2 / nn;
+      const double inn = rsqrt(fma(n2, n2, n1 * n1));
+      const double nx = n1 * inn, ny = n2 * inn;
       const double un = nx * ui[1] + ny * ui[2];
       const double ub[5] = {ui[0], ui[1] - 2.0 * un * nx, ui[2] - 2.0 * un * ny, ui[3], ui[4]};
       lmars(P, ui, ub, n1, n2, F);

@@ -23,7 +23,7 @@ struct PhysEnergy3D {
   static constexpr bool kHasSources = true;  // Coriolis, added per (node, variable)
 
   struct Params {
-    double gamma, gm1, inv_gm1, c_lmars, omega, half_inv_gm1;
+    double gamma, gm1, inv_gm1, c_lmars, quarter_c, inv_c, omega, half_inv_gm1;
   };
 
   static Params make_params(const double* p) {
@@ -33,24 +33,30 @@ struct PhysEnergy3D {
     q.inv_gm1 = 1.0 / (q.gamma - 1.0);
     q.half_inv_gm1 = 0.5 * q.inv_gm1;
     q.c_lmars = p[3];
+    q.quarter_c = 0.25 * p[3];
+    q.inv_c = 1.0 / p[3];
     q.omega = p[4];
     return q;
   }
 
+  // cons2prim (:568-578) once per node with one reciprocal: rho p =
+  // (gamma - 1)(rho E - |rho v|^2 / 2) needs no division, and r = 1/(rho^2 p)
+  // gives 1/(2 rho) = (rho p) r / 2 and rho/(2p) = rho^3 r / 2.
   TAG_DEV static void node_prims(const Params& P, const double* u, double* q, unsigned& bad) {
     const double rho = u[0];
-    const double irho = 1.0 / rho;
-    const double v1 = u[1] * irho, v2 = u[2] * irho, v3 = u[3] * irho;
-    const double p = P.gm1 * (u[4] - 0.5 * (u[1] * v1 + u[2] * v2 + u[3] * v3));
+    const double m2 = fma(u[3], u[3], fma(u[2], u[2], u[1] * u[1]));
+    const double rp = P.gm1 * fma(rho, u[4], -0.5 * m2);
+    const double r = 1.0 / (rho * rp);
+    const double hirho = 0.5 * (rp * r);
     q[0] = 0.5 * rho;
-    q[1] = 0.5 * v1;
-    q[2] = 0.5 * v2;
-    q[3] = 0.5 * v3;
-    q[4] = 0.5 * p;
+    q[1] = u[1] * hirho;
+    q[2] = u[2] * hirho;
+    q[3] = u[3] * hirho;
+    q[4] = rp * hirho;
     q[5] = 0.5 * u[5];
-    q[6] = 0.5 * rho / p;
-    if (!(rho > 0.0)) bad |= TAG_S_NEG_DENSITY;
-    if (!(p > 0.0)) bad |= TAG_S_NEG_PRESSURE;
+    q[6] = q[0] * rho * (rho * r);
+    if (not_positive(rho)) bad |= TAG_S_NEG_DENSITY;
+    if (not_positive(q[4])) bad |= TAG_S_NEG_PRESSURE;
   }
 
   // flux_ranocha (3D, :382-415) + half of flux_nonconservative_waruszewski_etal
@@ -92,21 +98,28 @@ struct PhysEnergy3D {
     Fb[4] = fma(2.0, e, -hv);
   }
 
-  // FluxLMARS (3D, :430-466)
+  // FluxLMARS (3D, :430-466) for the (unnormalised) normal n:
+  //   p = (p_ll + p_rr)/2 - c rho (v_rr - v_ll) / (2 |n|),
+  //   v = (v_ll + v_rr)/2 - (p_rr - p_ll) |n| / (2 c rho),  rho = (rho_ll + rho_rr)/2,
+  // with one reciprocal for 1/rho_ll, 1/rho_rr and 1/(rho_ll + rho_rr), one
+  // reciprocal square root for |n| and 1/|n|, and p = (gamma - 1)(rho e -
+  // |rho v|^2 / (2 rho)).
   TAG_DEV static void lmars(const Params& P, const double* ul, const double* ur, const double* n,
                             double* F) {
-    const double irl = 1.0 / ul[0], irr = 1.0 / ur[0];
-    const double v1l = ul[1] * irl, v2l = ul[2] * irl, v3l = ul[3] * irl;
-    const double v1r = ur[1] * irr, v2r = ur[2] * irr, v3r = ur[3] * irr;
-    const double pl = P.gm1 * (ul[4] - 0.5 * (ul[1] * v1l + ul[2] * v2l + ul[3] * v3l));
-    const double pr = P.gm1 * (ur[4] - 0.5 * (ur[1] * v1r + ur[2] * v2r + ur[3] * v3r));
-    const double vl = v1l * n[0] + v2l * n[1] + v3l * n[2];
-    const double vr = v1r * n[0] + v2r * n[1] + v3r * n[2];
-    const double norm_ = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-    const double c = P.c_lmars;
-    const double rho = 0.5 * (ul[0] + ur[0]);
-    const double p = 0.5 * (pl + pr) - 0.5 * c * rho * (vr - vl) / norm_;
-    const double v = 0.5 * (vl + vr) - 1.0 / (2.0 * c * rho) * (pr - pl) * norm_;
+    const double rho_ll = ul[0], rho_rr = ur[0];
+    const double srho = rho_ll + rho_rr, prho = rho_ll * rho_rr;
+    const double r = 1.0 / (prho * srho);
+    const double irl = (rho_rr * srho) * r, irr = (rho_ll * srho) * r, isum = prho * r;
+    const double ml = fma(ul[3], ul[3], fma(ul[2], ul[2], ul[1] * ul[1]));
+    const double mr = fma(ur[3], ur[3], fma(ur[2], ur[2], ur[1] * ur[1]));
+    const double pl = P.gm1 * fma(-0.5 * ml, irl, ul[4]);
+    const double pr = P.gm1 * fma(-0.5 * mr, irr, ur[4]);
+    const double vl = fma(ul[3], n[2], fma(ul[2], n[1], ul[1] * n[0])) * irl;
+    const double vr = fma(ur[3], n[2], fma(ur[2], n[1], ur[1] * n[0])) * irr;
+    const double nsq = fma(n[2], n[2], fma(n[1], n[1], n[0] * n[0]));
+    const double inorm = rsqrt(nsq), norm_ = nsq * inorm;
+    const double p = 0.5 * (pl + pr) - P.quarter_c * srho * (vr - vl) * inorm;
+    const double v = 0.5 * (vl + vr) - P.inv_c * (pr - pl) * norm_ * isum;
     const double* us = v >= 0.0 ? ul : ur;
     const double ps = v >= 0.0 ? pl : pr;
     F[0] = v * us[0];
@@ -123,8 +136,8 @@ struct PhysEnergy3D {
 
   // boundary_condition_slip_wall (3D), :93-116, with the outward normal n.
   TAG_DEV static void boundary_flux(const Params& P, const double* ui, const double* n, double* F) {
-    const double nn = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-    const double e0 = n[0] / nn, e1 = n[1] / nn, e2 = n[2] / nn;
+    const double inn = rsqrt(fma(n[2], n[2], fma(n[1], n[1], n[0] * n[0])));
+    const double e0 = n[0] * inn, e1 = n[1] * inn, e2 = n[2] * inn;
     const double un = e0 * ui[1] + e1 * ui[2] + e2 * ui[3];
     const double ub[6] = {ui[0], ui[1] - 2.0 * un * e0, ui[2] - 2.0 * un * e1,
                           ui[3] - 2.0 * un * e2, ui[4], ui[5]};
@@ -142,7 +155,7 @@ struct PhysEnergy3D {
     const double irho = 1.0 / u[0];
     const double v1 = u[1] * irho, v2 = u[2] * irho, v3 = u[3] * irho;
     const double p = P.gm1 * (u[4] - 0.5 * (u[1] * v1 + u[2] * v2 + u[3] * v3));
-    const double c = sqrt(P.gamma * p / u[0]);
+    const double c = sqrt(P.gamma * p * irho);
     l[0] = fabs(v1) + c;
     l[1] = fabs(v2) + c;
     l[2] = fabs(v3) + c;

@@ -1380,8 +1380,8 @@ int tag_set_newton(tag_handle h, int32_t mode, double tol, int32_t max_iteration
 
 int tag_set_newton_start(tag_handle h, int32_t start) {
   if (!h || !h->has_limiter) return fail(TAG_E_INVALID, "not a rainy handle");
-  if (start < 0 || start > 2) return fail(TAG_E_INVALID, "start must be 0, 1 or 2");
-  if (start == 1 && !h->d_mlp) return fail(TAG_E_INVALID, "no MLP parameters set");
+  if (start < 0 || start > 3) return fail(TAG_E_INVALID, "start must be 0, 1, 2 or 3");
+  if ((start == 1 || start == 3) && !h->d_mlp) return fail(TAG_E_INVALID, "no MLP parameters set");
   h->newton_start = start;
   h->graph_epb = -2;  // the limiter's arguments are baked into the captured graph
   return TAG_OK;
@@ -1415,9 +1415,10 @@ int tag_set_mlp(tag_handle h, const float* params) {
 
 int tag_newton_solve(tag_handle h, int32_t use_learned, int32_t* iters, tag_newton_stats* stats) {
   if (!h || !h->has_limiter) return fail(TAG_E_INVALID, "not a rainy handle");
-  if (use_learned < 0 || use_learned > 2) return fail(TAG_E_INVALID, "start must be 0, 1 or 2");
+  if (use_learned < 0 || use_learned > 3) return fail(TAG_E_INVALID, "start must be 0, 1, 2 or 3");
   NvtxRange r_solve("nonlinear system solver");
-  if (use_learned == 1 && !h->d_mlp) return fail(TAG_E_INVALID, "no MLP parameters set");
+  if ((use_learned == 1 || use_learned == 3) && !h->d_mlp)
+    return fail(TAG_E_INVALID, "no MLP parameters set");
   const long nodes = (long)h->nodes;
   NewtonArgs a = h->newton;
   a.learned = use_learned;

@@ -39,34 +39,83 @@ TAG_DEV double inv_ln_mean(double x, double y) {
 // logarithm in the common case.  With f2 = ((y-x)/(y+x))^2 and z = sqrt(f2):
 //   ln_mean(x, y)     = (x+y)/2 * z/atanh(z) = (x+y)/2 * R(f2)
 //   inv_ln_mean(x, y) = 2/(x+y) * atanh(z)/z = 2/(x+y) * Q(f2)
-// Q(f2) = sum_k f2^k/(2k+1); R = 1/Q, its Taylor coefficients derived exactly
-// from that definition.  Eight terms each are exact to ~1e-18 relative for
-// f2 < 0.01, so they agree with the reference's definition (4-term form below
-// f2 = 1e-4, (y-x)/log(y/x) above) to rounding.  For f2 >= 0.01 the exact
-// logarithmic form is used.
+// Q(f2) = sum_k f2^k/(2k+1) and R = 1/Q.  Below kShortF2 the four-term Taylor
+// forms are exact to < 2e-17 relative.  On the wider ranges [0, F] R and Q are
+// polynomials 1 + f2 (c0 + f2 (c1 + ...)), Chebyshev economizations of their
+// Taylor series (C. Lanczos, J. Math. Phys. 17 (1938) 123-199; coefficients
+// made and checked by csrc/log_mean_series.py): six coefficients each for
+// F = kSeriesF2 = 0.01 (exact to < 5e-19 relative), nine (R) and ten (Q) for
+// F = kLongF2 = 0.09 (< 4e-18).  So they agree with the reference's definition
+// (a 4-term series below f2 = 1e-4, (y-x)/log(y/x) above) to rounding.
 //   rho_mean = ln_mean(xa, xb), inv_beta_mean = inv_ln_mean(ya, yb).
-// For f2 >= 0.01 the logarithmic form (y - x)/log(y/x) is evaluated with the
-// per-node logarithms Lx = log x, Ly = log y (log(y/x) = Ly - Lx; with
-// |y/x - 1| > 0.2 there the difference is accurate to ~1e-14 relative).  The
-// caller guarantees the logarithms are valid whenever a pair can leave the
-// series range (see kLogMeanRange).
+// Beyond the series range the logarithmic form (y - x)/log(y/x) is evaluated,
+// from per-node logarithms Lx = log x, Ly = log y where the caller supplies
+// them (log(y/x) = Ly - Lx; with |y/x - 1| > 0.2 there the difference is
+// accurate to ~1e-14 relative).  Such a caller guarantees the logarithms are
+// valid whenever a pair can leave the series range (see kLogMeanRange).
+constexpr double kShortF2 = 1.0e-4;
 constexpr double kSeriesF2 = 1.0e-2;
 // An element whose node values x satisfy ((max-min)/(max+min))^2 below this
 // bound never leaves the series range (margin for rounding of f2).
 constexpr double kLogMeanRange = 0.9e-2;
+constexpr double kLongF2 = 0.09;
+// The same bound for kLongF2: a 3.75 km layer of an isothermal 250 K
+// atmosphere reaches f2 = 0.064, so tall shell elements stay in range.
+constexpr double kLongLogRange = 0.08;
 
-// The eight-term series R(f2) and Q(f2) described above
+TAG_DEV double ln_short_R(double f2) {
+  return fma(f2, fma(f2, fma(f2, -44.0 / 945.0, -4.0 / 45.0), -1.0 / 3.0), 1.0);
+}
+TAG_DEV double ln_short_Q(double f2) {
+  return fma(f2, fma(f2, fma(f2, 1.0 / 7.0, 1.0 / 5.0), 1.0 / 3.0), 1.0);
+}
+
+// R and Q on [0, kSeriesF2]
 TAG_DEV double ln_series_R(double f2) {
-  return 1.0 + f2 * (-1.0 / 3.0 + f2 * (-4.0 / 45.0 + f2 * (-44.0 / 945.0 +
-         f2 * (-428.0 / 14175.0 + f2 * (-10196.0 / 467775.0 +
-         f2 * (-10719068.0 / 638512875.0 + f2 * (-25865068.0 / 1915538625.0)))))));
+  double r = -0.01719901874634888;
+  r = fma(r, f2, -0.021792151641765893);
+  r = fma(r, f2, -0.030194027707754922);
+  r = fma(r, f2, -0.0465608465041037);
+  r = fma(r, f2, -0.08888888888893755);
+  r = fma(r, f2, -0.3333333333333333);
+  return fma(r, f2, 1.0);
 }
 TAG_DEV double ln_series_Q(double f2) {
-  return 1.0 + f2 * (1.0 / 3.0 + f2 * (1.0 / 5.0 + f2 * (1.0 / 7.0 +
-         f2 * (1.0 / 9.0 + f2 * (1.0 / 11.0 + f2 * (1.0 / 13.0 + f2 * (1.0 / 15.0)))))));
+  double r = 0.07895661799581076;
+  r = fma(r, f2, 0.09088609072099012);
+  r = fma(r, f2, 0.11111123067087354);
+  r = fma(r, f2, 0.14285714257655663);
+  r = fma(r, f2, 0.20000000000024065);
+  r = fma(r, f2, 0.3333333333333333);
+  return fma(r, f2, 1.0);
 }
-// Below kShortF2 the first four terms are exact to < 2e-17 relative.
-constexpr double kShortF2 = 1.0e-4;
+
+// R and Q on [0, kLongF2]
+TAG_DEV double ln_series_R_long(double f2) {
+  double r = -0.013669329626825622;
+  r = fma(r, f2, -0.01045355622562932);
+  r = fma(r, f2, -0.013573328231670736);
+  r = fma(r, f2, -0.016783737201999518);
+  r = fma(r, f2, -0.02179692429315078);
+  r = fma(r, f2, -0.030194001406289393);
+  r = fma(r, f2, -0.04656084657952881);
+  r = fma(r, f2, -0.08888888888882568);
+  r = fma(r, f2, -0.33333333333333337);
+  return fma(r, f2, 1.0);
+}
+TAG_DEV double ln_series_Q_long(double f2) {
+  double r = 0.07283496074780077;
+  r = fma(r, f2, 0.047418568133941144);
+  r = fma(r, f2, 0.05939688448611953);
+  r = fma(r, f2, 0.06662915697122629);
+  r = fma(r, f2, 0.07692458351815545);
+  r = fma(r, f2, 0.09090905424531916);
+  r = fma(r, f2, 0.11111111162196165);
+  r = fma(r, f2, 0.14285714285353665);
+  r = fma(r, f2, 0.20000000000000986);
+  r = fma(r, f2, 0.3333333333333333);
+  return fma(r, f2, 1.0);
+}
 
 // The rare branch, kept out of line so that the common path is not predicated
 // with its extra reciprocal; the series are evaluated only for a mean that is
@@ -103,8 +152,8 @@ TAG_DEV void ln_mean_pair(double xa, double xb, double ya, double yb, double Lxa
   const double fm = fmax(f2x, f2y);
   if (kShort && fm < kShortF2) {
     // nearly equal values (e.g. horizontal pairs of a smooth atmosphere)
-    rho_mean = 0.5 * sx * (1.0 + f2x * (-1.0 / 3.0 + f2x * (-4.0 / 45.0 + f2x * (-44.0 / 945.0))));
-    inv_beta_mean = 2.0 * isy * (1.0 + f2y * (1.0 / 3.0 + f2y * (1.0 / 5.0 + f2y * (1.0 / 7.0))));
+    rho_mean = 0.5 * sx * ln_short_R(f2x);
+    inv_beta_mean = 2.0 * isy * ln_short_Q(f2y);
   } else if (fm < kSeriesF2) {
     rho_mean = 0.5 * sx * ln_series_R(f2x);
     inv_beta_mean = 2.0 * isy * ln_series_Q(f2y);
@@ -116,69 +165,22 @@ TAG_DEV void ln_mean_pair(double xa, double xb, double ya, double yb, double Lxa
   }
 }
 
-// The same series R and Q to sixteen terms: exact to < 1e-18 relative for
-// f2 < kLongF2 = 0.09 (node values within a factor 1.86 of each other), which
-// covers every pair of a tall atmospheric element without logarithms (a 3.75 km
-// layer of an isothermal 250 K atmosphere reaches f2 = 0.064).  Coefficients:
-// Q_k = 1/(2k+1); R = 1/Q by exact series inversion, correctly rounded.
-constexpr double kLongF2 = 0.09;
-// An element whose node values satisfy ((max-min)/(max+min))^2 below this bound
-// keeps every pair inside kLongF2 (margin for the rounding of f2).
-constexpr double kLongLogRange = 0.08;
-
-TAG_DEV double ln_series_R16(double f2) {
-  double r = -0.004746430692874202;
-  r = fma(r, f2, -0.005208475658374312);
-  r = fma(r, f2, -0.005756954446288888);
-  r = fma(r, f2, -0.006417063031397296);
-  r = fma(r, f2, -0.007224464737393906);
-  r = fma(r, f2, -0.008231206567350501);
-  r = fma(r, f2, -0.009516073194527899);
-  r = fma(r, f2, -0.011203745637718733);
-  r = fma(r, f2, -0.013502765051265932);
-  r = fma(r, f2, -0.016787551856334924);
-  r = fma(r, f2, -0.021796804019026242);
-  r = fma(r, f2, -0.030194003527336862);
-  r = fma(r, f2, -0.04656084656084656);
-  r = fma(r, f2, -0.08888888888888889);
-  r = fma(r, f2, -0.3333333333333333);
-  return fma(r, f2, 1.0);
-}
-TAG_DEV double ln_series_Q16(double f2) {
-  double r = 1.0 / 31.0;
-  r = fma(r, f2, 1.0 / 29.0);
-  r = fma(r, f2, 1.0 / 27.0);
-  r = fma(r, f2, 1.0 / 25.0);
-  r = fma(r, f2, 1.0 / 23.0);
-  r = fma(r, f2, 1.0 / 21.0);
-  r = fma(r, f2, 1.0 / 19.0);
-  r = fma(r, f2, 1.0 / 17.0);
-  r = fma(r, f2, 1.0 / 15.0);
-  r = fma(r, f2, 1.0 / 13.0);
-  r = fma(r, f2, 1.0 / 11.0);
-  r = fma(r, f2, 1.0 / 9.0);
-  r = fma(r, f2, 1.0 / 7.0);
-  r = fma(r, f2, 1.0 / 5.0);
-  r = fma(r, f2, 1.0 / 3.0);
-  return fma(r, f2, 1.0);
-}
-
 // Out-of-line branch of ln_mean_pair_halved for a pair with f2 at or above
-// the series range `lim` in either mean (elements flagged by needs_logs give
-// per-node logarithms Lxa = log(xa/2) ...; kLogsInline takes log(y/x)
-// here instead, for kernels whose elements rarely need them; differences of
-// logarithms do not see the halving).  One reciprocal serves both means:
-// rho_mean = nx/ex and inv_beta_mean = ny/ey.
-template <int kTerms, bool kLogsInline>
+// the series range lim (kLongF2 or kSeriesF2) in either mean (elements
+// flagged by needs_logs give per-node logarithms Lxa = log(xa/2) ...;
+// kLogsInline takes log(y/x) here instead, for kernels whose elements rarely
+// need them; differences of logarithms do not see the halving).  One
+// reciprocal serves both means: rho_mean = nx/ex and inv_beta_mean = ny/ey.
+template <bool kLong, bool kLogsInline>
 static __device__ __noinline__ void ln_mean_pair_halved_log(double sx, double dx, double sy,
                                                             double dy, double f2x, double f2y,
                                                             double Lxa, double Lxb, double Lya,
                                                             double Lyb, double& rho_mean,
                                                             double& inv_beta_mean) {
-  constexpr double lim = kTerms == 16 ? kLongF2 : kSeriesF2;
+  constexpr double lim = kLong ? kLongF2 : kSeriesF2;
   const bool lx = f2x >= lim, ly = f2y >= lim;
-  const double Rx = kTerms == 16 ? ln_series_R16(f2x) : ln_series_R(f2x);
-  const double Qy = kTerms == 16 ? ln_series_Q16(f2y) : ln_series_Q(f2y);
+  const double Rx = kLong ? ln_series_R_long(f2x) : ln_series_R(f2x);
+  const double Qy = kLong ? ln_series_Q_long(f2y) : ln_series_Q(f2y);
   const double nx = lx ? 2.0 * dx : sx * Rx;
   const double ny = ly ? (kLogsInline ? log((sy + dy) / (sy - dy)) : Lyb - Lya) : Qy;
   const double ex = lx ? (kLogsInline ? log((sx + dx) / (sx - dx)) : Lxb - Lxa) : 1.0;
@@ -191,36 +193,44 @@ static __device__ __noinline__ void ln_mean_pair_halved_log(double sx, double dx
 // ln_mean(x_a, x_b) and inv_ln_mean(y_a, y_b) from HALVED node values
 // (hx = x/2, hy = y/2, which saves the factors 1/2 and 2 of the series forms:
 // ln_mean = (hx_a + hx_b) R(f2x), inv_ln_mean = Q(f2y) / (hy_a + hy_b)), one
-// reciprocal per pair.  The number of series terms follows the pair's own f2
-// (four below kShortF2 when kShort, else kTerms = 8 below kSeriesF2 or 16
-// below kLongF2, logarithms beyond), so a pair's result does not depend on
-// which pairs share its warp; the branch tests compare the bit patterns of
-// the non-negative f2 on the integer pipe.  kShort pays where a warp's pairs
-// share one direction (the 3D kernel); in the 2D kernel a warp mixes
-// horizontal and vertical pairs, and the extra branch would diverge.
-template <bool kShort = true, int kTerms = 16, bool kLogsInline = false>
+// reciprocal per pair.  Each mean takes the form its own f2 selects: the
+// four-term series below kShortF2 (when kShort), else the polynomial on
+// [0, kLongF2] (kLong) or [0, kSeriesF2]; logarithms for both once either f2
+// is beyond that range.  So a pair's result does not depend on which pairs
+// share its warp, and in a tall element's vertical lines, where the density
+// varies and the temperature hardly does, inv_ln_mean keeps its short form.
+// The branch tests compare the bit patterns of the non-negative f2 on the
+// integer pipe.  kShort pays where a warp's pairs share one direction (the 3D
+// kernel); in the 2D kernel a warp mixes horizontal and vertical pairs, and
+// the extra branches would diverge.
+template <bool kShort = true, bool kLong = true, bool kLogsInline = false>
 TAG_DEV void ln_mean_pair_halved(double hxa, double hxb, double hya, double hyb, double Lxa,
                                  double Lxb, double Lya, double Lyb, double& rho_mean,
                                  double& inv_beta_mean) {
-  static_assert(kTerms == 8 || kTerms == 16, "eight or sixteen series terms");
-  constexpr double lim = kTerms == 16 ? kLongF2 : kSeriesF2;
+  constexpr double lim = kLong ? kLongF2 : kSeriesF2;
   const double sx = hxa + hxb, dx = hxb - hxa;
   const double sy = hya + hyb, dy = hyb - hya;
   const double r = 1.0 / (sx * sy);
   const double isx = sy * r, isy = sx * r;
   const double tx = dx * isx, ty = dy * isy;
   const double f2x = tx * tx, f2y = ty * ty;
-  const long long fb = max(__double_as_longlong(f2x), __double_as_longlong(f2y));
-  if (kShort && fb < __double_as_longlong(kShortF2)) {
-    rho_mean = sx * fma(f2x, fma(f2x, fma(f2x, -44.0 / 945.0, -4.0 / 45.0), -1.0 / 3.0), 1.0);
-    inv_beta_mean = isy * fma(f2y, fma(f2y, fma(f2y, 1.0 / 7.0, 1.0 / 5.0), 1.0 / 3.0), 1.0);
-  } else if (fb < __double_as_longlong(lim)) {
-    rho_mean = sx * (kTerms == 16 ? ln_series_R16(f2x) : ln_series_R(f2x));
-    inv_beta_mean = isy * (kTerms == 16 ? ln_series_Q16(f2y) : ln_series_Q(f2y));
-  } else {
-    ln_mean_pair_halved_log<kTerms, kLogsInline>(sx, dx, sy, dy, f2x, f2y, Lxa, Lxb, Lya, Lyb,
-                                                 rho_mean, inv_beta_mean);
+  const long long bx = __double_as_longlong(f2x), by = __double_as_longlong(f2y);
+  if (max(bx, by) >= __double_as_longlong(lim)) {
+    ln_mean_pair_halved_log<kLong, kLogsInline>(sx, dx, sy, dy, f2x, f2y, Lxa, Lxb, Lya, Lyb,
+                                                rho_mean, inv_beta_mean);
+    return;
   }
+  double R, Q;
+  if (kShort && bx < __double_as_longlong(kShortF2))
+    R = ln_short_R(f2x);
+  else
+    R = kLong ? ln_series_R_long(f2x) : ln_series_R(f2x);
+  if (kShort && by < __double_as_longlong(kShortF2))
+    Q = ln_short_Q(f2y);
+  else
+    Q = kLong ? ln_series_Q_long(f2y) : ln_series_Q(f2y);
+  rho_mean = sx * R;
+  inv_beta_mean = isy * Q;
 }
 
 // One logarithmic mean (or its inverse) with its own reciprocal: the series of
@@ -228,24 +238,26 @@ TAG_DEV void ln_mean_pair_halved(double hxa, double hxb, double hya, double hyb,
 TAG_DEV double ln_mean_single(double x, double y) {
   const double s = x + y, d = y - x;
   const double t = d / s, f2 = t * t;
-  if (f2 < kSeriesF2) {
-    const double R = 1.0 + f2 * (-1.0 / 3.0 + f2 * (-4.0 / 45.0 + f2 * (-44.0 / 945.0 +
-                     f2 * (-428.0 / 14175.0 + f2 * (-10196.0 / 467775.0 +
-                     f2 * (-10719068.0 / 638512875.0 + f2 * (-25865068.0 / 1915538625.0)))))));
-    return 0.5 * s * R;
-  }
+  if (f2 < kSeriesF2) return 0.5 * s * ln_series_R(f2);
   return d / log(y / x);
 }
 
 TAG_DEV double inv_ln_mean_single(double x, double y) {
   const double s = x + y, d = y - x;
   const double t = d / s, f2 = t * t;
-  if (f2 < kSeriesF2) {
-    const double Q = 1.0 + f2 * (1.0 / 3.0 + f2 * (1.0 / 5.0 + f2 * (1.0 / 7.0 +
-                     f2 * (1.0 / 9.0 + f2 * (1.0 / 11.0 + f2 * (1.0 / 13.0 + f2 * (1.0 / 15.0)))))));
-    return 2.0 * Q / s;
-  }
+  if (f2 < kSeriesF2) return 2.0 * ln_series_Q(f2) / s;
   return log(y / x) / d;
+}
+
+// !(x > 0.0) and !isfinite(x) on the integer pipe (the FP64 pipe is the
+// element kernels' bottleneck): IEEE bit patterns of positive doubles order
+// like their values, and an exponent field of all ones is an infinity or NaN.
+TAG_DEV bool not_positive(double x) {
+  return (unsigned long long)__double_as_longlong(x) - 1ull >= 0x7ff0000000000000ull;
+}
+TAG_DEV bool not_finite(double x) {
+  return ((unsigned long long)__double_as_longlong(x) & 0x7ff0000000000000ull) ==
+         0x7ff0000000000000ull;
 }
 
 // Whether the values of one element can push a node pair out of the series
@@ -253,6 +265,33 @@ TAG_DEV double inv_ln_mean_single(double x, double y) {
 TAG_DEV bool needs_logs(double vmin, double vmax, double range = kLogMeanRange) {
   const double t = (vmax - vmin) / (vmax + vmin);
   return t * t >= range;
+}
+
+// needs_logs for the two positive node fields q[node * stride + ka] and
+// q[node * stride + kb] of one element, evaluated by one whole warp; the
+// minima and maxima are taken on the integer pipe (the bit patterns of
+// positive doubles order like their values).  Valid in every lane.
+TAG_DEV bool element_needs_logs(const double* q, int nodes, int stride, int ka, int kb,
+                                double range) {
+  const int lane = threadIdx.x & 31;
+  long long a0 = 0x7fefffffffffffffll, a1 = 0, b0 = 0x7fefffffffffffffll, b1 = 0;
+  for (int node = lane; node < nodes; node += 32) {
+    const long long x = __double_as_longlong(q[node * stride + ka]);
+    const long long y = __double_as_longlong(q[node * stride + kb]);
+    a0 = min(a0, x);
+    a1 = max(a1, x);
+    b0 = min(b0, y);
+    b1 = max(b1, y);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a0 = min(a0, __shfl_xor_sync(0xffffffffu, a0, o));
+    a1 = max(a1, __shfl_xor_sync(0xffffffffu, a1, o));
+    b0 = min(b0, __shfl_xor_sync(0xffffffffu, b0, o));
+    b1 = max(b1, __shfl_xor_sync(0xffffffffu, b1, o));
+  }
+  return needs_logs(__longlong_as_double(a0), __longlong_as_double(a1), range) ||
+         needs_logs(__longlong_as_double(b0), __longlong_as_double(b1), range);
 }
 
 // Face node (i, j) of face f (0 = xi-, 1 = xi+, 2 = eta-, 3 = eta+) at index l.

@@ -19,12 +19,15 @@ int mfail(int code, const std::string& msg) {
   return code;
 }
 
-// kind 0: ln_mean_pair (2D kernels: eight-term series, logarithms inline)
+// kind 0: ln_mean_pair (2D kernels: six-coefficient polynomials, logarithms inline)
 // kind 1: ln_mean_pair with per-node logarithms and the four-term short form
 // kind 2: ln_mean_pair_halved (3D energy kernel; halved inputs)
 // kind 3: ln_mean_single / inv_ln_mean_single
 // kind 4: Stolarsky mean of the potential-temperature kernels (out2 unused)
-// out1 = ln_mean(x, y) (kind 4: the Stolarsky mean), out2 = inv_ln_mean(x, y).
+// kind 5: ln_mean_pair_halved with the pair as the ln_mean pair and (1, 1) as
+//         the inv_ln_mean pair; kind 6 the other way round
+// out1 = ln_mean(x, y) (kind 4: the Stolarsky mean), out2 = inv_ln_mean(x, y);
+// kinds 5 and 6 return the means of their (x, y) and (1, 1) pairs.
 __global__ void k_eval_means(int kind, long n, const double* __restrict__ x,
                              const double* __restrict__ y, PhysPT2D::Params pt,
                              double* __restrict__ out1, double* __restrict__ out2) {
@@ -41,6 +44,13 @@ __global__ void k_eval_means(int kind, long n, const double* __restrict__ x,
     const double ha = 0.5 * a, hb = 0.5 * b;
     const double la = log(ha), lb = log(hb);
     ln_mean_pair_halved(ha, hb, ha, hb, la, lb, la, lb, m, im);
+  } else if (kind == 5 || kind == 6) {
+    const double ha = 0.5 * a, hb = 0.5 * b;
+    const double la = log(ha), lb = log(hb), l1 = log(0.5);
+    if (kind == 5)
+      ln_mean_pair_halved(ha, hb, 0.5, 0.5, la, lb, l1, l1, m, im);
+    else
+      ln_mean_pair_halved(0.5, 0.5, ha, hb, l1, l1, la, lb, m, im);
   } else if (kind == 3) {
     m = ln_mean_single(a, b);
     im = inv_ln_mean_single(a, b);
@@ -58,7 +68,7 @@ extern "C" {
 
 int tag_eval_means(int32_t kind, int64_t n, double gamma_cp, double gamma_cv, const double* x,
                    const double* y, double* out1, double* out2) {
-  if (kind < 0 || kind > 4 || n < 0 || (n > 0 && (!x || !y || !out1 || !out2)))
+  if (kind < 0 || kind > 6 || n < 0 || (n > 0 && (!x || !y || !out1 || !out2)))
     return mfail(TAG_E_INVALID, "tag_eval_means: bad argument");
   if (n == 0) return TAG_OK;
   const double pp[8] = {gamma_cp, gamma_cv, 9.81, 340.0, 0.0, 0.0, 0.0, 1.0};

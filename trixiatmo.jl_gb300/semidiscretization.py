@@ -587,7 +587,9 @@ class SemidiscretizationHyperbolic:
     def newton_solve(self, learned=False):
         """One Newton solve on every node of the resident state; returns
         (stats dict, per-node update counts).  learned: False / 0 the warm
-        start, True / 1 the learned guess, 2 its closed-form branch alone."""
+        start, True / 1 the learned guess, 2 its closed-form branch alone,
+        3 the closed-form branch and on saturated nodes the smaller-residual
+        one of the MLP guess and the warm start."""
         iters = np.zeros(self.ndofs, dtype=np.int32)
         st = _lib.NewtonStats()
         _lib.check(self._L.tag_newton_solve(self._h, int(learned), _ptr(iters, _ip),
@@ -598,7 +600,8 @@ class SemidiscretizationHyperbolic:
     def set_newton_start(self, start):
         """Start of the stage limiter's Newton solve inside rk_steps: 0 the
         warm start (the reference's), 1 the learned guess, 2 its closed-form
-        branch alone."""
+        branch alone, 3 the closed-form branch and on saturated nodes the
+        smaller-residual one of the MLP guess and the warm start."""
         _lib.check(self._L.tag_set_newton_start(self._h, int(start)))
 
     def newton_counters(self, reset=True):
