@@ -248,17 +248,22 @@ def swe_member_specs(nmembers, seed=5):
     return specs
 
 
+def swe_equations(tg, variant):
+    from trixiatmo_gb300.initial_conditions import (EARTH_GRAVITATIONAL_ACCELERATION as G,
+                                                    EARTH_ROTATION_RATE as OM)
+    cv = tg.covariant
+    if variant == "ec":
+        return cv.SplitCovariantShallowWaterEquations2D(G, OM)
+    return cv.CovariantShallowWaterEquations2D(G, OM)
+
+
 def make_swe_ensemble(tg, nmembers=64, variant="weak", seed=5, members=None):
     """64 covariant shallow-water members of uneven size and degree on the
     cubed sphere: weak form + flux_lax_friedrichs (elixir_geostrophic_balance)
     or the split entropy-conservative form; Cartesian global coordinates."""
     cv = tg.covariant
-    from trixiatmo_gb300.initial_conditions import (EARTH_GRAVITATIONAL_ACCELERATION as G,
-                                                    EARTH_RADIUS, EARTH_ROTATION_RATE as OM)
-    if variant == "ec":
-        eq = cv.SplitCovariantShallowWaterEquations2D(G, OM)
-    else:
-        eq = cv.CovariantShallowWaterEquations2D(G, OM)
+    from trixiatmo_gb300.initial_conditions import EARTH_RADIUS
+    eq = swe_equations(tg, variant)
     specs = swe_member_specs(nmembers, seed)
     if members is not None:
         specs = [specs[m] for m in members]
@@ -284,6 +289,40 @@ def make_swe_ensemble(tg, nmembers=64, variant="weak", seed=5, members=None):
     ens = tg.SemidiscretizationCovariantEnsemble(meshes, eq, ics, solvers,
                                                  source_terms=cv.source_terms_geometric_coriolis)
     return eq, ens, specs, (meshes, solvers, ics)
+
+
+def cpu_oracle_rate_swe(tg, args, eq):
+    """The oracle's covariant shallow-water steps on the host cores, on a
+    bounded sample of the uneven ensemble (its first four members): the same
+    members, states and step control as the GPU run.  The members' meshes and
+    metric terms come from the package's mesh construction; only the oracle's
+    CK2N54 steps are timed."""
+    orc = entry.load_oracle()
+    orc.build()
+    M = args.swe_members
+    sample = list(range(min(4, M)))
+    _, ens_s, specs_s, _ = make_swe_ensemble(tg, M, args.swe_variant, members=sample)
+    cov_ids = dict(volume=0, surf_sym=0, surf_diss=1) if args.swe_variant == "weak" else \
+        dict(volume=1, vol_sym=1, vol_nc=1, surf_sym=1, surf_diss=1, surf_nc=2)
+    a = time.perf_counter()
+    cdofs = 0
+    for i, m in enumerate(sample):
+        mesh = ens_s.meshes[i]
+        basis = ens_s.solvers[i].basis
+        conn = mesh.connectivity(basis)
+        ie, ifc, flip, _, _ = conn.arrays()
+        c = orc.CovSWE(basis.n - 1, ens_s._H.aux[i], ens_s._H.xyz[i], ie, ifc, flip,
+                       eq.gravity, eq.rotation_rate, eq.split, cov_ids)
+        um = np.ascontiguousarray(ens_s.member_state(ens_s.compute_coefficients(), i))
+        c.ck_steps(um, np.zeros_like(um), 0.0, 0.4, args.cpu_steps)
+        cdofs += um.size // 3
+    cel = time.perf_counter() - a
+    ens_s.close()
+    return {"value": cdofs * 5 * args.cpu_steps / cel, "unit": UNIT,
+            "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
+            "kind": "port",
+            "sample": f"{len(sample)} of the members x {args.cpu_steps} CK2N54 steps, oracle/ "
+                      f"C++ OpenMP ({cel:.1f} s)"}, cel
 
 
 def run_swe(args):
@@ -363,34 +402,7 @@ def run_swe(args):
     peak_fp64, peak_src, probe_fp64 = fp64_roofline_peak(tg, clock_info)
     achieved_tf = fl / (ms_el * 1e-3) / 1e12
     traffic = TRAFFIC_PER_DOF.get("swe" if args.swe_variant == "weak" else "swe_ec")
-    cpu = None
-    if not args.no_cpu:
-        orc = entry.load_oracle()
-        orc.build()
-        sample = list(range(min(4, M)))
-        _, ens_s, specs_s, _ = make_swe_ensemble(tg, args.swe_members, args.swe_variant,
-                                                 members=sample)
-        cov_ids = dict(volume=0, surf_sym=0, surf_diss=1) if args.swe_variant == "weak" else \
-            dict(volume=1, vol_sym=1, vol_nc=1, surf_sym=1, surf_diss=1, surf_nc=2)
-        a = time.perf_counter()
-        cdofs = 0
-        for i, m in enumerate(sample):
-            mesh = ens_s.meshes[i]
-            basis = ens_s.solvers[i].basis
-            conn = mesh.connectivity(basis)
-            ie, ifc, flip, _, _ = conn.arrays()
-            c = orc.CovSWE(basis.n - 1, ens_s._H.aux[i], ens_s._H.xyz[i], ie, ifc, flip,
-                           eq.gravity, eq.rotation_rate, eq.split, cov_ids)
-            um = np.ascontiguousarray(ens_s.member_state(ens_s.compute_coefficients(), i))
-            c.ck_steps(um, np.zeros_like(um), 0.0, 0.4, args.cpu_steps)
-            cdofs += um.size // 3
-        cel = time.perf_counter() - a
-        ens_s.close()
-        cpu = {"value": cdofs * 5 * args.cpu_steps / cel, "unit": UNIT,
-               "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
-               "kind": "port",
-               "sample": f"{len(sample)} of the members x {args.cpu_steps} CK2N54 steps, oracle/ "
-                         f"C++ OpenMP ({cel:.1f} s)"}
+    cpu = None if args.no_cpu else cpu_oracle_rate_swe(tg, args, eq)[0]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -673,6 +685,15 @@ def run_reference(args):
         config = {"workload": "3D cubed-sphere shell 6x16x16x8, polydeg 5, isothermal + Coriolis, "
                               "CK2N54 CFL 1", "dofs": 2654208}
         sample = f"the full shell workload, {steps} CK2N54 steps"
+    elif args.workload == "swe":
+        # the sampled members' meshes and metric terms are built by the package
+        tg = entry.load_package()
+        args.cpu_steps = steps
+        c, el = cpu_oracle_rate_swe(tg, args, swe_equations(tg, args.swe_variant))
+        rate, threads = c["value"], c["cores"]
+        config = {"workload": f"{args.swe_members} covariant shallow-water members on the cubed "
+                              f"sphere, {args.swe_variant} form", "members": args.swe_members}
+        sample = c["sample"]
     else:
         sample_m = args.ref_members
         rate, threads, el = cpu_oracle_rate(sample_m, steps, warmup=args.warmup > 0)

@@ -7,7 +7,8 @@
 // tournament scheduling) so that within a round the pairs of a line touch
 // disjoint nodes.  Each round therefore adds D_split-weighted pair fluxes
 // straight into per-direction node accumulators without atomics, and the
-// summation order is fixed (bitwise reproducible).
+// summation order is fixed (bitwise reproducible).  A warp owns whole lines,
+// so the rounds need only warp-level synchronisation.
 // Layouts: u[e][k][j][i][v]; Ja[e][k][j][i][d][c]; invJ[e][k][j][i];
 // sfv[e][face][l2][l1][NA].
 #pragma once
@@ -115,8 +116,9 @@ struct ElemSmem3D {
   static constexpr int nn = n * n, nnn = n * n * n;
   static constexpr int S = ((n + 1) & ~1) / 2;     // pair slots per line and round (incl. a bye)
   static constexpr int R = ((n + 1) & ~1) - 1;     // rounds
-  static constexpr int P = 3 * nn * S;             // pair threads per element
-  static constexpr int TPE = (P > nnn) ? P : nnn;  // threads per element
+  static constexpr int LPW = 32 / S;               // whole lines per warp
+  static constexpr int WPE = (3 * nn + LPW - 1) / LPW;  // warps per element in the pair phase
+  static constexpr int TPE = (32 * WPE > nnn) ? 32 * WPE : nnn;  // threads per element
   static constexpr int oU = 0;
   static constexpr int oQ = oU + nnn * NV;
   static constexpr int oJa = oQ + nnn * NQ;       // contravariant vectors as stored
@@ -201,43 +203,55 @@ __global__ void k_element3d(typename Phys::Params Pp, const BasisDev basis, doub
   }
   if (Phys::kNodeLogs) __syncthreads();
 
-  // volume integral: R rounds, one symmetric pair per thread and round
-  for (int r = 0; r < S::R; ++r) {
-    for (int t = threadIdx.x; t < ne * S::P; t += nthr) {
-      const int el = t / S::P, p = t % S::P;
-      const int slot = p % S::S, line = (p / S::S) % nn, d = p / (S::S * nn);
-      int a, b;
-      if (!round_robin_pair(n, r, slot, a, b)) continue;
+  // volume integral: each warp takes whole lines (LPW lines of one element,
+  // S slots each) and runs their R rounds with only __syncwarp between rounds:
+  // the pairs of one line meet the same nodes only across rounds, the lines of
+  // one direction are disjoint, and each direction has its own accumulators.
+  // A node's contributions arrive in round order whatever the launch shape.
+  {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = nthr >> 5;
+    const int lw = lane / S::S, slot = lane % S::S;
+    for (int task = warp; task < ne * S::WPE; task += nwarps) {
+      const int el = task / S::WPE;
+      const int lg = (task % S::WPE) * S::LPW + lw;  // d * nn + line
+      const bool on = lw < S::LPW && lg < 3 * nn;
+      const int d = lg / nn, line = lg % nn;
       // line = p1 + n * p2 over the two other directions (ascending)
       const int p1 = line % n, p2 = line / n;
-      int na_, nb_;
-      if (d == 0) {
-        na_ = (p2 * n + p1) * n + a;
-        nb_ = (p2 * n + p1) * n + b;
-      } else if (d == 1) {
-        na_ = (p2 * n + a) * n + p1;
-        nb_ = (p2 * n + b) * n + p1;
-      } else {
-        na_ = (a * n + p2) * n + p1;
-        nb_ = (b * n + p2) * n + p1;
-      }
       double* eb = base + el * S::per_elem;
-      const double* ja_a = eb + S::oJa + na_ * 9 + 3 * d;
-      const double* ja_b = eb + S::oJa + nb_ * 9 + 3 * d;
-      const double nrm[3] = {ja_a[0] + ja_b[0], ja_a[1] + ja_b[1], ja_a[2] + ja_b[2]};
-      double Fa[NA], Fb[NA];
-      Phys::volume_pair(Pp, eb + S::oQ + na_ * NQ, eb + S::oQ + nb_ * NQ, nrm, Fa, Fb);
-      const double dab = sb->Ds[a * n + b], dba = sb->Ds[b * n + a];
-      double* ca = eb + S::oA + (d * nnn + na_) * NA;
-      double* cb = eb + S::oA + (d * nnn + nb_) * NA;
+      for (int r = 0; r < S::R; ++r) {
+        int a, b;
+        if (on && round_robin_pair(n, r, slot, a, b)) {
+          int na_, nb_;
+          if (d == 0) {
+            na_ = (p2 * n + p1) * n + a;
+            nb_ = (p2 * n + p1) * n + b;
+          } else if (d == 1) {
+            na_ = (p2 * n + a) * n + p1;
+            nb_ = (p2 * n + b) * n + p1;
+          } else {
+            na_ = (a * n + p2) * n + p1;
+            nb_ = (b * n + p2) * n + p1;
+          }
+          const double* ja_a = eb + S::oJa + na_ * 9 + 3 * d;
+          const double* ja_b = eb + S::oJa + nb_ * 9 + 3 * d;
+          const double nrm[3] = {ja_a[0] + ja_b[0], ja_a[1] + ja_b[1], ja_a[2] + ja_b[2]};
+          double Fa[NA], Fb[NA];
+          Phys::volume_pair(Pp, eb + S::oQ + na_ * NQ, eb + S::oQ + nb_ * NQ, nrm, Fa, Fb);
+          const double dab = sb->Ds[a * n + b], dba = sb->Ds[b * n + a];
+          double* ca = eb + S::oA + (d * nnn + na_) * NA;
+          double* cb = eb + S::oA + (d * nnn + nb_) * NA;
 #pragma unroll
-      for (int v = 0; v < NA; ++v) {
-        ca[v] = fma(dab, Fa[v], ca[v]);
-        cb[v] = fma(dba, Fb[v], cb[v]);
+          for (int v = 0; v < NA; ++v) {
+            ca[v] = fma(dab, Fa[v], ca[v]);
+            cb[v] = fma(dba, Fb[v], cb[v]);
+          }
+        }
+        __syncwarp();
       }
     }
-    __syncthreads();
   }
+  __syncthreads();
 
   // per (node, variable): direction sums, surface integral, Jacobian, sources,
   // stage update
@@ -326,16 +340,21 @@ __global__ void k_element3d(typename Phys::Params Pp, const BasisDev basis, doub
   if (bad) atomicOr(status, bad);
 }
 
+// One warp per element (a 3D element has up to 512 nodes): the lanes stride
+// over the nodes, the per-direction maxima meet by shuffles, and lane 0 adds
+// the element's value into its member's running maximum.  Max is exact, so the
+// result does not depend on the order.  blockDim is a multiple of 32.
 template <class Phys, int n>
 __global__ void k_max_speed3d(typename Phys::Params Pp, const double* __restrict__ u,
                               const double* __restrict__ Ja, const double* __restrict__ invJ,
                               int nelem, const int* __restrict__ member,
                               double* __restrict__ max_speed) {
   constexpr int NV = Phys::NV, nnn = n * n * n;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= nelem) return;
+  const int lane = threadIdx.x & 31;
+  const int e = (int)(((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (e >= nelem) return;  // warp-uniform
   double m[3] = {0.0, 0.0, 0.0};
-  for (int node = 0; node < nnn; ++node) {
+  for (int node = lane; node < nnn; node += 32) {
     const size_t q = (size_t)e * nnn + node;
     double lam[3];
     Phys::max_speeds(Pp, u + q * NV, lam);
@@ -345,7 +364,11 @@ __global__ void k_max_speed3d(typename Phys::Params Pp, const double* __restrict
     for (int d = 0; d < 3; ++d)
       m[d] = fmax(m[d], fabs(ja[3 * d] * lam[0] + ja[3 * d + 1] * lam[1] + ja[3 * d + 2] * lam[2]) * ij);
   }
-  atomic_max_nonneg(max_speed + (member ? member[e] : 0), m[0] + m[1] + m[2]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) m[d] = fmax(m[d], __shfl_xor_sync(0xffffffffu, m[d], o));
+  if (lane == 0) atomic_max_nonneg(max_speed + (member ? member[e] : 0), m[0] + m[1] + m[2]);
 }
 
 }  // namespace tag

@@ -305,8 +305,8 @@ struct OpsImpl3D {
     return TAG_OK;
   }
   static int max_speed(tag_handle h, const double* u) {
-    const int threads = 128;
-    k_max_speed3d<Phys, n><<<(h->nelem + threads - 1) / threads, threads, 0, h->stream>>>(
+    const int threads = 256, warps = threads / 32;  // one warp per element
+    k_max_speed3d<Phys, n><<<(h->nelem + warps - 1) / warps, threads, 0, h->stream>>>(
         params_of<Phys>(h), u, h->d_Ja, h->d_invJ, h->nelem, h->d_member,
         h->d_mscal + 2 * h->nmembers);
     TAG_CUDA(cudaGetLastError());
