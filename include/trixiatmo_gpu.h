@@ -202,6 +202,34 @@ int tag_max_dt(tag_handle h, double* out);
  * (interface kernel + element kernel) pair per stage (5, 4 or 3 stages). */
 int tag_rk_steps(tag_handle h, int32_t nsteps, double cfl, double fixed_dt, double* t);
 
+typedef struct tag_adaptive_stats {
+  int64_t accepted;  /* steps taken                                   */
+  int64_t rejected;  /* steps repeated with a smaller dt               */
+  double dt_first;   /* the initial step size                          */
+  double dt_last;    /* the last accepted step (shortened at t_end)    */
+} tag_adaptive_stats;
+
+/* Error-controlled SSPRK43 from *t to t_end on a single mesh: what the
+ * reference's elixirs get from `solve(ode, SSPRK43(); abstol, reltol,
+ * callback = ...)` without a StepsizeCallback (e.g.
+ * examples/euler/dry_air/mountain_flow/elixir_potential_temperature_linear_hydrostatic.jl:83-86,
+ * examples/euler/dry_air/global_circulation/elixir_potential_temperature_baroclinic_instability.jl:62-66;
+ * OrdinaryDiffEq's integrator, an external dependency).  The handle's scheme
+ * must be SSPRK43 (tag_set_time_integrator).  Each step runs the four stages
+ * on the device (and the stage limiter after each, for the rainy equations)
+ * and one error kernel; the error estimate is the difference to the embedded
+ * second-order solution with weights (1/4, 1/4, 1/4, 1/4), in the
+ * root-mean-square norm of e / (abstol + max(|u_prev|, |u_new|) reltol) over
+ * every state entry.  The step size follows the PI controller with beta1 =
+ * 7/30, beta2 = 2/15, gamma = 0.9, qmin = 0.2, qmax = 10 (a rejected step is
+ * repeated from its starting state); the first step follows Hairer, Norsett
+ * and Wanner's starting-step algorithm.  A step never passes the next of the
+ * increasing `stops` (the times of a SaveSolutionCallback(dt)) or t_end.
+ * *t is updated to the time reached; TAG_E_INVALID after max_steps attempts. */
+int tag_rk_adaptive(tag_handle h, double* t, double t_end, double abstol, double reltol,
+                    const double* stops, int32_t nstops, int64_t max_steps,
+                    tag_adaptive_stats* stats);
+
 /* Time integrator of tag_rk_steps.  The reference picks it by the algorithm
  * passed to `solve(ode, alg; dt, callback = StepsizeCallback(cfl))`:
  *   TAG_RK_CK2N54   CarpenterKennedy2N54(williamson_condition = false), the default

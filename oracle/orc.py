@@ -107,6 +107,12 @@ def lib():
             f.restype = ctypes.c_double
             f.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                           ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.orc_pt_ssprk43_adaptive.restype = ctypes.c_double
+        L.orc_pt_ssprk43_adaptive.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double,
+                                              ctypes.c_double, _dp, ctypes.c_int, ctypes.c_double,
+                                              ctypes.c_double, ctypes.c_int, _dp]
+        L.orc_pt3d_ssprk43_adaptive.restype = ctypes.c_double
+        L.orc_pt3d_ssprk43_adaptive.argtypes = L.orc_pt_ssprk43_adaptive.argtypes
         L.orc_pt_ck_steps.restype = ctypes.c_double
         L.orc_pt_ck_steps.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_int]
@@ -364,6 +370,14 @@ class PotTemp3D:
     def ssp_steps(self, u, t, cfl, nsteps, scheme, fixed_dt=0.0, t_end=0.0):
         return lib().orc_pt3d_ssp_steps(self.h, _p(u), t, cfl, nsteps, scheme, fixed_dt, t_end)
 
+    def ssprk43_adaptive(self, u, t, t_end, abstol=1e-6, reltol=1e-3, stops=(), variant=0):
+        """Adaptive SSPRK43 (see PotTemp2D.ssprk43_adaptive)."""
+        st = np.zeros(5)
+        sp = np.ascontiguousarray(stops, dtype=np.float64)
+        tf = lib().orc_pt3d_ssprk43_adaptive(self.h, _p(u), t, t_end, _p(sp) if sp.size else None,
+                                             int(sp.size), abstol, reltol, variant, _p(st))
+        return tf, dict(zip(("accepted", "rejected", "rhs_calls", "dt_first", "dt_last"), st))
+
 
 def pt_pointwise(ndims, kind, ul, ur, n, volume=0, nc=0, c=340.0):
     """Pointwise potential-temperature fluxes (kind 0 flux, 1 volume flux,
@@ -530,6 +544,17 @@ class PotTemp2D:
     def ssp_steps(self, u, t, cfl, nsteps, scheme, fixed_dt=0.0, t_end=0.0):
         """SSPRK43 (scheme 1) or SSPRK33 (scheme 2) steps; returns the new time."""
         return lib().orc_pt_ssp_steps(self.h, _p(u), t, cfl, nsteps, scheme, fixed_dt, t_end)
+
+    def ssprk43_adaptive(self, u, t, t_end, abstol=1e-6, reltol=1e-3, stops=(), variant=0):
+        """Adaptive SSPRK43 with OrdinaryDiffEq's default error control
+        (orc_time.hpp) from t to t_end, never stepping past a stop; returns
+        (final time, dict of accepted / rejected steps, rhs calls, first and
+        last dt)."""
+        st = np.zeros(5)
+        sp = np.ascontiguousarray(stops, dtype=np.float64)
+        tf = lib().orc_pt_ssprk43_adaptive(self.h, _p(u), t, t_end, _p(sp) if sp.size else None,
+                                           int(sp.size), abstol, reltol, variant, _p(st))
+        return tf, dict(zip(("accepted", "rejected", "rhs_calls", "dt_first", "dt_last"), st))
 
     def __del__(self):
         if getattr(self, "h", None):

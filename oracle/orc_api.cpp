@@ -878,6 +878,26 @@ double orc_pt3d_ssp_steps(void* h, double* u, double t, double cfl, int nsteps, 
                    c->ndofs() * 6, t, cfl, nsteps, scheme, fixed_dt, t_end);
 }
 
+// Adaptive SSPRK43 (orc_time.hpp) on a 3D potential-temperature case; see
+// orc_pt_ssprk43_adaptive.
+double orc_pt3d_ssprk43_adaptive(void* h, double* u, double t, double t_end, const double* stops,
+                                 int nstops, double abstol, double reltol, int variant,
+                                 double* stats) {
+  auto* c = static_cast<PT3DCase*>(h);
+  AdaptiveStats st;
+  const double tf = ssprk43_adaptive(
+      [&](const double* uu, double* dd, double tt) { c->dg->rhs(uu, dd, tt); }, [](double*) {}, u,
+      c->ndofs() * 6, t, t_end, stops, nstops, abstol, reltol, variant, &st);
+  if (stats) {
+    stats[0] = (double)st.accepted;
+    stats[1] = (double)st.rejected;
+    stats[2] = (double)st.rhs_calls;
+    stats[3] = st.dt_first;
+    stats[4] = st.dt_last;
+  }
+  return tf;
+}
+
 // pointwise 3D fluxes for the consistency tests: kind 0 flux, 1 volume flux
 // (tec / ec / etec by `volume`), 2 nonconservative term (by `nc`), 3 LMARS(c)
 void orc_pt3d_pointwise(int kind, int volume, int nc, double c, const double* ul,
@@ -1520,6 +1540,27 @@ double orc_pt_ssp_steps(void* h, double* u, double t, double cfl, int nsteps, in
                    [&](const double* uu) { return c->dg->max_dt(uu); }, [](double*) {}, u,
                    c->ndofs() * 5, t,
                    cfl, nsteps, scheme, fixed_dt, t_end);
+}
+
+// Adaptive SSPRK43 (orc_time.hpp) on a 2D potential-temperature case from t
+// to t_end with optional stops; stats = (accepted, rejected, rhs calls,
+// first dt, last dt).  Returns the final time.
+double orc_pt_ssprk43_adaptive(void* h, double* u, double t, double t_end, const double* stops,
+                               int nstops, double abstol, double reltol, int variant,
+                               double* stats) {
+  auto* c = static_cast<PTCase*>(h);
+  AdaptiveStats st;
+  const double tf = ssprk43_adaptive(
+      [&](const double* uu, double* dd, double tt) { c->dg->rhs(uu, dd, tt); }, [](double*) {}, u,
+      c->ndofs() * 5, t, t_end, stops, nstops, abstol, reltol, variant, &st);
+  if (stats) {
+    stats[0] = (double)st.accepted;
+    stats[1] = (double)st.rejected;
+    stats[2] = (double)st.rhs_calls;
+    stats[3] = st.dt_first;
+    stats[4] = st.dt_last;
+  }
+  return tf;
 }
 
 // the logarithmic mean and its inverse of orc_means.hpp (Trixi's definitions)

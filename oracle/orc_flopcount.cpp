@@ -11,6 +11,7 @@
 // pragmas of the drivers are ignored).
 #include "orc_flop.hpp"
 
+#define ORC_FLOP_COUNTING
 #define double orc_count::Flop
 #include "orc_basis.hpp"
 #include "orc_means.hpp"

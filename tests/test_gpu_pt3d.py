@@ -116,3 +116,77 @@ def test_pt3d_analysis_integrals(tg, orc, gpu_lib):
         ref = (wJ * f).sum() / vol
         assert abs(got - ref) <= tol * (wJ * np.abs(f)).sum() / vol, (got, ref)
     semi.close()
+
+
+@pytest.mark.parametrize("name,volume,nc", [("souza", "tec", "souza"),
+                                            ("waruszewski", "ec", "waruszewski"),
+                                            ("artiano", "etec", "artiano")])
+def test_gpu_reproduces_baroclinic_instability_goldens(tg, orc, gpu_lib, name, volume, nc):
+    """test/test_3d_potential_temperature.jl:100-177 as the reference runs them:
+    error-controlled SSPRK43 (abstol = reltol = 1e-6, stops every 100 s) with
+    every stage and the error estimate on the GPU (tag_rk_adaptive).  The
+    stops every 100 s make the step count sensitive to the last bits of the
+    error norms: a step that ends just short of a stop adds one short step, so
+    the GPU's step count is within a few of the oracle's (equal for two of the
+    three cases) and its final state within 1e-6 of the oracle's; norms against the goldens within the bounds
+    of tests/test_oracle_pt3d.py."""
+    import analysis
+    from test_oracle_pt3d import BAROCLINIC_T_END, baroclinic_stops, check_baroclinic
+    eq, mesh, semi = make_pt3d(tg, 2, 2, 5, volume, nc)
+    u0 = semi.compute_coefficients()
+    semi.set_state(u0)
+    t, st = semi.solve_adaptive((0.0, BAROCLINIC_T_END), abstol=1e-6, reltol=1e-6, save_dt=100.0)
+    assert t == BAROCLINIC_T_END
+    u = semi.get_state()
+    basis = semi.solver.basis
+    ic = lambda x: tg.initial_condition_baroclinic_instability(x, 0.0, eq)  # noqa: E731
+    l2, linf = analysis.error_norms(u, semi.node_coordinates, semi.inverse_jacobian, basis.nodes,
+                                    ic, 3)
+    check_baroclinic(name, l2, linf)
+    o = oracle_pt3d(orc, tg, semi, mesh, volume, nc)
+    uo = np.ascontiguousarray(u0).copy()
+    to, sto = o.ssprk43_adaptive(uo, 0.0, BAROCLINIC_T_END, abstol=1e-6, reltol=1e-6,
+                                 stops=baroclinic_stops())
+    assert abs(st["accepted"] - sto["accepted"]) <= 5 and st["rejected"] == sto["rejected"], (
+        st, sto)
+    assert rel(u[..., :5], uo[..., :5]) <= 1e-6
+    semi.close()
+
+
+@pytest.mark.parametrize("case", ["galchen", "sleve"])
+def test_gpu_reproduces_vortex_shedding_goldens(tg, orc, gpu_lib, case):
+    """test/test_3d_potential_temperature.jl:244-296 (small-Earth vortex
+    shedding over a Gaussian mountain, GalChen or Sleve vertical coordinates)
+    with error-controlled SSPRK43 on the GPU: goldens at the test's own rtol
+    1e-9, step sequence and final state against the oracle's run."""
+    import analysis
+    from test_oracle_pt3d import VORTEX_T_END, check_vortex, vortex_mesh
+    eq = tg.CompressibleEulerPotentialTemperatureEquationsWithGravity3D(
+        c_p=1004, c_v=717, gravity=tg.EARTH_GRAVITATIONAL_ACCELERATION)
+    mesh = vortex_mesh(tg, case)
+    solver = tg.DGSEM(5, (tg.FluxLMARS(340.0), tg.flux_zero),
+                      tg.VolumeIntegralFluxDifferencing((tg.flux_tec,
+                                                         tg.flux_nonconservative_souza_etal)))
+    semi = tg.SemidiscretizationHyperbolic(
+        mesh, eq, tg.initial_condition_vortex_shedding, solver,
+        source_terms=tg.source_terms_coriolis_small_earth,
+        boundary_conditions={"inside": tg.boundary_condition_slip_wall,
+                             "outside": tg.boundary_condition_slip_wall})
+    u0 = semi.compute_coefficients()
+    semi.set_state(u0)
+    t, st = semi.solve_adaptive((0.0, VORTEX_T_END), abstol=1e-6, reltol=1e-6)
+    assert t == VORTEX_T_END
+    u = semi.get_state()
+    ic = lambda x: tg.initial_condition_vortex_shedding(x, 0.0, eq)  # noqa: E731
+    l2, linf = analysis.error_norms(u, semi.node_coordinates, semi.inverse_jacobian,
+                                    semi.solver.basis.nodes, ic, 3)
+    check_vortex(case, l2, linf)
+    o = orc.PotTemp3D(5, semi.contravariant_vectors, semi.inverse_jacobian, semi.node_coordinates,
+                      *mesh.connectivity(semi.solver.basis).arrays(), c_p=1004.0, c_v=717.0,
+                      g=tg.EARTH_GRAVITATIONAL_ACCELERATION, c_lmars=340.0,
+                      omega=tg.SMALL_EARTH_ROTATION_RATE, volume=0, nc=2)
+    uo = np.ascontiguousarray(u0).copy()
+    to, sto = o.ssprk43_adaptive(uo, 0.0, VORTEX_T_END, abstol=1e-6, reltol=1e-6)
+    assert (st["accepted"], st["rejected"]) == (sto["accepted"], sto["rejected"]), (st, sto)
+    assert rel(u[..., :5], uo[..., :5]) <= 1e-8  # step sizes from rounding-sensitive norms
+    semi.close()

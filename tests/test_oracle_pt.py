@@ -137,16 +137,23 @@ def check_well_balanced(l2, linf, g2, gi):
 # terrain-following P4estMesh (transfinite mapping of terrain_following_faces),
 # MountainWaveSetup as initial condition, Dirichlet boundary data (left, right,
 # top) and Rayleigh-damping source, slip wall at the ground.  The reference
-# integrates with adaptive (error-controlled) SSPRK43; SSPRK43 at fixed CFL 0.5
-# stands in for it.  With g = 9.81 (the goldens' gravity, see above) the l2
-# norms of the physical variables agree to 2.6e-6 (hydrostatic), 2.1e-4
-# (nonhydrostatic) and 4.4e-6 (Schaer) relative, the rest being the adaptive
-# step sequence; checked at the tests' own atol 1e-5 and 5e-4 relative on l2.
-# One linf norm, Schaer's rho_v1 (2.38, at the steepest ridges), moves with the
-# step sequence by 3e-5 between CFL 0.25 and 1.5 and stays 5e-5 off the
-# golden: it is checked at 1e-4 absolute (4e-5 relative).
+# integrates with error-controlled SSPRK43 at OrdinaryDiffEq's default
+# tolerances (abstol 1e-6, reltol 1e-3); so do the oracle (orc_time.hpp,
+# ssprk43_adaptive) and the GPU (tag_rk_adaptive).  Measured against the goldens
+# (g = 9.81, see above), l2 of the four physical variables relative: at most
+# 9.7e-7 (hydrostatic), 1.2e-4 (nonhydrostatic, rho_v2) and 1.1e-8 (Schaer);
+# SSPRK43 at fixed CFL 0.5 gave 2.6e-6, 2.1e-4 and 4.4e-6.  The remaining
+# differences are the step sequence's: the controller is restated from the
+# published algorithms, and a change of 1e-7 in its step-size factors moves the
+# nonhydrostatic norms by 1e-6 relative.  At 1e-3 reltol the time-integration
+# error itself is of that size (the nonhydrostatic rho_v2 norm moves by 2e-4
+# between reltol 1e-3 and 1e-7).  Checked at the tests' own atol 1e-5 and the
+# per-case l2 bounds below.  One linf norm, Schaer's rho_v1 (2.38, at the
+# steepest ridges), stays 5e-5 off the golden: it is checked at 1e-4 absolute
+# (4e-5 relative).
 G_EARTH = G_GOLDEN
-MOUNTAIN_L2_RTOL = 5e-4
+MOUNTAIN_L2_RTOL = {"linear_hydrostatic": 2e-6, "linear_nonhydrostatic": 2.5e-4,
+                    "schaer_mountain": 5e-8}
 MOUNTAIN_LINF_ATOL = {("schaer_mountain", 1): 1e-4}
 MOUNTAIN = {
     "linear_hydrostatic": dict(
@@ -180,7 +187,7 @@ MOUNTAIN = {
                 [0.0017570540164735249, 2.3792558995181707, 2.354152711825134,
                  0.0764797692902448, 8.731149137020111e-11])),
 }
-MOUNTAIN_CFL = 0.5
+MOUNTAIN_T_END = 360.0
 
 
 def mountain_case(tg, name, trees=(20, 12), polydeg=3):
@@ -226,7 +233,7 @@ def check_mountain(name, l2, linf, atol=1e-5):
         la = MOUNTAIN_LINF_ATOL.get((name, v), atol)
         assert abs(linf[v] - gi[v]) <= la, ("linf", v, linf[v], gi[v])
     for v in range(4):
-        assert abs(l2[v] / g2[v] - 1) <= MOUNTAIN_L2_RTOL, ("l2", v, l2[v], g2[v])
+        assert abs(l2[v] / g2[v] - 1) <= MOUNTAIN_L2_RTOL[name], ("l2", v, l2[v], g2[v])
 
 
 @pytest.mark.parametrize("name", list(MOUNTAIN))
@@ -236,8 +243,8 @@ def test_oracle_mountain_wave_golden(tg, orc, name):
     c = orc.PotTemp2D(3, 0, 0, 0, 0, 0, 0, mesh=arrays, **okw)
     c.set_mountain(setup.params(), bv)
     u = np.ascontiguousarray(setup(xy, 0.0, eq))
-    t = c.ssp_steps(u, 0.0, MOUNTAIN_CFL, 10 ** 7, 1, t_end=360.0)
-    assert abs(t - 360.0) < 1e-9
+    t, st = c.ssprk43_adaptive(u, 0.0, MOUNTAIN_T_END)
+    assert t == MOUNTAIN_T_END and st["accepted"] > 100
     l2, linf = analysis.error_norms(u, xy, invJ, basis.nodes, lambda x: setup(x, 0.0, eq), 2)
     check_mountain(name, l2, linf)
 

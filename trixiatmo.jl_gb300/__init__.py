@@ -30,7 +30,10 @@ from .equations import (CompressibleEulerEnergyEquationsWithGravity2D,
                         flux_tec, flux_etec, flux_nonconservative_artiano_etal,
                         flux_nonconservative_souza_etal)
 from .initial_conditions import (EARTH_GRAVITATIONAL_ACCELERATION, EARTH_RADIUS,
-                                 EARTH_ROTATION_RATE, IsothermalShell, MoistBubbleRainy,
+                                 EARTH_ROTATION_RATE, SMALL_EARTH_RADIUS,
+                                 SMALL_EARTH_ROTATION_RATE, SMALL_EARTH_SCALING,
+                                 initial_condition_vortex_shedding,
+                                 IsothermalShell, MoistBubbleRainy,
                                  WarmBubble, initial_condition_convergence_test_rainy,
                                  initial_condition_baroclinic_instability,
                                  initial_condition_gravity_waves, seeded_perturbation,
@@ -47,7 +50,8 @@ from .initial_conditions import MountainWaveSetup
 from .meshes3d import GalChen, P4estMeshCubedSphereTopography, Sleve
 from .semidiscretization import (DGSEM, SemidiscretizationCovariant,
                                  SemidiscretizationCovariantEnsemble, SemidiscretizationEnsemble,
-                                 SemidiscretizationHyperbolic, fp64_peak, source_terms_coriolis)
+                                 SemidiscretizationHyperbolic, fp64_peak, source_terms_coriolis,
+                                 source_terms_coriolis_small_earth)
 
 __all__ = [
     "LobattoLegendreBasis", "CompressibleEulerEnergyEquationsWithGravity2D", "FluxLMARS",
@@ -58,7 +62,9 @@ __all__ = [
     "SemidiscretizationEnsemble", "CompressibleEulerEnergyEquationsWithGravity3D",
     "EARTH_GRAVITATIONAL_ACCELERATION", "EARTH_RADIUS", "EARTH_ROTATION_RATE", "IsothermalShell",
     "initial_condition_baroclinic_instability", "P4estMeshCubedSphereTopography",
-    "source_terms_coriolis", "fp64_peak", "CompressibleRainyEulerEquations2D",
+    "source_terms_coriolis", "source_terms_coriolis_small_earth", "SMALL_EARTH_RADIUS",
+    "SMALL_EARTH_ROTATION_RATE", "SMALL_EARTH_SCALING", "initial_condition_vortex_shedding",
+    "fp64_peak", "CompressibleRainyEulerEquations2D",
     "VolumeIntegralWeakForm", "boundary_condition_simple_slip_wall", "flux_ec_rain",
     "flux_lax_friedrichs", "source_terms_convergence_test_rainy", "source_terms_rainy",
     "MoistBubbleRainy", "initial_condition_convergence_test_rainy", "learned_guess",

@@ -107,6 +107,11 @@ class NewtonStats(ctypes.Structure):
                 ("fallbacks", ctypes.c_int64), ("not_converged", ctypes.c_int64)]
 
 
+class AdaptiveStats(ctypes.Structure):
+    _fields_ = [("accepted", ctypes.c_int64), ("rejected", ctypes.c_int64),
+                ("dt_first", ctypes.c_double), ("dt_last", ctypes.c_double)]
+
+
 _fp = ctypes.POINTER(ctypes.c_float)
 
 # exported symbol -> (restype, argtypes)
@@ -125,6 +130,10 @@ SIGNATURES = {
     "tag_time_kernels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp, _dp]),
     "tag_rk_steps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double,
                                     ctypes.c_double, _dp]),
+    "tag_rk_adaptive": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                        ctypes.POINTER(ctypes.c_double), ctypes.c_int32,
+                                        ctypes.c_int64, ctypes.c_void_p]),
     "tag_set_time_integrator": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "tag_set_boundary_values": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "tag_set_source": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp, ctypes.c_int32]),

@@ -363,7 +363,7 @@ __global__ void k_element(typename Phys::Params Pp, const BasisDev basis, double
       u[gq * NV + v] = un;
     }
   }
-  if (MODE == kModeRhs) {
+  if constexpr (MODE == kModeRhs && NV > NA) {
     // passive variables have zero time derivative
     for (int t = threadIdx.x; t < ne * nn * (NV - NA); t += nthr) {
       const int el = t / (nn * (NV - NA)), r = t % (nn * (NV - NA));

@@ -313,13 +313,26 @@ __global__ void k_element3d(typename Phys::Params Pp, const BasisDev basis, doub
             fabs(ja[3 * d] * lam[0] + ja[3 * d + 1] * lam[1] + ja[3 * d + 2] * lam[2]) * ij;
     }
     __syncthreads();
-    for (int el = threadIdx.x; el < ne; el += nthr) {
-      double* eb = base + el * S::per_elem;
-      double m[3] = {0.0, 0.0, 0.0};
-      for (int node = 0; node < nnn; ++node)
+    // one warp per element: the per-direction maxima over its nodes on the
+    // integer pipe (the speeds are non-negative, and the bit patterns of
+    // non-negative doubles order like their values), then summed
+    {
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = nthr >> 5;
+      for (int el = warp; el < ne; el += nwarps) {
+        double* eb = base + el * S::per_elem;
+        long long m[3] = {0, 0, 0};
+        for (int node = lane; node < nnn; node += 32)
 #pragma unroll
-        for (int d = 0; d < 3; ++d) m[d] = fmax(m[d], eb[S::oL + d * nnn + node]);
-      eb[S::oL] = m[0] + m[1] + m[2];
+          for (int d = 0; d < 3; ++d)
+            m[d] = max(m[d], __double_as_longlong(eb[S::oL + d * nnn + node]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+          for (int d = 0; d < 3; ++d) m[d] = max(m[d], __shfl_xor_sync(0xffffffffu, m[d], o));
+        if (lane == 0)
+          eb[S::oL] = __longlong_as_double(m[0]) + __longlong_as_double(m[1]) +
+                      __longlong_as_double(m[2]);
+      }
     }
     __syncthreads();
     if (threadIdx.x == 0) {

@@ -160,10 +160,10 @@ struct PhysEnergy2D {
 
   // max_abs_speeds (:518-524)
   TAG_DEV static void max_speeds(const Params& P, const double* u, double& l1, double& l2) {
-    const double rho = u[0];
-    const double v1 = u[1] / rho, v2 = u[2] / rho;
+    const double irho = 1.0 / u[0];
+    const double v1 = u[1] * irho, v2 = u[2] * irho;
     const double p = P.gm1 * (u[3] - 0.5 * (u[1] * v1 + u[2] * v2));
-    const double c = sqrt(P.gamma * p / rho);
+    const double c = sqrt(P.gamma * p * irho);
     l1 = fabs(v1) + c;
     l2 = fabs(v2) + c;
   }

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -101,6 +102,8 @@ struct tag_handle_s {
   cudaStream_t stream = nullptr;
   double *d_u = nullptr, *d_k = nullptr, *d_Ja = nullptr, *d_invJ = nullptr, *d_xy = nullptr,
          *d_sfv = nullptr, *d_tmp_u = nullptr, *d_tmp_du = nullptr;
+  // adaptive SSPRK43: the stage value entering the last stage, error partials
+  double *d_u3 = nullptr, *d_err = nullptr;
   int *d_if_e = nullptr, *d_if_f = nullptr, *d_if_flip = nullptr, *d_bd_e = nullptr,
       *d_bd_f = nullptr, *d_bd_kind = nullptr;
   // states of the TAG_BC_DIRICHLET faces [B][n][nv] (allocated when the mesh has
@@ -1151,7 +1154,7 @@ int tag_destroy(tag_handle h) {
   double* dp[] = {h->d_u,       h->d_k,       h->d_Ja,         h->d_invJ,    h->d_xy,
                   h->d_sfv,     h->d_tmp_u,   h->d_tmp_du,     h->d_an_wj,   h->d_an_V,
                   h->d_an_wa,   h->d_an_rows, h->d_an_erows,   h->d_an_out,  h->d_an_uex,
-                  h->d_an_x,    h->d_bvals};
+                  h->d_an_x,    h->d_bvals,   h->d_u3,         h->d_err};
   for (double* p : dp)
     if (p) cudaFree(p);
   int* ip[] = {h->d_if_e, h->d_if_f, h->d_if_flip, h->d_bd_e, h->d_bd_f, h->d_bd_kind};
@@ -1290,6 +1293,205 @@ int tag_rk_steps(tag_handle h, int32_t nsteps, double cfl, double fixed_dt, doub
   TAG_CUDA(cudaStreamSynchronize(h->stream));
   for (int m = 0; m < M; ++m) t[m] = h->h_pin[m] + h->h_pin[M + m];
   h->speed_valid = true;
+  return TAG_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+constexpr int kErrBlocks = 512, kErrThreads = 256;
+
+// Embedded error of one SSPRK43 step for every active variable:
+//   e = (u_new - (2 u3 - u_prev)) / 2,
+// u3 the stage value entering the last stage, taken before any stage limiter,
+// so that 2 u3 - u_prev = u_prev/3 + 2/3 (u2 + dt/2 f(u2)) and e = u_new - u^
+// with u^ the embedded second-order value; u_prev is the k register, which
+// holds the step's starting state in the SSP form.  Sums of squares of
+// e / (abstol + max(|u_prev|, |u_new|) reltol) per block, in a fixed order
+// (a fixed grid), then summed in block order by k_err_total.  Passive
+// variables do not change, so their terms are zero.
+__global__ void __launch_bounds__(kErrThreads) k_ssp43_error(
+    const double* __restrict__ u, const double* __restrict__ u3, const double* __restrict__ kprev,
+    long nodes, int nv, int na, double abstol, double reltol, double* __restrict__ partial) {
+  __shared__ double red[kErrThreads];
+  double acc = 0.0;
+  const long items = nodes * na;
+  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < items;
+       q += (long)gridDim.x * blockDim.x) {
+    const long node = q / na;
+    const int v = (int)(q % na);
+    const double un = u[node * nv + v], up = kprev[q];
+    const double e = 0.5 * (un - (2.0 * u3[node * nv + v] - up));
+    const double x = e / (abstol + fmax(fabs(up), fabs(un)) * reltol);
+    acc = fma(x, x, acc);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = kErrThreads / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+__global__ void k_err_total(double* __restrict__ partial, int n) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s = 0.0;
+  for (int b = 0; b < n; ++b) s += partial[b];
+  partial[n] = s;
+}
+
+// A rejected step: the active variables return to the step's starting state.
+__global__ void k_restore_active(double* __restrict__ u, const double* __restrict__ kprev,
+                                 long nodes, int nv, int na) {
+  const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nodes * na) return;
+  u[(q / na) * nv + q % na] = kprev[q];
+}
+
+// Root mean square of x(q) over n entries, summed in index order.
+template <class F>
+double rms_host(long n, F&& x) {
+  double s = 0.0;
+  for (long q = 0; q < n; ++q) {
+    const double v = x(q);
+    s += v * v;
+  }
+  return std::sqrt(s / (double)n);
+}
+
+// du = rhs(u) on the device through the handle's kernels (time t).
+int rhs_device(tag_handle h, double* u, double* du, double t) {
+  int rc = h->ops->interface(h, u);
+  if (rc) return rc;
+  return h->ops->element(h, kModeRhs, u, du, 0, false, t);
+}
+
+}  // namespace
+
+extern "C" {
+
+int tag_rk_adaptive(tag_handle h, double* t, double t_end, double abstol, double reltol,
+                    const double* stops, int32_t nstops, int64_t max_steps,
+                    tag_adaptive_stats* stats) {
+  if (!h || !t || !(t_end > *t) || !(abstol > 0.0) || !(reltol >= 0.0) || nstops < 0 ||
+      (nstops > 0 && !stops) || max_steps <= 0)
+    return fail(TAG_E_INVALID, "bad argument");
+  if (h->nmembers != 1) return fail(TAG_E_INVALID, "adaptive steps integrate a single mesh");
+  if (h->scheme != TAG_RK_SSPRK43)
+    return fail(TAG_E_INVALID, "select SSPRK43 with tag_set_time_integrator first");
+  for (int i = 1; i < nstops; ++i)
+    if (!(stops[i] > stops[i - 1])) return fail(TAG_E_INVALID, "stops must increase");
+  NvtxRange r_ad("adaptive SSPRK43");
+  int rc = autotune(h, h->d_u);
+  if (rc) return rc;
+  const long nodes = (long)h->nodes;
+  const int nv = h->nv, na = h->na;
+  const size_t bytes = sizeof(double) * (size_t)nodes * nv;
+  if (!h->d_u3) TAG_CUDA(cudaMalloc(&h->d_u3, bytes));
+  if (!h->d_tmp_du) TAG_CUDA(cudaMalloc(&h->d_tmp_du, bytes));
+  if (!h->d_err) TAG_CUDA(cudaMalloc(&h->d_err, sizeof(double) * (kErrBlocks + 1)));
+  const long N = nodes * nv;  // the ODE state has every variable, passive ones included
+  // controller constants (OrdinaryDiffEq's defaults for SSPRK43, order 3)
+  const double beta1 = 7.0 / 30.0, beta2 = 2.0 / 15.0, qmin = 0.2, qmax = 10.0, gamma = 0.9,
+               qoldinit = 1e-4;
+  double tt = *t;
+  // initial step (Hairer, Norsett, Wanner II.4, as OrdinaryDiffEq's
+  // ode_determine_initdt): two rhs evaluations, norms on the host
+  double dt;
+  {
+    std::vector<double> u0(N), f0(N), f1(N);
+    if ((rc = rhs_device(h, h->d_u, h->d_tmp_du, tt))) return rc;
+    TAG_CUDA(cudaMemcpyAsync(u0.data(), h->d_u, bytes, cudaMemcpyDeviceToHost, h->stream));
+    TAG_CUDA(cudaMemcpyAsync(f0.data(), h->d_tmp_du, bytes, cudaMemcpyDeviceToHost, h->stream));
+    TAG_CUDA(cudaStreamSynchronize(h->stream));
+    auto sk = [&](long q) { return abstol + std::fabs(u0[q]) * reltol; };
+    const double d0 = rms_host(N, [&](long q) { return u0[q] / sk(q); });
+    const double d1 = rms_host(N, [&](long q) { return f0[q] / sk(q); });
+    double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
+    dt0 = std::min(dt0, t_end - tt);
+    for (long q = 0; q < N; ++q) f1[q] = u0[q] + dt0 * f0[q];
+    TAG_CUDA(cudaMemcpyAsync(h->d_u3, f1.data(), bytes, cudaMemcpyHostToDevice, h->stream));
+    if ((rc = rhs_device(h, h->d_u3, h->d_tmp_du, tt + dt0))) return rc;
+    TAG_CUDA(cudaMemcpyAsync(f1.data(), h->d_tmp_du, bytes, cudaMemcpyDeviceToHost, h->stream));
+    TAG_CUDA(cudaStreamSynchronize(h->stream));
+    const double d2 = rms_host(N, [&](long q) { return (f1[q] - f0[q]) / sk(q); }) / dt0;
+    const double m = std::max(d1, d2);
+    const double dt1 =
+        m <= 1e-15 ? std::max(1e-6, dt0 * 1e-3) : std::pow(10.0, -(2.0 + std::log10(m)) / 3.0);
+    dt = std::min(std::min(100.0 * dt0, dt1), t_end - tt);
+  }
+  tag_adaptive_stats out{};
+  out.dt_first = dt;
+  double qold = qoldinit;
+  int next = 0;
+  const int ns = rk_stages(h->scheme);
+  while (tt < t_end) {
+    if (out.accepted + out.rejected >= max_steps) {
+      *t = tt;
+      if (stats) *stats = out;
+      return fail(TAG_E_INVALID, "adaptive steps: max_steps reached before t_end");
+    }
+    while (next < nstops && stops[next] <= tt) ++next;
+    const double stop = next < nstops ? std::min(stops[next], t_end) : t_end;
+    const double hdt = std::min(dt, stop - tt);
+    h->h_pin[0] = tt;
+    h->h_pin[1] = hdt;
+    TAG_CUDA(cudaMemcpyAsync(h->d_mscal, h->h_pin, sizeof(double) * 2, cudaMemcpyHostToDevice,
+                             h->stream));
+    for (int s = 0; s < ns; ++s) {
+      if ((rc = h->ops->interface(h, h->d_u))) return rc;
+      if ((rc = h->ops->element(h, kModeStage, h->d_u, nullptr, s, false, 0.0))) return rc;
+      if (s == ns - 2)
+        TAG_CUDA(cudaMemcpyAsync(h->d_u3, h->d_u, bytes, cudaMemcpyDeviceToDevice, h->stream));
+      if (h->has_limiter) {
+        NewtonArgs a = h->newton;
+        a.learned = h->newton_start;
+        a.mlp = h->d_mlp;
+        a.iters = nullptr;
+        a.counters = h->d_run_counters;
+        k_newton_rainy<<<(unsigned)((nodes + 255) / 256), 256, 0, h->stream>>>(h->d_u, nodes, a,
+                                                                                h->d_status);
+        TAG_CUDA(cudaGetLastError());
+        h->run_node_solves += nodes;
+      }
+    }
+    k_ssp43_error<<<kErrBlocks, kErrThreads, 0, h->stream>>>(h->d_u, h->d_u3, h->d_k, nodes, nv,
+                                                             na, abstol, reltol, h->d_err);
+    TAG_CUDA(cudaGetLastError());
+    k_err_total<<<1, 32, 0, h->stream>>>(h->d_err, kErrBlocks);
+    TAG_CUDA(cudaGetLastError());
+    TAG_CUDA(cudaMemcpyAsync(h->h_pin + 2, h->d_err + kErrBlocks, sizeof(double),
+                             cudaMemcpyDeviceToHost, h->stream));
+    TAG_CUDA(cudaStreamSynchronize(h->stream));
+    const double eest = std::sqrt(h->h_pin[2] / (double)N);
+    if (!std::isfinite(eest)) {
+      *t = tt;
+      if (stats) *stats = out;
+      return fail(TAG_E_INVALID, "adaptive steps: non-finite error estimate");
+    }
+    const double q11 = std::pow(eest, beta1);
+    if (eest <= 1.0) {
+      double q = eest == 0.0 ? 1.0 / qmax : q11 / std::pow(qold, beta2);
+      if (eest != 0.0) q = std::max(1.0 / qmax, std::min(1.0 / qmin, q / gamma));
+      tt = (hdt == stop - tt) ? stop : tt + hdt;
+      qold = std::max(eest, qoldinit);
+      dt = hdt / q;
+      out.dt_last = hdt;
+      ++out.accepted;
+    } else {
+      k_restore_active<<<(unsigned)((nodes * na + 255) / 256), 256, 0, h->stream>>>(
+          h->d_u, h->d_k, nodes, nv, na);
+      TAG_CUDA(cudaGetLastError());
+      dt = hdt / std::min(1.0 / qmin, q11 / gamma);
+      ++out.rejected;
+    }
+  }
+  TAG_CUDA(cudaStreamSynchronize(h->stream));
+  h->speed_valid = false;
+  *t = tt;
+  if (stats) *stats = out;
   return TAG_OK;
 }
 

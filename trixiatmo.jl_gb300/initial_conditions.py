@@ -84,6 +84,9 @@ def seeded_perturbation(u, equations, seed, amplitude=1e-2, velocity=5.0):
 EARTH_RADIUS = 6.37122e6                  # src/equations/reference_data.jl:11
 EARTH_GRAVITATIONAL_ACCELERATION = 9.80616  # :19
 EARTH_ROTATION_RATE = 7.292e-5            # :27
+SMALL_EARTH_SCALING = 20                  # :46
+SMALL_EARTH_RADIUS = EARTH_RADIUS / SMALL_EARTH_SCALING  # :53
+SMALL_EARTH_ROTATION_RATE = EARTH_ROTATION_RATE * SMALL_EARTH_SCALING  # :61
 SECONDS_PER_DAY = 8.64e4                  # :35
 
 
@@ -164,6 +167,31 @@ def initial_condition_baroclinic_instability(x, t, equations):
     v2 = np.cos(lon) * u - np.sin(lat) * np.sin(lon) * v
     v3 = np.cos(lat) * v
     phi = -EARTH_RADIUS ** 2 * EARTH_GRAVITATIONAL_ACCELERATION / r
+    return equations.prim2cons(rho, v1, v2, v3, p, phi)
+
+
+def initial_condition_vortex_shedding(x, t, equations):
+    """src/equations/initial_condition_compressible_euler_3d.jl:217-240 (DCMIP-2025
+    test case 2 on the small Earth): solid-body rotation with u0 = 20 m/s in a
+    stratified atmosphere of Brunt-Vaisala frequency N = 0.0182 1/s at
+    T = 288 K; phi = g z with z = max(r - a, 0), a = SMALL_EARTH_RADIUS."""
+    lon, lat, r = cartesian_to_sphere(x)
+    a = SMALL_EARTH_RADIUS
+    R = equations.c_p - equations.c_v
+    k = R / equations.c_p
+    u0 = 20.0
+    v1 = -u0 * np.cos(lat) * np.sin(lon)
+    v2 = u0 * np.cos(lat) * np.cos(lon)
+    v3 = np.zeros_like(r)
+    g = EARTH_GRAVITATIONAL_ACCELERATION
+    T = 288.0
+    om = SMALL_EARTH_ROTATION_RATE
+    z = np.maximum(r - a, 0.0)
+    phi = g * z
+    N = 0.0182
+    p = equations.p_0 * np.exp(-a * N ** 2 * u0 / (2 * g ** 2 * k) * (u0 / a + 2 * om) *
+                               (np.sin(lat) ** 2 - 1) - N ** 2 / (g ** 2 * k) * phi)
+    rho = p / (R * T)
     return equations.prim2cons(rho, v1, v2, v3, p, phi)
 
 

@@ -40,7 +40,8 @@ from .equations import (CompressibleEulerInternalEnergyEquationsWithGravity2D,
                         flux_chandrashekar, flux_ec_rain, flux_lax_friedrichs, flux_LMARS,
                         flux_nonconservative_waruszewski_etal, flux_ranocha, flux_zero)
 from .equations import BoundaryConditionDirichlet
-from .initial_conditions import EARTH_ROTATION_RATE, MountainWaveSetup
+from .initial_conditions import (EARTH_ROTATION_RATE, SMALL_EARTH_ROTATION_RATE,
+                                 MountainWaveSetup)
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)
@@ -71,6 +72,20 @@ class _SourceTerms:
 # `source_terms_coriolis` (src/equations/initial_condition_compressible_euler_3d.jl:257-269):
 # -2 Omega x rho v with Omega = EARTH_ROTATION_RATE about the z axis.
 source_terms_coriolis = _SourceTerms("source_terms_coriolis")
+# `source_terms_coriolis_small_earth` (:271-287): the same with SMALL_EARTH_ROTATION_RATE
+source_terms_coriolis_small_earth = _SourceTerms("source_terms_coriolis_small_earth")
+
+
+def _coriolis_rate(source_terms):
+    """Rotation rate of a Coriolis source term (0 for none), or None for any
+    other source term."""
+    if source_terms is None:
+        return 0.0
+    if source_terms is source_terms_coriolis:
+        return EARTH_ROTATION_RATE
+    if source_terms is source_terms_coriolis_small_earth:
+        return SMALL_EARTH_ROTATION_RATE
+    return None
 
 
 def _flux_ids(equations, solver, source_terms=None):
@@ -163,9 +178,9 @@ def _flux_ids(equations, solver, source_terms=None):
                              + (" or (flux_ec, a gravity term)" if equations.ndims == 2 else ""))
         params = [equations.c_p, equations.c_v, equations.g, sf[0].speed_of_sound, float(nc)]
         if equations.ndims == 3:
-            if source_terms not in (None, source_terms_coriolis):
+            if _coriolis_rate(source_terms) is None:
                 raise ValueError(f"unsupported source terms {source_terms}")
-            omega = EARTH_ROTATION_RATE if source_terms is source_terms_coriolis else 0.0
+            omega = _coriolis_rate(source_terms)
             return vid, _lib.TAG_SF_LMARS, params + [0.0, omega]
         if source_terms is not None and not isinstance(source_terms, MountainWaveSetup):
             raise ValueError(f"unsupported source terms {source_terms}")
@@ -176,9 +191,9 @@ def _flux_ids(equations, solver, source_terms=None):
             raise ValueError("volume flux must be (flux_ranocha, flux_nonconservative_waruszewski_etal)")
         if not (isinstance(sf, tuple) and isinstance(sf[0], FluxLMARS) and sf[1] is flux_zero):
             raise ValueError("surface flux must be (FluxLMARS(c), flux_zero)")
-        if source_terms not in (None, source_terms_coriolis):
+        if _coriolis_rate(source_terms) is None:
             raise ValueError(f"unsupported source terms {source_terms}")
-        omega = EARTH_ROTATION_RATE if source_terms is source_terms_coriolis else 0.0
+        omega = _coriolis_rate(source_terms)
         return _lib.TAG_VF_RANOCHA_WARUSZEWSKI, _lib.TAG_SF_LMARS, [
             equations.c_p, equations.c_v, equations.g, sf[0].speed_of_sound, omega]
     if source_terms is not None:
@@ -492,6 +507,33 @@ class SemidiscretizationHyperbolic:
                 else:
                     t = self.rk_steps(1, cfl=cfl, t=t, fixed_dt=fixed_dt, method=method)
         return t
+
+    def solve_adaptive(self, tspan, abstol=1e-6, reltol=1e-3, save_dt=None, max_steps=10 ** 7):
+        """Integrates the resident state over tspan with error-controlled
+        SSPRK43, as the reference's `solve(ode, SSPRK43(); abstol, reltol,
+        callback = CallbackSet(..., SaveSolutionCallback(dt = save_dt)))` does
+        without a StepsizeCallback (OrdinaryDiffEq's defaults abstol = 1e-6,
+        reltol = 1e-3).  The save times t0 + k * save_dt are stops that no step
+        passes.  Returns (t_end, dict of accepted / rejected steps and the
+        first and last dt)."""
+        if self.nmembers != 1:
+            raise ValueError("solve_adaptive integrates a single mesh")
+        t0, t_end = float(tspan[0]), float(tspan[1])
+        stops = []
+        if save_dt:
+            k = 1
+            while t0 + k * save_dt < t_end:
+                stops.append(t0 + k * save_dt)
+                k += 1
+        sp = np.ascontiguousarray(stops, dtype=np.float64)
+        _lib.check(self._L.tag_set_time_integrator(self._h, _RK_METHODS["SSPRK43"]))
+        t = ctypes.c_double(t0)
+        st = _lib.AdaptiveStats()
+        _lib.check(self._L.tag_rk_adaptive(self._h, ctypes.byref(t), t_end, float(abstol),
+                                           float(reltol), _ptr(sp) if sp.size else None,
+                                           int(sp.size), int(max_steps), ctypes.byref(st)))
+        return t.value, {"accepted": st.accepted, "rejected": st.rejected,
+                         "dt_first": st.dt_first, "dt_last": st.dt_last}
 
     # ---- analysis (AnalysisCallback), on the resident state ---------------------
     def integrate(self, func="cons2cons", normalize=True):
