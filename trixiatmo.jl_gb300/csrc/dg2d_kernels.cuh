@@ -276,10 +276,15 @@ __global__ void k_element(typename Phys::Params Pp, const BasisDev basis, double
       for (int v = 0; v < NA; ++v) eb[S::oC + ((d * nn + node) * n + 0) * NA + v] = F[v];
     }
   }
-  // --- phase 2: one thread per symmetric pair (a < b) on a line
+  // --- phase 2: one thread per symmetric pair (a < b) on a line, ordered by
+  //     direction first, so that the warps of a CTA with several elements
+  //     hold pairs of one direction (the logarithmic means' forms then agree
+  //     across a warp: horizontal pairs of a stratified atmosphere take the
+  //     short series, vertical ones the longer)
   if constexpr (VOL == kVolFluxDiff) for (int t = threadIdx.x; t < ne * S::P; t += nthr) {
-    const int el = t / S::P, p = t % S::P;
-    const int d = p / (n * npl), r = p % (n * npl);
+    const int per_dir = ne * n * npl;
+    const int d = t / per_dir, rd = t % per_dir;
+    const int el = rd / (n * npl), r = rd % (n * npl);
     const int line = r / npl;
     int q = r % npl, a = 0;
     while (q >= n - 1 - a) { q -= n - 1 - a; ++a; }

@@ -71,8 +71,8 @@ struct PhysEnergy2D {
   TAG_DEV static void volume_pair(const Params& P, const double* qa, const double* qb,
                                   double n1, double n2, double* Fa, double* Fb) {
     double rho_mean, inv_rho_p_mean;
-    ln_mean_pair_halved<false, false, true>(qa[0], qb[0], qa[5], qb[5], 0.0, 0.0, 0.0, 0.0,
-                                            rho_mean, inv_rho_p_mean);
+    ln_mean_pair_halved<true, false, true>(qa[0], qb[0], qa[5], qb[5], 0.0, 0.0, 0.0, 0.0,
+                                           rho_mean, inv_rho_p_mean);
     const double v1 = qa[1] + qb[1];
     const double v2 = qa[2] + qb[2];
     const double vn = fma(v2, n2, v1 * n1);  // 0.5 (vn_a + vn_b)

@@ -200,9 +200,8 @@ static __device__ __noinline__ void ln_mean_pair_halved_log(double sx, double dx
 // share its warp, and in a tall element's vertical lines, where the density
 // varies and the temperature hardly does, inv_ln_mean keeps its short form.
 // The branch tests compare the bit patterns of the non-negative f2 on the
-// integer pipe.  kShort pays where a warp's pairs share one direction (the 3D
-// kernel); in the 2D kernel a warp mixes horizontal and vertical pairs, and
-// the extra branches would diverge.
+// integer pipe.  kShort pays where a warp's pairs share one direction (both
+// element kernels order their pairs so).
 template <bool kShort = true, bool kLong = true, bool kLogsInline = false>
 TAG_DEV void ln_mean_pair_halved(double hxa, double hxb, double hya, double hyb, double Lxa,
                                  double Lxb, double Lya, double Lyb, double& rho_mean,
