@@ -249,27 +249,36 @@ __global__ void k_element3d(typename Phys::Params Pp, const BasisDev basis, doub
         }
         __syncwarp();
       }
+      // surface integral: the line's two end nodes lie on the element's faces
+      // 2d and 2d+1; their surface fluxes (face-local index (p1, p2)) are
+      // added to the same direction's accumulators, here rather than in the
+      // per-node phase where they would be a divergent branch
+      if (on) {
+        for (int end = slot; end < 2; end += S::S) {
+          const int a = end == 0 ? 0 : n - 1;
+          const int nd = d == 0 ? (p2 * n + p1) * n + a
+                                : (d == 1 ? (p2 * n + a) * n + p1 : (a * n + p2) * n + p1);
+          const double w = end == 0 ? sb->winv0 : sb->winvN;
+          const double* sf =
+              sfv + ((((size_t)(e_first + el) * 6 + 2 * d + end) * n + p2) * n + p1) * NA;
+          double* c = eb + S::oA + (d * nnn + nd) * NA;
+#pragma unroll
+          for (int v = 0; v < NA; ++v) c[v] = fma(sf[v], w, c[v]);
+        }
+      }
     }
   }
   __syncthreads();
 
-  // per (node, variable): direction sums, surface integral, Jacobian, sources,
-  // stage update
+  // per (node, variable): direction sums (surface integral included),
+  // Jacobian, sources, stage update
   for (int t = threadIdx.x; t < ne * nnn * NA; t += nthr) {
     const int el = t / (nnn * NA), r = t % (nnn * NA);
     const int node = r / NA, v = r % NA;
-    const int i = node % n, j = (node / n) % n, k = node / nn;
     const int e = e_first + el;
     double* eb = base + el * S::per_elem;
-    double acc = eb[S::oA + (0 * nnn + node) * NA + v] + eb[S::oA + (1 * nnn + node) * NA + v] +
-                 eb[S::oA + (2 * nnn + node) * NA + v];
-    const double* se = sfv + (size_t)e * 6 * nn * NA;
-    if (i == 0) acc += se[((0 * n + k) * n + j) * NA + v] * sb->winv0;
-    if (i == n - 1) acc += se[((1 * n + k) * n + j) * NA + v] * sb->winvN;
-    if (j == 0) acc += se[((2 * n + k) * n + i) * NA + v] * sb->winv0;
-    if (j == n - 1) acc += se[((3 * n + k) * n + i) * NA + v] * sb->winvN;
-    if (k == 0) acc += se[((4 * n + j) * n + i) * NA + v] * sb->winv0;
-    if (k == n - 1) acc += se[((5 * n + j) * n + i) * NA + v] * sb->winvN;
+    const double acc = eb[S::oA + (0 * nnn + node) * NA + v] +
+                       eb[S::oA + (1 * nnn + node) * NA + v] + eb[S::oA + (2 * nnn + node) * NA + v];
     const size_t gq = (size_t)e * nnn + node;
     const double dv = acc * (-invJ[gq]) + Phys::source(Pp, eb + S::oU + node * NV, v);
     if (not_finite(dv)) bad |= TAG_S_NAN;
