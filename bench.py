@@ -823,7 +823,8 @@ def run_ours(args):
             "data": "synthetic (seeded)",
             "config": {"workload": workload, "dofs": dofs, "elements": semi.nelements,
                        "polydeg": n - 1, "members": nmem,
-                       "elements_per_cta": semi.elements_per_block(), "l2": l2_note,
+                       "elements_per_cta": semi.elements_per_block(),
+                       "threads_per_cta": semi.cta_threads(), "l2": l2_note,
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "fp64", "achieved": achieved_tf, "peak": peak_fp64 / 1e12,
                          "unit": "TFLOP/s", "frac": achieved_tf / (peak_fp64 / 1e12),

@@ -412,9 +412,18 @@ int tag_status(tag_handle h, uint32_t* flags, int32_t clear);
  * their own work against the library's. */
 void* tag_stream(tag_handle h);
 
-/* Tuning knob: elements per CTA of the element kernel (0 = autotune). */
+/* Tuning knob: elements per CTA of the element kernel (0 = autotune).  The
+ * autotuner, run on the first step or rhs call, times the element kernel for
+ * elements per CTA in {1, 2, 3, 4, 6, 8, 12, 16} (the shared-memory tile: each
+ * element's state, metric terms and accumulators staged once) and, for each,
+ * one or two work items per thread and phase (the CTA width), and keeps the
+ * fastest; setting a value here fixes the tile with one item per thread. */
 int tag_set_elements_per_block(tag_handle h, int32_t epb);
 int tag_get_elements_per_block(tag_handle h, int32_t* epb);
+/* Fixes the tile: epb elements per CTA, 1 or 2 work items per thread and phase. */
+int tag_set_tile(tag_handle h, int32_t epb, int32_t items_per_thread);
+/* Threads per CTA of the element kernel for the current tile (measurement). */
+int tag_get_cta_threads(tag_handle h, int32_t* threads);
 
 /* Geometry of the cubed-sphere shell built on the device: what TrixiAtmo's
  * P4estMeshCubedSphereTopography(trees, layers, inner_radius, thickness;

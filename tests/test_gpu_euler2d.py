@@ -111,9 +111,21 @@ def test_rhs_independent_of_elements_per_block_and_deterministic(tg, gpu_lib):
         semi.set_elements_per_block(epb)
         outs.append(semi.rhs(u))
         outs.append(semi.rhs(u))
+    # the autotuner's other dimension: two work items per thread and phase
+    for epb in (4, 8, 16):
+        semi.set_tile(epb, 2)
+        assert semi.cta_threads() < semi_threads_full(semi, epb)
+        outs.append(semi.rhs(u))
     for o in outs[1:]:
         assert np.array_equal(o, outs[0])
     semi.close()
+
+
+def semi_threads_full(semi, epb):
+    semi.set_tile(epb, 1)
+    full = semi.cta_threads()
+    semi.set_tile(epb, 2)
+    return full
 
 
 def test_max_dt_matches_oracle(tg, orc, gpu_lib):

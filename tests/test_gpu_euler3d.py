@@ -72,6 +72,9 @@ def test_rhs3d_independent_of_elements_per_block(tg, gpu_lib):
         semi.set_elements_per_block(epb)
         outs.append(semi.rhs(u))
         outs.append(semi.rhs(u))
+    for epb in (1, 2):  # half-width CTAs: each warp takes two groups of lines
+        semi.set_tile(epb, 2)
+        outs.append(semi.rhs(u))
     for o in outs[1:]:
         assert np.array_equal(o, outs[0])
     semi.close()

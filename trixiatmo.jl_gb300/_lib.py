@@ -134,6 +134,8 @@ SIGNATURES = {
                                         ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                         ctypes.POINTER(ctypes.c_double), ctypes.c_int32,
                                         ctypes.c_int64, ctypes.c_void_p]),
+    "tag_get_cta_threads": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]),
+    "tag_set_tile": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
     "tag_set_time_integrator": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "tag_set_boundary_values": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "tag_set_source": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp, ctypes.c_int32]),

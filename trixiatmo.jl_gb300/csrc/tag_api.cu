@@ -64,6 +64,10 @@ struct Ops;
 
 void tag::set_last_error(const std::string& msg) { g_last_error = msg; }
 
+// Threads of an element-kernel CTA: `items` work items split `div` ways,
+// rounded up to whole warps.
+inline int cta_threads(int items, int div) { return ((items + div - 1) / div + 31) / 32 * 32; }
+
 struct tag_handle_s {
   int eq = 0, n = 0, nelem = 0, nif = 0, nbd = 0, nv = 0, na = 0;
   int dim = 2, npe = 0, nface = 4, jpn = 4;  // nodes per element, faces, Ja doubles per node
@@ -72,6 +76,7 @@ struct tag_handle_s {
                                              // the kernels reduce n-scaled speeds
   // covariant equations: element groups, geometry, packed element data
   CovParams p_cov{};
+
   CovGroups h_groups{};
   CovGroups* d_groups = nullptr;
   BasisDev* d_bases = nullptr;
@@ -120,6 +125,9 @@ struct tag_handle_s {
   int graph_epb = -1;
   bool speed_valid = false;
   int epb = 0;
+  // threads of a CTA = its elements' work items / tile_div, rounded up to
+  // whole warps (1 or 2: one or two items per thread and phase)
+  int tile_div = 1;
   const Ops* ops = nullptr;
   // analysis (allocated by the first analysis call)
   bool an_ready = false;
@@ -205,7 +213,7 @@ struct OpsImpl {
                      double t) {
     const int epb = h->epb > 0 ? h->epb : 4;
     const int blocks = (h->nelem + epb - 1) / epb;
-    const int threads = std::min(cap(), epb * S::TPE);
+    const int threads = std::min(cap(), cta_threads(epb * S::TPE, h->tile_div));
     const size_t smem = S::bytes(epb);
     StageArgs st{};
     st.member = h->d_member;
@@ -288,7 +296,7 @@ struct OpsImpl3D {
                      double) {
     const int epb = h->epb > 0 ? h->epb : 1;
     const int blocks = (h->nelem + epb - 1) / epb;
-    const int threads = std::min(cap(), ((epb * S::TPE + 31) / 32) * 32);
+    const int threads = std::min(cap(), cta_threads(epb * S::TPE, h->tile_div));
     const size_t smem = S::bytes(epb);
     StageArgs st{};
     st.member = h->d_member;
@@ -429,7 +437,8 @@ int stage_sequence(tag_handle h) {
 }
 
 int build_graph(tag_handle h) {
-  if (h->graph && h->graph_epb == h->epb) return TAG_OK;
+  const int key = h->epb * 8 + h->tile_div;
+  if (h->graph && h->graph_epb == key) return TAG_OK;
   if (h->graph) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
@@ -442,13 +451,15 @@ int build_graph(tag_handle h) {
   if (e2 != cudaSuccess) return fail(TAG_E_CUDA, cudaGetErrorString(e2));
   TAG_CUDA(cudaGraphInstantiate(&h->graph, g, 0));
   cudaGraphDestroy(g);
-  h->graph_epb = h->epb;
+  h->graph_epb = key;
   return TAG_OK;
 }
 
-// Times the element kernel (rhs mode, on the state `u`) for candidate
-// elements-per-CTA values and keeps the fastest.  The trial launches' status
-// bits are discarded.
+// Times the element kernel (rhs mode, on the state `u`) for candidate tiles
+// and keeps the fastest: elements per CTA (the shared-memory tile, each
+// element's state, metric terms and accumulators staged once) times threads
+// per CTA (one or two work items per thread and phase).  The trial launches'
+// status bits are discarded.
 int autotune(tag_handle h, const double* u) {
   if (h->epb > 0) return TAG_OK;
   int dev;
@@ -459,13 +470,16 @@ int autotune(tag_handle h, const double* u) {
   cudaEvent_t a, b;
   TAG_CUDA(cudaEventCreate(&a));
   TAG_CUDA(cudaEventCreate(&b));
-  int best = 1;
+  int best = 1, best_div = 1;
   float best_ms = 1e30f;
   const int cands[] = {1, 2, 3, 4, 6, 8, 12, 16};
-  for (int c : cands) {
+  for (int trial = 0; trial < 16; ++trial) {
+    const int c = cands[trial >> 1], div = 1 + (trial & 1);
     if ((size_t)h->ops->smem_bytes(c) > (size_t)max_smem) continue;
     if (c * h->ops->threads_per_element > h->ops->max_threads() && c > 1) continue;
+    if (div == 2 && c * h->ops->threads_per_element < 128) continue;
     h->epb = c;
+    h->tile_div = div;
     double* uu = const_cast<double*>(u);
     int rc = h->ops->interface(h, uu);
     if (rc) return rc;
@@ -482,11 +496,13 @@ int autotune(tag_handle h, const double* u) {
     if (ms < best_ms) {
       best_ms = ms;
       best = c;
+      best_div = div;
     }
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   h->epb = best;
+  h->tile_div = best_div;
   TAG_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned), h->stream));
   return TAG_OK;
 }
@@ -1670,12 +1686,31 @@ int tag_set_elements_per_block(tag_handle h, int32_t epb) {
       return fail(TAG_E_INVALID, "elements per block too large for one CTA");
   }
   h->epb = epb;
+  h->tile_div = 1;
   return TAG_OK;
 }
 
 int tag_get_elements_per_block(tag_handle h, int32_t* epb) {
   if (!h || !epb) return fail(TAG_E_INVALID, "null argument");
   *epb = h->epb;
+  return TAG_OK;
+}
+
+int tag_set_tile(tag_handle h, int32_t epb, int32_t items_per_thread) {
+  if (!h || epb < 1 || items_per_thread < 1 || items_per_thread > 2)
+    return fail(TAG_E_INVALID, "bad argument");
+  int rc = tag_set_elements_per_block(h, epb);
+  if (rc) return rc;
+  h->tile_div = items_per_thread;
+  return TAG_OK;
+}
+
+int tag_get_cta_threads(tag_handle h, int32_t* threads) {
+  if (!h || !threads) return fail(TAG_E_INVALID, "null argument");
+  const int epb = h->epb > 0 ? h->epb : 1;
+  *threads = h->ops ? std::min(h->ops->max_threads(),
+                               cta_threads(epb * h->ops->threads_per_element, h->tile_div))
+                    : 0;
   return TAG_OK;
 }
 

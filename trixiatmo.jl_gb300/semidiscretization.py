@@ -669,6 +669,16 @@ class SemidiscretizationHyperbolic:
         _lib.check(self._L.tag_get_elements_per_block(self._h, ctypes.byref(v)))
         return v.value
 
+    def set_tile(self, epb, items_per_thread=1):
+        """Fixes the element kernel's tile (otherwise autotuned)."""
+        _lib.check(self._L.tag_set_tile(self._h, int(epb), int(items_per_thread)))
+
+    def cta_threads(self):
+        """Threads per CTA of the element kernel for the current tile."""
+        v = ctypes.c_int32()
+        _lib.check(self._L.tag_get_cta_threads(self._h, ctypes.byref(v)))
+        return v.value
+
 
 class SemidiscretizationEnsemble(SemidiscretizationHyperbolic):
     """Independent ensemble members (same equations and solver; each member its
