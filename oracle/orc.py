@@ -113,6 +113,11 @@ def lib():
                                               ctypes.c_double, ctypes.c_int, _dp]
         L.orc_pt3d_ssprk43_adaptive.restype = ctypes.c_double
         L.orc_pt3d_ssprk43_adaptive.argtypes = L.orc_pt_ssprk43_adaptive.argtypes
+        L.orc_rainy_ssprk43_adaptive.restype = ctypes.c_double
+        L.orc_rainy_ssprk43_adaptive.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double,
+                                                 ctypes.c_double, _dp, ctypes.c_int,
+                                                 ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                                 ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp]
         L.orc_pt_ck_steps.restype = ctypes.c_double
         L.orc_pt_ck_steps.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_int]
@@ -735,6 +740,17 @@ class Rainy2D:
         tot = lib().orc_rainy_newton(self.h, _p(u), mode, tol, maxit, polish, g, _ip(iters),
                                      ctypes.byref(nf))
         return tot, iters, nf.value
+
+    def ssprk43_adaptive(self, u, t, t_end, abstol=1e-6, reltol=1e-3, stops=(), variant=0,
+                         mode=0, tol=1e-9, maxit=20):
+        """Adaptive SSPRK43 with the Newton stage limiter after every stage
+        (see PotTemp2D.ssprk43_adaptive)."""
+        st = np.zeros(5)
+        sp = np.ascontiguousarray(stops, dtype=np.float64)
+        tf = lib().orc_rainy_ssprk43_adaptive(self.h, _p(u), t, t_end,
+                                              _p(sp) if sp.size else None, int(sp.size), abstol,
+                                              reltol, variant, mode, tol, maxit, _p(st))
+        return tf, dict(zip(("accepted", "rejected", "rhs_calls", "dt_first", "dt_last"), st))
 
     def ck_steps(self, u, k, t, cfl, nsteps, fixed_dt=0.0, mode=0, tol=1e-9, maxit=20,
                  t_end=0.0):

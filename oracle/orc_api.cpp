@@ -1227,6 +1227,31 @@ double orc_rainy_ssp_steps(void* h, double* u, double t, double cfl, int nsteps,
                    u, c->ndofs() * 9, t, cfl, nsteps, scheme, fixed_dt, t_end);
 }
 
+// Adaptive SSPRK43 (orc_time.hpp) on a rainy case with the Newton stage
+// limiter (mode, tol, maxit) after every stage, as SSPRK43(; stage_limiter!)
+// applies NonlinearSolveDG; stats as orc_pt_ssprk43_adaptive.
+double orc_rainy_ssprk43_adaptive(void* h, double* u, double t, double t_end,
+                                  const double* stops, int nstops, double abstol, double reltol,
+                                  int variant, int mode, double tol, int maxit, double* stats) {
+  auto* c = static_cast<RainyCase*>(h);
+  AdaptiveStats st;
+  const double tf = ssprk43_adaptive(
+      [&](const double* uu, double* dd, double tt) { c->dg->rhs(uu, dd, tt); },
+      [&](double* v) {
+        long nf;
+        orc_rainy_newton(h, v, mode, tol, maxit, 0, nullptr, nullptr, &nf);
+      },
+      u, c->ndofs() * 9, t, t_end, stops, nstops, abstol, reltol, variant, &st);
+  if (stats) {
+    stats[0] = (double)st.accepted;
+    stats[1] = (double)st.rejected;
+    stats[2] = (double)st.rhs_calls;
+    stats[3] = st.dt_first;
+    stats[4] = st.dt_last;
+  }
+  return tf;
+}
+
 // Pointwise helpers for tests: flux_ec_rain, flux_llf, residual, Jacobian.
 void orc_rainy_flux_ec(const double* ul, const double* ur, const double* n, double* f) {
   RainyEuler2D eq;

@@ -132,3 +132,66 @@ def test_rainy_lmars_and_pressure_wall(orc):
         assert np.allclose(f, [0, 0, 0, p * n[0], p * n[1], 0, 0, 0, 0], rtol=1e-14, atol=1e-12)
         w = orc.rainy_slip_wall(u, n)
         assert np.allclose(w, [0, 0, 0, p * n[0], p * n[1], 0, 0, 0, 0], rtol=1e-14, atol=1e-12)
+
+
+# test/test_2d_rainy_euler.jl:79-114: examples/euler/precipitation/buoyancy/
+# elixir_hoeck_bubble.jl on 16x16 cells of 2.4 km x 2.4 km, polydeg 3,
+# flux_lax_friedrichs / flux_ec_rain, source_terms_rainy, simple slip walls,
+# periodic in x, to t = 10 s with error-controlled SSPRK43 at OrdinaryDiffEq's
+# default tolerances and the NonlinearSolveDG stage limiter (tolerance 1e-9,
+# 20 iterations) after every stage.  The initial state (AtmosphereLayersRainyBubble
+# and the per-node solve of initial_condition_bubble_rainy) is computed by a
+# Newton iteration to the root's last bits where the reference calls NLsolve.
+# Measured against the goldens: l2 within 1e-6 relative and linf within 2.1e-5
+# for every variable except the rain density, whose norms are 1e-9 (l2) and
+# 2e-8 (linf) and agree to 1.1e-13 and 1.2e-11 absolute; the step-size controller
+# is restated (see tests/test_oracle_pt.py), so the agreement is that of the
+# step sequence.
+HOECK_RAIN_GOLDEN = (
+    [7.959523735914366e-5, 4.8983178144498016e-5, 1.2695889115092138e-9, 0.019951374355214414,
+     0.033830586959875855, 126.25361431033272, 4.899300381610471e-5, 3.4512985541873764e-7,
+     0.0016455875546178209],
+    [0.0011817049726382534, 0.0007153644712404369, 2.0653953346431095e-8, 0.12229462313083396,
+     0.1760334548347, 1831.4029281113471, 0.0007153644712404369, 6.113680304613196e-6,
+     0.008505948056836132])
+_RAIN_LAYERS = {}
+
+
+def hoeck_rain_setup(tg):
+    """(equations, initial condition, mesh, basis, xy, invJ, oracle mesh arrays)."""
+    from trixiatmo_gb300.initial_conditions import (AtmosphereLayersRainyBubble,
+                                                    initial_condition_bubble_rainy)
+    eq = tg.CompressibleRainyEulerEquations2D()
+    if "layers" not in _RAIN_LAYERS:
+        _RAIN_LAYERS["layers"] = AtmosphereLayersRainyBubble(eq, total_height=2401.0)
+    layers = _RAIN_LAYERS["layers"]
+
+    def ic(x, t, equations):
+        return initial_condition_bubble_rainy(x, t, equations, layers)
+    mesh = tg.StructuredMesh((16, 16), (0.0, 0.0), (2400.0, 2400.0), periodicity=(True, False))
+    basis = tg.LobattoLegendreBasis(3)
+    xy, Ja, invJ = mesh.geometry(basis)
+    ie, ifc, fl, be, bf = mesh.connectivity().arrays()
+    bk = np.zeros(len(be), dtype=np.int32)
+    return eq, ic, mesh, basis, xy, invJ, (xy, Ja, invJ, ie, ifc, fl, be, bf, bk)
+
+
+def check_hoeck_rain(l2, linf):
+    g2, gi = HOECK_RAIN_GOLDEN
+    for v in range(9):
+        if v == 2:
+            assert abs(l2[v] - g2[v]) <= 1e-12 and abs(linf[v] - gi[v]) <= 2e-11, (v, l2[v], linf[v])
+        else:
+            assert abs(l2[v] / g2[v] - 1) <= 2e-6, ("l2", v, l2[v], g2[v])
+            assert abs(linf[v] / gi[v] - 1) <= 5e-5, ("linf", v, linf[v], gi[v])
+
+
+def test_oracle_hoeck_precipitation_bubble_golden(tg, orc):
+    import analysis
+    eq, ic, mesh, basis, xy, invJ, arrays = hoeck_rain_setup(tg)
+    c = orc.Rainy2D(3, 0, 0, 0, 0, 0, 0, source_kind=0, mesh=arrays, surface=0, wall=0)
+    u = np.ascontiguousarray(ic(xy, 0.0, eq))
+    t, st = c.ssprk43_adaptive(u, 0.0, 10.0, mode=0, tol=1e-9, maxit=20)
+    assert t == 10.0 and st["accepted"] > 100
+    l2, linf = analysis.error_norms(u, xy, invJ, basis.nodes, lambda x: ic(x, 0.0, eq), 2)
+    check_hoeck_rain(l2, linf)

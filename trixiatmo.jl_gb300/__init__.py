@@ -33,6 +33,7 @@ from .initial_conditions import (EARTH_GRAVITATIONAL_ACCELERATION, EARTH_RADIUS,
                                  EARTH_ROTATION_RATE, SMALL_EARTH_RADIUS,
                                  SMALL_EARTH_ROTATION_RATE, SMALL_EARTH_SCALING,
                                  initial_condition_vortex_shedding,
+                                 AtmosphereLayersRainyBubble, initial_condition_bubble_rainy,
                                  IsothermalShell, MoistBubbleRainy,
                                  WarmBubble, initial_condition_convergence_test_rainy,
                                  initial_condition_baroclinic_instability,
@@ -64,6 +65,7 @@ __all__ = [
     "initial_condition_baroclinic_instability", "P4estMeshCubedSphereTopography",
     "source_terms_coriolis", "source_terms_coriolis_small_earth", "SMALL_EARTH_RADIUS",
     "SMALL_EARTH_ROTATION_RATE", "SMALL_EARTH_SCALING", "initial_condition_vortex_shedding",
+    "AtmosphereLayersRainyBubble", "initial_condition_bubble_rainy",
     "fp64_peak", "CompressibleRainyEulerEquations2D",
     "VolumeIntegralWeakForm", "boundary_condition_simple_slip_wall", "flux_ec_rain",
     "flux_lax_friedrichs", "source_terms_convergence_test_rainy", "source_terms_rainy",

@@ -576,3 +576,134 @@ def initial_condition_moist_bubble_rainy(atmosphere_layers, moist_equations):
                          s[..., 6]], axis=-1)
 
     return ic
+
+
+# ---- the rainy bubble with precipitation (elixir_hoeck_bubble.jl) ------------
+def _theta_d_rainy(z, eq):
+    """Hydrostatic dry potential temperature of the rainy bubble
+    (src/equations/compressible_rainy_euler_2d.jl:1062-1078): 283 K at 850 hPa,
+    stratification 1.3e-5 1/m."""
+    theta0 = 283.0 * (eq.ref_pressure / 85000.0) ** (eq.R_d / eq.c_pd)
+    return theta0 * np.exp(1.3e-5 * z)
+
+
+def _complex_step_newton(residual, y, scale, tol_rel=4e-16, maxit=60):
+    """Newton's method on independent small systems y[..., k] (k unknowns per
+    point) with the Jacobian by complex steps (exact to rounding), iterated to
+    the root's last bits.  The reference's NLsolve stops at a residual
+    tolerance; both find the same isolated root."""
+    y = np.array(y, dtype=np.float64)
+    k = y.shape[-1]
+    h = 1e-30
+    eye = np.eye(k)
+    norm = lambda F: np.abs(F).max(axis=-1)  # noqa: E731
+    for _ in range(maxit):
+        F = residual(y)
+        yc = y[..., None, :] + 1j * h * (scale[..., None, :] * eye)
+        # row c of the complex evaluation perturbs unknown c: dF/dy_c * h * scale_c
+        J = np.swapaxes(residual(yc).imag / (h * scale[..., :, None]), -1, -2)
+        step = np.linalg.solve(J, -F[..., None])[..., 0]
+        # halve the step where it does not reduce the residual (far from the root)
+        lam = np.ones(y.shape[:-1])
+        for _ in range(30):
+            Fn = residual(y + lam[..., None] * step)
+            bad = ~(np.isfinite(Fn).all(axis=-1) & ((norm(Fn) < norm(F)) | (norm(F) < 1e-12)))
+            if not np.any(bad):
+                break
+            lam = np.where(bad, 0.5 * lam, lam)
+        y = y + lam[..., None] * step
+        if np.all(np.abs(lam[..., None] * step) <= tol_rel * np.abs(y)):
+            break
+    return y
+
+
+class AtmosphereLayersRainyBubble:
+    """Hydrostatic background of the rainy bubble
+    (src/equations/compressible_rainy_euler_2d.jl:1087-1129): layer_data[i] =
+    (p, rho_dry, rho_vapour, T) at z = 0.01 + i * precision, each layer solving
+    the discrete hydrostatic balance (p - p_below)/dz + (rho_dry + rho_vapour) g
+    = 0, the gas law, the dry potential temperature profile and 20 % relative
+    humidity from the layer below (the surface layer with dz = 0.01 from
+    (850 hPa, 1.4, 0.04, 300 K))."""
+
+    def __init__(self, equations, total_height, precision=1.0):
+        eq = equations
+        self.total_height = float(total_height)
+        self.precision = float(precision)
+        n = int(round(self.total_height / self.precision))
+        h0 = 0.2
+        data = np.zeros((n + 1, 4))
+        z, dz = 0.01, 0.01
+        guess = np.array([85000.0, 1.4, 0.04, 300.0])
+        data[0] = self._solve(eq, guess, 85000.0, h0, z, dz)
+        dz = self.precision
+        for i in range(n):
+            z += dz
+            data[i + 1] = self._solve(eq, data[i], data[i, 0], h0, z, dz)
+        self.layer_data = data
+
+    @staticmethod
+    def _solve(eq, guess, p_below, h0, z, dz):
+        eps = eq.R_d / eq.R_v
+        th = _theta_d_rainy(z, eq)
+
+        def res(y):
+            p, rd, rv, T = y[..., 0], y[..., 1], y[..., 2], y[..., 3]
+            rvs = eq.saturation_vapour_pressure(T) / (eq.R_v * T)
+            return np.stack([(p - p_below) / dz + (rd + rv) * eq.gravity,
+                             p - T * (rd * eq.R_d + rv * eq.R_v),
+                             th - T * (eq.ref_pressure / p) ** (eq.R_d / eq.c_pd),
+                             (rvs * (rd + rv / eps) * h0 - rv * (rd + rvs / eps)) * 1000.0],
+                            axis=-1)
+        y = np.asarray(guess, dtype=np.float64)
+        return _complex_step_newton(res, y, np.abs(y) + 1e-3)
+
+
+def initial_condition_bubble_rainy(x, t, equations, atmosphere_layers):
+    """src/equations/compressible_rainy_euler_2d.jl:1131-1202: a humid bubble
+    (relative humidity 1 inside r = 200 m, a cos^2 ramp to the background 0.2 at
+    r = 300 m around (1200 m, 800 m)) in the hydrostatic background; per node
+    the pressure is interpolated between the layers around z and
+    (rho_dry, rho_vapour, T) solve the humidity, dry potential temperature and
+    pressure equations from the lower layer's values.  State (rho_dry,
+    rho_vapour, 0, 0, 0, energy, rho_vapour, 0, T), all moisture as vapour."""
+    eq = equations
+    x = np.asarray(x, dtype=np.float64)
+    r = np.sqrt((x[..., 0] - 1200.0) ** 2 + (x[..., 1] - 800.0) ** 2)
+    hb = 0.2
+    hum = np.where(r > 300.0, hb,
+                   np.where(r > 200.0,
+                            hb + (1.0 - hb) * np.cos(np.pi * (r - 200.0) / (2 * 100.0)) ** 2,
+                            1.0))
+    L = atmosphere_layers
+    dz = L.precision
+    z = x[..., 1]
+    n = np.floor((z + np.finfo(np.float64).eps) / dz).astype(np.int64) + 1  # Julia's 1-based row
+    z_lower = (n - 1) * dz
+    z_upper = n * dz
+    top = z_lower == L.total_height
+    z_upper = np.where(top, z_lower + dz, z_upper)
+    n = np.where(top, n - 1, n)
+    n = np.where(n == 0, 1, n)
+    if np.any(z > L.total_height + 1e-9 * L.total_height):
+        raise ValueError("The atmosphere does not match the simulation domain")
+    lo, up = L.layer_data[n - 1], L.layer_data[n]
+    p_h = (up[..., 0] * (z - z_lower) + lo[..., 0] * (z_upper - z)) / dz
+    eps = eq.R_d / eq.R_v
+    th = _theta_d_rainy(z, eq)
+
+    def res(y):
+        rd, rv, T = y[..., 0], y[..., 1], y[..., 2]
+        # the node fields broadcast over the Jacobian's extra axis
+        b = lambda a: a.reshape(a.shape + (1,) * (rd.ndim - a.ndim))  # noqa: E731
+        rvs = eq.saturation_vapour_pressure(T) / (eq.R_v * T)
+        p = (rd * eq.R_d + rv * eq.R_v) * T
+        return np.stack([(rvs * (rd + rv / eps) * b(hum) - rv * (rd + rvs / eps)) * 30.0,
+                         b(th) - T * (eq.ref_pressure / b(p_h)) ** (eq.R_d / eq.c_pd),
+                         b(p_h) - p], axis=-1)
+    y0 = lo[..., 1:4].copy()
+    y = _complex_step_newton(res, y0, np.abs(y0) + 1e-3)
+    rd, rv, T = y[..., 0], y[..., 1], y[..., 2]
+    energy = (eq.c_vd * rd + eq.c_vv * rv) * T + rv * eq.ref_latent_heat_vap_temp
+    zero = np.zeros_like(rd)
+    return np.stack([rd, rv, zero, zero, zero, energy, rv, zero, T], axis=-1)
