@@ -255,3 +255,43 @@ def test_pt_time_dependent_dirichlet_states(tg, orc, gpu_lib):
         du, du_ref = semi.rhs(u, t), c.rhs(u, t)
         assert np.abs(du - du_ref).max() <= 1e-12 * np.abs(du_ref).max(), t
     semi.close()
+
+
+def test_adaptive_steps_argument_checks_and_stops(tg, orc, gpu_lib):
+    """tag_rk_adaptive refuses what it does not define (a non-SSPRK43 scheme,
+    decreasing stops, max_steps exhausted) with TAG_E_INVALID and leaves the
+    state usable; with stops it lands on each of them (as the reference's
+    SaveSolutionCallback tstops) and on t_end, close to the oracle's run."""
+    import ctypes
+    eq, mesh, semi = make_pt(tg, 8, 6, 3)
+    u0 = semi.compute_coefficients()
+    semi.set_state(u0)
+    L, h = semi._L, semi._h
+    t = ctypes.c_double(0.0)
+    st = tg._lib.AdaptiveStats()
+    dp = ctypes.POINTER(ctypes.c_double)
+    _lib = tg._lib
+    assert L.tag_set_time_integrator(h, _lib.TAG_RK_CK2N54) == 0
+    assert L.tag_rk_adaptive(h, ctypes.byref(t), 10.0, 1e-6, 1e-3, None, 0, 100,
+                             ctypes.byref(st)) == _lib.TAG_E_INVALID
+    assert L.tag_set_time_integrator(h, _lib.TAG_RK_SSPRK43) == 0
+    bad = np.array([5.0, 2.0])
+    assert L.tag_rk_adaptive(h, ctypes.byref(t), 10.0, 1e-6, 1e-3, bad.ctypes.data_as(dp), 2,
+                             100, ctypes.byref(st)) == _lib.TAG_E_INVALID
+    assert L.tag_rk_adaptive(h, ctypes.byref(t), 1000.0, 1e-6, 1e-3, None, 0, 2,
+                             ctypes.byref(st)) == _lib.TAG_E_INVALID
+    assert st.accepted + st.rejected == 2 and 0.0 < t.value < 1000.0
+    # a fresh run with stops every 7 s to 60 s, against the oracle's
+    semi.set_state(u0)
+    tf, s = semi.solve_adaptive((0.0, 60.0), save_dt=7.0)
+    assert tf == 60.0
+    c = orc.PotTemp2D(3, 8, 6, 0.0, 300000.0, 0.0, 10000.0, periodic_x=True, periodic_y=False,
+                      volume=0, nc=0, g=9.80616, c_lmars=C_LMARS)
+    uo = np.ascontiguousarray(u0).copy()
+    to, so = c.ssprk43_adaptive(uo, 0.0, 60.0, stops=np.arange(7.0, 60.0, 7.0))
+    # a step that ends just short of a stop adds a short one, decided by the
+    # error norm's last bits: the counts agree to a step or two
+    assert to == 60.0 and abs(s["accepted"] - so["accepted"]) <= 2, (s, so)
+    u = semi.get_state()
+    assert np.abs(u[..., :4] - uo[..., :4]).max() <= 1e-7 * np.abs(uo[..., :4]).max()
+    semi.close()
