@@ -15,7 +15,7 @@ struct PhysEnergy3D {
   // log(beta/2) (odd stride); the halved rho and beta feed ln_mean_pair_halved
   static constexpr int NQ = 9;
   static constexpr int kRho = 0, kBeta = 6, kLogRho = 7, kLogBeta = 8;
-  // the sixteen-term series keeps every pair of a tall shell element (km-sized
+  // the polynomial forms up to f2 = 0.09 keep every pair of a tall shell element (km-sized
   // vertical node spacing) out of the logarithms; only elements whose values
   // spread further take logarithms, once per node
   static constexpr bool kNodeLogs = true;

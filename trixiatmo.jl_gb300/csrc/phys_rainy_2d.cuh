@@ -119,11 +119,19 @@ struct PhysRainy2D {
     const double rv_avg = 0.5 * (a[5] + b[5]);
     const double rc_avg = 0.5 * (a[6] + b[6]);
     const double rr_avg = 0.5 * (a[2] + b[2]);
-    const double rd_log = (a[0] != 0.0 && b[0] != 0.0) ? ln_mean_single(a[0], b[0]) : 0.0;
+    // ln_mean of the dry densities, inv_ln_mean of 1/T and 1/(1/T_a + 1/T_b)
+    // (= 1/(2 iT_avg), the pressure's divisor) from one shared reciprocal
+    double rd_log, iT_log, i_sum;
+    if (a[0] != 0.0 && b[0] != 0.0) {
+      ln_mean_pair<false, true>(a[0], b[0], a[8], b[8], 0.0, 0.0, 0.0, 0.0, rd_log, iT_log,
+                                &i_sum);
+    } else {
+      rd_log = 0.0;
+      iT_log = inv_ln_mean_single(a[8], b[8]);
+      i_sum = 1.0 / (a[8] + b[8]);
+    }
     const double rv_log = (a[5] != 0.0 && b[5] != 0.0) ? ln_mean_single(a[5], b[5]) : 0.0;
-    const double iT_avg = 0.5 * (a[8] + b[8]);
-    const double iT_log = inv_ln_mean_single(a[8], b[8]);
-    const double p_int = (C::R_d * rd_avg + C::R_v * rv_avg) / iT_avg;
+    const double p_int = (C::R_d * rd_avg + C::R_v * rv_avg) * (2.0 * i_sum);
     const double f_v = rv_log * vdn;
     const double f_c = rc_avg * vdn;
     const double f_d = rd_log * vdn;

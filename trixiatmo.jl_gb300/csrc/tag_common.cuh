@@ -140,13 +140,16 @@ static __device__ __noinline__ void ln_mean_pair_log(double sx, double dx, doubl
 // kShort: take the four-term series below kShortF2.  Worth it only where a
 // warp's pairs share one direction (the 3D kernel); in the 2D kernel a warp
 // mixes horizontal and vertical pairs and the extra branch diverges.
+// inv_sum_y (optional): 1/(ya + yb), a by-product of the shared reciprocal.
 template <bool kNodeLogs, bool kShort = kNodeLogs>
 TAG_DEV void ln_mean_pair(double xa, double xb, double ya, double yb, double Lxa, double Lxb,
-                          double Lya, double Lyb, double& rho_mean, double& inv_beta_mean) {
+                          double Lya, double Lyb, double& rho_mean, double& inv_beta_mean,
+                          double* inv_sum_y = nullptr) {
   const double sx = xa + xb, dx = xb - xa;
   const double sy = ya + yb, dy = yb - ya;
   const double r = 1.0 / (sx * sy);
   const double isx = sy * r, isy = sx * r;
+  if (inv_sum_y) *inv_sum_y = isy;
   const double tx = dx * isx, ty = dy * isy;
   const double f2x = tx * tx, f2y = ty * ty;
   const double fm = fmax(f2x, f2y);
