@@ -839,7 +839,8 @@ def run_ours(args):
                          "hbm_frac": achieved_gbs / hbm_peak, "hbm_peak_source": hbm_src,
                          "ms_element": ms_el, "ms_interface": ms_if,
                          "flops_per_launch": fl, "flops_source": FLOPS_SOURCE,
-                         "bytes_per_launch": by},
+                         "bytes_per_launch": by,
+                         "executed": executed_roofline(args.workload, dofs, ms_el, peak_fp64)},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(u0.nbytes),
                     "d2h_bytes_per_step": int(u0.nbytes)},
             "gpu_launches": args.steps * 11,
@@ -862,10 +863,24 @@ def run_ours(args):
 
 # DRAM bytes per DOF of the element kernel from ncu captures (read + write),
 # used to report `traffic` for the full-size launch.
-TRAFFIC_PER_DOF = {"shell": 282.45,      # k_element3d, stage mode, full shell
-                   "ensemble": 205.27,    # k_element 2D, stage mode, 128-member ensemble
+TRAFFIC_PER_DOF = {"shell": 281.26,      # k_element3d, stage mode, full shell
+                   "ensemble": 205.42,    # k_element 2D, stage mode, 128-member ensemble
                    "swe": 214.71,         # k_cov_element weak form, 8 of the SWE members
                    "swe_ec": 215.20}      # k_cov_element split EC form, the same 8 members
+# FP64 operations the element kernel executes per DOF (DFMA counted as 2), from
+# the same ncu captures (smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}),
+# beside the algorithmic count: the kernel computes per-node quantities once
+# where the reference's formulas recompute them per pair
+EXECUTED_FLOPS_PER_DOF = {"shell": 950.7, "ensemble": 368.7}
+
+
+def executed_roofline(workload, dofs, ms_el, peak_fp64):
+    f = EXECUTED_FLOPS_PER_DOF.get(workload)
+    if not f:
+        return None
+    tf = f * dofs / (ms_el * 1e-3) / 1e12
+    return {"flops_per_dof": f, "achieved": tf, "frac": tf / (peak_fp64 / 1e12),
+            "source": "ncu FP64 thread instructions of the element kernel (profiles/)"}
 
 
 def main():

@@ -141,3 +141,26 @@ def test_rhs3d_with_topography_matches_oracle(tg, orc, gpu_lib, vertical):
     assert per_var(du, du_ref) <= RTOL_VAR, per_var(du, du_ref)
     assert semi.status() == 0
     semi.close()
+
+
+def test_set_state_from_pinned_memory_matches_pageable(tg, gpu_lib):
+    """A state in pinned (mapped) host memory is read by one kernel that stores
+    it on the device and reduces the CFL speeds in the same pass; the result
+    equals the copy-engine path from pageable memory bit for bit: the state,
+    max_dt and the steps that follow."""
+    torch = pytest.importorskip("torch")
+    eq, mesh, semi = make_semi(tg, 2, 2, 4)
+    u = perturb3d(semi.compute_coefficients(), eq, seed=21)
+    pinned = torch.empty(u.shape, dtype=torch.float64, pin_memory=True).numpy()
+    pinned[...] = u
+    out = []
+    for src in (np.ascontiguousarray(u), pinned):
+        semi.set_state(src)
+        back = semi.get_state()
+        dt = semi.max_dt()
+        t = semi.rk_steps(2, cfl=0.8, t=0.0)
+        out.append((back, dt, t, semi.get_state()))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][0], u)
+    assert out[0][1] == out[1][1] and out[0][2] == out[1][2]
+    assert np.array_equal(out[0][3], out[1][3])
+    semi.close()

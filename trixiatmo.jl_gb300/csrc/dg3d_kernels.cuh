@@ -365,21 +365,58 @@ __global__ void k_element3d(typename Phys::Params Pp, const BasisDev basis, doub
 // One warp per element (a 3D element has up to 512 nodes): the lanes stride
 // over the nodes, the per-direction maxima meet by shuffles, and lane 0 adds
 // the element's value into its member's running maximum.  Max is exact, so the
-// result does not depend on the order.  blockDim is a multiple of 32.
+// result does not depend on the order.  blockDim is a multiple of 32.  With
+// copy_to the kernel also stores every value it reads there: a state read
+// from mapped host memory lands in device memory with its CFL speeds reduced
+// in the same pass.
 template <class Phys, int n>
 __global__ void k_max_speed3d(typename Phys::Params Pp, const double* __restrict__ u,
                               const double* __restrict__ Ja, const double* __restrict__ invJ,
                               int nelem, const int* __restrict__ member,
-                              double* __restrict__ max_speed) {
+                              double* __restrict__ max_speed, double* __restrict__ copy_to) {
   constexpr int NV = Phys::NV, nnn = n * n * n;
   const int lane = threadIdx.x & 31;
   const int e = (int)(((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   if (e >= nelem) return;  // warp-uniform
   double m[3] = {0.0, 0.0, 0.0};
-  for (int node = lane; node < nnn; node += 32) {
+  // chunks of 32 nodes; every lane takes part in each chunk (the shuffles of
+  // the copying path need the whole warp), lanes past the last node idle
+  for (int c0 = 0; c0 < nnn; c0 += 32) {
+    const int node = c0 + lane;
+    const bool on = node < nnn;
     const size_t q = (size_t)e * nnn + node;
+    double un[NV];
+    if (copy_to) {
+      // the chunk's nodes are consecutive NV-double records: read and store
+      // them lane-contiguously (the host link serves whole lines), then hand
+      // each lane its node's values by shuffles
+      const size_t base = ((size_t)e * nnn + c0) * NV;
+      const int avail = min(32, nnn - c0) * NV;
+      double r[NV];
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+        const int i = lane + 32 * k;
+        r[k] = i < avail ? u[base + i] : 0.0;
+        if (i < avail) copy_to[base + i] = r[k];
+      }
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        const int i = lane * NV + v, src = i & 31, reg = i >> 5;
+        double got = 0.0;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+          const double x = __shfl_sync(0xffffffffu, r[k], src);
+          if (k == reg) got = x;
+        }
+        un[v] = got;
+      }
+    } else if (on) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) un[v] = u[q * NV + v];
+    }
+    if (!on) continue;
     double lam[3];
-    Phys::max_speeds(Pp, u + q * NV, lam);
+    Phys::max_speeds(Pp, un, lam);
     const double* ja = Ja + q * 9;
     const double ij = fabs(invJ[q]);
 #pragma unroll

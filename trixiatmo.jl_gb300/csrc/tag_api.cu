@@ -146,6 +146,8 @@ struct Ops {
   int (*interface)(tag_handle h, const double* u);
   int (*element)(tag_handle h, int mode, double* u, double* du, int stage, bool last, double t);
   int (*max_speed)(tag_handle h, const double* u);
+  // optional: u from mapped host memory into d_u with the CFL speeds reduced
+  int (*load_state)(tag_handle h, const double* u_mapped);
   int (*init)(int max_smem);
   size_t (*smem_bytes)(int epb);
   int threads_per_element;
@@ -260,8 +262,8 @@ struct OpsImpl {
   static int max_threads() { return cap(); }
   static size_t smem_bytes(int epb) { return S::bytes(epb); }
   static const Ops* get() {
-    static const Ops ops{&interface, &element, &max_speed, &init, &smem_bytes, S::TPE,
-                         &max_threads};
+    static const Ops ops{&interface, &element, &max_speed, nullptr, &init, &smem_bytes,
+                         S::TPE, &max_threads};
     return &ops;
   }
 };
@@ -315,11 +317,16 @@ struct OpsImpl3D {
     TAG_CUDA(cudaGetLastError());
     return TAG_OK;
   }
-  static int max_speed(tag_handle h, const double* u) {
+  static int max_speed(tag_handle h, const double* u) { return speeds(h, u, nullptr); }
+  // the state from mapped host memory into the device copy, speeds on the way
+  static int load_state(tag_handle h, const double* u_mapped) {
+    return speeds(h, u_mapped, h->d_u);
+  }
+  static int speeds(tag_handle h, const double* u, double* copy_to) {
     const int threads = 256, warps = threads / 32;  // one warp per element
     k_max_speed3d<Phys, n><<<(h->nelem + warps - 1) / warps, threads, 0, h->stream>>>(
         params_of<Phys>(h), u, h->d_Ja, h->d_invJ, h->nelem, h->d_member,
-        h->d_mscal + 2 * h->nmembers);
+        h->d_mscal + 2 * h->nmembers, copy_to);
     TAG_CUDA(cudaGetLastError());
     return TAG_OK;
   }
@@ -338,8 +345,8 @@ struct OpsImpl3D {
   static int max_threads() { return cap(); }
   static size_t smem_bytes(int epb) { return S::bytes(epb); }
   static const Ops* get() {
-    static const Ops ops{&interface, &element, &max_speed, &init, &smem_bytes, S::TPE,
-                         &max_threads};
+    static const Ops ops{&interface, &element, &max_speed, &load_state, &init, &smem_bytes,
+                         S::TPE, &max_threads};
     return &ops;
   }
 };
@@ -570,8 +577,8 @@ int cov_init(int max_smem) {
 size_t cov_smem_bytes(int) { return 0; }
 int cov_max_threads() { return 256; }
 
-const Ops kCovOps{&cov_interface, &cov_element, &cov_max_speed, &cov_init, &cov_smem_bytes, 256,
-                  &cov_max_threads};
+const Ops kCovOps{&cov_interface, &cov_element, &cov_max_speed, nullptr, &cov_init,
+                  &cov_smem_bytes, 256, &cov_max_threads};
 
 // Flux options of a covariant member configuration; returns the reason it is
 // rejected, or null.
@@ -1231,6 +1238,22 @@ int tag_rhs(tag_handle h, const double* u, double* du, double t, int32_t on_devi
 
 int tag_set_state(tag_handle h, const double* u_host) {
   if (!h || !u_host) return fail(TAG_E_INVALID, "null argument");
+  // pinned (mapped) host memory: one kernel reads the state over the host link,
+  // stores it on the device and reduces the CFL speeds in the same pass
+  cudaPointerAttributes attr{};
+  const bool mapped = cudaPointerGetAttributes(&attr, u_host) == cudaSuccess &&
+                      attr.type == cudaMemoryTypeHost && attr.devicePointer != nullptr;
+  if (!mapped) cudaGetLastError();  // a pointer CUDA does not know is not an error here
+  if (mapped && h->ops->load_state) {
+    TAG_CUDA(cudaMemsetAsync(h->d_k, 0, sizeof(double) * (size_t)h->nodes * h->na, h->stream));
+    TAG_CUDA(cudaMemsetAsync(h->d_mscal + 2 * h->nmembers, 0, sizeof(double) * h->nmembers,
+                             h->stream));
+    int rc = h->ops->load_state(h, static_cast<const double*>(attr.devicePointer));
+    if (rc) return rc;
+    TAG_CUDA(cudaStreamSynchronize(h->stream));
+    h->speed_valid = true;
+    return TAG_OK;
+  }
   TAG_CUDA(cudaMemcpyAsync(h->d_u, u_host, sizeof(double) * (size_t)tag_ndofs_total(h),
                            cudaMemcpyHostToDevice, h->stream));
   TAG_CUDA(cudaMemsetAsync(h->d_k, 0, sizeof(double) * (size_t)h->nodes * h->na,
