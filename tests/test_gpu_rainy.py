@@ -176,8 +176,9 @@ def test_mlp_kernels_match_numpy_restatement(tg, orc, gpu_lib):
 def test_learned_guess_trains_and_reduces_newton_iterations(tg, orc, gpu_lib):
     """Trains the MLP on GPU-generated pairs, then solves the moist-bubble
     state from the plain warm start and from the learned guess: same bits
-    (canonical finish), fewer Newton updates, and the GPU's plain solve agrees
-    with the oracle's."""
+    (canonical finish), fewer Newton updates, fewer also than the closed-form
+    branch alone on the saturated nodes (the network's part), and the GPU's
+    plain solve agrees with the oracle's."""
     lg = tg.learned_guess
     p, st, losses = lg.train_guess(n=200_000, epochs=8, seed=3)
     assert st["not_converged"] == 0
@@ -196,6 +197,15 @@ def test_learned_guess_trains_and_reduces_newton_iterations(tg, orc, gpu_lib):
     same = np.all(u_learn.reshape(-1, 9) == u_plain.reshape(-1, 9), axis=1)
     assert same.mean() >= 0.999, same.mean()
     assert it_learn.mean() < 0.75 * it_plain.mean(), (it_learn.mean(), it_plain.mean())
+    # the network's own share: on saturated nodes the closed-form branch does
+    # not apply (start 2 takes the warm start there), and the MLP guess must
+    # need fewer updates than that
+    semi.set_state(u0)
+    st_cf, it_cf = semi.newton_solve(learned=2)
+    sat = lg.saturated(np.asarray(u0).reshape(-1, 9))
+    assert sat.any() and (~sat).any()
+    assert it_learn[sat].mean() < it_cf[sat].mean(), (it_learn[sat].mean(), it_cf[sat].mean())
+    assert np.array_equal(it_cf[sat], it_plain[sat])
     uo = np.ascontiguousarray(u0).copy()
     _, it_o, nf = orc.rainy_newton_states(uo, mode=1, tol=1e-12, maxit=30, polish=1)
     assert nf == 0 and np.mean(it_o == it_plain) > 0.99
