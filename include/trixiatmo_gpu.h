@@ -45,6 +45,7 @@ extern "C" {
 #define TAG_E_CUDA 2           /* a CUDA runtime call failed                   */
 #define TAG_E_NO_DEVICE 3      /* no CUDA device visible                       */
 #define TAG_E_STATE 4          /* device status word has an error bit set      */
+#define TAG_E_IO 5             /* a file could not be written                  */
 
 /* ---- device status word bits (tag_status) ------------------------------ */
 #define TAG_S_NAN 0x1u         /* non-finite value met in a kernel             */
@@ -486,6 +487,59 @@ int tag_eval_means(int32_t kind, int64_t n, double cp, double cv, const double* 
  * null) receives the TAG_S_* bits of this call. */
 int tag_rhs_noalloc(const tag_config* cfg, const double* u, double* du, void* stream,
                     uint32_t* status);
+
+/* ---- solution output (SaveSolutionCallback) ---------------------------- */
+/* Trixi's `solution_variables` functions for tag_solution_variables. */
+#define TAG_SOLVAR_CONS2CONS 0               /* the conservative variables, every equation system */
+#define TAG_SOLVAR_CONS2PRIM 1               /* covariant SWE: (H, vcon1, vcon2)                 */
+#define TAG_SOLVAR_CONTRAVARIANT2GLOBAL 2    /* covariant SWE: (h, h_v1, h_v2, h_v3)             */
+#define TAG_SOLVAR_CONS2PRIM_AND_VORTICITY 3 /* covariant SWE: (H, v1, v2, v3, b, vorticity)     */
+
+/* The solution variables of the handle's current state, computed on the
+ * device, in the layout Trixi writes them: data[v * nnodes + q] is variable v
+ * at node q = i + n (j + n element) (3D: i + n (j + n (k + n element))), so
+ * that each row is `vec(data[v, .., :])` of the reference.  member selects
+ * one member of an ensemble (0 .. nmembers-1; -1 = every element of the
+ * handle).  *nvars and *nnodes receive the sizes; data may be null to query
+ * them.  Replaces convert_variables (src/callbacks_step/
+ * save_solution_covariant.jl:5-33 with cons2prim_and_vorticity :64-78 and
+ * calc_vorticity_node :94-121; cons2prim / contravariant2global of
+ * src/equations/covariant_shallow_water.jl:113-145); cons2cons is the
+ * transposed state (save_solution_2d_manifold_in_3d_cartesian.jl:66-68). */
+int tag_solution_variables(tag_handle h, int32_t solution_variables, int32_t member,
+                           int32_t* nvars, int64_t* nnodes, double* data);
+
+/* A scalar attribute of tag_h5_write. */
+#define TAG_H5_INT64 0
+#define TAG_H5_FLOAT64 1
+#define TAG_H5_STRING 2
+typedef struct tag_h5_attribute {
+  const char* name;   /* at most 1024 bytes */
+  int32_t type;       /* TAG_H5_INT64 (i), TAG_H5_FLOAT64 (d) or TAG_H5_STRING (s, UTF-8) */
+  int64_t i;
+  double d;
+  const char* s;      /* at most 60000 bytes; null = "" */
+} tag_h5_attribute;
+
+/* A one-dimensional float64 dataset of tag_h5_write with an optional string
+ * attribute "name" (the variable's name in Trixi's files). */
+typedef struct tag_h5_dataset {
+  const char* name;       /* link name in the root group: no '/', at most 1024 bytes */
+  const double* data;     /* count doubles (host memory) */
+  int64_t count;
+  const char* var_name;   /* value of the "name" attribute, or null for none */
+} tag_h5_dataset;
+
+/* Writes an HDF5 file (clobbering `path`) whose root group holds the scalar
+ * attributes and up to 256 datasets: the layout of Trixi's solution files
+ * (src/callbacks_step/save_solution_2d_manifold_in_3d_cartesian.jl:72-116:
+ * attributes ndims, equations, polydeg, n_vars, n_elements, mesh_type,
+ * mesh_file, time, dt, timestep; datasets variables_1 .. variables_n with
+ * their names), readable by any HDF5 library and so by Trixi2Vtk.  Host
+ * only: no device work, no CUDA call.  Returns TAG_E_IO when the file cannot
+ * be written. */
+int tag_h5_write(const char* path, const tag_h5_attribute* attrs, int32_t nattrs,
+                 const tag_h5_dataset* sets, int32_t nsets);
 
 /* Last error message of this thread (static storage). */
 const char* tag_last_error(void);

@@ -7,7 +7,7 @@ The directory name is not a Python identifier; load it with
 ``load_package()`` from ``__graft_entry__`` (or importlib) under the name
 ``trixiatmo_gb300``.
 """
-from . import _lib, covariant, learned_guess, trixi_connectivity
+from . import _lib, covariant, learned_guess, output, trixi_connectivity
 from .basis import LobattoLegendreBasis
 from .equations import (CompressibleEulerEnergyEquationsWithGravity2D,
                         CompressibleEulerEnergyEquationsWithGravity3D,
@@ -49,6 +49,8 @@ from .meshes import (P4estMesh, SchaerMountain, SchärMountain, StructuredMesh, 
 from .equations import BoundaryConditionDirichlet
 from .initial_conditions import MountainWaveSetup
 from .meshes3d import GalChen, P4estMeshCubedSphereTopography, Sleve
+from .output import (convert_variables, cons2cons, cons2prim, cons2prim_and_vorticity,
+                     contravariant2global, save_solution_file, varnames)
 from .semidiscretization import (DGSEM, SemidiscretizationCovariant,
                                  SemidiscretizationCovariantEnsemble, SemidiscretizationEnsemble,
                                  SemidiscretizationHyperbolic, fp64_peak, source_terms_coriolis,
@@ -86,5 +88,6 @@ __all__ = [
     "flux_nonconservative_etec", "flux_conservative_es", "flux_nonconservative_es",
     "flux_ec", "flux_tec",
     "flux_etec", "flux_nonconservative_artiano_etal", "flux_nonconservative_souza_etal",
-    "trixi_connectivity",
+    "trixi_connectivity", "output", "save_solution_file", "convert_variables", "varnames",
+    "cons2cons", "cons2prim", "contravariant2global", "cons2prim_and_vorticity",
 ]

@@ -16,6 +16,15 @@ TAG_E_INVALID = 1
 TAG_E_CUDA = 2
 TAG_E_NO_DEVICE = 3
 TAG_E_STATE = 4
+TAG_E_IO = 5
+
+TAG_SOLVAR_CONS2CONS = 0
+TAG_SOLVAR_CONS2PRIM = 1
+TAG_SOLVAR_CONTRAVARIANT2GLOBAL = 2
+TAG_SOLVAR_CONS2PRIM_AND_VORTICITY = 3
+TAG_H5_INT64 = 0
+TAG_H5_FLOAT64 = 1
+TAG_H5_STRING = 2
 
 TAG_S_NAN = 0x1
 TAG_S_NEG_DENSITY = 0x2
@@ -115,6 +124,18 @@ class AdaptiveStats(ctypes.Structure):
 _fp = ctypes.POINTER(ctypes.c_float)
 
 # exported symbol -> (restype, argtypes)
+class H5Attribute(ctypes.Structure):
+    """tag_h5_attribute"""
+    _fields_ = [("name", ctypes.c_char_p), ("type", ctypes.c_int32), ("i", ctypes.c_int64),
+                ("d", ctypes.c_double), ("s", ctypes.c_char_p)]
+
+
+class H5Dataset(ctypes.Structure):
+    """tag_h5_dataset"""
+    _fields_ = [("name", ctypes.c_char_p), ("data", _dp), ("count", ctypes.c_int64),
+                ("var_name", ctypes.c_char_p)]
+
+
 SIGNATURES = {
     "tag_create": (ctypes.c_int, [ctypes.POINTER(TagConfig), ctypes.POINTER(ctypes.c_void_p)]),
     "tag_create_ensemble": (ctypes.c_int, [ctypes.POINTER(TagConfig), ctypes.c_int32,
@@ -176,6 +197,10 @@ SIGNATURES = {
                                      ctypes.c_int32, ctypes.c_float, ctypes.c_uint64, _fp]),
     "tag_rhs_noalloc": (ctypes.c_int, [ctypes.POINTER(TagConfig), _dp, _dp, ctypes.c_void_p,
                                        ctypes.POINTER(ctypes.c_uint32)]),
+    "tag_solution_variables": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                              _ip, ctypes.POINTER(ctypes.c_int64), _dp]),
+    "tag_h5_write": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(H5Attribute), ctypes.c_int32,
+                                    ctypes.POINTER(H5Dataset), ctypes.c_int32]),
 }
 
 _lib = None

@@ -1,8 +1,8 @@
 """Build recipe of libtrixiatmo_gpu.so (nvcc, sm_103a only, in-tree).
 
-The CUDA translation units under csrc/ are compiled in parallel to objects and
-linked into ``_build/libtrixiatmo_gpu.so``.  Rebuilds only when a source is
-newer than the library.
+The CUDA translation units and host-only C++ files under csrc/ are compiled
+in parallel to objects and linked into ``_build/libtrixiatmo_gpu.so``.
+Rebuilds only when a source is newer than the library.
 """
 from __future__ import annotations
 
@@ -32,7 +32,9 @@ def _nvcc() -> str:
 
 
 def _sources():
-    return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    """CUDA translation units (*.cu) and host-only C++ (*.cpp, compiled by
+    nvcc's host compiler into the same library)."""
+    return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
 
 
 def _deps():
@@ -54,7 +56,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     nvcc = _nvcc()
 
     def compile_one(src):
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(BUILD, os.path.splitext(os.path.basename(src))[0] + ".o")
         cmd = [nvcc, *NVCC_FLAGS, "-I", INCLUDE, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

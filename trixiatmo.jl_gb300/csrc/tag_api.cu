@@ -24,6 +24,7 @@
 #include "phys_ie_2d.cuh"
 #include "phys_rainy_2d.cuh"
 #include "tag_analysis.cuh"
+#include "output_kernels.cuh"
 
 using namespace tag;
 
@@ -875,11 +876,9 @@ const void* analysis_params(tag_handle h) {
   }
 }
 
-// Member node / element ranges, quadrature weights x |J| per node, the
-// analysis interpolation (Cartesian meshes) and reduction scratch; once per
-// handle.
-int analysis_setup(tag_handle h) {
-  if (h->an_ready) return TAG_OK;
+// Node and element ranges of the members, rng[4][nmembers]: node begin,
+// node end, element begin, element end (each member one contiguous range).
+int member_ranges(tag_handle h, std::vector<long>& rng) {
   const bool cov = h->eq == TAG_EQ_COVARIANT_SWE;
   const int M = h->nmembers, E = h->nelem;
   std::vector<int> member(E, 0);
@@ -898,7 +897,7 @@ int analysis_setup(tag_handle h) {
     for (int e = 0; e < E; ++e) enode[e] = (long)e * h->npe;
   }
   enode[E] = h->nodes;
-  std::vector<long> rng(4 * (size_t)M, -1);
+  rng.assign(4 * (size_t)M, -1);
   long *nb = rng.data(), *ne_ = nb + M, *eb = nb + 2 * M, *ee = nb + 3 * M;
   for (int e = 0; e < E; ++e) {
     const int m = member[e];
@@ -906,17 +905,30 @@ int analysis_setup(tag_handle h) {
     if (eb[m] < 0)
       eb[m] = e;
     else if (ee[m] != e)
-      return fail(TAG_E_INVALID, "analysis needs each member in one contiguous element range");
+      return fail(TAG_E_INVALID, "each member must be one contiguous element range");
     ee[m] = e + 1;
   }
-  long lmax = 1;
   for (int m = 0; m < M; ++m) {
     if (eb[m] < 0) return fail(TAG_E_INVALID, "a member has no elements");
     nb[m] = enode[eb[m]];
     ne_[m] = enode[ee[m]];
-    lmax = std::max(lmax, ne_[m] - nb[m]);
   }
-  int rc = upload(&h->d_an_rng, rng.data(), rng.size(), h->stream);
+  return TAG_OK;
+}
+
+// Member node / element ranges, quadrature weights x |J| per node, the
+// analysis interpolation (Cartesian meshes) and reduction scratch; once per
+// handle.
+int analysis_setup(tag_handle h) {
+  if (h->an_ready) return TAG_OK;
+  const bool cov = h->eq == TAG_EQ_COVARIANT_SWE;
+  const int M = h->nmembers, E = h->nelem;
+  std::vector<long> rng;
+  int rc = member_ranges(h, rng);
+  if (rc) return rc;
+  long lmax = 1;
+  for (int m = 0; m < M; ++m) lmax = std::max(lmax, rng[M + m] - rng[m]);
+  rc = upload(&h->d_an_rng, rng.data(), rng.size(), h->stream);
   if (rc) return rc;
   TAG_CUDA(cudaMalloc(&h->d_an_wj, sizeof(double) * h->nodes));
   std::vector<double*> tmp;
@@ -1268,6 +1280,51 @@ int tag_get_state(tag_handle h, double* u_host) {
   TAG_CUDA(cudaMemcpyAsync(u_host, h->d_u, sizeof(double) * (size_t)tag_ndofs_total(h),
                            cudaMemcpyDeviceToHost, h->stream));
   TAG_CUDA(cudaStreamSynchronize(h->stream));
+  return TAG_OK;
+}
+
+int tag_solution_variables(tag_handle h, int32_t solution_variables, int32_t member,
+                           int32_t* nvars, int64_t* nnodes, double* data) {
+  if (!h || !nvars || !nnodes) return fail(TAG_E_INVALID, "null argument");
+  const bool cov = h->eq == TAG_EQ_COVARIANT_SWE;
+  const int kind = solution_variables;
+  if (kind < TAG_SOLVAR_CONS2CONS || kind > TAG_SOLVAR_CONS2PRIM_AND_VORTICITY ||
+      (!cov && kind != TAG_SOLVAR_CONS2CONS))
+    return fail(TAG_E_INVALID, cov ? "solution_variables out of range 0..3"
+                                   : "this equation system writes cons2cons only");
+  if (member < -1 || member >= h->nmembers) return fail(TAG_E_INVALID, "member out of range");
+  long q0 = 0, q1 = h->nodes;
+  if (member >= 0 && h->nmembers > 1) {
+    std::vector<long> rng;
+    const int rc = member_ranges(h, rng);
+    if (rc) return rc;
+    q0 = rng[member];
+    q1 = rng[h->nmembers + member];
+  }
+  const long nq = q1 - q0;
+  const int nr = !cov ? h->nv : kind == TAG_SOLVAR_CONTRAVARIANT2GLOBAL ? 4
+                 : kind == TAG_SOLVAR_CONS2PRIM_AND_VORTICITY ? 6 : 3;
+  *nvars = nr;
+  *nnodes = nq;
+  if (!data) return TAG_OK;
+  NvtxRange nv_("save_solution");
+  double* d_out = nullptr;
+  TAG_CUDA(cudaMallocAsync(&d_out, sizeof(double) * (size_t)nr * nq, h->stream));
+  const unsigned blocks = (unsigned)((nq + 255) / 256);
+  if (cov)
+    k_cov_solution_rows<<<blocks, 256, 0, h->stream>>>(h->d_groups, h->d_bases, h->d_u, h->d_aux,
+                                                       kind, q0, nq, d_out);
+  else
+    k_state_rows<<<blocks, 256, 0, h->stream>>>(h->d_u, h->nv, q0, nq, d_out);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(data, d_out, sizeof(double) * (size_t)nr * nq, cudaMemcpyDeviceToHost,
+                        h->stream);
+  const cudaError_t ef = cudaFreeAsync(d_out, h->stream);
+  const cudaError_t es = cudaStreamSynchronize(h->stream);
+  if (e == cudaSuccess) e = ef != cudaSuccess ? ef : es;
+  if (e != cudaSuccess) return fail(TAG_E_CUDA, std::string("tag_solution_variables: ") +
+                                                    cudaGetErrorString(e));
   return TAG_OK;
 }
 

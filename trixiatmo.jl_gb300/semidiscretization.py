@@ -791,6 +791,7 @@ class _CovHandle:
         m = len(members)
         cfgs = (_lib.TagConfig * m)()
         self.keep = []
+        self.ndims = 2  # a two-dimensional manifold (P4estMesh{2})
         self.aux, self.xyz, self.ns, self.member_nelements = [], [], [], []
         for k, (mesh, solver, topo) in enumerate(members):
             basis = solver.basis
