@@ -82,7 +82,8 @@ struct NewtonArgs {
   unsigned long long* counters;  // [0] updates, [1] fallbacks, [2] not converged, or null
 };
 
-TAG_DEV void rainy_residual(const double* u, const double* x, double* r) {
+// Residual of the saturation system at x, given svp = e_s(x[2]).
+TAG_DEV void rainy_residual_at(const double* u, const double* x, double svp, double* r) {
   using C = RainyConst;
   const double rho = u[0] + u[1] + u[2];
   const double ri = 1.0 / rho;
@@ -90,7 +91,7 @@ TAG_DEV void rainy_residual(const double* u, const double* x, double* r) {
   double r1 = (C::c_vd * u[0] + C::c_vv * x[0] + C::c_l * (x[1] + u[2])) * x[2];
   r1 += x[0] * C::ref_L;
   r1 -= (u[5] - rho * 0.5 * (v1 * v1 + v2 * v2));
-  double r2 = fmin(rainy_e_s(x[2]) / (C::R_v * x[2]), u[1]);
+  double r2 = fmin(svp / (C::R_v * x[2]), u[1]);
   r2 -= x[0];
   r2 *= 1.0e7;
   double r3 = u[1];
@@ -101,11 +102,20 @@ TAG_DEV void rainy_residual(const double* u, const double* x, double* r) {
   r[2] = r3;
 }
 
-// Newton update dx = J^{-1} r with the reference Jacobian (Cramer's rule)
-TAG_DEV void rainy_newton_step(const double* u, const double* x, const double* r, double* dx) {
-  using C = RainyConst;
+// Residual of the saturation system at x; returns e_s(x[2]), which the
+// Newton update at the same x reuses.
+TAG_DEV double rainy_residual(const double* u, const double* x, double* r) {
   const double svp = rainy_e_s(x[2]);
-  const double svp_t = rainy_e_s_T(x[2]);
+  rainy_residual_at(u, x, svp, r);
+  return svp;
+}
+
+// Newton update dx = J^{-1} r with the reference Jacobian (Cramer's rule);
+// svp = e_s(x[2]) as the residual at x returned it
+TAG_DEV void rainy_newton_step(const double* u, const double* x, const double* r, double svp,
+                               double* dx) {
+  using C = RainyConst;
+  const double svp_t = rainy_e_s_T_from(x[2], svp);
   const double a = C::c_vv * x[2] + C::ref_L, b = C::c_l * x[2];
   const double c = C::c_vd * u[0] + C::c_vv * x[0] + C::c_l * (x[1] + u[2]);
   const double d = -10000000.0, e = 0.0;
@@ -155,19 +165,26 @@ TAG_DEV void rainy_snap(const double* u, double* x) {
 // Newton from x; returns updates until the criterion held (maxit if never).
 // With polish > 0 a converged iterate is snapped (rainy_snap) and `polish`
 // further updates are taken from there; if the criterion then fails, the
-// iterate before the snap is kept.
+// iterate before the snap is kept.  svp0 > 0 is e_s(x[2]) of the start when
+// the caller has it already (a guess computed it), else 0.
 TAG_DEV int rainy_newton_run(const double* u, double* x, int mode, double tol, int maxit,
-                             int polish, bool& converged) {
+                             int polish, bool& converged, double svp0 = 0.0) {
   double r[3], dx[3];
   int it = 0;
   converged = false;
   for (; it < maxit; ++it) {
-    rainy_residual(u, x, r);
+    double svp;
+    if (it == 0 && svp0 > 0.0) {
+      svp = svp0;
+      rainy_residual_at(u, x, svp, r);
+    } else {
+      svp = rainy_residual(u, x, r);
+    }
     if (rainy_newton_done(u, r, mode, tol)) {
       converged = true;
       break;
     }
-    rainy_newton_step(u, x, r, dx);
+    rainy_newton_step(u, x, r, svp, dx);
     x[0] -= dx[0];
     x[1] -= dx[1];
     x[2] -= dx[2];
@@ -180,8 +197,8 @@ TAG_DEV int rainy_newton_run(const double* u, double* x, int mode, double tol, i
     double y[3] = {x[0], x[1], x[2]};
     rainy_snap(u, y);
     for (int p = 0; p < polish; ++p) {
-      rainy_residual(u, y, r);
-      rainy_newton_step(u, y, r, dx);
+      const double svp = rainy_residual(u, y, r);
+      rainy_newton_step(u, y, r, svp, dx);
       y[0] -= dx[0];
       y[1] -= dx[1];
       y[2] -= dx[2];
@@ -198,11 +215,13 @@ TAG_DEV int rainy_newton_run(const double* u, double* x, int mode, double tol, i
 
 // The closed-form unsaturated equilibrium (all moisture as vapour at T_unsat)
 // when it is valid, i.e. when the vapour fits under the saturation density;
-// returns false for a saturated node.
-TAG_DEV bool rainy_closed_form_guess(const double* u, double* x, double& tu, double& e_int) {
+// returns false for a saturated node.  svp = e_s(T_unsat) (0 if T_unsat <= 0).
+TAG_DEV bool rainy_closed_form_guess(const double* u, double* x, double& tu, double& e_int,
+                                     double& svp) {
   using C = RainyConst;
   tu = rainy_t_unsat(u, e_int);
-  if (tu > 0.0 && rainy_e_s(tu) / (C::R_v * tu) >= u[1]) {
+  svp = tu > 0.0 ? rainy_e_s(tu) : 0.0;
+  if (tu > 0.0 && svp / (C::R_v * tu) >= u[1]) {
     x[0] = u[1];
     x[1] = 0.0;
     x[2] = tu;
@@ -214,58 +233,58 @@ TAG_DEV bool rainy_closed_form_guess(const double* u, double* x, double& tu, dou
 // Learned start: the closed-form unsaturated equilibrium where it is valid,
 // else T_unsat plus the network's latent-heat offset, with vapour and cloud
 // from the saturation relation at that temperature.
-// Returns true where the closed form was taken.
-TAG_DEV bool rainy_learned_guess(const float* __restrict__ P, const double* u, double* x) {
+// Returns true where the closed form was taken; svp = e_s(x[2]).
+TAG_DEV bool rainy_learned_guess(const float* __restrict__ P, const double* u, double* x,
+                                 double& svp) {
   using C = RainyConst;
   double e_int, tu;
-  if (rainy_closed_form_guess(u, x, tu, e_int)) return true;
+  if (rainy_closed_form_guess(u, x, tu, e_int, svp)) return true;
   float xin[kMlpIn];
   mlp_inputs(u, e_int, tu, xin);
   const double T = tu + fmax((double)mlp_forward(P, xin), 0.0);
+  svp = rainy_e_s(T);
   x[2] = T;
-  x[0] = fmin(rainy_e_s(T) / (C::R_v * T), u[1]);
+  x[0] = fmin(svp / (C::R_v * T), u[1]);
   x[1] = u[1] - x[0];
   return false;
 }
 
-static __global__ void __launch_bounds__(256) k_newton_rainy(double* __restrict__ u, long nodes,
-                                                      NewtonArgs a, unsigned* __restrict__ status) {
-  __shared__ float sp[kMlpParams];
-  if ((a.learned == 1 || a.learned == 3) && a.mlp) {
-    for (int t = threadIdx.x; t < kMlpParams; t += blockDim.x) sp[t] = a.mlp[t];
-    __syncthreads();
-  }
-  const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nodes) return;
-  double* un = u + q * 9;
+// The stage limiter at one node: the node's saturation solve from the start
+// that NewtonArgs::learned selects, the guessed start falling back to the
+// warm start (slots 7-9) when it has not converged after maxit_learned
+// updates.  Writes slots 7-9 (and clamps negative rain); returns the Newton
+// updates taken, with whether a fallback happened and whether it converged.
+TAG_DEV int newton_rainy_node(const float* sp, double* __restrict__ un, const NewtonArgs& a,
+                              int& fallback, bool& conv) {
   double s[9];
 #pragma unroll
   for (int v = 0; v < 9; ++v) s[v] = un[v];  // the node copy is taken before the rain clamp
   if (un[2] < 0.0) un[2] = 0.0;
   double x[3] = {s[6], s[7], s[8]};
-  bool conv = false;
-  int its = 0, fallback = 0;
-  double xg[3];
+  conv = false;
+  fallback = 0;
+  int its = 0;
+  double xg[3], svp_g = 0.0;
   bool guessed = false;
   if (a.learned == 1 && a.mlp) {
-    rainy_learned_guess(sp, s, xg);
+    rainy_learned_guess(sp, s, xg, svp_g);
     guessed = true;
   } else if (a.learned == 3 && a.mlp) {
-    guessed = rainy_learned_guess(sp, s, xg);
+    guessed = rainy_learned_guess(sp, s, xg, svp_g);
     if (!guessed) {
       // saturated node: keep the MLP guess only where it starts closer
       double rg[3], rw[3];
-      rainy_residual(s, xg, rg);
+      rainy_residual_at(s, xg, svp_g, rg);
       rainy_residual(s, x, rw);
       const double sg = rainy_residual_size(s, rg, a.mode);
       guessed = isfinite(sg) && sg < rainy_residual_size(s, rw, a.mode);
     }
   } else if (a.learned == 2) {
     double tu, e_int;
-    guessed = rainy_closed_form_guess(s, xg, tu, e_int);
+    guessed = rainy_closed_form_guess(s, xg, tu, e_int, svp_g);
   }
   if (guessed) {
-    its = rainy_newton_run(s, xg, a.mode, a.tol, a.maxit_learned, a.polish, conv);
+    its = rainy_newton_run(s, xg, a.mode, a.tol, a.maxit_learned, a.polish, conv, svp_g);
     if (conv && isfinite(xg[2])) {
       x[0] = xg[0];
       x[1] = xg[1];
@@ -279,12 +298,39 @@ static __global__ void __launch_bounds__(256) k_newton_rainy(double* __restrict_
   un[6] = x[0];
   un[7] = x[1];
   un[8] = x[2];
-  if (a.iters) a.iters[q] = its;
-  if (!conv) atomicOr(status, TAG_S_NEWTON_MAXIT);
+  return its;
+}
+
+static __global__ void __launch_bounds__(256) k_newton_rainy(double* __restrict__ u, long nodes,
+                                                      NewtonArgs a, unsigned* __restrict__ status) {
+  __shared__ float sp[kMlpParams];
+  if ((a.learned == 1 || a.learned == 3) && a.mlp) {
+    for (int t = threadIdx.x; t < kMlpParams; t += blockDim.x) sp[t] = a.mlp[t];
+    __syncthreads();
+  }
+  const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  // every lane stays to the end for the warp's counter reduction; lanes past
+  // the last node do no work and contribute zeros
+  unsigned its = 0, fallbacks = 0, unconverged = 0;
+  if (q < nodes) {
+    int fb;
+    bool conv;
+    its = (unsigned)newton_rainy_node(sp, u + q * 9, a, fb, conv);
+    if (a.iters) a.iters[q] = (int)its;
+    if (!conv) atomicOr(status, TAG_S_NEWTON_MAXIT);
+    fallbacks = (unsigned)fb;
+    unconverged = conv ? 0u : 1u;
+  }
   if (a.counters) {
-    atomicAdd(a.counters, (unsigned long long)its);
-    if (fallback) atomicAdd(a.counters + 1, 1ull);
-    if (!conv) atomicAdd(a.counters + 2, 1ull);
+    // one atomic per warp and counter instead of one per node
+    its = __reduce_add_sync(0xffffffffu, its);
+    fallbacks = __reduce_add_sync(0xffffffffu, fallbacks);
+    unconverged = __reduce_add_sync(0xffffffffu, unconverged);
+    if ((threadIdx.x & 31) == 0) {
+      if (its) atomicAdd(a.counters, (unsigned long long)its);
+      if (fallbacks) atomicAdd(a.counters + 1, (unsigned long long)fallbacks);
+      if (unconverged) atomicAdd(a.counters + 2, (unsigned long long)unconverged);
+    }
   }
 }
 

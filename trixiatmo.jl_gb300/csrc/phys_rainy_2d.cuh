@@ -18,29 +18,39 @@ struct RainyConst {
   static constexpr double pi = 3.14159265358979323846;
 };
 
-// saturation_vapour_pressure (:397-419) and its derivative (:421-446)
+// saturation_vapour_pressure (:397-419),
+//   e_s(T) = ref_s_p (T / ref_temp)^c1 exp(c2 (1 / ref_temp - 1 / T)),
+// evaluated as ref_s_p exp(c1 log(T / ref_temp) + c2 (1 / ref_temp - 1 / T)):
+// one logarithm and one exponential where the power costs both again (FP64
+// transcendentals are the rainy kernels' main cost).  Relative difference to
+// the reference's form: a few ulp.
+constexpr double kRainyC1 = (RainyConst::c_pv - RainyConst::c_l) / RainyConst::R_v;
+constexpr double kRainyC2 =
+    (RainyConst::ref_L - (RainyConst::c_pv - RainyConst::c_l) * RainyConst::ref_temp) /
+    RainyConst::R_v;
+
 TAG_DEV double rainy_e_s(double T) {
   using C = RainyConst;
-  const double e = C::ref_s_p * pow(T / C::ref_temp, (C::c_pv - C::c_l) / C::R_v);
-  return e * exp(((C::ref_L - (C::c_pv - C::c_l) * C::ref_temp) / C::R_v) *
-                 (1.0 / C::ref_temp - 1.0 / T));
+  return C::ref_s_p * exp(kRainyC1 * log(T / C::ref_temp) + kRainyC2 * (1.0 / C::ref_temp - 1.0 / T));
 }
 
-TAG_DEV double rainy_e_s_T(double T) {
-  using C = RainyConst;
-  const double c1 = (C::c_pv - C::c_l) / C::R_v;
-  const double c2 = (C::ref_L - (C::c_pv - C::c_l) * C::ref_temp) / C::R_v;
-  double d = C::ref_s_p / pow(C::ref_temp, c1);
-  d *= (c1 * pow(T, c1 - 1.0) + c2 * pow(T, c1 - 2.0));
-  d *= exp(c2 * (1.0 / C::ref_temp - 1.0 / T));
-  return d;
-}
+// saturation_vapour_pressure_derivative (:421-446) from the value e_s = e_s(T):
+// the reference's ref_s_p / ref_temp^c1 (c1 T^(c1-1) + c2 T^(c1-2)) exp(...)
+// equals e_s(T) (c1 + c2 / T) / T
+TAG_DEV double rainy_e_s_T_from(double T, double e_s) { return e_s * (kRainyC1 + kRainyC2 / T) / T; }
+
+TAG_DEV double rainy_e_s_T(double T) { return rainy_e_s_T_from(T, rainy_e_s(T)); }
+
+// x^(1/8) by three correctly rounded square roots (x^0.125 to a few ulp;
+// NaN for x < 0, as the power)
+TAG_DEV double rainy_root8(double x) { return sqrt(sqrt(sqrt(x))); }
 
 // terminal_velocity_rain, :380-395
 TAG_DEV double rainy_v_rain(double rho_moist, double rho_rain) {
   using C = RainyConst;
   if (rho_rain > 0.0)
-    return C::v_0 * 1.9386213994279082 * pow(rho_rain / (C::pi * (rho_moist + rho_rain) * C::N_0), 0.125);
+    return C::v_0 * 1.9386213994279082 *
+           rainy_root8(rho_rain / (C::pi * (rho_moist + rho_rain) * C::N_0));
   return 0.0;
 }
 
@@ -174,6 +184,35 @@ struct PhysRainy2D {
     f[6] = f[7] = f[8] = 0.0;
   }
 
+  // flux(u, n) together with the two speeds of max_abs_speed_naive
+  // (:595-611) at the same state: |v.n| + |v_rain n2| and the speed of sound,
+  // each primitive computed once
+  TAG_DEV static void flux_and_speeds(const double* u, double n1, double n2, double* f,
+                                      double& vabs, double& c) {
+    using C = RainyConst;
+    double rv, rc, T;
+    nlsol(u, rv, rc, T);
+    const double rho = u[0] + u[1] + u[2];
+    const double ri = 1.0 / rho;
+    const double v1 = u[3] * ri, v2 = u[4] * ri;
+    const double vr = rainy_v_rain(u[1], u[2]);
+    const double vn = v1 * n1 + v2 * n2;
+    const double vrn = vr * n2;
+    const double p = (C::R_d * u[0] + C::R_v * rv) * T;
+    f[0] = u[0] * vn;
+    f[1] = u[1] * vn;
+    f[2] = u[2] * (vn - vrn);
+    f[3] = rho * vn * v1 + p * n1 - u[2] * vrn * v1;
+    f[4] = rho * vn * v2 + p * n2 - u[2] * vrn * v2;
+    f[5] = (u[5] + p) * vn - (C::c_l * T + 0.5 * (v1 * v1 + v2 * v2)) * u[2] * vrn;
+    f[6] = f[7] = f[8] = 0.0;
+    vabs = fabs(vn) + fabs(vrn);
+    const double q_v = rv / u[0];
+    const double q_l = (rc + u[2]) / u[0];
+    const double gm = 1.0 + (C::R_d + C::R_v * q_v) / (C::c_vd + C::c_vv * q_v + C::c_l * q_l);
+    c = sqrt(gm * p * ri);
+  }
+
   // speed_of_sound (:332-366) and the normal speeds of max_abs_speed_naive (:595-611)
   TAG_DEV static double sound(const double* u) {
     using C = RainyConst;
@@ -257,13 +296,10 @@ struct PhysRainy2D {
       lmars(ul, ur, n1, n2, F);
       return;
     }
-    double fl[9], fr[9];
-    flux(P, ul, n1, n2, fl);
-    flux(P, ur, n1, n2, fr);
-    const double ril = 1.0 / (ul[0] + ul[1] + ul[2]), rir = 1.0 / (ur[0] + ur[1] + ur[2]);
-    const double vl = fabs(ul[3] * ril * n1 + ul[4] * ril * n2) + fabs(rainy_v_rain(ul[1], ul[2]) * n2);
-    const double vr = fabs(ur[3] * rir * n1 + ur[4] * rir * n2) + fabs(rainy_v_rain(ur[1], ur[2]) * n2);
-    const double lam = fmax(vl, vr) + fmax(sound(ul), sound(ur)) * sqrt(n1 * n1 + n2 * n2);
+    double fl[9], fr[9], vl, vr, cl, cr;
+    flux_and_speeds(ul, n1, n2, fl, vl, cl);
+    flux_and_speeds(ur, n1, n2, fr, vr, cr);
+    const double lam = fmax(vl, vr) + fmax(cl, cr) * sqrt(n1 * n1 + n2 * n2);
 #pragma unroll
     for (int v = 0; v < 9; ++v) F[v] = 0.5 * (fl[v] + fr[v]) - 0.5 * lam * (ur[v] - ul[v]);
   }
@@ -315,10 +351,14 @@ struct PhysRainy2D {
       nlsol(u, rv, rc, T);
       const double rho = u[0] + u[1] + u[2];
       const double rho_vs = rainy_e_s(T) / (C::R_v * T);
-      double S_ev = (3.86e-3 - 9.41e-5 * (T - C::ref_temp)) * (1.0 + 9.1 * pow(u[2], 0.1875));
-      S_ev *= (rho_vs - rv) * pow(u[2], 0.5);
+      // rho_r^0.1875, rho_r^0.5 and rho_r^0.875 from square roots: with
+      // r8 = rho_r^(1/8) and r16 = r8^(1/2), r16^3, sqrt(rho_r) and r8^7
+      const double r8 = rainy_root8(u[2]), r16 = sqrt(r8);
+      const double r8_2 = r8 * r8, r8_4 = r8_2 * r8_2;
+      double S_ev = (3.86e-3 - 9.41e-5 * (T - C::ref_temp)) * (1.0 + 9.1 * (r16 * r16 * r16));
+      S_ev *= (rho_vs - rv) * sqrt(u[2]);
       const double S_auto = 0.001 * rc;
-      const double S_acc = 1.72 * rc * pow(u[2], 0.875);
+      const double S_acc = 1.72 * rc * (r8_4 * r8_2 * r8);
       const double S_rain = S_auto + S_acc - S_ev;
       s[0] = 0.0; s[1] = -S_rain; s[2] = S_rain; s[3] = 0.0;
       s[4] = -rho * C::g; s[5] = -u[4] * C::g; s[6] = s[7] = s[8] = 0.0;
