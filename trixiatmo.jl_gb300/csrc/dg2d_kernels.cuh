@@ -423,25 +423,65 @@ __global__ void k_element(typename Phys::Params Pp, const BasisDev basis, double
 // ---------------------------------------------------------------------------
 // CFL speed reduction of a state (Trixi.max_dt) and per-step scalars
 // ---------------------------------------------------------------------------
+// Tile of k_max_speed: EPB elements per CTA, one thread per node.
+template <int n>
+struct MaxSpeedTile {
+  static constexpr int nn = n * n;
+  static constexpr int EPB = nn >= 256 ? 1 : 256 / nn;
+  static constexpr int T = EPB * nn;
+};
+
+// One thread per node: the node's two contravariant speeds |Ja^d . lambda| / J
+// go to shared memory; per element the maxima over its nodes are summed
+// (Trixi's max_lambda1 + max_lambda2); one atomic per CTA when all its
+// elements belong to one member, else one per element.
 template <class Phys, int n>
-__global__ void k_max_speed(typename Phys::Params Pp, const double* __restrict__ u,
-                            const double* __restrict__ Ja, const double* __restrict__ invJ,
-                            int nelem, const int* __restrict__ member,
-                            double* __restrict__ max_speed) {
+__global__ void __launch_bounds__(MaxSpeedTile<n>::T) k_max_speed(
+    typename Phys::Params Pp, const double* __restrict__ u, const double* __restrict__ Ja,
+    const double* __restrict__ invJ, int nelem, const int* __restrict__ member,
+    double* __restrict__ max_speed) {
+  using K = MaxSpeedTile<n>;
   constexpr int NV = Phys::NV, nn = n * n;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= nelem) return;
-  double m1 = 0.0, m2 = 0.0;
-  for (int node = 0; node < nn; ++node) {
-    const size_t q = (size_t)e * nn + node;
+  __shared__ double s1[K::T], s2[K::T], se[K::EPB];
+  const int e0 = blockIdx.x * K::EPB;
+  const int t = threadIdx.x;
+  double a = 0.0, b = 0.0;
+  if (e0 + t / nn < nelem) {
+    const size_t q = (size_t)e0 * nn + t;
     double l1, l2;
     Phys::max_speeds(Pp, u + q * NV, l1, l2);
     const double* ja = Ja + q * 4;
     const double ij = fabs(invJ[q]);
-    m1 = fmax(m1, fabs(ja[0] * l1 + ja[1] * l2) * ij);
-    m2 = fmax(m2, fabs(ja[2] * l1 + ja[3] * l2) * ij);
+    a = fabs(ja[0] * l1 + ja[1] * l2) * ij;
+    b = fabs(ja[2] * l1 + ja[3] * l2) * ij;
   }
-  atomic_max_nonneg(max_speed + (member ? member[e] : 0), m1 + m2);
+  s1[t] = a;
+  s2[t] = b;
+  __syncthreads();
+  if (t < K::EPB) {
+    double m1 = 0.0, m2 = 0.0;
+    for (int k = 0; k < nn; ++k) {
+      m1 = fmax(m1, s1[t * nn + k]);
+      m2 = fmax(m2, s2[t * nn + k]);
+    }
+    se[t] = m1 + m2;
+  }
+  __syncthreads();
+  if (t == 0) {
+    const int ne = min(K::EPB, nelem - e0);
+    const int m0 = member ? member[e0] : 0;
+    bool uniform = true;
+    double mx = 0.0;
+    for (int k = 0; k < ne; ++k) {
+      if (member && member[e0 + k] != m0) uniform = false;
+      mx = fmax(mx, se[k]);
+    }
+    if (uniform) {
+      atomic_max_nonneg(max_speed + m0, mx);
+    } else {
+      for (int k = 0; k < ne; ++k) atomic_max_nonneg(max_speed + member[e0 + k], se[k]);
+    }
+  }
 }
 
 // Start of an RK step, per member: t += previous dt; dt = cfl * 2 / (n *

@@ -312,8 +312,7 @@ int tag_newton_solve_states(double* u, int64_t n, int32_t mode, double tol, int3
     MLP_CUDA(cudaMemcpy(dP, mlp, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice));
   }
   NewtonArgs a{mode, max_iterations, polish, mlp ? 1 : 0, 8, tol, dP, dI, dC};
-  k_newton_rainy<<<(unsigned)((n + 255) / 256), 256>>>(dU, (long)n, a, dS);
-  MLP_CUDA(cudaGetLastError());
+  MLP_CUDA(launch_newton_rainy(dU, (long)n, a, dS, nullptr));
   unsigned long long c[4];
   MLP_CUDA(cudaMemcpy(u, dU, sizeof(double) * 9 * n, cudaMemcpyDeviceToHost));
   MLP_CUDA(cudaMemcpy(c, dC, sizeof(c), cudaMemcpyDeviceToHost));

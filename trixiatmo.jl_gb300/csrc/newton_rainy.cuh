@@ -256,11 +256,13 @@ TAG_DEV bool rainy_learned_guess(const float* __restrict__ P, const double* u, d
 // updates taken, with whether a fallback happened and whether it converged.
 TAG_DEV int newton_rainy_node(const float* sp, double* __restrict__ un, const NewtonArgs& a,
                               int& fallback, bool& conv) {
-  double s[9];
+  // the node's conserved variables (slots 1-6), copied before the rain
+  // clamp; the solve reads no other slot
+  double s[6];
 #pragma unroll
-  for (int v = 0; v < 9; ++v) s[v] = un[v];  // the node copy is taken before the rain clamp
+  for (int v = 0; v < 6; ++v) s[v] = un[v];
   if (un[2] < 0.0) un[2] = 0.0;
-  double x[3] = {s[6], s[7], s[8]};
+  double x[3] = {un[6], un[7], un[8]};
   conv = false;
   fallback = 0;
   int its = 0;
@@ -301,6 +303,9 @@ TAG_DEV int newton_rainy_node(const float* sp, double* __restrict__ un, const Ne
   return its;
 }
 
+// The stage limiter over all nodes, one thread per node, 256 threads per CTA
+// (launch through launch_newton_rainy); the network's parameters are staged
+// in shared memory for starts 1 and 3.
 static __global__ void __launch_bounds__(256) k_newton_rainy(double* __restrict__ u, long nodes,
                                                       NewtonArgs a, unsigned* __restrict__ status) {
   __shared__ float sp[kMlpParams];
@@ -332,6 +337,13 @@ static __global__ void __launch_bounds__(256) k_newton_rainy(double* __restrict_
       if (unconverged) atomicAdd(a.counters + 2, (unsigned long long)unconverged);
     }
   }
+}
+
+// Launches k_newton_rainy over `nodes` nodes (u[nodes][9]) on `stream`.
+static inline cudaError_t launch_newton_rainy(double* u, long nodes, const NewtonArgs& a,
+                                              unsigned* status, cudaStream_t stream) {
+  k_newton_rainy<<<(unsigned)((nodes + 255) / 256), 256, 0, stream>>>(u, nodes, a, status);
+  return cudaGetLastError();
 }
 
 }  // namespace tag

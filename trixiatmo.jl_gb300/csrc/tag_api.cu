@@ -239,8 +239,8 @@ struct OpsImpl {
     return TAG_OK;
   }
   static int max_speed(tag_handle h, const double* u) {
-    const int threads = 128;
-    k_max_speed<Phys, n><<<(h->nelem + threads - 1) / threads, threads, 0, h->stream>>>(
+    using K = MaxSpeedTile<n>;
+    k_max_speed<Phys, n><<<(h->nelem + K::EPB - 1) / K::EPB, K::T, 0, h->stream>>>(
         params_of<Phys>(h), u, h->d_Ja, h->d_invJ, h->nelem, h->d_member,
         h->d_mscal + 2 * h->nmembers);
     TAG_CUDA(cudaGetLastError());
@@ -432,9 +432,7 @@ int stage_sequence(tag_handle h) {
       a.mlp = h->d_mlp;
       a.iters = nullptr;
       a.counters = h->d_run_counters;
-      k_newton_rainy<<<(unsigned)((nodes + 255) / 256), 256, 0, h->stream>>>(h->d_u, nodes, a,
-                                                                              h->d_status);
-      TAG_CUDA(cudaGetLastError());
+      TAG_CUDA(launch_newton_rainy(h->d_u, nodes, a, h->d_status, h->stream));
       if (s == ns - 1) {
         rc = h->ops->max_speed(h, h->d_u);
         if (rc) return rc;
@@ -1547,9 +1545,7 @@ int tag_rk_adaptive(tag_handle h, double* t, double t_end, double abstol, double
         a.mlp = h->d_mlp;
         a.iters = nullptr;
         a.counters = h->d_run_counters;
-        k_newton_rainy<<<(unsigned)((nodes + 255) / 256), 256, 0, h->stream>>>(h->d_u, nodes, a,
-                                                                                h->d_status);
-        TAG_CUDA(cudaGetLastError());
+        TAG_CUDA(launch_newton_rainy(h->d_u, nodes, a, h->d_status, h->stream));
         h->run_node_solves += nodes;
       }
     }
@@ -1724,9 +1720,7 @@ int tag_newton_solve(tag_handle h, int32_t use_learned, int32_t* iters, tag_newt
   a.iters = h->d_iters;
   a.counters = h->d_counters;
   TAG_CUDA(cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * 4, h->stream));
-  k_newton_rainy<<<(unsigned)((nodes + 255) / 256), 256, 0, h->stream>>>(h->d_u, nodes, a,
-                                                                          h->d_status);
-  TAG_CUDA(cudaGetLastError());
+  TAG_CUDA(launch_newton_rainy(h->d_u, nodes, a, h->d_status, h->stream));
   unsigned long long c[4];
   TAG_CUDA(cudaMemcpyAsync(c, h->d_counters, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
   if (iters)
