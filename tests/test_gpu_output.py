@@ -128,3 +128,29 @@ def test_save_solution_file_round_trip(tg, gpu_lib, out, tmp_path):
         "h", "h_vcon1", "h_vcon2"]
     assert g.datasets["variables_1"].data.tobytes() == u1.reshape(-1, 3)[:, 0].copy().tobytes()
     semi.close()
+
+
+def test_ensemble_files_one_per_member(tg, gpu_lib, out, tmp_path):
+    """A Cartesian ensemble written whole: one file per member (its own
+    system), each with the member's element count and its slice of the state."""
+    eq = tg.CompressibleEulerEnergyEquationsWithGravity2D(c_p=1004, c_v=717, gravity=9.81)
+    solver = tg.DGSEM(3, (tg.FluxLMARS(340.0), tg.flux_zero),
+                      tg.VolumeIntegralFluxDifferencing(
+                          (tg.flux_ranocha, tg.flux_nonconservative_waruszewski_etal)))
+    meshes = [tg.StructuredMesh((nx, 2), (0.0, 0.0), (20000.0, 10000.0), periodicity=(True, False))
+              for nx in (4, 6)]
+    bcs = {"y_neg": tg.boundary_condition_slip_wall, "y_pos": tg.boundary_condition_slip_wall}
+    ens = tg.SemidiscretizationEnsemble(meshes, eq, [tg.WarmBubble()] * 2, solver,
+                                        boundary_conditions=bcs)
+    u = ens.compute_coefficients()
+    ens.set_state(u)
+    names = out.save_solution_file(ens, 0.0, 0.0, 0, str(tmp_path), system="bubble")
+    assert names == [str(tmp_path / f"solution_bubble_member{m}_000000000.h5") for m in range(2)]
+    for m, name in enumerate(names):
+        f = H5File(name)
+        assert f.attrs["n_elements"] == (8, 12)[m] and f.attrs["polydeg"] == 3
+        assert f.attrs["mesh_type"] == "StructuredMesh" and f.attrs["n_vars"] == 5
+        um = u.reshape(-1, 5)[ens.member_slice(m).start * 16:ens.member_slice(m).stop * 16]
+        for v in range(5):
+            assert np.array_equal(f.datasets[f"variables_{v + 1}"].data, um[:, v])
+    ens.close()

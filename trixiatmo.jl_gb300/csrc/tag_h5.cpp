@@ -224,7 +224,7 @@ extern "C" int tag_h5_write(const char* path, const tag_h5_attribute* attrs, int
   for (int32_t k = 0; k < nsets; ++k) {
     const tag_h5_dataset& d = sets[k];
     if (!valid_name(d.name)) return h5fail(TAG_E_INVALID, "dataset name empty or with '/'");
-    if (d.count < 0 || (d.count > 0 && !d.data))
+    if (d.count < 0 || d.count > (int64_t(1) << 56) || (d.count > 0 && !d.data))
       return h5fail(TAG_E_INVALID, std::string("dataset ") + d.name + ": bad data or count");
     if (d.var_name && std::strlen(d.var_name) > 60000)
       return h5fail(TAG_E_INVALID, "variable name longer than 60000 bytes");

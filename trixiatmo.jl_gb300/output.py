@@ -199,11 +199,12 @@ def save_solution_file(semi, time, dt, timestep, output_directory,
                        element_variables=None, node_variables=None):
     """Trixi.save_solution_file for the handle's current state; returns the
     file name (a list of names, one per member, for an ensemble written
-    whole: each member is its own system `member<m>`)."""
+    whole: each member is its own system, `member<m>` or `<system>_member<m>`)."""
     nm = getattr(semi, "nmembers", 1)
     if nm > 1 and member is None:
         return [save_solution_file(semi, time, dt, timestep, output_directory,
-                                   solution_variables, system or f"member{m}", m, mesh_file)
+                                   solution_variables,
+                                   f"{system}_member{m}" if system else f"member{m}", m, mesh_file)
                 for m in range(nm)]
     names = varnames(solution_variables, semi.equations)
     data = convert_variables(semi, solution_variables, member)
