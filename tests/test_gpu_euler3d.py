@@ -164,3 +164,39 @@ def test_set_state_from_pinned_memory_matches_pageable(tg, gpu_lib):
     assert out[0][1] == out[1][1] and out[0][2] == out[1][2]
     assert np.array_equal(out[0][3], out[1][3])
     semi.close()
+
+
+def test_state_sink_holds_each_steps_result(tg, gpu_lib):
+    """With a state sink registered, the last stage of every step stores the
+    new state into the pinned buffer from inside its kernel: after rk_steps it
+    equals get_state bit for bit, for one step and for several; the steps
+    themselves are unchanged; a cleared sink is no longer written; a pageable
+    array or a 2D handle is refused."""
+    torch = pytest.importorskip("torch")
+    eq, mesh, semi = make_semi(tg, 2, 2, 4)
+    u = perturb3d(semi.compute_coefficients(), eq, seed=5)
+    ref = []
+    semi.set_state(u)
+    for nsteps in (1, 3):
+        semi.rk_steps(nsteps, cfl=0.8, t=0.0)
+        ref.append(semi.get_state())
+    sink = torch.empty(u.shape, dtype=torch.float64, pin_memory=True).numpy()
+    sink[...] = np.nan
+    semi.set_state_sink(sink)
+    semi.set_state(u)
+    for k, nsteps in enumerate((1, 3)):
+        semi.rk_steps(nsteps, cfl=0.8, t=0.0)
+        assert np.array_equal(sink, semi.get_state())
+        assert np.array_equal(sink, ref[k])
+    semi.set_state_sink(None)
+    sink[...] = 0.0
+    semi.rk_steps(1, cfl=0.8, t=0.0)
+    assert not sink.any()
+    with pytest.raises(tg._lib.TagError, match="pinned"):
+        semi.set_state_sink(np.zeros_like(u))
+    semi.close()
+    from test_gpu_euler2d import make_semi as make_2d
+    _, semi2 = make_2d(tg, 4, 2)
+    with pytest.raises(tg._lib.TagError, match="3D handle"):
+        semi2.set_state_sink(torch.empty(semi2.shape, dtype=torch.float64, pin_memory=True).numpy())
+    semi2.close()

@@ -197,6 +197,7 @@ SIGNATURES = {
                                      ctypes.c_int32, ctypes.c_float, ctypes.c_uint64, _fp]),
     "tag_rhs_noalloc": (ctypes.c_int, [ctypes.POINTER(TagConfig), _dp, _dp, ctypes.c_void_p,
                                        ctypes.POINTER(ctypes.c_uint32)]),
+    "tag_set_state_sink": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "tag_solution_variables": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                               _ip, ctypes.POINTER(ctypes.c_int64), _dp]),
     "tag_h5_write": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(H5Attribute), ctypes.c_int32,

@@ -36,6 +36,8 @@ struct StageArgs {
   const double* t_member;         // per-member step start time (stage mode)
   double t_rhs;                   // time of an rhs evaluation (rhs mode)
   const double* xy;               // node coordinates (sources), or null
+  double* sink;                   // last stage of a 3D step: the new state is also stored
+                                  // here (mapped host memory), or null
 };
 
 inline void set_stage(StageArgs& st, int scheme, int stage) {

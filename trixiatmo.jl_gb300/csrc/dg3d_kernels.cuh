@@ -322,6 +322,18 @@ __global__ void k_element3d(typename Phys::Params Pp, const BasisDev basis, doub
             fabs(ja[3 * d] * lam[0] + ja[3 * d + 1] * lam[1] + ja[3 * d + 2] * lam[2]) * ij;
     }
     __syncthreads();
+    // the step's result to the registered sink (host memory over the host
+    // link): each element's state is one contiguous block, stored by
+    // consecutive threads at consecutive addresses
+    if (st.sink != nullptr) {
+      double* o = st.sink + (size_t)e_first * nnn * NV;
+      for (int t = threadIdx.x; t < ne * nnn * NV; t += nthr) {
+        const int el = t / (nnn * NV), r = t % (nnn * NV);
+        const int node = r / NV, v = r % NV;
+        const double* eb = base + el * S::per_elem;
+        o[t] = v < NA ? eb[S::oA + node * NA + v] : eb[S::oU + node * NV + v];
+      }
+    }
     // one warp per element: the per-direction maxima over its nodes on the
     // integer pipe (the speeds are non-negative, and the bit patterns of
     // non-negative doubles order like their values), then summed

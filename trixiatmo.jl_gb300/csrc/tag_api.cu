@@ -124,6 +124,12 @@ struct tag_handle_s {
   unsigned* d_status = nullptr;
   cudaGraphExec_t graph = nullptr;
   int graph_epb = -1;
+  // 3D: mapped host array that the last stage of every tag_rk_steps step also
+  // stores the new state into (tag_set_state_sink); armed only while the step
+  // graph is captured, so that no other stage sequence writes it
+  double* sink = nullptr;
+  double* graph_sink = nullptr;
+  bool capturing_steps = false;
   bool speed_valid = false;
   int epb = 0;
   // threads of a CTA = its elements' work items / tile_div, rounded up to
@@ -307,6 +313,7 @@ struct OpsImpl3D {
       set_stage(st, h->scheme, stage);
       st.dt = h->d_mscal + h->nmembers;
       st.max_speed = last ? h->d_mscal + 2 * h->nmembers : nullptr;
+      st.sink = last && h->capturing_steps ? h->sink : nullptr;
       k_element3d<Phys, n, kModeStage><<<blocks, threads, smem, h->stream>>>(
           params_of<Phys>(h), h->basis, u, du, h->d_k, h->d_Ja, h->d_invJ, h->d_sfv, h->nelem,
           epb, st, h->d_status);
@@ -444,20 +451,23 @@ int stage_sequence(tag_handle h) {
 
 int build_graph(tag_handle h) {
   const int key = h->epb * 8 + h->tile_div;
-  if (h->graph && h->graph_epb == key) return TAG_OK;
+  if (h->graph && h->graph_epb == key && h->graph_sink == h->sink) return TAG_OK;
   if (h->graph) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
   }
   cudaGraph_t g;
   TAG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  h->capturing_steps = true;
   int rc = stage_sequence(h);
+  h->capturing_steps = false;
   cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
   if (rc) return rc;
   if (e2 != cudaSuccess) return fail(TAG_E_CUDA, cudaGetErrorString(e2));
   TAG_CUDA(cudaGraphInstantiate(&h->graph, g, 0));
   cudaGraphDestroy(g);
   h->graph_epb = key;
+  h->graph_sink = h->sink;
   return TAG_OK;
 }
 
@@ -1323,6 +1333,24 @@ int tag_solution_variables(tag_handle h, int32_t solution_variables, int32_t mem
   if (e == cudaSuccess) e = ef != cudaSuccess ? ef : es;
   if (e != cudaSuccess) return fail(TAG_E_CUDA, std::string("tag_solution_variables: ") +
                                                     cudaGetErrorString(e));
+  return TAG_OK;
+}
+
+int tag_set_state_sink(tag_handle h, double* u_host) {
+  if (!h) return fail(TAG_E_INVALID, "null handle");
+  if (h->dim != 3) return fail(TAG_E_INVALID, "a state sink needs a 3D handle");
+  if (!u_host) {
+    h->sink = nullptr;
+    return TAG_OK;
+  }
+  cudaPointerAttributes attr{};
+  const bool mapped = cudaPointerGetAttributes(&attr, u_host) == cudaSuccess &&
+                      attr.type == cudaMemoryTypeHost && attr.devicePointer != nullptr;
+  if (!mapped) {
+    cudaGetLastError();
+    return fail(TAG_E_INVALID, "the state sink must be pinned host memory mapped for the device");
+  }
+  h->sink = static_cast<double*>(attr.devicePointer);
   return TAG_OK;
 }
 

@@ -432,6 +432,20 @@ class SemidiscretizationHyperbolic:
             raise ValueError("u has the wrong size")
         _lib.check(self._L.tag_set_state(self._h, _ptr(u)))
 
+    def set_state_sink(self, out):
+        """tag_set_state_sink (3D): while registered, the last stage of every
+        rk_steps step stores the new state into `out` (pinned host memory,
+        float64, the state's shape) from inside its kernel; None clears it."""
+        if out is None:
+            _lib.check(self._L.tag_set_state_sink(self._h, None))
+            self._sink = None
+            return
+        if (out.dtype != np.float64 or not out.flags.c_contiguous
+                or out.size != int(np.prod(self.shape))):
+            raise ValueError("the sink must be a C-contiguous float64 array of the state's size")
+        _lib.check(self._L.tag_set_state_sink(self._h, _ptr(out)))
+        self._sink = out  # kept alive while registered
+
     def get_state(self, out=None):
         if out is None:
             out = np.empty(self.shape)
