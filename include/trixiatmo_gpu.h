@@ -73,6 +73,7 @@ extern "C" {
 #define TAG_VF_PT_EC 8               /* potential temperature: (flux_ec, nonconservative gravity term)  */
 #define TAG_VF_PT_ETEC 9             /* potential temperature: (flux_etec, nonconservative gravity term) */
 #define TAG_VF_IE_ETEC 10            /* internal energy: (flux_conservative_etec, flux_nonconservative_etec) */
+#define TAG_VF_PT_KG 11              /* potential temperature 3D: (flux_kennedy_gruber, a nonconservative gravity term) */
 #define TAG_SF_LMARS 1               /* (FluxLMARS(c), flux_zero)                       */
 #define TAG_SF_LAX_FRIEDRICHS 2      /* flux_lax_friedrichs (max_abs_speed_naive)       */
 #define TAG_SF_CHANDRASHEKAR 3       /* flux_chandrashekar as surface flux (moist)      */

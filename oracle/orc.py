@@ -337,7 +337,7 @@ class Euler3D:
 class PotTemp3D:
     """Potential-temperature Euler with gravity in 3D (shell geometry and
     connectivity are the host mirror's arrays).  volume 0 flux_tec, 1 flux_ec,
-    2 flux_etec; nc 0 waruszewski, 1 artiano, 2 souza."""
+    2 flux_etec, 3 flux_kennedy_gruber; nc 0 waruszewski, 1 artiano, 2 souza."""
 
     nv = 6
 

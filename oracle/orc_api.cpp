@@ -899,7 +899,8 @@ double orc_pt3d_ssprk43_adaptive(void* h, double* u, double t, double t_end, con
 }
 
 // pointwise 3D fluxes for the consistency tests: kind 0 flux, 1 volume flux
-// (tec / ec / etec by `volume`), 2 nonconservative term (by `nc`), 3 LMARS(c)
+// (tec / ec / etec / kennedy_gruber by `volume`), 2 nonconservative term (by
+// `nc`), 3 LMARS(c)
 void orc_pt3d_pointwise(int kind, int volume, int nc, double c, const double* ul,
                         const double* ur, const double* n, double* f) {
   PotTemp3D eq;

@@ -22,7 +22,7 @@ struct PotTemp3D {
   using State = std::array<double, 6>;
   double c_p = 1004.0, c_v = 717.0, g = 9.80616, p_0 = 100000.0;
   double R = 287.0, gamma = 1004.0 / 717.0, K = 0.0, sc[8];
-  int volume = 0;   // 0 flux_tec, 1 flux_ec, 2 flux_etec
+  int volume = 0;   // 0 flux_tec, 1 flux_ec, 2 flux_etec, 3 flux_kennedy_gruber
   int nc_kind = 0;  // 0 waruszewski (ln_mean rho), 1 artiano (stolarsky rho), 2 souza (average)
 
   void init(double cp, double cv, double grav) {
@@ -83,6 +83,11 @@ struct PotTemp3D {
     } else if (volume == 1) {
       f1 = ln_mean(rl, rr) * 0.5 * (vnl + vnr);
       f5 = f1 * inv_ln_mean(rl / ul[4], rr / ur[4]);
+    } else if (volume == 3) {
+      // flux_kennedy_gruber, src/equations/compressible_euler_potential_temperature_gravity_3d.jl:333-359
+      const double v_dot_n_avg = va[0] * n[0] + va[1] * n[1] + va[2] * n[2];
+      f1 = 0.5 * (rl + rr) * v_dot_n_avg;
+      f5 = f1 * (0.5 * (ul[4] / rl + ur[4] / rr));
     } else {
       f5 = stolarsky(ul[4], ur[4]) * 0.5 * (vnl + vnr);
       f1 = f5 * ln_mean(rl / ul[4], rr / ur[4]);

@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 RTOL = 1e-12
 RTOL_VAR = 1e-11
-VOLUME = {"tec": 0, "ec": 1, "etec": 2}
+VOLUME = {"tec": 0, "ec": 1, "etec": 2, "kennedy_gruber": 3}
 NC = {"waruszewski": 0, "artiano": 1, "souza": 2}
 
 
@@ -25,7 +25,8 @@ def make_pt3d(tg, trees, layers, polydeg, volume="tec", nc="souza"):
         c_p=1004, c_v=717, gravity=tg.EARTH_GRAVITATIONAL_ACCELERATION)
     mesh = tg.P4estMeshCubedSphereTopography(trees, layers, tg.EARTH_RADIUS, 30000.0,
                                              polydeg=polydeg)
-    vf = {"tec": tg.flux_tec, "ec": tg.flux_ec, "etec": tg.flux_etec}[volume]
+    vf = {"tec": tg.flux_tec, "ec": tg.flux_ec, "etec": tg.flux_etec,
+          "kennedy_gruber": tg.flux_kennedy_gruber}[volume]
     ncf = {"waruszewski": tg.flux_nonconservative_waruszewski_etal,
            "artiano": tg.flux_nonconservative_artiano_etal,
            "souza": tg.flux_nonconservative_souza_etal}[nc]
@@ -53,7 +54,9 @@ def rel(a, b):
 
 @pytest.mark.parametrize("polydeg", [2, 3, 4, 5, 7])
 @pytest.mark.parametrize("volume,nc", [("tec", "souza"), ("ec", "waruszewski"),
-                                       ("etec", "artiano"), ("tec", "waruszewski")])
+                                       ("etec", "artiano"), ("tec", "waruszewski"),
+                                       ("kennedy_gruber", "souza"),
+                                       ("kennedy_gruber", "waruszewski")])
 def test_pt3d_rhs_matches_oracle(tg, orc, gpu_lib, polydeg, volume, nc):
     eq, mesh, semi = make_pt3d(tg, 3, 2, polydeg, volume, nc)
     u = perturb_pt3d(semi.compute_coefficients(), seed=polydeg)
@@ -190,3 +193,37 @@ def test_gpu_reproduces_vortex_shedding_goldens(tg, orc, gpu_lib, case):
     assert (st["accepted"], st["rejected"]) == (sto["accepted"], sto["rejected"]), (st, sto)
     assert rel(u[..., :5], uo[..., :5]) <= 1e-8  # step sizes from rounding-sensitive norms
     semi.close()
+
+
+def test_combined_fluxes_run_as_their_tuples(tg, orc, gpu_lib):
+    """The reference's "combined fluxes" testset
+    (test/test_3d_potential_temperature.jl:179-208): the baroclinic instability
+    on trees_per_cube_face = (2, 2) for 100 s with (flux_kennedy_gruber,
+    flux_nonconservative_souza_etal) / (FluxLMARS(340), flux_zero), and the
+    same with the fused flux_kennedy_gruber_souza_etal / flux_lmars_combined.
+    The fused spellings run the same kernels (same bits); the run matches the
+    oracle's step for step (error-controlled SSPRK43, abstol = reltol = 1e-6 as
+    the elixir; no stop before the end)."""
+    eq, mesh, semi = make_pt3d(tg, 2, 2, 5, "kennedy_gruber", "souza")
+    fused = tg.SemidiscretizationHyperbolic(
+        mesh, eq, tg.initial_condition_baroclinic_instability,
+        tg.DGSEM(5, tg.flux_lmars_combined,
+                 tg.VolumeIntegralFluxDifferencing(tg.flux_kennedy_gruber_souza_etal)),
+        source_terms=tg.source_terms_coriolis,
+        boundary_conditions={"inside": tg.boundary_condition_slip_wall,
+                             "outside": tg.boundary_condition_slip_wall})
+    u0 = semi.compute_coefficients()
+    runs = []
+    for s_ in (semi, fused):
+        s_.set_state(u0)
+        t, st = s_.solve_adaptive((0.0, 100.0), abstol=1e-6, reltol=1e-6)
+        assert t == 100.0
+        runs.append((s_.get_state(), st))
+    assert np.array_equal(runs[0][0], runs[1][0]) and runs[0][1] == runs[1][1]
+    o = oracle_pt3d(orc, tg, semi, mesh, "kennedy_gruber", "souza")
+    uo = np.ascontiguousarray(u0).copy()
+    to, sto = o.ssprk43_adaptive(uo, 0.0, 100.0, abstol=1e-6, reltol=1e-6)
+    assert to == 100.0 and abs(runs[0][1]["accepted"] - sto["accepted"]) <= 1, (runs[0][1], sto)
+    assert rel(runs[0][0][..., :5], uo[..., :5]) <= 1e-8, rel(runs[0][0][..., :5], uo[..., :5])
+    semi.close()
+    fused.close()

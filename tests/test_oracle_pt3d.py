@@ -21,13 +21,36 @@ NORMALS = [(1.0, 0.0, 0.0), (0.0, 1.0, 0.0), (0.0, 0.0, 1.0), (0.5, -0.5, 0.2), 
 RTOL = 1.4901161193847656e-08  # Julia's isapprox default, sqrt(eps)
 
 
-@pytest.mark.parametrize("volume", [0, 1, 2])
+@pytest.mark.parametrize("volume", [0, 1, 2, 3])
 def test_volume_fluxes_consistent(orc, volume):
     u = np.array([1.1, -0.5, 2.34, 2.4, 330.0, 1500.0])
     for n in NORMALS:
         f = orc.pt_pointwise(3, 0, u, u, n)
         fv = orc.pt_pointwise(3, 1, u, u, n, volume=volume)
         assert np.allclose(fv, f, rtol=RTOL, atol=0.0), (n, fv, f)
+
+
+def test_kennedy_gruber_formula(orc):
+    """flux_kennedy_gruber
+    (src/equations/compressible_euler_potential_temperature_gravity_3d.jl:333-359),
+    restated here in NumPy, against the oracle's on random state pairs."""
+    c_p, c_v = 1004.0, 717.0
+    R, gamma, p0 = c_p - c_v, c_p / c_v, 1.0e5
+    rng = np.random.default_rng(11)
+    for _ in range(50):
+        ul = np.array([rng.uniform(0.5, 1.5), *rng.normal(size=3), rng.uniform(250, 400), 0.0])
+        ur = np.array([rng.uniform(0.5, 1.5), *rng.normal(size=3), rng.uniform(250, 400), 0.0])
+        n = rng.normal(size=3)
+        p = [p0 * (R * u[4] / p0) ** gamma for u in (ul, ur)]
+        v = [u[1:4] / u[0] for u in (ul, ur)]
+        rho_avg = 0.5 * (ul[0] + ur[0])
+        v_avg = 0.5 * (v[0] + v[1])
+        p_avg = 0.5 * (p[0] + p[1])
+        theta_avg = 0.5 * (ul[4] / ul[0] + ur[4] / ur[0])
+        f1 = rho_avg * (v_avg @ n)
+        ref = np.array([f1, *(f1 * v_avg + p_avg * n), f1 * theta_avg, 0.0])
+        got = orc.pt_pointwise(3, 1, ul, ur, n, volume=3)
+        assert np.allclose(got, ref, rtol=1e-13, atol=1e-13 * np.abs(ref).max()), (got, ref)
 
 
 def test_lmars_consistent(orc):

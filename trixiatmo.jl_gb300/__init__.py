@@ -27,7 +27,9 @@ from .equations import (CompressibleEulerEnergyEquationsWithGravity2D,
                         CompressibleEulerInternalEnergyEquationsWithGravity2D,
                         flux_conservative_etec, flux_nonconservative_etec,
                         flux_conservative_es, flux_nonconservative_es, flux_ec,
-                        flux_tec, flux_etec, flux_nonconservative_artiano_etal,
+                        flux_tec, flux_etec, flux_kennedy_gruber,
+                        flux_kennedy_gruber_souza_etal, flux_lmars_combined,
+                        flux_nonconservative_artiano_etal,
                         flux_nonconservative_souza_etal)
 from .initial_conditions import (EARTH_GRAVITATIONAL_ACCELERATION, EARTH_RADIUS,
                                  EARTH_ROTATION_RATE, SMALL_EARTH_RADIUS,
@@ -88,6 +90,7 @@ __all__ = [
     "flux_nonconservative_etec", "flux_conservative_es", "flux_nonconservative_es",
     "flux_ec", "flux_tec",
     "flux_etec", "flux_nonconservative_artiano_etal", "flux_nonconservative_souza_etal",
+    "flux_kennedy_gruber", "flux_kennedy_gruber_souza_etal", "flux_lmars_combined",
     "trixi_connectivity", "output", "save_solution_file", "convert_variables", "varnames",
     "cons2cons", "cons2prim", "contravariant2global", "cons2prim_and_vorticity",
 ]

@@ -56,6 +56,7 @@ TAG_EQ_POTENTIAL_TEMPERATURE_2D = 6
 TAG_EQ_POTENTIAL_TEMPERATURE_3D = 7
 TAG_EQ_INTERNAL_ENERGY_2D = 8
 TAG_VF_IE_ETEC = 10
+TAG_VF_PT_KG = 11
 TAG_SF_IE_ES = 7
 TAG_SF_PT_EC = 8
 TAG_VF_PT_TEC = 7

@@ -32,7 +32,8 @@ struct PhysPT2D {
   struct Params {
     double gamma, K, c_lmars, stol_fac;  // stol_fac = (gamma - 1) / gamma
     double sc[8];                        // Stolarsky series coefficients
-    int volume;                          // 0 flux_tec, 1 flux_ec, 2 flux_etec
+    int volume;                          // 0 flux_tec, 1 flux_ec, 2 flux_etec,
+                                         // 3 flux_kennedy_gruber (3D only)
     int nc;                              // 0 waruszewski, 1 artiano, 2 souza
     int surface;                         // 0 FluxLMARS(c), 1 flux_ec
     int snc;                             // surface gravity term: -1 none (flux_zero), else as nc

@@ -63,7 +63,7 @@ struct PhysPT3D {
     } else {
       q[10] = q[11] = 0.0;
     }
-    q[12] = 0.0;
+    q[12] = P.volume == 3 ? 0.5 * u[4] * irho : 0.0;  // theta / 2 (flux_kennedy_gruber)
     if (!(rho > 0.0)) bad |= TAG_S_NEG_DENSITY;
     if (!(u[4] > 0.0)) bad |= TAG_S_NEG_PRESSURE;
   }
@@ -83,6 +83,10 @@ struct PhysPT3D {
       ln_mean_pair<false>(a[0], b[0], a[7], b[7], 0.0, 0.0, 0.0, 0.0, rho_ln, inv_sig);
       f1 = rho_ln * vn;
       f5 = f1 * inv_sig;
+    } else if (P.volume == 3) {
+      // flux_kennedy_gruber (:333-359): arithmetic means of rho, v, p and theta
+      f1 = 0.5 * (a[0] + b[0]) * vn;
+      f5 = f1 * (a[12] + b[12]);
     } else {
       f5 = PhysPT2D::stolarsky(P, a[6], b[6], a[8], a[9], b[8], b[9]) * vn;
       if (P.volume == 0) {
@@ -93,7 +97,7 @@ struct PhysPT3D {
       }
     }
     double ravg;
-    if (P.nc == 0) ravg = (P.volume == 2) ? ln_mean_single(a[0], b[0]) : rho_ln;
+    if (P.nc == 0) ravg = (P.volume >= 2) ? ln_mean_single(a[0], b[0]) : rho_ln;
     else if (P.nc == 1) ravg = PhysPT2D::stolarsky(P, a[0], b[0], a[10], a[11], b[10], b[11]);
     else ravg = 0.5 * (a[0] + b[0]);
     const double h = ravg * (b[5] - a[5]);  // (phi_b - phi_a) / 2 rho_avg (stored halved)

@@ -817,7 +817,8 @@ const char* check_equations(const tag_config* cfg) {
     case TAG_EQ_POTENTIAL_TEMPERATURE_3D: {
       const bool ec_surface =
           sf == TAG_SF_PT_EC && cfg->equations == TAG_EQ_POTENTIAL_TEMPERATURE_2D;
-      if ((vf != TAG_VF_PT_TEC && vf != TAG_VF_PT_EC && vf != TAG_VF_PT_ETEC) ||
+      const bool kg = vf == TAG_VF_PT_KG && cfg->equations == TAG_EQ_POTENTIAL_TEMPERATURE_3D;
+      if ((vf != TAG_VF_PT_TEC && vf != TAG_VF_PT_EC && vf != TAG_VF_PT_ETEC && !kg) ||
           (sf != TAG_SF_LMARS && !ec_surface))
         return "unsupported flux combination for the potential-temperature equations";
       const double k = cfg->params[4];
@@ -1107,7 +1108,10 @@ int tag_create(const tag_config* cfg, tag_handle* out) {
     h->na = PhysPT3D::NA;
     double pp[8];
     for (int k = 0; k < 8; ++k) pp[k] = cfg->params[k];
-    pp[5] = cfg->volume_flux == TAG_VF_PT_TEC ? 0 : cfg->volume_flux == TAG_VF_PT_EC ? 1 : 2;
+    pp[5] = cfg->volume_flux == TAG_VF_PT_TEC  ? 0
+            : cfg->volume_flux == TAG_VF_PT_EC ? 1
+            : cfg->volume_flux == TAG_VF_PT_KG ? 3
+                                               : 2;
     h->p_pt3d = PhysPT3D::make_params(pp);
     h->ops = ops3d_for_n<PhysPT3D>(n);
   } else if (dim == 3) {

@@ -249,6 +249,15 @@ flux_nonconservative_es = _NamedFlux("flux_nonconservative_es")
 flux_etec = _NamedFlux("flux_etec")
 flux_nonconservative_artiano_etal = _NamedFlux("flux_nonconservative_artiano_etal")
 flux_nonconservative_souza_etal = _NamedFlux("flux_nonconservative_souza_etal")
+# CompressibleEulerPotentialTemperatureEquationsWithGravity3D
+# (src/equations/compressible_euler_potential_temperature_gravity_3d.jl):
+# flux_kennedy_gruber (:333-359); the fused flux_kennedy_gruber_souza_etal
+# (:377-414), which equals (flux_kennedy_gruber, flux_nonconservative_souza_etal);
+# the fused surface flux flux_lmars_combined (:258-293), which equals
+# (FluxLMARS(340), flux_zero), and its slip wall (:299-320), the one of the tuple
+flux_kennedy_gruber = _NamedFlux("flux_kennedy_gruber")
+flux_kennedy_gruber_souza_etal = _NamedFlux("flux_kennedy_gruber_souza_etal")
+flux_lmars_combined = _NamedFlux("flux_lmars_combined")
 
 
 class FluxLMARS:

@@ -152,12 +152,21 @@ def _flux_ids(equations, solver, source_terms=None):
         return _lib.TAG_VF_IE_ETEC, _lib.TAG_SF_IE_ES, [equations.c_p, equations.c_v, equations.g]
     if isinstance(equations, (CompressibleEulerPotentialTemperatureEquationsWithGravity2D,
                               CompressibleEulerPotentialTemperatureEquationsWithGravity3D)):
-        from .equations import flux_ec
+        from .equations import (flux_ec, flux_kennedy_gruber, flux_kennedy_gruber_souza_etal,
+                                flux_lmars_combined)
+        if equations.ndims == 3:
+            # the fused forms of the reference (3D only) are its tuples in one call
+            if vf is flux_kennedy_gruber_souza_etal:
+                vf = (flux_kennedy_gruber, flux_nonconservative_souza_etal)
+            if sf is flux_lmars_combined:
+                sf = (FluxLMARS(340.0), flux_zero)
         if not isinstance(vf, tuple):
             raise ValueError("volume flux must be (flux_tec | flux_ec | flux_etec, a "
                              "nonconservative gravity term)")
         vid = {id(flux_tec): _lib.TAG_VF_PT_TEC, id(flux_ec): _lib.TAG_VF_PT_EC,
                id(flux_etec): _lib.TAG_VF_PT_ETEC}.get(id(vf[0]))
+        if vf[0] is flux_kennedy_gruber and equations.ndims == 3:
+            vid = _lib.TAG_VF_PT_KG
         nc = {id(flux_nonconservative_waruszewski_etal): 0,
               id(flux_nonconservative_artiano_etal): 1,
               id(flux_nonconservative_souza_etal): 2}.get(id(vf[1]))
