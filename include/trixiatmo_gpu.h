@@ -162,7 +162,7 @@ typedef struct {
 /* Creates a handle on the current CUDA device.  Replaces the cache build of
  * Trixi.SemidiscretizationHyperbolic (reference: src/semidiscretization/
  * semidiscretization_hyperbolic_2d_manifold_in_3d.jl:78-111, create_cache in
- * src/solvers/solvers.jl:7-33): geometry and connectivity are uploaded once. */
+ * src/solvers/dgsem_p4est/dg.jl:5-32): geometry and connectivity are uploaded once. */
 int tag_create(const tag_config* cfg, tag_handle* out);
 
 /* One handle for many independent members (COVARIANT_SWE), each its own mesh,
@@ -516,8 +516,8 @@ int tag_set_state_sink(tag_handle h, double* u_host);
  * one member of an ensemble (0 .. nmembers-1; -1 = every element of the
  * handle).  *nvars and *nnodes receive the sizes; data may be null to query
  * them.  Replaces convert_variables (src/callbacks_step/
- * save_solution_covariant.jl:5-33 with cons2prim_and_vorticity :64-78 and
- * calc_vorticity_node :94-121; cons2prim / contravariant2global of
+ * save_solution_covariant.jl:5-33 with cons2prim_and_vorticity :64-74 and
+ * calc_vorticity_node :93-118; cons2prim / contravariant2global of
  * src/equations/covariant_shallow_water.jl:113-145); cons2cons is the
  * transposed state (save_solution_2d_manifold_in_3d_cartesian.jl:66-68). */
 int tag_solution_variables(tag_handle h, int32_t solution_variables, int32_t member,

@@ -5,7 +5,7 @@
 //   five-stage fourth-order 2N-storage scheme "RK4(3)5[2N] solution 3" of
 //   M. H. Carpenter, C. A. Kennedy, NASA TM-109112 (1994). Per stage s:
 //     du = f(u, t + c_s dt);  k = A_s k + dt du;  u = u + B_s k.
-//   Used by e.g. examples/euler/moist_air/buoyancy/elixir_gemein_bubble.jl:121.
+//   Used by e.g. examples/euler/moist_air/buoyancy/elixir_gemein_bubble.jl:100-102.
 // * SSPRK43 (OrdinaryDiffEqSSPRK, external): the four-stage third-order SSP
 //   scheme with SSP coefficient 2 (J. F. B. M. Kraaijevanger, BIT 31 (1991);
 //   R. J. Spiteri, S. J. Ruuth, SINUM 40 (2002)), run with adaptive = false

@@ -7,9 +7,9 @@ before writing a solution file, for the covariant shallow-water equations:
 * cons2prim  (H, vcon1, vcon2), H = h + b     :88-90, :113-118
 * contravariant2global (h, h_v1, h_v2, h_v3) = (h, A (h_vcon1, h_vcon2))   :97-100, :140-145
 * cons2prim_and_vorticity (H, v1, v2, v3, b, zeta)
-      src/callbacks_step/save_solution_covariant.jl:64-78, with the relative
+      src/callbacks_step/save_solution_covariant.jl:64-74, with the relative
       vorticity zeta = (d v_2/d xi^1 - d v_1/d xi^2) / J of
-      calc_vorticity_node :94-121, v_k = G_kl v^l the covariant velocity,
+      calc_vorticity_node :93-118, v_k = G_kl v^l the covariant velocity,
       derivatives by the nodal derivative matrix along the node's grid lines.
 
 The auxiliary slots follow src/equations/equations.jl:210-244 (0-based: 0-5

@@ -4,7 +4,7 @@ members, cons2cons of a Cartesian system, and save_solution_file written by
 the library's HDF5 encoder and read back by the strict checker
 (tests/h5_reader.py) — the file of the reference's SaveSolutionCallback
 (src/callbacks_step/save_solution_2d_manifold_in_3d_cartesian.jl:44-118,
-src/callbacks_step/save_solution_covariant.jl:5-128)."""
+src/callbacks_step/save_solution_covariant.jl:5-125)."""
 import numpy as np
 import pytest
 

@@ -6,10 +6,10 @@ test/test_2d_moist_euler.jl:
     FluxLMARS(360), source_terms_geopotential, pressure-Riemann slip walls,
     P4estMesh of 2x2 trees refined 5 times (64x64 affine elements over
     [0, 20 km] x [-5 km, 15 km]), polydeg 4, CK2N54 at CFL 0.2 to t = 0.1;
-  * "elixir_gemein_source_terms moist" (:152-177): examples/euler/moist_air/tests/
+  * "elixir_gemein_source_terms moist" (:113-138): examples/euler/moist_air/tests/
     elixir_gemein_source_terms.jl with polydeg 3 and 10x8 cells, flux_chandrashekar
     as volume and surface flux, the moist convergence source (phase change);
-  * "elixir_gemein_source_terms dry" (:126-150): examples/euler/dry_air/tests/
+  * "elixir_gemein_source_terms dry" (:86-111): examples/euler/dry_air/tests/
     elixir_gemein_source_terms.jl, weak form, flux_lax_friedrichs, gravity 0;
   * "elixir_gemein_nonhydrostatic_gravity_waves" (:59-84):
     examples/euler/dry_air/buoyancy/elixir_gemein_nonhydrostatic_gravity_waves.jl

@@ -4,8 +4,8 @@
 // the file (row v = variable v over the nodes of the selected range).
 //
 // Reference: src/callbacks_step/save_solution_covariant.jl (convert_variables
-// :5-33, cons2prim_and_vorticity :64-78, calc_vorticity_node :94-121,
-// varnames :125-128); src/equations/covariant_shallow_water.jl (varnames
+// :5-33, cons2prim_and_vorticity :64-74, calc_vorticity_node :93-118,
+// varnames :122-125); src/equations/covariant_shallow_water.jl (varnames
 // :83-100, cons2prim :113-118, contravariant2global :140-145);
 // src/equations/equations.jl (aux-variable slots :210-244).
 #pragma once

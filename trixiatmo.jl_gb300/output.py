@@ -66,7 +66,7 @@ _CONS2CONS = {
 }
 
 # covariant shallow water: src/equations/covariant_shallow_water.jl:83-100 and
-# src/callbacks_step/save_solution_covariant.jl:125-128
+# src/callbacks_step/save_solution_covariant.jl:122-125
 _COVARIANT = {
     "cons2cons": ("h", "h_vcon1", "h_vcon2"),
     "cons2prim": ("H", "vcon1", "vcon2"),
