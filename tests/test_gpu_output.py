@@ -154,3 +154,23 @@ def test_ensemble_files_one_per_member(tg, gpu_lib, out, tmp_path):
         for v in range(5):
             assert np.array_equal(f.datasets[f"variables_{v + 1}"].data, um[:, v])
     ens.close()
+
+
+def test_save_solution_file_3d_shell(tg, gpu_lib, out, tmp_path):
+    """The 3D shell (a P4estMesh{3} in the reference): ndims 3, the
+    conservative variables with their names, bit for bit the state."""
+    from test_gpu_euler3d import make_semi as make_shell
+    eq, mesh, semi = make_shell(tg, 2, 2, 4)
+    u = semi.compute_coefficients()
+    semi.set_state(u)
+    fname = out.save_solution_file(semi, 0.5, 0.25, 7, str(tmp_path))
+    f = H5File(fname)
+    assert f.attrs["ndims"] == 3 and f.attrs["mesh_type"] == "P4estMesh"
+    assert f.attrs["polydeg"] == 4 and f.attrs["n_elements"] == semi.nelements
+    assert f.attrs["n_vars"] == 6 and f.attrs["timestep"] == 7 and f.attrs["time"] == 0.5
+    names = ("rho", "rho_v1", "rho_v2", "rho_v3", "rho_e", "phi")
+    for v, name in enumerate(names):
+        d = f.datasets[f"variables_{v + 1}"]
+        assert d.attrs == {"name": name}
+        assert d.data.tobytes() == np.ascontiguousarray(u.reshape(-1, 6)[:, v]).tobytes()
+    semi.close()
