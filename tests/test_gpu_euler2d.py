@@ -256,3 +256,37 @@ def test_ensemble_members_match_independent_oracle_runs(tg, orc, gpu_lib):
     # members really have different time steps
     assert len(set(np.round(t, 12))) == 3
     ens.close()
+
+
+def test_state_sink_2d_ensemble_and_refusals(tg, gpu_lib):
+    """A 2D ensemble's state sink: after rk_steps it holds every member's new
+    state, bit for bit what get_state copies; the rainy equations (their stage
+    limiter changes the state after the last stage) refuse a sink."""
+    torch = pytest.importorskip("torch")
+    eq = tg.CompressibleEulerEnergyEquationsWithGravity2D(c_p=1004, c_v=717, gravity=9.81)
+    solver = tg.DGSEM(3, (tg.FluxLMARS(340.0), tg.flux_zero),
+                      tg.VolumeIntegralFluxDifferencing(
+                          (tg.flux_ranocha, tg.flux_nonconservative_waruszewski_etal)))
+    meshes = [tg.StructuredMesh((nx, 4), (0.0, 0.0), (LX, LZ), periodicity=(True, False))
+              for nx in (6, 8, 4)]
+    bcs = {"y_neg": tg.boundary_condition_slip_wall, "y_pos": tg.boundary_condition_slip_wall}
+    ens = tg.SemidiscretizationEnsemble(meshes, eq, [tg.WarmBubble()] * 3, solver,
+                                        boundary_conditions=bcs)
+    u = ens.compute_coefficients()
+    ens.set_state(u)
+    ens.rk_steps(2, cfl=1.0, t=np.zeros(3))
+    ref = ens.get_state()
+    sink = torch.empty(u.shape, dtype=torch.float64, pin_memory=True).numpy()
+    sink[...] = np.nan
+    ens.set_state_sink(sink)
+    ens.set_state(u)
+    ens.rk_steps(2, cfl=1.0, t=np.zeros(3))
+    assert np.array_equal(sink, ref) and np.array_equal(sink, ens.get_state())
+    ens.set_state_sink(None)
+    ens.close()
+    from test_gpu_rainy import make_rainy
+    _, rainy = make_rainy(tg, 4, 2, 3)
+    with pytest.raises(tg._lib.TagError, match="stage limiter"):
+        rainy.set_state_sink(torch.empty(rainy.shape, dtype=torch.float64,
+                                         pin_memory=True).numpy())
+    rainy.close()

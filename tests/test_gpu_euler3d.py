@@ -171,7 +171,7 @@ def test_state_sink_holds_each_steps_result(tg, gpu_lib):
     new state into the pinned buffer from inside its kernel: after rk_steps it
     equals get_state bit for bit, for one step and for several; the steps
     themselves are unchanged; a cleared sink is no longer written; a pageable
-    array or a 2D handle is refused."""
+    array is refused."""
     torch = pytest.importorskip("torch")
     eq, mesh, semi = make_semi(tg, 2, 2, 4)
     u = perturb3d(semi.compute_coefficients(), eq, seed=5)
@@ -195,8 +195,3 @@ def test_state_sink_holds_each_steps_result(tg, gpu_lib):
     with pytest.raises(tg._lib.TagError, match="pinned"):
         semi.set_state_sink(np.zeros_like(u))
     semi.close()
-    from test_gpu_euler2d import make_semi as make_2d
-    _, semi2 = make_2d(tg, 4, 2)
-    with pytest.raises(tg._lib.TagError, match="3D handle"):
-        semi2.set_state_sink(torch.empty(semi2.shape, dtype=torch.float64, pin_memory=True).numpy())
-    semi2.close()

@@ -382,6 +382,17 @@ __global__ void k_element(typename Phys::Params Pp, const BasisDev basis, double
   // --- phase 4 (last stage of a step): CFL speeds of the updated state
   if (MODE == kModeStage && st.max_speed != nullptr) {
     __syncthreads();
+    // the step's result to the registered sink (host memory over the host
+    // link): each element's new state is one contiguous block in shared
+    // memory and in the sink, stored by consecutive threads at consecutive
+    // addresses
+    if (st.sink != nullptr) {
+      double* o = st.sink + (size_t)e_first * nn * NV;
+      for (int t = threadIdx.x; t < ne * nn * NV; t += nthr) {
+        const int el = t / (nn * NV), r = t % (nn * NV);
+        o[t] = base[el * S::per_elem + S::oU + r];
+      }
+    }
     for (int t = threadIdx.x; t < ne * nn; t += nthr) {
       const int el = t / nn, node = t % nn;
       double* eb = base + el * S::per_elem;

@@ -233,6 +233,7 @@ struct OpsImpl {
       st.t_member = h->d_mscal;
       st.dt = h->d_mscal + h->nmembers;
       st.max_speed = last ? h->d_mscal + 2 * h->nmembers : nullptr;
+      st.sink = last && h->capturing_steps ? h->sink : nullptr;
       k_element<Phys, n, kModeStage, VOL><<<blocks, threads, smem, h->stream>>>(
           params_of<Phys>(h), h->basis, u, du, h->d_k, h->d_Ja, h->d_invJ, h->d_sfv, h->nelem,
           epb, st, h->d_status);
@@ -1342,7 +1343,10 @@ int tag_solution_variables(tag_handle h, int32_t solution_variables, int32_t mem
 
 int tag_set_state_sink(tag_handle h, double* u_host) {
   if (!h) return fail(TAG_E_INVALID, "null handle");
-  if (h->dim != 3) return fail(TAG_E_INVALID, "a state sink needs a 3D handle");
+  if (h->eq == TAG_EQ_COVARIANT_SWE || h->has_limiter)
+    return fail(TAG_E_INVALID,
+                "a state sink needs a Cartesian handle without a stage limiter (the covariant "
+                "kernels and the rainy limiter do not store one)");
   if (!u_host) {
     h->sink = nullptr;
     return TAG_OK;
