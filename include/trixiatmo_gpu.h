@@ -497,9 +497,9 @@ int tag_rhs_noalloc(const tag_config* cfg, const double* u, double* du, void* st
  * must be pinned host memory mapped for the device (cudaHostAlloc /
  * cudaHostRegister under unified addressing) of tag_ndofs_total doubles; the
  * caller keeps it alive while registered.  tag_rk_adaptive, tag_rhs and the
- * other entry points do not write it.  TAG_E_INVALID for the covariant
- * equations, for a handle with the rainy stage limiter (which changes the
- * state after the last stage), or for an unmapped pointer.  No counterpart in
+ * other entry points do not write it.  TAG_E_INVALID for a handle with the
+ * rainy stage limiter (which changes the state after the last stage) or for
+ * an unmapped pointer.  No counterpart in
  * the reference (Julia keeps u_ode on the host); the end-to-end path of a
  * step that returns its state. */
 int tag_set_state_sink(tag_handle h, double* u_host);

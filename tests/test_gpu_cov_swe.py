@@ -155,3 +155,31 @@ def test_uneven_ensemble_matches_members_alone(tg, gpu_lib):
         assert np.array_equal(alone.get_state(), ens.member_state(ue, m)), m
         alone.close()
     ens.close()
+
+
+def test_state_sink_uneven_ensemble(tg, gpu_lib):
+    """The state sink of an uneven covariant ensemble: after rk_steps it holds
+    every member's new state, bit for bit what get_state copies."""
+    torch = pytest.importorskip("torch")
+    cv = tg.covariant
+    from trixiatmo_gb300.initial_conditions import EARTH_RADIUS
+    eq = cv.SplitCovariantShallowWaterEquations2D(G_, OM_)
+    specs = [(3, 3), (2, 5), (4, 4)]
+    meshes = [cv.P4estMeshCubedSphere2D(k, EARTH_RADIUS, polydeg=N) for k, N in specs]
+    solvers = [tg.DGSEM(N, cv.flux_ec, tg.VolumeIntegralFluxDifferencing(cv.flux_ec))
+               for _, N in specs]
+    ics = [cv.transform_initial_condition(cv.initial_condition_geostrophic_balance, eq)] * 3
+    ens = tg.SemidiscretizationCovariantEnsemble(meshes, eq, ics, solvers,
+                                                 source_terms=cv.source_terms_geometric_coriolis)
+    u = ens.compute_coefficients()
+    ens.set_state(u)
+    ens.rk_steps(2, cfl=0.4, t=np.zeros(3))
+    ref = ens.get_state()
+    sink = torch.empty(u.shape, dtype=torch.float64, pin_memory=True).numpy()
+    sink[...] = np.nan
+    ens.set_state_sink(sink)
+    ens.set_state(u)
+    ens.rk_steps(2, cfl=0.4, t=np.zeros(3))
+    assert np.array_equal(sink, ref) and np.array_equal(sink, ens.get_state())
+    ens.set_state_sink(None)
+    ens.close()

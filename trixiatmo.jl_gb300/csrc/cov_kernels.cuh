@@ -503,6 +503,23 @@ TAG_DEV void cov_element_body(const CovParams& P, const CovGroup& G, int lblk,
     }
   }
   if (MODE == kModeStage && st.max_speed != nullptr) {
+    // the step's result to the registered sink (host memory over the host
+    // link).  A warp's nodes are consecutive, so its 32 nodes x 3 values are
+    // 96 consecutive doubles: lane l stores doubles l, l + 32 and l + 64,
+    // fetched from their nodes' lanes, so that every store is contiguous
+    if (st.sink != nullptr) {
+      const int lane = threadIdx.x & 31, w_first = threadIdx.x & ~31;
+      const long q0 = G.node0 + (long)el_first * nn + w_first;
+      const int valid = ne * nn - w_first;  // the warp's nodes in range (may be <= 0)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int d = lane + 32 * k, src = d / 3, c = d % 3;
+        const double s0 = __shfl_sync(0xffffffffu, un[0], src);
+        const double s1 = __shfl_sync(0xffffffffu, un[1], src);
+        const double s2 = __shfl_sync(0xffffffffu, un[2], src);
+        if (src < valid) st.sink[q0 * 3 + d] = c == 0 ? s0 : (c == 1 ? s1 : s2);
+      }
+    }
     // CFL speeds of the updated state, scaled by n: dt = cfl 2 / (n max_e(l1 + l2))
     __syncthreads();
     if (act) {

@@ -553,6 +553,7 @@ int cov_element(tag_handle h, int mode, double* u, double* du, int stage, bool l
     st.t_member = h->d_mscal;
     st.dt = h->d_mscal + h->nmembers;
     st.max_speed = last ? h->d_mscal + 2 * h->nmembers : nullptr;
+    st.sink = last && h->capturing_steps ? h->sink : nullptr;
     auto kern = h->p_cov.volume == 0 ? k_cov_element<kModeStage, 0> : k_cov_element<kModeStage, 1>;
     kern<<<h->cov_blocks, h->cov_threads, h->cov_smem, h->stream>>>(
         h->p_cov, h->d_groups, h->d_bases, u, du, h->d_k, h->d_pk, h->d_sfv, st, h->d_status);
@@ -1343,10 +1344,10 @@ int tag_solution_variables(tag_handle h, int32_t solution_variables, int32_t mem
 
 int tag_set_state_sink(tag_handle h, double* u_host) {
   if (!h) return fail(TAG_E_INVALID, "null handle");
-  if (h->eq == TAG_EQ_COVARIANT_SWE || h->has_limiter)
+  if (h->has_limiter)
     return fail(TAG_E_INVALID,
-                "a state sink needs a Cartesian handle without a stage limiter (the covariant "
-                "kernels and the rainy limiter do not store one)");
+                "a state sink needs a handle without a stage limiter (the rainy limiter changes "
+                "the state after the last stage)");
   if (!u_host) {
     h->sink = nullptr;
     return TAG_OK;
