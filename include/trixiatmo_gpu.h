@@ -490,18 +490,17 @@ int tag_rhs_noalloc(const tag_config* cfg, const double* u, double* du, void* st
                     uint32_t* status);
 
 /* Registers (u_host) or clears (null) a state sink: while it is registered,
- * the last stage of every tag_rk_steps step also stores its new state into
- * u_host, from inside the element kernel, so that the copy to the host
- * overlaps the stage's work; when tag_rk_steps returns, u_host holds what
- * tag_get_state would copy (every ensemble member, Trixi's layout).  u_host
- * must be pinned host memory mapped for the device (cudaHostAlloc /
- * cudaHostRegister under unified addressing) of tag_ndofs_total doubles; the
- * caller keeps it alive while registered.  tag_rk_adaptive, tag_rhs and the
- * other entry points do not write it.  TAG_E_INVALID for a handle with the
- * rainy stage limiter (which changes the state after the last stage) or for
- * an unmapped pointer.  No counterpart in
- * the reference (Julia keeps u_ode on the host); the end-to-end path of a
- * step that returns its state. */
+ * the last kernel of every tag_rk_steps step (the element kernel's last stage,
+ * or for the rainy equations the Newton stage limiter after it) also stores
+ * the step's new state into u_host, so that the copy to the host overlaps the
+ * step's work; when tag_rk_steps returns, u_host holds what tag_get_state
+ * would copy (every ensemble member, Trixi's layout).  u_host must be pinned
+ * host memory mapped for the device (cudaHostAlloc / cudaHostRegister under
+ * unified addressing) of tag_ndofs_total doubles; the caller keeps it alive
+ * while registered.  tag_rk_adaptive, tag_rhs and the other entry points do
+ * not write it.  TAG_E_INVALID for an unmapped pointer.  No counterpart in the
+ * reference (Julia keeps u_ode on the host); the end-to-end path of a step
+ * that returns its state. */
 int tag_set_state_sink(tag_handle h, double* u_host);
 
 /* ---- solution output (SaveSolutionCallback) ---------------------------- */

@@ -258,10 +258,10 @@ def test_ensemble_members_match_independent_oracle_runs(tg, orc, gpu_lib):
     ens.close()
 
 
-def test_state_sink_2d_ensemble_and_refusals(tg, gpu_lib):
+def test_state_sink_2d_ensemble_and_rainy(tg, gpu_lib):
     """A 2D ensemble's state sink: after rk_steps it holds every member's new
-    state, bit for bit what get_state copies; the rainy equations (their stage
-    limiter changes the state after the last stage) refuse a sink."""
+    state, bit for bit what get_state copies; for the rainy equations the
+    stage limiter after the last stage stores the limited state."""
     torch = pytest.importorskip("torch")
     eq = tg.CompressibleEulerEnergyEquationsWithGravity2D(c_p=1004, c_v=717, gravity=9.81)
     solver = tg.DGSEM(3, (tg.FluxLMARS(340.0), tg.flux_zero),
@@ -285,8 +285,15 @@ def test_state_sink_2d_ensemble_and_refusals(tg, gpu_lib):
     ens.set_state_sink(None)
     ens.close()
     from test_gpu_rainy import make_rainy
-    _, rainy = make_rainy(tg, 4, 2, 3)
-    with pytest.raises(tg._lib.TagError, match="stage limiter"):
-        rainy.set_state_sink(torch.empty(rainy.shape, dtype=torch.float64,
-                                         pin_memory=True).numpy())
+    _, rainy = make_rainy(tg, 8, 4, 3)
+    u = rainy.compute_coefficients()
+    rainy.set_state(u)
+    rainy.rk_steps(2, cfl=0.5, t=0.0)
+    ref = rainy.get_state()
+    sink = torch.empty(u.shape, dtype=torch.float64, pin_memory=True).numpy()
+    sink[...] = np.nan
+    rainy.set_state_sink(sink)
+    rainy.set_state(u)
+    rainy.rk_steps(2, cfl=0.5, t=0.0)
+    assert np.array_equal(sink, ref) and np.array_equal(sink, rainy.get_state())
     rainy.close()

@@ -170,8 +170,8 @@ def test_state_sink_holds_each_steps_result(tg, gpu_lib):
     """With a state sink registered, the last stage of every step stores the
     new state into the pinned buffer from inside its kernel: after rk_steps it
     equals get_state bit for bit, for one step and for several; the steps
-    themselves are unchanged; a cleared sink is no longer written; a pageable
-    array is refused."""
+    themselves are unchanged; error-controlled stepping does not write it, nor
+    do steps after it is cleared; a pageable array is refused."""
     torch = pytest.importorskip("torch")
     eq, mesh, semi = make_semi(tg, 2, 2, 4)
     u = perturb3d(semi.compute_coefficients(), eq, seed=5)
@@ -188,8 +188,12 @@ def test_state_sink_holds_each_steps_result(tg, gpu_lib):
         semi.rk_steps(nsteps, cfl=0.8, t=0.0)
         assert np.array_equal(sink, semi.get_state())
         assert np.array_equal(sink, ref[k])
-    semi.set_state_sink(None)
+    # error-controlled stepping (whose rejected steps are discarded) leaves it alone
     sink[...] = 0.0
+    semi.set_state(u)
+    semi.solve_adaptive((0.0, 2.0), abstol=1e-6, reltol=1e-6)
+    assert not sink.any()
+    semi.set_state_sink(None)
     semi.rk_steps(1, cfl=0.8, t=0.0)
     assert not sink.any()
     with pytest.raises(tg._lib.TagError, match="pinned"):

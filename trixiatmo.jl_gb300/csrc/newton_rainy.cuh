@@ -80,6 +80,8 @@ struct NewtonArgs {
   const float* mlp;  // device parameters (kMlpParams floats) or null
   int* iters;        // per-node Newton updates, or null
   unsigned long long* counters;  // [0] updates, [1] fallbacks, [2] not converged, or null
+  double* sink;      // the limited state of every node is also stored here (mapped host
+                     // memory; the limiter after the last stage of a step), or null
 };
 
 // Residual of the saturation system at x, given svp = e_s(x[2]).
@@ -325,6 +327,29 @@ static __global__ void __launch_bounds__(256) k_newton_rainy(double* __restrict_
     if (!conv) atomicOr(status, TAG_S_NEWTON_MAXIT);
     fallbacks = (unsigned)fb;
     unconverged = conv ? 0u : 1u;
+  }
+  if (a.sink != nullptr) {
+    // the step's result to the registered sink (host memory over the host
+    // link).  A warp's nodes are consecutive, so their 32 x 9 values are 288
+    // consecutive doubles: lane l stores doubles l + 32 k (k = 0..8), each
+    // fetched from its node's lane, so that every store is contiguous
+    const long w_first = q - (threadIdx.x & 31);
+    const long valid = nodes - w_first;  // the warp's nodes in range
+    double fin[9];
+#pragma unroll
+    for (int v = 0; v < 9; ++v) fin[v] = q < nodes ? u[q * 9 + v] : 0.0;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const int d = lane + 32 * k, src = d / 9, c = d % 9;
+      double val = 0.0;
+#pragma unroll
+      for (int v = 0; v < 9; ++v) {
+        const double x = __shfl_sync(0xffffffffu, fin[v], src);
+        if (v == c) val = x;
+      }
+      if (src < valid) a.sink[w_first * 9 + d] = val;
+    }
   }
   if (a.counters) {
     // one atomic per warp and counter instead of one per node

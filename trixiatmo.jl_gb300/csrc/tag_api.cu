@@ -440,6 +440,7 @@ int stage_sequence(tag_handle h) {
       a.mlp = h->d_mlp;
       a.iters = nullptr;
       a.counters = h->d_run_counters;
+      a.sink = s == ns - 1 && h->capturing_steps ? h->sink : nullptr;  // the limited state
       TAG_CUDA(launch_newton_rainy(h->d_u, nodes, a, h->d_status, h->stream));
       if (s == ns - 1) {
         rc = h->ops->max_speed(h, h->d_u);
@@ -1344,10 +1345,6 @@ int tag_solution_variables(tag_handle h, int32_t solution_variables, int32_t mem
 
 int tag_set_state_sink(tag_handle h, double* u_host) {
   if (!h) return fail(TAG_E_INVALID, "null handle");
-  if (h->has_limiter)
-    return fail(TAG_E_INVALID,
-                "a state sink needs a handle without a stage limiter (the rainy limiter changes "
-                "the state after the last stage)");
   if (!u_host) {
     h->sink = nullptr;
     return TAG_OK;

@@ -442,11 +442,9 @@ class SemidiscretizationHyperbolic:
         _lib.check(self._L.tag_set_state(self._h, _ptr(u)))
 
     def set_state_sink(self, out):
-        """tag_set_state_sink (every handle but the rainy equations', whose
-        stage limiter follows the last stage): while registered, the last
-        stage of every rk_steps step stores the new state into `out` (pinned
-        host memory, float64, the state's shape) from inside its kernel; None
-        clears it."""
+        """tag_set_state_sink: while registered, the last kernel of every
+        rk_steps step stores the step's new state into `out` (pinned host
+        memory, float64, the state's shape); None clears it."""
         if out is None:
             _lib.check(self._L.tag_set_state_sink(self._h, None))
             self._sink = None
